@@ -1,0 +1,364 @@
+"""Benchmark: one-site TDVP sweeps/sec on the T-tree at chi=256 (GB300 engine).
+
+Workload (seeded, synthetic): root + 3 arms of 20 sites (61 sites, d=2),
+Heisenberg couplings + random fields h_i ~ U[-1, 1] (TTNO bond 5), Gaussian
+complex TTNS at chi=256 on every bond, canonicalised and normalised; first-order
+one-site TDVP, dt=0.01, Krylov exponential with krylov_tol=1e-10. One step =
+one sweep (run_one_time_step). Inputs are larger than L2 (the root tensor alone
+is 537 MB in complex128), so no L2 flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--chi 256] [--arm 20]
+
+Multi-GPU: replicas only (a sweep is sequential); each rank advances its own
+realisation and ``value`` is the sum of sweeps over ranks / max time.
+The reference arm (--impl reference) times the NumPy oracle (the reference's
+algorithm restated; PyTreeNet itself is a Python package that cannot run at
+chi=256 -- its contraction order needs a 67 GB intermediate) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "TDVP sweeps/sec at chi=256 (one-site, 61-site T-tree, Heisenberg+fields)"
+FP64_NOMINAL_TFLOPS = 1.25
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--chi", type=int, default=256)
+    ap.add_argument("--arm", type=int, default=20)
+    ap.add_argument("--dt", type=float, default=0.01)
+    ap.add_argument("--tol", type=float, default=1e-10)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def config(args, precision):
+    return {"workload": f"T-tree root+3x{args.arm} ({3 * args.arm + 1} sites), chi={args.chi}, d=2, "
+                        f"TTNO bond 5, Heisenberg+fields, first-order 1TDVP, dt={args.dt}, "
+                        f"krylov_tol={args.tol}",
+            "precision": precision, "l2": "inputs larger than L2 (root tensor > 129 MB); no flush",
+            "parallelism": "replicas"}
+
+
+# ----------------------------------------------------------------------------
+# CPU baseline: the NumPy oracle on a bounded sample, extrapolated to a sweep
+# ----------------------------------------------------------------------------
+def oracle_schedule_counts(arm, tol, dt):
+    """Operation counts of one sweep, from a dry run of the oracle driver at chi=8
+    (the schedule and Krylov depths do not depend on chi in any material way)."""
+    import oracle as O
+    import oracle.ptn_oracle as OP
+    from pytreenet_gb300.workloads import t_tree_state, t_tree_heisenberg, t_tree_spec
+    st, spec, tensors = t_tree_state(arm_len=arm, chi=8, seed=0)
+    H, W = t_tree_heisenberg(st, seed=1)
+    tree = O.OTree()
+    for nid, p in spec:
+        tree.add_root(nid) if p is None else tree.add_child(nid, p)
+    counts = {}
+    deg = {nid: len(tree.neighbours(nid)) for nid, _ in spec}
+
+    def wrap(name, fn, key):
+        def w(*a, **k):
+            nid = key(*a)
+            counts[(name, deg[nid])] = counts.get((name, deg[nid]), 0) + 1
+            return fn(*a, **k)
+        return w
+    saved = (OP.heff_apply, OP.env_update, OP.qr_keep_split)
+    OP.heff_apply = wrap("heff", OP.heff_apply, lambda x, tree, nid, *r: nid)
+    OP.env_update = wrap("env", OP.env_update, lambda tree, nid, *r: nid)
+    OP.qr_keep_split = wrap("qr", OP.qr_keep_split, lambda state, nid, *r: nid)
+    try:
+        algo = O.FirstOrderOneSiteTDVPOracle(O.OState(tree, tensors), W, dt, krylov_tol=tol)
+        c0 = algo.state.orth_center
+        algo.state.tensors[c0] = algo.state.tensors[c0] / np.linalg.norm(algo.state.tensors[c0])
+        counts.clear()
+        algo.run_one_time_step()
+    finally:
+        OP.heff_apply, OP.env_update, OP.qr_keep_split = saved
+    return counts
+
+
+def oracle_op_times(chi, reps=1):
+    """Seconds per oracle operation at this chi, by node degree (bounded sample)."""
+    import oracle as O
+    rng = np.random.default_rng(0)
+    w, d = 5, 2
+
+    def c(*s):
+        return (rng.standard_normal(s) + 1j * rng.standard_normal(s)) / np.sqrt(2)
+    times = {}
+    for degn in (1, 2, 3):
+        tree = O.OTree()
+        tree.add_root("v")
+        for i in range(degn):
+            tree.add_child(f"u{i}", "v")
+        shape = [chi] * degn + [d]
+        x = c(*shape)
+        W = c(*([w] * degn + [d, d]))
+        envs = {(f"u{i}", "v"): c(chi, w, chi) for i in range(degn)}
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            O.heff_apply(x, tree, "v", W, envs)
+        times[("heff", degn)] = (time.perf_counter() - t0) / reps
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            O.env_update(tree, "v", "u0", x, W, envs)
+        times[("env", degn)] = (time.perf_counter() - t0) / reps
+        mat = x.reshape(-1, chi)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            np.linalg.qr(mat)
+        times[("qr", degn)] = (time.perf_counter() - t0) / reps
+    return times
+
+
+def cpu_sweeps_per_s(args):
+    t0 = time.perf_counter()
+    counts = oracle_schedule_counts(args.arm, args.tol, args.dt)
+    times = oracle_op_times(args.chi)
+    sweep = sum(n * times.get(k, 0.0) for k, n in counts.items())
+    wall = time.perf_counter() - t0
+    return 1.0 / sweep, {"counts": {f"{a}/deg{b}": n for (a, b), n in sorted(counts.items())},
+                         "sample_seconds": round(wall, 2)}
+
+
+def cpu_baseline_obj(args):
+    v, info = cpu_sweeps_per_s(args)
+    return {"value": v, "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": (f"NumPy oracle (OpenBLAS, all host threads): one heff matvec, env update and QR per "
+                       f"node degree at chi={args.chi}, weighted by the operation counts of one oracle sweep "
+                       f"(from a chi=8 dry run); {info['sample_seconds']} s of CPU work"),
+            "detail": info}
+
+
+# ----------------------------------------------------------------------------
+# clocks
+# ----------------------------------------------------------------------------
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        rows = [l.split(",") for l in open(self.path).read().strip().splitlines() if l.strip()]
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4)
+                          if len(r) > 5 + i and r[5 + i].strip().lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ----------------------------------------------------------------------------
+# GPU arm
+# ----------------------------------------------------------------------------
+def run_gb300(args, rank, world):
+    import torch
+    import pytreenet_gb300 as P
+    from pytreenet_gb300 import _lib
+    from pytreenet_gb300.workloads import t_tree_state, t_tree_heisenberg
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+    lib = _lib.load()
+    st, spec, _ = t_tree_state(arm_len=args.arm, chi=args.chi, seed=rank)
+    H, _ = t_tree_heisenberg(st, seed=1000 + rank)
+    total = args.warmup + 2 * args.steps + 1
+    algo = P.FirstOrderOneSiteTDVP(st, H, args.dt, args.dt * total, {},
+                                   config=P.TDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV),
+                                   solver_options={"krylov_tol": args.tol})
+    net = algo.net
+    net.normalise_center()
+    for _ in range(args.warmup):
+        algo.run_one_time_step()
+    torch.cuda.synchronize()
+
+    # -- timed region: K sweeps, device-resident ---------------------------------
+    heff_events = []
+    orig = net.evolve_site
+
+    def timed_evolve(nid, *a, **k):
+        p = net.heff_plan(nid)
+        run = p.run
+
+        def run_timed(xp=0, yp=0):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            run(xp, yp)
+            e1.record()
+            heff_events.append((e0, e1, p.flops))
+        p.run = run_timed
+        try:
+            return orig(nid, *a, **k)
+        finally:
+            p.run = run
+    net.evolve_site = timed_evolve
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    l0 = lib.ptn_launch_counter()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(torch.cuda.current_device()) as clk:
+        start.record()
+        for _ in range(args.steps):
+            algo.run_one_time_step()
+        stop.record()
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    launches = int(lib.ptn_launch_counter() - l0)
+    net.evolve_site = orig
+    ms = start.elapsed_time(stop)
+    heff_ms = sum(a.elapsed_time(b) for a, b, _ in heff_events)
+    heff_flops = sum(f for _, _, f in heff_events)
+    n_heff = len(heff_events)
+    t_max = ms
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = world * args.steps / (t_max / 1000.0)
+
+    # -- end to end: state uploaded from pinned host memory, sweep, state read back
+    e2e = None
+    if not args.no_e2e:
+        pinned = {nid: torch.empty(net.t[nid].shape, dtype=net.t[nid].dtype, pin_memory=True)
+                  for nid in net.t}
+        for nid, t in net.t.items():
+            pinned[nid].copy_(t)
+        nbytes = sum(t.numel() * t.element_size() for t in net.t.values())
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        w0 = time.perf_counter()
+        for _ in range(args.steps):
+            for nid, t in net.t.items():
+                t.copy_(pinned[nid], non_blocking=True)
+            algo.run_one_time_step()
+            for nid, t in net.t.items():
+                pinned[nid].copy_(t, non_blocking=True)
+            torch.cuda.synchronize()
+        w1 = time.perf_counter()
+        e2e_s = w1 - w0
+        if dist:
+            t = torch.tensor([e2e_s], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        e2e = {"value": world * args.steps / e2e_s, "unit": "sweeps/s",
+               "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes}
+
+    achieved = heff_flops / (heff_ms / 1000.0) / 1e12 if heff_ms > 0 else None
+    roof = {"bound": "tensor", "kernel": "ptn_zcontract (heff matvec chain, FP64)",
+            "achieved": achieved, "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+            "frac": (achieved / FP64_NOMINAL_TFLOPS) if achieved else None,
+            "peak_source": "nominal GB300 FP64 (1.25 TFLOP/s); FP64 is not in MEASURED_PEAKS.json",
+            "traffic": None,
+            "algorithmic_flops_per_matvec": heff_flops / max(n_heff, 1),
+            "matvecs_timed": n_heff, "matvec_ms_total": heff_ms, "share_of_step": heff_ms / ms}
+    line = {"metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128 (fp64)", "data": "synthetic",
+            "config": config(args, "plain complex128"), "roofline": roof, "e2e": e2e,
+            "gpu_launches": launches, "clocks": clk.summary(),
+            "krylov_depth_mean": float(np.mean(net.krylov.depths[-n_heff:])) if n_heff else None}
+    return line
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    samples = []
+    for i in range(args.warmup + args.steps):
+        v, info = cpu_sweeps_per_s(args)
+        if i >= args.warmup:
+            samples.append(1.0 / v)
+    v = 1.0 / float(np.mean(samples))
+    cb = {"value": v, "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
+          "sample": (f"NumPy oracle restatement of the reference algorithm; each step times one heff "
+                     f"matvec, env update and QR per node degree at chi={args.chi} and weights them by "
+                     f"one sweep's operation counts")}
+    return {"metric": METRIC, "value": v, "unit": "sweeps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128 (fp64)", "data": "synthetic",
+            "config": config(args, "plain complex128 (CPU)"), "impl": "reference", "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        return
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    line = run_gb300(args, rank, world)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline_obj(args)
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,117 @@
+/*
+ * ptn_gb300.h -- C ABI of the GB300 engine for PyTreeNet's TDVP local-update path.
+ *
+ * Every entry point takes caller-owned device pointers and a cudaStream_t (passed
+ * as void*), allocates nothing, launches asynchronously on that stream, and
+ * returns an int status (PTN_OK = 0). Complex numbers are interleaved
+ * (re, im) pairs: complex128 = two doubles. All sizes and strides are in
+ * elements of the operand's complex type.
+ *
+ * The reference (PyTreeNet) is pure Python/NumPy and has no FFI of its own; each
+ * entry point below names the reference function whose NumPy call chain it
+ * replaces. The Python layer (pytreenet_gb300) binds these with ctypes.
+ */
+#ifndef PTN_GB300_H
+#define PTN_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  PTN_OK = 0,
+  PTN_ERR_ARG = 1,          /* bad shape / stride / null pointer          */
+  PTN_ERR_LAUNCH = 2,       /* CUDA launch or runtime error               */
+  PTN_ERR_NONFINITE = 3,    /* NaN or Inf found in an input               */
+  PTN_ERR_BREAKDOWN = 4,    /* Krylov breakdown that cannot be continued  */
+  PTN_ERR_NOCONVERGE = 5,   /* iterative decomposition did not converge   */
+  PTN_ERR_UNSUPPORTED = 6   /* configuration outside the kernel's limits  */
+};
+
+#define PTN_MAX_MODES 6
+
+/* A group of tensor modes that a contraction treats as one GEMM index.
+ * n modes, row-major (mode 0 slowest); stride_x[i] is the element stride of
+ * mode i inside operand x. */
+typedef struct {
+  int32_t n;
+  int32_t pad_;
+  int64_t dim[PTN_MAX_MODES];
+  int64_t stride_a[PTN_MAX_MODES];
+  int64_t stride_b[PTN_MAX_MODES];
+  int64_t stride_c[PTN_MAX_MODES];
+} ptn_modes;
+
+/* C[m, n] = alpha * sum_k opA(A)[m, k] * opB(B)[k, n] + beta * C[m, n]
+ * with m, n, k each a multi-mode index (ptn_modes). For the M group the
+ * strides used are stride_a (A) and stride_c (C); for N: stride_b, stride_c;
+ * for K: stride_a, stride_b. opX = conjugate when conj_x != 0.
+ * This is np.tensordot without the transposes: the strides address the legs
+ * in place, and C may be written in any leg order. */
+typedef struct {
+  const void* A;
+  const void* B;
+  void* C;
+  double alpha_re, alpha_im;
+  double beta_re, beta_im;
+  int32_t conj_a, conj_b;
+  ptn_modes m, n, k;
+} ptn_contract_desc;
+
+/* Complex128 tensor contraction in FP64 (plain path).
+ * Replaces np.tensordot inside contract_ket_ham_with_envs
+ * (contractions/state_operator_contraction.py:227-273), contract_any / contract_leaf /
+ * contract_subtrees_using_dictionary (:407-694), contract_bond_tensor (:984-1040)
+ * and contract_nodes (contractions/node_contraction.py:62-86). */
+int ptn_zcontract(const ptn_contract_desc* d, void* stream);
+
+/* ---- Krylov (Lanczos/Arnoldi) vector kernels, complex128 -------------------
+ * Replace the np.vdot / np.linalg.norm / axpy loop of krylov_exp_action
+ * (time_evolution/time_evolution.py:721-821). Vectors q_i are rows of a
+ * matrix Q with leading dimension ldq (elements). partial buffers are
+ * device scratch of at least ptn_krylov_partials(n) * (nq + 1) complex128. */
+int64_t ptn_krylov_partials(int64_t n);
+
+/* h[i] (+)= sum_x conj(Q[i, x]) w[x] for i < nq; h is device complex128[nq].
+ * accumulate != 0 adds to h instead of overwriting. */
+int ptn_zdot_multi(const void* Q, int64_t ldq, int32_t nq, const void* w, int64_t n,
+                   void* h, int32_t accumulate, void* partial, void* stream);
+
+/* w[x] -= sum_i h[i] * Q[i, x]. */
+int ptn_zaxpy_multi(const void* Q, int64_t ldq, int32_t nq, const void* h,
+                    void* w, int64_t n, void* stream);
+
+/* out_norm[0] = ||w||_2 (double, device). */
+int ptn_dznrm2(const void* w, int64_t n, void* out_norm, void* partial, void* stream);
+
+/* y[x] = w[x] * (1 / scale[0]) with scale a device double. */
+int ptn_zscal_inv(const void* w, const double* scale, void* y, int64_t n, void* stream);
+
+/* out[x] = sum_i c[i] * Q[i, x], c device complex128[nq]. */
+int ptn_zcombine(const void* Q, int64_t ldq, int32_t nq, const void* c,
+                 void* out, int64_t n, void* stream);
+
+/* ---- Householder QR (LAPACK zgeqrf/zungqr conventions) ----------------------
+ * Replaces np.linalg.qr inside tensor_qr_decomposition(mode=KEEP)
+ * (util/tensor_splitting.py:60-107). The m x k matrix lives inside a tensor:
+ * element (i, c) is at A[rowoff[i] + c * colstride]; rowoff (device int64[m])
+ * encodes the reference's row order. On return A holds Q (KEEP: columns past
+ * min(m, k) are zero) and R (device complex128[k * k], row-major, rows past
+ * min(m, k) zero) holds R. work: device scratch of ptn_zqr_work_bytes(m, k). */
+int64_t ptn_zqr_work_bytes(int64_t m, int64_t k);
+int ptn_zqr_keep(void* A, const int64_t* rowoff, int64_t m, int64_t k, int64_t colstride,
+                 void* R, void* work, void* stream);
+
+/* Number of kernel launches this library has issued since it was loaded
+ * (host-side counter; used to report launches inside a timed region). */
+unsigned long long ptn_launch_counter(void);
+
+/* Scan a complex128 buffer for NaN/Inf; flag (device int32) is set to 1 if found. */
+int ptn_check_finite(const void* x, int64_t n, int32_t* flag, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PTN_GB300_H */

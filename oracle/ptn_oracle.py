@@ -1,0 +1,587 @@
+"""NumPy restatement of PyTreeNet's one-site TDVP hot path (oracle, test infrastructure).
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` may use this module; the GPU engine never imports it.
+
+Every function cites the reference function whose algorithm it restates
+(paths are relative to the PyTreeNet project root). The data model differs
+from the reference on purpose: each node tensor keeps ONE physical leg layout
+(parent, children in insertion order, physical), while the reference's
+*logical* children order -- which the reference reshuffles during QR splits
+and contractions (``core/ttn.py:1235-1313``, ``contractions/node_contraction.py:88-138``)
+-- is tracked separately and used only where it changes numbers: the row order
+of every QR matricisation (``util/tensor_splitting.py:60-107``) and the
+processing order of ``canonical_form`` (``core/canonical_form.py:162-208``).
+On rank-deficient (zero-padded) tensors the Householder complement chosen by
+LAPACK depends on that row order, and one-site TDVP's result depends on the
+complement, so the order has to match for 1e-10 parity.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+__all__ = [
+    "OTree", "OState", "init_cache_but_one", "heff_apply", "bond_apply",
+    "env_update", "krylov_exp_action", "qr_keep_split", "canonical_form",
+    "leaf_to_root_path", "orthogonalisation_paths", "FirstOrderOneSiteTDVPOracle",
+    "SecondOrderOneSiteTDVPOracle", "state_vector", "expect_product",
+    "scalar_product",
+]
+
+
+# ----------------------------------------------------------------------------
+# tree structure
+# ----------------------------------------------------------------------------
+class OTree:
+    """Rooted tree; physical children order is fixed, logical order evolves."""
+
+    def __init__(self):
+        self.parent: dict[str, str | None] = {}
+        self.children: dict[str, list[str]] = {}
+        self.lchildren: dict[str, list[str]] = {}
+        self.root: str | None = None
+        self.nodes: list[str] = []
+
+    def copy(self) -> "OTree":
+        t = OTree()
+        t.parent = dict(self.parent)
+        t.children = {k: list(v) for k, v in self.children.items()}
+        t.lchildren = {k: list(v) for k, v in self.lchildren.items()}
+        t.root = self.root
+        t.nodes = list(self.nodes)
+        return t
+
+    def add_root(self, nid: str):
+        assert self.root is None
+        self.root = nid
+        self.parent[nid] = None
+        self.children[nid] = []
+        self.lchildren[nid] = []
+        self.nodes.append(nid)
+
+    def add_child(self, nid: str, pid: str):
+        self.parent[nid] = pid
+        self.children[nid] = []
+        self.lchildren[nid] = []
+        self.children[pid].append(nid)
+        self.lchildren[pid].append(nid)
+        self.nodes.append(nid)
+
+    def is_leaf(self, nid):
+        return len(self.children[nid]) == 0
+
+    def neighbours(self, nid):
+        """Physical order: parent first, then children in insertion order."""
+        p = self.parent[nid]
+        return ([p] if p is not None else []) + list(self.children[nid])
+
+    def lneighbours(self, nid):
+        """Reference order (``core/graph_node.py:340-355``)."""
+        p = self.parent[nid]
+        return ([p] if p is not None else []) + list(self.lchildren[nid])
+
+    def axis(self, nid, nbr):
+        """Physical tensor axis of ``nid`` that points to neighbour ``nbr``."""
+        return self.neighbours(nid).index(nbr)
+
+    def path_to_root(self, nid):
+        """``core/tree_structure.py:609-624``."""
+        path = [nid]
+        while self.parent[nid] is not None:
+            nid = self.parent[nid]
+            path.append(nid)
+        return path
+
+    def path_from_to(self, a, b):
+        """Unique tree path a -> b (``core/tree_structure.py:626-651``)."""
+        if a == b:
+            return [a]
+        pa = self.path_to_root(a)
+        pb = self.path_to_root(b)
+        sb = set(pb)
+        lca = next(x for x in pa if x in sb)
+        up = pa[:pa.index(lca) + 1]
+        down = pb[:pb.index(lca)]
+        return up + list(reversed(down))
+
+    def distance_to_node(self, center):
+        """Pre-order DFS over logical neighbours (``core/tree_structure.py:225-271``)."""
+        out = {center: 0}
+
+        def rec(nid, last, d):
+            out[nid] = d
+            for nb in self.lneighbours(nid):
+                if nb != last:
+                    rec(nb, nid, d + 1)
+        for nb in self.lneighbours(center):
+            rec(nb, center, 1)
+        return out
+
+
+class OState:
+    """A TTNS on an :class:`OTree`: one tensor per node in physical layout."""
+
+    def __init__(self, tree: OTree, tensors: dict[str, np.ndarray]):
+        self.tree = tree
+        self.tensors = {k: np.asarray(v) for k, v in tensors.items()}
+        self.orth_center: str | None = None
+
+    def copy(self) -> "OState":
+        s = OState(self.tree.copy(), {k: v.copy() for k, v in self.tensors.items()})
+        s.orth_center = self.orth_center
+        return s
+
+
+# ----------------------------------------------------------------------------
+# QR split with KEEP padding, in the reference's row order
+# ----------------------------------------------------------------------------
+def qr_keep_split(state: OState, nid: str, nbr: str):
+    """Split ``nid`` toward neighbour ``nbr``: tensor[nid] <- Q, return R.
+
+    Restates ``tensor_qr_decomposition(mode=KEEP)`` (``util/tensor_splitting.py:60-107``)
+    as called by ``OneSiteTDVP._split_updated_site`` (``time_evolution/tdvp_algorithms/onesitetdvp.py:69-101``)
+    and ``split_qr_contract_r_to_neighbour`` (``core/canonical_form.py:76-120``).
+    Rows are matricised in the reference's logical order: (parent, logical
+    children without ``nbr``, physical) when ``nbr`` is a child, (logical
+    children, physical) when ``nbr`` is the parent. R has legs
+    (new bond on the Q side, bond on the ``nbr`` side).
+    Logical order afterwards: a split toward child X puts X first in
+    ``nid``'s children (``core/ttn.py:1409-1440``).
+    """
+    tree = state.tree
+    A = state.tensors[nid]
+    if tree.parent[nid] == nbr:
+        row_nbrs = list(tree.lchildren[nid])
+    else:
+        p = tree.parent[nid]
+        row_nbrs = ([p] if p is not None else []) + [c for c in tree.lchildren[nid] if c != nbr]
+    row_axes = [tree.axis(nid, x) for x in row_nbrs] + [A.ndim - 1]
+    col_axis = tree.axis(nid, nbr)
+    k = A.shape[col_axis]
+    mat = np.transpose(A, row_axes + [col_axis]).reshape(-1, k)
+    q, r = np.linalg.qr(mat, mode="reduced")
+    if q.shape[1] < k:
+        diff = k - q.shape[1]
+        q = np.pad(q, [(0, 0), (0, diff)])
+        r = np.pad(r, [(0, diff), (0, 0)])
+    qt = q.reshape([A.shape[a] for a in row_axes] + [k])
+    perm_to_phys = np.argsort(row_axes + [col_axis])
+    state.tensors[nid] = np.ascontiguousarray(np.transpose(qt, perm_to_phys))
+    if tree.parent[nid] != nbr:
+        tree.lchildren[nid] = [nbr] + [c for c in tree.lchildren[nid] if c != nbr]
+    return r
+
+
+def absorb_r(state: OState, r: np.ndarray, src: str, dst: str, link_variant: bool):
+    """Contract R (legs: src-side, dst-side) into ``dst``'s leg toward ``src``.
+
+    Logical order when ``dst`` is the parent of ``src``: the move-orthogonality
+    variant (``contract_nodes(neighbour, r)``, ``core/canonical_form.py:113-114``)
+    puts ``src`` LAST among ``dst``'s children, the link-update variant
+    (``contract_nodes(link, next)``, ``onesitetdvp.py:125-126``) puts it FIRST
+    (``contractions/node_contraction.py:120-131``).
+    """
+    tree = state.tree
+    T = state.tensors[dst]
+    ax = tree.axis(dst, src)
+    out = np.tensordot(r, T, axes=([1], [ax]))          # new leg first
+    out = np.moveaxis(out, 0, ax)
+    state.tensors[dst] = out
+    if tree.parent[src] == dst:
+        others = [c for c in tree.lchildren[dst] if c != src]
+        tree.lchildren[dst] = ([src] + others) if link_variant else (others + [src])
+
+
+def move_orth_one_hop(state: OState, a: str, b: str):
+    """``split_qr_contract_r_to_neighbour(a -> b)`` with KEEP (``core/canonical_form.py:76-120``)."""
+    r = qr_keep_split(state, a, b)
+    absorb_r(state, r, a, b, link_variant=False)
+
+
+def move_orth_center(state: OState, new_center: str):
+    """``TreeTensorNetwork.move_orthogonalization_center`` (``core/ttn.py:1530-1552``)."""
+    assert state.orth_center is not None
+    path = state.tree.path_from_to(state.orth_center, new_center)
+    for a, b in zip(path[:-1], path[1:]):
+        move_orth_one_hop(state, a, b)
+    state.orth_center = new_center
+
+
+def canonical_form(state: OState, center: str):
+    """``canonical_form`` (``core/canonical_form.py:162-208``): farthest nodes first,
+    each split toward its neighbour closest to the centre, within one distance
+    in pre-order DFS order."""
+    dist = state.tree.distance_to_node(center)
+    maxd = max(dist.values()) if dist else 0
+    for d in range(maxd, 0, -1):
+        for nid in [n for n in dist if dist[n] == d]:
+            nbrs = state.tree.lneighbours(nid)
+            target = min(nbrs, key=lambda x: dist[x])
+            move_orth_one_hop(state, nid, target)
+    state.orth_center = center
+
+
+# ----------------------------------------------------------------------------
+# contractions
+# ----------------------------------------------------------------------------
+class _L:
+    """A tensor with one label per leg; contractions go through np.tensordot."""
+    __slots__ = ("t", "legs")
+
+    def __init__(self, t, legs):
+        self.t, self.legs = t, list(legs)
+
+    def dot(self, other: "_L", labels):
+        ia = [self.legs.index(x) for x in labels]
+        ib = [other.legs.index(x) for x in labels]
+        t = np.tensordot(self.t, other.t, axes=(ia, ib))
+        legs = [x for x in self.legs if x not in labels] + [x for x in other.legs if x not in labels]
+        return _L(t, legs)
+
+    def out(self, order):
+        return np.transpose(self.t, [self.legs.index(x) for x in order])
+
+
+def _site_chain(x, W, nbrs, envs_of, open_k=None):
+    """Apply the environments and W to a site tensor in the interleaved order:
+    the first half of the environments, then W, then the rest (the cheapest
+    order for degree >= 2; the reference contracts all environments first).
+    ``open_k`` leaves neighbour k's bond (ket leg and ham leg) open.
+    Returns a labelled tensor with legs a'_k (bra), s', and for ``open_k``
+    also a_k, b_k."""
+    n = len(nbrs)
+    T = _L(x, [f"a{k}" for k in range(n)] + ["s"])
+    ks = [k for k in range(n) if k != open_k]
+    half = len(ks) // 2
+    for k in ks[:half]:
+        T = T.dot(_L(envs_of(nbrs[k]), [f"a{k}", f"b{k}", f"c{k}"]), [f"a{k}"])
+    Wl = _L(W, [f"b{k}" for k in range(n)] + ["t", "s"])
+    T = T.dot(Wl, [f"b{k}" for k in ks[:half]] + ["s"])
+    for k in ks[half:]:
+        T = T.dot(_L(envs_of(nbrs[k]), [f"a{k}", f"b{k}", f"c{k}"]), [f"a{k}", f"b{k}"])
+    return T
+
+
+def heff_apply(x, tree: OTree, nid: str, W, envs):
+    """y = H_eff x for one site (``contract_ket_ham_with_envs``,
+    ``contractions/state_operator_contraction.py:227-273``).
+
+    x legs (physical neighbours..., s); env for neighbour k is the cache entry
+    (k -> nid) with legs (ket, ham, bra); W legs (neighbours..., out, in).
+    y[a'..., s'] = sum E_k[a_k, b_k, a'_k] W[b..., s', s] x[a..., s].
+    """
+    nbrs = tree.neighbours(nid)
+    T = _site_chain(x, W, nbrs, lambda nb: envs[(nb, nid)])
+    return T.out([f"c{k}" for k in range(len(nbrs))] + ["t"])
+
+
+def env_update(tree: OTree, nid: str, nxt: str, A, W, envs):
+    """Environment E(nid -> nxt), legs (ket, ham, bra)
+    (``contract_any``/``contract_leaf``/``contract_subtrees_using_dictionary``,
+    ``contractions/state_operator_contraction.py:407-694``)."""
+    nbrs = tree.neighbours(nid)
+    k = nbrs.index(nxt)
+    T = _site_chain(A, W, nbrs, lambda nb: envs[(nb, nid)], open_k=k)
+    B = _L(A.conj(), [f"c{j}" if j != k else "z" for j in range(len(nbrs))] + ["t"])
+    E = T.dot(B, [f"c{j}" for j in range(len(nbrs)) if j != k] + ["t"])
+    return E.out([f"a{k}", f"b{k}", "z"])
+
+
+def bond_apply(r, e_q, e_n):
+    """Bond H_eff matvec (``contract_bond_tensor``,
+    ``contractions/state_operator_contraction.py:984-1040``):
+    y[a', c'] = sum E_q[a, b, a'] r[a, c] E_n[c, b, c']."""
+    t = np.tensordot(e_q, r, axes=([0], [0]))          # (b, a', c)
+    return np.tensordot(t, e_n, axes=([0, 2], [1, 0]))
+
+
+def init_cache_but_one(state: OState, W: dict, left_out: str) -> dict:
+    """All environments pointing toward ``left_out``
+    (``SandwichCache.init_cache_but_one``, ``contractions/sandwich_caching.py:97-126``)."""
+    tree = state.tree
+    envs = {}
+
+    def rec(nid, toward):
+        for nb in tree.neighbours(nid):
+            if nb != toward:
+                rec(nb, nid)
+        if toward is not None:
+            envs[(nid, toward)] = env_update(tree, nid, toward, state.tensors[nid], W[nid], envs)
+    rec(left_out, None)
+    return envs
+
+
+# ----------------------------------------------------------------------------
+# Krylov exponential
+# ----------------------------------------------------------------------------
+def _small_propagator(T, dt, exp_factor, hermitian=True):
+    """First column of exp(exp_factor dt T) (``_krylov_small_propagator``,
+    ``time_evolution/time_evolution.py:696-718``)."""
+    if hermitian:
+        H = 0.5 * (T + T.conj().T)
+        ev, V = np.linalg.eigh(H)
+        return V @ (np.exp(exp_factor * dt * ev) * V[0].conj())
+    import scipy.linalg
+    return scipy.linalg.expm(exp_factor * dt * T)[:, 0]
+
+
+def krylov_exp_action(psi, action, dt, exp_factor, krylov_tol=1e-10,
+                      max_krylov_dim=None, hermitian=True, stats=None):
+    """exp(exp_factor dt A) psi by Arnoldi with two Gram-Schmidt passes
+    (``krylov_exp_action``, ``time_evolution/time_evolution.py:721-821``)."""
+    shape = psi.shape
+    v0 = np.asarray(psi, dtype=complex).reshape(-1)
+    n = v0.size
+    beta0 = float(np.linalg.norm(v0))
+    if beta0 == 0.0:
+        return v0.copy().reshape(shape)
+    max_steps = n if max_krylov_dim is None else min(n, int(max_krylov_dim))
+    floor_abs = np.finfo(float).eps * max(n, 1)
+    Q = [v0 / beta0]
+    T = np.zeros((max_steps + 1, max_steps + 1), dtype=complex)
+    m = 0
+    for j in range(max_steps):
+        w = np.asarray(action(Q[j].reshape(shape)), dtype=complex).reshape(-1)
+        w0 = float(np.linalg.norm(w))
+        for _ in range(2):
+            for i in range(j + 1):
+                h = np.vdot(Q[i], w)
+                T[i, j] += h
+                w = w - h * Q[i]
+        beta = float(np.linalg.norm(w))
+        T[j + 1, j] = beta
+        m = j + 1
+        if beta <= max(floor_abs, 1e-12 * w0):
+            break
+        if krylov_tol > 0.0:
+            col = _small_propagator(T[:m, :m], dt, exp_factor, hermitian)
+            if beta0 * beta * abs(col[m - 1]) < krylov_tol:
+                break
+        Q.append(w / beta)
+    if stats is not None:
+        stats.append(m)
+    c = beta0 * _small_propagator(T[:m, :m], dt, exp_factor, hermitian)
+    out = np.zeros(n, dtype=complex)
+    for i in range(m):
+        out += c[i] * Q[i]
+    return out.reshape(shape)
+
+
+# ----------------------------------------------------------------------------
+# update paths
+# ----------------------------------------------------------------------------
+def _postorder(tree: OTree, nid):
+    if tree.is_leaf(nid):
+        return [nid]
+    out = []
+    for c in tree.lchildren[nid]:
+        out += _postorder(tree, c)
+    return out + [nid]
+
+
+def leaf_to_root_path(tree: OTree):
+    """``TDVPUpdatePathFinder_LeafToRoot.find_path``
+    (``time_evolution/time_evo_util/update_path.py:63-254``)."""
+    root = tree.root
+    dist = tree.distance_to_node(root)
+    start = max(dist, key=dist.get)
+    main = tree.path_to_root(start)
+    path = []
+    for origin in main:
+        if origin != root:
+            path += [x for c in tree.lchildren[origin] if c not in main
+                     for x in _postorder(tree, c)] + [origin]
+            continue
+        if len(tree.lchildren[root]) == 1:
+            path += [root]
+            continue
+        leaves = [nid for nid in tree.nodes if tree.is_leaf(nid) and nid not in path]
+        ld = {nid: d for nid, d in dist.items() if nid in leaves}
+        last = max(ld, key=ld.get)
+        down = list(reversed(tree.path_to_root(last)))
+        for o in down:
+            if o == root:
+                excl = (main[-2], down[1])
+                path += [x for c in tree.lchildren[root] if c not in excl
+                         for x in _postorder(tree, c)] + [root]
+            else:
+                path += [x for c in tree.lchildren[o] if c not in down
+                         for x in _postorder(tree, c)] + [o]
+    return path
+
+
+def orthogonalisation_paths(tree: OTree, path):
+    """``find_orthogonalisation_path`` (``update_path.py:400-421``)."""
+    return [tree.path_from_to(path[i], path[i + 1])[1:] for i in range(len(path) - 1)]
+
+
+# ----------------------------------------------------------------------------
+# one-site TDVP drivers
+# ----------------------------------------------------------------------------
+class _OneSiteBase:
+    """Shared machinery of ``TDVPAlgorithm`` / ``OneSiteTDVP``
+    (``tdvp_algorithms/tdvp_algorithm.py:58-221``, ``onesitetdvp.py:17-134``)."""
+
+    def __init__(self, state: OState, W: dict, dt: float, krylov_tol=1e-10,
+                 max_krylov_dim=None):
+        self.state = state.copy()
+        self.W = W
+        self.dt = dt
+        self.tol = krylov_tol
+        self.maxdim = max_krylov_dim
+        self.krylov_dims = []
+        init_tree = state.tree.copy()
+        self.update_path = leaf_to_root_path(init_tree)
+        self.orth_paths = orthogonalisation_paths(init_tree, self.update_path)
+        if self.state.orth_center is None:
+            canonical_form(self.state, self.update_path[0])
+        else:
+            move_orth_center(self.state, self.update_path[0])
+        self.envs = init_cache_but_one(self.state, W, self.update_path[0])
+
+    def _krylov(self, x, action, factor, exp_factor):
+        return krylov_exp_action(x, action, self.dt * factor, exp_factor,
+                                 krylov_tol=self.tol, max_krylov_dim=self.maxdim,
+                                 stats=self.krylov_dims)
+
+    def update_site(self, nid, factor=1.0):
+        tree = self.state.tree
+        W = self.W[nid]
+        act = lambda y: heff_apply(y, tree, nid, W, self.envs)
+        self.state.tensors[nid] = self._krylov(self.state.tensors[nid], act, factor, -1j)
+
+    def update_link(self, nid, nxt, factor=1.0):
+        assert self.state.orth_center == nid
+        tree = self.state.tree
+        r = qr_keep_split(self.state, nid, nxt)
+        self.envs[(nid, nxt)] = env_update(tree, nid, nxt, self.state.tensors[nid],
+                                           self.W[nid], self.envs)
+        e_q, e_n = self.envs[(nid, nxt)], self.envs[(nxt, nid)]
+        act = lambda y: bond_apply(y, e_q, e_n)
+        r = self._krylov(r, act, factor, +1j)
+        absorb_r(self.state, r, nid, nxt, link_variant=True)
+        self.state.orth_center = nxt
+
+    def move_orth_and_update_cache(self, path):
+        if len(path) == 0:
+            return
+        assert self.state.orth_center == path[0]
+        tree = self.state.tree
+        for prev, nid in zip(path[:-1], path[1:]):
+            move_orth_center(self.state, nid)
+            self.envs[(prev, nid)] = env_update(tree, prev, nid, self.state.tensors[prev],
+                                                self.W[prev], self.envs)
+
+
+class FirstOrderOneSiteTDVPOracle(_OneSiteBase):
+    """``FirstOrderOneSiteTDVP.run_one_time_step`` (``firstorderonesite.py:23-104``)."""
+
+    def run_one_time_step(self):
+        path = self.update_path
+        for i, nid in enumerate(path):
+            if i == len(path) - 1:
+                if len(self.orth_paths) > 0:
+                    self.move_orth_and_update_cache(self.orth_paths[-1])
+                self.update_site(nid)
+                move_orth_center(self.state, path[0])
+                self.envs = init_cache_but_one(self.state, self.W, path[0])
+            elif i == 0:
+                self.update_site(nid)
+                self.update_link(nid, self.orth_paths[0][0])
+            else:
+                self.move_orth_and_update_cache(self.orth_paths[i - 1])
+                self.update_site(nid)
+                self.update_link(nid, self.orth_paths[i][0])
+
+
+class SecondOrderOneSiteTDVPOracle(_OneSiteBase):
+    """``SecondOrderOneSiteTDVP.run_one_time_step`` (``secondorderonesite.py:60-193``)."""
+
+    def __init__(self, *a, **k):
+        super().__init__(*a, **k)
+        self.back_path = list(reversed(self.update_path))
+        tree = self.state.tree
+        bo = []
+        for i, nid in enumerate(self.back_path[1:-1]):
+            bo.append(tree.path_from_to(nid, self.back_path[i + 2])[:-1])
+        bo.append([self.back_path[-1]])
+        self.back_orth = bo
+
+    def run_one_time_step(self):
+        path = self.update_path
+        for i, nid in enumerate(path[:-1]):
+            if i > 0:
+                self.move_orth_and_update_cache(self.orth_paths[i - 1])
+            nxt = self.orth_paths[i][0]
+            self.update_site(nid, 0.5)
+            self.update_link(nid, nxt, 0.5)
+        self.update_site(path[-1], 1.0)
+        bp = self.back_path
+        self.update_link(self.state.orth_center, bp[1], 0.5)
+        for i, nid in enumerate(bp[1:-1]):
+            idx = i + 1
+            self.update_site(nid, 0.5)
+            self.move_orth_and_update_cache(self.back_orth[idx - 1])
+            self.update_link(self.state.orth_center, bp[idx + 1], 0.5)
+        self.update_site(bp[-1], 0.5)
+
+
+# ----------------------------------------------------------------------------
+# observables and full contractions
+# ----------------------------------------------------------------------------
+def expect_product(state: OState, ops: dict, bra: OState | None = None) -> complex:
+    """<bra| prod_i O_i |ket> for single-site operators (``TTNS.tensor_product_expectation_value``,
+    ``ttns/ttns.py:240-264``; bra defaults to the state)."""
+    bra = state if bra is None else bra
+    tree = state.tree
+
+    def rec(nid, toward):
+        A = state.tensors[nid]
+        if nid in ops:
+            A = np.moveaxis(np.tensordot(ops[nid], A, axes=([1], [A.ndim - 1])), 0, -1)
+        nbrs = tree.neighbours(nid)
+        T = _L(A, [f"a{k}" for k in range(len(nbrs))] + ["s"])
+        for k, nb in enumerate(nbrs):
+            if nb != toward:
+                T = T.dot(_L(rec(nb, nid), [f"a{k}", f"c{k}"]), [f"a{k}"])
+        B = _L(bra.tensors[nid].conj(), [f"c{k}" if nb != toward else "z"
+                                          for k, nb in enumerate(nbrs)] + ["s"])
+        E = T.dot(B, [f"c{k}" for k, nb in enumerate(nbrs) if nb != toward] + ["s"])
+        if toward is None:
+            return E.t
+        k = nbrs.index(toward)
+        return E.out([f"a{k}", "z"])
+    return complex(rec(tree.root, None))
+
+
+def scalar_product(a: OState, b: OState) -> complex:
+    """<a|b> (``contract_two_ttns``, ``contractions/state_state_contraction.py:29-66``)."""
+    return expect_product(b, {}, bra=a)
+
+
+def state_vector(state: OState, site_order):
+    """Dense state vector with sites in ``site_order`` (small trees only)."""
+    tree = state.tree
+
+    def rec(nid, toward):
+        A = state.tensors[nid]
+        legs = tree.neighbours(nid)
+        sites = [nid]
+        T = A
+        cur = list(legs) + ["#" + nid]
+        for nb in legs:
+            if nb == toward:
+                continue
+            sub, subsites = rec(nb, nid)
+            ax = cur.index(nb)
+            T = np.tensordot(T, sub, axes=([ax], [0]))
+            cur = cur[:ax] + cur[ax + 1:] + ["#" + s for s in subsites]
+            sites += subsites
+        if toward is not None:
+            ax = cur.index(toward)
+            T = np.moveaxis(T, ax, 0)
+            cur = [cur[ax]] + cur[:ax] + cur[ax + 1:]
+        return T, [c[1:] for c in cur if c.startswith("#")]
+    T, sites = rec(tree.root, None)
+    perm = [sites.index(s) for s in site_order]
+    return np.transpose(T, perm).reshape(-1)

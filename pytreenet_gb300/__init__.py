@@ -1,0 +1,19 @@
+"""pytreenet_gb300 -- GB300 engine for PyTreeNet's TDVP local-update hot path.
+
+Drop-in surface for the path (names as in PyTreeNet):
+TreeTensorNetworkState/TTNS, TreeTensorNetworkOperator/TTNO, Node,
+FirstOrderOneSiteTDVP, SecondOrderOneSiteTDVP, TDVPConfig, TimeEvoMode,
+EvoDirection, TensorProduct. Numerics run in libptn_gb300.so (hand-written
+CUDA for sm_103a) through a C ABI; see include/ptn_gb300.h.
+"""
+from .ttn import Node, TreeTensorNetworkState, TreeTensorNetworkOperator, TTNS, TTNO
+from .tdvp import (TimeEvoMode, EvoDirection, PathFinderMode, TDVPConfig, TensorProduct,
+                   FirstOrderOneSiteTDVP, SecondOrderOneSiteTDVP, leaf_to_root_update_path)
+from .operators import nearest_neighbour_ttno, tfim_ttno, heisenberg_ttno
+
+__all__ = [
+    "Node", "TreeTensorNetworkState", "TreeTensorNetworkOperator", "TTNS", "TTNO",
+    "TimeEvoMode", "EvoDirection", "PathFinderMode", "TDVPConfig", "TensorProduct",
+    "FirstOrderOneSiteTDVP", "SecondOrderOneSiteTDVP", "leaf_to_root_update_path",
+    "nearest_neighbour_ttno", "tfim_ttno", "heisenberg_ttno",
+]

@@ -1,0 +1,100 @@
+"""ctypes binding of libptn_gb300.so (the C ABI declared in include/ptn_gb300.h).
+
+The library is loaded on first use. There is no CPU fallback: if the library
+is missing or CUDA is unavailable, every engine call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from .build import LIB
+
+MAX_MODES = 6
+
+PTN_OK = 0
+_STATUS = {
+    1: "invalid argument (shape, stride or null pointer)",
+    2: "CUDA launch/runtime error",
+    3: "non-finite value in input",
+    4: "Krylov breakdown",
+    5: "decomposition did not converge",
+    6: "configuration outside the kernel's limits",
+}
+
+
+class PtnError(RuntimeError):
+    """Error status returned by libptn_gb300."""
+
+    def __init__(self, status: int, what: str):
+        super().__init__(f"{what}: ptn status {status} ({_STATUS.get(status, 'unknown')})")
+        self.status = status
+
+
+class PtnArgumentError(PtnError, ValueError):
+    pass
+
+
+class Modes(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int32), ("pad_", ctypes.c_int32),
+                ("dim", ctypes.c_int64 * MAX_MODES),
+                ("stride_a", ctypes.c_int64 * MAX_MODES),
+                ("stride_b", ctypes.c_int64 * MAX_MODES),
+                ("stride_c", ctypes.c_int64 * MAX_MODES)]
+
+
+class ContractDesc(ctypes.Structure):
+    _fields_ = [("A", ctypes.c_void_p), ("B", ctypes.c_void_p), ("C", ctypes.c_void_p),
+                ("alpha_re", ctypes.c_double), ("alpha_im", ctypes.c_double),
+                ("beta_re", ctypes.c_double), ("beta_im", ctypes.c_double),
+                ("conj_a", ctypes.c_int32), ("conj_b", ctypes.c_int32),
+                ("m", Modes), ("n", Modes), ("k", Modes)]
+
+
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_I32 = ctypes.c_int32
+SIGNATURES = {
+    "ptn_zcontract": (ctypes.c_int, [ctypes.POINTER(ContractDesc), _P]),
+    "ptn_krylov_partials": (_I64, [_I64]),
+    "ptn_zdot_multi": (ctypes.c_int, [_P, _I64, _I32, _P, _I64, _P, _I32, _P, _P]),
+    "ptn_zaxpy_multi": (ctypes.c_int, [_P, _I64, _I32, _P, _P, _I64, _P]),
+    "ptn_dznrm2": (ctypes.c_int, [_P, _I64, _P, _P, _P]),
+    "ptn_zscal_inv": (ctypes.c_int, [_P, _P, _P, _I64, _P]),
+    "ptn_zcombine": (ctypes.c_int, [_P, _I64, _I32, _P, _P, _I64, _P]),
+    "ptn_zqr_work_bytes": (_I64, [_I64, _I64]),
+    "ptn_zqr_keep": (ctypes.c_int, [_P, _P, _I64, _I64, _I64, _P, _P, _P]),
+    "ptn_check_finite": (ctypes.c_int, [_P, _I64, _P, _P]),
+    "ptn_launch_counter": (ctypes.c_ulonglong, []),
+}
+
+_lib = None
+
+
+def library_path() -> str:
+    return LIB
+
+
+def load():
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB):
+        raise RuntimeError(
+            f"{LIB} is missing: build it with `python -m pytreenet_gb300.build` "
+            "(the engine has no CPU fallback)")
+    lib = ctypes.CDLL(LIB)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(status: int, what: str):
+    if status != PTN_OK:
+        if status == 1:
+            raise PtnArgumentError(status, what)
+        raise PtnError(status, what)

@@ -1,0 +1,279 @@
+// Householder QR in complex128 with LAPACK's zgeqr2/zung2r conventions.
+//
+// PyTreeNet splits a site with np.linalg.qr (LAPACK zgeqrf + zungqr) inside
+// tensor_qr_decomposition(mode=KEEP) (util/tensor_splitting.py:60-107). On the
+// zero-padded, rank-deficient tensors that one-site TDVP starts from, the
+// orthonormal complement that Householder QR produces decides the TDVP result,
+// so this follows the same published reflector convention (zlarfg: beta real,
+// beta = -sign(Re alpha) * ||(alpha, x)||, tau = (beta - alpha) / beta,
+// v = x / (alpha - beta); H = I - tau v v^H applied as H^H during the
+// factorisation and as H when Q is formed). Exact zeros stay exact zeros, so
+// the complement is reproduced exactly.
+//
+// The matrix is addressed in place inside the site tensor: element (i, c) at
+// A[rowoff[i] + c * colstride], where the row-offset table carries the
+// reference's (logical) row order. Each Householder step is a short sequence
+// of ordinary launches (column norm, reflector, column dots, dot reduction,
+// trailing update); no kernel waits on another.
+#include "ptn_common.cuh"
+
+namespace {
+
+constexpr int QT = 256;          // threads per CTA
+constexpr int RB = 1024;         // rows per row-chunk
+constexpr int CB = 8;            // columns per column-chunk (one warp each)
+
+struct QRWork {
+  // device layout of the work buffer
+  double2* tau;       // [k]
+  double2* scal;      // [k]
+  double2* w;         // [k]
+  double* npart;      // [nrb]
+  double2* dpart;     // [nrb * k]
+};
+
+inline int64_t nrb_for(int64_t m) { return (m + RB - 1) / RB; }
+
+inline QRWork carve(void* work, int64_t m, int64_t k) {
+  QRWork q;
+  char* p = static_cast<char*>(work);
+  q.tau = reinterpret_cast<double2*>(p);
+  p += 16 * k;
+  q.scal = reinterpret_cast<double2*>(p);
+  p += 16 * k;
+  q.w = reinterpret_cast<double2*>(p);
+  p += 16 * k;
+  q.npart = reinterpret_cast<double*>(p);
+  p += 16 * ((nrb_for(m) + 1) / 2 + 1);
+  q.dpart = reinterpret_cast<double2*>(p);
+  return q;
+}
+
+__device__ __forceinline__ double2 ld(const double2* A, const int64_t* rowoff, int64_t cs,
+                                      int64_t i, int64_t c) {
+  return A[rowoff[i] + c * cs];
+}
+
+// partial[b] = sum_{i in chunk b, i > j} |A[i, j]|^2
+__global__ void __launch_bounds__(QT) colnorm_kernel(const double2* __restrict__ A,
+                                                     const int64_t* __restrict__ rowoff, int64_t cs,
+                                                     int64_t m, int64_t j, double* __restrict__ part) {
+  const int64_t r0 = (j + 1) + (int64_t)blockIdx.x * RB;
+  double acc = 0.0;
+  for (int64_t i = r0 + threadIdx.x; i < m && i < r0 + RB; i += QT) acc += cabs2(ld(A, rowoff, cs, i, j));
+  __shared__ double red[QT / 32];
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < QT / 32; ++i) s += red[i];
+    part[blockIdx.x] = s;
+  }
+}
+
+// One thread: zlarfg on (A[j, j], A[j+1:, j]).
+__global__ void reflector_kernel(double2* __restrict__ A, const int64_t* __restrict__ rowoff, int64_t cs,
+                                 int64_t j, const double* __restrict__ part, int nparts,
+                                 double2* __restrict__ tau, double2* __restrict__ scal) {
+  if (threadIdx.x != 0) return;
+  double s = 0.0;
+  for (int b = 0; b < nparts; ++b) s += part[b];
+  const double xnorm = sqrt(s);
+  double2* pa = A + rowoff[j] + j * cs;
+  const double2 alpha = *pa;
+  if (xnorm == 0.0 && alpha.y == 0.0) {
+    tau[j] = make_double2(0.0, 0.0);
+    scal[j] = make_double2(0.0, 0.0);
+    return;
+  }
+  double nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xnorm * xnorm);
+  const double beta = (alpha.x >= 0.0) ? -nrm : nrm;
+  tau[j] = make_double2((beta - alpha.x) / beta, -alpha.y / beta);
+  // scal = 1 / (alpha - beta)
+  double2 d = make_double2(alpha.x - beta, alpha.y);
+  double den = d.x * d.x + d.y * d.y;
+  scal[j] = make_double2(d.x / den, -d.y / den);
+  *pa = make_double2(beta, 0.0);
+}
+
+// Reflector component v_i (v_j = 1).
+__device__ __forceinline__ double2 vcomp(const double2* A, const int64_t* rowoff, int64_t cs, int64_t i,
+                                         int64_t j, double2 sc, bool stored) {
+  if (i == j) return make_double2(1.0, 0.0);
+  double2 a = ld(A, rowoff, cs, i, j);
+  return stored ? a : cmul(a, sc);
+}
+
+// dpart[rb * k + c] = sum_{i in chunk rb, i >= j} conj(v_i) X[i, c], for c in [c_lo, k)
+// grid: (row chunks, column chunks of CB); one warp per column.
+// stored != 0: column j already holds v (Q formation); else v = scal * A[:, j].
+__global__ void __launch_bounds__(QT) dots_kernel(const double2* __restrict__ A,
+                                                  const int64_t* __restrict__ rowoff, int64_t cs,
+                                                  int64_t m, int64_t k, int64_t j, int64_t c_lo,
+                                                  const double2* __restrict__ scal, int stored,
+                                                  double2* __restrict__ dpart) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t c = c_lo + (int64_t)blockIdx.y * CB + warp;
+  const int64_t r0 = j + (int64_t)blockIdx.x * RB;
+  const double2 sc = scal[j];
+  __shared__ double2 vs[RB];
+  for (int64_t t = threadIdx.x; t < RB; t += QT) {
+    int64_t i = r0 + t;
+    vs[t] = (i < m) ? vcomp(A, rowoff, cs, i, j, sc, stored != 0) : make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  if (c >= k) return;
+  double2 acc = make_double2(0.0, 0.0);
+  for (int64_t t = lane; t < RB; t += 32) {
+    int64_t i = r0 + t;
+    if (i >= m) break;
+    acc = cfmac(vs[t], ld(A, rowoff, cs, i, c), acc);
+  }
+  acc = warp_sum2(acc);
+  if (lane == 0) dpart[(int64_t)blockIdx.x * k + c] = acc;
+}
+
+__global__ void dots_finish_kernel(const double2* __restrict__ dpart, int nrb, int64_t k, int64_t c_lo,
+                                   double2* __restrict__ w) {
+  const int64_t c = c_lo + blockIdx.x;
+  double2 s = make_double2(0.0, 0.0);
+  for (int b = threadIdx.x; b < nrb; b += 32) s = cadd(s, dpart[(int64_t)b * k + c]);
+  s = warp_sum2(s);
+  if (threadIdx.x == 0) w[c] = s;
+}
+
+// X[i, c] -= f * v_i * w_c for i >= j, c in [c_lo, k); f = conj(tau) (factorisation)
+// or tau (Q formation).
+__global__ void __launch_bounds__(QT) update_kernel(double2* __restrict__ A,
+                                                    const int64_t* __restrict__ rowoff, int64_t cs,
+                                                    int64_t m, int64_t k, int64_t j, int64_t c_lo,
+                                                    const double2* __restrict__ tau,
+                                                    const double2* __restrict__ scal,
+                                                    const double2* __restrict__ w, int stored,
+                                                    int conj_tau) {
+  const int64_t r0 = j + (int64_t)blockIdx.x * RB;
+  const int64_t cbase = c_lo + (int64_t)blockIdx.y * CB;
+  double2 f = tau[j];
+  if (conj_tau) f.y = -f.y;
+  const double2 sc = scal[j];
+  for (int64_t t = threadIdx.x; t < RB; t += QT) {
+    int64_t i = r0 + t;
+    if (i >= m) break;
+    double2 v = vcomp(A, rowoff, cs, i, j, sc, stored != 0);
+    double2 fv = cmul(f, v);
+    const int64_t ro = rowoff[i];
+    for (int cc = 0; cc < CB; ++cc) {
+      int64_t c = cbase + cc;
+      if (c >= k) break;
+      double2* p = A + ro + c * cs;
+      *p = csub(*p, cmul(fv, w[c]));
+    }
+  }
+}
+
+// After the trailing update of step j: A[i, j] <- scal * A[i, j] (the stored v_i), i > j.
+__global__ void __launch_bounds__(QT) store_v_kernel(double2* __restrict__ A, const int64_t* __restrict__ rowoff,
+                                                     int64_t cs, int64_t m, int64_t j,
+                                                     const double2* __restrict__ scal) {
+  const double2 sc = scal[j];
+  for (int64_t i = j + 1 + blockIdx.x * (int64_t)QT + threadIdx.x; i < m; i += (int64_t)gridDim.x * QT) {
+    double2* p = A + rowoff[i] + j * cs;
+    *p = cmul(*p, sc);
+  }
+}
+
+// Copy the upper triangle of rows < p into R (k x k row-major), zero elsewhere.
+__global__ void extract_r_kernel(const double2* __restrict__ A, const int64_t* __restrict__ rowoff,
+                                 int64_t cs, int64_t k, int64_t p, double2* __restrict__ R) {
+  for (int64_t e = blockIdx.x * (int64_t)QT + threadIdx.x; e < k * k; e += (int64_t)gridDim.x * QT) {
+    int64_t r = e / k, c = e - r * k;
+    R[e] = (r < p && c >= r) ? ld(A, rowoff, cs, r, c) : make_double2(0.0, 0.0);
+  }
+}
+
+// Column j of Q: Q[j, j] = 1 - tau, Q[i > j, j] = -tau v_i, Q[i < j, j] = 0.
+__global__ void __launch_bounds__(QT) qcol_kernel(double2* __restrict__ A, const int64_t* __restrict__ rowoff,
+                                                  int64_t cs, int64_t m, int64_t j,
+                                                  const double2* __restrict__ tau) {
+  const double2 t = tau[j];
+  for (int64_t i = blockIdx.x * (int64_t)QT + threadIdx.x; i < m; i += (int64_t)gridDim.x * QT) {
+    double2* p = A + rowoff[i] + j * cs;
+    if (i < j) *p = make_double2(0.0, 0.0);
+    else if (i == j) *p = make_double2(1.0 - t.x, -t.y);
+    else *p = make_double2(-(t.x * p->x - t.y * p->y), -(t.x * p->y + t.y * p->x));
+  }
+}
+
+// KEEP padding: zero the columns p..k-1 of Q.
+__global__ void zero_cols_kernel(double2* __restrict__ A, const int64_t* __restrict__ rowoff, int64_t cs,
+                                 int64_t m, int64_t k, int64_t p) {
+  const int64_t nc = k - p;
+  for (int64_t e = blockIdx.x * (int64_t)QT + threadIdx.x; e < m * nc; e += (int64_t)gridDim.x * QT) {
+    int64_t i = e / nc, c = p + (e - (e / nc) * nc);
+    A[rowoff[i] + c * cs] = make_double2(0.0, 0.0);
+  }
+}
+
+inline unsigned grid1(int64_t n) {
+  int64_t b = (n + QT - 1) / QT;
+  if (b < 1) b = 1;
+  if (b > 2048) b = 2048;
+  return (unsigned)b;
+}
+
+}  // namespace
+
+extern "C" int64_t ptn_zqr_work_bytes(int64_t m, int64_t k) {
+  return 16 * (3 * k + (nrb_for(m) + 1) / 2 + 1 + nrb_for(m) * k) + 256;
+}
+
+extern "C" int ptn_zqr_keep(void* Av, const int64_t* rowoff, int64_t m, int64_t k, int64_t cs, void* Rv,
+                            void* work, void* stream) {
+  if (!Av || !rowoff || !Rv || !work || m < 1 || k < 1 || cs < 1) return PTN_ERR_ARG;
+  cudaStream_t s = ptn_stream(stream);
+  double2* A = static_cast<double2*>(Av);
+  double2* R = static_cast<double2*>(Rv);
+  QRWork q = carve(work, m, k);
+  const int64_t p = m < k ? m : k;
+  // factorisation
+  for (int64_t j = 0; j < p; ++j) {
+    const int64_t below = m - (j + 1);
+    const int nb_norm = below > 0 ? (int)((below + RB - 1) / RB) : 0;
+    if (nb_norm > 0) { PTN_COUNT(1); colnorm_kernel<<<nb_norm, QT, 0, s>>>(A, rowoff, cs, m, j, q.npart); }
+    PTN_COUNT(1);
+    reflector_kernel<<<1, 32, 0, s>>>(A, rowoff, cs, j, q.npart, nb_norm, q.tau, q.scal);
+    const int64_t ncols = k - (j + 1);
+    if (ncols > 0) {
+      const int nrb = (int)((m - j + RB - 1) / RB);
+      dim3 g(nrb, (unsigned)((ncols + CB - 1) / CB));
+      PTN_COUNT(1);
+      dots_kernel<<<g, QT, 0, s>>>(A, rowoff, cs, m, k, j, j + 1, q.scal, 0, q.dpart);
+      PTN_COUNT(1);
+      dots_finish_kernel<<<(unsigned)ncols, 32, 0, s>>>(q.dpart, nrb, k, j + 1, q.w);
+      PTN_COUNT(1);
+      update_kernel<<<g, QT, 0, s>>>(A, rowoff, cs, m, k, j, j + 1, q.tau, q.scal, q.w, 0, 1);
+    }
+    if (below > 0) { PTN_COUNT(1); store_v_kernel<<<grid1(below), QT, 0, s>>>(A, rowoff, cs, m, j, q.scal); }
+  }
+  PTN_COUNT(1);
+  extract_r_kernel<<<grid1(k * k), QT, 0, s>>>(A, rowoff, cs, k, p, R);
+  // Q formation (zung2r): columns p-1 .. 0
+  for (int64_t j = p - 1; j >= 0; --j) {
+    const int64_t ncols = p - (j + 1);
+    if (ncols > 0) {
+      const int nrb = (int)((m - j + RB - 1) / RB);
+      dim3 g(nrb, (unsigned)((ncols + CB - 1) / CB));
+      PTN_COUNT(1);
+      dots_kernel<<<g, QT, 0, s>>>(A, rowoff, cs, m, p, j, j + 1, q.scal, 1, q.dpart);
+      PTN_COUNT(1);
+      dots_finish_kernel<<<(unsigned)ncols, 32, 0, s>>>(q.dpart, nrb, p, j + 1, q.w);
+      PTN_COUNT(1);
+      update_kernel<<<g, QT, 0, s>>>(A, rowoff, cs, m, p, j, j + 1, q.tau, q.scal, q.w, 1, 0);
+    }
+    PTN_COUNT(1);
+    qcol_kernel<<<grid1(m), QT, 0, s>>>(A, rowoff, cs, m, j, q.tau);
+  }
+  if (p < k) { PTN_COUNT(1); zero_cols_kernel<<<grid1(m * (k - p)), QT, 0, s>>>(A, rowoff, cs, m, k, p); }
+  return ptn_launch_status();
+}

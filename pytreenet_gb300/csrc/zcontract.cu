@@ -1,0 +1,190 @@
+// Strided multi-mode complex128 tensor contraction (FP64 plain path).
+//
+// C[m, n] = alpha * sum_k opA(A)[m, k] opB(B)[k, n] + beta * C[m, n], where m, n
+// and k are each a group of up to PTN_MAX_MODES tensor legs addressed through
+// per-operand strides. Legs are never transposed in memory: the environment,
+// TTNO and site tensors of a tree node are contracted where they lie.
+//
+// GB300 FP64 issues about two DFMA per clock per SM, so this kernel is bound by
+// the FP64 pipe at modest tile sizes: 64 x 64 complex outputs per CTA, 256
+// threads with a 4 x 4 register tile each, K staged through shared memory in
+// steps of 8. Tile offsets of the M and N rows are decoded once per CTA; the K
+// offsets once per K step.
+#include "ptn_common.cuh"
+
+namespace {
+
+constexpr int BM = 64, BN = 64, BK = 8;
+
+struct ModeDev {
+  int n;
+  int64_t dim[PTN_MAX_MODES];
+  int64_t s0[PTN_MAX_MODES];
+  int64_t s1[PTN_MAX_MODES];
+};
+
+struct ContractArgs {
+  const double2* A;
+  const double2* B;
+  double2* C;
+  double2 alpha, beta;
+  int conj_a, conj_b;
+  int beta_zero;
+  int64_t M, N, K;
+  int64_t tiles_n;
+  ModeDev m, n, k;  // m: (A, C) strides; n: (B, C); k: (A, B)
+};
+
+__device__ __forceinline__ void decode(const ModeDev& md, int64_t idx, int64_t& o0, int64_t& o1) {
+  o0 = 0;
+  o1 = 0;
+  for (int d = md.n - 1; d >= 0; --d) {
+    int64_t dd = md.dim[d];
+    int64_t q = idx / dd;
+    int64_t r = idx - q * dd;
+    o0 += r * md.s0[d];
+    o1 += r * md.s1[d];
+    idx = q;
+  }
+}
+
+__global__ void __launch_bounds__(256) zcontract_kernel(const ContractArgs a) {
+  __shared__ double2 As[BK][BM];
+  __shared__ double2 Bs[BK][BN];
+  __shared__ int64_t offAm[BM], offCm[BM], offBn[BN], offCn[BN];
+  __shared__ int64_t offAk[BK], offBk[BK];
+
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int64_t tile = blockIdx.x;
+  const int64_t tm = tile / a.tiles_n;
+  const int64_t tn = tile - tm * a.tiles_n;
+  const int64_t m0 = tm * BM, n0 = tn * BN;
+
+  if (tid < BM) {
+    int64_t mi = m0 + tid;
+    int64_t oa = -1, oc = -1;
+    if (mi < a.M) decode(a.m, mi, oa, oc);
+    offAm[tid] = oa;
+    offCm[tid] = oc;
+  } else if (tid < BM + BN) {
+    int t = tid - BM;
+    int64_t ni = n0 + t;
+    int64_t ob = -1, oc = -1;
+    if (ni < a.N) decode(a.n, ni, ob, oc);
+    offBn[t] = ob;
+    offCn[t] = oc;
+  }
+
+  double2 acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = make_double2(0.0, 0.0);
+
+  for (int64_t k0 = 0; k0 < a.K; k0 += BK) {
+    __syncthreads();
+    if (tid < BK) {
+      int64_t ki = k0 + tid;
+      int64_t oa = -1, ob = -1;
+      if (ki < a.K) decode(a.k, ki, oa, ob);
+      offAk[tid] = oa;
+      offBk[tid] = ob;
+    }
+    __syncthreads();
+    // 512 elements of each tile, two per thread.
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      int e = tid + r * 256;
+      int kk = e / BM, mm = e - kk * BM;
+      double2 v = make_double2(0.0, 0.0);
+      if (offAk[kk] >= 0 && offAm[mm] >= 0) {
+        v = a.A[offAm[mm] + offAk[kk]];
+        if (a.conj_a) v.y = -v.y;
+      }
+      As[kk][mm] = v;
+      int nn = e - kk * BN;
+      double2 w = make_double2(0.0, 0.0);
+      if (offBk[kk] >= 0 && offBn[nn] >= 0) {
+        w = a.B[offBk[kk] + offBn[nn]];
+        if (a.conj_b) w.y = -w.y;
+      }
+      Bs[kk][nn] = w;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      double2 av[4], bv[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) av[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) bv[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = cfma(av[i], bv[j], acc[i][j]);
+    }
+  }
+
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    int mm = ty + 16 * i;
+    if (offCm[mm] < 0) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      int nn = tx + 16 * j;
+      if (offCn[nn] < 0) continue;
+      double2* p = a.C + offCm[mm] + offCn[nn];
+      double2 v = cmul(a.alpha, acc[i][j]);
+      if (!a.beta_zero) v = cfma(a.beta, *p, v);
+      *p = v;
+    }
+  }
+}
+
+int fill_modes(const ptn_modes& src, ModeDev& dst, int which, int64_t& total) {
+  // which: 0 -> (a, c) strides, 1 -> (b, c), 2 -> (a, b)
+  if (src.n < 0 || src.n > PTN_MAX_MODES) return PTN_ERR_ARG;
+  dst.n = src.n;
+  total = 1;
+  for (int i = 0; i < src.n; ++i) {
+    if (src.dim[i] <= 0) return PTN_ERR_ARG;
+    dst.dim[i] = src.dim[i];
+    total *= src.dim[i];
+    switch (which) {
+      case 0: dst.s0[i] = src.stride_a[i]; dst.s1[i] = src.stride_c[i]; break;
+      case 1: dst.s0[i] = src.stride_b[i]; dst.s1[i] = src.stride_c[i]; break;
+      default: dst.s0[i] = src.stride_a[i]; dst.s1[i] = src.stride_b[i]; break;
+    }
+  }
+  return PTN_OK;
+}
+
+}  // namespace
+
+extern "C" int ptn_zcontract(const ptn_contract_desc* d, void* stream) {
+  if (!d || !d->A || !d->B || !d->C) return PTN_ERR_ARG;
+  ContractArgs a;
+  int64_t M, N, K;
+  if (fill_modes(d->m, a.m, 0, M) || fill_modes(d->n, a.n, 1, N) || fill_modes(d->k, a.k, 2, K))
+    return PTN_ERR_ARG;
+  a.A = static_cast<const double2*>(d->A);
+  a.B = static_cast<const double2*>(d->B);
+  a.C = static_cast<double2*>(d->C);
+  a.alpha = make_double2(d->alpha_re, d->alpha_im);
+  a.beta = make_double2(d->beta_re, d->beta_im);
+  a.beta_zero = (d->beta_re == 0.0 && d->beta_im == 0.0);
+  a.conj_a = d->conj_a;
+  a.conj_b = d->conj_b;
+  a.M = M;
+  a.N = N;
+  a.K = K;
+  if (M == 0 || N == 0) return PTN_OK;
+  int64_t tm = (M + BM - 1) / BM, tn = (N + BN - 1) / BN;
+  a.tiles_n = tn;
+  int64_t tiles = tm * tn;
+  if (tiles > 0x7fffffffLL) return PTN_ERR_UNSUPPORTED;
+  PTN_COUNT(1);
+  zcontract_kernel<<<(unsigned)tiles, 256, 0, ptn_stream(stream)>>>(a);
+  return ptn_launch_status();
+}

@@ -1,0 +1,626 @@
+"""GPU engine: device-resident TTNS/TTNO/environment data and the local-update kernels.
+
+Everything numerical runs in libptn_gb300 (hand-written CUDA for sm_103a); this
+module only plans the calls. PyTorch provides device memory and the stream.
+
+Data layout in HBM
+------------------
+* site tensor of node v: complex128, contiguous, legs (parent, children in
+  attachment order, physical) -- one buffer per node, updated in place;
+* TTNO tensor of node v: legs (parent, children, out, in), same neighbour order;
+* environment E(u -> v) for every directed edge: (ket, ham, bra) =
+  (chi_uv, w_uv, chi_uv), one persistent buffer per directed edge;
+* workspace slots: contraction intermediates and Krylov basis, grown on demand
+  and shared by all plans (one stream, so no two plans run at once).
+
+A contraction step is ``ptn_zcontract``: tensordot semantics, but the legs are
+addressed through strides, so no tensor is ever transposed in memory.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import ContractDesc, MAX_MODES, check
+
+CDT = torch.complex128
+DEFAULT_DEVICE = "cuda"
+
+
+def _stream_ptr():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+# ----------------------------------------------------------------------------
+# workspace
+# ----------------------------------------------------------------------------
+class Workspace:
+    """Named device scratch buffers that only grow."""
+
+    def __init__(self, device):
+        self.device = device
+        self.bufs: dict[str, torch.Tensor] = {}
+
+    def get(self, name: str, numel: int, dtype=CDT) -> torch.Tensor:
+        b = self.bufs.get(name)
+        if b is None or b.numel() < numel or b.dtype != dtype:
+            b = torch.empty(max(numel, 1), dtype=dtype, device=self.device)
+            self.bufs[name] = b
+        return b[:numel]
+
+    def ptr(self, name: str) -> int:
+        return self.bufs[name].data_ptr()
+
+
+# ----------------------------------------------------------------------------
+# labelled operands and contraction steps
+# ----------------------------------------------------------------------------
+@dataclass
+class Operand:
+    """A tensor operand of a plan: how to find its pointer, and its legs."""
+    ref: tuple               # ("fixed", tensor) | ("in",) | ("out",) | ("ws", name)
+    labels: list
+    dims: list
+    strides: list
+
+    @staticmethod
+    def contiguous(ref, labels, dims):
+        strides = [0] * len(dims)
+        s = 1
+        for i in range(len(dims) - 1, -1, -1):
+            strides[i] = s
+            s *= dims[i]
+        return Operand(ref, list(labels), list(dims), strides)
+
+    def numel(self):
+        return int(np.prod(self.dims)) if self.dims else 1
+
+    def permuted_to(self, order):
+        """Same memory, legs listed in ``order``."""
+        idx = [self.labels.index(x) for x in order]
+        return Operand(self.ref, list(order), [self.dims[i] for i in idx], [self.strides[i] for i in idx])
+
+
+def _merge_modes(dims, sa, sb):
+    """Merge adjacent modes that are contiguous in both operands."""
+    od, oa, ob = [], [], []
+    for d, a, b in zip(dims, sa, sb):
+        if d == 1:
+            continue
+        if od and oa[-1] == a * d and ob[-1] == b * d:
+            od[-1] *= d
+            oa[-1] = a
+            ob[-1] = b
+        else:
+            od.append(d)
+            oa.append(a)
+            ob.append(b)
+    return od, oa, ob
+
+
+def _fill(modes, dims, s_first, s_second, which):
+    dims, s1, s2 = _merge_modes(dims, s_first, s_second)
+    if len(dims) > MAX_MODES:
+        raise ValueError(f"contraction needs {len(dims)} modes in one group (max {MAX_MODES})")
+    modes.n = len(dims)
+    for i, (d, a, b) in enumerate(zip(dims, s1, s2)):
+        modes.dim[i] = d
+        if which == "m":
+            modes.stride_a[i], modes.stride_c[i] = a, b
+        elif which == "n":
+            modes.stride_b[i], modes.stride_c[i] = a, b
+        else:
+            modes.stride_a[i], modes.stride_b[i] = a, b
+
+
+class Step:
+    """One ptn_zcontract call with prebuilt strides; pointers resolved at run time."""
+
+    __slots__ = ("desc", "refs", "flops")
+
+    def __init__(self, A: Operand, B: Operand, klabels, C: Operand, conj_a=False, conj_b=False,
+                 alpha=1.0, beta=0.0):
+        d = ContractDesc()
+        mlab = [l for l in A.labels if l not in klabels]
+        nlab = [l for l in B.labels if l not in klabels]
+        if sorted(C.labels) != sorted(mlab + nlab):
+            raise ValueError(f"output legs {C.labels} do not match {mlab + nlab}")
+
+        def col(op, labs, what):
+            return [getattr(op, what)[op.labels.index(l)] for l in labs]
+        for l in klabels:
+            if A.dims[A.labels.index(l)] != B.dims[B.labels.index(l)]:
+                raise ValueError(f"dimension mismatch on leg {l}")
+        _fill(d.m, col(A, mlab, "dims"), col(A, mlab, "strides"), col(C, mlab, "strides"), "m")
+        _fill(d.n, col(B, nlab, "dims"), col(B, nlab, "strides"), col(C, nlab, "strides"), "n")
+        _fill(d.k, col(A, klabels, "dims"), col(A, klabels, "strides"), col(B, klabels, "strides"), "k")
+        d.alpha_re, d.alpha_im = float(np.real(alpha)), float(np.imag(alpha))
+        d.beta_re, d.beta_im = float(np.real(beta)), float(np.imag(beta))
+        d.conj_a, d.conj_b = int(conj_a), int(conj_b)
+        self.desc = d
+        self.refs = (A.ref, B.ref, C.ref)
+        self.flops = 8 * int(np.prod(col(A, mlab, "dims") or [1])) * \
+            int(np.prod(col(B, nlab, "dims") or [1])) * int(np.prod(col(A, klabels, "dims") or [1]))
+
+
+class Plan:
+    """A sequence of contraction steps with one dynamic input and output."""
+
+    def __init__(self, ws: Workspace, steps, ws_sizes):
+        self.ws = ws
+        self.steps = steps
+        self.ws_sizes = ws_sizes  # name -> numel
+        self.flops = sum(s.flops for s in steps)
+
+    def run(self, x_ptr: int = 0, y_ptr: int = 0):
+        lib = _lib.load()
+        for name, n in self.ws_sizes.items():
+            self.ws.get(name, n)
+        stream = _stream_ptr()
+        for st in self.steps:
+            ptrs = []
+            for ref in st.refs:
+                kind = ref[0]
+                if kind == "fixed":
+                    ptrs.append(ref[1].data_ptr())
+                elif kind == "in":
+                    ptrs.append(x_ptr)
+                elif kind == "out":
+                    ptrs.append(y_ptr)
+                else:
+                    ptrs.append(self.ws.ptr(ref[1]))
+            st.desc.A, st.desc.B, st.desc.C = ptrs
+            check(lib.ptn_zcontract(ctypes.byref(st.desc), stream), "ptn_zcontract")
+
+
+class ChainBuilder:
+    """Builds a Plan from tensordot-style steps on labelled operands."""
+
+    def __init__(self, ws: Workspace):
+        self.ws = ws
+        self.steps = []
+        self.sizes = {}
+        self.slot = 0
+
+    def contract(self, A: Operand, B: Operand, klabels, out: Operand | None = None, **kw) -> Operand:
+        if out is None:
+            mlab = [l for l in A.labels if l not in klabels]
+            nlab = [l for l in B.labels if l not in klabels]
+            dims = [A.dims[A.labels.index(l)] for l in mlab] + [B.dims[B.labels.index(l)] for l in nlab]
+            name = f"chain{self.slot % 2}"
+            self.slot += 1
+            out = Operand.contiguous(("ws", name), mlab + nlab, dims)
+            self.sizes[name] = max(self.sizes.get(name, 0), out.numel())
+        self.steps.append(Step(A, B, klabels, out, **kw))
+        return out
+
+    def plan(self) -> Plan:
+        return Plan(self.ws, self.steps, self.sizes)
+
+
+# ----------------------------------------------------------------------------
+# Krylov exponential (krylov_exp_action, time_evolution/time_evolution.py:721-821)
+# ----------------------------------------------------------------------------
+def small_propagator(T, dt, exp_factor, hermitian=True):
+    """First column of exp(exp_factor dt T) for the m x m projection
+    (``_krylov_small_propagator``, ``time_evolution/time_evolution.py:696-718``)."""
+    if hermitian:
+        H = 0.5 * (T + T.conj().T)
+        ev, V = np.linalg.eigh(H)
+        return V @ (np.exp(exp_factor * dt * ev) * V[0].conj())
+    import scipy.linalg
+    return scipy.linalg.expm(exp_factor * dt * T)[:, 0]
+
+
+class KrylovSolver:
+    """Matrix-free Arnoldi/Lanczos exponential on the device.
+
+    Two Gram-Schmidt passes per step (classical, each a multi-dot + multi-axpy
+    kernel pair; the reference does the same projections one vector at a time).
+    The adaptive stop, the happy-breakdown floors and the symmetrised ``eigh``
+    propagator follow the reference; the m x m projection is tiny and is
+    diagonalised on the host after each step.
+    """
+
+    def __init__(self, ws: Workspace):
+        self.ws = ws
+        self.depths: list[int] = []
+
+    def expm(self, x: torch.Tensor, apply, dt: float, exp_factor: complex, krylov_tol=1e-10,
+             max_krylov_dim=None, hermitian=True, out: torch.Tensor | None = None) -> torch.Tensor:
+        lib = _lib.load()
+        stream = _stream_ptr()
+        n = x.numel()
+        out = x if out is None else out
+        part = self.ws.get("kry_part", int(lib.ptn_krylov_partials(n)) + 8)
+        scal = self.ws.get("kry_scal", 8, torch.float64)
+        check(lib.ptn_dznrm2(x.data_ptr(), n, scal.data_ptr(), part.data_ptr(), stream), "dznrm2")
+        beta0 = float(scal[0].item())
+        if beta0 == 0.0:
+            if out.data_ptr() != x.data_ptr():
+                out.copy_(x)
+            return out
+        max_steps = n if max_krylov_dim is None else min(n, int(max_krylov_dim))
+        floor_abs = np.finfo(float).eps * max(n, 1)
+        cap = min(max_steps + 1, 8)
+        Q = self.ws.get("kry_Q", cap * n).view(cap, n)
+        w = self.ws.get("kry_w", n)
+        check(lib.ptn_zscal_inv(x.data_ptr(), scal.data_ptr(), Q[0].data_ptr(), n, stream), "zscal")
+        T = np.zeros((min(max_steps, 64) + 1,) * 2, dtype=complex)
+        m = 0
+        for j in range(max_steps):
+            if j + 2 > T.shape[0]:
+                T2 = np.zeros((2 * T.shape[0],) * 2, dtype=complex)
+                T2[:T.shape[0], :T.shape[0]] = T
+                T = T2
+            apply(Q[j].data_ptr(), w.data_ptr())
+            nq = j + 1
+            hbuf = self.ws.get("kry_h", 2 * nq + 8)
+            check(lib.ptn_dznrm2(w.data_ptr(), n, scal.data_ptr(), part.data_ptr(), stream), "dznrm2")
+            h1 = hbuf[0:nq]
+            h2 = hbuf[nq:2 * nq]
+            for h in (h1, h2):
+                check(lib.ptn_zdot_multi(Q.data_ptr(), n, nq, w.data_ptr(), n, h.data_ptr(), 0,
+                                         part.data_ptr(), stream), "zdot_multi")
+                check(lib.ptn_zaxpy_multi(Q.data_ptr(), n, nq, h.data_ptr(), w.data_ptr(), n, stream),
+                      "zaxpy_multi")
+            check(lib.ptn_dznrm2(w.data_ptr(), n, scal[1:].data_ptr(), part.data_ptr(), stream), "dznrm2")
+            hh = hbuf[:2 * nq].cpu().numpy()
+            sc = scal[:2].cpu().numpy()
+            w0, beta = float(sc[0]), float(sc[1])
+            T[:nq, j] = hh[:nq] + hh[nq:]
+            T[j + 1, j] = beta
+            m = j + 1
+            if not np.isfinite(beta):
+                raise _lib.PtnError(3, "Krylov exponential: non-finite vector")
+            if beta <= max(floor_abs, 1e-12 * w0):
+                break
+            if krylov_tol > 0.0:
+                col = small_propagator(T[:m, :m], dt, exp_factor, hermitian)
+                if beta0 * beta * abs(col[m - 1]) < krylov_tol:
+                    break
+            if j + 1 >= Q.shape[0]:
+                newcap = min(max_steps + 1, 2 * Q.shape[0])
+                Qn = torch.empty((newcap, n), dtype=CDT, device=x.device)
+                Qn[:Q.shape[0]].copy_(Q)
+                self.ws.bufs["kry_Q"] = Qn.view(-1)
+                Q = Qn
+            check(lib.ptn_zscal_inv(w.data_ptr(), scal[1:].data_ptr(), Q[j + 1].data_ptr(), n, stream),
+                  "zscal")
+        self.depths.append(m)
+        c = beta0 * small_propagator(T[:m, :m], dt, exp_factor, hermitian)
+        cdev = self.ws.get("kry_h", m + 8)[:m]
+        cdev.copy_(torch.from_numpy(np.ascontiguousarray(c)).to(x.device))
+        for i0 in range(0, m, 64):
+            cnt = min(64, m - i0)
+            if i0 == 0:
+                check(lib.ptn_zcombine(Q.data_ptr(), n, cnt, cdev.data_ptr(), out.data_ptr(), n, stream),
+                      "zcombine")
+            else:
+                tmp = self.ws.get("kry_tmp", n)
+                check(lib.ptn_zcombine(Q[i0:].data_ptr(), n, cnt, cdev[i0:].data_ptr(), tmp.data_ptr(), n,
+                                       stream), "zcombine")
+                out.view(-1).add_(tmp)
+        return out
+
+
+# ----------------------------------------------------------------------------
+# device network
+# ----------------------------------------------------------------------------
+class DeviceNetwork:
+    """Device copy of a TTNS (+ TTNO) with environment buffers and cached plans."""
+
+    def __init__(self, state, hamiltonian=None, device=None):
+        _lib.load()
+        if not torch.cuda.is_available():
+            raise RuntimeError("pytreenet_gb300 needs a CUDA device (no CPU fallback)")
+        self.device = torch.device(device or DEFAULT_DEVICE)
+        self.state = state
+        self.ham = hamiltonian
+        self.ws = Workspace(self.device)
+        self.krylov = KrylovSolver(self.ws)
+        state._finalise()
+        self.t = {}
+        for nid in state._order:
+            t = state._phys[nid]
+            if isinstance(t, np.ndarray):
+                t = torch.from_numpy(np.ascontiguousarray(t, dtype=np.complex128))
+            t = t.to(self.device, CDT).contiguous()
+            self.t[nid] = t
+            state._phys[nid] = t
+        self.W = {}
+        if hamiltonian is not None:
+            hamiltonian._finalise()
+            for nid in state._order:
+                Wn = hamiltonian.phys(nid)
+                # TTNO legs are matched to the state's physical neighbour order
+                hn = hamiltonian.nodes[nid]
+                order = state.nodes[nid].phys_neighbours()
+                hax = [hn.phys_neighbours().index(x) for x in order]
+                Wn = np.asarray(Wn.detach().cpu().numpy() if isinstance(Wn, torch.Tensor) else Wn)
+                Wn = np.transpose(Wn, hax + [Wn.ndim - 2, Wn.ndim - 1])
+                self.W[nid] = torch.from_numpy(np.ascontiguousarray(Wn, dtype=np.complex128)).to(self.device)
+        self.env: dict[tuple, torch.Tensor] = {}
+        self.plans: dict = {}
+        self.rowoff: dict = {}
+        self.flops = 0
+
+    # -- shapes ------------------------------------------------------------------
+    def nbrs(self, nid):
+        return self.state.nodes[nid].phys_neighbours()
+
+    def shape(self, nid):
+        return list(self.t[nid].shape)
+
+    def env_buf(self, u, v):
+        key = (u, v)
+        if key not in self.env:
+            chi = self.t[u].shape[self.state.phys_axis(u, v)]
+            w = self.W[u].shape[self.state.phys_axis(u, v)]
+            self.env[key] = torch.zeros((chi, w, chi), dtype=CDT, device=self.device)
+        return self.env[key]
+
+    def _env_op(self, u, v, labels):
+        return Operand.contiguous(("fixed", self.env_buf(u, v)), labels, list(self.env_buf(u, v).shape))
+
+    # -- site chain (shared by the matvec and the environment update) -------------
+    def _site_chain(self, cb: ChainBuilder, x: Operand, nid: str, open_k=None) -> Operand:
+        """Environments of the first half of the neighbours, then W, then the
+        rest. Cost chi^{n+1} d (S(h) + S(n-h)) + chi^n d^2 w^n complex MAC;
+        the reference contracts every environment before W (w^n larger)."""
+        nb = self.nbrs(nid)
+        n = len(nb)
+        ks = [k for k in range(n) if k != open_k]
+        half = len(ks) // 2
+        T = x
+        for k in ks[:half]:
+            T = cb.contract(T, self._env_op(nb[k], nid, [f"a{k}", f"b{k}", f"c{k}"]), [f"a{k}"])
+        Wop = Operand.contiguous(("fixed", self.W[nid]), [f"b{k}" for k in range(n)] + ["t", "s"],
+                                 list(self.W[nid].shape))
+        T = cb.contract(T, Wop, [f"b{k}" for k in ks[:half]] + ["s"])
+        return T, ks[half:], nb
+
+    def heff_plan(self, nid) -> Plan:
+        """y = H_eff x (``contract_ket_ham_with_envs``,
+        ``contractions/state_operator_contraction.py:227-273``)."""
+        key = ("heff", nid)
+        if key in self.plans:
+            return self.plans[key]
+        cb = ChainBuilder(self.ws)
+        shape = self.shape(nid)
+        n = len(shape) - 1
+        x = Operand.contiguous(("in",), [f"a{k}" for k in range(n)] + ["s"], shape)
+        y = Operand.contiguous(("out",), [f"c{k}" for k in range(n)] + ["t"], shape)
+        T, rest, nb = self._site_chain(cb, x, nid)
+        for i, k in enumerate(rest):
+            E = self._env_op(nb[k], nid, [f"a{k}", f"b{k}", f"c{k}"])
+            if i == len(rest) - 1:
+                cb.contract(T, E, [f"a{k}", f"b{k}"], out=y)
+            else:
+                T = cb.contract(T, E, [f"a{k}", f"b{k}"])
+        if not rest:
+            # leafless case cannot happen for n >= 1; W was the last step
+            raise RuntimeError("site without neighbours")
+        p = cb.plan()
+        self.plans[key] = p
+        return p
+
+    def env_plan(self, nid, nxt) -> Plan:
+        """E(nid -> nxt) (``contract_any``, ``contractions/state_operator_contraction.py:407-694``)."""
+        key = ("env", nid, nxt)
+        if key in self.plans:
+            return self.plans[key]
+        cb = ChainBuilder(self.ws)
+        shape = self.shape(nid)
+        n = len(shape) - 1
+        nb = self.nbrs(nid)
+        k0 = nb.index(nxt)
+        A = Operand.contiguous(("fixed", self.t[nid]), [f"a{k}" for k in range(n)] + ["s"], shape)
+        T, rest, _ = self._site_chain(cb, A, nid, open_k=k0)
+        for k in rest:
+            T = cb.contract(T, self._env_op(nb[k], nid, [f"a{k}", f"b{k}", f"c{k}"]), [f"a{k}", f"b{k}"])
+        B = Operand.contiguous(("fixed", self.t[nid]),
+                               [f"c{k}" if k != k0 else "z" for k in range(n)] + ["t"], shape)
+        E = self._env_op(nid, nxt, [f"a{k0}", f"b{k0}", "z"])
+        cb.contract(T, B, [f"c{k}" for k in range(n) if k != k0] + ["t"], out=E, conj_b=True)
+        p = cb.plan()
+        self.plans[key] = p
+        return p
+
+    def bond_plan(self, nid, nxt) -> Plan:
+        """Bond matvec on R (legs: nid side, nxt side) (``contract_bond_tensor``,
+        ``contractions/state_operator_contraction.py:984-1040``)."""
+        key = ("bond", nid, nxt)
+        if key in self.plans:
+            return self.plans[key]
+        cb = ChainBuilder(self.ws)
+        eq = self._env_op(nid, nxt, ["a", "b", "x"])
+        en = self._env_op(nxt, nid, ["c", "b", "y"])
+        chi_q, chi_n = eq.dims[0], en.dims[0]
+        r = Operand.contiguous(("in",), ["a", "c"], [chi_q, chi_n])
+        y = Operand.contiguous(("out",), ["x", "y"], [chi_q, chi_n])
+        T = cb.contract(eq, r, ["a"])
+        cb.contract(T, en, ["c", "b"], out=y)
+        p = cb.plan()
+        self.plans[key] = p
+        return p
+
+    # -- environment cache --------------------------------------------------------
+    def update_env(self, nid, nxt):
+        p = self.env_plan(nid, nxt)
+        p.run()
+        self.flops += p.flops
+
+    def init_cache_but_one(self, left_out):
+        """All environments pointing toward ``left_out``
+        (``SandwichCache.init_cache_but_one``, ``contractions/sandwich_caching.py:97-126``)."""
+        def rec(nid, toward):
+            for nb in self.nbrs(nid):
+                if nb != toward:
+                    rec(nb, nid)
+            if toward is not None:
+                self.update_env(nid, toward)
+        rec(left_out, None)
+
+    # -- local evolutions ------------------------------------------------------------
+    def evolve_site(self, nid, dt, exp_factor, tol, maxdim):
+        p = self.heff_plan(nid)
+
+        def apply(xp, yp):
+            p.run(xp, yp)
+            self.flops += p.flops
+        x = self.t[nid]
+        self.krylov.expm(x, apply, dt, exp_factor, tol, maxdim, out=x)
+
+    def evolve_bond(self, r: torch.Tensor, nid, nxt, dt, exp_factor, tol, maxdim):
+        p = self.bond_plan(nid, nxt)
+
+        def apply(xp, yp):
+            p.run(xp, yp)
+            self.flops += p.flops
+        return self.krylov.expm(r, apply, dt, exp_factor, tol, maxdim, out=r)
+
+    # -- QR split and R absorption ---------------------------------------------------
+    def qr_split(self, nid, nbr) -> torch.Tensor:
+        """tensor[nid] <- Q (KEEP), returns R (k x k; legs: new bond, nbr-side bond).
+        Rows in the reference's logical order (``util/tensor_splitting.py:60-107``)."""
+        st = self.state
+        node = st.nodes[nid]
+        if node.parent == nbr:
+            row_nbrs = list(node.children)
+        else:
+            row_nbrs = ([node.parent] if node.parent is not None else []) + \
+                [c for c in node.children if c != nbr]
+        shape = self.shape(nid)
+        row_axes = [st.phys_axis(nid, x) for x in row_nbrs] + [len(shape) - 1]
+        col_axis = st.phys_axis(nid, nbr)
+        key = (tuple(shape), tuple(row_axes), col_axis)
+        strides = self.t[nid].stride()
+        if key not in self.rowoff:
+            idx = np.zeros(1, dtype=np.int64)
+            for ax in row_axes:
+                idx = (idx[:, None] + np.arange(shape[ax], dtype=np.int64)[None, :] * strides[ax]).reshape(-1)
+            self.rowoff[key] = torch.from_numpy(idx).to(self.device)
+        rowoff = self.rowoff[key]
+        m = rowoff.numel()
+        k = shape[col_axis]
+        lib = _lib.load()
+        R = self.ws.get(f"qr_R", k * k).view(k, k)
+        work = self.ws.get("qr_work", (int(lib.ptn_zqr_work_bytes(m, k)) + 15) // 16)
+        check(lib.ptn_zqr_keep(self.t[nid].data_ptr(), rowoff.data_ptr(), m, k, strides[col_axis],
+                               R.data_ptr(), work.data_ptr(), _stream_ptr()), "ptn_zqr_keep")
+        if node.parent != nbr:
+            node.children = [nbr] + [c for c in node.children if c != nbr]
+        self.flops += 8 * 2 * m * k * k
+        return R
+
+    def absorb(self, R: torch.Tensor, src, dst, link_variant: bool):
+        """dst[..., new, ...] = sum_a R[new, a] dst[..., a, ...] on dst's leg toward src.
+        Logical order as in ``contract_nodes`` (``contractions/node_contraction.py:88-138``)."""
+        st = self.state
+        shape = self.shape(dst)
+        n = len(shape) - 1
+        ax = st.phys_axis(dst, src)
+        key = ("absorb", dst, src)
+        if key not in self.plans:
+            cb = ChainBuilder(self.ws)
+            Rop = Operand.contiguous(("in",), ["new", f"a{ax}"], [shape[ax], shape[ax]])
+            T = Operand.contiguous(("fixed", self.t[dst]), [f"a{k}" for k in range(n)] + ["s"], shape)
+            labels = [f"a{k}" if k != ax else "new" for k in range(n)] + ["s"]
+            out = Operand.contiguous(("ws", "absorb"), labels, shape)
+            cb.sizes["absorb"] = out.numel()
+            cb.contract(Rop, T, [f"a{ax}"], out=out)
+            self.plans[key] = cb.plan()
+        p = self.plans[key]
+        p.run(R.data_ptr(), 0)
+        self.t[dst].view(-1).copy_(self.ws.bufs["absorb"][:self.t[dst].numel()])
+        self.flops += p.flops
+        node = st.nodes[src]
+        if node.parent == dst:
+            dn = st.nodes[dst]
+            others = [c for c in dn.children if c != src]
+            dn.children = ([src] + others) if link_variant else (others + [src])
+
+    def move_orth_one_hop(self, a, b):
+        R = self.qr_split(a, b)
+        self.absorb(R, a, b, link_variant=False)
+
+    def move_orth_center(self, new_center):
+        st = self.state
+        if st.orthogonality_center_id is None:
+            raise AssertionError("The TTN is not in canonical form, so the orth. center cannot be moved!")
+        path = st.path_from_to(st.orthogonality_center_id, new_center)
+        for a, b in zip(path[:-1], path[1:]):
+            self.move_orth_one_hop(a, b)
+        st.orthogonality_center_id = new_center
+
+    def normalise_center(self) -> float:
+        """Divide the orthogonality centre by its norm (``TTNS.normalise``,
+        ``ttns/ttns.py:105-125``); returns the old norm."""
+        c = self.state.orthogonality_center_id
+        lib = _lib.load()
+        t = self.t[c]
+        part = self.ws.get("kry_part", int(lib.ptn_krylov_partials(t.numel())) + 8)
+        scal = self.ws.get("kry_scal", 8, torch.float64)
+        check(lib.ptn_dznrm2(t.data_ptr(), t.numel(), scal.data_ptr(), part.data_ptr(), _stream_ptr()), "dznrm2")
+        check(lib.ptn_zscal_inv(t.data_ptr(), scal.data_ptr(), t.data_ptr(), t.numel(), _stream_ptr()), "zscal")
+        return float(scal[0].item())
+
+    def canonical_form(self, center):
+        """``canonical_form`` (``core/canonical_form.py:162-208``)."""
+        st = self.state
+        dist = st.distance_to_node(center)
+        maxd = max(dist.values()) if dist else 0
+        for d in range(maxd, 0, -1):
+            for nid in [x for x in dist if dist[x] == d]:
+                target = min(st.nodes[nid].neighbouring_nodes(), key=lambda x: dist[x])
+                self.move_orth_one_hop(nid, target)
+        st.orthogonality_center_id = center
+
+    # -- observables ------------------------------------------------------------------
+    def expect_local(self, ops: dict) -> complex:
+        """<psi| prod_i O_i |psi> for single-site operators
+        (``TTNS.tensor_product_expectation_value``, ``ttns/ttns.py:240-264``)."""
+        st = self.state
+        cache = {}
+
+        def rec(nid, toward):
+            shape = self.shape(nid)
+            n = len(shape) - 1
+            nb = self.nbrs(nid)
+            cb = ChainBuilder(self.ws)
+            base = Operand.contiguous(("fixed", self.t[nid]), [f"a{k}" for k in range(n)] + ["s"], shape)
+            T = base
+            if nid in ops:
+                O = torch.as_tensor(np.asarray(ops[nid], dtype=np.complex128)).to(self.device)
+                cache[("op", nid)] = O
+                T = cb.contract(T, Operand.contiguous(("fixed", O), ["t", "s"], list(O.shape)), ["s"])
+                T = Operand(T.ref, [l if l != "t" else "s" for l in T.labels], T.dims, T.strides)
+            subs = []
+            for k, x in enumerate(nb):
+                if x == toward:
+                    continue
+                sub = rec(x, nid)
+                subs.append(sub)
+                T = cb.contract(T, Operand.contiguous(("fixed", sub), [f"a{k}", f"c{k}"], list(sub.shape)),
+                                [f"a{k}"])
+            B = Operand.contiguous(("fixed", self.t[nid]),
+                                   [f"c{k}" if nb[k] != toward else "z" for k in range(n)] + ["s"], shape)
+            if toward is None:
+                res = torch.zeros((1,), dtype=CDT, device=self.device)
+                outop = Operand(("fixed", res), [], [], [])
+                cb.contract(T, B, [f"c{k}" for k in range(n)] + ["s"], out=outop, conj_b=True)
+            else:
+                k0 = nb.index(toward)
+                chi = shape[k0]
+                res = torch.zeros((chi, chi), dtype=CDT, device=self.device)
+                outop = Operand.contiguous(("fixed", res), [f"a{k0}", "z"], [chi, chi])
+                cb.contract(T, B, [f"c{k}" for k in range(n) if k != k0] + ["s"], out=outop, conj_b=True)
+            cb.plan().run()
+            return res
+        r = rec(st.root_id, None)
+        return complex(r.cpu().numpy()[0])

@@ -1,0 +1,285 @@
+"""One-site TDVP drivers running on the GB300 engine.
+
+Public surface mirrors PyTreeNet's drivers
+(``time_evolution/tdvp_algorithms/*.py``): the constructor
+``(initial_state, hamiltonian, time_step_size, final_time, operators,
+config=None, solver_options=None)``, ``run_one_time_step()``, ``run()``,
+``update_path``, ``orthogonalization_path``, ``state`` and ``results``.
+"""
+from __future__ import annotations
+
+import copy
+from dataclasses import dataclass, field
+from enum import Enum
+from typing import Any
+
+import numpy as np
+
+from .engine import DeviceNetwork
+from .ttn import TreeTensorNetworkOperator, TreeTensorNetworkState
+
+
+class TimeEvoMode(Enum):
+    """Local exponential method (``time_evolution/time_evolution.py:431-655``).
+
+    Only KRYLOV (matrix-free Lanczos, the GPU path) is executed by this engine.
+    FASTEST maps to the dense CHEBYSHEV path in the reference, which builds the
+    N x N effective Hamiltonian; it is not ported."""
+    FASTEST = "fastest"
+    EXPM = "expm"
+    CHEBYSHEV = "chebyshev"
+    SPARSE = "sparse"
+    RK45 = "RK45"
+    RK23 = "RK23"
+    DOP853 = "DOP853"
+    BDF = "BDF"
+    KRYLOV = "krylov"
+
+    @staticmethod
+    def default_solver_options(mode) -> dict:
+        if mode is TimeEvoMode.KRYLOV:
+            return {"krylov_tol": 1e-10}
+        if mode in (TimeEvoMode.RK45, TimeEvoMode.RK23, TimeEvoMode.DOP853, TimeEvoMode.BDF):
+            return {"atol": 1e-10, "rtol": 1e-10}
+        return {}
+
+    @staticmethod
+    def valid_solver_options(mode) -> set:
+        if mode is TimeEvoMode.KRYLOV:
+            return {"krylov_tol", "max_krylov_dim", "hermitian", "exp_factor"}
+        return {"exp_factor"}
+
+
+class EvoDirection(Enum):
+    """``time_evolution/time_evolution.py:384-429``: FORWARD = exp(-i H t)."""
+    FORWARD = -1
+    BACKWARD = 1
+
+    def exp_factor(self) -> complex:
+        return 1.0j * self.value
+
+
+class PathFinderMode(Enum):
+    LeafToLeaf = "LeafToLeaf"
+    LeafToRoot = "LeafToRoot"
+
+
+@dataclass
+class TTNTimeEvolutionConfig:
+    record_bond_dim: bool = False
+    record_max_bdim: bool = False
+    record_average_bdim: bool = False
+    record_total_size: bool = False
+    record_norm: bool = False
+    record_loschmidt_amplitude: bool = False
+    time_dep: bool = False
+
+
+@dataclass
+class TDVPConfig(TTNTimeEvolutionConfig):
+    """``tdvp_algorithms/tdvp_algorithm.py:23-34``."""
+    time_evo_mode: TimeEvoMode = TimeEvoMode.FASTEST
+    main_path_mode: PathFinderMode = PathFinderMode.LeafToRoot
+
+
+def _postorder(ttn, nid):
+    node = ttn.nodes[nid]
+    if node.is_leaf():
+        return [nid]
+    out = []
+    for c in node.children:
+        out += _postorder(ttn, c)
+    return out + [nid]
+
+
+def leaf_to_root_update_path(ttn) -> list[str]:
+    """``TDVPUpdatePathFinder_LeafToRoot.find_path``
+    (``time_evolution/time_evo_util/update_path.py:63-254``)."""
+    root = ttn.root_id
+    dist = ttn.distance_to_node(root)
+    start = max(dist, key=dist.get)
+    main = ttn.find_path_to_root(start)
+    path = []
+    for origin in main:
+        if origin != root:
+            path += [x for c in ttn.nodes[origin].children if c not in main
+                     for x in _postorder(ttn, c)] + [origin]
+            continue
+        if len(ttn.nodes[root].children) == 1:
+            path += [root]
+            continue
+        leaves = [x for x in ttn.get_leaves() if x not in path]
+        ld = {x: d for x, d in dist.items() if x in leaves}
+        if not ld:
+            raise AssertionError("no unvisited leaf left")
+        last = max(ld, key=ld.get)
+        down = list(reversed(ttn.find_path_to_root(last)))
+        for o in down:
+            if o == root:
+                excl = (main[-2], down[1])
+                path += [x for c in ttn.nodes[root].children if c not in excl
+                         for x in _postorder(ttn, c)] + [root]
+            else:
+                path += [x for c in ttn.nodes[o].children if c not in down
+                         for x in _postorder(ttn, c)] + [o]
+    return path
+
+
+class TensorProduct(dict):
+    """Single-site operators keyed by node id (``operators/tensorproduct.py:33``)."""
+
+
+class OneSiteTDVP:
+    """Common machinery of the one-site TDVP drivers
+    (``tdvp_algorithms/tdvp_algorithm.py:37-221``, ``onesitetdvp.py:17-134``)."""
+
+    config_class = TDVPConfig
+
+    def __init__(self, initial_state: TreeTensorNetworkState, hamiltonian: TreeTensorNetworkOperator,
+                 time_step_size: float, final_time: float, operators, config: TDVPConfig | None = None,
+                 solver_options: dict[str, Any] | None = None):
+        if len(initial_state.nodes) != len(hamiltonian.nodes):
+            raise AssertionError("state and Hamiltonian must have the same nodes")
+        if time_step_size <= 0 or final_time <= 0:
+            raise ValueError("time step and final time must be positive")
+        self.config = config if config is not None else self.config_class()
+        if self.config.time_evo_mode is not TimeEvoMode.KRYLOV:
+            raise NotImplementedError(
+                f"time_evo_mode={self.config.time_evo_mode}: the GPU engine runs the matrix-free "
+                "KRYLOV exponential only (the dense modes build the full effective Hamiltonian)")
+        opts = TimeEvoMode.default_solver_options(TimeEvoMode.KRYLOV)
+        opts.update(solver_options or {})
+        bad = set(opts) - TimeEvoMode.valid_solver_options(TimeEvoMode.KRYLOV)
+        if bad:
+            raise ValueError(f"solver options {sorted(bad)} are not valid for KRYLOV")
+        self.solver_options = opts
+        self.time_step_size = float(time_step_size)
+        self.final_time = float(final_time)
+        self.num_time_steps = int(np.ceil(final_time / time_step_size))
+        self.operators = operators if operators is not None else []
+        self.hamiltonian = hamiltonian
+        initial_state._finalise()
+        self._initial_state = initial_state.copy_structure()
+        self.state = initial_state.copy_structure()
+        self.update_path = leaf_to_root_update_path(self._initial_state)
+        self.orthogonalization_path = [self.state.path_from_to(self.update_path[i], self.update_path[i + 1])[1:]
+                                       for i in range(len(self.update_path) - 1)]
+        self.net = DeviceNetwork(self.state, hamiltonian)
+        if self.state.orthogonality_center_id is None:
+            self.net.canonical_form(self.update_path[0])
+        else:
+            self.net.move_orth_center(self.update_path[0])
+        self.net.init_cache_but_one(self.update_path[0])
+        self.results = None
+        self.times = []
+
+    # -- Krylov options ------------------------------------------------------------
+    def _kry(self):
+        o = self.solver_options
+        return o.get("krylov_tol", 1e-10), o.get("max_krylov_dim", None)
+
+    def _factor(self, forward: bool) -> complex:
+        override = self.solver_options.get("exp_factor")
+        if override is None:
+            return -1j if forward else 1j
+        return override if forward else -override
+
+    # -- building blocks --------------------------------------------------------------
+    def _update_site(self, node_id, time_step_factor=1.0):
+        tol, maxdim = self._kry()
+        self.net.evolve_site(node_id, self.time_step_size * time_step_factor, self._factor(True), tol, maxdim)
+
+    def _update_link(self, node_id, next_node_id, time_step_factor=1.0):
+        st = self.state
+        assert st.orthogonality_center_id == node_id
+        R = self.net.qr_split(node_id, next_node_id)
+        self.net.update_env(node_id, next_node_id)
+        tol, maxdim = self._kry()
+        self.net.evolve_bond(R, node_id, next_node_id, self.time_step_size * time_step_factor,
+                             self._factor(False), tol, maxdim)
+        self.net.absorb(R, node_id, next_node_id, link_variant=True)
+        st.orthogonality_center_id = next_node_id
+
+    def _move_orth_and_update_cache_for_path(self, path):
+        if len(path) == 0:
+            return
+        assert self.state.orthogonality_center_id == path[0]
+        for prev, nid in zip(path[:-1], path[1:]):
+            self.net.move_orth_center(nid)
+            self.net.update_env(prev, nid)
+
+    # -- observables -----------------------------------------------------------------
+    def evaluate_operator(self, operator) -> complex:
+        return self.net.expect_local(dict(operator))
+
+    def evaluate_operators(self):
+        ops = self.operators
+        if isinstance(ops, dict):
+            ops = list(ops.values())
+        elif isinstance(ops, TensorProduct):
+            ops = [ops]
+        return np.array([self.evaluate_operator(o) for o in ops])
+
+    def run(self, evaluation_time: int = 1, pgbar: bool = False):
+        """``TimeEvolution.run`` (``time_evolution/time_evolution.py:346-368``)."""
+        res = [self.evaluate_operators()]
+        self.times = [0.0]
+        for i in range(self.num_time_steps):
+            self.run_one_time_step()
+            if evaluation_time != "inf" and (i + 1) % evaluation_time == 0:
+                res.append(self.evaluate_operators())
+                self.times.append((i + 1) * self.time_step_size)
+        self.results = np.array(res)
+        return self.results
+
+
+class FirstOrderOneSiteTDVP(OneSiteTDVP):
+    """``tdvp_algorithms/firstorderonesite.py:7-104``."""
+
+    def run_one_time_step(self):
+        path = self.update_path
+        op = self.orthogonalization_path
+        for i, nid in enumerate(path):
+            if i == len(path) - 1:
+                if len(op) > 0:
+                    self._move_orth_and_update_cache_for_path(op[-1])
+                self._update_site(nid)
+                self.net.move_orth_center(path[0])
+                self.net.init_cache_but_one(path[0])
+            elif i == 0:
+                assert self.state.orthogonality_center_id == nid
+                self._update_site(nid)
+                self._update_link(nid, op[0][0])
+            else:
+                self._move_orth_and_update_cache_for_path(op[i - 1])
+                self._update_site(nid)
+                self._update_link(nid, op[i][0])
+
+
+class SecondOrderOneSiteTDVP(OneSiteTDVP):
+    """``tdvp_algorithms/secondorderonesite.py:11-193``."""
+
+    def __init__(self, *args, **kwargs):
+        super().__init__(*args, **kwargs)
+        self.backwards_update_path = list(reversed(self.update_path))
+        bp = self.backwards_update_path
+        bo = [self.state.path_from_to(nid, bp[i + 2])[:-1] for i, nid in enumerate(bp[1:-1])]
+        bo.append([bp[-1]])
+        self.backwards_orth_path = bo
+
+    def run_one_time_step(self):
+        path, op = self.update_path, self.orthogonalization_path
+        for i, nid in enumerate(path[:-1]):
+            if i > 0:
+                self._move_orth_and_update_cache_for_path(op[i - 1])
+            self._update_site(nid, 0.5)
+            self._update_link(nid, op[i][0], 0.5)
+        self._update_site(path[-1])
+        bp = self.backwards_update_path
+        self._update_link(self.state.orthogonality_center_id, bp[1], 0.5)
+        for i, nid in enumerate(bp[1:-1]):
+            idx = i + 1
+            self._update_site(nid, 0.5)
+            self._move_orth_and_update_cache_for_path(self.backwards_orth_path[idx - 1])
+            self._update_link(self.state.orthogonality_center_id, bp[idx + 1], 0.5)
+        self._update_site(bp[-1], 0.5)

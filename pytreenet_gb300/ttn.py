@@ -1,0 +1,270 @@
+"""Tree tensor network containers: TreeTensorNetworkState and TreeTensorNetworkOperator.
+
+These mirror the construction API of PyTreeNet's ``TreeTensorNetwork``
+(``core/ttn.py:117-1840``): ``add_root``, ``add_child_to_parent``, ``nodes``,
+``tensors``, ``root_id``, ``orthogonality_center_id``. Storage differs: every
+node tensor is kept in ONE physical leg layout -- (parent, children in the
+order they were attached, open legs) -- on the GPU once an engine uses it. The
+reference reorders a node's children as QR splits and contractions go by
+(``core/ttn.py:1235-1313``, ``contractions/node_contraction.py:88-138``); that
+*logical* order is tracked here as metadata (``Node.children``) because the
+row order of each QR depends on it, and ``tensors[node_id]`` returns the
+tensor permuted to the logical order, as the reference's lazy ``TensorDict``
+(``core/ttn.py:72-115``) does.
+"""
+from __future__ import annotations
+
+from collections.abc import Mapping
+from typing import Iterator
+
+import numpy as np
+
+
+class Node:
+    """A node of a tree: identifier, parent and (logical) children."""
+
+    def __init__(self, identifier: str = "", tensor=None):
+        self.identifier = str(identifier)
+        self.parent: str | None = None
+        self.children: list[str] = []          # logical (reference) order
+        self.phys_children: list[str] = []     # physical layout order
+        self.shape: tuple = tuple(np.shape(tensor)) if tensor is not None else ()
+
+    def is_root(self) -> bool:
+        return self.parent is None
+
+    def is_leaf(self) -> bool:
+        return len(self.children) == 0
+
+    def nneighbours(self) -> int:
+        return len(self.children) + (0 if self.parent is None else 1)
+
+    def neighbouring_nodes(self) -> list[str]:
+        """Logical order, parent first (``core/graph_node.py:340-355``)."""
+        return ([self.parent] if self.parent is not None else []) + list(self.children)
+
+    def phys_neighbours(self) -> list[str]:
+        return ([self.parent] if self.parent is not None else []) + list(self.phys_children)
+
+    def is_parent_of(self, other: str) -> bool:
+        return other in self.children
+
+    def is_child_of(self, other: str) -> bool:
+        return self.parent == other
+
+    def __repr__(self):
+        return f"Node({self.identifier!r}, parent={self.parent!r}, children={self.children!r})"
+
+
+class _TensorView(Mapping):
+    """``ttn.tensors``: numpy arrays in the logical leg order of each node."""
+
+    def __init__(self, ttn: "TreeTensorNetwork"):
+        self._ttn = ttn
+
+    def __getitem__(self, nid):
+        return self._ttn.get_tensor(nid)
+
+    def __setitem__(self, nid, value):
+        self._ttn.set_tensor(nid, value)
+
+    def __iter__(self) -> Iterator[str]:
+        return iter(self._ttn._order)
+
+    def __len__(self):
+        return len(self._ttn._order)
+
+
+class TreeTensorNetwork:
+    """Common tree + tensor storage for states and operators."""
+
+    n_open = 1
+
+    def __init__(self):
+        self.nodes: dict[str, Node] = {}
+        self._order: list[str] = []
+        self._phys: dict[str, object] = {}     # node id -> numpy or torch tensor, physical layout
+        self.root_id: str | None = None
+        self.orthogonality_center_id: str | None = None
+
+    # -- construction (mirrors core/ttn.py:497-640) ---------------------------
+    def add_root(self, node, tensor):
+        node = node if isinstance(node, Node) else Node(node)
+        if self.root_id is not None:
+            raise ValueError("The tree already has a root")
+        tensor = np.asarray(tensor)
+        node.shape = tensor.shape
+        node._open = list(range(tensor.ndim))   # leg indices of the given tensor still open
+        node._legmap = []                       # physical leg -> index of the given tensor
+        self.nodes[node.identifier] = node
+        self._order.append(node.identifier)
+        self._phys[node.identifier] = tensor
+        self.root_id = node.identifier
+        return node
+
+    def add_child_to_parent(self, child, tensor, child_leg: int, parent_id: str, parent_leg: int,
+                            compatible: bool = True):
+        """Attach ``child`` below ``parent_id``. ``parent_leg`` indexes the parent's
+        legs in the reference convention (parent, attached children, open legs)."""
+        child = child if isinstance(child, Node) else Node(child)
+        if child.identifier in self.nodes:
+            raise ValueError(f"Node {child.identifier} already exists")
+        parent = self.nodes[parent_id]
+        tensor = np.asarray(tensor)
+        nattached = (0 if parent.parent is None else 1) + len(parent.phys_children)
+        open_idx = parent_leg - nattached
+        if open_idx < 0 or open_idx >= len(parent._open) - self.n_open:
+            raise ValueError(f"Leg {parent_leg} of {parent_id} is not an open virtual leg")
+        if tensor.shape[child_leg] != parent.shape[parent._open[open_idx]]:
+            raise ValueError("Bond dimensions of parent and child do not match")
+        parent._legmap.append(parent._open.pop(open_idx))
+        parent.phys_children.append(child.identifier)
+        parent.children.append(child.identifier)
+        child.parent = parent_id
+        child.shape = tensor.shape
+        child._open = [i for i in range(tensor.ndim) if i != child_leg]
+        child._legmap = [child_leg]
+        self.nodes[child.identifier] = child
+        self._order.append(child.identifier)
+        self._phys[child.identifier] = tensor
+        return child
+
+    def _finalise(self):
+        """Permute every tensor given at construction into the physical layout."""
+        for nid in self._order:
+            node = self.nodes[nid]
+            if hasattr(node, "_legmap"):
+                perm = list(node._legmap) + list(node._open)
+                t = self._phys[nid]
+                self._phys[nid] = np.ascontiguousarray(np.transpose(t, perm))
+                node.shape = self._phys[nid].shape
+                del node._legmap, node._open
+
+    # -- access ------------------------------------------------------------------
+    @property
+    def tensors(self) -> _TensorView:
+        return _TensorView(self)
+
+    def phys(self, nid):
+        self._finalise()
+        return self._phys[nid]
+
+    def logical_perm(self, nid) -> list[int]:
+        node = self.nodes[nid]
+        off = 0 if node.parent is None else 1
+        perm = list(range(off)) + [off + node.phys_children.index(c) for c in node.children]
+        nv = off + len(node.children)
+        return perm + list(range(nv, nv + self.n_open))
+
+    def get_tensor(self, nid):
+        t = self.phys(nid)
+        if not isinstance(t, np.ndarray):
+            t = t.detach().cpu().numpy()
+        return np.transpose(t, self.logical_perm(nid))
+
+    def set_tensor(self, nid, value):
+        """Set a tensor given in the node's logical leg order."""
+        self._finalise()
+        inv = np.argsort(self.logical_perm(nid))
+        self._phys[nid] = np.ascontiguousarray(np.transpose(np.asarray(value), inv))
+
+    def __getitem__(self, nid):
+        return self.nodes[nid], self.tensors[nid]
+
+    def __contains__(self, nid):
+        return nid in self.nodes
+
+    # -- structure helpers (core/tree_structure.py) ----------------------------
+    def phys_axis(self, nid, nbr) -> int:
+        return self.nodes[nid].phys_neighbours().index(nbr)
+
+    def find_path_to_root(self, nid) -> list[str]:
+        path = [nid]
+        while self.nodes[nid].parent is not None:
+            nid = self.nodes[nid].parent
+            path.append(nid)
+        return path
+
+    def path_from_to(self, a, b) -> list[str]:
+        if a == b:
+            return [a]
+        pa, pb = self.find_path_to_root(a), self.find_path_to_root(b)
+        sb = set(pb)
+        lca = next(x for x in pa if x in sb)
+        return pa[:pa.index(lca) + 1] + list(reversed(pb[:pb.index(lca)]))
+
+    def distance_to_node(self, center) -> dict[str, int]:
+        """Pre-order DFS over logical neighbours (``core/tree_structure.py:225-271``)."""
+        out = {center: 0}
+
+        def rec(nid, last, d):
+            out[nid] = d
+            for nb in self.nodes[nid].neighbouring_nodes():
+                if nb != last:
+                    rec(nb, nid, d + 1)
+        for nb in self.nodes[center].neighbouring_nodes():
+            rec(nb, center, 1)
+        return out
+
+    def get_leaves(self) -> list[str]:
+        return [nid for nid in self._order if self.nodes[nid].is_leaf()]
+
+    def bond_dim(self, a, b) -> int:
+        return self.phys(a).shape[self.phys_axis(a, b)]
+
+    def copy_structure(self):
+        """Deep copy of the structure (tensors are shared)."""
+        import copy
+        self._finalise()
+        new = self.__class__.__new__(self.__class__)
+        new.nodes = copy.deepcopy(self.nodes)
+        new._order = list(self._order)
+        new._phys = dict(self._phys)
+        new.root_id = self.root_id
+        new.orthogonality_center_id = self.orthogonality_center_id
+        return new
+
+
+class TreeTensorNetworkState(TreeTensorNetwork):
+    """TTNS: one open (physical) leg per node (``ttns/ttns.py:18-444``)."""
+
+    n_open = 1
+
+    def to_dense(self, site_order=None) -> np.ndarray:
+        """Contract to a dense state vector (small trees only)."""
+        self._finalise()
+        site_order = site_order or list(self._order)
+
+        def rec(nid, toward):
+            A = np.asarray(self.get_phys_numpy(nid))
+            legs = self.nodes[nid].phys_neighbours()
+            cur = list(legs) + ["#" + nid]
+            T = A
+            for nb in legs:
+                if nb == toward:
+                    continue
+                sub, subs = rec(nb, nid)
+                ax = cur.index(nb)
+                T = np.tensordot(T, sub, axes=([ax], [0]))
+                cur = cur[:ax] + cur[ax + 1:] + ["#" + s for s in subs]
+            if toward is not None:
+                ax = cur.index(toward)
+                T = np.moveaxis(T, ax, 0)
+                cur = [cur[ax]] + cur[:ax] + cur[ax + 1:]
+            return T, [c[1:] for c in cur if c.startswith("#")]
+        T, sites = rec(self.root_id, None)
+        return np.transpose(T, [sites.index(s) for s in site_order]).reshape(-1)
+
+    def get_phys_numpy(self, nid):
+        t = self.phys(nid)
+        return t if isinstance(t, np.ndarray) else t.detach().cpu().numpy()
+
+
+class TreeTensorNetworkOperator(TreeTensorNetwork):
+    """TTNO: two open legs (out, in) per node (``ttno/ttno_class.py:35-363``)."""
+
+    n_open = 2
+
+
+TTNS = TreeTensorNetworkState
+TTNO = TreeTensorNetworkOperator

@@ -1,0 +1,95 @@
+"""Seeded synthetic workloads in the shapes of the benchmark configurations.
+
+* T-tree: root with three arms of ``arm_len`` sites (61 sites for arm_len=20),
+  every bond of dimension ``chi``, Gaussian complex entries (each tensor scaled
+  to unit Frobenius norm so the contraction of 61 tensors stays in range),
+  Heisenberg couplings plus random fields h_i ~ U[-1, 1] (TTNO bond 5).
+* binary tree: heap-ordered (node i has children 2i+1, 2i+2), transverse-field
+  Ising H = -J sum Z_i Z_j - g sum X_i, product state on the Bloch sphere
+  zero-padded to ``chi`` (TTNO bond 3).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .operators import heisenberg_ttno, tfim_ttno
+from .ttn import TreeTensorNetworkState
+
+
+def _build(spec, tensors) -> TreeTensorNetworkState:
+    st = TreeTensorNetworkState()
+    parent = dict(spec)
+    slot = {nid: 0 for nid, _ in spec}
+    for nid, p in spec:
+        if p is None:
+            st.add_root(nid, tensors[nid])
+        else:
+            off = 1 if parent[p] is not None else 0
+            st.add_child_to_parent(nid, tensors[nid], 0, p, off + slot[p])
+            slot[p] += 1
+    st._finalise()
+    return st
+
+
+def t_tree_spec(arm_len: int):
+    spec = [("root", None)]
+    for a in range(3):
+        prev = "root"
+        for k in range(arm_len):
+            nid = f"a{a}_{k}"
+            spec.append((nid, prev))
+            prev = nid
+    return spec
+
+
+def t_tree_state(arm_len: int = 20, chi: int = 256, seed: int = 0, dtype=np.complex128):
+    """Returns (TTNS, spec, tensors in physical layout)."""
+    rng = np.random.default_rng(seed)
+    spec = t_tree_spec(arm_len)
+    nkids = {nid: 0 for nid, _ in spec}
+    for nid, p in spec:
+        if p is not None:
+            nkids[p] += 1
+    tensors = {}
+    for nid, p in spec:
+        nv = nkids[nid] + (0 if p is None else 1)
+        shape = [chi] * nv + [2]
+        t = (rng.standard_normal(size=shape, dtype=np.float64)
+             + 1j * rng.standard_normal(size=shape, dtype=np.float64)).astype(dtype)
+        t /= np.linalg.norm(t)
+        tensors[nid] = t
+    return _build(spec, tensors), spec, tensors
+
+
+def t_tree_heisenberg(state: TreeTensorNetworkState, seed: int = 1):
+    """Heisenberg + random fields on the state's tree; returns (TTNO, W in physical layout)."""
+    rng = np.random.default_rng(seed)
+    fields = {nid: rng.uniform(-1.0, 1.0) for nid in state._order}
+    H = heisenberg_ttno(state, fields)
+    return H, {nid: H.phys(nid) for nid in state._order}
+
+
+def binary_tree_spec(n: int):
+    return [(f"s{i}", None if i == 0 else f"s{(i - 1) // 2}") for i in range(n)]
+
+
+def binary_tfim_product_state(n: int = 15, chi: int = 8, seed: int = 0, J: float = 1.0, g: float = 0.5):
+    rng = np.random.default_rng(seed)
+    spec = binary_tree_spec(n)
+    nkids = {nid: 0 for nid, _ in spec}
+    for nid, p in spec:
+        if p is not None:
+            nkids[p] += 1
+    tensors = {}
+    for nid, p in spec:
+        v = rng.normal(size=3)
+        v /= np.linalg.norm(v)
+        th, ph = np.arccos(v[2]), np.arctan2(v[1], v[0])
+        site = np.array([np.cos(th / 2), np.exp(1j * ph) * np.sin(th / 2)], dtype=complex)
+        nv = nkids[nid] + (0 if p is None else 1)
+        t = np.zeros([chi] * nv + [2], dtype=complex)
+        t[(0,) * nv] = site
+        tensors[nid] = t
+    st = _build(spec, tensors)
+    H = tfim_ttno(st, J=J, g=g)
+    return st, H, spec, tensors

@@ -1,0 +1,270 @@
+"""Generate golden fixtures by running PyTreeNet's own TDVP drivers.
+
+Run (in a container where the reference sources are available):
+
+    python tests/golden/make_golden.py /root/reference
+
+The reference needs ``h5py`` only for HDF5 result I/O; when it is missing, a
+stand-in module whose ``File`` raises is registered before the import. Every
+fixture stores the seeded inputs (state tensors and TTNO tensors in the engine's
+physical leg layout: parent, children in insertion order, physical / out, in),
+the reference's outputs after each time step (state tensors in the same layout,
+single-site expectation values) and the reference's update path.
+"""
+from __future__ import annotations
+
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _import_reference(ref_root: str):
+    try:
+        import h5py  # noqa: F401
+    except ImportError:
+        stub = types.ModuleType("h5py")
+
+        class File:  # noqa: D401
+            def __init__(self, *a, **k):
+                raise RuntimeError("h5py unavailable")
+        stub.File = File
+        sys.modules["h5py"] = stub
+    sys.path.insert(0, ref_root)
+    import pytreenet as ptn
+    return ptn
+
+
+X = np.array([[0, 1], [1, 0]], dtype=complex)
+Y = np.array([[0, -1j], [1j, 0]], dtype=complex)
+Z = np.diag([1.0, -1.0]).astype(complex)
+
+
+def binary_tree(n):
+    """Heap-ordered binary tree: node i has children 2i+1, 2i+2."""
+    return [(f"s{i}", None if i == 0 else f"s{(i - 1) // 2}") for i in range(n)]
+
+
+def t_tree(arm_len):
+    """Root with three arms of ``arm_len`` sites."""
+    spec = [("root", None)]
+    for a in range(3):
+        prev = "root"
+        for k in range(arm_len):
+            nid = f"a{a}_{k}"
+            spec.append((nid, prev))
+            prev = nid
+    return spec
+
+
+def ternary_tree(depth):
+    spec = [("t0", None)]
+    frontier = ["t0"]
+    idx = 1
+    for _ in range(depth):
+        nxt = []
+        for p in frontier:
+            for _ in range(3):
+                nid = f"t{idx}"
+                idx += 1
+                spec.append((nid, p))
+                nxt.append(nid)
+        frontier = nxt
+    return spec
+
+
+def children_of(spec):
+    ch = {nid: [] for nid, _ in spec}
+    for nid, p in spec:
+        if p is not None:
+            ch[p].append(nid)
+    return ch
+
+
+def build_reference_state(ptn, spec, tensors):
+    """Build the reference TTNS from tensors in physical layout."""
+    ch = children_of(spec)
+    ttns = ptn.TreeTensorNetworkState()
+    slot = {nid: 0 for nid, _ in spec}
+    for nid, p in spec:
+        if p is None:
+            ttns.add_root(ptn.Node(identifier=nid), tensors[nid])
+        else:
+            off = 1 if dict(spec)[p] is not None else 0
+            ttns.add_child_to_parent(ptn.Node(identifier=nid), tensors[nid], 0, p, off + slot[p])
+            slot[p] += 1
+    return ttns
+
+
+def phys_layout(ttn_node_parent, ttn_node_children, tensor, spec_children, nopen):
+    """Permute a reference tensor (parent, logical children, open...) into
+    (parent, children in insertion order, open...)."""
+    off = 0 if ttn_node_parent is None else 1
+    perm = list(range(off))
+    perm += [off + ttn_node_children.index(c) for c in spec_children]
+    nv = off + len(ttn_node_children)
+    perm += list(range(nv, nv + nopen))
+    return np.ascontiguousarray(np.transpose(tensor, perm))
+
+
+def export_state(ttns, spec):
+    ch = children_of(spec)
+    out = {}
+    for nid, _ in spec:
+        node = ttns.nodes[nid]
+        out[nid] = phys_layout(node.parent, list(node.children), ttns.tensors[nid], ch[nid], 1)
+    return out
+
+
+def export_ttno(ttno, spec):
+    ch = children_of(spec)
+    out = {}
+    for nid, _ in spec:
+        node = ttno.nodes[nid]
+        out[nid] = phys_layout(node.parent, list(node.children), ttno.tensors[nid], ch[nid], 2)
+    return out
+
+
+def product_state_tensors(spec, rng, bond):
+    """Product state uniform on the Bloch sphere, zero-padded to ``bond``."""
+    ch = children_of(spec)
+    parent = dict(spec)
+    out = {}
+    for nid, p in spec:
+        v = rng.normal(size=3)
+        v /= np.linalg.norm(v)
+        th, ph = np.arccos(v[2]), np.arctan2(v[1], v[0])
+        site = np.array([np.cos(th / 2), np.exp(1j * ph) * np.sin(th / 2)], dtype=complex)
+        nv = len(ch[nid]) + (0 if p is None else 1)
+        t = np.zeros([bond] * nv + [2], dtype=complex)
+        t[(0,) * nv] = site
+        out[nid] = t
+    return out
+
+
+def random_state_tensors(spec, rng, bond):
+    ch = children_of(spec)
+    out = {}
+    for nid, p in spec:
+        nv = len(ch[nid]) + (0 if p is None else 1)
+        shape = [bond] * nv + [2]
+        out[nid] = (rng.normal(size=shape) + 1j * rng.normal(size=shape)) / np.sqrt(2)
+    return out
+
+
+def tfim(ptn, spec, J=1.0, g=0.5):
+    conv = {"mJZ": -J * Z, "Z": Z, "mgX": -g * X, "I2": np.eye(2, dtype=complex)}
+    terms = [ptn.TensorProduct({nid: "mJZ", p: "Z"}) for nid, p in spec if p is not None]
+    terms += [ptn.TensorProduct({nid: "mgX"}) for nid, _ in spec]
+    return ptn.Hamiltonian(terms, conv)
+
+
+def heisenberg_fields(ptn, spec, fields, jxy=None, jz=None):
+    conv = {"I2": np.eye(2, dtype=complex)}
+    terms = []
+    for i, (nid, p) in enumerate(spec):
+        conv[f"h{nid}"] = fields[i] * Z
+        terms.append(ptn.TensorProduct({nid: f"h{nid}"}))
+    for e, (nid, p) in enumerate([x for x in spec if x[1] is not None]):
+        cxy = 1.0 if jxy is None else jxy[e]
+        cz = 1.0 if jz is None else jz[e]
+        conv[f"X{e}"] = cxy * X
+        conv[f"Y{e}"] = cxy * Y
+        conv[f"Z{e}"] = cz * Z
+        conv["X"], conv["Y"], conv["Z"] = X, Y, Z
+        terms.append(ptn.TensorProduct({nid: f"X{e}", p: "X"}))
+        terms.append(ptn.TensorProduct({nid: f"Y{e}", p: "Y"}))
+        terms.append(ptn.TensorProduct({nid: f"Z{e}", p: "Z"}))
+    return ptn.Hamiltonian(terms, conv)
+
+
+def run_case(ptn, name, spec, tensors, ham_fn, dt, steps, order, tol, canonical_random=False):
+    from pytreenet.time_evolution.time_evolution import TimeEvoMode
+    from pytreenet.time_evolution.tdvp_algorithms.tdvp_algorithm import TDVPConfig
+    psi = build_reference_state(ptn, spec, tensors)
+    if canonical_random:
+        psi.canonical_form(spec[0][0])
+        psi.normalise()
+        tensors = export_state(psi, spec)
+        psi = build_reference_state(ptn, spec, tensors)
+    H = ptn.TTNO.from_hamiltonian(ham_fn(psi), psi)
+    cls = ptn.FirstOrderOneSiteTDVP if order == 1 else ptn.SecondOrderOneSiteTDVP
+    ops = {nid: ptn.TensorProduct({nid: Z}) for nid, _ in spec}
+    algo = cls(psi, H, dt, dt * steps, ops,
+               config=TDVPConfig(time_evo_mode=TimeEvoMode.KRYLOV),
+               solver_options={"krylov_tol": tol})
+    rec = {"spec_ids": np.array([s[0] for s in spec]),
+           "spec_parents": np.array(["" if s[1] is None else s[1] for s in spec]),
+           "dt": dt, "steps": steps, "order": order, "krylov_tol": tol,
+           "update_path": np.array(algo.update_path)}
+    for nid, t in tensors.items():
+        rec[f"init/{nid}"] = t
+    for nid, t in export_ttno(H, spec).items():
+        rec[f"ttno/{nid}"] = t
+    zs = []
+    for step in range(steps):
+        algo.run_one_time_step()
+        zs.append([algo.state.operator_expectation_value(ops[nid]) for nid, _ in spec])
+    rec["z"] = np.array(zs)
+    for nid, t in export_state(algo.state, spec).items():
+        rec[f"final/{nid}"] = t
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **rec)
+    print(name, "written; path", algo.update_path[:6], "...")
+
+
+def unit_cases(ptn):
+    """Krylov exponential and single-site matvec known answers."""
+    from pytreenet.time_evolution.time_evolution import krylov_exp_action
+    from pytreenet.contractions.state_operator_contraction import contract_ket_ham_with_envs
+    rng = np.random.default_rng(7)
+    rec = {}
+    for n, tol in ((40, 1e-10), (48, 1e-12), (16, 0.0)):
+        A = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
+        Hm = (A + A.conj().T) / 2
+        psi = rng.normal(size=n) + 1j * rng.normal(size=n)
+        for ef, tag in ((-1j, "fwd"), (1j, "bwd")):
+            out = krylov_exp_action(psi, lambda y: Hm @ y, 0.05, ef, krylov_tol=tol)
+            rec[f"krylov/{n}/{tag}/H"] = Hm
+            rec[f"krylov/{n}/{tag}/psi"] = psi
+            rec[f"krylov/{n}/{tag}/out"] = out
+            rec[f"krylov/{n}/{tag}/tol"] = tol
+    np.savez_compressed(os.path.join(HERE, "units.npz"), **rec)
+    print("units written")
+
+
+def main(ref_root):
+    ptn = _import_reference(ref_root)
+    rng = np.random.default_rng(1234)
+    # C1 as specified: 15-node binary TFIM, padded product state chi=8, 50 steps.
+    spec = binary_tree(15)
+    run_case(ptn, "c1_binary15_tfim_chi8", spec, product_state_tensors(spec, rng, 8),
+             lambda psi: tfim(ptn, spec), 0.01, 50, 1, 1e-12)
+    # Small padded case, second order.
+    spec = binary_tree(7)
+    run_case(ptn, "binary7_tfim_chi4_o2", spec, product_state_tensors(spec, rng, 4),
+             lambda psi: tfim(ptn, spec), 0.02, 8, 2, 1e-12)
+    # T-tree, random canonicalised state, Heisenberg + fields (C3 shape, small).
+    spec = t_tree(3)
+    h = rng.uniform(-1, 1, size=len(spec))
+    run_case(ptn, "ttree3_heis_chi6_o1", spec, random_state_tensors(spec, rng, 6),
+             lambda psi: heisenberg_fields(ptn, spec, h), 0.01, 4, 1, 1e-12,
+             canonical_random=True)
+    run_case(ptn, "ttree3_heis_chi6_o2", spec, random_state_tensors(spec, rng, 6),
+             lambda psi: heisenberg_fields(ptn, spec, h), 0.01, 3, 2, 1e-12,
+             canonical_random=True)
+    # Ternary depth 2, XXZ with random couplings, random chi=4 state.
+    spec = ternary_tree(2)
+    ne = len(spec) - 1
+    jxy = rng.uniform(0.5, 1.5, size=ne)
+    jz = rng.uniform(0.5, 1.5, size=ne)
+    run_case(ptn, "ternary2_xxz_chi4_o1", spec, random_state_tensors(spec, rng, 4),
+             lambda psi: heisenberg_fields(ptn, spec, np.zeros(len(spec)), jxy, jz),
+             0.02, 4, 1, 1e-12, canonical_random=True)
+    unit_cases(ptn)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,66 @@
+"""Load golden fixtures into the oracle's data model (shared by the tests)."""
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load_case(name):
+    d = np.load(os.path.join(GOLDEN, name + ".npz"))
+    ids = [str(x) for x in d["spec_ids"]]
+    parents = [str(x) or None for x in d["spec_parents"]]
+    spec = list(zip(ids, parents))
+    case = {
+        "spec": spec,
+        "init": {i: d[f"init/{i}"] for i in ids},
+        "ttno": {i: d[f"ttno/{i}"] for i in ids},
+        "final": {i: d[f"final/{i}"] for i in ids},
+        "z": d["z"],
+        "dt": float(d["dt"]),
+        "steps": int(d["steps"]),
+        "order": int(d["order"]),
+        "krylov_tol": float(d["krylov_tol"]),
+        "update_path": [str(x) for x in d["update_path"]],
+    }
+    return case
+
+
+CASES = ["c1_binary15_tfim_chi8", "binary7_tfim_chi4_o2", "ttree3_heis_chi6_o1",
+         "ttree3_heis_chi6_o2", "ternary2_xxz_chi4_o1"]
+
+
+def build_ttn(cls, spec, tensors):
+    """Build a pytreenet_gb300 TTNS/TTNO from tensors in physical layout."""
+    t = cls()
+    parent = dict(spec)
+    slot = {nid: 0 for nid, _ in spec}
+    for nid, p in spec:
+        if p is None:
+            t.add_root(nid, tensors[nid])
+        else:
+            off = 1 if parent[p] is not None else 0
+            t.add_child_to_parent(nid, tensors[nid], 0, p, off + slot[p])
+            slot[p] += 1
+    return t
+
+
+def oracle_state(case, key="init"):
+    import oracle as O
+    tree = O.OTree()
+    for nid, p in case["spec"]:
+        tree.add_root(nid) if p is None else tree.add_child(nid, p)
+    return O.OState(tree, case[key])
+
+
+def fidelity_and_dist(a_state, b_state):
+    """1 - |<a|b>|/(|a||b|) and the phase-aligned relative distance, by oracle contractions."""
+    import numpy as np
+    import oracle as O
+    ab = O.scalar_product(a_state, b_state)
+    aa = O.scalar_product(a_state, a_state).real
+    bb = O.scalar_product(b_state, b_state).real
+    f = abs(ab) / np.sqrt(aa * bb)
+    # ||a - e^{i phi} b||^2 / ||a||^2 with the optimal phase; guard the cancellation
+    d2 = max(aa + bb - 2 * abs(ab), 0.0) / aa
+    return 1 - f, np.sqrt(d2)

@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "plain"])
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison sweep")
     return ap.parse_args()
 
 
@@ -211,14 +213,17 @@ def run_gb300(args, rank, world):
     if world > 1:
         import torch.distributed as dist
     lib = _lib.load()
-    st, spec, _ = t_tree_state(arm_len=args.arm, chi=args.chi, seed=rank)
-    H, _ = t_tree_heisenberg(st, seed=1000 + rank)
-    total = args.warmup + 2 * args.steps + 1
-    algo = P.FirstOrderOneSiteTDVP(st, H, args.dt, args.dt * total, {},
-                                   config=P.TDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV),
-                                   solver_options={"krylov_tol": args.tol})
+    def make(precision):
+        st, spec, _ = t_tree_state(arm_len=args.arm, chi=args.chi, seed=rank)
+        H, _ = t_tree_heisenberg(st, seed=1000 + rank)
+        total = args.warmup + 2 * args.steps + 1
+        a = P.FirstOrderOneSiteTDVP(st, H, args.dt, args.dt * total, {},
+                                    config=P.TDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV),
+                                    solver_options={"krylov_tol": args.tol}, precision=precision)
+        a.net.normalise_center()
+        return a
+    algo = make(args.precision)
     net = algo.net
-    net.normalise_center()
     for _ in range(args.warmup):
         algo.run_one_time_step()
     torch.cuda.synchronize()
@@ -299,20 +304,72 @@ def run_gb300(args, rank, world):
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes}
 
     achieved = heff_flops / (heff_ms / 1000.0) / 1e12 if heff_ms > 0 else None
-    roof = {"bound": "tensor", "kernel": "ptn_zcontract (heff matvec chain, FP64)",
-            "achieved": achieved, "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
-            "frac": (achieved / FP64_NOMINAL_TFLOPS) if achieved else None,
-            "peak_source": "nominal GB300 FP64 (1.25 TFLOP/s); FP64 is not in MEASURED_PEAKS.json",
-            "traffic": None,
+    if args.precision == "mixed":
+        peak, peak_src = _measured_bf16_peak()
+        # algorithmic complex flops (8 per complex MAC); the BF16x3 split issues 3x that on the pipe
+        roof = {"bound": "tensor", "kernel": "ptn_cgemm_bf16x3 (heff matvec chain, tcgen05)",
+                "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": (achieved / peak) if achieved else None,
+                "peak_source": peak_src + "; achieved counts algorithmic complex flops, the BF16x3 "
+                               "split issues 3x as many tensor flops",
+                "traffic": None}
+    else:
+        roof = {"bound": "tensor", "kernel": "ptn_zcontract (heff matvec chain, FP64)",
+                "achieved": achieved, "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+                "frac": (achieved / FP64_NOMINAL_TFLOPS) if achieved else None,
+                "peak_source": "nominal GB300 FP64 (1.25 TFLOP/s); FP64 is not in MEASURED_PEAKS.json",
+                "traffic": None}
+    roof.update({
             "algorithmic_flops_per_matvec": heff_flops / max(n_heff, 1),
-            "matvecs_timed": n_heff, "matvec_ms_total": heff_ms, "share_of_step": heff_ms / ms}
+            "matvecs_timed": n_heff, "matvec_ms_total": heff_ms, "share_of_step": heff_ms / ms})
+    plain = None
+    if args.precision == "mixed" and not args.no_plain and rank == 0:
+        plain = compare_with_plain(args, make)
+        plain["speedup_mixed_over_plain"] = value / plain["sweeps_per_s"]
     line = {"metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "c128 (fp64)", "data": "synthetic",
-            "config": config(args, "plain complex128"), "roofline": roof, "e2e": e2e,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "c64 bf16x3 contractions / f64 Krylov" if args.precision == "mixed" else "c128 (fp64)",
+            "data": "synthetic",
+            "config": config(args, "mixed: BF16x3 tcgen05 contractions, FP32 accumulate, FP64 Krylov/QR/norm"
+                             if args.precision == "mixed" else "plain complex128"),
+            "roofline": roof, "e2e": e2e, "plain_fp64": plain,
             "gpu_launches": launches, "clocks": clk.summary(),
             "krylov_depth_mean": float(np.mean(net.krylov.depths[-n_heff:])) if n_heff else None}
     return line
+
+
+def _measured_bf16_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(path))
+        return float(d["bf16_tflops"]), "MEASURED_PEAKS.json bf16_tflops (burst, cuBLAS), of measured"
+    except Exception:
+        return 1900.0, "fallback 1.9 PFLOP/s bf16 (MEASURED_PEAKS.json absent), of fallback"
+
+
+def compare_with_plain(args, make):
+    """One sweep on the plain complex128 path from the same initial state as one
+    sweep on the mixed path: plain sweep time and the fidelity error of the
+    mixed result (1 - |<mixed|plain>| / (|mixed| |plain|))."""
+    import torch
+    a_m = make("mixed")
+    a_m.run_one_time_step()
+    a_p = make("plain")
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    a_p.run_one_time_step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    ov = a_m.net.overlap(a_p.net)
+    nm = a_m.net.overlap(a_m.net).real
+    npl = a_p.net.overlap(a_p.net).real
+    err = 1.0 - abs(ov) / np.sqrt(nm * npl)
+    t = args.dt
+    return {"sweeps_per_s": 1000.0 / ms, "ms_per_sweep": ms, "fidelity_error_one_sweep": err,
+            "fidelity_error_per_unit_time": err / t, "sweeps_compared": 1}
 
 
 def run_reference(args, rank, world):

@@ -27,7 +27,8 @@ enum {
   PTN_ERR_NONFINITE = 3,    /* NaN or Inf found in an input               */
   PTN_ERR_BREAKDOWN = 4,    /* Krylov breakdown that cannot be continued  */
   PTN_ERR_NOCONVERGE = 5,   /* iterative decomposition did not converge   */
-  PTN_ERR_UNSUPPORTED = 6   /* configuration outside the kernel's limits  */
+  PTN_ERR_UNSUPPORTED = 6,  /* configuration outside the kernel's limits  */
+  PTN_ERR_TIMEOUT = 7       /* a bounded device-side wait ran out         */
 };
 
 #define PTN_MAX_MODES 6
@@ -103,6 +104,51 @@ int ptn_zcombine(const void* Q, int64_t ldq, int32_t nq, const void* c,
 int64_t ptn_zqr_work_bytes(int64_t m, int64_t k);
 int ptn_zqr_keep(void* A, const int64_t* rowoff, int64_t m, int64_t k, int64_t colstride,
                  void* R, void* work, void* stream);
+
+/* ---- Mixed precision (tcgen05 tensor cores, BF16x3, FP32 accumulation) -------
+ * C[m, n] = sum_k A[m, k] * B[n, k] over complex numbers; A and B are given as
+ * BF16 hi/lo splits. A: 4 planes (Re hi, Im hi, Re lo, Im lo), plane p at
+ * A + p * a_plane, row m at m * lda (lda, a_plane multiples of 8, 16-byte
+ * aligned base). Bx: bf16 [2 levels][3 blocks (-Im, Re, Im)][N][ldb] as
+ * written by ptn_expand_b. The result is written through m_out / n_out
+ * (dims + stride_c): out_kind 0 = complex128 at C, 1 = BF16 hi/lo planes at C
+ * with plane stride c_plane. status: device int32, set on a device-side timeout.
+ * Replaces the np.tensordot chain of contract_ket_ham_with_envs /
+ * contract_any (contractions/state_operator_contraction.py:227-273, 407-694)
+ * in the mixed-precision path. */
+typedef struct {
+  const void* A;
+  int64_t lda, a_plane;
+  int64_t M, K;
+  const void* Bx;
+  int64_t ldb, N;
+  int32_t out_kind, pad_;
+  void* C;
+  int64_t c_plane;
+  ptn_modes m_out, n_out;
+  int32_t* status;
+} ptn_cgemm_desc;
+int ptn_cgemm_bf16x3(const ptn_cgemm_desc* d, void* stream);
+int ptn_cgemm_smem_bytes(void);
+
+/* Gather a complex128 tensor into the split BF16 operand layouts above.
+ * rows / cols: source mode groups (dims + stride_a); element (r, c) of the
+ * operand is src[off_rows(r) + off_cols(c)], conjugated when conj != 0.
+ * ptn_to_planes writes 4 planes of [rows][ld] with plane stride `plane`;
+ * ptn_expand_b writes [2][3][rows][ld] (rows = N). */
+typedef struct {
+  const void* src;
+  void* dst;
+  int64_t ld, plane;
+  int32_t conj, pad_;
+  ptn_modes rows, cols;
+} ptn_convert_desc;
+int ptn_to_planes(const ptn_convert_desc* d, void* stream);
+int ptn_expand_b(const ptn_convert_desc* d, void* stream);
+
+/* Self-test of the tcgen05 descriptors: D[128][128] (fp32) = A[128][64] * B[128][64]^T
+ * for bf16 A, B (K contiguous); one CTA. */
+int ptn_tc_selftest(const void* A, const void* B, void* D, int32_t* status, void* stream);
 
 /* Number of kernel launches this library has issued since it was loaded
  * (host-side counter; used to report launches inside a timed region). */

@@ -20,6 +20,7 @@ _STATUS = {
     4: "Krylov breakdown",
     5: "decomposition did not converge",
     6: "configuration outside the kernel's limits",
+    7: "a bounded device-side wait ran out",
 }
 
 
@@ -51,6 +52,20 @@ class ContractDesc(ctypes.Structure):
                 ("m", Modes), ("n", Modes), ("k", Modes)]
 
 
+class CgemmDesc(ctypes.Structure):
+    _fields_ = [("A", ctypes.c_void_p), ("lda", ctypes.c_int64), ("a_plane", ctypes.c_int64),
+                ("M", ctypes.c_int64), ("K", ctypes.c_int64), ("Bx", ctypes.c_void_p),
+                ("ldb", ctypes.c_int64), ("N", ctypes.c_int64), ("out_kind", ctypes.c_int32),
+                ("pad_", ctypes.c_int32), ("C", ctypes.c_void_p), ("c_plane", ctypes.c_int64),
+                ("m_out", Modes), ("n_out", Modes), ("status", ctypes.c_void_p)]
+
+
+class ConvertDesc(ctypes.Structure):
+    _fields_ = [("src", ctypes.c_void_p), ("dst", ctypes.c_void_p), ("ld", ctypes.c_int64),
+                ("plane", ctypes.c_int64), ("conj", ctypes.c_int32), ("pad_", ctypes.c_int32),
+                ("rows", Modes), ("cols", Modes)]
+
+
 _P = ctypes.c_void_p
 _I64 = ctypes.c_int64
 _I32 = ctypes.c_int32
@@ -66,6 +81,11 @@ SIGNATURES = {
     "ptn_zqr_keep": (ctypes.c_int, [_P, _P, _I64, _I64, _I64, _P, _P, _P]),
     "ptn_check_finite": (ctypes.c_int, [_P, _I64, _P, _P]),
     "ptn_launch_counter": (ctypes.c_ulonglong, []),
+    "ptn_cgemm_bf16x3": (ctypes.c_int, [ctypes.POINTER(CgemmDesc), _P]),
+    "ptn_cgemm_smem_bytes": (ctypes.c_int, []),
+    "ptn_to_planes": (ctypes.c_int, [ctypes.POINTER(ConvertDesc), _P]),
+    "ptn_expand_b": (ctypes.c_int, [ctypes.POINTER(ConvertDesc), _P]),
+    "ptn_tc_selftest": (ctypes.c_int, [_P, _P, _P, _P, _P]),
 }
 
 _lib = None

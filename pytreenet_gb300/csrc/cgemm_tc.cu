@@ -1,0 +1,396 @@
+// Mixed-precision complex contraction on the 5th-generation tensor cores.
+//
+// C[m, n] = sum_k A[m, k] * B[n, k] (complex), with A and B split into BF16
+// hi/lo parts (x = hi + lo, each bf16) and products accumulated in FP32 in
+// TMEM: A*B ~ Ah*Bh + Ah*Bl + Al*Bh ("BF16x3"). The complex product is written
+// as one real product with doubled width:
+//   [Cr | Ci] = Ar * [Br | Bi] + Ai * [-Bi | Br]
+// so each K=16 slice issues 6 tcgen05.mma (M=128, N=2*NT, K=16): for each of
+// (Ah,Bh), (Ah,Bl), (Al,Bh) one with Ar and one with Ai. The expanded B keeps
+// the three blocks [-Bi; Br; Bi] adjacent in shared memory, so the Ar operand
+// is the window [Br; Bi] and the Ai operand the window [-Bi; Br].
+//
+// Operands (both K-major, K contiguous):
+//   A: 4 bf16 planes (Ar_hi, Ai_hi, Ar_lo, Ai_lo), each [M][lda]
+//   Bx: bf16 [level(hi, lo)][block(-Bi, Br, Bi)][N][ldb]
+// Tiles are staged by TMA (128-byte swizzle) through a 2-stage mbarrier ring;
+// one warp issues TMA, one warp issues MMA and owns the TMEM allocation, four
+// warps run the epilogue (TMEM -> registers -> global, strided by output mode
+// tables so the result lands directly in the layout the next step reads).
+// Every mbarrier wait is bounded; a timeout sets *status and the CTA exits.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+
+#include "ptn_common.cuh"
+#include "tc_ptx.cuh"
+
+namespace {
+
+constexpr int MT = 128;         // rows of C per CTA
+constexpr int NT = 64;          // complex columns of C per CTA (MMA N = 2*NT)
+constexpr int KT = 64;          // K per stage (one 128-byte swizzle row)
+constexpr int STAGES = 2;
+constexpr int A_PLANE_BYTES = MT * 128;            // 16 KB
+constexpr int A_STAGE_BYTES = 4 * A_PLANE_BYTES;   // 64 KB
+constexpr int B_BLOCK_BYTES = NT * 128;            // 8 KB
+constexpr int B_STAGE_BYTES = 6 * B_BLOCK_BYTES;   // 48 KB
+constexpr int STAGE_BYTES = A_STAGE_BYTES + B_STAGE_BYTES;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;
+constexpr int THREADS = 192;
+constexpr long long WAIT_CYCLES = 4000000000LL;    // ~2 s at 2 GHz
+
+struct OutModes {
+  int n;
+  int64_t dim[PTN_MAX_MODES];
+  int64_t stride[PTN_MAX_MODES];
+};
+
+struct GemmArgs {
+  int64_t M, N, K;
+  int out_kind;              // 0: complex128, 1: bf16 planes
+  void* C;
+  int64_t c_plane;           // plane stride (elements) for out_kind 1
+  OutModes mo, no;
+  int32_t* status;
+  int64_t tiles_n;
+};
+
+__device__ __forceinline__ int64_t decode_off(const OutModes& md, int64_t idx) {
+  int64_t o = 0;
+  for (int d = md.n - 1; d >= 0; --d) {
+    int64_t q = idx / md.dim[d];
+    o += (idx - q * md.dim[d]) * md.stride[d];
+    idx = q;
+  }
+  return o;
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    cgemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                        const GemmArgs g) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  __shared__ uint64_t full_bar[STAGES], empty_bar[STAGES], done_bar;
+  __shared__ uint32_t tmem_base;
+  __shared__ int64_t noff[NT];
+  __shared__ int s_abort;
+  const volatile int32_t* vstatus = g.status;
+  if (threadIdx.x == 0) s_abort = *vstatus;
+  __syncthreads();
+  if (s_abort != 0) return;  // an earlier CTA failed: skip the work
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t tile = blockIdx.x;
+  const int64_t tm = tile / g.tiles_n, tn = tile - tm * g.tiles_n;
+  const int64_t m0 = tm * MT, n0 = tn * NT;
+  const int ktiles = (int)((g.K + KT - 1) / KT);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      tc::mbar_init(&full_bar[s], 1);
+      tc::mbar_init(&empty_bar[s], 1);
+    }
+    tc::mbar_init(&done_bar, 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 1) {
+    tc::tmem_alloc(&tmem_base, 2 * NT);
+    tc::tmem_relinquish();
+  }
+  if (threadIdx.x >= 64 && threadIdx.x < 64 + NT) {
+    const int j = threadIdx.x - 64;
+    const int64_t n = n0 + j;
+    noff[j] = (n < g.N) ? decode_off(g.no, n) : -1;
+  }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = tmem_base;
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      tc::prefetch_tmap(&tmA);
+      tc::prefetch_tmap(&tmB);
+      for (int kt = 0; kt < ktiles; ++kt) {
+        const int s = kt % STAGES;
+        const int use = kt / STAGES;
+        if (use > 0 && !tc::mbar_wait_abortable(&empty_bar[s], (use - 1) & 1, WAIT_CYCLES, vstatus)) {
+          atomicExch(g.status, PTN_ERR_TIMEOUT);
+          break;
+        }
+        uint8_t* st = smem + s * STAGE_BYTES;
+        tc::mbar_arrive_expect_tx(&full_bar[s], STAGE_BYTES);
+        const int kx = kt * KT;
+        for (int p = 0; p < 4; ++p)
+          tc::tma_load_3d(st + p * A_PLANE_BYTES, &tmA, &full_bar[s], kx, (int)m0, p);
+        for (int b = 0; b < 6; ++b)
+          tc::tma_load_3d(st + A_STAGE_BYTES + b * B_BLOCK_BYTES, &tmB, &full_bar[s], kx, (int)n0, b);
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      const uint32_t idesc = tc::idesc_bf16(MT, 2 * NT);
+      bool ok = true;
+      for (int kt = 0; kt < ktiles; ++kt) {
+        const int s = kt % STAGES;
+        if (!tc::mbar_wait_abortable(&full_bar[s], (kt / STAGES) & 1, WAIT_CYCLES, vstatus)) {
+          atomicExch(g.status, PTN_ERR_TIMEOUT);
+          ok = false;
+          break;
+        }
+        tc::fence_after();
+        const uint32_t sa = tc::smem_u32(smem + s * STAGE_BYTES);
+        const uint32_t sb = sa + A_STAGE_BYTES;
+#pragma unroll
+        for (int kk = 0; kk < KT / 16; ++kk) {
+          const uint32_t ko = kk * 32;
+          // A planes: 0 Ar_hi, 1 Ai_hi, 2 Ar_lo, 3 Ai_lo
+          // B windows: level L at sb + L*3*B_BLOCK; top = +B_BLOCK ([Br; Bi]), bot = +0 ([-Bi; Br])
+          const uint64_t arh = tc::sdesc_sw128(sa + 0 * A_PLANE_BYTES + ko);
+          const uint64_t aih = tc::sdesc_sw128(sa + 1 * A_PLANE_BYTES + ko);
+          const uint64_t arl = tc::sdesc_sw128(sa + 2 * A_PLANE_BYTES + ko);
+          const uint64_t ail = tc::sdesc_sw128(sa + 3 * A_PLANE_BYTES + ko);
+          const uint64_t bht = tc::sdesc_sw128(sb + 1 * B_BLOCK_BYTES + ko);
+          const uint64_t bhb = tc::sdesc_sw128(sb + 0 * B_BLOCK_BYTES + ko);
+          const uint64_t blt = tc::sdesc_sw128(sb + 4 * B_BLOCK_BYTES + ko);
+          const uint64_t blb = tc::sdesc_sw128(sb + 3 * B_BLOCK_BYTES + ko);
+          const uint32_t first = (kt == 0 && kk == 0) ? 0u : 1u;
+          tc::mma_bf16(tmem, arh, bht, idesc, first);
+          tc::mma_bf16(tmem, aih, bhb, idesc, 1u);
+          tc::mma_bf16(tmem, arh, blt, idesc, 1u);
+          tc::mma_bf16(tmem, aih, blb, idesc, 1u);
+          tc::mma_bf16(tmem, arl, bht, idesc, 1u);
+          tc::mma_bf16(tmem, ail, bhb, idesc, 1u);
+        }
+        tc::mma_commit(&empty_bar[s]);
+      }
+      if (ok) tc::mma_commit(&done_bar);
+    }
+  } else {
+    // ---------------- epilogue (warps 2..5) ----------------
+    const int q = warp & 3;                 // TMEM lane quarter of this warp
+    const int row = q * 32 + lane;
+    const int64_t m = m0 + row;
+    bool ok = tc::mbar_wait_abortable(&done_bar, 0, WAIT_CYCLES, vstatus);
+    tc::fence_after();
+    if (!ok) {
+      if (lane == 0) atomicExch(g.status, PTN_ERR_TIMEOUT);
+    } else {
+      const int64_t moff = (m < g.M) ? decode_off(g.mo, m) : -1;
+      const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16);
+#pragma unroll 1
+      for (int j0 = 0; j0 < NT; j0 += 16) {
+        float re[16], im[16];
+        tc::tmem_ld16(tbase + (uint32_t)j0, re);
+        tc::tmem_ld16(tbase + (uint32_t)(NT + j0), im);
+        if (moff < 0) continue;
+        if (g.out_kind == 0) {
+          double2* C = static_cast<double2*>(g.C);
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            const int64_t no = noff[j0 + i];
+            if (no >= 0) C[moff + no] = make_double2((double)re[i], (double)im[i]);
+          }
+        } else {
+          __nv_bfloat16* C = static_cast<__nv_bfloat16*>(g.C);
+          const int64_t ps = g.c_plane;
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            const int64_t no = noff[j0 + i];
+            if (no < 0) continue;
+            const __nv_bfloat16 rh = __float2bfloat16_rn(re[i]);
+            const __nv_bfloat16 ih = __float2bfloat16_rn(im[i]);
+            const __nv_bfloat16 rl = __float2bfloat16_rn(re[i] - __bfloat162float(rh));
+            const __nv_bfloat16 il = __float2bfloat16_rn(im[i] - __bfloat162float(ih));
+            const int64_t o = moff + no;
+            C[o] = rh;
+            C[ps + o] = ih;
+            C[2 * ps + o] = rl;
+            C[3 * ps + o] = il;
+          }
+        }
+      }
+    }
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 1) tc::tmem_dealloc(tmem, 2 * NT);
+}
+
+// ---- tensor maps ---------------------------------------------------------------------
+// cuTensorMapEncodeTiled is fetched through the runtime's driver entry point so
+// the library does not link libcuda (it still loads on a machine without a driver).
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+int make_map_3d(CUtensorMap* map, const void* base, uint64_t d0, uint64_t d1, uint64_t d2, uint64_t s1_bytes,
+                uint64_t s2_bytes, uint32_t b0, uint32_t b1) {
+  cuuint64_t dims[3] = {d0, d1, d2};
+  cuuint64_t strides[2] = {s1_bytes, s2_bytes};
+  cuuint32_t box[3] = {b0, b1, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
+  if (!enc) return PTN_ERR_LAUNCH;
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims,
+                                      strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                      CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? PTN_OK : PTN_ERR_ARG;
+}
+
+// ---- conversions ---------------------------------------------------------------------
+// planes[p][m * lda + k] <- split(src[off_m(m) + off_k(k)]) for the complex128 source.
+__global__ void to_planes_kernel(const double2* __restrict__ src, OutModes mm, OutModes km, int64_t M, int64_t K,
+                                 int64_t lda, int64_t plane, int conj, __nv_bfloat16* __restrict__ dst) {
+  const int64_t total = M * K;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t m = e / K, k = e - (e / K) * K;
+    double2 v = src[decode_off(mm, m) + decode_off(km, k)];
+    if (conj) v.y = -v.y;
+    const __nv_bfloat16 rh = __double2bfloat16(v.x);
+    const __nv_bfloat16 ih = __double2bfloat16(v.y);
+    const __nv_bfloat16 rl = __double2bfloat16(v.x - (double)__bfloat162float(rh));
+    const __nv_bfloat16 il = __double2bfloat16(v.y - (double)__bfloat162float(ih));
+    const int64_t o = m * lda + k;
+    dst[o] = rh;
+    dst[plane + o] = ih;
+    dst[2 * plane + o] = rl;
+    dst[3 * plane + o] = il;
+  }
+}
+
+// Bx[level][block][n][k]: block 0 = -Bi, 1 = Br, 2 = Bi; level 0 = hi, 1 = lo.
+__global__ void expand_b_kernel(const double2* __restrict__ src, OutModes nm, OutModes km, int64_t N, int64_t K,
+                                int64_t ldb, int conj, __nv_bfloat16* __restrict__ dst) {
+  const int64_t total = N * K;
+  const int64_t blk = N * ldb;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t n = e / K, k = e - (e / K) * K;
+    double2 v = src[decode_off(nm, n) + decode_off(km, k)];
+    if (conj) v.y = -v.y;
+    const __nv_bfloat16 rh = __double2bfloat16(v.x);
+    const __nv_bfloat16 ih = __double2bfloat16(v.y);
+    const __nv_bfloat16 rl = __double2bfloat16(v.x - (double)__bfloat162float(rh));
+    const __nv_bfloat16 il = __double2bfloat16(v.y - (double)__bfloat162float(ih));
+    const int64_t o = n * ldb + k;
+    dst[0 * blk + o] = __hneg(ih);
+    dst[1 * blk + o] = rh;
+    dst[2 * blk + o] = ih;
+    dst[3 * blk + o] = __hneg(il);
+    dst[4 * blk + o] = rl;
+    dst[5 * blk + o] = il;
+  }
+}
+
+int fill_out(const ptn_modes& src, OutModes& dst) {
+  if (src.n < 0 || src.n > PTN_MAX_MODES) return PTN_ERR_ARG;
+  dst.n = src.n;
+  for (int i = 0; i < src.n; ++i) {
+    if (src.dim[i] <= 0) return PTN_ERR_ARG;
+    dst.dim[i] = src.dim[i];
+    dst.stride[i] = src.stride_c[i];
+  }
+  return PTN_OK;
+}
+
+int fill_src(const ptn_modes& src, OutModes& dst, int64_t& total) {
+  if (src.n < 0 || src.n > PTN_MAX_MODES) return PTN_ERR_ARG;
+  dst.n = src.n;
+  total = 1;
+  for (int i = 0; i < src.n; ++i) {
+    if (src.dim[i] <= 0) return PTN_ERR_ARG;
+    dst.dim[i] = src.dim[i];
+    dst.stride[i] = src.stride_a[i];
+    total *= src.dim[i];
+  }
+  return PTN_OK;
+}
+
+unsigned grid_for(int64_t n) {
+  int64_t b = (n + 255) / 256;
+  if (b < 1) b = 1;
+  if (b > 4096) b = 4096;
+  return (unsigned)b;
+}
+
+}  // namespace
+
+extern "C" int ptn_cgemm_smem_bytes(void) { return SMEM_BYTES; }
+
+extern "C" int ptn_cgemm_bf16x3(const ptn_cgemm_desc* d, void* stream) {
+  if (!d || !d->A || !d->Bx || !d->C || !d->status) return PTN_ERR_ARG;
+  if (d->M < 1 || d->N < 1 || d->K < 1) return PTN_ERR_ARG;
+  if (d->lda % 8 || d->ldb % 8 || d->lda < d->K || d->ldb < d->K) return PTN_ERR_ARG;
+  if (d->a_plane % 8 || (reinterpret_cast<uintptr_t>(d->A) & 15) || (reinterpret_cast<uintptr_t>(d->Bx) & 15))
+    return PTN_ERR_ARG;
+  if (d->M > 0x7fffffffLL || d->N > 0x7fffffffLL) return PTN_ERR_UNSUPPORTED;
+  GemmArgs g;
+  g.M = d->M;
+  g.N = d->N;
+  g.K = d->K;
+  g.out_kind = d->out_kind;
+  g.C = d->C;
+  g.c_plane = d->c_plane;
+  g.status = d->status;
+  if (fill_out(d->m_out, g.mo) || fill_out(d->n_out, g.no)) return PTN_ERR_ARG;
+  CUtensorMap ta, tb;
+  if (make_map_3d(&ta, d->A, (uint64_t)d->K, (uint64_t)d->M, 4, (uint64_t)d->lda * 2, (uint64_t)d->a_plane * 2, KT,
+                  MT))
+    return PTN_ERR_ARG;
+  if (make_map_3d(&tb, d->Bx, (uint64_t)d->K, (uint64_t)d->N, 6, (uint64_t)d->ldb * 2,
+                  (uint64_t)d->N * (uint64_t)d->ldb * 2, KT, NT))
+    return PTN_ERR_ARG;
+  const int64_t tm = (d->M + MT - 1) / MT, tn = (d->N + NT - 1) / NT;
+  g.tiles_n = tn;
+  if (tm * tn > 0x7fffffffLL) return PTN_ERR_UNSUPPORTED;
+  static bool attr_set = false;
+  if (!attr_set) {
+    if (cudaFuncSetAttribute(cgemm_bf16x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) !=
+        cudaSuccess)
+      return PTN_ERR_LAUNCH;
+    attr_set = true;
+  }
+  PTN_COUNT(1);
+  cgemm_bf16x3_kernel<<<(unsigned)(tm * tn), THREADS, SMEM_BYTES, ptn_stream(stream)>>>(ta, tb, g);
+  return ptn_launch_status();
+}
+
+extern "C" int ptn_to_planes(const ptn_convert_desc* d, void* stream) {
+  if (!d || !d->src || !d->dst) return PTN_ERR_ARG;
+  OutModes mm, km;
+  int64_t M, K;
+  if (fill_src(d->rows, mm, M) || fill_src(d->cols, km, K)) return PTN_ERR_ARG;
+  if (d->ld < K) return PTN_ERR_ARG;
+  PTN_COUNT(1);
+  to_planes_kernel<<<grid_for(M * K), 256, 0, ptn_stream(stream)>>>(
+      static_cast<const double2*>(d->src), mm, km, M, K, d->ld, d->plane, d->conj,
+      static_cast<__nv_bfloat16*>(d->dst));
+  return ptn_launch_status();
+}
+
+extern "C" int ptn_expand_b(const ptn_convert_desc* d, void* stream) {
+  if (!d || !d->src || !d->dst) return PTN_ERR_ARG;
+  OutModes nm, km;
+  int64_t N, K;
+  if (fill_src(d->rows, nm, N) || fill_src(d->cols, km, K)) return PTN_ERR_ARG;
+  if (d->ld < K) return PTN_ERR_ARG;
+  PTN_COUNT(1);
+  expand_b_kernel<<<grid_for(N * K), 256, 0, ptn_stream(stream)>>>(
+      static_cast<const double2*>(d->src), nm, km, N, K, d->ld, d->conj, static_cast<__nv_bfloat16*>(d->dst));
+  return ptn_launch_status();
+}

@@ -183,6 +183,7 @@ class ChainBuilder:
     def __init__(self, ws: Workspace):
         self.ws = ws
         self.steps = []
+        self.logical = []
         self.sizes = {}
         self.slot = 0
 
@@ -196,10 +197,162 @@ class ChainBuilder:
             out = Operand.contiguous(("ws", name), mlab + nlab, dims)
             self.sizes[name] = max(self.sizes.get(name, 0), out.numel())
         self.steps.append(Step(A, B, klabels, out, **kw))
+        self.logical.append((A, B, list(klabels), out, kw))
         return out
 
     def plan(self) -> Plan:
         return Plan(self.ws, self.steps, self.sizes)
+
+    def mixed_plan(self) -> "MixedPlan":
+        return MixedPlan(self.ws, self.logical)
+
+
+def _modes_single(dims, strides):
+    """Merge adjacent modes contiguous in one layout; drop unit modes."""
+    od, os_ = [], []
+    for d, st in zip(dims, strides):
+        if d == 1:
+            continue
+        if od and os_[-1] == st * d:
+            od[-1] *= d
+            os_[-1] = st
+        else:
+            od.append(d)
+            os_.append(st)
+    return od, os_
+
+
+def _set_modes(modes, dims, strides, field):
+    dims, strides = _modes_single(dims, strides)
+    if len(dims) > MAX_MODES:
+        raise ValueError("too many modes")
+    modes.n = len(dims)
+    for i, (d, st) in enumerate(zip(dims, strides)):
+        modes.dim[i] = d
+        getattr(modes, field)[i] = st
+
+
+def _round8(x):
+    return (x + 7) // 8 * 8
+
+
+class MixedPlan:
+    """The same contraction chain on the tensor cores (BF16x3, FP32 accumulation).
+
+    Every step is ``ptn_cgemm_bf16x3`` with both operands K-major. The running
+    tensor is kept as BF16 hi/lo planes whose layout is chosen for the step that
+    reads it: [rows = that step's free legs][cols = its contracted legs]; each
+    GEMM's epilogue writes straight into that layout, and the last one writes
+    complex128 into the destination. Small operands (environments, TTNO
+    tensors, the conjugate site tensor) are expanded per call by
+    ``ptn_expand_b``; the first operand is gathered by ``ptn_to_planes``.
+    """
+
+    def __init__(self, ws: Workspace, logical):
+        from ._lib import CgemmDesc, ConvertDesc
+        self.ws = ws
+        self.ops = []            # ("conv"|"expand"|"gemm", desc, refs)
+        self.sizes = {}          # ws name -> (numel, dtype)
+        self.flops = 0
+        nsteps = len(logical)
+        prev_layout = None       # for step i>0: (slot, label -> stride, lda, plane)
+        for i, (A, B, kl, out, kw) in enumerate(logical):
+            mlab = [l for l in A.labels if l not in kl]
+            nlab = [l for l in B.labels if l not in kl]
+            dimA = dict(zip(A.labels, A.dims))
+            dimB = dict(zip(B.labels, B.dims))
+            M = int(np.prod([dimA[l] for l in mlab] or [1]))
+            N = int(np.prod([dimB[l] for l in nlab] or [1]))
+            K = int(np.prod([dimA[l] for l in kl] or [1]))
+            self.flops += 8 * M * N * K
+            lda = _round8(K)
+            aslot = f"mp{i % 2}"
+            plane = M * lda
+            if i == 0:
+                d = ConvertDesc()
+                _set_modes(d.rows, [dimA[l] for l in mlab], [A.strides[A.labels.index(l)] for l in mlab], "stride_a")
+                _set_modes(d.cols, [dimA[l] for l in kl], [A.strides[A.labels.index(l)] for l in kl], "stride_a")
+                d.ld, d.plane, d.conj = lda, plane, int(kw.get("conj_a", False))
+                self.ops.append(("conv", d, (A.ref, ("ws", aslot))))
+                self._need(aslot, 4 * plane)
+            else:
+                # the previous GEMM already wrote this step's A in [mlab][kl] order
+                assert prev_layout[0] == aslot and prev_layout[2] == lda
+            ldb = _round8(K)
+            d = ConvertDesc()
+            _set_modes(d.rows, [dimB[l] for l in nlab], [B.strides[B.labels.index(l)] for l in nlab], "stride_a")
+            _set_modes(d.cols, [dimB[l] for l in kl], [B.strides[B.labels.index(l)] for l in kl], "stride_a")
+            d.ld, d.plane, d.conj = ldb, 0, int(kw.get("conj_b", False))
+            self.ops.append(("expand", d, (B.ref, ("ws", "bx"))))
+            self._need("bx", 6 * N * ldb)
+            g = CgemmDesc()
+            g.lda, g.a_plane, g.M, g.K, g.ldb, g.N = lda, plane, M, K, ldb, N
+            if i < nsteps - 1:
+                nA, nB, nkl, _, _ = logical[i + 1]
+                nm = [l for l in nA.labels if l not in nkl]
+                ndim = dict(zip(nA.labels, nA.dims))
+                nK = int(np.prod([ndim[l] for l in nkl] or [1]))
+                nM = int(np.prod([ndim[l] for l in nm] or [1]))
+                nlda = _round8(nK)
+                stride = {}
+                s_ = 1
+                for l in reversed(nkl):
+                    stride[l] = s_
+                    s_ *= ndim[l]
+                s_ = nlda
+                for l in reversed(nm):
+                    stride[l] = s_
+                    s_ *= ndim[l]
+                cslot = f"mp{(i + 1) % 2}"
+                g.out_kind = 1
+                g.c_plane = nM * nlda
+                self._need(cslot, 4 * nM * nlda)
+                _set_modes(g.m_out, [dimA[l] for l in mlab], [stride[l] for l in mlab], "stride_c")
+                _set_modes(g.n_out, [dimB[l] for l in nlab], [stride[l] for l in nlab], "stride_c")
+                prev_layout = (cslot, stride, nlda, nM * nlda)
+                self.ops.append(("gemm", g, (("ws", aslot), ("ws", "bx"), ("ws", cslot))))
+            else:
+                g.out_kind = 0
+                g.c_plane = 0
+                _set_modes(g.m_out, [dimA[l] for l in mlab], [out.strides[out.labels.index(l)] for l in mlab],
+                           "stride_c")
+                _set_modes(g.n_out, [dimB[l] for l in nlab], [out.strides[out.labels.index(l)] for l in nlab],
+                           "stride_c")
+                self.ops.append(("gemm", g, (("ws", aslot), ("ws", "bx"), out.ref)))
+
+    def _need(self, name, numel):
+        self.sizes[name] = max(self.sizes.get(name, 0), numel)
+
+    def run(self, x_ptr: int = 0, y_ptr: int = 0):
+        lib = _lib.load()
+        for name, n in self.sizes.items():
+            self.ws.get(name, n + 64, torch.bfloat16)
+        status = self.ws.bufs.get("tc_status")
+        if status is None:
+            status = torch.zeros(1, dtype=torch.int32, device=self.ws.device)
+            self.ws.bufs["tc_status"] = status
+        stream = _stream_ptr()
+
+        def ptr(ref):
+            kind = ref[0]
+            if kind == "fixed":
+                return ref[1].data_ptr()
+            if kind == "in":
+                return x_ptr
+            if kind == "out":
+                return y_ptr
+            return self.ws.ptr(ref[1])
+        for kind, d, refs in self.ops:
+            if kind == "conv":
+                d.src, d.dst = ptr(refs[0]), ptr(refs[1])
+                check(lib.ptn_to_planes(ctypes.byref(d), stream), "ptn_to_planes")
+            elif kind == "expand":
+                d.src, d.dst = ptr(refs[0]), ptr(refs[1])
+                check(lib.ptn_expand_b(ctypes.byref(d), stream), "ptn_expand_b")
+            else:
+                d.A, d.Bx, d.C = ptr(refs[0]), ptr(refs[1]), ptr(refs[2])
+                d.status = status.data_ptr()
+                check(lib.ptn_cgemm_bf16x3(ctypes.byref(d), stream), "ptn_cgemm_bf16x3")
 
 
 # ----------------------------------------------------------------------------
@@ -314,7 +467,10 @@ class KrylovSolver:
 class DeviceNetwork:
     """Device copy of a TTNS (+ TTNO) with environment buffers and cached plans."""
 
-    def __init__(self, state, hamiltonian=None, device=None):
+    def __init__(self, state, hamiltonian=None, device=None, precision: str = "plain"):
+        if precision not in ("plain", "mixed"):
+            raise ValueError("precision must be 'plain' (complex128) or 'mixed' (BF16x3 tensor cores)")
+        self.precision = precision
         _lib.load()
         if not torch.cuda.is_available():
             raise RuntimeError("pytreenet_gb300 needs a CUDA device (no CPU fallback)")
@@ -403,9 +559,8 @@ class DeviceNetwork:
             else:
                 T = cb.contract(T, E, [f"a{k}", f"b{k}"])
         if not rest:
-            # leafless case cannot happen for n >= 1; W was the last step
             raise RuntimeError("site without neighbours")
-        p = cb.plan()
+        p = cb.mixed_plan() if self.precision == "mixed" else cb.plan()
         self.plans[key] = p
         return p
 
@@ -427,7 +582,7 @@ class DeviceNetwork:
                                [f"c{k}" if k != k0 else "z" for k in range(n)] + ["t"], shape)
         E = self._env_op(nid, nxt, [f"a{k0}", f"b{k0}", "z"])
         cb.contract(T, B, [f"c{k}" for k in range(n) if k != k0] + ["t"], out=E, conj_b=True)
-        p = cb.plan()
+        p = cb.mixed_plan() if self.precision == "mixed" else cb.plan()
         self.plans[key] = p
         return p
 
@@ -475,6 +630,14 @@ class DeviceNetwork:
             self.flops += p.flops
         x = self.t[nid]
         self.krylov.expm(x, apply, dt, exp_factor, tol, maxdim, out=x)
+        self.check_device_status()
+
+    def check_device_status(self):
+        st = self.ws.bufs.get("tc_status")
+        if st is not None and int(st.item()) != 0:
+            code = int(st.item())
+            st.zero_()
+            raise _lib.PtnError(code, "tensor-core contraction")
 
     def evolve_bond(self, r: torch.Tensor, nid, nxt, dt, exp_factor, tol, maxdim):
         p = self.bond_plan(nid, nxt)
@@ -582,6 +745,39 @@ class DeviceNetwork:
         st.orthogonality_center_id = center
 
     # -- observables ------------------------------------------------------------------
+    def overlap(self, other: "DeviceNetwork") -> complex:
+        """<self|other> for two states on the same tree (``contract_two_ttns``,
+        ``contractions/state_state_contraction.py:29-66``)."""
+        st = self.state
+
+        def rec(nid, toward):
+            shape = self.shape(nid)
+            n = len(shape) - 1
+            nb = self.nbrs(nid)
+            cb = ChainBuilder(self.ws)
+            T = Operand.contiguous(("fixed", other.t[nid]), [f"a{k}" for k in range(n)] + ["s"], shape)
+            for k, x in enumerate(nb):
+                if x == toward:
+                    continue
+                sub = rec(x, nid)
+                T = cb.contract(T, Operand.contiguous(("fixed", sub), [f"a{k}", f"c{k}"], list(sub.shape)),
+                                [f"a{k}"])
+            B = Operand.contiguous(("fixed", self.t[nid]),
+                                   [f"c{k}" if nb[k] != toward else "z" for k in range(n)] + ["s"], shape)
+            if toward is None:
+                res = torch.zeros((1,), dtype=CDT, device=self.device)
+                cb.contract(T, B, [f"c{k}" for k in range(n)] + ["s"], out=Operand(("fixed", res), [], [], []),
+                            conj_b=True)
+            else:
+                k0 = nb.index(toward)
+                res = torch.zeros((shape[k0], shape[k0]), dtype=CDT, device=self.device)
+                cb.contract(T, B, [f"c{k}" for k in range(n) if k != k0] + ["s"],
+                            out=Operand.contiguous(("fixed", res), [f"a{k0}", "z"], [shape[k0]] * 2), conj_b=True)
+            cb.plan().run()
+            return res
+        return complex(rec(st.root_id, None).cpu().numpy()[0])
+
+
     def expect_local(self, ops: dict) -> complex:
         """<psi| prod_i O_i |psi> for single-site operators
         (``TTNS.tensor_product_expectation_value``, ``ttns/ttns.py:240-264``)."""

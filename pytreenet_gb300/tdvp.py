@@ -137,7 +137,7 @@ class OneSiteTDVP:
 
     def __init__(self, initial_state: TreeTensorNetworkState, hamiltonian: TreeTensorNetworkOperator,
                  time_step_size: float, final_time: float, operators, config: TDVPConfig | None = None,
-                 solver_options: dict[str, Any] | None = None):
+                 solver_options: dict[str, Any] | None = None, precision: str = "plain"):
         if len(initial_state.nodes) != len(hamiltonian.nodes):
             raise AssertionError("state and Hamiltonian must have the same nodes")
         if time_step_size <= 0 or final_time <= 0:
@@ -164,7 +164,8 @@ class OneSiteTDVP:
         self.update_path = leaf_to_root_update_path(self._initial_state)
         self.orthogonalization_path = [self.state.path_from_to(self.update_path[i], self.update_path[i + 1])[1:]
                                        for i in range(len(self.update_path) - 1)]
-        self.net = DeviceNetwork(self.state, hamiltonian)
+        self.precision = precision
+        self.net = DeviceNetwork(self.state, hamiltonian, precision=precision)
         if self.state.orthogonality_center_id is None:
             self.net.canonical_form(self.update_path[0])
         else:

@@ -128,3 +128,105 @@ def install(monkeypatch):
     monkeypatch.setattr(E, "DEFAULT_DEVICE", "cpu")
     monkeypatch.setattr(torch.cuda, "is_available", lambda: True)
     return fake
+
+
+# ---- mixed-precision entry points (BF16 hi/lo splits emulated in NumPy) ----------
+def _bf16_bits(x):
+    """float64 -> bf16 bit patterns (round to nearest even), as uint16."""
+    f = np.asarray(x, dtype=np.float32).view(np.uint32)
+    rounded = f + 0x7FFF + ((f >> 16) & 1)
+    return (rounded >> 16).astype(np.uint16)
+
+
+def _bf16_val(bits):
+    return (bits.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+
+
+def _split(v):
+    hi = _bf16_bits(v)
+    lo = _bf16_bits(v - _bf16_val(hi))
+    return hi, lo
+
+
+def _modes(m, field):
+    return [m.dim[i] for i in range(m.n)], [getattr(m, field)[i] for i in range(m.n)]
+
+
+def _offsets(dims, strides):
+    idx = np.zeros(1, dtype=np.int64)
+    for d, s in zip(dims, strides):
+        idx = (idx[:, None] + np.arange(d, dtype=np.int64)[None, :] * s).reshape(-1)
+    return idx
+
+
+def _gather(ptr, rows, cols, conj):
+    rd, rs = _modes(rows, "stride_a")
+    cd, cs = _modes(cols, "stride_a")
+    ro, co = _offsets(rd, rs), _offsets(cd, cs)
+    ext = int(ro.max() + co.max()) + 1
+    src = _view(ptr, ext)
+    v = src[ro[:, None] + co[None, :]]
+    return v.conj() if conj else v
+
+
+def _fake_to_planes(self, d_ref, stream):
+    d = d_ref._obj
+    v = _gather(d.src, d.rows, d.cols, d.conj)
+    M, K = v.shape
+    dst = _view(d.dst, 3 * d.plane + M * d.ld, np.uint16)
+    for p, part in enumerate([v.real, v.imag]):
+        hi, lo = _split(part)
+        for lvl, arr in ((0, hi), (1, lo)):
+            plane = (2 * lvl + p) * d.plane
+            blk = dst[plane:plane + M * d.ld].reshape(M, d.ld)
+            blk[:, :K] = arr
+    return 0
+
+
+def _fake_expand_b(self, d_ref, stream):
+    d = d_ref._obj
+    v = _gather(d.src, d.rows, d.cols, d.conj)
+    N, K = v.shape
+    blk = N * d.ld
+    dst = _view(d.dst, 6 * blk, np.uint16)
+    rh, rl = _split(v.real)
+    ih, il = _split(v.imag)
+    for b, arr in enumerate([_bf16_bits(-_bf16_val(ih)), rh, ih, _bf16_bits(-_bf16_val(il)), rl, il]):
+        dst[b * blk:(b + 1) * blk].reshape(N, d.ld)[:, :K] = arr
+    return 0
+
+
+def _fake_cgemm(self, d_ref, stream):
+    d = d_ref._obj
+    M, K, N = d.M, d.K, d.N
+    a = _view(d.A, 3 * d.a_plane + M * d.lda, np.uint16)
+
+    def plane(p):
+        return _bf16_val(a[p * d.a_plane:p * d.a_plane + M * d.lda].reshape(M, d.lda)[:, :K])
+    A = (plane(0) + plane(2)) + 1j * (plane(1) + plane(3))
+    b = _view(d.Bx, 6 * N * d.ldb, np.uint16)
+
+    def blk(i):
+        return _bf16_val(b[i * N * d.ldb:(i + 1) * N * d.ldb].reshape(N, d.ldb)[:, :K])
+    B = (blk(1) + blk(4)) + 1j * (blk(2) + blk(5))
+    C = A @ B.T
+    md, ms = _modes(d.m_out, "stride_c")
+    nd, ns = _modes(d.n_out, "stride_c")
+    off = _offsets(md, ms)[:, None] + _offsets(nd, ns)[None, :]
+    C = C.astype(np.complex64).astype(np.complex128)
+    if d.out_kind == 0:
+        out = _view(d.C, int(off.max()) + 1)
+        out[off] = C
+    else:
+        out = _view(d.C, 3 * d.c_plane + int(off.max()) + 1, np.uint16)
+        for p, part in enumerate([C.real, C.imag]):
+            hi, lo = _split(part)
+            out[(0 + p) * d.c_plane + off] = hi
+            out[(2 + p) * d.c_plane + off] = lo
+    return 0
+
+
+FakeLib.ptn_to_planes = _fake_to_planes
+FakeLib.ptn_expand_b = _fake_expand_b
+FakeLib.ptn_cgemm_bf16x3 = _fake_cgemm
+FakeLib.ptn_launch_counter = lambda self: 0

@@ -52,3 +52,24 @@ def test_engine_host_c1_padded(monkeypatch):
     fake_ptn.install(monkeypatch)
     c, out, zerr = _run_case("c1_binary15_tfim_chi8", steps=10)
     assert zerr < 2e-8
+
+
+@pytest.mark.parametrize("name", ["ttree3_heis_chi6_o1", "ternary2_xxz_chi4_o1", "binary7_tfim_chi4_o2"])
+def test_engine_host_mixed_layouts(monkeypatch, name):
+    """The tensor-core plans (operand layouts chosen per step, epilogue strides)
+    give the reference's result up to BF16x3 rounding."""
+    fake_ptn.install(monkeypatch)
+    import pytreenet_gb300 as P
+    import oracle as O
+    c = load_case(name)
+    st = build_ttn(P.TTNS, c["spec"], c["init"])
+    H = build_ttn(P.TTNO, c["spec"], c["ttno"])
+    cls = P.FirstOrderOneSiteTDVP if c["order"] == 1 else P.SecondOrderOneSiteTDVP
+    algo = cls(st, H, c["dt"], c["dt"] * c["steps"], {},
+               config=P.TDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV),
+               solver_options={"krylov_tol": c["krylov_tol"]}, precision="mixed")
+    for _ in range(c["steps"]):
+        algo.run_one_time_step()
+    got = O.OState(oracle_state(c).tree, {nid: algo.state.get_phys_numpy(nid) for nid, _ in c["spec"]})
+    one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), got)
+    assert one_minus_f < 1e-8

@@ -1,0 +1,100 @@
+"""Tensor-core (tcgen05, BF16x3) contraction path on the GPU."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+RNG = np.random.default_rng(21)
+
+
+def crandn(*shape):
+    return (RNG.normal(size=shape) + 1j * RNG.normal(size=shape)) / np.sqrt(2)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from pytreenet_gb300 import _lib, build
+    build.build()
+    return _lib.load()
+
+
+def _bf16_round(x):
+    return torch.from_numpy(np.ascontiguousarray(x, dtype=np.float32)).to(torch.bfloat16)
+
+
+def test_tcgen05_descriptor_selftest(lib):
+    from pytreenet_gb300.engine import _stream_ptr
+    A = _bf16_round(RNG.normal(size=(128, 64)))
+    B = _bf16_round(RNG.normal(size=(128, 64)))
+    D = torch.zeros((128, 128), dtype=torch.float32, device="cuda")
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    assert lib.ptn_tc_selftest(A.cuda().data_ptr(), B.cuda().data_ptr(), D.data_ptr(), st.data_ptr(),
+                               _stream_ptr()) == 0
+    torch.cuda.synchronize()
+    assert int(st.item()) == 0
+    ref = A.float().numpy() @ B.float().numpy().T
+    assert np.max(np.abs(D.cpu().numpy() - ref)) < 1e-3
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 64, 64), (200, 70, 100), (1000, 130, 256), (4096, 512, 1280),
+                                   (37, 5, 10), (131072 // 32, 256, 256)])
+def test_cgemm_bf16x3_matches_complex128(lib, M, N, K):
+    """C = A B^T with the BF16x3 split: error ~ 2^-16 relative to |A||B| per term."""
+    from pytreenet_gb300.engine import Operand, ChainBuilder, Workspace
+    A, B = crandn(M, K), crandn(N, K)
+    Ad = torch.from_numpy(A).cuda()
+    Bd = torch.from_numpy(B).cuda()
+    C = torch.zeros((M, N), dtype=torch.complex128, device="cuda")
+    ws = Workspace("cuda")
+    cb = ChainBuilder(ws)
+    cb.contract(Operand.contiguous(("fixed", Ad), ["m", "k"], [M, K]),
+                Operand.contiguous(("fixed", Bd), ["n", "k"], [N, K]), ["k"],
+                out=Operand.contiguous(("fixed", C), ["m", "n"], [M, N]))
+    p = cb.mixed_plan()
+    p.run()
+    torch.cuda.synchronize()
+    assert int(ws.bufs["tc_status"].item()) == 0
+    ref = A @ B.T
+    err = np.max(np.abs(C.cpu().numpy() - ref)) / np.sqrt(K)
+    assert err < 5e-5, err
+
+
+def test_cgemm_chain_matches_fp64_plan(lib):
+    """A three-step chain (the degree-2 site matvec) on both paths."""
+    import pytreenet_gb300 as P
+    from pytreenet_gb300.workloads import t_tree_state, t_tree_heisenberg
+    from pytreenet_gb300.engine import DeviceNetwork
+    st, spec, tensors = t_tree_state(arm_len=3, chi=32, seed=2)
+    H, _ = t_tree_heisenberg(st, seed=3)
+    outs = {}
+    for prec in ("plain", "mixed"):
+        st2, _, _ = t_tree_state(arm_len=3, chi=32, seed=2)
+        net = DeviceNetwork(st2, H, precision=prec)
+        st2.orthogonality_center_id = None
+        net.canonical_form("a0_1")
+        net.init_cache_but_one("a0_1")
+        x = net.t["a0_1"].clone()
+        y = torch.zeros_like(x)
+        net.heff_plan("a0_1").run(x.data_ptr(), y.data_ptr())
+        torch.cuda.synchronize()
+        outs[prec] = y.cpu().numpy()
+    rel = np.linalg.norm(outs["mixed"] - outs["plain"]) / np.linalg.norm(outs["plain"])
+    assert rel < 1e-4, rel
+
+
+@pytest.mark.parametrize("name", ["ttree3_heis_chi6_o1", "ternary2_xxz_chi4_o1"])
+def test_gpu_mixed_tdvp_matches_reference(name):
+    import oracle as O
+    import pytreenet_gb300 as P
+    from golden_util import build_ttn, load_case, oracle_state, fidelity_and_dist
+    c = load_case(name)
+    st = build_ttn(P.TTNS, c["spec"], c["init"])
+    H = build_ttn(P.TTNO, c["spec"], c["ttno"])
+    algo = P.FirstOrderOneSiteTDVP(st, H, c["dt"], c["dt"] * c["steps"], {},
+                                   config=P.TDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV),
+                                   solver_options={"krylov_tol": c["krylov_tol"]}, precision="mixed")
+    for _ in range(c["steps"]):
+        algo.run_one_time_step()
+    got = O.OState(oracle_state(c).tree, {nid: algo.state.get_phys_numpy(nid) for nid, _ in c["spec"]})
+    one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), got)
+    assert one_minus_f < 1e-8

@@ -107,12 +107,14 @@ int ptn_zqr_keep(void* A, const int64_t* rowoff, int64_t m, int64_t k, int64_t c
 
 /* ---- Mixed precision (tcgen05 tensor cores, BF16x3, FP32 accumulation) -------
  * C[m, n] = sum_k A[m, k] * B[n, k] over complex numbers; A and B are given as
- * BF16 hi/lo splits. A: 4 planes (Re hi, Im hi, Re lo, Im lo), plane p at
- * A + p * a_plane, row m at m * lda (lda, a_plane multiples of 8, 16-byte
- * aligned base). Bx: bf16 [2 levels][3 blocks (-Im, Re, Im)][N][ldb] as
- * written by ptn_expand_b. The result is written through m_out / n_out
- * (dims + stride_c): out_kind 0 = complex128 at C, 1 = BF16 hi/lo planes at C
- * with plane stride c_plane. status: device int32, set on a device-side timeout.
+ * `levels` BF16 pieces (2: ~16-bit mantissa, products i+j<2 = "BF16x3";
+ * 3: ~24-bit, products i+j<3 = "BF16x6"). A: 2*levels planes (Re_0, Im_0,
+ * Re_1, Im_1, ...), plane p at A + p * a_plane, row m at m * lda (lda, a_plane
+ * multiples of 8, 16-byte aligned base). Bx: bf16 [levels][3 blocks
+ * (-Im, Re, Im)][N][ldb] as written by ptn_expand_b. The result is written
+ * through m_out / n_out (dims + stride_c): out_kind 0 = complex128 at C,
+ * 1 = BF16 level planes at C with plane stride c_plane. status: device int32,
+ * set on a device-side timeout.
  * Replaces the np.tensordot chain of contract_ket_ham_with_envs /
  * contract_any (contractions/state_operator_contraction.py:227-273, 407-694)
  * in the mixed-precision path. */
@@ -122,33 +124,34 @@ typedef struct {
   int64_t M, K;
   const void* Bx;
   int64_t ldb, N;
-  int32_t out_kind, pad_;
+  int32_t out_kind, levels;
   void* C;
   int64_t c_plane;
   ptn_modes m_out, n_out;
   int32_t* status;
 } ptn_cgemm_desc;
 int ptn_cgemm_bf16x3(const ptn_cgemm_desc* d, void* stream);
-int ptn_cgemm_smem_bytes(void);
+int ptn_cgemm_smem_bytes(int32_t levels);
 
 /* Gather a complex128 tensor into the split BF16 operand layouts above.
  * rows / cols: source mode groups (dims + stride_a); element (r, c) of the
  * operand is src[off_rows(r) + off_cols(c)], conjugated when conj != 0.
- * ptn_to_planes writes 4 planes of [rows][ld] with plane stride `plane`;
- * ptn_expand_b writes [2][3][rows][ld] (rows = N). */
+ * ptn_to_planes writes 2*levels planes of [rows][ld] with plane stride `plane`;
+ * ptn_expand_b writes [levels][3][rows][ld] (rows = N). */
 typedef struct {
   const void* src;
   void* dst;
   int64_t ld, plane;
-  int32_t conj, pad_;
+  int32_t conj, levels;
   ptn_modes rows, cols;
 } ptn_convert_desc;
 int ptn_to_planes(const ptn_convert_desc* d, void* stream);
 int ptn_expand_b(const ptn_convert_desc* d, void* stream);
 
 /* Self-test of the tcgen05 descriptors: D[128][128] (fp32) = A[128][64] * B[128][64]^T
- * for bf16 A, B (K contiguous); one CTA. */
-int ptn_tc_selftest(const void* A, const void* B, void* D, int32_t* status, void* stream);
+ * for bf16 A, B (K contiguous); one CTA; sw64 != 0 stages K as two 64-byte-swizzled
+ * tiles instead of one 128-byte-swizzled tile. */
+int ptn_tc_selftest(const void* A, const void* B, void* D, int32_t* status, int32_t sw64, void* stream);
 
 /* Number of kernel launches this library has issued since it was loaded
  * (host-side counter; used to report launches inside a timed region). */

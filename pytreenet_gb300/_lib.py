@@ -56,13 +56,13 @@ class CgemmDesc(ctypes.Structure):
     _fields_ = [("A", ctypes.c_void_p), ("lda", ctypes.c_int64), ("a_plane", ctypes.c_int64),
                 ("M", ctypes.c_int64), ("K", ctypes.c_int64), ("Bx", ctypes.c_void_p),
                 ("ldb", ctypes.c_int64), ("N", ctypes.c_int64), ("out_kind", ctypes.c_int32),
-                ("pad_", ctypes.c_int32), ("C", ctypes.c_void_p), ("c_plane", ctypes.c_int64),
+                ("levels", ctypes.c_int32), ("C", ctypes.c_void_p), ("c_plane", ctypes.c_int64),
                 ("m_out", Modes), ("n_out", Modes), ("status", ctypes.c_void_p)]
 
 
 class ConvertDesc(ctypes.Structure):
     _fields_ = [("src", ctypes.c_void_p), ("dst", ctypes.c_void_p), ("ld", ctypes.c_int64),
-                ("plane", ctypes.c_int64), ("conj", ctypes.c_int32), ("pad_", ctypes.c_int32),
+                ("plane", ctypes.c_int64), ("conj", ctypes.c_int32), ("levels", ctypes.c_int32),
                 ("rows", Modes), ("cols", Modes)]
 
 
@@ -82,10 +82,10 @@ SIGNATURES = {
     "ptn_check_finite": (ctypes.c_int, [_P, _I64, _P, _P]),
     "ptn_launch_counter": (ctypes.c_ulonglong, []),
     "ptn_cgemm_bf16x3": (ctypes.c_int, [ctypes.POINTER(CgemmDesc), _P]),
-    "ptn_cgemm_smem_bytes": (ctypes.c_int, []),
+    "ptn_cgemm_smem_bytes": (ctypes.c_int, [_I32]),
     "ptn_to_planes": (ctypes.c_int, [ctypes.POINTER(ConvertDesc), _P]),
     "ptn_expand_b": (ctypes.c_int, [ctypes.POINTER(ConvertDesc), _P]),
-    "ptn_tc_selftest": (ctypes.c_int, [_P, _P, _P, _P, _P]),
+    "ptn_tc_selftest": (ctypes.c_int, [_P, _P, _P, _P, _I32, _P]),
 }
 
 _lib = None

@@ -1,19 +1,21 @@
 // Mixed-precision complex contraction on the 5th-generation tensor cores.
 //
-// C[m, n] = sum_k A[m, k] * B[n, k] (complex), with A and B split into BF16
-// hi/lo parts (x = hi + lo, each bf16) and products accumulated in FP32 in
-// TMEM: A*B ~ Ah*Bh + Ah*Bl + Al*Bh ("BF16x3"). The complex product is written
-// as one real product with doubled width:
+// C[m, n] = sum_k A[m, k] * B[n, k] (complex), with A and B split into L BF16
+// levels (x = x0 + x1 [+ x2], each bf16, 8 more mantissa bits per level) and
+// the products of levels i + j < L accumulated in FP32 in TMEM:
+//   L = 2 ("BF16x3"): A0B0 + A0B1 + A1B0, relative error ~2^-16;
+//   L = 3 ("BF16x6"): + A0B2 + A1B1 + A2B0, relative error ~2^-24 (FP32 level).
+// The complex product is written as one real product with doubled width:
 //   [Cr | Ci] = Ar * [Br | Bi] + Ai * [-Bi | Br]
-// so each K=16 slice issues 6 tcgen05.mma (M=128, N=2*NT, K=16): for each of
-// (Ah,Bh), (Ah,Bl), (Al,Bh) one with Ar and one with Ai. The expanded B keeps
-// the three blocks [-Bi; Br; Bi] adjacent in shared memory, so the Ar operand
-// is the window [Br; Bi] and the Ai operand the window [-Bi; Br].
+// so each (i, j) term issues two tcgen05.mma (M=128, N=2*NT, K=16). The
+// expanded B keeps the three blocks [-Bi; Br; Bi] of a level adjacent in shared
+// memory, so the Ar operand is the window [Br; Bi] and the Ai operand the
+// window [-Bi; Br].
 //
 // Operands (both K-major, K contiguous):
-//   A: 4 bf16 planes (Ar_hi, Ai_hi, Ar_lo, Ai_lo), each [M][lda]
-//   Bx: bf16 [level(hi, lo)][block(-Bi, Br, Bi)][N][ldb]
-// Tiles are staged by TMA (128-byte swizzle) through a 2-stage mbarrier ring;
+//   A: 2L bf16 planes (Ar_0, Ai_0, Ar_1, Ai_1, ...), each [M][lda]
+//   Bx: bf16 [level][block(-Bi, Br, Bi)][N][ldb]
+// Tiles are staged by TMA (64-byte swizzle, K=32 per stage) through an mbarrier ring;
 // one warp issues TMA, one warp issues MMA and owns the TMEM allocation, four
 // warps run the epilogue (TMEM -> registers -> global, strided by output mode
 // tables so the result lands directly in the layout the next step reads).
@@ -29,15 +31,20 @@ namespace {
 
 constexpr int MT = 128;         // rows of C per CTA
 constexpr int NT = 64;          // complex columns of C per CTA (MMA N = 2*NT)
-constexpr int KT = 64;          // K per stage (one 128-byte swizzle row)
-constexpr int STAGES = 2;
-constexpr int A_PLANE_BYTES = MT * 128;            // 16 KB
-constexpr int A_STAGE_BYTES = 4 * A_PLANE_BYTES;   // 64 KB
-constexpr int B_BLOCK_BYTES = NT * 128;            // 8 KB
-constexpr int B_STAGE_BYTES = 6 * B_BLOCK_BYTES;   // 48 KB
-constexpr int STAGE_BYTES = A_STAGE_BYTES + B_STAGE_BYTES;
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;
+constexpr int KT = 32;          // K per stage (one 64-byte swizzle row)
+constexpr int A_PLANE_BYTES = MT * 64;             // 8 KB
+constexpr int B_BLOCK_BYTES = NT * 64;             // 4 KB
+constexpr int SMEM_LIMIT = 227 * 1024;
 constexpr int THREADS = 192;
+
+template <int L>
+struct Cfg {
+  static constexpr int A_STAGE = 2 * L * A_PLANE_BYTES;
+  static constexpr int B_STAGE = 3 * L * B_BLOCK_BYTES;
+  static constexpr int STAGE = A_STAGE + B_STAGE;
+  static constexpr int STAGES = (SMEM_LIMIT - 2048) / STAGE > 4 ? 4 : (SMEM_LIMIT - 2048) / STAGE;
+  static constexpr int SMEM = STAGES * STAGE + 1024;
+};
 constexpr long long WAIT_CYCLES = 4000000000LL;    // ~2 s at 2 GHz
 
 struct OutModes {
@@ -66,9 +73,14 @@ __device__ __forceinline__ int64_t decode_off(const OutModes& md, int64_t idx) {
   return o;
 }
 
+template <int L>
 __global__ void __launch_bounds__(THREADS, 1)
-    cgemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                        const GemmArgs g) {
+    cgemm_bf16_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                      const GemmArgs g) {
+  using C_ = Cfg<L>;
+  constexpr int STAGES = C_::STAGES;
+  constexpr int STAGE_BYTES = C_::STAGE;
+  constexpr int A_STAGE_BYTES = C_::A_STAGE;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   __shared__ uint64_t full_bar[STAGES], empty_bar[STAGES], done_bar;
@@ -123,9 +135,9 @@ __global__ void __launch_bounds__(THREADS, 1)
         uint8_t* st = smem + s * STAGE_BYTES;
         tc::mbar_arrive_expect_tx(&full_bar[s], STAGE_BYTES);
         const int kx = kt * KT;
-        for (int p = 0; p < 4; ++p)
+        for (int p = 0; p < 2 * L; ++p)
           tc::tma_load_3d(st + p * A_PLANE_BYTES, &tmA, &full_bar[s], kx, (int)m0, p);
-        for (int b = 0; b < 6; ++b)
+        for (int b = 0; b < 3 * L; ++b)
           tc::tma_load_3d(st + A_STAGE_BYTES + b * B_BLOCK_BYTES, &tmB, &full_bar[s], kx, (int)n0, b);
       }
     }
@@ -147,23 +159,22 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
         for (int kk = 0; kk < KT / 16; ++kk) {
           const uint32_t ko = kk * 32;
-          // A planes: 0 Ar_hi, 1 Ai_hi, 2 Ar_lo, 3 Ai_lo
-          // B windows: level L at sb + L*3*B_BLOCK; top = +B_BLOCK ([Br; Bi]), bot = +0 ([-Bi; Br])
-          const uint64_t arh = tc::sdesc_sw128(sa + 0 * A_PLANE_BYTES + ko);
-          const uint64_t aih = tc::sdesc_sw128(sa + 1 * A_PLANE_BYTES + ko);
-          const uint64_t arl = tc::sdesc_sw128(sa + 2 * A_PLANE_BYTES + ko);
-          const uint64_t ail = tc::sdesc_sw128(sa + 3 * A_PLANE_BYTES + ko);
-          const uint64_t bht = tc::sdesc_sw128(sb + 1 * B_BLOCK_BYTES + ko);
-          const uint64_t bhb = tc::sdesc_sw128(sb + 0 * B_BLOCK_BYTES + ko);
-          const uint64_t blt = tc::sdesc_sw128(sb + 4 * B_BLOCK_BYTES + ko);
-          const uint64_t blb = tc::sdesc_sw128(sb + 3 * B_BLOCK_BYTES + ko);
-          const uint32_t first = (kt == 0 && kk == 0) ? 0u : 1u;
-          tc::mma_bf16(tmem, arh, bht, idesc, first);
-          tc::mma_bf16(tmem, aih, bhb, idesc, 1u);
-          tc::mma_bf16(tmem, arh, blt, idesc, 1u);
-          tc::mma_bf16(tmem, aih, blb, idesc, 1u);
-          tc::mma_bf16(tmem, arl, bht, idesc, 1u);
-          tc::mma_bf16(tmem, ail, bhb, idesc, 1u);
+          bool first = (kt == 0 && kk == 0);
+          // A planes: 2i = Re level i, 2i+1 = Im level i.
+          // B level j at sb + 3j*B_BLOCK: window [Br; Bi] at +1 block, [-Bi; Br] at +0.
+#pragma unroll
+          for (int i = 0; i < L; ++i) {
+#pragma unroll
+            for (int j = 0; j + i < L; ++j) {
+              const uint64_t ar = tc::sdesc_sw64(sa + (2 * i) * A_PLANE_BYTES + ko);
+              const uint64_t ai = tc::sdesc_sw64(sa + (2 * i + 1) * A_PLANE_BYTES + ko);
+              const uint64_t bt = tc::sdesc_sw64(sb + (3 * j + 1) * B_BLOCK_BYTES + ko);
+              const uint64_t bb = tc::sdesc_sw64(sb + (3 * j) * B_BLOCK_BYTES + ko);
+              tc::mma_bf16(tmem, ar, bt, idesc, first ? 0u : 1u);
+              tc::mma_bf16(tmem, ai, bb, idesc, 1u);
+              first = false;
+            }
+          }
         }
         tc::mma_commit(&empty_bar[s]);
       }
@@ -201,15 +212,17 @@ __global__ void __launch_bounds__(THREADS, 1)
           for (int i = 0; i < 16; ++i) {
             const int64_t no = noff[j0 + i];
             if (no < 0) continue;
-            const __nv_bfloat16 rh = __float2bfloat16_rn(re[i]);
-            const __nv_bfloat16 ih = __float2bfloat16_rn(im[i]);
-            const __nv_bfloat16 rl = __float2bfloat16_rn(re[i] - __bfloat162float(rh));
-            const __nv_bfloat16 il = __float2bfloat16_rn(im[i] - __bfloat162float(ih));
             const int64_t o = moff + no;
-            C[o] = rh;
-            C[ps + o] = ih;
-            C[2 * ps + o] = rl;
-            C[3 * ps + o] = il;
+            float r = re[i], v = im[i];
+#pragma unroll
+            for (int lv = 0; lv < L; ++lv) {
+              const __nv_bfloat16 rb = __float2bfloat16_rn(r);
+              const __nv_bfloat16 ib = __float2bfloat16_rn(v);
+              C[(2 * lv) * ps + o] = rb;
+              C[(2 * lv + 1) * ps + o] = ib;
+              r -= __bfloat162float(rb);
+              v -= __bfloat162float(ib);
+            }
           }
         }
       }
@@ -246,36 +259,43 @@ int make_map_3d(CUtensorMap* map, const void* base, uint64_t d0, uint64_t d1, ui
   if (!enc) return PTN_ERR_LAUNCH;
   CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims,
                                       strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                      CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                      CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? PTN_OK : PTN_ERR_ARG;
 }
 
 // ---- conversions ---------------------------------------------------------------------
 // planes[p][m * lda + k] <- split(src[off_m(m) + off_k(k)]) for the complex128 source.
+__device__ __forceinline__ void split_levels(double x, int L, __nv_bfloat16* out) {
+  for (int lv = 0; lv < L; ++lv) {
+    const __nv_bfloat16 b = __double2bfloat16(x);
+    out[lv] = b;
+    x -= (double)__bfloat162float(b);
+  }
+}
+
 __global__ void to_planes_kernel(const double2* __restrict__ src, OutModes mm, OutModes km, int64_t M, int64_t K,
-                                 int64_t lda, int64_t plane, int conj, __nv_bfloat16* __restrict__ dst) {
+                                 int64_t lda, int64_t plane, int conj, int L, __nv_bfloat16* __restrict__ dst) {
   const int64_t total = M * K;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
        e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t m = e / K, k = e - (e / K) * K;
     double2 v = src[decode_off(mm, m) + decode_off(km, k)];
     if (conj) v.y = -v.y;
-    const __nv_bfloat16 rh = __double2bfloat16(v.x);
-    const __nv_bfloat16 ih = __double2bfloat16(v.y);
-    const __nv_bfloat16 rl = __double2bfloat16(v.x - (double)__bfloat162float(rh));
-    const __nv_bfloat16 il = __double2bfloat16(v.y - (double)__bfloat162float(ih));
+    __nv_bfloat16 re[3], im[3];
+    split_levels(v.x, L, re);
+    split_levels(v.y, L, im);
     const int64_t o = m * lda + k;
-    dst[o] = rh;
-    dst[plane + o] = ih;
-    dst[2 * plane + o] = rl;
-    dst[3 * plane + o] = il;
+    for (int lv = 0; lv < L; ++lv) {
+      dst[(2 * lv) * plane + o] = re[lv];
+      dst[(2 * lv + 1) * plane + o] = im[lv];
+    }
   }
 }
 
-// Bx[level][block][n][k]: block 0 = -Bi, 1 = Br, 2 = Bi; level 0 = hi, 1 = lo.
+// Bx[level][block][n][k]: block 0 = -Bi, 1 = Br, 2 = Bi.
 __global__ void expand_b_kernel(const double2* __restrict__ src, OutModes nm, OutModes km, int64_t N, int64_t K,
-                                int64_t ldb, int conj, __nv_bfloat16* __restrict__ dst) {
+                                int64_t ldb, int conj, int L, __nv_bfloat16* __restrict__ dst) {
   const int64_t total = N * K;
   const int64_t blk = N * ldb;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
@@ -283,17 +303,15 @@ __global__ void expand_b_kernel(const double2* __restrict__ src, OutModes nm, Ou
     const int64_t n = e / K, k = e - (e / K) * K;
     double2 v = src[decode_off(nm, n) + decode_off(km, k)];
     if (conj) v.y = -v.y;
-    const __nv_bfloat16 rh = __double2bfloat16(v.x);
-    const __nv_bfloat16 ih = __double2bfloat16(v.y);
-    const __nv_bfloat16 rl = __double2bfloat16(v.x - (double)__bfloat162float(rh));
-    const __nv_bfloat16 il = __double2bfloat16(v.y - (double)__bfloat162float(ih));
+    __nv_bfloat16 re[3], im[3];
+    split_levels(v.x, L, re);
+    split_levels(v.y, L, im);
     const int64_t o = n * ldb + k;
-    dst[0 * blk + o] = __hneg(ih);
-    dst[1 * blk + o] = rh;
-    dst[2 * blk + o] = ih;
-    dst[3 * blk + o] = __hneg(il);
-    dst[4 * blk + o] = rl;
-    dst[5 * blk + o] = il;
+    for (int lv = 0; lv < L; ++lv) {
+      dst[(3 * lv + 0) * blk + o] = __hneg(im[lv]);
+      dst[(3 * lv + 1) * blk + o] = re[lv];
+      dst[(3 * lv + 2) * blk + o] = im[lv];
+    }
   }
 }
 
@@ -330,11 +348,26 @@ unsigned grid_for(int64_t n) {
 
 }  // namespace
 
-extern "C" int ptn_cgemm_smem_bytes(void) { return SMEM_BYTES; }
+extern "C" int ptn_cgemm_smem_bytes(int32_t levels) { return levels == 3 ? Cfg<3>::SMEM : Cfg<2>::SMEM; }
+
+template <int L>
+int launch_gemm(const CUtensorMap& ta, const CUtensorMap& tb, const GemmArgs& g, unsigned grid, cudaStream_t st) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    if (cudaFuncSetAttribute(cgemm_bf16_kernel<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg<L>::SMEM) !=
+        cudaSuccess)
+      return PTN_ERR_LAUNCH;
+    attr_set = true;
+  }
+  PTN_COUNT(1);
+  cgemm_bf16_kernel<L><<<grid, THREADS, Cfg<L>::SMEM, st>>>(ta, tb, g);
+  return ptn_launch_status();
+}
 
 extern "C" int ptn_cgemm_bf16x3(const ptn_cgemm_desc* d, void* stream) {
   if (!d || !d->A || !d->Bx || !d->C || !d->status) return PTN_ERR_ARG;
   if (d->M < 1 || d->N < 1 || d->K < 1) return PTN_ERR_ARG;
+  if (d->levels != 2 && d->levels != 3) return PTN_ERR_ARG;
   if (d->lda % 8 || d->ldb % 8 || d->lda < d->K || d->ldb < d->K) return PTN_ERR_ARG;
   if (d->a_plane % 8 || (reinterpret_cast<uintptr_t>(d->A) & 15) || (reinterpret_cast<uintptr_t>(d->Bx) & 15))
     return PTN_ERR_ARG;
@@ -349,48 +382,42 @@ extern "C" int ptn_cgemm_bf16x3(const ptn_cgemm_desc* d, void* stream) {
   g.status = d->status;
   if (fill_out(d->m_out, g.mo) || fill_out(d->n_out, g.no)) return PTN_ERR_ARG;
   CUtensorMap ta, tb;
-  if (make_map_3d(&ta, d->A, (uint64_t)d->K, (uint64_t)d->M, 4, (uint64_t)d->lda * 2, (uint64_t)d->a_plane * 2, KT,
-                  MT))
+  const int L = d->levels;
+  if (make_map_3d(&ta, d->A, (uint64_t)d->K, (uint64_t)d->M, 2 * L, (uint64_t)d->lda * 2,
+                  (uint64_t)d->a_plane * 2, KT, MT))
     return PTN_ERR_ARG;
-  if (make_map_3d(&tb, d->Bx, (uint64_t)d->K, (uint64_t)d->N, 6, (uint64_t)d->ldb * 2,
+  if (make_map_3d(&tb, d->Bx, (uint64_t)d->K, (uint64_t)d->N, 3 * L, (uint64_t)d->ldb * 2,
                   (uint64_t)d->N * (uint64_t)d->ldb * 2, KT, NT))
     return PTN_ERR_ARG;
   const int64_t tm = (d->M + MT - 1) / MT, tn = (d->N + NT - 1) / NT;
   g.tiles_n = tn;
   if (tm * tn > 0x7fffffffLL) return PTN_ERR_UNSUPPORTED;
-  static bool attr_set = false;
-  if (!attr_set) {
-    if (cudaFuncSetAttribute(cgemm_bf16x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) !=
-        cudaSuccess)
-      return PTN_ERR_LAUNCH;
-    attr_set = true;
-  }
-  PTN_COUNT(1);
-  cgemm_bf16x3_kernel<<<(unsigned)(tm * tn), THREADS, SMEM_BYTES, ptn_stream(stream)>>>(ta, tb, g);
-  return ptn_launch_status();
+  const unsigned grid = (unsigned)(tm * tn);
+  return L == 3 ? launch_gemm<3>(ta, tb, g, grid, ptn_stream(stream)) : launch_gemm<2>(ta, tb, g, grid, ptn_stream(stream));
 }
 
 extern "C" int ptn_to_planes(const ptn_convert_desc* d, void* stream) {
-  if (!d || !d->src || !d->dst) return PTN_ERR_ARG;
+  if (!d || !d->src || !d->dst || (d->levels != 2 && d->levels != 3)) return PTN_ERR_ARG;
   OutModes mm, km;
   int64_t M, K;
   if (fill_src(d->rows, mm, M) || fill_src(d->cols, km, K)) return PTN_ERR_ARG;
   if (d->ld < K) return PTN_ERR_ARG;
   PTN_COUNT(1);
   to_planes_kernel<<<grid_for(M * K), 256, 0, ptn_stream(stream)>>>(
-      static_cast<const double2*>(d->src), mm, km, M, K, d->ld, d->plane, d->conj,
+      static_cast<const double2*>(d->src), mm, km, M, K, d->ld, d->plane, d->conj, d->levels,
       static_cast<__nv_bfloat16*>(d->dst));
   return ptn_launch_status();
 }
 
 extern "C" int ptn_expand_b(const ptn_convert_desc* d, void* stream) {
-  if (!d || !d->src || !d->dst) return PTN_ERR_ARG;
+  if (!d || !d->src || !d->dst || (d->levels != 2 && d->levels != 3)) return PTN_ERR_ARG;
   OutModes nm, km;
   int64_t N, K;
   if (fill_src(d->rows, nm, N) || fill_src(d->cols, km, K)) return PTN_ERR_ARG;
   if (d->ld < K) return PTN_ERR_ARG;
   PTN_COUNT(1);
   expand_b_kernel<<<grid_for(N * K), 256, 0, ptn_stream(stream)>>>(
-      static_cast<const double2*>(d->src), nm, km, N, K, d->ld, d->conj, static_cast<__nv_bfloat16*>(d->dst));
+      static_cast<const double2*>(d->src), nm, km, N, K, d->ld, d->conj, d->levels,
+      static_cast<__nv_bfloat16*>(d->dst));
   return ptn_launch_status();
 }

@@ -142,6 +142,23 @@ __device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
   return d;
 }
 
+// Shared-memory matrix descriptor: K-major, SWIZZLE_64B (rows of 32 bf16,
+// 8-row atoms of 512 B).
+__device__ __forceinline__ uint64_t sdesc_sw64(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1u << 16;
+  d |= (uint64_t)(512u >> 4) << 32;
+  d |= (uint64_t)1u << 46;
+  d |= (uint64_t)4u << 61;                        // layout: SWIZZLE_64B
+  return d;
+}
+
+// Byte offset of element (row, k) in a K-major SW64 tile of 32-wide rows.
+__host__ __device__ __forceinline__ uint32_t sw64_offset(uint32_t row, uint32_t k) {
+  return row * 64u + ((((k >> 3) ^ ((row >> 1) & 3u)) & 3u) << 4) + ((k & 7u) << 1);
+}
+
 // Instruction descriptor, kind::f16: D=F32, A=B=BF16, both K-major, M x N.
 __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);

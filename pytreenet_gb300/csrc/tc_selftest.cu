@@ -11,7 +11,7 @@ namespace {
 
 __global__ void __launch_bounds__(128) tc_selftest_kernel(const uint16_t* __restrict__ A,
                                                           const uint16_t* __restrict__ B, float* __restrict__ D,
-                                                          int32_t* status) {
+                                                          int32_t* status, int sw64) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint8_t* sA = base;
@@ -19,10 +19,12 @@ __global__ void __launch_bounds__(128) tc_selftest_kernel(const uint16_t* __rest
   __shared__ uint64_t bar;
   __shared__ uint32_t tmem_base;
   const int tid = threadIdx.x;
+  // K = 64: one SW128 tile, or two SW64 tiles of 32 (second at +8 KB)
   for (int e = tid; e < 128 * 64; e += 128) {
     const int r = e >> 6, k = e & 63;
-    *reinterpret_cast<uint16_t*>(sA + tc::sw128_offset(r, k)) = A[e];
-    *reinterpret_cast<uint16_t*>(sB + tc::sw128_offset(r, k)) = B[e];
+    const uint32_t off = sw64 ? (uint32_t)(k >> 5) * 8192u + tc::sw64_offset(r, k & 31) : tc::sw128_offset(r, k);
+    *reinterpret_cast<uint16_t*>(sA + off) = A[e];
+    *reinterpret_cast<uint16_t*>(sB + off) = B[e];
   }
   if (tid == 0) {
     tc::mbar_init(&bar, 1);
@@ -41,8 +43,9 @@ __global__ void __launch_bounds__(128) tc_selftest_kernel(const uint16_t* __rest
     const uint32_t idesc = tc::idesc_bf16(128, 128);
 #pragma unroll
     for (int kk = 0; kk < 4; ++kk) {
-      const uint64_t ad = tc::sdesc_sw128(tc::smem_u32(sA) + kk * 32);
-      const uint64_t bd = tc::sdesc_sw128(tc::smem_u32(sB) + kk * 32);
+      const uint32_t o = sw64 ? (uint32_t)(kk >> 1) * 8192u + (kk & 1) * 32u : kk * 32u;
+      const uint64_t ad = sw64 ? tc::sdesc_sw64(tc::smem_u32(sA) + o) : tc::sdesc_sw128(tc::smem_u32(sA) + o);
+      const uint64_t bd = sw64 ? tc::sdesc_sw64(tc::smem_u32(sB) + o) : tc::sdesc_sw128(tc::smem_u32(sB) + o);
       tc::mma_bf16(tmem, ad, bd, idesc, kk > 0 ? 1u : 0u);
     }
     tc::mma_commit(&bar);
@@ -68,10 +71,11 @@ __global__ void __launch_bounds__(128) tc_selftest_kernel(const uint16_t* __rest
 
 }  // namespace
 
-extern "C" int ptn_tc_selftest(const void* A, const void* B, void* D, int32_t* status, void* stream) {
+extern "C" int ptn_tc_selftest(const void* A, const void* B, void* D, int32_t* status, int32_t sw64,
+                               void* stream) {
   if (!A || !B || !D || !status) return PTN_ERR_ARG;
   PTN_COUNT(1);
   tc_selftest_kernel<<<1, 128, 32768 + 1024, ptn_stream(stream)>>>(
-      static_cast<const uint16_t*>(A), static_cast<const uint16_t*>(B), static_cast<float*>(D), status);
+      static_cast<const uint16_t*>(A), static_cast<const uint16_t*>(B), static_cast<float*>(D), status, sw64);
   return ptn_launch_status();
 }

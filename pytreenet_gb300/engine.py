@@ -203,8 +203,8 @@ class ChainBuilder:
     def plan(self) -> Plan:
         return Plan(self.ws, self.steps, self.sizes)
 
-    def mixed_plan(self) -> "MixedPlan":
-        return MixedPlan(self.ws, self.logical)
+    def mixed_plan(self, levels: int = 3) -> "MixedPlan":
+        return MixedPlan(self.ws, self.logical, levels)
 
 
 def _modes_single(dims, strides):
@@ -237,7 +237,7 @@ def _round8(x):
 
 
 class MixedPlan:
-    """The same contraction chain on the tensor cores (BF16x3, FP32 accumulation).
+    """The same contraction chain on the tensor cores (BF16 splits, FP32 accumulation).
 
     Every step is ``ptn_cgemm_bf16x3`` with both operands K-major. The running
     tensor is kept as BF16 hi/lo planes whose layout is chosen for the step that
@@ -248,9 +248,10 @@ class MixedPlan:
     ``ptn_expand_b``; the first operand is gathered by ``ptn_to_planes``.
     """
 
-    def __init__(self, ws: Workspace, logical):
+    def __init__(self, ws: Workspace, logical, levels: int = 3):
         from ._lib import CgemmDesc, ConvertDesc
         self.ws = ws
+        self.levels = L = int(levels)
         self.ops = []            # ("conv"|"expand"|"gemm", desc, refs)
         self.sizes = {}          # ws name -> (numel, dtype)
         self.flops = 0
@@ -272,9 +273,9 @@ class MixedPlan:
                 d = ConvertDesc()
                 _set_modes(d.rows, [dimA[l] for l in mlab], [A.strides[A.labels.index(l)] for l in mlab], "stride_a")
                 _set_modes(d.cols, [dimA[l] for l in kl], [A.strides[A.labels.index(l)] for l in kl], "stride_a")
-                d.ld, d.plane, d.conj = lda, plane, int(kw.get("conj_a", False))
+                d.ld, d.plane, d.conj, d.levels = lda, plane, int(kw.get("conj_a", False)), L
                 self.ops.append(("conv", d, (A.ref, ("ws", aslot))))
-                self._need(aslot, 4 * plane)
+                self._need(aslot, 2 * L * plane)
             else:
                 # the previous GEMM already wrote this step's A in [mlab][kl] order
                 assert prev_layout[0] == aslot and prev_layout[2] == lda
@@ -282,11 +283,12 @@ class MixedPlan:
             d = ConvertDesc()
             _set_modes(d.rows, [dimB[l] for l in nlab], [B.strides[B.labels.index(l)] for l in nlab], "stride_a")
             _set_modes(d.cols, [dimB[l] for l in kl], [B.strides[B.labels.index(l)] for l in kl], "stride_a")
-            d.ld, d.plane, d.conj = ldb, 0, int(kw.get("conj_b", False))
+            d.ld, d.plane, d.conj, d.levels = ldb, 0, int(kw.get("conj_b", False)), L
             self.ops.append(("expand", d, (B.ref, ("ws", "bx"))))
-            self._need("bx", 6 * N * ldb)
+            self._need("bx", 3 * L * N * ldb)
             g = CgemmDesc()
             g.lda, g.a_plane, g.M, g.K, g.ldb, g.N = lda, plane, M, K, ldb, N
+            g.levels = L
             if i < nsteps - 1:
                 nA, nB, nkl, _, _ = logical[i + 1]
                 nm = [l for l in nA.labels if l not in nkl]
@@ -306,7 +308,7 @@ class MixedPlan:
                 cslot = f"mp{(i + 1) % 2}"
                 g.out_kind = 1
                 g.c_plane = nM * nlda
-                self._need(cslot, 4 * nM * nlda)
+                self._need(cslot, 2 * L * nM * nlda)
                 _set_modes(g.m_out, [dimA[l] for l in mlab], [stride[l] for l in mlab], "stride_c")
                 _set_modes(g.n_out, [dimB[l] for l in nlab], [stride[l] for l in nlab], "stride_c")
                 prev_layout = (cslot, stride, nlda, nM * nlda)
@@ -370,6 +372,18 @@ def small_propagator(T, dt, exp_factor, hermitian=True):
 
 
 class KrylovSolver:
+    @staticmethod
+    def _proj(T, m, tridiagonal):
+        if not tridiagonal:
+            return T[:m, :m]
+        P = np.zeros((m, m), dtype=complex)
+        idx = np.arange(m)
+        P[idx, idx] = T[idx, idx].real
+        if m > 1:
+            P[idx[1:], idx[:-1]] = T[idx[1:], idx[:-1]].real
+            P[idx[:-1], idx[1:]] = T[idx[1:], idx[:-1]].real
+        return P
+
     """Matrix-free Arnoldi/Lanczos exponential on the device.
 
     Two Gram-Schmidt passes per step (classical, each a multi-dot + multi-axpy
@@ -384,7 +398,13 @@ class KrylovSolver:
         self.depths: list[int] = []
 
     def expm(self, x: torch.Tensor, apply, dt: float, exp_factor: complex, krylov_tol=1e-10,
-             max_krylov_dim=None, hermitian=True, out: torch.Tensor | None = None) -> torch.Tensor:
+             max_krylov_dim=None, hermitian=True, out: torch.Tensor | None = None,
+             tridiagonal: bool = False) -> torch.Tensor:
+        """``tridiagonal``: project on the Lanczos tridiagonal (alpha_j, beta_j)
+        only. Used with reduced-precision operators, whose rounding leaves
+        entries far from the diagonal of the Arnoldi projection that the
+        reference's full symmetrised projection would turn into a spurious
+        first-order coupling (the adaptive stop then never triggers)."""
         lib = _lib.load()
         stream = _stream_ptr()
         n = x.numel()
@@ -424,6 +444,11 @@ class KrylovSolver:
             check(lib.ptn_dznrm2(w.data_ptr(), n, scal[1:].data_ptr(), part.data_ptr(), stream), "dznrm2")
             hh = hbuf[:2 * nq].cpu().numpy()
             sc = scal[:2].cpu().numpy()
+            st = self.ws.bufs.get("tc_status")
+            if st is not None and int(st.item()) != 0:
+                code = int(st.item())
+                st.zero_()
+                raise _lib.PtnError(code, "tensor-core contraction inside the Krylov exponential")
             w0, beta = float(sc[0]), float(sc[1])
             T[:nq, j] = hh[:nq] + hh[nq:]
             T[j + 1, j] = beta
@@ -433,7 +458,7 @@ class KrylovSolver:
             if beta <= max(floor_abs, 1e-12 * w0):
                 break
             if krylov_tol > 0.0:
-                col = small_propagator(T[:m, :m], dt, exp_factor, hermitian)
+                col = small_propagator(self._proj(T, m, tridiagonal), dt, exp_factor, hermitian)
                 if beta0 * beta * abs(col[m - 1]) < krylov_tol:
                     break
             if j + 1 >= Q.shape[0]:
@@ -445,7 +470,7 @@ class KrylovSolver:
             check(lib.ptn_zscal_inv(w.data_ptr(), scal[1:].data_ptr(), Q[j + 1].data_ptr(), n, stream),
                   "zscal")
         self.depths.append(m)
-        c = beta0 * small_propagator(T[:m, :m], dt, exp_factor, hermitian)
+        c = beta0 * small_propagator(self._proj(T, m, tridiagonal), dt, exp_factor, hermitian)
         cdev = self.ws.get("kry_h", m + 8)[:m]
         cdev.copy_(torch.from_numpy(np.ascontiguousarray(c)).to(x.device))
         for i0 in range(0, m, 64):
@@ -467,10 +492,14 @@ class KrylovSolver:
 class DeviceNetwork:
     """Device copy of a TTNS (+ TTNO) with environment buffers and cached plans."""
 
+    PRECISIONS = {"plain": 0, "bf16x3": 2, "bf16x6": 3, "mixed": 3}
+
     def __init__(self, state, hamiltonian=None, device=None, precision: str = "plain"):
-        if precision not in ("plain", "mixed"):
-            raise ValueError("precision must be 'plain' (complex128) or 'mixed' (BF16x3 tensor cores)")
+        if precision not in self.PRECISIONS:
+            raise ValueError("precision must be 'plain' (complex128), 'bf16x3', 'bf16x6' or 'mixed' "
+                             "(= bf16x6) tensor-core contractions")
         self.precision = precision
+        self.levels = self.PRECISIONS[precision]
         _lib.load()
         if not torch.cuda.is_available():
             raise RuntimeError("pytreenet_gb300 needs a CUDA device (no CPU fallback)")
@@ -560,7 +589,7 @@ class DeviceNetwork:
                 T = cb.contract(T, E, [f"a{k}", f"b{k}"])
         if not rest:
             raise RuntimeError("site without neighbours")
-        p = cb.mixed_plan() if self.precision == "mixed" else cb.plan()
+        p = cb.mixed_plan(self.levels) if self.levels else cb.plan()
         self.plans[key] = p
         return p
 
@@ -582,7 +611,7 @@ class DeviceNetwork:
                                [f"c{k}" if k != k0 else "z" for k in range(n)] + ["t"], shape)
         E = self._env_op(nid, nxt, [f"a{k0}", f"b{k0}", "z"])
         cb.contract(T, B, [f"c{k}" for k in range(n) if k != k0] + ["t"], out=E, conj_b=True)
-        p = cb.mixed_plan() if self.precision == "mixed" else cb.plan()
+        p = cb.mixed_plan(self.levels) if self.levels else cb.plan()
         self.plans[key] = p
         return p
 
@@ -629,7 +658,7 @@ class DeviceNetwork:
             p.run(xp, yp)
             self.flops += p.flops
         x = self.t[nid]
-        self.krylov.expm(x, apply, dt, exp_factor, tol, maxdim, out=x)
+        self.krylov.expm(x, apply, dt, exp_factor, tol, maxdim, out=x, tridiagonal=self.levels > 0)
         self.check_device_status()
 
     def check_device_status(self):
@@ -645,7 +674,7 @@ class DeviceNetwork:
         def apply(xp, yp):
             p.run(xp, yp)
             self.flops += p.flops
-        return self.krylov.expm(r, apply, dt, exp_factor, tol, maxdim, out=r)
+        return self.krylov.expm(r, apply, dt, exp_factor, tol, maxdim, out=r, tridiagonal=self.levels > 0)
 
     # -- QR split and R absorption ---------------------------------------------------
     def qr_split(self, nid, nbr) -> torch.Tensor:

@@ -142,10 +142,13 @@ def _bf16_val(bits):
     return (bits.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
 
 
-def _split(v):
-    hi = _bf16_bits(v)
-    lo = _bf16_bits(v - _bf16_val(hi))
-    return hi, lo
+def _split_levels(v, L):
+    out = []
+    for _ in range(L):
+        b = _bf16_bits(v)
+        out.append(b)
+        v = v - _bf16_val(b)
+    return out
 
 
 def _modes(m, field):
@@ -173,10 +176,10 @@ def _fake_to_planes(self, d_ref, stream):
     d = d_ref._obj
     v = _gather(d.src, d.rows, d.cols, d.conj)
     M, K = v.shape
-    dst = _view(d.dst, 3 * d.plane + M * d.ld, np.uint16)
+    L = d.levels
+    dst = _view(d.dst, (2 * L - 1) * d.plane + M * d.ld, np.uint16)
     for p, part in enumerate([v.real, v.imag]):
-        hi, lo = _split(part)
-        for lvl, arr in ((0, hi), (1, lo)):
+        for lvl, arr in enumerate(_split_levels(part, L)):
             plane = (2 * lvl + p) * d.plane
             blk = dst[plane:plane + M * d.ld].reshape(M, d.ld)
             blk[:, :K] = arr
@@ -187,28 +190,31 @@ def _fake_expand_b(self, d_ref, stream):
     d = d_ref._obj
     v = _gather(d.src, d.rows, d.cols, d.conj)
     N, K = v.shape
+    L = d.levels
     blk = N * d.ld
-    dst = _view(d.dst, 6 * blk, np.uint16)
-    rh, rl = _split(v.real)
-    ih, il = _split(v.imag)
-    for b, arr in enumerate([_bf16_bits(-_bf16_val(ih)), rh, ih, _bf16_bits(-_bf16_val(il)), rl, il]):
-        dst[b * blk:(b + 1) * blk].reshape(N, d.ld)[:, :K] = arr
+    dst = _view(d.dst, 3 * L * blk, np.uint16)
+    re = _split_levels(v.real, L)
+    im = _split_levels(v.imag, L)
+    for lv in range(L):
+        for b, arr in enumerate([_bf16_bits(-_bf16_val(im[lv])), re[lv], im[lv]]):
+            i = 3 * lv + b
+            dst[i * blk:(i + 1) * blk].reshape(N, d.ld)[:, :K] = arr
     return 0
 
 
 def _fake_cgemm(self, d_ref, stream):
     d = d_ref._obj
-    M, K, N = d.M, d.K, d.N
-    a = _view(d.A, 3 * d.a_plane + M * d.lda, np.uint16)
+    M, K, N, L = d.M, d.K, d.N, d.levels
+    a = _view(d.A, (2 * L - 1) * d.a_plane + M * d.lda, np.uint16)
 
     def plane(p):
         return _bf16_val(a[p * d.a_plane:p * d.a_plane + M * d.lda].reshape(M, d.lda)[:, :K])
-    A = (plane(0) + plane(2)) + 1j * (plane(1) + plane(3))
-    b = _view(d.Bx, 6 * N * d.ldb, np.uint16)
+    A = sum(plane(2 * lv) + 1j * plane(2 * lv + 1) for lv in range(L))
+    b = _view(d.Bx, 3 * L * N * d.ldb, np.uint16)
 
     def blk(i):
         return _bf16_val(b[i * N * d.ldb:(i + 1) * N * d.ldb].reshape(N, d.ldb)[:, :K])
-    B = (blk(1) + blk(4)) + 1j * (blk(2) + blk(5))
+    B = sum(blk(3 * lv + 1) + 1j * blk(3 * lv + 2) for lv in range(L))
     C = A @ B.T
     md, ms = _modes(d.m_out, "stride_c")
     nd, ns = _modes(d.n_out, "stride_c")
@@ -218,11 +224,10 @@ def _fake_cgemm(self, d_ref, stream):
         out = _view(d.C, int(off.max()) + 1)
         out[off] = C
     else:
-        out = _view(d.C, 3 * d.c_plane + int(off.max()) + 1, np.uint16)
+        out = _view(d.C, (2 * L - 1) * d.c_plane + int(off.max()) + 1, np.uint16)
         for p, part in enumerate([C.real, C.imag]):
-            hi, lo = _split(part)
-            out[(0 + p) * d.c_plane + off] = hi
-            out[(2 + p) * d.c_plane + off] = lo
+            for lv, arr in enumerate(_split_levels(part.astype(np.float32).astype(np.float64), L)):
+                out[(2 * lv + p) * d.c_plane + off] = arr
     return 0
 
 

@@ -54,8 +54,9 @@ def test_engine_host_c1_padded(monkeypatch):
     assert zerr < 2e-8
 
 
-@pytest.mark.parametrize("name", ["ttree3_heis_chi6_o1", "ternary2_xxz_chi4_o1", "binary7_tfim_chi4_o2"])
-def test_engine_host_mixed_layouts(monkeypatch, name):
+@pytest.mark.parametrize("name,precision", [("ttree3_heis_chi6_o1", "bf16x6"), ("ternary2_xxz_chi4_o1", "bf16x3"),
+                                            ("binary7_tfim_chi4_o2", "bf16x6")])
+def test_engine_host_mixed_layouts(monkeypatch, name, precision):
     """The tensor-core plans (operand layouts chosen per step, epilogue strides)
     give the reference's result up to BF16x3 rounding."""
     fake_ptn.install(monkeypatch)
@@ -67,9 +68,9 @@ def test_engine_host_mixed_layouts(monkeypatch, name):
     cls = P.FirstOrderOneSiteTDVP if c["order"] == 1 else P.SecondOrderOneSiteTDVP
     algo = cls(st, H, c["dt"], c["dt"] * c["steps"], {},
                config=P.TDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV),
-               solver_options={"krylov_tol": c["krylov_tol"]}, precision="mixed")
+               solver_options={"krylov_tol": c["krylov_tol"]}, precision=precision)
     for _ in range(c["steps"]):
         algo.run_one_time_step()
     got = O.OState(oracle_state(c).tree, {nid: algo.state.get_phys_numpy(nid) for nid, _ in c["spec"]})
     one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), got)
-    assert one_minus_f < 1e-8
+    assert one_minus_f < (1e-8 if precision == "bf16x3" else 1e-11)

@@ -81,9 +81,10 @@ __global__ void __launch_bounds__(THREADS, 1)
   constexpr int STAGES = C_::STAGES;
   constexpr int STAGE_BYTES = C_::STAGE;
   constexpr int A_STAGE_BYTES = C_::A_STAGE;
+  constexpr uint32_t ACC_COLS = 2 * NT;          // one accumulator: [Re | Im]
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  __shared__ uint64_t full_bar[STAGES], empty_bar[STAGES], done_bar;
+  __shared__ uint64_t full_bar[STAGES], empty_bar[STAGES], tfull_bar[2], tempty_bar[2];
   __shared__ uint32_t tmem_base;
   __shared__ int64_t noff[NT];
   __shared__ int s_abort;
@@ -103,11 +104,14 @@ __global__ void __launch_bounds__(THREADS, 1)
       tc::mbar_init(&full_bar[s], 1);
       tc::mbar_init(&empty_bar[s], 1);
     }
-    tc::mbar_init(&done_bar, 1);
+    for (int b = 0; b < 2; ++b) {
+      tc::mbar_init(&tfull_bar[b], 1);
+      tc::mbar_init(&tempty_bar[b], 4);   // one arrival per epilogue warp
+    }
     tc::fence_mbar_init();
   }
   if (warp == 1) {
-    tc::tmem_alloc(&tmem_base, 2 * NT);
+    tc::tmem_alloc(&tmem_base, 2 * ACC_COLS);
     tc::tmem_relinquish();
   }
   if (threadIdx.x >= 64 && threadIdx.x < 64 + NT) {
@@ -143,86 +147,114 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
+    // Each K tile accumulates into a fresh TMEM buffer (two, alternating); the
+    // epilogue warps add the tile's partial sum into FP32 registers. The
+    // tensor-core accumulator loses precision in proportion to the number of
+    // accumulations it absorbs, so this bounds that loss to one tile.
     if (lane == 0) {
       const uint32_t idesc = tc::idesc_bf16(MT, 2 * NT);
-      bool ok = true;
       for (int kt = 0; kt < ktiles; ++kt) {
         const int s = kt % STAGES;
+        const int b = kt & 1, ub = kt >> 1;
+        if (ub > 0 && !tc::mbar_wait_abortable(&tempty_bar[b], (ub - 1) & 1, WAIT_CYCLES, vstatus)) {
+          atomicExch(g.status, PTN_ERR_TIMEOUT);
+          break;
+        }
         if (!tc::mbar_wait_abortable(&full_bar[s], (kt / STAGES) & 1, WAIT_CYCLES, vstatus)) {
           atomicExch(g.status, PTN_ERR_TIMEOUT);
-          ok = false;
           break;
         }
         tc::fence_after();
         const uint32_t sa = tc::smem_u32(smem + s * STAGE_BYTES);
         const uint32_t sb = sa + A_STAGE_BYTES;
+        const uint32_t acc = tmem + (uint32_t)b * ACC_COLS;
+        bool first = true;
+        // smallest split products first, the leading (0, 0) product last
 #pragma unroll
-        for (int kk = 0; kk < KT / 16; ++kk) {
-          const uint32_t ko = kk * 32;
-          bool first = (kt == 0 && kk == 0);
-          // A planes: 2i = Re level i, 2i+1 = Im level i.
-          // B level j at sb + 3j*B_BLOCK: window [Br; Bi] at +1 block, [-Bi; Br] at +0.
+        for (int lvl = L - 1; lvl >= 0; --lvl) {
 #pragma unroll
-          for (int i = 0; i < L; ++i) {
+          for (int i = 0; i <= lvl; ++i) {
+            const int j = lvl - i;
 #pragma unroll
-            for (int j = 0; j + i < L; ++j) {
+            for (int kk = 0; kk < KT / 16; ++kk) {
+              const uint32_t ko = kk * 32;
+              // A planes: 2i = Re level i, 2i+1 = Im level i.
+              // B level j at sb + 3j*B_BLOCK: window [Br; Bi] at +1 block, [-Bi; Br] at +0.
               const uint64_t ar = tc::sdesc_sw64(sa + (2 * i) * A_PLANE_BYTES + ko);
               const uint64_t ai = tc::sdesc_sw64(sa + (2 * i + 1) * A_PLANE_BYTES + ko);
               const uint64_t bt = tc::sdesc_sw64(sb + (3 * j + 1) * B_BLOCK_BYTES + ko);
               const uint64_t bb = tc::sdesc_sw64(sb + (3 * j) * B_BLOCK_BYTES + ko);
-              tc::mma_bf16(tmem, ar, bt, idesc, first ? 0u : 1u);
-              tc::mma_bf16(tmem, ai, bb, idesc, 1u);
+              tc::mma_bf16(acc, ar, bt, idesc, first ? 0u : 1u);
+              tc::mma_bf16(acc, ai, bb, idesc, 1u);
               first = false;
             }
           }
         }
         tc::mma_commit(&empty_bar[s]);
+        tc::mma_commit(&tfull_bar[b]);
       }
-      if (ok) tc::mma_commit(&done_bar);
     }
   } else {
     // ---------------- epilogue (warps 2..5) ----------------
     const int q = warp & 3;                 // TMEM lane quarter of this warp
     const int row = q * 32 + lane;
     const int64_t m = m0 + row;
-    bool ok = tc::mbar_wait_abortable(&done_bar, 0, WAIT_CYCLES, vstatus);
-    tc::fence_after();
+    const uint32_t lane_off = (uint32_t)(q * 32) << 16;
+    float acc_re[NT], acc_im[NT];
+#pragma unroll
+    for (int i = 0; i < NT; ++i) {
+      acc_re[i] = 0.f;
+      acc_im[i] = 0.f;
+    }
+    bool ok = true;
+    for (int kt = 0; kt < ktiles && ok; ++kt) {
+      const int b = kt & 1;
+      ok = tc::mbar_wait_abortable(&tfull_bar[b], (kt >> 1) & 1, WAIT_CYCLES, vstatus);
+      if (!ok) break;
+      tc::fence_after();
+      const uint32_t tb = tmem + lane_off + (uint32_t)b * ACC_COLS;
+#pragma unroll
+      for (int j0 = 0; j0 < NT; j0 += 16) {
+        float v[16];
+        tc::tmem_ld16(tb + (uint32_t)j0, v);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) acc_re[j0 + i] += v[i];
+        tc::tmem_ld16(tb + (uint32_t)(NT + j0), v);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) acc_im[j0 + i] += v[i];
+      }
+      tc::fence_before();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&tempty_bar[b]);
+    }
     if (!ok) {
       if (lane == 0) atomicExch(g.status, PTN_ERR_TIMEOUT);
-    } else {
-      const int64_t moff = (m < g.M) ? decode_off(g.mo, m) : -1;
-      const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16);
-#pragma unroll 1
-      for (int j0 = 0; j0 < NT; j0 += 16) {
-        float re[16], im[16];
-        tc::tmem_ld16(tbase + (uint32_t)j0, re);
-        tc::tmem_ld16(tbase + (uint32_t)(NT + j0), im);
-        if (moff < 0) continue;
-        if (g.out_kind == 0) {
-          double2* C = static_cast<double2*>(g.C);
+    } else if (m < g.M) {
+      const int64_t moff = decode_off(g.mo, m);
+      if (g.out_kind == 0) {
+        double2* C = static_cast<double2*>(g.C);
 #pragma unroll
-          for (int i = 0; i < 16; ++i) {
-            const int64_t no = noff[j0 + i];
-            if (no >= 0) C[moff + no] = make_double2((double)re[i], (double)im[i]);
-          }
-        } else {
-          __nv_bfloat16* C = static_cast<__nv_bfloat16*>(g.C);
-          const int64_t ps = g.c_plane;
+        for (int i = 0; i < NT; ++i) {
+          const int64_t no = noff[i];
+          if (no >= 0) C[moff + no] = make_double2((double)acc_re[i], (double)acc_im[i]);
+        }
+      } else {
+        __nv_bfloat16* C = static_cast<__nv_bfloat16*>(g.C);
+        const int64_t ps = g.c_plane;
 #pragma unroll
-          for (int i = 0; i < 16; ++i) {
-            const int64_t no = noff[j0 + i];
-            if (no < 0) continue;
-            const int64_t o = moff + no;
-            float r = re[i], v = im[i];
+        for (int i = 0; i < NT; ++i) {
+          const int64_t no = noff[i];
+          if (no < 0) continue;
+          const int64_t o = moff + no;
+          float r = acc_re[i], v = acc_im[i];
 #pragma unroll
-            for (int lv = 0; lv < L; ++lv) {
-              const __nv_bfloat16 rb = __float2bfloat16_rn(r);
-              const __nv_bfloat16 ib = __float2bfloat16_rn(v);
-              C[(2 * lv) * ps + o] = rb;
-              C[(2 * lv + 1) * ps + o] = ib;
-              r -= __bfloat162float(rb);
-              v -= __bfloat162float(ib);
-            }
+          for (int lv = 0; lv < L; ++lv) {
+            const __nv_bfloat16 rb = __float2bfloat16_rn(r);
+            const __nv_bfloat16 ib = __float2bfloat16_rn(v);
+            C[(2 * lv) * ps + o] = rb;
+            C[(2 * lv + 1) * ps + o] = ib;
+            r -= __bfloat162float(rb);
+            v -= __bfloat162float(ib);
           }
         }
       }
@@ -230,7 +262,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   }
   tc::fence_before();
   __syncthreads();
-  if (warp == 1) tc::tmem_dealloc(tmem, 2 * NT);
+  if (warp == 1) tc::tmem_dealloc(tmem, 2 * ACC_COLS);
 }
 
 // ---- tensor maps ---------------------------------------------------------------------

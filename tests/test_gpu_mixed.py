@@ -84,7 +84,7 @@ def test_cgemm_chain_matches_fp64_plan(lib):
     rel3 = np.linalg.norm(outs["bf16x3"] - outs["plain"]) / np.linalg.norm(outs["plain"])
     rel6 = np.linalg.norm(outs["bf16x6"] - outs["plain"]) / np.linalg.norm(outs["plain"])
     assert rel3 < 1e-4, rel3
-    assert rel6 < 1e-6, rel6
+    assert rel6 < 2e-6, rel6
 
 
 @pytest.mark.parametrize("name", ["ttree3_heis_chi6_o1", "ternary2_xxz_chi4_o1"])

@@ -307,11 +307,11 @@ def run_gb300(args, rank, world):
     if args.precision == "mixed":
         peak, peak_src = _measured_bf16_peak()
         # algorithmic complex flops (8 per complex MAC); the BF16x3 split issues 3x that on the pipe
-        roof = {"bound": "tensor", "kernel": "ptn_cgemm_bf16x3 (heff matvec chain, tcgen05)",
+        roof = {"bound": "tensor", "kernel": "ptn_cgemm_bf16x3 (heff matvec chain, tcgen05, 3 split levels)",
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": (achieved / peak) if achieved else None,
-                "peak_source": peak_src + "; achieved counts algorithmic complex flops, the BF16x3 "
-                               "split issues 3x as many tensor flops",
+                "peak_source": peak_src + "; achieved counts algorithmic complex flops, the BF16x6 "
+                               "split issues 6x as many tensor flops",
                 "traffic": None}
     else:
         roof = {"bound": "tensor", "kernel": "ptn_zcontract (heff matvec chain, FP64)",
@@ -329,9 +329,9 @@ def run_gb300(args, rank, world):
     line = {"metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "c64 bf16x3 contractions / f64 Krylov" if args.precision == "mixed" else "c128 (fp64)",
+            "dtype": "bf16x6 split (tcgen05, fp32 accumulate) contractions / f64 Krylov+QR" if args.precision == "mixed" else "c128 (fp64)",
             "data": "synthetic",
-            "config": config(args, "mixed: BF16x3 tcgen05 contractions, FP32 accumulate, FP64 Krylov/QR/norm"
+            "config": config(args, "mixed: BF16x6 (3-level split) tcgen05 contractions, FP32 accumulate, FP64 Krylov/QR/norm"
                              if args.precision == "mixed" else "plain complex128"),
             "roofline": roof, "e2e": e2e, "plain_fp64": plain,
             "gpu_launches": launches, "clocks": clk.summary(),

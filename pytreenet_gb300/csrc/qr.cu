@@ -277,3 +277,4 @@ extern "C" int ptn_zqr_keep(void* Av, const int64_t* rowoff, int64_t m, int64_t 
   if (p < k) { PTN_COUNT(1); zero_cols_kernel<<<grid1(m * (k - p)), QT, 0, s>>>(A, rowoff, cs, m, k, p); }
   return ptn_launch_status();
 }
+

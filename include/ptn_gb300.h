@@ -153,6 +153,24 @@ int ptn_expand_b(const ptn_convert_desc* d, void* stream);
  * tiles instead of one 128-byte-swizzled tile. */
 int ptn_tc_selftest(const void* A, const void* B, void* D, int32_t* status, int32_t sw64, void* stream);
 
+/* Same as ptn_zqr_keep, but without a caller-provided work buffer. This entry
+ * point has no counterpart in the reference. It is meant for callers that
+ * cannot allocate device memory when they need a QR -- a host framework bound
+ * through a plain C FFI with no CUDA allocator of its own, or code that must
+ * not allocate while a stream is being captured. The scratch is a fixed 4 MiB
+ * array inside the library (ptn_zqr_noalloc_max_bytes()); every GPU that loads
+ * the library holds it until the process exits. Problems whose
+ * ptn_zqr_work_bytes(m, k) exceeds it are rejected with PTN_ERR_UNSUPPORTED
+ * before anything is launched. The first call on each device looks up the
+ * array's device address (with that device current), so make one call on a
+ * device before capturing a stream that uses it. All calls share the one
+ * array: calls that can overlap on the GPU (different streams, or different
+ * host threads) race on it, so serialise them. Nothing in the scratch needs
+ * to start at zero; each call writes every entry it later reads. */
+int64_t ptn_zqr_noalloc_max_bytes(void);
+int ptn_zqr_keep_noalloc(void* A, const int64_t* rowoff, int64_t m, int64_t k, int64_t colstride,
+                         void* R, void* stream);
+
 /* Number of kernel launches this library has issued since it was loaded
  * (host-side counter; used to report launches inside a timed region). */
 unsigned long long ptn_launch_counter(void);

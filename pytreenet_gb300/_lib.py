@@ -81,6 +81,8 @@ SIGNATURES = {
     "ptn_zqr_keep": (ctypes.c_int, [_P, _P, _I64, _I64, _I64, _P, _P, _P]),
     "ptn_check_finite": (ctypes.c_int, [_P, _I64, _P, _P]),
     "ptn_launch_counter": (ctypes.c_ulonglong, []),
+    "ptn_zqr_noalloc_max_bytes": (_I64, []),
+    "ptn_zqr_keep_noalloc": (ctypes.c_int, [_P, _P, _I64, _I64, _I64, _P, _P]),
     "ptn_cgemm_bf16x3": (ctypes.c_int, [ctypes.POINTER(CgemmDesc), _P]),
     "ptn_cgemm_smem_bytes": (ctypes.c_int, [_I32]),
     "ptn_to_planes": (ctypes.c_int, [ctypes.POINTER(ConvertDesc), _P]),

@@ -278,3 +278,46 @@ extern "C" int ptn_zqr_keep(void* Av, const int64_t* rowoff, int64_t m, int64_t 
   return ptn_launch_status();
 }
 
+// ---- QR with a library-owned scratch area --------------------------------------------
+// Some callers cannot allocate device memory at the moment they need a QR: a
+// host framework that binds this library through a plain C FFI and owns no
+// CUDA allocator, or code that must not allocate while a stream is being
+// captured into a graph. ptn_zqr_keep_noalloc runs the same Householder
+// kernels as ptn_zqr_keep but takes its scratch from a fixed array compiled
+// into the library (every GPU that loads the library keeps these 4 MiB until
+// the process exits).
+#include <mutex>
+
+#define PTN_QR_STATIC_SCRATCH_BYTES (4ll << 20)
+static __device__ __align__(256) unsigned char g_qr_static_scratch[PTN_QR_STATIC_SCRATCH_BYTES];
+
+namespace {
+std::mutex g_qr_static_mu;
+void* g_qr_static_ptr[256] = {};  // device address of the array, per device ordinal
+}  // namespace
+
+extern "C" int64_t ptn_zqr_noalloc_max_bytes(void) { return PTN_QR_STATIC_SCRATCH_BYTES; }
+
+extern "C" int ptn_zqr_keep_noalloc(void* A, const int64_t* rowoff, int64_t m, int64_t k, int64_t colstride,
+                                    void* R, void* stream) {
+  if (!A || !rowoff || !R || m < 1 || k < 1 || colstride < 1) return PTN_ERR_ARG;
+  if (ptn_zqr_work_bytes(m, k) > PTN_QR_STATIC_SCRATCH_BYTES) return PTN_ERR_UNSUPPORTED;
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) return PTN_ERR_LAUNCH;
+  void* work = nullptr;
+  {
+    std::lock_guard<std::mutex> guard(g_qr_static_mu);
+    if (!g_qr_static_ptr[dev]) {
+      // Host code cannot pass the array's name to a kernel: it is a host-side
+      // stand-in. Resolve its device address once, with this device current.
+      void* p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_qr_static_scratch) != cudaSuccess || !p) return PTN_ERR_LAUNCH;
+      g_qr_static_ptr[dev] = p;
+    }
+    work = g_qr_static_ptr[dev];
+  }
+  // Every scratch entry the kernels read is written earlier in the same call
+  // (column-norm partials, reflector scalars, dot partials), so nothing needs
+  // clearing between calls.
+  return ptn_zqr_keep(A, rowoff, m, k, colstride, R, work, stream);
+}

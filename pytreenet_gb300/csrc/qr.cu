@@ -215,6 +215,142 @@ __global__ void zero_cols_kernel(double2* __restrict__ A, const int64_t* __restr
   }
 }
 
+// ---- small-m path: one launch per Householder step ------------------------------------
+// For m <= QR_SMALL_M each step is one kernel: every CTA recomputes the
+// reflector from column j (a few KB, identical arithmetic in every CTA, so the
+// result is the same everywhere) and then owns one trailing column (dot and
+// update). The reflectors go to a separate V buffer and the diagonal of R to
+// `betas`, so no CTA writes what another reads in the same launch.
+constexpr int64_t QR_SMALL_M = 2048;
+constexpr int ST = 256;
+
+__device__ __forceinline__ double block_sum(double v, double* red) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < ST / 32; ++i) s += red[i];
+    red[ST / 32] = s;
+  }
+  __syncthreads();
+  s = red[ST / 32];
+  __syncthreads();
+  return s;
+}
+
+__device__ __forceinline__ double2 block_sum2(double2 v, double* red) {
+  double re = block_sum(v.x, red);
+  double im = block_sum(v.y, red);
+  return make_double2(re, im);
+}
+
+// Step j of the factorisation. grid = max(1, k - j - 1); CTA b owns column j+1+b.
+__global__ void __launch_bounds__(ST) hh_fact_small(double2* __restrict__ A, const int64_t* __restrict__ rowoff,
+                                                    int64_t cs, int64_t m, int64_t k, int64_t j,
+                                                    double2* __restrict__ tau, double2* __restrict__ betas,
+                                                    double2* __restrict__ V) {
+  __shared__ double2 vs[QR_SMALL_M];
+  __shared__ double red[ST / 32 + 1];
+  __shared__ double2 sc[3];  // tau, scal, w
+  const int64_t len = m - j;
+  double acc = 0.0;
+  for (int64_t t = threadIdx.x; t < len; t += ST) {
+    const double2 a = A[rowoff[j + t] + j * cs];
+    vs[t] = a;
+    if (t > 0) acc += cabs2(a);
+  }
+  const double xn2 = block_sum(acc, red);
+  if (threadIdx.x == 0) {
+    const double2 alpha = vs[0];
+    const double xnorm = sqrt(xn2);
+    double2 t_, s_, b_;
+    if (xnorm == 0.0 && alpha.y == 0.0) {
+      t_ = make_double2(0.0, 0.0);
+      s_ = make_double2(0.0, 0.0);
+      b_ = alpha;
+    } else {
+      const double nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xnorm * xnorm);
+      const double beta = (alpha.x >= 0.0) ? -nrm : nrm;
+      t_ = make_double2((beta - alpha.x) / beta, -alpha.y / beta);
+      const double2 d = make_double2(alpha.x - beta, alpha.y);
+      const double den = d.x * d.x + d.y * d.y;
+      s_ = make_double2(d.x / den, -d.y / den);
+      b_ = make_double2(beta, 0.0);
+    }
+    sc[0] = t_;
+    sc[1] = s_;
+    if (blockIdx.x == 0) {
+      tau[j] = t_;
+      betas[j] = b_;
+    }
+  }
+  __syncthreads();
+  const double2 s_ = sc[1];
+  for (int64_t t = threadIdx.x; t < len; t += ST) {
+    const double2 v = (t == 0) ? make_double2(1.0, 0.0) : cmul(vs[t], s_);
+    vs[t] = v;
+    if (blockIdx.x == 0) V[j * m + j + t] = v;
+  }
+  __syncthreads();
+  const int64_t c = j + 1 + blockIdx.x;
+  if (c >= k) return;
+  double2 w = make_double2(0.0, 0.0);
+  for (int64_t t = threadIdx.x; t < len; t += ST) w = cfmac(vs[t], A[rowoff[j + t] + c * cs], w);
+  w = block_sum2(w, red);
+  double2 f = sc[0];
+  f.y = -f.y;  // conj(tau): the factorisation applies H^H
+  const double2 fw = cmul(f, w);
+  for (int64_t t = threadIdx.x; t < len; t += ST) {
+    double2* p = A + rowoff[j + t] + c * cs;
+    *p = csub(*p, cmul(vs[t], fw));
+  }
+}
+
+// R[r][c]: strictly-upper part from A, diagonal from betas (rows < p), zero elsewhere.
+__global__ void extract_r_small(const double2* __restrict__ A, const int64_t* __restrict__ rowoff, int64_t cs,
+                                int64_t k, int64_t p, const double2* __restrict__ betas, double2* __restrict__ R) {
+  for (int64_t e = blockIdx.x * (int64_t)ST + threadIdx.x; e < k * k; e += (int64_t)gridDim.x * ST) {
+    const int64_t r = e / k, c = e - r * k;
+    double2 v = make_double2(0.0, 0.0);
+    if (r < p) {
+      if (c == r) v = betas[r];
+      else if (c > r) v = A[rowoff[r] + c * cs];
+    }
+    R[e] = v;
+  }
+}
+
+// Step j of forming Q (zung2r): CTAs 0..ncols-1 apply H_j to columns j+1..p-1,
+// CTA ncols writes column j itself.
+__global__ void __launch_bounds__(ST) hh_form_small(double2* __restrict__ A, const int64_t* __restrict__ rowoff,
+                                                    int64_t cs, int64_t m, int64_t p, int64_t j,
+                                                    const double2* __restrict__ tau, const double2* __restrict__ V) {
+  __shared__ double red[ST / 32 + 1];
+  const int64_t ncols = p - (j + 1);
+  const double2 t_ = tau[j];
+  const double2* v = V + j * m;
+  if (blockIdx.x == ncols) {
+    for (int64_t i = threadIdx.x; i < m; i += ST) {
+      double2* q = A + rowoff[i] + j * cs;
+      if (i < j) *q = make_double2(0.0, 0.0);
+      else if (i == j) *q = make_double2(1.0 - t_.x, -t_.y);
+      else *q = make_double2(-(t_.x * v[i].x - t_.y * v[i].y), -(t_.x * v[i].y + t_.y * v[i].x));
+    }
+    return;
+  }
+  const int64_t c = j + 1 + blockIdx.x;
+  double2 w = make_double2(0.0, 0.0);
+  for (int64_t i = j + threadIdx.x; i < m; i += ST) w = cfmac(v[i], A[rowoff[i] + c * cs], w);
+  w = block_sum2(w, red);
+  const double2 fw = cmul(t_, w);
+  for (int64_t i = j + threadIdx.x; i < m; i += ST) {
+    double2* q = A + rowoff[i] + c * cs;
+    *q = csub(*q, cmul(v[i], fw));
+  }
+}
+
 inline unsigned grid1(int64_t n) {
   int64_t b = (n + QT - 1) / QT;
   if (b < 1) b = 1;
@@ -225,7 +361,32 @@ inline unsigned grid1(int64_t n) {
 }  // namespace
 
 extern "C" int64_t ptn_zqr_work_bytes(int64_t m, int64_t k) {
+  if (m <= QR_SMALL_M) {
+    const int64_t p = m < k ? m : k;
+    return 16 * (2 * k + m * p) + 256;   // tau, betas, V
+  }
   return 16 * (3 * k + (nrb_for(m) + 1) / 2 + 1 + nrb_for(m) * k) + 256;
+}
+
+static int zqr_keep_small(double2* A, const int64_t* rowoff, int64_t m, int64_t k, int64_t cs, double2* R,
+                          void* work, cudaStream_t s) {
+  double2* tau = static_cast<double2*>(work);
+  double2* betas = tau + k;
+  double2* V = betas + k;
+  const int64_t p = m < k ? m : k;
+  for (int64_t j = 0; j < p; ++j) {
+    const int64_t ncols = k - (j + 1);
+    PTN_COUNT(1);
+    hh_fact_small<<<(unsigned)(ncols > 0 ? ncols : 1), ST, 0, s>>>(A, rowoff, cs, m, k, j, tau, betas, V);
+  }
+  PTN_COUNT(1);
+  extract_r_small<<<grid1(k * k), ST, 0, s>>>(A, rowoff, cs, k, p, betas, R);
+  for (int64_t j = p - 1; j >= 0; --j) {
+    PTN_COUNT(1);
+    hh_form_small<<<(unsigned)(p - j), ST, 0, s>>>(A, rowoff, cs, m, p, j, tau, V);
+  }
+  if (p < k) { PTN_COUNT(1); zero_cols_kernel<<<grid1(m * (k - p)), QT, 0, s>>>(A, rowoff, cs, m, k, p); }
+  return ptn_launch_status();
 }
 
 extern "C" int ptn_zqr_keep(void* Av, const int64_t* rowoff, int64_t m, int64_t k, int64_t cs, void* Rv,
@@ -234,6 +395,7 @@ extern "C" int ptn_zqr_keep(void* Av, const int64_t* rowoff, int64_t m, int64_t 
   cudaStream_t s = ptn_stream(stream);
   double2* A = static_cast<double2*>(Av);
   double2* R = static_cast<double2*>(Rv);
+  if (m <= QR_SMALL_M) return zqr_keep_small(A, rowoff, m, k, cs, R, work, s);
   QRWork q = carve(work, m, k);
   const int64_t p = m < k ? m : k;
   // factorisation

@@ -256,70 +256,88 @@ class MixedPlan:
         self.sizes = {}          # ws name -> (numel, dtype)
         self.flops = 0
         nsteps = len(logical)
-        prev_layout = None       # for step i>0: (slot, label -> stride, lda, plane)
-        for i, (A, B, kl, out, kw) in enumerate(logical):
+        info = []
+        for (A, B, kl, out, kw) in logical:
             mlab = [l for l in A.labels if l not in kl]
             nlab = [l for l in B.labels if l not in kl]
-            dimA = dict(zip(A.labels, A.dims))
-            dimB = dict(zip(B.labels, B.dims))
-            M = int(np.prod([dimA[l] for l in mlab] or [1]))
-            N = int(np.prod([dimB[l] for l in nlab] or [1]))
-            K = int(np.prod([dimA[l] for l in kl] or [1]))
-            self.flops += 8 * M * N * K
+            dims = {**dict(zip(A.labels, A.dims)), **dict(zip(B.labels, B.dims))}
+            info.append((mlab, list(kl), nlab, dims))
+        # Layouts are assigned from the last step backwards. The output of step i
+        # is the A operand of step i+1, laid out [rows][cols] with cols = the
+        # legs step i+1 contracts (contiguous). Rows are ordered by the stride the
+        # legs get in step i+1's own output (largest first), and cols put a leg
+        # that step i's rows carry innermost: the epilogue maps one thread to one
+        # row, so the row leg that varies fastest then writes consecutive
+        # addresses.
+        out_stride = [None] * nsteps          # label -> stride in step i's output
+        A_layout = [None] * nsteps            # (rows order, cols order, lda, stride map)
+        A_last, _, _, out_last, _ = logical[-1]
+        out_stride[-1] = dict(zip(out_last.labels, out_last.strides))
+        for i in range(nsteps - 1, -1, -1):
+            mlab, kl, nlab, dims = info[i]
+            ost = out_stride[i]
+            rows = sorted(mlab, key=lambda l: -ost[l])
+            if i > 0:
+                prev_m = set(info[i - 1][0])
+                cols = sorted(kl, key=lambda l: (l in prev_m, dims[l]))
+            else:
+                cols = list(kl)
+            K = int(np.prod([dims[l] for l in cols] or [1]))
             lda = _round8(K)
+            stride = {}
+            s_ = 1
+            for l in reversed(cols):
+                stride[l] = s_
+                s_ *= dims[l]
+            s_ = lda
+            for l in reversed(rows):
+                stride[l] = s_
+                s_ *= dims[l]
+            A_layout[i] = (rows, cols, lda, stride)
+            if i > 0:
+                out_stride[i - 1] = stride
+        for i, (A, B, kl, out, kw) in enumerate(logical):
+            mlab, _, nlab, dims = info[i]
+            rows, cols, lda, stride = A_layout[i]
+            M = int(np.prod([dims[l] for l in rows] or [1]))
+            N = int(np.prod([dims[l] for l in nlab] or [1]))
+            K = int(np.prod([dims[l] for l in cols] or [1]))
+            self.flops += 8 * M * N * K
             aslot = f"mp{i % 2}"
             plane = M * lda
             if i == 0:
                 d = ConvertDesc()
-                _set_modes(d.rows, [dimA[l] for l in mlab], [A.strides[A.labels.index(l)] for l in mlab], "stride_a")
-                _set_modes(d.cols, [dimA[l] for l in kl], [A.strides[A.labels.index(l)] for l in kl], "stride_a")
+                _set_modes(d.rows, [dims[l] for l in rows], [A.strides[A.labels.index(l)] for l in rows], "stride_a")
+                _set_modes(d.cols, [dims[l] for l in cols], [A.strides[A.labels.index(l)] for l in cols], "stride_a")
                 d.ld, d.plane, d.conj, d.levels = lda, plane, int(kw.get("conj_a", False)), L
                 self.ops.append(("conv", d, (A.ref, ("ws", aslot))))
                 self._need(aslot, 2 * L * plane)
-            else:
-                # the previous GEMM already wrote this step's A in [mlab][kl] order
-                assert prev_layout[0] == aslot and prev_layout[2] == lda
             ldb = _round8(K)
             d = ConvertDesc()
-            _set_modes(d.rows, [dimB[l] for l in nlab], [B.strides[B.labels.index(l)] for l in nlab], "stride_a")
-            _set_modes(d.cols, [dimB[l] for l in kl], [B.strides[B.labels.index(l)] for l in kl], "stride_a")
+            _set_modes(d.rows, [dims[l] for l in nlab], [B.strides[B.labels.index(l)] for l in nlab], "stride_a")
+            _set_modes(d.cols, [dims[l] for l in cols], [B.strides[B.labels.index(l)] for l in cols], "stride_a")
             d.ld, d.plane, d.conj, d.levels = ldb, 0, int(kw.get("conj_b", False)), L
             self.ops.append(("expand", d, (B.ref, ("ws", "bx"))))
             self._need("bx", 3 * L * N * ldb)
             g = CgemmDesc()
             g.lda, g.a_plane, g.M, g.K, g.ldb, g.N = lda, plane, M, K, ldb, N
             g.levels = L
+            ost = out_stride[i]
             if i < nsteps - 1:
-                nA, nB, nkl, _, _ = logical[i + 1]
-                nm = [l for l in nA.labels if l not in nkl]
-                ndim = dict(zip(nA.labels, nA.dims))
-                nK = int(np.prod([ndim[l] for l in nkl] or [1]))
-                nM = int(np.prod([ndim[l] for l in nm] or [1]))
-                nlda = _round8(nK)
-                stride = {}
-                s_ = 1
-                for l in reversed(nkl):
-                    stride[l] = s_
-                    s_ *= ndim[l]
-                s_ = nlda
-                for l in reversed(nm):
-                    stride[l] = s_
-                    s_ *= ndim[l]
+                nrows, ncols, nlda, _ = A_layout[i + 1]
+                nM = int(np.prod([info[i + 1][3][l] for l in nrows] or [1]))
                 cslot = f"mp{(i + 1) % 2}"
                 g.out_kind = 1
                 g.c_plane = nM * nlda
                 self._need(cslot, 2 * L * nM * nlda)
-                _set_modes(g.m_out, [dimA[l] for l in mlab], [stride[l] for l in mlab], "stride_c")
-                _set_modes(g.n_out, [dimB[l] for l in nlab], [stride[l] for l in nlab], "stride_c")
-                prev_layout = (cslot, stride, nlda, nM * nlda)
+                _set_modes(g.m_out, [dims[l] for l in rows], [ost[l] for l in rows], "stride_c")
+                _set_modes(g.n_out, [dims[l] for l in nlab], [ost[l] for l in nlab], "stride_c")
                 self.ops.append(("gemm", g, (("ws", aslot), ("ws", "bx"), ("ws", cslot))))
             else:
                 g.out_kind = 0
                 g.c_plane = 0
-                _set_modes(g.m_out, [dimA[l] for l in mlab], [out.strides[out.labels.index(l)] for l in mlab],
-                           "stride_c")
-                _set_modes(g.n_out, [dimB[l] for l in nlab], [out.strides[out.labels.index(l)] for l in nlab],
-                           "stride_c")
+                _set_modes(g.m_out, [dims[l] for l in rows], [ost[l] for l in rows], "stride_c")
+                _set_modes(g.n_out, [dims[l] for l in nlab], [ost[l] for l in nlab], "stride_c")
                 self.ops.append(("gemm", g, (("ws", aslot), ("ws", "bx"), out.ref)))
 
     def _need(self, name, numel):
@@ -629,7 +647,7 @@ class DeviceNetwork:
         y = Operand.contiguous(("out",), ["x", "y"], [chi_q, chi_n])
         T = cb.contract(eq, r, ["a"])
         cb.contract(T, en, ["c", "b"], out=y)
-        p = cb.plan()
+        p = cb.mixed_plan(self.levels) if self.levels else cb.plan()
         self.plans[key] = p
         return p
 
@@ -710,14 +728,14 @@ class DeviceNetwork:
         self.flops += 8 * 2 * m * k * k
         return R
 
-    def absorb(self, R: torch.Tensor, src, dst, link_variant: bool):
+    def absorb(self, R: torch.Tensor, src, dst, link_variant: bool, precise: bool = False):
         """dst[..., new, ...] = sum_a R[new, a] dst[..., a, ...] on dst's leg toward src.
         Logical order as in ``contract_nodes`` (``contractions/node_contraction.py:88-138``)."""
         st = self.state
         shape = self.shape(dst)
         n = len(shape) - 1
         ax = st.phys_axis(dst, src)
-        key = ("absorb", dst, src)
+        key = ("absorb", dst, src, precise)
         if key not in self.plans:
             cb = ChainBuilder(self.ws)
             Rop = Operand.contiguous(("in",), ["new", f"a{ax}"], [shape[ax], shape[ax]])
@@ -725,9 +743,15 @@ class DeviceNetwork:
             labels = [f"a{k}" if k != ax else "new" for k in range(n)] + ["s"]
             out = Operand.contiguous(("ws", "absorb"), labels, shape)
             cb.sizes["absorb"] = out.numel()
-            cb.contract(Rop, T, [f"a{ax}"], out=out)
-            self.plans[key] = cb.plan()
+            cb.contract(T, Rop, [f"a{ax}"], out=out)
+            if self.levels and not precise:
+                mp = cb.mixed_plan(self.levels)
+                mp.sizes_c128 = dict(cb.sizes)
+                self.plans[key] = mp
+            else:
+                self.plans[key] = cb.plan()
         p = self.plans[key]
+        self.ws.get("absorb", self.t[dst].numel())
         p.run(R.data_ptr(), 0)
         self.t[dst].view(-1).copy_(self.ws.bufs["absorb"][:self.t[dst].numel()])
         self.flops += p.flops
@@ -737,9 +761,9 @@ class DeviceNetwork:
             others = [c for c in dn.children if c != src]
             dn.children = ([src] + others) if link_variant else (others + [src])
 
-    def move_orth_one_hop(self, a, b):
+    def move_orth_one_hop(self, a, b, precise: bool = False):
         R = self.qr_split(a, b)
-        self.absorb(R, a, b, link_variant=False)
+        self.absorb(R, a, b, link_variant=False, precise=precise)
 
     def move_orth_center(self, new_center):
         st = self.state
@@ -770,7 +794,9 @@ class DeviceNetwork:
         for d in range(maxd, 0, -1):
             for nid in [x for x in dist if dist[x] == d]:
                 target = min(st.nodes[nid].neighbouring_nodes(), key=lambda x: dist[x])
-                self.move_orth_one_hop(nid, target)
+                # complex128 here: before normalisation the state's norm can be far
+                # outside the BF16/FP32 range (1e-55 for 61 unit-norm random tensors)
+                self.move_orth_one_hop(nid, target, precise=True)
         st.orthogonality_center_id = center
 
     # -- observables ------------------------------------------------------------------

@@ -414,6 +414,15 @@ class KrylovSolver:
     def __init__(self, ws: Workspace):
         self.ws = ws
         self.depths: list[int] = []
+        self._host = None
+
+    def _pinned(self, n):
+        if self._host is None or self._host[0].numel() < n:
+            pin = self.ws.device.type == "cuda"
+            self._host = (torch.empty(max(n, 64), dtype=CDT, pin_memory=pin),
+                          torch.empty(2, dtype=torch.float64, pin_memory=pin),
+                          torch.zeros(1, dtype=torch.int32, pin_memory=pin))
+        return self._host
 
     def expm(self, x: torch.Tensor, apply, dt: float, exp_factor: complex, krylov_tol=1e-10,
              max_krylov_dim=None, hermitian=True, out: torch.Tensor | None = None,
@@ -460,11 +469,20 @@ class KrylovSolver:
                 check(lib.ptn_zaxpy_multi(Q.data_ptr(), n, nq, h.data_ptr(), w.data_ptr(), n, stream),
                       "zaxpy_multi")
             check(lib.ptn_dznrm2(w.data_ptr(), n, scal[1:].data_ptr(), part.data_ptr(), stream), "dznrm2")
-            hh = hbuf[:2 * nq].cpu().numpy()
-            sc = scal[:2].cpu().numpy()
+            # one synchronisation per step: projections, norms and the status
+            # word go to pinned host memory asynchronously, then the stream syncs
+            hh_host, sc_host, st_host = self._pinned(2 * nq)
+            hh_host[:2 * nq].copy_(hbuf[:2 * nq], non_blocking=True)
+            sc_host.copy_(scal[:2], non_blocking=True)
             st = self.ws.bufs.get("tc_status")
-            if st is not None and int(st.item()) != 0:
-                code = int(st.item())
+            if st is not None:
+                st_host.copy_(st[:1], non_blocking=True)
+            if self.ws.device.type == "cuda":
+                torch.cuda.current_stream().synchronize()
+            hh = hh_host[:2 * nq].numpy()
+            sc = sc_host.numpy()
+            if st is not None and int(st_host[0]) != 0:
+                code = int(st_host[0])
                 st.zero_()
                 raise _lib.PtnError(code, "tensor-core contraction inside the Krylov exponential")
             w0, beta = float(sc[0]), float(sc[1])
@@ -551,6 +569,23 @@ class DeviceNetwork:
         self.plans: dict = {}
         self.rowoff: dict = {}
         self.flops = 0
+        # QR launch sequences are captured into CUDA graphs (one per node and
+        # direction) after their first eager run; R and the work area then
+        # must never move, so they are sized for the largest split up front.
+        self.use_graphs = True
+        self.qr_graphs: dict = {}
+        self.qr_seen: set = set()
+        self.cholqr_fails: set = set()
+        self.graph_launches = 0
+        lib = _lib.load()
+        kmax, wmax = 1, 1
+        for nid in state._order:
+            n = self.t[nid].numel()
+            for k in self.t[nid].shape[:-1]:
+                kmax = max(kmax, k)
+                wmax = max(wmax, int(lib.ptn_zqr_work_bytes(n // k, k)))
+        self.qr_R = torch.zeros((kmax * kmax,), dtype=CDT, device=self.device)
+        self.qr_work = torch.zeros(((wmax + 15) // 16,), dtype=CDT, device=self.device)
 
     # -- shapes ------------------------------------------------------------------
     def nbrs(self, nid):
@@ -695,6 +730,61 @@ class DeviceNetwork:
         return self.krylov.expm(r, apply, dt, exp_factor, tol, maxdim, out=r, tridiagonal=self.levels > 0)
 
     # -- QR split and R absorption ---------------------------------------------------
+    CHOLQR_MIN_ROWS = 256
+
+    def _cholqr2(self, nid, row_axes, col_axis) -> torch.Tensor | None:
+        """Mixed path, tall full-rank matrices: CholeskyQR2 with the Gram matrices
+        and the triangular solves on the tensor cores (BF16x6, FP32-level) and the
+        k x k Cholesky factorisations on the host. Returns R, or None when the
+        matrix is too ill-conditioned (then the caller falls back to Householder).
+        Q differs from the Householder Q only by a diagonal phase, which the
+        one-site TDVP absorbs as a gauge transformation."""
+        shape = self.shape(nid)
+        n = len(shape) - 1
+        labels = [f"a{i}" for i in range(n)] + ["s"]
+        rows = [labels[a] for a in row_axes]
+        col = labels[col_axis]
+        k = shape[col_axis]
+        key = ("cholqr", nid, tuple(row_axes), col_axis)
+        if key not in self.plans:
+            Gt = torch.zeros((k, k), dtype=CDT, device=self.device)
+            Rinv = torch.zeros((k, k), dtype=CDT, device=self.device)
+            cb = ChainBuilder(self.ws)
+            A1 = Operand.contiguous(("fixed", self.t[nid]), [l if l != col else "p" for l in labels], shape)
+            A2 = Operand.contiguous(("fixed", self.t[nid]), [l if l != col else "q" for l in labels], shape)
+            cb.contract(A1, A2, rows, out=Operand.contiguous(("fixed", Gt), ["p", "q"], [k, k]), conj_a=True)
+            gram = cb.mixed_plan(self.levels)
+            cb = ChainBuilder(self.ws)
+            A = Operand.contiguous(("fixed", self.t[nid]), [l if l != col else "p" for l in labels], shape)
+            Ri = Operand.contiguous(("fixed", Rinv), ["p", "q"], [k, k])
+            out = Operand.contiguous(("ws", "cholqr_out"), [l if l != col else "q" for l in labels], shape)
+            cb.contract(A, Ri, ["p"], out=out)
+            apply = cb.mixed_plan(self.levels)
+            self.plans[key] = (gram, apply, Gt, Rinv)
+        gram, apply, Gt, Rinv = self.plans[key]
+        Rtot = None
+        for _ in range(2):
+            gram.run()
+            G = Gt.cpu().numpy()
+            G = 0.5 * (G + G.conj().T)
+            try:
+                Lc = np.linalg.cholesky(G)
+            except np.linalg.LinAlgError:
+                return None
+            d = np.abs(np.diag(Lc))
+            if d.min() <= 1e-3 * d.max():
+                return None
+            R = Lc.conj().T                         # G = R^H R, R upper triangular
+            Rinv.copy_(torch.from_numpy(np.ascontiguousarray(np.linalg.inv(R))).to(self.device))
+            self.ws.get("cholqr_out", self.t[nid].numel())
+            apply.run()
+            self.t[nid].view(-1).copy_(self.ws.bufs["cholqr_out"][:self.t[nid].numel()])
+            Rtot = R if Rtot is None else R @ Rtot
+            self.flops += gram.flops + apply.flops
+        Rd = self.qr_R[:k * k].view(k, k)
+        Rd.copy_(torch.from_numpy(np.ascontiguousarray(Rtot)).to(self.device))
+        return Rd
+
     def qr_split(self, nid, nbr) -> torch.Tensor:
         """tensor[nid] <- Q (KEEP), returns R (k x k; legs: new bond, nbr-side bond).
         Rows in the reference's logical order (``util/tensor_splitting.py:60-107``)."""
@@ -719,10 +809,44 @@ class DeviceNetwork:
         m = rowoff.numel()
         k = shape[col_axis]
         lib = _lib.load()
-        R = self.ws.get(f"qr_R", k * k).view(k, k)
-        work = self.ws.get("qr_work", (int(lib.ptn_zqr_work_bytes(m, k)) + 15) // 16)
-        check(lib.ptn_zqr_keep(self.t[nid].data_ptr(), rowoff.data_ptr(), m, k, strides[col_axis],
-                               R.data_ptr(), work.data_ptr(), _stream_ptr()), "ptn_zqr_keep")
+        ckey = (nid, tuple(row_axes), col_axis)
+        if self.levels and m >= self.CHOLQR_MIN_ROWS and m >= 2 * k and ckey not in self.cholqr_fails:
+            backup = self.ws.get("cholqr_backup", self.t[nid].numel())
+            backup.copy_(self.t[nid].view(-1))
+            R = self._cholqr2(nid, row_axes, col_axis)
+            if R is not None:
+                if node.parent != nbr:
+                    node.children = [nbr] + [c for c in node.children if c != nbr]
+                return R
+            # rank-deficient (e.g. zero-padded bonds): keep LAPACK's Householder
+            # complement, which the one-site TDVP result depends on
+            self.cholqr_fails.add(ckey)
+            self.t[nid].view(-1).copy_(backup)
+        R = self.qr_R[:k * k].view(k, k)
+        work = self.qr_work
+
+        def launch():
+            check(lib.ptn_zqr_keep(self.t[nid].data_ptr(), rowoff.data_ptr(), m, k, strides[col_axis],
+                                   R.data_ptr(), work.data_ptr(), _stream_ptr()), "ptn_zqr_keep")
+        gkey = (nid, nbr, key)
+        if not self.use_graphs or self.device.type != "cuda":
+            launch()
+        elif gkey in self.qr_graphs:
+            g, nlaunch = self.qr_graphs[gkey]
+            g.replay()
+            self.graph_launches += nlaunch
+        elif gkey in self.qr_seen:
+            g = torch.cuda.CUDAGraph()
+            c0 = int(lib.ptn_launch_counter())
+            with torch.cuda.graph(g):
+                launch()
+            nlaunch = int(lib.ptn_launch_counter()) - c0
+            self.qr_graphs[gkey] = (g, nlaunch)
+            g.replay()
+            self.graph_launches += nlaunch
+        else:
+            self.qr_seen.add(gkey)
+            launch()
         if node.parent != nbr:
             node.children = [nbr] + [c for c in node.children if c != nbr]
         self.flops += 8 * 2 * m * k * k

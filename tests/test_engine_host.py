@@ -74,3 +74,25 @@ def test_engine_host_mixed_layouts(monkeypatch, name, precision):
     got = O.OState(oracle_state(c).tree, {nid: algo.state.get_phys_numpy(nid) for nid, _ in c["spec"]})
     one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), got)
     assert one_minus_f < (1e-8 if precision == "bf16x3" else 1e-11)
+
+
+def test_engine_host_cholqr2_split(monkeypatch):
+    """Mixed path, tall full-rank split: CholeskyQR2 (tensor-core Gram and
+    solves) gives an isometric Q with Q R = A, like the Householder split."""
+    fake_ptn.install(monkeypatch)
+    import torch
+    from pytreenet_gb300.workloads import t_tree_state, t_tree_heisenberg
+    from pytreenet_gb300.engine import DeviceNetwork
+    st, spec, tensors = t_tree_state(arm_len=1, chi=64, seed=4)
+    H, _ = t_tree_heisenberg(st, seed=5)
+    net = DeviceNetwork(st, H, precision="mixed")
+    A0 = net.t["root"].clone()
+    R = net.qr_split("root", "a1_0").clone()
+    Q = net.t["root"]
+    # root legs (a0_0, a1_0, a2_0, s); split toward a1_0 (axis 1)
+    Qm = Q.permute(0, 2, 3, 1).reshape(-1, 64).numpy()
+    Am = A0.permute(0, 2, 3, 1).reshape(-1, 64).numpy()
+    assert np.max(np.abs(Qm.conj().T @ Qm - np.eye(64))) < 1e-6
+    assert np.max(np.abs(Qm @ R.numpy() - Am)) < 1e-6 * np.max(np.abs(Am))
+    assert np.allclose(np.tril(R.numpy(), -1), 0)
+    assert net.state.nodes["root"].children[0] == "a1_0"

@@ -730,7 +730,7 @@ class DeviceNetwork:
         return self.krylov.expm(r, apply, dt, exp_factor, tol, maxdim, out=r, tridiagonal=self.levels > 0)
 
     # -- QR split and R absorption ---------------------------------------------------
-    CHOLQR_MIN_ROWS = 256
+    CHOLQR_MIN_ROWS = 8192
 
     def _cholqr2(self, nid, row_axes, col_axis) -> torch.Tensor | None:
         """Mixed path, tall full-rank matrices: CholeskyQR2 with the Gram matrices

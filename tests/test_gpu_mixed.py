@@ -63,28 +63,31 @@ def test_cgemm_bf16_matches_complex128(lib, M, N, K, levels, tol):
 
 
 def test_cgemm_chain_matches_fp64_plan(lib):
-    """A three-step chain (the degree-2 site matvec) on both paths."""
-    import pytreenet_gb300 as P
+    """The degree-2 and degree-3 site matvecs on both paths, same operands."""
     from pytreenet_gb300.workloads import t_tree_state, t_tree_heisenberg
     from pytreenet_gb300.engine import DeviceNetwork
     st, spec, tensors = t_tree_state(arm_len=3, chi=32, seed=2)
     H, _ = t_tree_heisenberg(st, seed=3)
-    outs = {}
-    for prec in ("plain", "bf16x3", "bf16x6"):
-        st2, _, _ = t_tree_state(arm_len=3, chi=32, seed=2)
-        net = DeviceNetwork(st2, H, precision=prec)
-        st2.orthogonality_center_id = None
-        net.canonical_form("a0_1")
-        net.init_cache_but_one("a0_1")
-        x = net.t["a0_1"].clone()
-        y = torch.zeros_like(x)
-        net.heff_plan("a0_1").run(x.data_ptr(), y.data_ptr())
-        torch.cuda.synchronize()
-        outs[prec] = y.cpu().numpy()
-    rel3 = np.linalg.norm(outs["bf16x3"] - outs["plain"]) / np.linalg.norm(outs["plain"])
-    rel6 = np.linalg.norm(outs["bf16x6"] - outs["plain"]) / np.linalg.norm(outs["plain"])
-    assert rel3 < 1e-4, rel3
-    assert rel6 < 2e-6, rel6
+    ref = DeviceNetwork(st, H, precision="plain")
+    ref.canonical_form("a0_1")
+    ref.init_cache_but_one("a0_1")
+    ref.init_cache_but_one("root")
+    for nid in ("a0_1", "root"):
+        outs = {}
+        for prec in ("plain", "bf16x3", "bf16x6"):
+            st2, _, _ = t_tree_state(arm_len=3, chi=32, seed=2)
+            net = DeviceNetwork(st2, H, precision=prec)
+            for key, e in ref.env.items():
+                net.env_buf(*key).copy_(e)
+            x = ref.t[nid].clone()
+            y = torch.zeros_like(x)
+            net.heff_plan(nid).run(x.data_ptr(), y.data_ptr())
+            torch.cuda.synchronize()
+            outs[prec] = y.cpu().numpy()
+        rel3 = np.linalg.norm(outs["bf16x3"] - outs["plain"]) / np.linalg.norm(outs["plain"])
+        rel6 = np.linalg.norm(outs["bf16x6"] - outs["plain"]) / np.linalg.norm(outs["plain"])
+        assert rel3 < 1e-4, (nid, rel3)
+        assert rel6 < 2e-6, (nid, rel6)
 
 
 @pytest.mark.parametrize("name", ["ttree3_heis_chi6_o1", "ternary2_xxz_chi4_o1"])

@@ -255,11 +255,13 @@ def run_gb300(args, rank, world):
     l0 = lib.ptn_launch_counter() + net.graph_launches
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with Clocks(torch.cuda.current_device()) as clk:
+        torch.cuda.nvtx.range_push("timed_region")
         start.record()
         for _ in range(args.steps):
             algo.run_one_time_step()
         stop.record()
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
     if dist:
         dist.barrier()
     launches = int(lib.ptn_launch_counter() + net.graph_launches - l0)

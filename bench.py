@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "plain"])
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison sweep")
+    ap.add_argument("--no-graphs", action="store_true",
+                    help="launch the QR sequences eagerly instead of replaying CUDA graphs")
     return ap.parse_args()
 
 
@@ -224,6 +226,7 @@ def run_gb300(args, rank, world):
         return a
     algo = make(args.precision)
     net = algo.net
+    net.use_graphs = not args.no_graphs
     for _ in range(args.warmup):
         algo.run_one_time_step()
     torch.cuda.synchronize()

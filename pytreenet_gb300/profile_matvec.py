@@ -37,10 +37,12 @@ def main():
     plan = net.heff_plan(a.node)
     plan.run(x.data_ptr(), y.data_ptr())
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("matvec")
     t0 = time.perf_counter()
     for _ in range(a.reps):
         plan.run(x.data_ptr(), y.data_ptr())
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     dt = (time.perf_counter() - t0) / a.reps
     print(f"{a.node} matvec chi={a.chi} {a.precision}: {dt * 1e3:.3f} ms, "
           f"{plan.flops / dt / 1e12:.1f} TFLOP/s algorithmic")

@@ -1,4 +1,4 @@
-"""NumPy restatement of PyTreeNet's one-site TDVP hot path (oracle, test infrastructure).
+"""NumPy restatement of PyTreeNet's one-site and two-site TDVP hot path (oracle, test infrastructure).
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
 ``bench.py`` may use this module; the GPU engine never imports it.
@@ -25,7 +25,9 @@ __all__ = [
     "env_update", "krylov_exp_action", "qr_keep_split", "canonical_form",
     "leaf_to_root_path", "orthogonalisation_paths", "FirstOrderOneSiteTDVPOracle",
     "SecondOrderOneSiteTDVPOracle", "state_vector", "expect_product",
-    "scalar_product",
+    "scalar_product", "SVDParams", "truncate_singular_values", "two_site_merge",
+    "two_site_heff_apply", "two_site_split", "SecondOrderTwoSiteTDVPOracle",
+    "FirstOrderTwoSiteTDVPOracle",
 ]
 
 
@@ -585,3 +587,197 @@ def state_vector(state: OState, site_order):
     T, sites = rec(tree.root, None)
     perm = [sites.index(s) for s in site_order]
     return np.transpose(T, perm).reshape(-1)
+
+
+# ----------------------------------------------------------------------------
+# truncated SVD and two-site TDVP
+# ----------------------------------------------------------------------------
+class SVDParams:
+    """Fields of ``SVDParameters`` (``util/tensor_splitting.py:253-328``)."""
+
+    def __init__(self, max_bond_dim=100, rel_tol=1e-15, total_tol=1e-15, renorm=False,
+                 sum_trunc=False, sum_renorm=False):
+        self.max_bond_dim = max_bond_dim
+        self.rel_tol = rel_tol
+        self.total_tol = total_tol
+        self.renorm = renorm
+        self.sum_trunc = sum_trunc
+        self.sum_renorm = sum_renorm
+
+
+def truncate_singular_values(s, p: SVDParams):
+    """Number of singular values kept and their (possibly renormalised) values
+    (``truncate_singular_values``, ``value_truncation``, ``_sum_truncation_index``,
+    ``renormalise_singular_values``; ``util/tensor_splitting.py:330-486``).
+    ``s`` is sorted in descending order."""
+    s = np.asarray(s, dtype=float)
+    if len(s) == 0:
+        raise ValueError("No singular values to truncate!")
+    if p.sum_trunc:
+        normsq = float(np.linalg.norm(s)) ** 2
+        keep = 0
+        if normsq != 0.0:
+            acc = 0.0
+            for i, v in enumerate(s[::-1]):
+                acc += v * v
+                if (acc / normsq if p.sum_renorm else acc) > p.total_tol ** 2:
+                    keep = len(s) - i
+                    break
+    else:
+        cut = max(p.rel_tol * s[0], p.total_tol)
+        keep = int(np.count_nonzero(s > cut))
+    keep = min(keep, p.max_bond_dim)
+    if keep == 0:
+        keep = 1
+    new_s = s[:keep].copy()
+    if p.renorm:
+        new_s = new_s * np.linalg.norm(s) / np.linalg.norm(new_s)
+    return keep, new_s
+
+
+def two_site_merge(state: OState, u: str, v: str):
+    """Contract the tensors of neighbours ``u`` and ``v`` (``contract_nodes``,
+    ``contractions/node_contraction.py:12-141``). Returns the merged tensor
+    with legs (u's other neighbours in physical order, s_u, v's other
+    neighbours in physical order, s_v) and the two neighbour lists."""
+    tree = state.tree
+    nu = [x for x in tree.neighbours(u) if x != v]
+    nv = [x for x in tree.neighbours(v) if x != u]
+    A = _L(state.tensors[u], [f"u:{x}" if x != v else "bond" for x in tree.neighbours(u)] + ["su"])
+    B = _L(state.tensors[v], [f"v:{x}" if x != u else "bond" for x in tree.neighbours(v)] + ["sv"])
+    T = A.dot(B, ["bond"])
+    return T.out([f"u:{x}" for x in nu] + ["su"] + [f"v:{x}" for x in nv] + ["sv"]), nu, nv
+
+
+def two_site_heff_apply(x, nu, nv, u, v, Wu, Wv, tree: OTree, envs):
+    """H_eff of the merged pair applied to ``x`` (legs as ``two_site_merge``)
+    (``effective_two_site_evolution``, ``time_evo_util/effective_time_evolution.py:326-410``:
+    the two TTNO tensors joined over their shared bond, then the single-site
+    contraction of ``contract_ket_ham_with_envs``)."""
+    lab_x = [f"au{k}" for k in range(len(nu))] + ["su"] + [f"av{k}" for k in range(len(nv))] + ["sv"]
+    T = _L(x, lab_x)
+    for k, nb in enumerate(nu):
+        T = T.dot(_L(envs[(nb, u)], [f"au{k}", f"bu{k}", f"cu{k}"]), [f"au{k}"])
+    wl_u = [f"bu{nu.index(x)}" if x != v else "bw" for x in tree.neighbours(u)] + ["tu", "su"]
+    T = T.dot(_L(Wu, wl_u), [f"bu{k}" for k in range(len(nu))] + ["su"])
+    for k, nb in enumerate(nv):
+        T = T.dot(_L(envs[(nb, v)], [f"av{k}", f"bv{k}", f"cv{k}"]), [f"av{k}"])
+    wl_v = [f"bv{nv.index(x)}" if x != u else "bw" for x in tree.neighbours(v)] + ["tv", "sv"]
+    T = T.dot(_L(Wv, wl_v), [f"bv{k}" for k in range(len(nv))] + ["bw", "sv"])
+    return T.out([f"cu{k}" for k in range(len(nu))] + ["tu"] + [f"cv{k}" for k in range(len(nv))] + ["tv"])
+
+
+def two_site_split(state: OState, merged, nu, nv, u: str, v: str, params: SVDParams):
+    """Truncated SVD split of the merged pair; singular values go to ``v``
+    (``split_node_svd`` -> ``contr_truncated_svd_splitting`` with VCONTR,
+    ``core/ttn.py:1476-1497``, ``util/tensor_splitting.py:488-572``).
+    Rows are matricised in the reference's order (parent, logical children,
+    physical) on each side. Logical order afterwards: the node that gains a
+    child through the split lists it first (``core/ttn.py:1400-1448``).
+    Returns the kept singular values."""
+    tree = state.tree
+
+    def side(node, other, nbrs):
+        p = tree.parent[node]
+        order = ([p] if (p is not None and p != other) else []) + [c for c in tree.lchildren[node] if c != other]
+        return [nbrs.index(x) for x in order]
+    iu = side(u, v, nu)
+    iv = side(v, u, nv)
+    nuu = len(nu)
+    row_axes = iu + [nuu]
+    col_axes = [nuu + 1 + i for i in iv] + [nuu + 1 + len(nv)]
+    mat = np.transpose(merged, row_axes + col_axes)
+    rshape = mat.shape[:len(row_axes)]
+    cshape = mat.shape[len(row_axes):]
+    mat = mat.reshape(int(np.prod(rshape)), int(np.prod(cshape)))
+    U, s, Vh = np.linalg.svd(mat, full_matrices=False)
+    r, new_s = truncate_singular_values(s, params)
+    U = U[:, :r].reshape(list(rshape) + [r])
+    SV = (new_s[:, None] * Vh[:r, :]).reshape([r] + list(cshape))
+    # U legs: (u's row legs in reference order, bond) -> u's physical layout
+    labels_u = [nu[i] for i in iu] + ["#phys", v]
+    tgt_u = tree.neighbours(u) + ["#phys"]
+    state.tensors[u] = np.ascontiguousarray(np.transpose(U, [labels_u.index(x) for x in tgt_u]))
+    labels_v = [u] + [nv[i] for i in iv] + ["#phys"]
+    tgt_v = tree.neighbours(v) + ["#phys"]
+    state.tensors[v] = np.ascontiguousarray(np.transpose(SV, [labels_v.index(x) for x in tgt_v]))
+    if tree.parent[v] == u:
+        tree.lchildren[u] = [v] + [c for c in tree.lchildren[u] if c != v]
+    else:
+        tree.lchildren[v] = [u] + [c for c in tree.lchildren[v] if c != u]
+    return new_s
+
+
+class _TwoSiteBase(_OneSiteBase):
+    """``TwoSiteTDVP`` (``tdvp_algorithms/twositetdvp.py:29-146``)."""
+
+    def __init__(self, state: OState, W: dict, dt: float, svd: SVDParams, krylov_tol=1e-10,
+                 max_krylov_dim=None):
+        super().__init__(state, W, dt, krylov_tol, max_krylov_dim)
+        self.svd = svd
+        self.bond_history = []
+
+    def update_two_sites(self, u, v, factor=1.0):
+        """``_update_two_site_nodes`` (``twositetdvp.py:89-125``)."""
+        assert self.state.orth_center == u
+        tree = self.state.tree
+        x, nu, nv = two_site_merge(self.state, u, v)
+        act = lambda y: two_site_heff_apply(y, nu, nv, u, v, self.W[u], self.W[v], tree, self.envs)
+        x = self._krylov(x, act, factor, -1j)
+        s = two_site_split(self.state, x, nu, nv, u, v, self.svd)
+        self.bond_history.append(len(s))
+        self.state.orth_center = v
+        self.envs[(u, v)] = env_update(tree, u, v, self.state.tensors[u], self.W[u], self.envs)
+
+    def backward_site(self, nid, factor=1.0):
+        """``_single_site_backwards_update`` (``twositetdvp.py:127-138``)."""
+        self.update_site(nid, -factor)
+
+
+class SecondOrderTwoSiteTDVPOracle(_TwoSiteBase):
+    """``SecondOrderTwoSiteTDVP.run_one_time_step`` (``secondordertwosite.py:55-193``)."""
+
+    def __init__(self, *a, **k):
+        super().__init__(*a, **k)
+        self.back_path = list(reversed(self.update_path))
+        self.back_orth = [list(reversed(p)) for p in reversed(self.orth_paths)]
+
+    def run_one_time_step(self):
+        path, orth = self.update_path, self.orth_paths
+        for i, nid in enumerate(path[:-2]):
+            if i > 0:
+                self.move_orth_and_update_cache(orth[i - 1])
+            nxt = orth[i][0]
+            self.update_two_sites(nid, nxt, 0.5)
+            self.backward_site(nxt, 0.5)
+        self.update_two_sites(path[-2], path[-1], 0.5)
+        bp = self.back_path
+        for i in range(len(bp) - 1):
+            if i == 0:
+                self.update_two_sites(bp[0], bp[1], 0.5)
+                continue
+            op = self.back_orth[i]
+            self.move_orth_and_update_cache(op)
+            tgt = op[-1]
+            self.backward_site(tgt, 0.5)
+            self.update_two_sites(tgt, bp[i + 1], 0.5)
+
+
+class FirstOrderTwoSiteTDVPOracle(_TwoSiteBase):
+    """``FirstOrderTwoSiteTDVP.run_one_time_step`` (``firstordertwosite.py:11-30``) as
+    intended: the partner of update-path node i is the first node of the
+    i-th orthogonalisation sub-path, and the environments are rebuilt after
+    the centre returns to the start (as ``firstorderonesite.py:66-75`` does).
+    The reference indexes sub-path i+1 and raises ValueError on the second
+    pair of any tree with a branching root."""
+
+    def run_one_time_step(self):
+        path, orth = self.update_path, self.orth_paths
+        for i, nid in enumerate(path[:-2]):
+            nxt = orth[i][0]
+            self.update_two_sites(nid, nxt)
+            self.backward_site(nxt)
+            self.move_orth_and_update_cache(orth[i])
+        self.update_two_sites(path[-2], path[-1])
+        move_orth_center(self.state, path[0])
+        self.envs = init_cache_but_one(self.state, self.W, path[0])

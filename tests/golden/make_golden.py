@@ -215,6 +215,86 @@ def run_case(ptn, name, spec, tensors, ham_fn, dt, steps, order, tol, canonical_
     print(name, "written; path", algo.update_path[:6], "...")
 
 
+def neel_state_tensors(spec):
+    """Neel product state by depth parity, every bond of dimension 1."""
+    ch = children_of(spec)
+    parent = dict(spec)
+    depth = {}
+    out = {}
+    for nid, p in spec:
+        depth[nid] = 0 if p is None else depth[p] + 1
+        v = np.array([1, 0], dtype=complex) if depth[nid] % 2 == 0 else np.array([0, 1], dtype=complex)
+        nv = len(ch[nid]) + (0 if p is None else 1)
+        out[nid] = v.reshape([1] * nv + [2])
+    return out
+
+
+def run_case_two_site(ptn, name, spec, tensors, ham_fn, dt, steps, tol, svd, canonical_random=False):
+    """Second-order two-site TDVP (``secondordertwosite.py``) with truncation ``svd``
+    = (max_bond_dim, rel_tol, total_tol, renorm)."""
+    from pytreenet.time_evolution.time_evolution import TimeEvoMode
+    from pytreenet.time_evolution.tdvp_algorithms.twositetdvp import TwoSiteTDVPConfig
+    from pytreenet.time_evolution.tdvp_algorithms.secondordertwosite import SecondOrderTwoSiteTDVP
+    psi = build_reference_state(ptn, spec, tensors)
+    if canonical_random:
+        psi.canonical_form(spec[0][0])
+        psi.normalise()
+        tensors = export_state(psi, spec)
+        psi = build_reference_state(ptn, spec, tensors)
+    H = ptn.TTNO.from_hamiltonian(ham_fn(psi), psi)
+    ops = {nid: ptn.TensorProduct({nid: Z}) for nid, _ in spec}
+    maxd, rel, tot, renorm = svd
+    cfg = TwoSiteTDVPConfig(time_evo_mode=TimeEvoMode.KRYLOV, max_bond_dim=maxd, rel_tol=rel,
+                            total_tol=tot, renorm=renorm)
+    algo = SecondOrderTwoSiteTDVP(psi, H, dt, dt * steps, ops, config=cfg,
+                                  solver_options={"krylov_tol": tol})
+    rec = {"spec_ids": np.array([s[0] for s in spec]),
+           "spec_parents": np.array(["" if s[1] is None else s[1] for s in spec]),
+           "dt": dt, "steps": steps, "order": 2, "krylov_tol": tol,
+           "two_site": 1, "svd_max_bond_dim": maxd, "svd_rel_tol": rel, "svd_total_tol": tot,
+           "svd_renorm": int(renorm), "update_path": np.array(algo.update_path)}
+    for nid, t in tensors.items():
+        rec[f"init/{nid}"] = t
+    for nid, t in export_ttno(H, spec).items():
+        rec[f"ttno/{nid}"] = t
+    zs = []
+    for step in range(steps):
+        algo.run_one_time_step()
+        zs.append([algo.state.operator_expectation_value(ops[nid]) for nid, _ in spec])
+    rec["z"] = np.array(zs)
+    for nid, t in export_state(algo.state, spec).items():
+        rec[f"final/{nid}"] = t
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **rec)
+    print(name, "written; max bond", algo.state.max_bond_dim())
+
+
+def svd_cases():
+    """Truncation known answers: the reference's own truncation of fixed spectra."""
+    from pytreenet.util.tensor_splitting import SVDParameters, truncate_singular_values
+    rec = {}
+    spectra = [np.array([1.0, 0.5, 1e-3, 1e-9, 1e-12]), np.array([3.0, 3.0, 2.0, 1e-16]),
+               np.array([1e-20, 1e-21]), np.linspace(1.0, 0.01, 40)]
+    params = [(100, 1e-15, 1e-15, False, False), (2, 1e-15, 1e-15, False, False),
+              (100, 1e-10, 1e-10, False, False), (100, 1e-2, 1e-15, True, False),
+              (3, 1e-15, 1e-15, True, False), (100, 1e-15, 1e-3, False, True),
+              (100, 1e-15, 0.1, False, True)]
+    i = 0
+    for s in spectra:
+        for (maxd, rel, tot, renorm, sumt) in params:
+            p = SVDParameters(max_bond_dim=maxd, rel_tol=rel, total_tol=tot, renorm=renorm,
+                              sum_trunc=sumt)
+            import warnings
+            with warnings.catch_warnings():
+                warnings.simplefilter("ignore")
+                new_s, _ = truncate_singular_values(s, p)
+            rec[f"{i}/s"] = s
+            rec[f"{i}/params"] = np.array([maxd, rel, tot, float(renorm), float(sumt)])
+            rec[f"{i}/out"] = np.asarray(new_s)
+            i += 1
+    rec["n"] = i
+    return rec
+
+
 def unit_cases(ptn):
     """Krylov exponential and single-site matvec known answers."""
     from pytreenet.time_evolution.time_evolution import krylov_exp_action
@@ -231,6 +311,8 @@ def unit_cases(ptn):
             rec[f"krylov/{n}/{tag}/psi"] = psi
             rec[f"krylov/{n}/{tag}/out"] = out
             rec[f"krylov/{n}/{tag}/tol"] = tol
+    for k, v in svd_cases().items():
+        rec[f"svd/{k}"] = v
     np.savez_compressed(os.path.join(HERE, "units.npz"), **rec)
     print("units written")
 
@@ -263,6 +345,21 @@ def main(ref_root):
     run_case(ptn, "ternary2_xxz_chi4_o1", spec, random_state_tensors(spec, rng, 4),
              lambda psi: heisenberg_fields(ptn, spec, np.zeros(len(spec)), jxy, jz),
              0.02, 4, 1, 1e-12, canonical_random=True)
+    # Two-site TDVP (second order): ternary depth 2 from a Neel product state
+    # (bond dimensions grow from 1), and a random binary tree truncated by
+    # max_bond_dim with renormalisation.
+    spec = ternary_tree(2)
+    ne = len(spec) - 1
+    jxy = rng.uniform(0.5, 1.5, size=ne)
+    jz = rng.uniform(0.5, 1.5, size=ne)
+    run_case_two_site(ptn, "ternary2_xxz_neel_2tdvp", spec, neel_state_tensors(spec),
+                      lambda psi: heisenberg_fields(ptn, spec, np.zeros(len(spec)), jxy, jz),
+                      0.02, 6, 1e-12, (8, 1e-10, 1e-10, False))
+    spec = binary_tree(7)
+    h = rng.uniform(-1, 1, size=len(spec))
+    run_case_two_site(ptn, "binary7_heis_2tdvp_trunc", spec, random_state_tensors(spec, rng, 4),
+                      lambda psi: heisenberg_fields(ptn, spec, h), 0.05, 3, 1e-12,
+                      (3, 1e-10, 1e-10, True), canonical_random=True)
     unit_cases(ptn)
 
 

@@ -22,12 +22,17 @@ def load_case(name):
         "order": int(d["order"]),
         "krylov_tol": float(d["krylov_tol"]),
         "update_path": [str(x) for x in d["update_path"]],
+        "two_site": bool(int(d["two_site"])) if "two_site" in d.files else False,
     }
+    if case["two_site"]:
+        case["svd"] = dict(max_bond_dim=int(d["svd_max_bond_dim"]), rel_tol=float(d["svd_rel_tol"]),
+                           total_tol=float(d["svd_total_tol"]), renorm=bool(int(d["svd_renorm"])))
     return case
 
 
 CASES = ["c1_binary15_tfim_chi8", "binary7_tfim_chi4_o2", "ttree3_heis_chi6_o1",
          "ttree3_heis_chi6_o2", "ternary2_xxz_chi4_o1"]
+TWO_SITE_CASES = ["ternary2_xxz_neel_2tdvp", "binary7_heis_2tdvp_trunc"]
 
 
 def build_ttn(cls, spec, tensors):

@@ -63,3 +63,65 @@ def test_update_path_and_orth_paths():
         c = load_case(name)
         st = oracle_state(c)
         assert O.leaf_to_root_path(st.tree) == c["update_path"]
+
+
+# ---------------------------------------------------------------------------
+# two-site TDVP and truncation
+# ---------------------------------------------------------------------------
+from golden_util import TWO_SITE_CASES  # noqa: E402
+
+
+def test_oracle_truncation_known_answers():
+    d = np.load(f"{GOLDEN}/units.npz")
+    n = int(d["svd/n"])
+    assert n > 20
+    for i in range(n):
+        maxd, rel, tot, renorm, sumt = d[f"svd/{i}/params"]
+        p = O.SVDParams(max_bond_dim=int(maxd), rel_tol=rel, total_tol=tot, renorm=bool(renorm),
+                        sum_trunc=bool(sumt))
+        keep, new_s = O.truncate_singular_values(d[f"svd/{i}/s"], p)
+        ref = d[f"svd/{i}/out"]
+        assert keep == len(ref), i
+        np.testing.assert_allclose(new_s, ref, rtol=1e-15, atol=0)
+
+
+@pytest.mark.parametrize("name", TWO_SITE_CASES)
+def test_oracle_two_site_cases(name):
+    c = load_case(name)
+    st = oracle_state(c)
+    algo = O.SecondOrderTwoSiteTDVPOracle(st, c["ttno"], c["dt"], O.SVDParams(**c["svd"]),
+                                          krylov_tol=c["krylov_tol"])
+    assert algo.update_path == c["update_path"]
+    zerr = 0.0
+    for k in range(c["steps"]):
+        algo.run_one_time_step()
+        z = np.array([O.expect_product(algo.state, {nid: Zm}) for nid, _ in c["spec"]])
+        zerr = max(zerr, float(np.max(np.abs(z - c["z"][k]))))
+    fin = oracle_state(c, "final")
+    for nid in fin.tensors:
+        assert fin.tensors[nid].shape == algo.state.tensors[nid].shape, nid
+    one_minus_f, dist = fidelity_and_dist(fin, algo.state)
+    assert zerr < 1e-10
+    assert one_minus_f < 1e-12
+    assert dist < 1e-8
+
+
+def test_oracle_first_order_two_site_runs():
+    """First-order two-site TDVP (the reference's driver raises on branching
+    trees; the oracle runs the intended schedule): norm kept, energy drift small."""
+    c = load_case("ternary2_xxz_neel_2tdvp")
+    st = oracle_state(c)
+    algo = O.FirstOrderTwoSiteTDVPOracle(st, c["ttno"], 0.01, O.SVDParams(**c["svd"]),
+                                         krylov_tol=1e-12)
+    for _ in range(3):
+        algo.run_one_time_step()
+    nrm = O.scalar_product(algo.state, algo.state).real
+    assert abs(nrm - 1) < 1e-9
+    # second order and first order agree to O(dt) on <Z>
+    algo2 = O.SecondOrderTwoSiteTDVPOracle(oracle_state(c), c["ttno"], 0.01, O.SVDParams(**c["svd"]),
+                                           krylov_tol=1e-12)
+    for _ in range(3):
+        algo2.run_one_time_step()
+    z1 = np.array([O.expect_product(algo.state, {nid: Zm}) for nid, _ in c["spec"]])
+    z2 = np.array([O.expect_product(algo2.state, {nid: Zm}) for nid, _ in c["spec"]])
+    assert np.max(np.abs(z1 - z2)) < 5e-3

@@ -173,6 +173,54 @@ int ptn_zqr_keep_noalloc(void* A, const int64_t* rowoff, int64_t m, int64_t k, i
 
 /* Number of kernel launches this library has issued since it was loaded
  * (host-side counter; used to report launches inside a timed region). */
+/* ---- Singular value decomposition (FP64, one-sided Jacobi) ------------------
+ * Replaces np.linalg.svd inside tensor_svd / truncated_tensor_svd
+ * (util/tensor_splitting.py:122-177, 488-527), as called by split_node_svd
+ * (core/ttn.py:1476-1497) in the two-site TDVP and TEBD splits. The truncation
+ * rule itself (truncate_singular_values, :448-486) needs only S and is applied
+ * by the caller. A (m x n, m >= n): element (i, j) at A[i * row_stride +
+ * j * col_stride], read only. Outputs: U (m x n, column j at U + j * ldu), S
+ * (device double[n], descending), V (n x n, column j at V + j * ldv) with
+ * A = U diag(S) V^H; columns of U for zero singular values are zero.
+ * work: ptn_zsvd_work_bytes(m, n) bytes of device scratch. status (device
+ * int32, caller zeroes it): set to PTN_ERR_NOCONVERGE when the sweep limit is
+ * reached, PTN_ERR_TIMEOUT when a bounded grid-barrier wait runs out. */
+typedef struct {
+  const void* A;
+  int64_t m, n;
+  int64_t row_stride, col_stride;
+  void* U;
+  int64_t ldu;
+  double* S;
+  void* V;
+  int64_t ldv;
+  void* work;
+  int32_t* status;
+} ptn_svd_desc;
+
+int64_t ptn_zsvd_work_bytes(int64_t m, int64_t n);
+int ptn_zsvd_jacobi(const ptn_svd_desc* d, void* stream);
+
+/* dst[idx] = op(src[idx]) * (scale ? scale[idx_{scale_mode}] : 1) over an
+ * n-mode index (mode n-1 fastest), op = conj when conj != 0. The strides
+ * address both operands in place: this writes SVD factors straight into a
+ * node's leg order (the transposes and np.diag(s) products of
+ * contr_truncated_svd_splitting, util/tensor_splitting.py:541-572). */
+typedef struct {
+  const void* src;
+  void* dst;
+  int32_t n;
+  int32_t conj;
+  int64_t dim[PTN_MAX_MODES];
+  int64_t stride_src[PTN_MAX_MODES];
+  int64_t stride_dst[PTN_MAX_MODES];
+  const double* scale;
+  int32_t scale_mode;
+  int32_t pad_;
+} ptn_permute_desc;
+
+int ptn_zpermute(const ptn_permute_desc* d, void* stream);
+
 unsigned long long ptn_launch_counter(void);
 
 /* Scan a complex128 buffer for NaN/Inf; flag (device int32) is set to 1 if found. */

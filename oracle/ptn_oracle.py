@@ -340,9 +340,13 @@ def krylov_exp_action(psi, action, dt, exp_factor, krylov_tol=1e-10,
     max_steps = n if max_krylov_dim is None else min(n, int(max_krylov_dim))
     floor_abs = np.finfo(float).eps * max(n, 1)
     Q = [v0 / beta0]
-    T = np.zeros((max_steps + 1, max_steps + 1), dtype=complex)
+    T = np.zeros((min(max_steps, 32) + 1,) * 2, dtype=complex)
     m = 0
     for j in range(max_steps):
+        if j + 2 > T.shape[0]:
+            T2 = np.zeros((2 * T.shape[0],) * 2, dtype=complex)
+            T2[:T.shape[0], :T.shape[0]] = T
+            T = T2
         w = np.asarray(action(Q[j].reshape(shape)), dtype=complex).reshape(-1)
         w0 = float(np.linalg.norm(w))
         for _ in range(2):

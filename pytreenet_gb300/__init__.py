@@ -2,18 +2,23 @@
 
 Drop-in surface for the path (names as in PyTreeNet):
 TreeTensorNetworkState/TTNS, TreeTensorNetworkOperator/TTNO, Node,
-FirstOrderOneSiteTDVP, SecondOrderOneSiteTDVP, TDVPConfig, TimeEvoMode,
-EvoDirection, TensorProduct. Numerics run in libptn_gb300.so (hand-written
-CUDA for sm_103a) through a C ABI; see include/ptn_gb300.h.
+FirstOrderOneSiteTDVP, SecondOrderOneSiteTDVP, FirstOrderTwoSiteTDVP,
+SecondOrderTwoSiteTDVP, TDVPConfig, TwoSiteTDVPConfig, SVDParameters,
+TimeEvoMode, EvoDirection, TensorProduct. Numerics run in libptn_gb300.so
+(hand-written CUDA for sm_103a) through a C ABI; see include/ptn_gb300.h.
 """
 from .ttn import Node, TreeTensorNetworkState, TreeTensorNetworkOperator, TTNS, TTNO
 from .tdvp import (TimeEvoMode, EvoDirection, PathFinderMode, TDVPConfig, TensorProduct,
-                   FirstOrderOneSiteTDVP, SecondOrderOneSiteTDVP, leaf_to_root_update_path)
+                   FirstOrderOneSiteTDVP, SecondOrderOneSiteTDVP, leaf_to_root_update_path,
+                   TwoSiteTDVPConfig, FirstOrderTwoSiteTDVP, SecondOrderTwoSiteTDVP)
+from .truncation import SVDParameters, truncate_singular_values
 from .operators import nearest_neighbour_ttno, tfim_ttno, heisenberg_ttno
 
 __all__ = [
     "Node", "TreeTensorNetworkState", "TreeTensorNetworkOperator", "TTNS", "TTNO",
     "TimeEvoMode", "EvoDirection", "PathFinderMode", "TDVPConfig", "TensorProduct",
     "FirstOrderOneSiteTDVP", "SecondOrderOneSiteTDVP", "leaf_to_root_update_path",
+    "TwoSiteTDVPConfig", "FirstOrderTwoSiteTDVP", "SecondOrderTwoSiteTDVP",
+    "SVDParameters", "truncate_singular_values",
     "nearest_neighbour_ttno", "tfim_ttno", "heisenberg_ttno",
 ]

@@ -66,6 +66,21 @@ class ConvertDesc(ctypes.Structure):
                 ("rows", Modes), ("cols", Modes)]
 
 
+class SvdDesc(ctypes.Structure):
+    _fields_ = [("A", ctypes.c_void_p), ("m", ctypes.c_int64), ("n", ctypes.c_int64),
+                ("row_stride", ctypes.c_int64), ("col_stride", ctypes.c_int64),
+                ("U", ctypes.c_void_p), ("ldu", ctypes.c_int64), ("S", ctypes.c_void_p),
+                ("V", ctypes.c_void_p), ("ldv", ctypes.c_int64), ("work", ctypes.c_void_p),
+                ("status", ctypes.c_void_p)]
+
+
+class PermuteDesc(ctypes.Structure):
+    _fields_ = [("src", ctypes.c_void_p), ("dst", ctypes.c_void_p), ("n", ctypes.c_int32),
+                ("conj", ctypes.c_int32), ("dim", ctypes.c_int64 * MAX_MODES),
+                ("stride_src", ctypes.c_int64 * MAX_MODES), ("stride_dst", ctypes.c_int64 * MAX_MODES),
+                ("scale", ctypes.c_void_p), ("scale_mode", ctypes.c_int32), ("pad_", ctypes.c_int32)]
+
+
 _P = ctypes.c_void_p
 _I64 = ctypes.c_int64
 _I32 = ctypes.c_int32
@@ -88,6 +103,9 @@ SIGNATURES = {
     "ptn_to_planes": (ctypes.c_int, [ctypes.POINTER(ConvertDesc), _P]),
     "ptn_expand_b": (ctypes.c_int, [ctypes.POINTER(ConvertDesc), _P]),
     "ptn_tc_selftest": (ctypes.c_int, [_P, _P, _P, _P, _I32, _P]),
+    "ptn_zsvd_work_bytes": (_I64, [_I64, _I64]),
+    "ptn_zsvd_jacobi": (ctypes.c_int, [ctypes.POINTER(SvdDesc), _P]),
+    "ptn_zpermute": (ctypes.c_int, [ctypes.POINTER(PermuteDesc), _P]),
 }
 
 _lib = None

@@ -898,6 +898,287 @@ class DeviceNetwork:
             self.move_orth_one_hop(a, b)
         st.orthogonality_center_id = new_center
 
+    # -- two-site update: merge, matvec, truncated SVD split -----------------------
+    def _two_site_info(self, u, v) -> dict:
+        """Leg bookkeeping of the merged pair. The merged tensor holds u's other
+        neighbours (physical order) and u's physical leg ("u side", m entries),
+        and the same for v ("v side", n entries). The larger side is stored
+        first, so the SVD sees a tall column-major matrix T = M (m >= n) or
+        T = M^T (m < n) without a transpose."""
+        su, sv = self.shape(u), self.shape(v)
+        key = ("2info", u, v, tuple(su), tuple(sv))
+        info = self.plans.get(key)
+        if info is not None:
+            return info
+        st = self.state
+        nu = [x for x in self.nbrs(u) if x != v]
+        nv = [x for x in self.nbrs(v) if x != u]
+        du = [su[st.phys_axis(u, x)] for x in nu] + [su[-1]]
+        dv = [sv[st.phys_axis(v, x)] for x in nv] + [sv[-1]]
+        lu = [f"au{k}" for k in range(len(nu))] + ["su"]
+        lv = [f"av{k}" for k in range(len(nv))] + ["sv"]
+        m, n = int(np.prod(du)), int(np.prod(dv))
+        vfirst = m >= n
+        info = dict(nu=nu, nv=nv, du=du, dv=dv, lu=lu, lv=lv, m=m, n=n, vfirst=vfirst,
+                    labels=(lv + lu) if vfirst else (lu + lv), dims=(dv + du) if vfirst else (du + dv))
+        self.plans[key] = info
+        return info
+
+    def merge_plan(self, u, v) -> Plan:
+        """The two site tensors contracted over their bond (``contract_nodes``,
+        ``contractions/node_contraction.py:12-141``), written in the merged layout."""
+        info = self._two_site_info(u, v)
+        key = ("merge", u, v, tuple(info["dims"]))
+        if key in self.plans:
+            return self.plans[key]
+        cb = ChainBuilder(self.ws)
+        A = Operand.contiguous(("fixed", self.t[u]),
+                               ["bond" if x == v else info["lu"][info["nu"].index(x)] for x in self.nbrs(u)]
+                               + ["su"], self.shape(u))
+        B = Operand.contiguous(("fixed", self.t[v]),
+                               ["bond" if x == u else info["lv"][info["nv"].index(x)] for x in self.nbrs(v)]
+                               + ["sv"], self.shape(v))
+        cb.contract(A, B, ["bond"], out=Operand.contiguous(("out",), info["labels"], info["dims"]))
+        p = cb.mixed_plan(self.levels) if self.levels else cb.plan()
+        self.plans[key] = p
+        return p
+
+    def heff2_plan(self, u, v) -> Plan:
+        """H_eff of the merged pair (``effective_two_site_evolution``,
+        ``time_evo_util/effective_time_evolution.py:326-410``). The reference joins
+        the two TTNO tensors and contracts every environment before them; here
+        each side runs the single-site order (half of its environments, its W,
+        the rest), so no intermediate carries more than two TTNO bond legs."""
+        info = self._two_site_info(u, v)
+        key = ("heff2", u, v, tuple(info["dims"]))
+        if key in self.plans:
+            return self.plans[key]
+        cb = ChainBuilder(self.ws)
+        out_labels = [l.replace("au", "cu").replace("av", "cv").replace("su", "tu").replace("sv", "tv")
+                      for l in info["labels"]]
+        x = Operand.contiguous(("in",), info["labels"], info["dims"])
+        y = Operand.contiguous(("out",), out_labels, info["dims"])
+        ops = []
+        for side, node, other, nbl in (("u", u, v, info["nu"]), ("v", v, u, info["nv"])):
+            half = len(nbl) // 2
+            envs = [self._env_op(nb, node, [f"a{side}{k}", f"b{side}{k}", f"c{side}{k}"])
+                    for k, nb in enumerate(nbl)]
+            for k in range(half):
+                ops.append((envs[k], [f"a{side}{k}"]))
+            wl = ["bw" if x_ == other else f"b{side}{nbl.index(x_)}" for x_ in self.nbrs(node)]
+            W = Operand.contiguous(("fixed", self.W[node]), wl + [f"t{side}", f"s{side}"],
+                                   list(self.W[node].shape))
+            kl = [f"b{side}{k}" for k in range(half)] + [f"s{side}"] + (["bw"] if side == "v" else [])
+            ops.append((W, kl))
+            for k in range(half, len(nbl)):
+                ops.append((envs[k], [f"a{side}{k}", f"b{side}{k}"]))
+        T = x
+        for i, (op, kl) in enumerate(ops):
+            if i == len(ops) - 1:
+                cb.contract(T, op, kl, out=y)
+            else:
+                T = cb.contract(T, op, kl)
+        p = cb.mixed_plan(self.levels) if self.levels else cb.plan()
+        self.plans[key] = p
+        return p
+
+    def _permute(self, src_ptr, dst_ptr, dims, s_src, s_dst, conj=False, scale_ptr=0, scale_mode=0):
+        d = _lib.PermuteDesc()
+        if len(dims) > MAX_MODES:
+            raise ValueError(f"permute needs {len(dims)} modes (max {MAX_MODES})")
+        d.src, d.dst, d.n, d.conj = src_ptr, dst_ptr, len(dims), int(conj)
+        for i, (n_, a, b) in enumerate(zip(dims, s_src, s_dst)):
+            d.dim[i], d.stride_src[i], d.stride_dst[i] = n_, a, b
+        d.scale = scale_ptr or None
+        d.scale_mode = scale_mode
+        check(_lib.load().ptn_zpermute(ctypes.byref(d), _stream_ptr()), "ptn_zpermute")
+
+    @staticmethod
+    def _cstrides(dims):
+        out, s = [], 1
+        for d in reversed(dims):
+            out.append(s)
+            s *= d
+        return list(reversed(out))
+
+    def _ensure_qr_buffers(self, m, k):
+        """Grow the QR R/work buffers (bond dimensions change in two-site
+        updates); captured QR graphs point at the old buffers and are dropped."""
+        lib = _lib.load()
+        need_w = (int(lib.ptn_zqr_work_bytes(m, k)) + 15) // 16
+        if k * k > self.qr_R.numel() or need_w > self.qr_work.numel():
+            self.qr_R = torch.zeros((max(k * k, self.qr_R.numel()),), dtype=CDT, device=self.device)
+            self.qr_work = torch.zeros((max(need_w, self.qr_work.numel()),), dtype=CDT, device=self.device)
+            self.qr_graphs.clear()
+            self.qr_seen.clear()
+
+    def _forget_node(self, nid):
+        """Drop every cached plan, QR graph and environment that depends on the
+        shape or storage of ``nid``'s tensor."""
+        for key in [k for k in self.plans if any(x == nid for x in k[1:3])]:
+            del self.plans[key]
+        for key in [k for k in self.qr_graphs if k[0] == nid]:
+            del self.qr_graphs[key]
+        self.qr_seen = {k for k in self.qr_seen if k[0] != nid}
+        self.cholqr_fails = {k for k in self.cholqr_fails if k[0] != nid}
+
+    def _set_node_tensor(self, nid, t: torch.Tensor):
+        self.t[nid] = t
+        self.state._phys[nid] = t
+        self.state.nodes[nid].shape = tuple(t.shape)
+
+    def svd_split(self, u, v, x2: torch.Tensor, svd) -> np.ndarray:
+        """Truncated SVD of the merged pair with the singular values moved into
+        v (``split_node_svd`` -> ``contr_truncated_svd_splitting`` (VCONTR),
+        ``core/ttn.py:1476-1497``, ``util/tensor_splitting.py:488-572``).
+        T (p x q, column-major in ``x2``) is reduced by Householder QR when
+        p > q, the q x q factor goes through the Jacobi SVD, the kept rank comes
+        from ``truncate_singular_values`` (``:448-486``) on the host, and the
+        factors are written straight into u's and v's leg layouts. Returns the
+        kept singular values."""
+        from .truncation import truncate_singular_values
+        info = self._two_site_info(u, v)
+        lib = _lib.load()
+        st = self.state
+        m, n, vfirst = info["m"], info["n"], info["vfirst"]
+        p, q = (m, n) if vfirst else (n, m)
+        use_qr = p > q
+        if use_qr:
+            key = ("rowoff_lin", p)
+            if key not in self.rowoff:
+                self.rowoff[key] = torch.arange(p, dtype=torch.int64, device=self.device)
+            R = self.ws.get("svd_R", q * q)
+            qw = self.ws.get("svd_qrwork", (int(lib.ptn_zqr_work_bytes(p, q)) + 15) // 16)
+            check(lib.ptn_zqr_keep(x2.data_ptr(), self.rowoff[key].data_ptr(), p, q, p, R.data_ptr(),
+                                   qw.data_ptr(), _stream_ptr()), "ptn_zqr_keep")
+            self.flops += 8 * 2 * p * q * q
+            jm, src, rs, cs = q, R, q, 1
+        else:
+            jm, src, rs, cs = p, x2, 1, p
+        Uj = self.ws.get("svd_U", jm * q)
+        Vj = self.ws.get("svd_V", q * q)
+        Sb = self.ws.get("svd_S", q + 2, torch.float64)
+        Sb.zero_()
+        sw = self.ws.get("svd_work", (int(lib.ptn_zsvd_work_bytes(jm, q)) + 15) // 16)
+        d = _lib.SvdDesc()
+        d.A, d.m, d.n, d.row_stride, d.col_stride = src.data_ptr(), jm, q, rs, cs
+        d.U, d.ldu, d.S, d.V, d.ldv = Uj.data_ptr(), jm, Sb.data_ptr(), Vj.data_ptr(), q
+        d.work = sw.data_ptr()
+        d.status = Sb[q:].data_ptr()
+        check(lib.ptn_zsvd_jacobi(ctypes.byref(d), _stream_ptr()), "ptn_zsvd_jacobi")
+        host = Sb.cpu()
+        code = int(host[q:q + 1].view(torch.int32)[0])
+        if code != 0:
+            raise _lib.PtnError(code, "Jacobi SVD")
+        s = host[:q].numpy()
+        if not np.all(np.isfinite(s)):
+            raise _lib.PtnError(3, "Jacobi SVD: non-finite singular values")
+        new_s, _ = truncate_singular_values(s, svd)
+        r = len(new_s)
+        scale = self.ws.get("svd_scale", r, torch.float64)
+        scale.copy_(torch.from_numpy(np.ascontiguousarray(new_s, dtype=np.float64)))
+        # destination tensors (new storage when the bond dimension changes)
+        old_r = self.shape(u)[st.phys_axis(u, v)]
+        shp_u = self.shape(u)
+        shp_u[st.phys_axis(u, v)] = r
+        shp_v = self.shape(v)
+        shp_v[st.phys_axis(v, u)] = r
+        if r == old_r:
+            tu, tv = self.t[u], self.t[v]
+        else:
+            tu = torch.empty(shp_u, dtype=CDT, device=self.device)
+            tv = torch.empty(shp_v, dtype=CDT, device=self.device)
+        su_str, sv_str = self._cstrides(shp_u), self._cstrides(shp_v)
+        ax_u = [st.phys_axis(u, x) for x in info["nu"]] + [len(shp_u) - 1]   # u-side legs in u
+        ax_v = [st.phys_axis(v, x) for x in info["nv"]] + [len(shp_v) - 1]
+        bu, bv = st.phys_axis(u, v), st.phys_axis(v, u)
+        du, dv = info["du"], info["dv"]
+        cu, cv = self._cstrides(du), self._cstrides(dv)
+        if vfirst:
+            # M = (Q Uj) S Vj^H: u <- Q Uj[:, :r], v <- S Vj^H
+            if use_qr:
+                cb = ChainBuilder(self.ws)
+                Q = Operand.contiguous(("fixed", x2), ["k"] + info["lu"], [q] + du)
+                Uo = Operand(("fixed", Uj), ["k", "c"], [q, r], [1, q])
+                lab = [None] * len(shp_u)
+                for l_, a in zip(info["lu"], ax_u):
+                    lab[a] = l_
+                lab[bu] = "c"
+                cb.contract(Q, Uo, ["k"], out=Operand(("fixed", tu), lab, shp_u, su_str))
+                pl = cb.plan()
+                pl.run()
+                self.flops += pl.flops
+            else:
+                self._permute(Uj.data_ptr(), tu.data_ptr(), du + [r], cu + [jm],
+                              [su_str[a] for a in ax_u] + [su_str[bu]])
+            self._permute(Vj.data_ptr(), tv.data_ptr(), dv + [r], cv + [q],
+                          [sv_str[a] for a in ax_v] + [sv_str[bv]], conj=True,
+                          scale_ptr=scale.data_ptr(), scale_mode=len(dv))
+        else:
+            # M^T = (Q Uj) S Vj^H, so M = conj(Vj) S (Q Uj)^T: u <- conj(Vj[:, :r]), v <- S (Q Uj)^T
+            self._permute(Vj.data_ptr(), tu.data_ptr(), du + [r], cu + [q],
+                          [su_str[a] for a in ax_u] + [su_str[bu]], conj=True)
+            if use_qr:
+                Us = self.ws.get("svd_Us", q * r)
+                self._permute(Uj.data_ptr(), Us.data_ptr(), [r, q], [jm, 1], [q, 1],
+                              scale_ptr=scale.data_ptr(), scale_mode=0)
+                cb = ChainBuilder(self.ws)
+                Q = Operand.contiguous(("fixed", x2), ["k"] + info["lv"], [q] + dv)
+                Uo = Operand(("fixed", Us), ["k", "c"], [q, r], [1, q])
+                lab = [None] * len(shp_v)
+                for l_, a in zip(info["lv"], ax_v):
+                    lab[a] = l_
+                lab[bv] = "c"
+                cb.contract(Q, Uo, ["k"], out=Operand(("fixed", tv), lab, shp_v, sv_str))
+                pl = cb.plan()
+                pl.run()
+                self.flops += pl.flops
+            else:
+                self._permute(Uj.data_ptr(), tv.data_ptr(), dv + [r], cv + [jm],
+                              [sv_str[a] for a in ax_v] + [sv_str[bv]],
+                              scale_ptr=scale.data_ptr(), scale_mode=len(dv))
+        if r != old_r:
+            self._forget_node(u)
+            self._forget_node(v)
+            self.env.pop((u, v), None)
+            self.env.pop((v, u), None)
+            self._set_node_tensor(u, tu)
+            self._set_node_tensor(v, tv)
+        # logical order: the node that gains the new child lists it first (core/ttn.py:1400-1448)
+        if st.nodes[v].parent == u:
+            nu_ = st.nodes[u]
+            nu_.children = [v] + [c for c in nu_.children if c != v]
+        else:
+            nv_ = st.nodes[v]
+            nv_.children = [u] + [c for c in nv_.children if c != u]
+        return new_s
+
+    def evolve_two_site(self, u, v, dt, exp_factor, tol, maxdim, svd) -> np.ndarray:
+        """Two-site update of (u, v) with u the orthogonality centre: merge,
+        Krylov exponential of the pair's H_eff, truncated SVD split, centre to
+        v, environment E(u -> v) (``TwoSiteTDVP._update_two_site_nodes``,
+        ``tdvp_algorithms/twositetdvp.py:89-125``). Returns the kept singular values."""
+        info = self._two_site_info(u, v)
+        x2 = self.ws.get("two_site", info["m"] * info["n"])
+        mp = self.merge_plan(u, v)
+        mp.run(0, x2.data_ptr())
+        self.flops += mp.flops
+        hp = self.heff2_plan(u, v)
+
+        def apply(xp, yp):
+            hp.run(xp, yp)
+            self.flops += hp.flops
+        self.krylov.expm(x2, apply, dt, exp_factor, tol, maxdim, out=x2, tridiagonal=self.levels > 0)
+        self.check_device_status()
+        s = self.svd_split(u, v, x2, svd)
+        self.state.orthogonality_center_id = v
+        for a, b in ((u, v), (v, u)):
+            k = self.shape(a)[self.state.phys_axis(a, b)]
+            rows = self.t[a].numel() // max(k, 1)
+            self._ensure_qr_buffers(rows, k)
+        self.update_env(u, v)
+        return s
+
     def normalise_center(self) -> float:
         """Divide the orthogonality centre by its norm (``TTNS.normalise``,
         ``ttns/ttns.py:105-125``); returns the old norm."""

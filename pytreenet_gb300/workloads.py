@@ -93,3 +93,64 @@ def binary_tfim_product_state(n: int = 15, chi: int = 8, seed: int = 0, J: float
     st = _build(spec, tensors)
     H = tfim_ttno(st, J=J, g=g)
     return st, H, spec, tensors
+
+
+def ternary_spec(depth: int):
+    """Complete ternary tree: t0 at the root, three children per internal node
+    (1 + 3 + 9 + 27 = 40 sites for depth 3)."""
+    spec = [("t0", None)]
+    frontier, idx = ["t0"], 1
+    for _ in range(depth):
+        nxt = []
+        for p in frontier:
+            for _ in range(3):
+                nid = f"t{idx}"
+                idx += 1
+                spec.append((nid, p))
+                nxt.append(nid)
+        frontier = nxt
+    return spec
+
+
+def ternary_state(depth: int = 2, chi: int = 4, seed: int = 0):
+    """Random ternary-tree TTNS (unit-norm Gaussian tensors, every bond ``chi``).
+    Returns (TTNS, spec, tensors in physical layout)."""
+    rng = np.random.default_rng(seed)
+    spec = ternary_spec(depth)
+    nkids = {nid: 0 for nid, _ in spec}
+    for nid, p in spec:
+        if p is not None:
+            nkids[p] += 1
+    tensors = {}
+    for nid, p in spec:
+        shape = [chi] * (nkids[nid] + (0 if p is None else 1)) + [2]
+        t = rng.normal(size=shape) + 1j * rng.normal(size=shape)
+        tensors[nid] = t / np.linalg.norm(t)
+    return _build(spec, tensors), spec, tensors
+
+
+def ternary_neel_state(depth: int = 3):
+    """Neel product state by depth parity (up on even depths), every bond of
+    dimension 1. Returns (TTNS, spec, tensors)."""
+    spec = ternary_spec(depth)
+    nkids = {nid: 0 for nid, _ in spec}
+    depth_of = {}
+    for nid, p in spec:
+        depth_of[nid] = 0 if p is None else depth_of[p] + 1
+        if p is not None:
+            nkids[p] += 1
+    tensors = {}
+    for nid, p in spec:
+        v = np.array([1, 0], dtype=complex) if depth_of[nid] % 2 == 0 else np.array([0, 1], dtype=complex)
+        tensors[nid] = v.reshape([1] * (nkids[nid] + (0 if p is None else 1)) + [2])
+    return _build(spec, tensors), spec, tensors
+
+
+def ternary_xxz(state: TreeTensorNetworkState, seed: int = 7):
+    """XXZ with per-edge couplings Jxy, Jz ~ U[0.5, 1.5]; returns (TTNO, W in physical layout)."""
+    rng = np.random.default_rng(seed)
+    edges = [(state.nodes[nid].parent, nid) for nid in state._order if state.nodes[nid].parent is not None]
+    jxy = {e: rng.uniform(0.5, 1.5) for e in edges}
+    jz = {e: rng.uniform(0.5, 1.5) for e in edges}
+    H = heisenberg_ttno(state, None, jxy, jz)
+    return H, {nid: H.phys(nid) for nid in state._order}

@@ -235,3 +235,42 @@ FakeLib.ptn_to_planes = _fake_to_planes
 FakeLib.ptn_expand_b = _fake_expand_b
 FakeLib.ptn_cgemm_bf16x3 = _fake_cgemm
 FakeLib.ptn_launch_counter = lambda self: 0
+
+
+# ---- SVD and permute ------------------------------------------------------------
+def _fake_svd_work_bytes(self, m, n):
+    return 256
+
+
+def _fake_svd(self, d_ref, stream):
+    d = d_ref._obj
+    m, n = d.m, d.n
+    A = _strided(d.A, [m, n], [d.row_stride, d.col_stride]).copy()
+    u, s, vh = np.linalg.svd(A, full_matrices=False)
+    U = _strided(d.U, [n, m], [d.ldu, 1])
+    U[...] = u.T
+    _view(d.S, n, np.float64)[:] = s
+    V = _strided(d.V, [n, n], [d.ldv, 1])
+    V[...] = vh.conj()
+    return 0
+
+
+def _fake_permute(self, d_ref, stream):
+    d = d_ref._obj
+    dims = [d.dim[i] for i in range(d.n)]
+    src = _strided(d.src, dims, [d.stride_src[i] for i in range(d.n)]).copy()
+    if d.conj:
+        src = src.conj()
+    if d.scale:
+        sc = _view(d.scale, dims[d.scale_mode], np.float64)
+        shp = [1] * d.n
+        shp[d.scale_mode] = dims[d.scale_mode]
+        src = src * sc.reshape(shp)
+    dst = _strided(d.dst, dims, [d.stride_dst[i] for i in range(d.n)])
+    dst[...] = src
+    return 0
+
+
+FakeLib.ptn_zsvd_work_bytes = _fake_svd_work_bytes
+FakeLib.ptn_zsvd_jacobi = _fake_svd
+FakeLib.ptn_zpermute = _fake_permute

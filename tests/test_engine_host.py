@@ -96,3 +96,79 @@ def test_engine_host_cholqr2_split(monkeypatch):
     assert np.max(np.abs(Qm @ R.numpy() - Am)) < 1e-6 * np.max(np.abs(Am))
     assert np.allclose(np.tril(R.numpy(), -1), 0)
     assert net.state.nodes["root"].children[0] == "a1_0"
+
+
+# ---------------------------------------------------------------------------
+# two-site TDVP (truncated SVD split) on the fake library
+# ---------------------------------------------------------------------------
+from golden_util import TWO_SITE_CASES  # noqa: E402
+
+
+def _run_two_site(name, precision="plain", order=2, dt=None, steps=None):
+    import pytreenet_gb300 as P
+    c = load_case(name)
+    st = build_ttn(P.TTNS, c["spec"], c["init"])
+    H = build_ttn(P.TTNO, c["spec"], c["ttno"])
+    cfg = P.TwoSiteTDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV, **c["svd"])
+    cls = P.SecondOrderTwoSiteTDVP if order == 2 else P.FirstOrderTwoSiteTDVP
+    dt = c["dt"] if dt is None else dt
+    algo = cls(st, H, dt, dt * c["steps"], {}, config=cfg,
+               solver_options={"krylov_tol": c["krylov_tol"]}, precision=precision)
+    assert algo.update_path == c["update_path"]
+    zs = []
+    for k in range(c["steps"] if steps is None else steps):
+        algo.run_one_time_step()
+        zs.append([algo.evaluate_operator({nid: Zm}) for nid, _ in c["spec"]])
+    out = {nid: algo.state.get_phys_numpy(nid) for nid, _ in c["spec"]}
+    return c, algo, out, np.array(zs)
+
+
+@pytest.mark.parametrize("name", TWO_SITE_CASES)
+def test_engine_host_two_site_matches_reference(monkeypatch, name):
+    fake_ptn.install(monkeypatch)
+    import oracle as O
+    c, algo, out, zs = _run_two_site(name)
+    got = O.OState(oracle_state(c).tree, out)
+    fin = oracle_state(c, "final")
+    for nid in fin.tensors:
+        assert fin.tensors[nid].shape == out[nid].shape, nid
+    one_minus_f, dist = fidelity_and_dist(fin, got)
+    assert np.max(np.abs(zs - c["z"])) < 1e-10
+    assert one_minus_f < 1e-12
+    # the logical children order follows the reference's split rules
+    for nid, _ in c["spec"]:
+        assert algo.state.nodes[nid].children == algo.net.state.nodes[nid].children
+
+
+def test_engine_host_first_order_two_site_matches_oracle(monkeypatch):
+    fake_ptn.install(monkeypatch)
+    import oracle as O
+    c, algo, out, zs = _run_two_site("ternary2_xxz_neel_2tdvp", order=1, dt=0.01, steps=3)
+    ora = O.FirstOrderTwoSiteTDVPOracle(oracle_state(c), c["ttno"], 0.01, O.SVDParams(**c["svd"]),
+                                        krylov_tol=c["krylov_tol"])
+    for _ in range(3):
+        ora.run_one_time_step()
+    got = O.OState(oracle_state(c).tree, out)
+    one_minus_f, dist = fidelity_and_dist(ora.state, got)
+    assert one_minus_f < 1e-12
+    assert algo.bond_dims_history == ora.bond_history
+
+
+def test_svd_parameters_validation():
+    import pytreenet_gb300 as P
+    with pytest.raises(TypeError):
+        P.SVDParameters(max_bond_dim=2.5)
+    with pytest.raises(ValueError):
+        P.SVDParameters(rel_tol=-1.0)
+    with pytest.raises(ValueError):
+        P.SVDParameters(max_bond_dim=0)
+    d = np.load(f"{__import__('golden_util').GOLDEN}/units.npz")
+    for i in range(int(d["svd/n"])):
+        maxd, rel, tot, renorm, sumt = d[f"svd/{i}/params"]
+        p = P.SVDParameters(max_bond_dim=int(maxd), rel_tol=rel, total_tol=tot, renorm=bool(renorm),
+                            sum_trunc=bool(sumt))
+        import warnings
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            new_s, _ = P.truncate_singular_values(d[f"svd/{i}/s"], p)
+        np.testing.assert_allclose(new_s, d[f"svd/{i}/out"], rtol=1e-15, atol=0)

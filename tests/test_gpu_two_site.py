@@ -1,0 +1,150 @@
+"""GPU: Jacobi SVD, strided permute, and two-site TDVP against the reference's fixtures."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle as O
+from golden_util import TWO_SITE_CASES, build_ttn, load_case, oracle_state, fidelity_and_dist
+
+pytestmark = pytest.mark.gpu
+Zm = np.diag([1.0, -1.0]).astype(complex)
+
+
+def _svd_gpu(A_np, transpose_input=False):
+    import torch
+    from pytreenet_gb300 import _lib
+    lib = _lib.load()
+    m, n = A_np.shape
+    if transpose_input:
+        src = torch.from_numpy(np.ascontiguousarray(A_np)).cuda()          # row-major: (i, j) at i*n + j
+        rs, cs = n, 1
+    else:
+        src = torch.from_numpy(np.ascontiguousarray(A_np.T)).cuda()        # column-major
+        rs, cs = 1, m
+    U = torch.zeros(n * m, dtype=torch.complex128, device="cuda")
+    V = torch.zeros(n * n, dtype=torch.complex128, device="cuda")
+    S = torch.zeros(n + 2, dtype=torch.float64, device="cuda")
+    work = torch.zeros((lib.ptn_zsvd_work_bytes(m, n) + 15) // 16, dtype=torch.complex128, device="cuda")
+    d = _lib.SvdDesc()
+    d.A, d.m, d.n, d.row_stride, d.col_stride = src.data_ptr(), m, n, rs, cs
+    d.U, d.ldu, d.S, d.V, d.ldv = U.data_ptr(), m, S.data_ptr(), V.data_ptr(), n
+    d.work, d.status = work.data_ptr(), S[n:].data_ptr()
+    st = lib.ptn_zsvd_jacobi(ctypes.byref(d), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert st == 0
+    torch.cuda.synchronize()
+    h = S.cpu()
+    code = int(h[n:n + 1].view(torch.int32)[0])
+    Uh = U.cpu().numpy().reshape(n, m).T
+    Vh = V.cpu().numpy().reshape(n, n).T
+    return Uh, h[:n].numpy(), Vh, code
+
+
+def _graded(rng, m, n, rank=None, spread=1e-12):
+    k = min(m, n)
+    r = k if rank is None else rank
+    Qa, _ = np.linalg.qr(rng.normal(size=(m, k)) + 1j * rng.normal(size=(m, k)))
+    Qb, _ = np.linalg.qr(rng.normal(size=(n, k)) + 1j * rng.normal(size=(n, k)))
+    s = np.zeros(k)
+    s[:r] = np.geomspace(1.0, spread, r)
+    return (Qa * s) @ Qb.conj().T, s
+
+
+@pytest.mark.parametrize("m,n,rank,spread,transpose", [
+    (1, 1, None, 1.0, False), (7, 5, None, 1e-3, False), (64, 64, None, 1e-12, False),
+    (200, 37, None, 1e-10, True), (96, 96, 10, 1e-6, False), (513, 129, None, 1e-13, False),
+    (300, 256, None, 1e-9, True)])
+def test_jacobi_svd_matches_lapack(m, n, rank, spread, transpose):
+    rng = np.random.default_rng(m * 1000 + n)
+    A, s_true = _graded(rng, m, n, rank, spread)
+    U, s, V, code = _svd_gpu(A, transpose)
+    assert code == 0
+    s_ref = np.linalg.svd(A, compute_uv=False)
+    assert np.all(np.diff(s) <= 0)
+    np.testing.assert_allclose(s, s_ref, rtol=0, atol=1e-14 * max(1.0, s_ref[0]) * np.sqrt(m))
+    # high relative accuracy on the graded spectrum (one-sided Jacobi)
+    nz = s_true > 0
+    assert np.max(np.abs(s[:nz.sum()] - s_true[nz]) / s_true[nz]) < 1e-9
+    rec = (U * s) @ V.conj().T
+    assert np.linalg.norm(rec - A) <= 1e-13 * np.linalg.norm(A) * np.sqrt(m)
+    k = int(np.sum(s > 1e-12 * s[0]))
+    assert np.linalg.norm(U[:, :k].conj().T @ U[:, :k] - np.eye(k)) < 1e-12 * np.sqrt(m)
+    assert np.linalg.norm(V.conj().T @ V - np.eye(n)) < 1e-12 * np.sqrt(n)
+
+
+def test_permute_kernel():
+    import torch
+    from pytreenet_gb300.engine import DeviceNetwork
+    rng = np.random.default_rng(3)
+    a = rng.normal(size=(3, 4, 5, 6)) + 1j * rng.normal(size=(3, 4, 5, 6))
+    scale = rng.normal(size=5)
+    src = torch.from_numpy(a).cuda()
+    dst = torch.zeros((6, 5, 3, 4), dtype=torch.complex128, device="cuda")
+    sc = torch.from_numpy(scale).cuda()
+    dims = [3, 4, 5, 6]
+    s_src = list(np.array(a.strides) // 16)
+    s_dst = [4, 1, 12, 60]
+    DeviceNetwork._permute(None, src.data_ptr(), dst.data_ptr(), dims, s_src, s_dst, conj=True,
+                           scale_ptr=sc.data_ptr(), scale_mode=2)
+    torch.cuda.synchronize()
+    ref = np.transpose(a.conj() * scale[None, None, :, None], (3, 2, 0, 1))
+    np.testing.assert_array_equal(dst.cpu().numpy(), ref)
+
+
+def _run_two_site(name, precision="plain"):
+    import pytreenet_gb300 as P
+    c = load_case(name)
+    st = build_ttn(P.TTNS, c["spec"], c["init"])
+    H = build_ttn(P.TTNO, c["spec"], c["ttno"])
+    cfg = P.TwoSiteTDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV, **c["svd"])
+    algo = P.SecondOrderTwoSiteTDVP(st, H, c["dt"], c["dt"] * c["steps"], {}, config=cfg,
+                                    solver_options={"krylov_tol": c["krylov_tol"]}, precision=precision)
+    zs = []
+    for k in range(c["steps"]):
+        algo.run_one_time_step()
+        zs.append([algo.evaluate_operator({nid: Zm}) for nid, _ in c["spec"]])
+    out = {nid: algo.state.get_phys_numpy(nid) for nid, _ in c["spec"]}
+    return c, O.OState(oracle_state(c).tree, out), np.array(zs)
+
+
+@pytest.mark.parametrize("name", TWO_SITE_CASES)
+def test_gpu_two_site_tdvp_matches_reference(name):
+    c, got, zs = _run_two_site(name)
+    fin = oracle_state(c, "final")
+    for nid in fin.tensors:
+        assert fin.tensors[nid].shape == got.tensors[nid].shape, nid
+    one_minus_f, dist = fidelity_and_dist(fin, got)
+    assert np.max(np.abs(zs - c["z"])) < 1e-10
+    assert one_minus_f < 1e-12
+
+
+def test_gpu_two_site_tdvp_mixed():
+    """Tensor-core (BF16x6) contractions in the two-site path: FP32-level parity."""
+    c, got, zs = _run_two_site("ternary2_xxz_neel_2tdvp", precision="mixed")
+    one_minus_f, dist = fidelity_and_dist(oracle_state(c, "final"), got)
+    assert np.max(np.abs(zs - c["z"])) < 1e-6
+    assert one_minus_f < 1e-9
+
+
+def test_gpu_two_site_ternary_chi16_vs_oracle():
+    """Ternary depth 2 from a random chi=6 state, truncation to 16: bond
+    growth, QR-reduced SVD on both orientations, against the oracle."""
+    import pytreenet_gb300 as P
+    from pytreenet_gb300.workloads import ternary_state, ternary_xxz
+    st, spec, tensors = ternary_state(depth=2, chi=6, seed=11)
+    H, Wphys = ternary_xxz(st, seed=12)
+    svd = dict(max_bond_dim=16, rel_tol=1e-10, total_tol=1e-10)
+    cfg = P.TwoSiteTDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV, **svd)
+    algo = P.SecondOrderTwoSiteTDVP(st, H, 0.02, 0.04, {}, config=cfg, solver_options={"krylov_tol": 1e-12})
+    tree = O.OTree()
+    for nid, p in spec:
+        tree.add_root(nid) if p is None else tree.add_child(nid, p)
+    ora = O.SecondOrderTwoSiteTDVPOracle(O.OState(tree, tensors), Wphys, 0.02, O.SVDParams(**svd),
+                                         krylov_tol=1e-12)
+    for _ in range(2):
+        algo.run_one_time_step()
+        ora.run_one_time_step()
+    assert algo.bond_dims_history == ora.bond_history
+    got = O.OState(tree, {nid: algo.state.get_phys_numpy(nid) for nid, _ in spec})
+    one_minus_f, dist = fidelity_and_dist(ora.state, got)
+    assert one_minus_f < 1e-11

@@ -90,6 +90,12 @@ int ptn_dznrm2(const void* w, int64_t n, void* out_norm, void* partial, void* st
 /* y[x] = w[x] * (1 / scale[0]) with scale a device double. */
 int ptn_zscal_inv(const void* w, const double* scale, void* y, int64_t n, void* stream);
 
+/* y[x] = w[x] * (num[0] / den[0]) with num, den device doubles (den = 0: copy).
+ * Restores the FP64 norm of a tensor after a reduced-precision contraction that
+ * must preserve it (the orthogonality centre after an R absorption). No
+ * counterpart in the reference, whose contractions run in FP64. */
+int ptn_zscal_ratio(const void* w, const double* num, const double* den, void* y, int64_t n, void* stream);
+
 /* out[x] = sum_i c[i] * Q[i, x], c device complex128[nq]. */
 int ptn_zcombine(const void* Q, int64_t ldq, int32_t nq, const void* c,
                  void* out, int64_t n, void* stream);

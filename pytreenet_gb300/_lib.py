@@ -92,6 +92,7 @@ SIGNATURES = {
     "ptn_dznrm2": (ctypes.c_int, [_P, _I64, _P, _P, _P]),
     "ptn_zscal_inv": (ctypes.c_int, [_P, _P, _P, _I64, _P]),
     "ptn_zcombine": (ctypes.c_int, [_P, _I64, _I32, _P, _P, _I64, _P]),
+    "ptn_zscal_ratio": (ctypes.c_int, [_P, _P, _P, _P, _I64, _P]),
     "ptn_zqr_work_bytes": (_I64, [_I64, _I64]),
     "ptn_zqr_keep": (ctypes.c_int, [_P, _P, _I64, _I64, _I64, _P, _P, _P]),
     "ptn_check_finite": (ctypes.c_int, [_P, _I64, _P, _P]),

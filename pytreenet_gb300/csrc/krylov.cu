@@ -108,6 +108,15 @@ __global__ void __launch_bounds__(RT) zscal_inv_kernel(const double2* __restrict
     y[x] = cscale(w[x], inv);
 }
 
+__global__ void __launch_bounds__(RT) zscal_ratio_kernel(const double2* __restrict__ w,
+                                                         const double* __restrict__ num,
+                                                         const double* __restrict__ den,
+                                                         double2* __restrict__ y, int64_t n) {
+  const double f = den[0] > 0.0 ? num[0] / den[0] : 1.0;
+  for (int64_t x = blockIdx.x * (int64_t)RT + threadIdx.x; x < n; x += (int64_t)gridDim.x * RT)
+    y[x] = cscale(w[x], f);
+}
+
 __global__ void __launch_bounds__(RT) zcombine_kernel(const double2* __restrict__ Q, int64_t ldq,
                                                       int nq, const double2* __restrict__ c,
                                                       double2* __restrict__ out, int64_t n) {
@@ -187,6 +196,15 @@ extern "C" int ptn_zscal_inv(const void* w, const double* scale, void* y, int64_
   PTN_COUNT(1);
   zscal_inv_kernel<<<(int)nblocks_for(n), RT, 0, ptn_stream(stream)>>>(
       static_cast<const double2*>(w), scale, static_cast<double2*>(y), n);
+  return ptn_launch_status();
+}
+
+extern "C" int ptn_zscal_ratio(const void* w, const double* num, const double* den, void* y, int64_t n,
+                               void* stream) {
+  if (!w || !num || !den || !y || n < 1) return PTN_ERR_ARG;
+  PTN_COUNT(1);
+  zscal_ratio_kernel<<<(int)nblocks_for(n), RT, 0, ptn_stream(stream)>>>(
+      static_cast<const double2*>(w), num, den, static_cast<double2*>(y), n);
   return ptn_launch_status();
 }
 

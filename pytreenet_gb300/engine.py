@@ -879,6 +879,20 @@ class DeviceNetwork:
         p.run(R.data_ptr(), 0)
         self.t[dst].view(-1).copy_(self.ws.bufs["absorb"][:self.t[dst].numel()])
         self.flops += p.flops
+        if self.levels and not precise:
+            # dst is an isometry toward src, so the new centre has exactly R's
+            # norm; restore it in FP64 so the reduced-precision product cannot
+            # drift the state norm (fidelity is unaffected either way)
+            lib = _lib.load()
+            t = self.t[dst]
+            k = R.numel()
+            part = self.ws.get("kry_part", int(lib.ptn_krylov_partials(max(t.numel(), k))) + 8)
+            scal = self.ws.get("absorb_norms", 2, torch.float64)
+            check(lib.ptn_dznrm2(R.data_ptr(), k, scal[0:].data_ptr(), part.data_ptr(), _stream_ptr()), "dznrm2")
+            check(lib.ptn_dznrm2(t.data_ptr(), t.numel(), scal[1:].data_ptr(), part.data_ptr(), _stream_ptr()),
+                  "dznrm2")
+            check(lib.ptn_zscal_ratio(t.data_ptr(), scal[0:].data_ptr(), scal[1:].data_ptr(), t.data_ptr(),
+                                      t.numel(), _stream_ptr()), "zscal_ratio")
         node = st.nodes[src]
         if node.parent == dst:
             dn = st.nodes[dst]
@@ -939,7 +953,10 @@ class DeviceNetwork:
                                ["bond" if x == u else info["lv"][info["nv"].index(x)] for x in self.nbrs(v)]
                                + ["sv"], self.shape(v))
         cb.contract(A, B, ["bond"], out=Operand.contiguous(("out",), info["labels"], info["dims"]))
-        p = cb.mixed_plan(self.levels) if self.levels else cb.plan()
+        # FP64 on every path: the merged tensor IS the state (a reduced-precision
+        # product here would move its norm), and the merge is one contraction
+        # against the several matvecs of the Krylov exponential
+        p = cb.plan()
         self.plans[key] = p
         return p
 

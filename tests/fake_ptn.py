@@ -85,6 +85,12 @@ class FakeLib:
         _view(y, n)[:] = _view(w, n) / s
         return 0
 
+    def ptn_zscal_ratio(self, w, num, den, y, n, stream):
+        a, b = _view(num, 1, np.float64)[0], _view(den, 1, np.float64)[0]
+        f = a / b if b > 0 else 1.0
+        _view(y, n)[:] = _view(w, n) * f
+        return 0
+
     def ptn_zcombine(self, Q, ldq, nq, c, out, n, stream):
         Qm = _view(Q, (nq - 1) * ldq + n)
         cv = _view(c, nq)

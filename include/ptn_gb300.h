@@ -31,7 +31,7 @@ enum {
   PTN_ERR_TIMEOUT = 7       /* a bounded device-side wait ran out         */
 };
 
-#define PTN_MAX_MODES 6
+#define PTN_MAX_MODES 8
 
 /* A group of tensor modes that a contraction treats as one GEMM index.
  * n modes, row-major (mode 0 slowest); stride_x[i] is the element stride of

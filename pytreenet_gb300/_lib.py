@@ -10,7 +10,7 @@ import os
 
 from .build import LIB
 
-MAX_MODES = 6
+MAX_MODES = 8
 
 PTN_OK = 0
 _STATUS = {

@@ -1044,116 +1044,190 @@ class DeviceNetwork:
         self.state._phys[nid] = t
         self.state.nodes[nid].shape = tuple(t.shape)
 
+    # Jacobi runs on the q x q core when q is at most this, or when the kept
+    # rank could exceed half of q; otherwise a subspace iteration reduces T to
+    # max_bond_dim + SUBSPACE_OVERSAMPLE columns first.
+    SVD_DIRECT_MAX = 384
+    SUBSPACE_OVERSAMPLE = 16
+    SUBSPACE_MAX_ITERS = 8
+
+    def _qr_inplace(self, buf: torch.Tensor, p: int, k: int, rname: str) -> torch.Tensor:
+        """Householder QR of the p x k column-major matrix in ``buf`` (Q in place);
+        returns R (k x k, row-major) in a workspace slot."""
+        lib = _lib.load()
+        key = ("rowoff_lin", p)
+        if key not in self.rowoff:
+            self.rowoff[key] = torch.arange(p, dtype=torch.int64, device=self.device)
+        R = self.ws.get(rname, k * k)
+        qw = self.ws.get("svd_qrwork", (int(lib.ptn_zqr_work_bytes(p, k)) + 15) // 16)
+        check(lib.ptn_zqr_keep(buf.data_ptr(), self.rowoff[key].data_ptr(), p, k, p, R.data_ptr(),
+                               qw.data_ptr(), _stream_ptr()), "ptn_zqr_keep")
+        self.flops += 8 * 2 * p * k * k
+        return R
+
+    def _jacobi(self, src: torch.Tensor, m: int, n: int, rs: int, cs: int):
+        """Jacobi SVD of an m x n (m >= n) matrix; returns (U slot, V slot, S on host)."""
+        lib = _lib.load()
+        Uj = self.ws.get("svd_U", m * n)
+        Vj = self.ws.get("svd_V", n * n)
+        Sb = self.ws.get("svd_S", n + 2, torch.float64)
+        Sb.zero_()
+        sw = self.ws.get("svd_work", (int(lib.ptn_zsvd_work_bytes(m, n)) + 15) // 16)
+        d = _lib.SvdDesc()
+        d.A, d.m, d.n, d.row_stride, d.col_stride = src.data_ptr(), m, n, rs, cs
+        d.U, d.ldu, d.S, d.V, d.ldv = Uj.data_ptr(), m, Sb.data_ptr(), Vj.data_ptr(), n
+        d.work = sw.data_ptr()
+        d.status = Sb[n:].data_ptr()
+        check(lib.ptn_zsvd_jacobi(ctypes.byref(d), _stream_ptr()), "ptn_zsvd_jacobi")
+        host = Sb.cpu()
+        code = int(host[n:n + 1].view(torch.int32)[0])
+        if code != 0:
+            raise _lib.PtnError(code, "Jacobi SVD")
+        s = host[:n].numpy().copy()
+        if not np.all(np.isfinite(s)):
+            raise _lib.PtnError(3, "Jacobi SVD: non-finite singular values")
+        return Uj, Vj, s
+
+    def _mat(self, t: torch.Tensor, rows: int, cols: int, row_label: str, col_label: str, ld=None) -> Operand:
+        """A column-major rows x cols matrix held in ``t`` as a labelled operand."""
+        return Operand(("fixed", t), [row_label, col_label], [rows, cols], [1, rows if ld is None else ld])
+
+    def _subspace_factor(self, x2: torch.Tensor, p: int, q: int, l: int):
+        """Range finder with subspace (power) iteration and Rayleigh-Ritz on the
+        tall p x q matrix T in ``x2``: T ~= Q1 Vj diag(S) (Qz Uj)^H with
+        Q1 (p x l) and Qz (q x l) orthonormal. Iterates until the leading
+        l - oversample singular values agree to 1e-14 relative between two
+        iterations. The reference computes the full SVD (LAPACK gesdd) and
+        keeps at most max_bond_dim values; the kept triplets agree to that
+        accuracy when the spectrum has left the subspace by then."""
+        key = ("omega", q, l)
+        if key not in self.rowoff:
+            rng = np.random.default_rng(12345)
+            om = (rng.standard_normal((q, l)) + 1j * rng.standard_normal((q, l))) / np.sqrt(2)
+            self.rowoff[key] = torch.from_numpy(np.asfortranarray(om).T.copy()).to(self.device).view(-1)
+        omega = self.rowoff[key]
+        Y = self.ws.get("sub_Y", p * l)
+        Z = self.ws.get("sub_Z", q * l)
+        T = self._mat(x2, p, q, "i", "k")
+        Th = Operand(T.ref, ["i", "k"], [p, q], [1, p])
+        # the range-finding products may run on the tensor cores (the FP64
+        # Rayleigh-Ritz step below fixes the accuracy); T^H Q1 is always FP64
+        cb = ChainBuilder(self.ws)
+        cb.contract(T, self._mat(omega, q, l, "k", "c"), ["k"], out=self._mat(Y, p, l, "i", "c"))
+        first = cb.mixed_plan(self.levels) if self.levels else cb.plan()
+        cb = ChainBuilder(self.ws)
+        cb.contract(Th, self._mat(Y, p, l, "i", "c"), ["i"], out=self._mat(Z, q, l, "k", "c"), conj_a=True)
+        back = cb.plan()
+        cb = ChainBuilder(self.ws)
+        cb.contract(T, self._mat(Z, q, l, "k", "c"), ["k"], out=self._mat(Y, p, l, "i", "c"))
+        fwd = cb.mixed_plan(self.levels) if self.levels else cb.plan()
+        first.run()
+        self.flops += first.flops
+        prev = None
+        keep = max(1, l - self.SUBSPACE_OVERSAMPLE)
+        for it in range(self.SUBSPACE_MAX_ITERS):
+            if it > 0:
+                fwd.run()                      # Y = T Qz
+                self.flops += fwd.flops
+            self._qr_inplace(Y, p, l, "sub_RY")   # Y <- Q1
+            back.run()                         # Z = T^H Q1
+            self.flops += back.flops
+            Rz = self._qr_inplace(Z, q, l, "sub_RZ")   # Z <- Qz, Rz
+            Uj, Vj, s = self._jacobi(Rz, l, l, l, 1)
+            if prev is not None and np.max(np.abs(s[:keep] - prev[:keep])) <= 1e-14 * max(s[0], 1e-300):
+                break
+            prev = s
+        return Y, Z, Uj, Vj, s
+
+    def _write_factor(self, dst: torch.Tensor, ax_side, ax_bond, side_dims, side_labels, Q, q_ld, small,
+                      small_ld, k, r, conj=False, scale=None):
+        """dst[side legs, bond c] = op(Q @ small)[row, c] * scale[c] for c < r,
+        where Q (rows x k, column-major, ld q_ld) may be None (identity), small
+        is k x (>= r) column-major with leading dimension small_ld, rows run
+        over the side legs in C order, and op = conj when ``conj``."""
+        shp = list(dst.shape)
+        dstr = self._cstrides(shp)
+        srow = self._cstrides(side_dims)
+        if Q is None:
+            self._permute(small.data_ptr(), dst.data_ptr(), side_dims + [r], srow + [small_ld],
+                          [dstr[a] for a in ax_side] + [dstr[ax_bond]], conj=conj,
+                          scale_ptr=scale.data_ptr() if scale is not None else 0, scale_mode=len(side_dims))
+            return
+        conj_b = conj
+        if scale is not None:
+            tmp = self.ws.get("svd_small_scaled", k * r)
+            self._permute(small.data_ptr(), tmp.data_ptr(), [r, k], [small_ld, 1], [k, 1], conj=conj,
+                          scale_ptr=scale.data_ptr(), scale_mode=0)
+            small, small_ld, conj_b = tmp, k, False
+        lab = [None] * len(shp)
+        for l_, a in zip(side_labels, ax_side):
+            lab[a] = l_
+        lab[ax_bond] = "c"
+        cb = ChainBuilder(self.ws)
+        A = Operand(("fixed", Q), ["k"] + side_labels, [k] + side_dims, [q_ld] + srow)
+        B = Operand(("fixed", small), ["k", "c"], [k, r], [1, small_ld])
+        cb.contract(A, B, ["k"], out=Operand(("fixed", dst), lab, shp, dstr), conj_a=conj, conj_b=conj_b)
+        pl = cb.plan()
+        pl.run()
+        self.flops += pl.flops
+
     def svd_split(self, u, v, x2: torch.Tensor, svd) -> np.ndarray:
         """Truncated SVD of the merged pair with the singular values moved into
         v (``split_node_svd`` -> ``contr_truncated_svd_splitting`` (VCONTR),
         ``core/ttn.py:1476-1497``, ``util/tensor_splitting.py:488-572``).
-        T (p x q, column-major in ``x2``) is reduced by Householder QR when
-        p > q, the q x q factor goes through the Jacobi SVD, the kept rank comes
-        from ``truncate_singular_values`` (``:448-486``) on the host, and the
-        factors are written straight into u's and v's leg layouts. Returns the
-        kept singular values."""
+        T (p x q, column-major in ``x2``; T = M or M^T, p >= q) is factored as
+        T = Ut diag(S) Vt^H by one of: Jacobi directly (p == q), Householder QR
+        then Jacobi on the q x q R (p > q, q small), or subspace iteration to
+        max_bond_dim + oversample columns then Jacobi (q large). The kept rank
+        comes from ``truncate_singular_values`` (``:448-486``) on the host; the
+        factors go straight into u's and v's leg layouts. Returns the kept
+        singular values."""
         from .truncation import truncate_singular_values
         info = self._two_site_info(u, v)
-        lib = _lib.load()
         st = self.state
         m, n, vfirst = info["m"], info["n"], info["vfirst"]
         p, q = (m, n) if vfirst else (n, m)
-        use_qr = p > q
-        if use_qr:
-            key = ("rowoff_lin", p)
-            if key not in self.rowoff:
-                self.rowoff[key] = torch.arange(p, dtype=torch.int64, device=self.device)
-            R = self.ws.get("svd_R", q * q)
-            qw = self.ws.get("svd_qrwork", (int(lib.ptn_zqr_work_bytes(p, q)) + 15) // 16)
-            check(lib.ptn_zqr_keep(x2.data_ptr(), self.rowoff[key].data_ptr(), p, q, p, R.data_ptr(),
-                                   qw.data_ptr(), _stream_ptr()), "ptn_zqr_keep")
-            self.flops += 8 * 2 * p * q * q
-            jm, src, rs, cs = q, R, q, 1
+        mbd = svd.max_bond_dim
+        l = q if mbd == float("inf") else min(q, int(mbd) + self.SUBSPACE_OVERSAMPLE)
+        if q > self.SVD_DIRECT_MAX and 2 * l <= q:
+            Y, Z, Uj, Vj, s = self._subspace_factor(x2, p, q, l)
+            left = (Y, p, Vj, l, l)        # Ut = Q1 Vj
+            right = (Z, q, Uj, l, l)       # Vt = Qz Uj
+        elif p > q:
+            R = self._qr_inplace(x2, p, q, "svd_R")
+            Uj, Vj, s = self._jacobi(R, q, q, q, 1)
+            left = (x2, p, Uj, q, q)       # Ut = Q Uj
+            right = (None, 0, Vj, q, q)    # Vt = Vj
         else:
-            jm, src, rs, cs = p, x2, 1, p
-        Uj = self.ws.get("svd_U", jm * q)
-        Vj = self.ws.get("svd_V", q * q)
-        Sb = self.ws.get("svd_S", q + 2, torch.float64)
-        Sb.zero_()
-        sw = self.ws.get("svd_work", (int(lib.ptn_zsvd_work_bytes(jm, q)) + 15) // 16)
-        d = _lib.SvdDesc()
-        d.A, d.m, d.n, d.row_stride, d.col_stride = src.data_ptr(), jm, q, rs, cs
-        d.U, d.ldu, d.S, d.V, d.ldv = Uj.data_ptr(), jm, Sb.data_ptr(), Vj.data_ptr(), q
-        d.work = sw.data_ptr()
-        d.status = Sb[q:].data_ptr()
-        check(lib.ptn_zsvd_jacobi(ctypes.byref(d), _stream_ptr()), "ptn_zsvd_jacobi")
-        host = Sb.cpu()
-        code = int(host[q:q + 1].view(torch.int32)[0])
-        if code != 0:
-            raise _lib.PtnError(code, "Jacobi SVD")
-        s = host[:q].numpy()
-        if not np.all(np.isfinite(s)):
-            raise _lib.PtnError(3, "Jacobi SVD: non-finite singular values")
+            Uj, Vj, s = self._jacobi(x2, p, q, 1, p)
+            left = (None, 0, Uj, p, q)
+            right = (None, 0, Vj, q, q)
         new_s, _ = truncate_singular_values(s, svd)
         r = len(new_s)
         scale = self.ws.get("svd_scale", r, torch.float64)
         scale.copy_(torch.from_numpy(np.ascontiguousarray(new_s, dtype=np.float64)))
-        # destination tensors (new storage when the bond dimension changes)
-        old_r = self.shape(u)[st.phys_axis(u, v)]
-        shp_u = self.shape(u)
-        shp_u[st.phys_axis(u, v)] = r
-        shp_v = self.shape(v)
-        shp_v[st.phys_axis(v, u)] = r
+        bu, bv = st.phys_axis(u, v), st.phys_axis(v, u)
+        old_r = self.shape(u)[bu]
+        shp_u, shp_v = self.shape(u), self.shape(v)
+        shp_u[bu] = r
+        shp_v[bv] = r
         if r == old_r:
             tu, tv = self.t[u], self.t[v]
         else:
             tu = torch.empty(shp_u, dtype=CDT, device=self.device)
             tv = torch.empty(shp_v, dtype=CDT, device=self.device)
-        su_str, sv_str = self._cstrides(shp_u), self._cstrides(shp_v)
-        ax_u = [st.phys_axis(u, x) for x in info["nu"]] + [len(shp_u) - 1]   # u-side legs in u
+        ax_u = [st.phys_axis(u, x) for x in info["nu"]] + [len(shp_u) - 1]
         ax_v = [st.phys_axis(v, x) for x in info["nv"]] + [len(shp_v) - 1]
-        bu, bv = st.phys_axis(u, v), st.phys_axis(v, u)
-        du, dv = info["du"], info["dv"]
-        cu, cv = self._cstrides(du), self._cstrides(dv)
+        U_side = (tu, ax_u, bu, info["du"], info["lu"])
+        V_side = (tv, ax_v, bv, info["dv"], info["lv"])
         if vfirst:
-            # M = (Q Uj) S Vj^H: u <- Q Uj[:, :r], v <- S Vj^H
-            if use_qr:
-                cb = ChainBuilder(self.ws)
-                Q = Operand.contiguous(("fixed", x2), ["k"] + info["lu"], [q] + du)
-                Uo = Operand(("fixed", Uj), ["k", "c"], [q, r], [1, q])
-                lab = [None] * len(shp_u)
-                for l_, a in zip(info["lu"], ax_u):
-                    lab[a] = l_
-                lab[bu] = "c"
-                cb.contract(Q, Uo, ["k"], out=Operand(("fixed", tu), lab, shp_u, su_str))
-                pl = cb.plan()
-                pl.run()
-                self.flops += pl.flops
-            else:
-                self._permute(Uj.data_ptr(), tu.data_ptr(), du + [r], cu + [jm],
-                              [su_str[a] for a in ax_u] + [su_str[bu]])
-            self._permute(Vj.data_ptr(), tv.data_ptr(), dv + [r], cv + [q],
-                          [sv_str[a] for a in ax_v] + [sv_str[bv]], conj=True,
-                          scale_ptr=scale.data_ptr(), scale_mode=len(dv))
+            # M = Ut S Vt^H: u <- Ut[:, :r], v[c, j] = S_c conj(Vt[j, c])
+            self._write_factor(*U_side, *left[:4], left[4], r)
+            self._write_factor(*V_side, *right[:4], right[4], r, conj=True, scale=scale)
         else:
-            # M^T = (Q Uj) S Vj^H, so M = conj(Vj) S (Q Uj)^T: u <- conj(Vj[:, :r]), v <- S (Q Uj)^T
-            self._permute(Vj.data_ptr(), tu.data_ptr(), du + [r], cu + [q],
-                          [su_str[a] for a in ax_u] + [su_str[bu]], conj=True)
-            if use_qr:
-                Us = self.ws.get("svd_Us", q * r)
-                self._permute(Uj.data_ptr(), Us.data_ptr(), [r, q], [jm, 1], [q, 1],
-                              scale_ptr=scale.data_ptr(), scale_mode=0)
-                cb = ChainBuilder(self.ws)
-                Q = Operand.contiguous(("fixed", x2), ["k"] + info["lv"], [q] + dv)
-                Uo = Operand(("fixed", Us), ["k", "c"], [q, r], [1, q])
-                lab = [None] * len(shp_v)
-                for l_, a in zip(info["lv"], ax_v):
-                    lab[a] = l_
-                lab[bv] = "c"
-                cb.contract(Q, Uo, ["k"], out=Operand(("fixed", tv), lab, shp_v, sv_str))
-                pl = cb.plan()
-                pl.run()
-                self.flops += pl.flops
-            else:
-                self._permute(Uj.data_ptr(), tv.data_ptr(), dv + [r], cv + [jm],
-                              [sv_str[a] for a in ax_v] + [sv_str[bv]],
-                              scale_ptr=scale.data_ptr(), scale_mode=len(dv))
+            # M = conj(Vt) S Ut^T: u <- conj(Vt[:, :r]), v[c, j] = S_c Ut[j, c]
+            self._write_factor(*U_side, *right[:4], right[4], r, conj=True)
+            self._write_factor(*V_side, *left[:4], left[4], r, scale=scale)
         if r != old_r:
             self._forget_node(u)
             self._forget_node(v)

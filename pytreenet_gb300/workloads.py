@@ -154,3 +154,31 @@ def ternary_xxz(state: TreeTensorNetworkState, seed: int = 7):
     jz = {e: rng.uniform(0.5, 1.5) for e in edges}
     H = heisenberg_ttno(state, None, jxy, jz)
     return H, {nid: H.phys(nid) for nid in state._order}
+
+
+def ternary_saturated_state(depth: int = 3, chi: int = 64, seed: int = 0):
+    """Random ternary-tree TTNS whose bonds are as large as a two-site TDVP run
+    with max_bond_dim ``chi`` makes them: min(chi, 2^(sites below the bond),
+    2^(sites above it)). Returns (TTNS, spec, tensors)."""
+    rng = np.random.default_rng(seed)
+    spec = ternary_spec(depth)
+    kids = {nid: [] for nid, _ in spec}
+    for nid, p in spec:
+        if p is not None:
+            kids[p].append(nid)
+    below = {}
+
+    def count(nid):
+        below[nid] = 1 + sum(count(c) for c in kids[nid])
+        return below[nid]
+    total = count(spec[0][0])
+
+    def bond(child):
+        b = min(below[child], total - below[child])
+        return int(min(chi, 2 ** min(b, 30)))
+    tensors = {}
+    for nid, p in spec:
+        shape = ([bond(nid)] if p is not None else []) + [bond(c) for c in kids[nid]] + [2]
+        t = rng.normal(size=shape) + 1j * rng.normal(size=shape)
+        tensors[nid] = t / np.linalg.norm(t)
+    return _build(spec, tensors), spec, tensors

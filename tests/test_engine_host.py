@@ -172,3 +172,39 @@ def test_svd_parameters_validation():
             warnings.simplefilter("ignore")
             new_s, _ = P.truncate_singular_values(d[f"svd/{i}/s"], p)
         np.testing.assert_allclose(new_s, d[f"svd/{i}/out"], rtol=1e-15, atol=0)
+
+
+def _two_site_vs_oracle(chi, max_bond_dim, steps=2):
+    import pytreenet_gb300 as P
+    import oracle as O
+    from pytreenet_gb300.workloads import ternary_state, ternary_xxz
+    st, spec, tensors = ternary_state(depth=2, chi=chi, seed=11)
+    H, Wphys = ternary_xxz(st, seed=12)
+    svd = dict(max_bond_dim=max_bond_dim, rel_tol=1e-10, total_tol=1e-10)
+    cfg = P.TwoSiteTDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV, **svd)
+    algo = P.SecondOrderTwoSiteTDVP(st, H, 0.02, 0.02 * steps, {}, config=cfg,
+                                    solver_options={"krylov_tol": 1e-12})
+    tree = O.OTree()
+    for nid, p in spec:
+        tree.add_root(nid) if p is None else tree.add_child(nid, p)
+    ora = O.SecondOrderTwoSiteTDVPOracle(O.OState(tree, tensors), Wphys, 0.02, O.SVDParams(**svd),
+                                         krylov_tol=1e-12)
+    for _ in range(steps):
+        algo.run_one_time_step()
+        ora.run_one_time_step()
+    got = O.OState(tree, {nid: algo.state.get_phys_numpy(nid) for nid, _ in spec})
+    return algo, ora, fidelity_and_dist(ora.state, got)
+
+
+def test_engine_host_two_site_subspace_split(monkeypatch):
+    """Subspace-iteration reduction of large merged pairs (forced on small ones)."""
+    fake_ptn.install(monkeypatch)
+    import pytreenet_gb300.engine as E
+    monkeypatch.setattr(E.DeviceNetwork, "SVD_DIRECT_MAX", 8)
+    calls = []
+    orig = E.DeviceNetwork._subspace_factor
+    monkeypatch.setattr(E.DeviceNetwork, "_subspace_factor", lambda self, *a: calls.append(a[1:]) or orig(self, *a))
+    algo, ora, (one_minus_f, dist) = _two_site_vs_oracle(12, 5)
+    assert calls
+    assert algo.bond_dims_history == ora.bond_history
+    assert one_minus_f < 1e-12

@@ -148,3 +148,17 @@ def test_gpu_two_site_ternary_chi16_vs_oracle():
     got = O.OState(tree, {nid: algo.state.get_phys_numpy(nid) for nid, _ in spec})
     one_minus_f, dist = fidelity_and_dist(ora.state, got)
     assert one_minus_f < 1e-11
+
+
+def test_gpu_two_site_subspace_split(monkeypatch):
+    """Subspace-iteration reduction (forced on small pairs) against the oracle."""
+    import pytreenet_gb300.engine as E
+    from test_engine_host import _two_site_vs_oracle
+    monkeypatch.setattr(E.DeviceNetwork, "SVD_DIRECT_MAX", 8)
+    calls = []
+    orig = E.DeviceNetwork._subspace_factor
+    monkeypatch.setattr(E.DeviceNetwork, "_subspace_factor", lambda self, *a: calls.append(a[1:]) or orig(self, *a))
+    algo, ora, (one_minus_f, dist) = _two_site_vs_oracle(12, 5)
+    assert calls
+    assert algo.bond_dims_history == ora.bond_history
+    assert one_minus_f < 1e-11

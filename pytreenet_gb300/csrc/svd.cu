@@ -8,7 +8,7 @@
 // (circle) order: n_even - 1 rounds of n_even / 2 disjoint pairs, one warp per
 // pair. Rounds are separated by a grid-wide barrier; the kernel is launched
 // cooperatively so all CTAs are resident. A pair (a, b) is rotated when
-// |a^H b| > tol * |a| |b| (tol = sqrt(m) * 2^-53, as LAPACK's zgesvj); the
+// |a^H b| > tol * |a| |b| (tol = 8 sqrt(m) * 2^-53); the
 // iteration stops after the first sweep without a rotation. Every barrier wait
 // is bounded: on timeout the kernel records PTN_ERR_TIMEOUT in *status and all
 // CTAs leave. A sweep limit that is reached records PTN_ERR_NOCONVERGE (the
@@ -24,7 +24,7 @@ namespace {
 
 constexpr int SVD_WARPS = 4;
 constexpr int SVD_THREADS = SVD_WARPS * 32;
-constexpr int SVD_MAX_SWEEPS = 48;
+constexpr int SVD_MAX_SWEEPS = 56;
 constexpr long long SVD_WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
 constexpr int CTRL_WORDS = 64;                       // barrier words + per-sweep rotation counts
 constexpr int64_t CTRL_BYTES = 256;
@@ -88,8 +88,11 @@ __device__ bool grid_barrier(unsigned* ctrl, int32_t* status) {
 }
 
 // Rotate columns i and j of Aw (and of Vw) so that they become orthogonal.
+// Columns whose squared norm is at most `zero2` (numerically zero: norm below
+// tol times the largest input column norm) are left alone; their directions
+// are rounding noise, and rotating such pairs can cycle without converging.
 // Returns true when a rotation was applied.
-__device__ bool rotate_pair(const SvdArgs& a, int64_t i, int64_t j, int lane) {
+__device__ bool rotate_pair(const SvdArgs& a, int64_t i, int64_t j, int lane, double zero2) {
   double2* ci = a.Aw + i * a.m;
   double2* cj = a.Aw + j * a.m;
   double al = 0.0, be = 0.0;
@@ -103,6 +106,7 @@ __device__ bool rotate_pair(const SvdArgs& a, int64_t i, int64_t j, int lane) {
   al = warp_sum(al);
   be = warp_sum(be);
   ga = warp_sum2(ga);
+  if (al <= zero2 || be <= zero2) return false;
   const double g = hypot(ga.x, ga.y);
   if (!(g > a.tol * sqrt(al) * sqrt(be))) return false;
   // Real rotation on (a, e^{-i phi} b), e^{i phi} = ga / |ga|, angle from
@@ -150,6 +154,17 @@ __global__ void __launch_bounds__(SVD_THREADS) zsvd_jacobi_kernel(SvdArgs a) {
     stcg2(a.Vw + e, make_double2(i == j ? 1.0 : 0.0, 0.0));
   }
   if (!grid_barrier(a.ctrl, a.status)) return;
+  // largest squared column norm (non-negative doubles order like their bit patterns)
+  unsigned long long* amax_bits = reinterpret_cast<unsigned long long*>(a.ctrl + 4);
+  for (int64_t j = gw; j < n; j += nw) {
+    double s2 = 0.0;
+    for (int64_t k = lane; k < m; k += 32) s2 += cabs2(ldcg2(a.Aw + j * m + k));
+    s2 = warp_sum(s2);
+    if (lane == 0) atomicMax(amax_bits, (unsigned long long)__double_as_longlong(s2));
+  }
+  if (!grid_barrier(a.ctrl, a.status)) return;
+  const double amax2 = __longlong_as_double((long long)*((volatile unsigned long long*)amax_bits));
+  const double zero2 = a.tol * a.tol * amax2;
 
   const int64_t np = (n + 1) & ~int64_t(1);
   int sweep = 0;
@@ -161,7 +176,7 @@ __global__ void __launch_bounds__(SVD_THREADS) zsvd_jacobi_kernel(SvdArgs a) {
         const int64_t i = (x == 0) ? 0 : 1 + (x - 1 + r) % (np - 1);
         const int64_t j = 1 + (y - 1 + r) % (np - 1);
         if (i >= n || j >= n) continue;
-        const bool rot = rotate_pair(a, i < j ? i : j, i < j ? j : i, lane);
+        const bool rot = rotate_pair(a, i < j ? i : j, i < j ? j : i, lane, zero2);
         if (rot && lane == 0) atomicAdd(a.ctrl + 8 + (sweep % (CTRL_WORDS - 8)), 1u);
       }
       if (!grid_barrier(a.ctrl, a.status)) return;
@@ -263,7 +278,10 @@ extern "C" int ptn_zsvd_jacobi(const ptn_svd_desc* d, void* stream) {
   a.S = d->S;
   a.V = static_cast<double2*>(d->V);
   a.ldv = d->ldv;
-  a.tol = sqrt((double)d->m) * 1.1102230246251565e-16;
+  // sqrt(m) * 2^-53 (LAPACK's zgesvj) sits at the rounding floor of one
+  // rotation for small m, and a pair can then cycle without ever passing the
+  // test; 8 sqrt(m) * 2^-53 keeps U and V orthonormal to ~1e-14.
+  a.tol = 8.0 * sqrt((double)d->m) * 1.1102230246251565e-16;
   a.status = d->status;
   cudaStream_t s = ptn_stream(stream);
   if (cudaMemsetAsync(a.ctrl, 0, CTRL_BYTES, s) != cudaSuccess) return PTN_ERR_LAUNCH;

@@ -587,6 +587,17 @@ class DeviceNetwork:
         self.qr_R = torch.zeros((kmax * kmax,), dtype=CDT, device=self.device)
         self.qr_work = torch.zeros(((wmax + 15) // 16,), dtype=CDT, device=self.device)
 
+    # Chains below this many algorithmic flops run in FP64 even on the mixed
+    # path: there the tensor-core plan's extra conversion launches cost more
+    # than the FP64 arithmetic (leaves, small bonds, small two-site pairs).
+    MIXED_MIN_FLOPS = 2e8
+
+    def _use_mixed(self, cb: "ChainBuilder") -> bool:
+        return bool(self.levels) and sum(st.flops for st in cb.steps) >= self.MIXED_MIN_FLOPS
+
+    def _finish(self, cb: "ChainBuilder"):
+        return cb.mixed_plan(self.levels) if self._use_mixed(cb) else cb.plan()
+
     # -- shapes ------------------------------------------------------------------
     def nbrs(self, nid):
         return self.state.nodes[nid].phys_neighbours()
@@ -642,7 +653,7 @@ class DeviceNetwork:
                 T = cb.contract(T, E, [f"a{k}", f"b{k}"])
         if not rest:
             raise RuntimeError("site without neighbours")
-        p = cb.mixed_plan(self.levels) if self.levels else cb.plan()
+        p = self._finish(cb)
         self.plans[key] = p
         return p
 
@@ -664,7 +675,7 @@ class DeviceNetwork:
                                [f"c{k}" if k != k0 else "z" for k in range(n)] + ["t"], shape)
         E = self._env_op(nid, nxt, [f"a{k0}", f"b{k0}", "z"])
         cb.contract(T, B, [f"c{k}" for k in range(n) if k != k0] + ["t"], out=E, conj_b=True)
-        p = cb.mixed_plan(self.levels) if self.levels else cb.plan()
+        p = self._finish(cb)
         self.plans[key] = p
         return p
 
@@ -682,7 +693,7 @@ class DeviceNetwork:
         y = Operand.contiguous(("out",), ["x", "y"], [chi_q, chi_n])
         T = cb.contract(eq, r, ["a"])
         cb.contract(T, en, ["c", "b"], out=y)
-        p = cb.mixed_plan(self.levels) if self.levels else cb.plan()
+        p = self._finish(cb)
         self.plans[key] = p
         return p
 
@@ -868,7 +879,7 @@ class DeviceNetwork:
             out = Operand.contiguous(("ws", "absorb"), labels, shape)
             cb.sizes["absorb"] = out.numel()
             cb.contract(T, Rop, [f"a{ax}"], out=out)
-            if self.levels and not precise:
+            if not precise and self._use_mixed(cb):
                 mp = cb.mixed_plan(self.levels)
                 mp.sizes_c128 = dict(cb.sizes)
                 self.plans[key] = mp
@@ -879,7 +890,7 @@ class DeviceNetwork:
         p.run(R.data_ptr(), 0)
         self.t[dst].view(-1).copy_(self.ws.bufs["absorb"][:self.t[dst].numel()])
         self.flops += p.flops
-        if self.levels and not precise:
+        if isinstance(p, MixedPlan):
             # dst is an isometry toward src, so the new centre has exactly R's
             # norm; restore it in FP64 so the reduced-precision product cannot
             # drift the state norm (fidelity is unaffected either way)
@@ -995,7 +1006,7 @@ class DeviceNetwork:
                 cb.contract(T, op, kl, out=y)
             else:
                 T = cb.contract(T, op, kl)
-        p = cb.mixed_plan(self.levels) if self.levels else cb.plan()
+        p = self._finish(cb)
         self.plans[key] = p
         return p
 
@@ -1114,13 +1125,13 @@ class DeviceNetwork:
         # Rayleigh-Ritz step below fixes the accuracy); T^H Q1 is always FP64
         cb = ChainBuilder(self.ws)
         cb.contract(T, self._mat(omega, q, l, "k", "c"), ["k"], out=self._mat(Y, p, l, "i", "c"))
-        first = cb.mixed_plan(self.levels) if self.levels else cb.plan()
+        first = self._finish(cb)
         cb = ChainBuilder(self.ws)
         cb.contract(Th, self._mat(Y, p, l, "i", "c"), ["i"], out=self._mat(Z, q, l, "k", "c"), conj_a=True)
         back = cb.plan()
         cb = ChainBuilder(self.ws)
         cb.contract(T, self._mat(Z, q, l, "k", "c"), ["k"], out=self._mat(Y, p, l, "i", "c"))
-        fwd = cb.mixed_plan(self.levels) if self.levels else cb.plan()
+        fwd = self._finish(cb)
         first.run()
         self.flops += first.flops
         prev = None

@@ -162,3 +162,19 @@ def test_gpu_two_site_subspace_split(monkeypatch):
     assert calls
     assert algo.bond_dims_history == ora.bond_history
     assert one_minus_f < 1e-11
+
+
+@pytest.mark.parametrize("n", [2, 3, 4, 8, 16, 32])
+def test_jacobi_svd_converges_on_many_small_matrices(n):
+    """Small and triangular matrices (the R factors the split feeds in), many seeds."""
+    rng = np.random.default_rng(100 + n)
+    for trial in range(24):
+        A = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
+        if trial % 2:
+            A = np.triu(A)
+        if trial % 3 == 0:
+            A[:, -1] *= 1e-9
+        U, s, V, code = _svd_gpu(A, transpose_input=bool(trial % 4 == 1))
+        assert code == 0, (n, trial)
+        np.testing.assert_allclose(s, np.linalg.svd(A, compute_uv=False), rtol=0, atol=1e-13 * s[0])
+        assert np.linalg.norm((U * s) @ V.conj().T - A) <= 1e-13 * np.linalg.norm(A)

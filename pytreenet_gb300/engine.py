@@ -820,6 +820,9 @@ class DeviceNetwork:
         m = rowoff.numel()
         k = shape[col_axis]
         lib = _lib.load()
+        # two-site splits change bond dimensions, and with them the row count of
+        # every other split of the two nodes: size R and the work area for this one
+        self._ensure_qr_buffers(m, k)
         ckey = (nid, tuple(row_axes), col_axis)
         if self.levels and m >= self.CHOLQR_MIN_ROWS and m >= 2 * k and ckey not in self.cholqr_fails:
             backup = self.ws.get("cholqr_backup", self.t[nid].numel())
@@ -1274,10 +1277,6 @@ class DeviceNetwork:
         self.check_device_status()
         s = self.svd_split(u, v, x2, svd)
         self.state.orthogonality_center_id = v
-        for a, b in ((u, v), (v, u)):
-            k = self.shape(a)[self.state.phys_axis(a, b)]
-            rows = self.t[a].numel() // max(k, 1)
-            self._ensure_qr_buffers(rows, k)
         self.update_env(u, v)
         return s
 

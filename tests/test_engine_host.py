@@ -208,3 +208,36 @@ def test_engine_host_two_site_subspace_split(monkeypatch):
     assert calls
     assert algo.bond_dims_history == ora.bond_history
     assert one_minus_f < 1e-12
+
+
+def test_engine_host_qr_buffers_follow_bond_growth(monkeypatch):
+    """Two-site splits grow bonds; every later QR split must find R and the
+    work area large enough for its own (rows, k) -- sized by the library's own
+    ptn_zqr_work_bytes (a host-only function of the real .so)."""
+    import ctypes
+    fake = fake_ptn.install(monkeypatch)
+    from pytreenet_gb300.build import LIB, build
+    build()
+    real = ctypes.CDLL(LIB)
+    real.ptn_zqr_work_bytes.restype = ctypes.c_int64
+    real.ptn_zqr_work_bytes.argtypes = [ctypes.c_int64, ctypes.c_int64]
+    monkeypatch.setattr(type(fake), "ptn_zqr_work_bytes", lambda self, m, k: int(real.ptn_zqr_work_bytes(m, k)))
+    import pytreenet_gb300.engine as E
+    orig = E.DeviceNetwork.qr_split
+    checked = []
+
+    def qr_split(self, nid, nbr):
+        R = orig(self, nid, nbr)
+        k = self.shape(nid)[self.state.phys_axis(nid, nbr)]
+        m = self.t[nid].numel() // k
+        assert self.qr_R.numel() >= k * k
+        assert self.qr_work.numel() * 16 >= real.ptn_zqr_work_bytes(m, k), (nid, nbr, m, k)
+        checked.append((m, k))
+        return R
+    monkeypatch.setattr(E.DeviceNetwork, "qr_split", qr_split)
+    # chi = 12: the first splits shrink a depth-1 node's leg to 2, so its QR
+    # toward the root drops from 3456 rows (multi-kernel path) to 576 rows
+    # (one-launch path, whose V buffer needs m * min(m, k) entries)
+    algo, ora, (one_minus_f, dist) = _two_site_vs_oracle(12, 5, steps=1)
+    assert checked
+    assert one_minus_f < 1e-12

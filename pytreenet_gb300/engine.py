@@ -587,16 +587,12 @@ class DeviceNetwork:
         self.qr_R = torch.zeros((kmax * kmax,), dtype=CDT, device=self.device)
         self.qr_work = torch.zeros(((wmax + 15) // 16,), dtype=CDT, device=self.device)
 
-    # Chains below this many algorithmic flops run in FP64 even on the mixed
-    # path: there the tensor-core plan's extra conversion launches cost more
-    # than the FP64 arithmetic (leaves, small bonds, small two-site pairs).
-    MIXED_MIN_FLOPS = 2e8
-
-    def _use_mixed(self, cb: "ChainBuilder") -> bool:
-        return bool(self.levels) and sum(st.flops for st in cb.steps) >= self.MIXED_MIN_FLOPS
-
     def _finish(self, cb: "ChainBuilder"):
-        return cb.mixed_plan(self.levels) if self._use_mixed(cb) else cb.plan()
+        """The chain as a tensor-core plan on the reduced-precision paths, else FP64.
+        (Small chains stay on the tensor cores too: the FP64 kernel's 64 x 64
+        tiles leave most of the GPU idle on skinny shapes such as a leaf's
+        2 x 256 x 1280 step, measured 16x slower than the tensor-core plan.)"""
+        return cb.mixed_plan(self.levels) if self.levels else cb.plan()
 
     # -- shapes ------------------------------------------------------------------
     def nbrs(self, nid):
@@ -882,7 +878,7 @@ class DeviceNetwork:
             out = Operand.contiguous(("ws", "absorb"), labels, shape)
             cb.sizes["absorb"] = out.numel()
             cb.contract(T, Rop, [f"a{ax}"], out=out)
-            if not precise and self._use_mixed(cb):
+            if self.levels and not precise:
                 mp = cb.mixed_plan(self.levels)
                 mp.sizes_c128 = dict(cb.sizes)
                 self.plans[key] = mp

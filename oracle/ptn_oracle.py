@@ -1,4 +1,4 @@
-"""NumPy restatement of PyTreeNet's one-site and two-site TDVP hot path (oracle, test infrastructure).
+"""NumPy restatement of PyTreeNet's TDVP (one-site, two-site) and TEBD hot path (oracle, test infrastructure).
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
 ``bench.py`` may use this module; the GPU engine never imports it.
@@ -27,7 +27,7 @@ __all__ = [
     "SecondOrderOneSiteTDVPOracle", "state_vector", "expect_product",
     "scalar_product", "SVDParams", "truncate_singular_values", "two_site_merge",
     "two_site_heff_apply", "two_site_split", "SecondOrderTwoSiteTDVPOracle",
-    "FirstOrderTwoSiteTDVPOracle",
+    "FirstOrderTwoSiteTDVPOracle", "tebd_apply_gate", "TEBDOracle", "ttno_expectation",
 ]
 
 
@@ -785,3 +785,54 @@ class FirstOrderTwoSiteTDVPOracle(_TwoSiteBase):
         self.update_two_sites(path[-2], path[-1])
         move_orth_center(self.state, path[0])
         self.envs = init_cache_but_one(self.state, self.W, path[0])
+
+
+# ----------------------------------------------------------------------------
+# TEBD
+# ----------------------------------------------------------------------------
+def tebd_apply_gate(state: OState, op, ids, params: SVDParams):
+    """One exponentiated Trotter operator (``TEBD._apply_one_trotter_step``,
+    ``time_evolution/tebd.py:84-155``): a one-site gate is absorbed into the
+    physical leg (``absorb_into_open_legs``, ``core/ttn.py:929-964``); a two-site
+    gate (legs out_1, out_2, in_1, in_2 for ids = (u, v)) acts on the merged
+    pair, which is split again by the truncated SVD with the singular values
+    moved into v."""
+    op = np.asarray(op)
+    if len(ids) == 1:
+        A = state.tensors[ids[0]]
+        state.tensors[ids[0]] = np.moveaxis(np.tensordot(op, A, axes=([1], [A.ndim - 1])), 0, -1)
+        return None
+    if len(ids) != 2:
+        raise NotImplementedError("More than two-site interactions are not implemented.")
+    u, v = ids
+    x, nu, nv = two_site_merge(state, u, v)
+    iu, iv = len(nu), x.ndim - 1
+    y = np.tensordot(x, op, axes=([iu, iv], [2, 3]))          # (nu..., nv..., gu, gv)
+    y = np.moveaxis(y, [y.ndim - 2, y.ndim - 1], [iu, y.ndim - 1])
+    return two_site_split(state, y, nu, nv, u, v, params)
+
+
+class TEBDOracle:
+    """``TEBD.run_one_time_step`` (``time_evolution/tebd.py:84-155``): every
+    exponentiated Trotter operator applied once, in order."""
+
+    def __init__(self, state: OState, gates, params: SVDParams):
+        self.state = state.copy()
+        self.gates = list(gates)
+        self.params = params
+
+    def run_one_time_step(self):
+        for op, ids in self.gates:
+            tebd_apply_gate(self.state, op, ids, self.params)
+
+
+def ttno_expectation(state: OState, W: dict) -> complex:
+    """<psi| H |psi> for a TTNO (``TTNS.ttno_expectation_value`` through
+    ``expectation_value``, ``contractions/state_operator_contraction.py:26-74``):
+    every environment toward the root, then the root's H_eff applied to the
+    root tensor and contracted with its conjugate."""
+    root = state.tree.root
+    envs = init_cache_but_one(state, W, root)
+    x = state.tensors[root]
+    y = heff_apply(x, state.tree, root, W[root], envs)
+    return complex(np.vdot(x.reshape(-1), y.reshape(-1)))

@@ -3,8 +3,8 @@
 Drop-in surface for the path (names as in PyTreeNet):
 TreeTensorNetworkState/TTNS, TreeTensorNetworkOperator/TTNO, Node,
 FirstOrderOneSiteTDVP, SecondOrderOneSiteTDVP, FirstOrderTwoSiteTDVP,
-SecondOrderTwoSiteTDVP, TDVPConfig, TwoSiteTDVPConfig, SVDParameters,
-TimeEvoMode, EvoDirection, TensorProduct. Numerics run in libptn_gb300.so
+SecondOrderTwoSiteTDVP, TDVPConfig, TwoSiteTDVPConfig, SVDParameters, TEBD,
+TrotterStep, TrotterSplitting, TimeEvoMode, EvoDirection, TensorProduct. Numerics run in libptn_gb300.so
 (hand-written CUDA for sm_103a) through a C ABI; see include/ptn_gb300.h.
 """
 from .ttn import Node, TreeTensorNetworkState, TreeTensorNetworkOperator, TTNS, TTNO
@@ -12,6 +12,7 @@ from .tdvp import (TimeEvoMode, EvoDirection, PathFinderMode, TDVPConfig, Tensor
                    FirstOrderOneSiteTDVP, SecondOrderOneSiteTDVP, leaf_to_root_update_path,
                    TwoSiteTDVPConfig, FirstOrderTwoSiteTDVP, SecondOrderTwoSiteTDVP)
 from .truncation import SVDParameters, truncate_singular_values
+from .tebd import TEBD, TrotterStep, TrotterSplitting, NumericOperator
 from .operators import nearest_neighbour_ttno, tfim_ttno, heisenberg_ttno
 
 __all__ = [
@@ -19,6 +20,7 @@ __all__ = [
     "TimeEvoMode", "EvoDirection", "PathFinderMode", "TDVPConfig", "TensorProduct",
     "FirstOrderOneSiteTDVP", "SecondOrderOneSiteTDVP", "leaf_to_root_update_path",
     "TwoSiteTDVPConfig", "FirstOrderTwoSiteTDVP", "SecondOrderTwoSiteTDVP",
-    "SVDParameters", "truncate_singular_values",
+    "SVDParameters", "truncate_singular_values", "TEBD", "TrotterStep", "TrotterSplitting",
+    "NumericOperator",
     "nearest_neighbour_ttno", "tfim_ttno", "heisenberg_ttno",
 ]

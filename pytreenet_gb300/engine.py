@@ -1276,6 +1276,44 @@ class DeviceNetwork:
         self.update_env(u, v)
         return s
 
+    # -- TEBD gates -------------------------------------------------------------------
+    def apply_single_site_gate(self, nid, op: torch.Tensor):
+        """t[nid][..., s'] = sum_s op[s', s] t[nid][..., s] (``absorb_into_open_legs``,
+        ``core/ttn.py:929-964``)."""
+        shape = self.shape(nid)
+        n = len(shape) - 1
+        cb = ChainBuilder(self.ws)
+        T = Operand.contiguous(("fixed", self.t[nid]), [f"a{k}" for k in range(n)] + ["s"], shape)
+        G = Operand.contiguous(("fixed", op), ["t", "s"], list(op.shape))
+        out = Operand.contiguous(("ws", "gate_out"), [f"a{k}" for k in range(n)] + ["t"], shape)
+        cb.sizes["gate_out"] = out.numel()
+        cb.contract(T, G, ["s"], out=out)
+        p = cb.plan()
+        p.run()
+        self.flops += p.flops
+        self.t[nid].view(-1).copy_(self.ws.bufs["gate_out"][:self.t[nid].numel()])
+
+    def apply_two_site_gate(self, u, v, op: torch.Tensor, svd) -> np.ndarray:
+        """A two-site gate (legs out_u, out_v, in_u, in_v) on neighbours u, v:
+        merge, apply, truncated SVD split with the singular values moved into v
+        (``TEBD._apply_one_trotter_step_two_site``, ``time_evolution/tebd.py:103-125``).
+        FP64 throughout (one contraction per gate). Returns the kept singular values."""
+        info = self._two_site_info(u, v)
+        x2 = self.ws.get("two_site", info["m"] * info["n"])
+        mp = self.merge_plan(u, v)
+        mp.run(0, x2.data_ptr())
+        self.flops += mp.flops
+        y = self.ws.get("two_site_gate", info["m"] * info["n"])
+        cb = ChainBuilder(self.ws)
+        X = Operand.contiguous(("fixed", x2), info["labels"], info["dims"])
+        G = Operand.contiguous(("fixed", op), ["tu", "tv", "su", "sv"], list(op.shape))
+        out_labels = [{"su": "tu", "sv": "tv"}.get(l, l) for l in info["labels"]]
+        cb.contract(X, G, ["su", "sv"], out=Operand.contiguous(("fixed", y), out_labels, info["dims"]))
+        p = cb.plan()
+        p.run()
+        self.flops += p.flops
+        return self.svd_split(u, v, y, svd)
+
     def normalise_center(self) -> float:
         """Divide the orthogonality centre by its norm (``TTNS.normalise``,
         ``ttns/ttns.py:105-125``); returns the old norm."""
@@ -1334,6 +1372,28 @@ class DeviceNetwork:
             return res
         return complex(rec(st.root_id, None).cpu().numpy()[0])
 
+
+    def expect_ttno(self, ttno) -> complex:
+        """<psi| O |psi> for a TTNO on the same tree (``TTNS.operator_expectation_value``,
+        ``ttns/ttns.py:278-297`` -> ``expectation_value``,
+        ``contractions/state_operator_contraction.py:26-74``): a second network
+        over the same device tensors (no copies) holds O and its own
+        environments; all of them point to the root, whose H_eff applied to the
+        root tensor is contracted with its conjugate."""
+        other = DeviceNetwork(self.state, ttno, device=self.device,
+                              precision="plain")
+        root = self.state.root_id
+        other.init_cache_but_one(root)
+        x = self.t[root]
+        y = torch.empty_like(x)
+        other.heff_plan(root).run(x.data_ptr(), y.data_ptr())
+        lib = _lib.load()
+        n = x.numel()
+        part = self.ws.get("kry_part", int(lib.ptn_krylov_partials(n)) * 2 + 8)
+        h = self.ws.get("expect_h", 1)
+        check(lib.ptn_zdot_multi(x.data_ptr(), n, 1, y.data_ptr(), n, h.data_ptr(), 0, part.data_ptr(),
+                                 _stream_ptr()), "zdot_multi")
+        return complex(h.cpu().numpy()[0])
 
     def expect_local(self, ops: dict) -> complex:
         """<psi| prod_i O_i |psi> for single-site operators

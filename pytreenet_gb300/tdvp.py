@@ -212,6 +212,11 @@ class OneSiteTDVP:
 
     # -- observables -----------------------------------------------------------------
     def evaluate_operator(self, operator) -> complex:
+        """``TTNTimeEvolution.evaluate_operator`` (``time_evolution/ttn_time_evolution.py:181-211``):
+        a TensorProduct of one-site operators, or a TTNO on the state's tree."""
+        from .ttn import TreeTensorNetworkOperator
+        if isinstance(operator, TreeTensorNetworkOperator):
+            return self.net.expect_ttno(operator)
         return self.net.expect_local(dict(operator))
 
     def evaluate_operators(self):

@@ -1,0 +1,151 @@
+"""TEBD on the GB300 engine, and a nearest-neighbour Trotter splitting.
+
+Public surface mirrors PyTreeNet's ``TEBD`` (``time_evolution/tebd.py:18-155``):
+``TEBD(initial_state, trotter_splitting, time_step_size, final_time, operators,
+svd_parameters=None, config=None)`` with ``exponents``, ``trotter_splitting``,
+``run_one_time_step()`` and ``run()``. Any object with
+``exponentiate_splitting(delta_time, ttn)`` returning operators that carry
+``.operator`` (legs: outputs, then inputs) and ``.node_identifiers`` can be
+passed as the splitting -- PyTreeNet's own ``TrotterSplitting`` included. The
+module's ``TrotterStep`` / ``TrotterSplitting`` cover one- and two-site terms
+on neighbouring nodes (``time_evolution/trotter.py:105-322``, without the SWAP
+bookkeeping that non-neighbouring terms need).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+import scipy.linalg
+import torch
+
+from .engine import CDT, DeviceNetwork
+from .tdvp import TTNTimeEvolutionConfig, TensorProduct
+from .truncation import SVDParameters
+
+
+@dataclass
+class NumericOperator:
+    """``operators/operator.py:18-60``: a matrix or tensor (outputs, then inputs)
+    and the node identifiers its legs act on, in the same order."""
+    operator: np.ndarray
+    node_identifiers: list
+
+
+class TrotterStep:
+    """``time_evolution/trotter.py:105-194``: a tensor product of one-site
+    operators and the factor of its exponent."""
+
+    def __init__(self, operator: TensorProduct | dict, factor: float):
+        self.operator = dict(operator)
+        self.factor = factor
+
+    def exponentiate_operator(self, delta_time: float) -> NumericOperator:
+        """exp(-i factor dt (A_1 x A_2 x ...)) with the factors in the tensor
+        product's order, reshaped to (out_1, ..., out_n, in_1, ..., in_n)."""
+        ids = list(self.operator)
+        mats = [np.asarray(self.operator[i], dtype=complex) for i in ids]
+        full = mats[0]
+        for m in mats[1:]:
+            full = np.kron(full, m)
+        u = scipy.linalg.expm(-1j * self.factor * delta_time * full)
+        dims = [m.shape[0] for m in mats]
+        return NumericOperator(u.reshape(dims + dims), ids)
+
+
+class TrotterSplitting(list):
+    """``time_evolution/trotter.py:196-322`` for neighbouring terms: the
+    exponentiated steps in order."""
+
+    def exponentiate_splitting(self, delta_time: float, ttn=None, dim=None) -> list:
+        out = []
+        for step in self:
+            ids = list(step.operator)
+            if len(ids) == 2 and ttn is not None:
+                a, b = ids
+                if ttn.nodes[a].parent != b and ttn.nodes[b].parent != a:
+                    raise NotImplementedError("two-site terms on non-neighbouring nodes need SWAP gates")
+            out.append(step.exponentiate_operator(delta_time))
+        return out
+
+
+class TEBD:
+    """``time_evolution/tebd.py:18-155``."""
+
+    def __init__(self, initial_state, trotter_splitting, time_step_size: float, final_time: float,
+                 operators, svd_parameters: SVDParameters | None = None,
+                 config: TTNTimeEvolutionConfig | None = None, precision: str = "plain"):
+        if time_step_size <= 0 or final_time <= 0:
+            raise ValueError("time step and final time must be positive")
+        self.config = config if config is not None else TTNTimeEvolutionConfig()
+        self._trotter_splitting = trotter_splitting
+        self.svd_parameters = svd_parameters if svd_parameters is not None else SVDParameters()
+        self.time_step_size = float(time_step_size)
+        self.final_time = float(final_time)
+        self.num_time_steps = int(np.ceil(final_time / time_step_size))
+        self.operators = operators if operators is not None else []
+        initial_state._finalise()
+        self.initial_state = initial_state
+        self.state = initial_state.copy_structure()
+        self.state.orthogonality_center_id = None
+        self._exponents = trotter_splitting.exponentiate_splitting(self.time_step_size, self.state)
+        self.net = DeviceNetwork(self.state, None, precision=precision)
+        self._dev_ops = [torch.from_numpy(np.ascontiguousarray(np.asarray(u.operator, dtype=np.complex128)))
+                         .to(self.net.device, CDT) for u in self._exponents]
+        self.results = None
+        self.times = []
+
+    @property
+    def exponents(self) -> list:
+        return self._exponents
+
+    @property
+    def trotter_splitting(self):
+        return self._trotter_splitting
+
+    def _apply_one_trotter_step(self, index: int):
+        """``_apply_one_trotter_step`` (``tebd.py:127-147``)."""
+        unitary = self._exponents[index]
+        ids = list(unitary.node_identifiers) if not isinstance(unitary.node_identifiers, str) \
+            else [unitary.node_identifiers]
+        if len(ids) == 0:
+            return
+        if len(ids) == 1:
+            self.net.apply_single_site_gate(ids[0], self._dev_ops[index])
+        elif len(ids) == 2:
+            self.net.apply_two_site_gate(ids[0], ids[1], self._dev_ops[index], self.svd_parameters)
+        else:
+            raise NotImplementedError("More than two-site interactions are not implemented.")
+
+    def run_one_time_step(self, **kwargs):
+        """Every exponentiated Trotter operator applied once (``tebd.py:149-155``)."""
+        for i in range(len(self._exponents)):
+            self._apply_one_trotter_step(i)
+
+    def evaluate_operator(self, operator) -> complex:
+        """``TTNTimeEvolution.evaluate_operator`` (``time_evolution/ttn_time_evolution.py:181-211``):
+        a TensorProduct of one-site operators, or a TTNO on the state's tree."""
+        from .ttn import TreeTensorNetworkOperator
+        if isinstance(operator, TreeTensorNetworkOperator):
+            return self.net.expect_ttno(operator)
+        return self.net.expect_local(dict(operator))
+
+    def evaluate_operators(self):
+        ops = self.operators
+        if isinstance(ops, dict) and not isinstance(ops, TensorProduct):
+            ops = list(ops.values())
+        elif isinstance(ops, TensorProduct):
+            ops = [ops]
+        return np.array([self.evaluate_operator(o) for o in ops])
+
+    def run(self, evaluation_time: int = 1, pgbar: bool = False):
+        """``TimeEvolution.run`` (``time_evolution/time_evolution.py:346-368``)."""
+        res = [self.evaluate_operators()]
+        self.times = [0.0]
+        for i in range(self.num_time_steps):
+            self.run_one_time_step()
+            if evaluation_time != "inf" and (i + 1) % evaluation_time == 0:
+                res.append(self.evaluate_operators())
+                self.times.append((i + 1) * self.time_step_size)
+        self.results = np.array(res)
+        return self.results

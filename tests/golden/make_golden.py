@@ -209,6 +209,7 @@ def run_case(ptn, name, spec, tensors, ham_fn, dt, steps, order, tol, canonical_
         algo.run_one_time_step()
         zs.append([algo.state.operator_expectation_value(ops[nid]) for nid, _ in spec])
     rec["z"] = np.array(zs)
+    rec["energy_final"] = algo.state.operator_expectation_value(H)
     for nid, t in export_state(algo.state, spec).items():
         rec[f"final/{nid}"] = t
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **rec)
@@ -266,6 +267,42 @@ def run_case_two_site(ptn, name, spec, tensors, ham_fn, dt, steps, tol, svd, can
         rec[f"final/{nid}"] = t
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **rec)
     print(name, "written; max bond", algo.state.max_bond_dim())
+
+
+def run_case_tebd(ptn, name, spec, tensors, dt, steps, svd, J=1.0, g=0.7):
+    """TEBD (``time_evolution/tebd.py``) with a first-order Trotter splitting of
+    H = -J sum Z Z - g sum X: every edge term and every field term is one
+    TrotterStep with factor 1, in the order: edges (spec order), then fields.
+    The exponentiated gates the reference applies are stored with the result."""
+    psi = build_reference_state(ptn, spec, tensors)
+    steps_ = [ptn.TrotterStep(ptn.TensorProduct({p: -J * Z, nid: Z}), 1.0) for nid, p in spec if p is not None]
+    steps_ += [ptn.TrotterStep(ptn.TensorProduct({nid: -g * X}), 1.0) for nid, _ in spec]
+    split = ptn.TrotterSplitting(steps_)
+    maxd, rel, tot, renorm = svd
+    params = ptn.SVDParameters(max_bond_dim=maxd, rel_tol=rel, total_tol=tot, renorm=renorm)
+    ops = {nid: ptn.TensorProduct({nid: Z}) for nid, _ in spec}
+    tebd = ptn.TEBD(psi, split, dt, dt * steps, ops, svd_parameters=params)
+    rec = {"spec_ids": np.array([s[0] for s in spec]),
+           "spec_parents": np.array(["" if s[1] is None else s[1] for s in spec]),
+           "dt": dt, "steps": steps, "order": 0, "krylov_tol": 0.0, "tebd": 1,
+           "svd_max_bond_dim": maxd, "svd_rel_tol": rel, "svd_total_tol": tot, "svd_renorm": int(renorm),
+           "update_path": np.array([s[0] for s in spec]), "n_gates": len(tebd.exponents)}
+    for i, u in enumerate(tebd.exponents):
+        rec[f"gate/{i}/op"] = np.asarray(u.operator)
+        rec[f"gate/{i}/ids"] = np.array(list(u.node_identifiers))
+    for nid, t in tensors.items():
+        rec[f"init/{nid}"] = t
+    for nid, _ in spec:
+        rec[f"ttno/{nid}"] = np.zeros(1)
+    zs = []
+    for step in range(steps):
+        tebd.run_one_time_step()
+        zs.append([tebd.state.operator_expectation_value(ops[nid]) for nid, _ in spec])
+    rec["z"] = np.array(zs)
+    for nid, t in export_state(tebd.state, spec).items():
+        rec[f"final/{nid}"] = t
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **rec)
+    print(name, "written; max bond", tebd.state.max_bond_dim())
 
 
 def svd_cases():
@@ -360,6 +397,10 @@ def main(ref_root):
     run_case_two_site(ptn, "binary7_heis_2tdvp_trunc", spec, random_state_tensors(spec, rng, 4),
                       lambda psi: heisenberg_fields(ptn, spec, h), 0.05, 3, 1e-12,
                       (3, 1e-10, 1e-10, True), canonical_random=True)
+    # TEBD on the 7-node binary tree (random chi=3 state, truncation to 4)
+    spec = binary_tree(7)
+    run_case_tebd(ptn, "binary7_tfim_tebd", spec, random_state_tensors(spec, rng, 3), 0.05, 4,
+                  (4, 1e-10, 1e-10, False))
     unit_cases(ptn)
 
 

@@ -23,8 +23,12 @@ def load_case(name):
         "krylov_tol": float(d["krylov_tol"]),
         "update_path": [str(x) for x in d["update_path"]],
         "two_site": bool(int(d["two_site"])) if "two_site" in d.files else False,
+        "energy_final": complex(d["energy_final"]) if "energy_final" in d.files else None,
     }
-    if case["two_site"]:
+    case["tebd"] = bool(int(d["tebd"])) if "tebd" in d.files else False
+    if case["tebd"]:
+        case["gates"] = [(d[f"gate/{i}/op"], [str(x) for x in d[f"gate/{i}/ids"]]) for i in range(int(d["n_gates"]))]
+    if case["two_site"] or case["tebd"]:
         case["svd"] = dict(max_bond_dim=int(d["svd_max_bond_dim"]), rel_tol=float(d["svd_rel_tol"]),
                            total_tol=float(d["svd_total_tol"]), renorm=bool(int(d["svd_renorm"])))
     return case
@@ -33,6 +37,7 @@ def load_case(name):
 CASES = ["c1_binary15_tfim_chi8", "binary7_tfim_chi4_o2", "ttree3_heis_chi6_o1",
          "ttree3_heis_chi6_o2", "ternary2_xxz_chi4_o1"]
 TWO_SITE_CASES = ["ternary2_xxz_neel_2tdvp", "binary7_heis_2tdvp_trunc"]
+TEBD_CASES = ["binary7_tfim_tebd"]
 
 
 def build_ttn(cls, spec, tensors):
@@ -69,3 +74,34 @@ def fidelity_and_dist(a_state, b_state):
     # ||a - e^{i phi} b||^2 / ||a||^2 with the optimal phase; guard the cancellation
     d2 = max(aa + bb - 2 * abs(ab), 0.0) / aa
     return 1 - f, np.sqrt(d2)
+
+
+class FixedSplitting:
+    """A Trotter splitting whose exponentiated operators are given (taken from
+    a fixture): what the reference's TrotterSplitting.exponentiate_splitting
+    returned for the recorded run."""
+
+    def __init__(self, gates):
+        from pytreenet_gb300 import NumericOperator
+        self._ops = [NumericOperator(op, ids) for op, ids in gates]
+
+    def exponentiate_splitting(self, delta_time, ttn=None, dim=None):
+        return list(self._ops)
+
+
+def run_tebd_case(name, steps=None):
+    """Run the engine's TEBD on a TEBD fixture; returns (case, oracle-state of the result, <Z> per step)."""
+    import numpy as np
+    import oracle as O
+    import pytreenet_gb300 as P
+    c = load_case(name)
+    st = build_ttn(P.TTNS, c["spec"], c["init"])
+    Zm = np.diag([1.0, -1.0]).astype(complex)
+    algo = P.TEBD(st, FixedSplitting(c["gates"]), c["dt"], c["dt"] * c["steps"], {},
+                  svd_parameters=P.SVDParameters(**c["svd"]))
+    zs = []
+    for _ in range(c["steps"] if steps is None else steps):
+        algo.run_one_time_step()
+        zs.append([algo.evaluate_operator({nid: Zm}) for nid, _ in c["spec"]])
+    out = {nid: algo.state.get_phys_numpy(nid) for nid, _ in c["spec"]}
+    return c, O.OState(oracle_state(c).tree, out), np.array(zs), algo

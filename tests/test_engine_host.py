@@ -241,3 +241,45 @@ def test_engine_host_qr_buffers_follow_bond_growth(monkeypatch):
     algo, ora, (one_minus_f, dist) = _two_site_vs_oracle(12, 5, steps=1)
     assert checked
     assert one_minus_f < 1e-12
+
+
+def test_engine_host_tebd_matches_reference(monkeypatch):
+    fake_ptn.install(monkeypatch)
+    from golden_util import TEBD_CASES, run_tebd_case
+    for name in TEBD_CASES:
+        c, got, zs, algo = run_tebd_case(name)
+        fin = oracle_state(c, "final")
+        for nid in fin.tensors:
+            assert fin.tensors[nid].shape == got.tensors[nid].shape
+        one_minus_f, _ = fidelity_and_dist(fin, got)
+        assert np.max(np.abs(zs - c["z"])) < 1e-13 * np.max(np.abs(c["z"]))
+        assert one_minus_f < 1e-13
+
+
+def test_engine_host_trotter_splitting_matches_fixture_gates(monkeypatch):
+    """The engine's own TrotterSplitting gives the gates the reference built."""
+    import pytreenet_gb300 as P
+    c = load_case("binary7_tfim_tebd")
+    Xm = np.array([[0, 1], [1, 0]], dtype=complex)
+    steps = [P.TrotterStep({p: -1.0 * Zm, nid: Zm}, 1.0) for nid, p in c["spec"] if p is not None]
+    steps += [P.TrotterStep({nid: -0.7 * Xm}, 1.0) for nid, _ in c["spec"]]
+    ops = P.TrotterSplitting(steps).exponentiate_splitting(c["dt"])
+    assert len(ops) == len(c["gates"])
+    for mine, (op, ids) in zip(ops, c["gates"]):
+        assert list(mine.node_identifiers) == ids
+        np.testing.assert_allclose(mine.operator, op, atol=1e-14)
+
+
+def test_engine_host_ttno_expectation(monkeypatch):
+    """<psi|H|psi> through a TDVP driver's evaluate_operator, against the
+    reference's value on the reference's final state."""
+    fake_ptn.install(monkeypatch)
+    import pytreenet_gb300 as P
+    for name in ["ttree3_heis_chi6_o1", "ternary2_xxz_chi4_o1"]:
+        c = load_case(name)
+        st = build_ttn(P.TTNS, c["spec"], c["final"])
+        H = build_ttn(P.TTNO, c["spec"], c["ttno"])
+        algo = P.FirstOrderOneSiteTDVP(st, H, c["dt"], c["dt"], {},
+                                       config=P.TDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV))
+        e = algo.evaluate_operator(H)
+        assert abs(e - c["energy_final"]) < 1e-11 * max(1.0, abs(c["energy_final"]))

@@ -178,3 +178,27 @@ def test_jacobi_svd_converges_on_many_small_matrices(n):
         assert code == 0, (n, trial)
         np.testing.assert_allclose(s, np.linalg.svd(A, compute_uv=False), rtol=0, atol=1e-13 * s[0])
         assert np.linalg.norm((U * s) @ V.conj().T - A) <= 1e-13 * np.linalg.norm(A)
+
+
+def test_gpu_tebd_matches_reference():
+    from golden_util import TEBD_CASES, run_tebd_case
+    for name in TEBD_CASES:
+        c, got, zs, algo = run_tebd_case(name)
+        fin = oracle_state(c, "final")
+        for nid in fin.tensors:
+            assert fin.tensors[nid].shape == got.tensors[nid].shape
+        one_minus_f, _ = fidelity_and_dist(fin, got)
+        assert np.max(np.abs(zs - c["z"])) < 1e-12 * np.max(np.abs(c["z"]))
+        assert one_minus_f < 1e-13
+
+
+def test_gpu_ttno_expectation():
+    import pytreenet_gb300 as P
+    for name in ["ttree3_heis_chi6_o1", "ternary2_xxz_chi4_o1", "c1_binary15_tfim_chi8"]:
+        c = load_case(name)
+        st = build_ttn(P.TTNS, c["spec"], c["final"])
+        H = build_ttn(P.TTNO, c["spec"], c["ttno"])
+        algo = P.FirstOrderOneSiteTDVP(st, H, c["dt"], c["dt"], {},
+                                       config=P.TDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV))
+        e = algo.evaluate_operator(H)
+        assert abs(e - c["energy_final"]) < 1e-11 * max(1.0, abs(c["energy_final"]))

@@ -125,3 +125,29 @@ def test_oracle_first_order_two_site_runs():
     z1 = np.array([O.expect_product(algo.state, {nid: Zm}) for nid, _ in c["spec"]])
     z2 = np.array([O.expect_product(algo2.state, {nid: Zm}) for nid, _ in c["spec"]])
     assert np.max(np.abs(z1 - z2)) < 5e-3
+
+
+def test_oracle_tebd_matches_reference():
+    from golden_util import TEBD_CASES
+    for name in TEBD_CASES:
+        c = load_case(name)
+        algo = O.TEBDOracle(oracle_state(c), c["gates"], O.SVDParams(**c["svd"]))
+        zerr = 0.0
+        for k in range(c["steps"]):
+            algo.run_one_time_step()
+            z = np.array([O.expect_product(algo.state, {nid: Zm}) for nid, _ in c["spec"]])
+            zerr = max(zerr, float(np.max(np.abs(z - c["z"][k]))))
+        fin = oracle_state(c, "final")
+        for nid in fin.tensors:
+            assert fin.tensors[nid].shape == algo.state.tensors[nid].shape
+        one_minus_f, dist = fidelity_and_dist(fin, algo.state)
+        # the state is not normalised (TEBD keeps the norm, here ~6e4): relative <Z> error
+        assert zerr < 1e-13 * np.max(np.abs(c["z"]))
+        assert one_minus_f < 1e-13
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_ttno_expectation_matches_reference(name):
+    c = load_case(name)
+    e = O.ttno_expectation(oracle_state(c, "final"), c["ttno"])
+    assert abs(e - c["energy_final"]) < 1e-12 * max(1.0, abs(c["energy_final"]))

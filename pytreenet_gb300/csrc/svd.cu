@@ -19,6 +19,7 @@
 #include <mutex>
 
 #include "ptn_common.cuh"
+#include "coop.cuh"
 
 namespace {
 
@@ -49,42 +50,11 @@ struct SvdArgs {
 __device__ __forceinline__ double2 ldcg2(const double2* p) { return __ldcg(p); }
 __device__ __forceinline__ void stcg2(double2* p, double2 v) { __stcg(p, v); }
 
-// Grid-wide barrier: ctrl[0] arrivals, ctrl[1] generation, ctrl[2] abort flag.
-// Returns false when the kernel must leave (timeout here or abort elsewhere).
+// Grid-wide barrier (coop.cuh); a timeout is also recorded in *status.
 __device__ bool grid_barrier(unsigned* ctrl, int32_t* status) {
-  __shared__ int s_ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    volatile unsigned* vgen = ctrl + 1;
-    volatile unsigned* vabort = ctrl + 2;
-    const unsigned g = *vgen;
-    __threadfence();
-    int ok = 1;
-    const unsigned arrived = atomicAdd(ctrl, 1u);
-    if (arrived == gridDim.x - 1) {
-      atomicExch(ctrl, 0u);
-      __threadfence();
-      atomicAdd(ctrl + 1, 1u);
-    } else {
-      const long long t0 = clock64();
-      while (*vgen == g) {
-        if (*vabort != 0u) {
-          ok = 0;
-          break;
-        }
-        if (clock64() - t0 > SVD_WAIT_CYCLES) {
-          atomicExch(ctrl + 2, 1u);
-          atomicCAS(status, 0, PTN_ERR_TIMEOUT);
-          ok = 0;
-          break;
-        }
-      }
-    }
-    __threadfence();
-    s_ok = ok;
-  }
-  __syncthreads();
-  return s_ok != 0;
+  const bool ok = ptn_grid_barrier(ctrl, SVD_WAIT_CYCLES);
+  if (!ok && threadIdx.x == 0 && *((volatile unsigned*)(ctrl + 2)) != 0u) atomicCAS(status, 0, PTN_ERR_TIMEOUT);
+  return ok;
 }
 
 // Rotate columns i and j of Aw (and of Vw) so that they become orthogonal.

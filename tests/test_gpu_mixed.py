@@ -131,15 +131,17 @@ def test_gpu_qr_graph_replay_matches_eager():
     from pytreenet_gb300.engine import DeviceNetwork
     outs = []
     for graphs in (False, True):
-        st, spec, tensors = t_tree_state(arm_len=3, chi=32, seed=6)
+        # the root split has 48 * 48 * 2 = 4608 rows: the multi-kernel path that graphs capture
+        st, spec, tensors = t_tree_state(arm_len=1, chi=48, seed=6)
         H, _ = t_tree_heisenberg(st, seed=7)
         net = DeviceNetwork(st, H, precision="plain")
         net.use_graphs = graphs
         rs = []
         for _ in range(3):     # eager, capture + replay, replay
-            x = net.t["a0_1"]
-            x.copy_(torch.from_numpy(tensors["a0_1"]).cuda())
-            rs.append((net.qr_split("a0_1", "a0_2").clone(), net.t["a0_1"].clone()))
+            x = net.t["root"]
+            x.copy_(torch.from_numpy(tensors["root"]).cuda())
+            rs.append((net.qr_split("root", "a0_0").clone(), net.t["root"].clone()))
         outs.append(rs)
     for (r0, q0), (r1, q1) in zip(outs[0], outs[1]):
         assert torch.equal(r0, r1) and torch.equal(q0, q1)
+    assert net.qr_graphs, "the multi-kernel split was not captured"

@@ -16,9 +16,6 @@
 // of ordinary launches (column norm, reflector, column dots, dot reduction,
 // trailing update); no kernel waits on another.
 #include "ptn_common.cuh"
-#include "coop.cuh"
-
-#include <mutex>
 
 namespace {
 
@@ -354,151 +351,6 @@ __global__ void __launch_bounds__(ST) hh_form_small(double2* __restrict__ A, con
   }
 }
 
-// ---- small-m path in one cooperative launch ---------------------------------------------
-// The same steps as hh_fact_small / extract_r_small / hh_form_small with the
-// same arithmetic (so the same Q and R bit for bit), but all reflectors run
-// inside one kernel: CTA b owns the trailing columns c = j+1+b, j+1+b+G, ...
-// and a grid barrier separates consecutive steps. Data written by another CTA
-// is read through L2 (__ldcg). A barrier that times out aborts every CTA and
-// leaves NaN in R[0], which the caller's finiteness checks turn into an error.
-constexpr long long QR_WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
-
-struct QrCoopArgs {
-  double2* A;
-  const int64_t* rowoff;
-  int64_t cs, m, k, p;
-  double2* tau;
-  double2* betas;
-  double2* V;
-  double2* R;
-  unsigned* ctrl;
-};
-
-__device__ __forceinline__ void qr_coop_abort(const QrCoopArgs& a) {
-  if (threadIdx.x == 0) a.R[0] = make_double2(__longlong_as_double(0x7ff8000000000000LL), 0.0);
-}
-
-__global__ void __launch_bounds__(ST) zqr_coop_kernel(QrCoopArgs a) {
-  __shared__ double2 vs[QR_SMALL_M];
-  __shared__ double red[ST / 32 + 1];
-  __shared__ double2 sc[2];
-  const int64_t m = a.m, k = a.k, p = a.p, cs = a.cs;
-  const int64_t G = gridDim.x;
-  for (int64_t j = 0; j < p; ++j) {
-    const int64_t len = m - j;
-    double acc = 0.0;
-    for (int64_t t = threadIdx.x; t < len; t += ST) {
-      const double2 x = __ldcg(a.A + a.rowoff[j + t] + j * cs);
-      vs[t] = x;
-      if (t > 0) acc += cabs2(x);
-    }
-    const double xn2 = block_sum(acc, red);
-    if (threadIdx.x == 0) {
-      const double2 alpha = vs[0];
-      const double xnorm = sqrt(xn2);
-      double2 t_, s_, b_;
-      if (xnorm == 0.0 && alpha.y == 0.0) {
-        t_ = make_double2(0.0, 0.0);
-        s_ = make_double2(0.0, 0.0);
-        b_ = alpha;
-      } else {
-        const double nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xnorm * xnorm);
-        const double beta = (alpha.x >= 0.0) ? -nrm : nrm;
-        t_ = make_double2((beta - alpha.x) / beta, -alpha.y / beta);
-        const double2 d = make_double2(alpha.x - beta, alpha.y);
-        const double den = d.x * d.x + d.y * d.y;
-        s_ = make_double2(d.x / den, -d.y / den);
-        b_ = make_double2(beta, 0.0);
-      }
-      sc[0] = t_;
-      sc[1] = s_;
-      if (blockIdx.x == 0) {
-        __stcg(a.tau + j, t_);
-        __stcg(a.betas + j, b_);
-      }
-    }
-    __syncthreads();
-    const double2 s_ = sc[1];
-    for (int64_t t = threadIdx.x; t < len; t += ST) {
-      const double2 v = (t == 0) ? make_double2(1.0, 0.0) : cmul(vs[t], s_);
-      vs[t] = v;
-      if (blockIdx.x == 0) __stcg(a.V + j * m + j + t, v);
-    }
-    __syncthreads();
-    double2 f = sc[0];
-    f.y = -f.y;  // conj(tau): the factorisation applies H^H
-    for (int64_t c = j + 1 + blockIdx.x; c < k; c += G) {
-      double2 w = make_double2(0.0, 0.0);
-      for (int64_t t = threadIdx.x; t < len; t += ST) w = cfmac(vs[t], __ldcg(a.A + a.rowoff[j + t] + c * cs), w);
-      w = block_sum2(w, red);
-      const double2 fw = cmul(f, w);
-      for (int64_t t = threadIdx.x; t < len; t += ST) {
-        double2* q = a.A + a.rowoff[j + t] + c * cs;
-        __stcg(q, csub(__ldcg(q), cmul(vs[t], fw)));
-      }
-    }
-    if (!ptn_grid_barrier(a.ctrl, QR_WAIT_CYCLES)) {
-      qr_coop_abort(a);
-      return;
-    }
-  }
-  // R[r][c]: strictly-upper part from A, diagonal from betas (rows < p), zero elsewhere.
-  for (int64_t e = blockIdx.x * (int64_t)ST + threadIdx.x; e < k * k; e += G * ST) {
-    const int64_t r = e / k, c = e - r * k;
-    double2 v = make_double2(0.0, 0.0);
-    if (r < p) {
-      if (c == r) v = __ldcg(a.betas + r);
-      else if (c > r) v = __ldcg(a.A + a.rowoff[r] + c * cs);
-    }
-    a.R[e] = v;
-  }
-  if (!ptn_grid_barrier(a.ctrl, QR_WAIT_CYCLES)) {
-    qr_coop_abort(a);
-    return;
-  }
-  // Q (zung2r): step j applies H_j to columns j+1..p-1 and writes column j.
-  for (int64_t j = p - 1; j >= 0; --j) {
-    const int64_t ncols = p - (j + 1);
-    const double2 t_ = __ldcg(a.tau + j);
-    const double2* v = a.V + j * m;
-    for (int64_t it = blockIdx.x; it <= ncols; it += G) {
-      if (it == ncols) {
-        for (int64_t i = threadIdx.x; i < m; i += ST) {
-          double2* q = a.A + a.rowoff[i] + j * cs;
-          double2 val;
-          if (i < j) val = make_double2(0.0, 0.0);
-          else if (i == j) val = make_double2(1.0 - t_.x, -t_.y);
-          else {
-            const double2 vi = __ldcg(v + i);
-            val = make_double2(-(t_.x * vi.x - t_.y * vi.y), -(t_.x * vi.y + t_.y * vi.x));
-          }
-          __stcg(q, val);
-        }
-      } else {
-        const int64_t c = j + 1 + it;
-        double2 w = make_double2(0.0, 0.0);
-        for (int64_t i = j + threadIdx.x; i < m; i += ST) w = cfmac(__ldcg(v + i), __ldcg(a.A + a.rowoff[i] + c * cs), w);
-        w = block_sum2(w, red);
-        const double2 fw = cmul(t_, w);
-        for (int64_t i = j + threadIdx.x; i < m; i += ST) {
-          double2* q = a.A + a.rowoff[i] + c * cs;
-          __stcg(q, csub(__ldcg(q), cmul(__ldcg(v + i), fw)));
-        }
-      }
-    }
-    if (!ptn_grid_barrier(a.ctrl, QR_WAIT_CYCLES)) {
-      qr_coop_abort(a);
-      return;
-    }
-  }
-  // KEEP padding: zero the columns p..k-1 of Q.
-  const int64_t nc = k - p;
-  for (int64_t e = blockIdx.x * (int64_t)ST + threadIdx.x; e < m * nc; e += G * ST) {
-    const int64_t i = e / nc, c = p + (e - (e / nc) * nc);
-    a.A[a.rowoff[i] + c * cs] = make_double2(0.0, 0.0);
-  }
-}
-
 inline unsigned grid1(int64_t n) {
   int64_t b = (n + QT - 1) / QT;
   if (b < 1) b = 1;
@@ -516,56 +368,12 @@ extern "C" int64_t ptn_zqr_work_bytes(int64_t m, int64_t k) {
   return 16 * (3 * k + (nrb_for(m) + 1) / 2 + 1 + nrb_for(m) * k) + 256;
 }
 
-static int coop_max_blocks() {
-  static int cached[64] = {0};
-  static std::mutex mu;
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
-  std::lock_guard<std::mutex> lock(mu);
-  if (cached[dev] == 0) {
-    int per_sm = 0, sms = 0, coop = 0;
-    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, zqr_coop_kernel, ST, 0) != cudaSuccess) return 0;
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
-    cached[dev] = per_sm * sms;
-  }
-  return cached[dev];
-}
-
 static int zqr_keep_small(double2* A, const int64_t* rowoff, int64_t m, int64_t k, int64_t cs, double2* R,
                           void* work, cudaStream_t s) {
   double2* tau = static_cast<double2*>(work);
   double2* betas = tau + k;
   double2* V = betas + k;
   const int64_t p = m < k ? m : k;
-  // One cooperative launch for all steps (256 control bytes after V).
-  const int maxb = coop_max_blocks();
-  if (maxb > 0) {
-    QrCoopArgs a;
-    a.A = A;
-    a.rowoff = rowoff;
-    a.cs = cs;
-    a.m = m;
-    a.k = k;
-    a.p = p;
-    a.tau = tau;
-    a.betas = betas;
-    a.V = V;
-    a.R = R;
-    a.ctrl = reinterpret_cast<unsigned*>(V + m * p);
-    if (cudaMemsetAsync(a.ctrl, 0, 256, s) != cudaSuccess) return PTN_ERR_LAUNCH;
-    int64_t grid = k > 1 ? k - 1 : 1;
-    if (grid > 152) grid = 152;
-    if (grid > maxb) grid = maxb;
-    void* args[] = {&a};
-    PTN_COUNT(1);
-    if (cudaLaunchCooperativeKernel((const void*)zqr_coop_kernel, dim3((unsigned)grid), dim3(ST), args, 0, s) !=
-        cudaSuccess) {
-      cudaGetLastError();
-      return PTN_ERR_LAUNCH;
-    }
-    return PTN_OK;
-  }
   for (int64_t j = 0; j < p; ++j) {
     const int64_t ncols = k - (j + 1);
     PTN_COUNT(1);

@@ -738,7 +738,6 @@ class DeviceNetwork:
 
     # -- QR split and R absorption ---------------------------------------------------
     CHOLQR_MIN_ROWS = 8192
-    QR_ONE_LAUNCH_ROWS = 2048
 
     def _cholqr2(self, nid, row_axes, col_axis) -> torch.Tensor | None:
         """Mixed path, tall full-rank matrices: CholeskyQR2 with the Gram matrices
@@ -840,9 +839,7 @@ class DeviceNetwork:
             check(lib.ptn_zqr_keep(self.t[nid].data_ptr(), rowoff.data_ptr(), m, k, strides[col_axis],
                                    R.data_ptr(), work.data_ptr(), _stream_ptr()), "ptn_zqr_keep")
         gkey = (nid, nbr, key)
-        # splits of up to QR_ONE_LAUNCH_ROWS rows are a single cooperative launch
-        # in the library; graphs only pay for the multi-kernel path above that
-        if not self.use_graphs or self.device.type != "cuda" or m <= self.QR_ONE_LAUNCH_ROWS:
+        if not self.use_graphs or self.device.type != "cuda":
             launch()
         elif gkey in self.qr_graphs:
             g, nlaunch = self.qr_graphs[gkey]

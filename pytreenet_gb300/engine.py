@@ -411,16 +411,35 @@ class KrylovSolver:
     diagonalised on the host after each step.
     """
 
+    # Krylov solves on vectors up to this length run speculative batches (the
+    # matvec is cheap there, so a host round trip per step would dominate).
+    SPECULATE_MAX_N = 1 << 21
+
     def __init__(self, ws: Workspace):
         self.ws = ws
         self.depths: list[int] = []
         self._host = None
+        self._spec_depth: dict[int, int] = {}
+        self._qcap = 0
 
-    def _pinned(self, n):
-        if self._host is None or self._host[0].numel() < n:
+    def _ensure_Q(self, x, n, cap):
+        """Krylov basis of ``cap`` rows of length n (existing rows kept)."""
+        cur = self.ws.bufs.get("kry_Q")
+        if cur is not None and cur.numel() >= cap * n:
+            self._qcap = cur.numel() // n
+            return
+        Qn = torch.empty((cap * n,), dtype=CDT, device=x.device)
+        if cur is not None and self._qcap > 0:
+            keep = min(cur.numel(), cap * n, self._qcap * n)
+            Qn[:keep].copy_(cur[:keep])
+        self.ws.bufs["kry_Q"] = Qn
+        self._qcap = cap
+
+    def _pinned(self, n, ns=2):
+        if self._host is None or self._host[0].numel() < n or self._host[1].numel() < ns:
             pin = self.ws.device.type == "cuda"
             self._host = (torch.empty(max(n, 64), dtype=CDT, pin_memory=pin),
-                          torch.empty(2, dtype=torch.float64, pin_memory=pin),
+                          torch.empty(max(ns, 64), dtype=torch.float64, pin_memory=pin),
                           torch.zeros(1, dtype=torch.int32, pin_memory=pin))
         return self._host
 
@@ -446,65 +465,87 @@ class KrylovSolver:
             return out
         max_steps = n if max_krylov_dim is None else min(n, int(max_krylov_dim))
         floor_abs = np.finfo(float).eps * max(n, 1)
-        cap = min(max_steps + 1, 8)
-        Q = self.ws.get("kry_Q", cap * n).view(cap, n)
+        T = np.zeros((min(max_steps, 64) + 1,) * 2, dtype=complex)
+        # Speculation: for vectors up to SPECULATE_MAX_N the steps of a batch are
+        # enqueued back to back and the host reads their coefficients once per
+        # batch (the first batch as deep as the last solve of this size). The
+        # decisions below are the same, taken on the same numbers, so the result
+        # equals the one-step-at-a-time loop; vectors computed past the stop are
+        # discarded.
+        spec = self._spec_depth.get(n, 4) if n <= self.SPECULATE_MAX_N else 1
+        self._ensure_Q(x, n, min(max_steps + 1, max(spec + 1, 8)))
+        Q = self.ws.bufs["kry_Q"][:self._qcap * n].view(self._qcap, n)
         w = self.ws.get("kry_w", n)
         check(lib.ptn_zscal_inv(x.data_ptr(), scal.data_ptr(), Q[0].data_ptr(), n, stream), "zscal")
-        T = np.zeros((min(max_steps, 64) + 1,) * 2, dtype=complex)
         m = 0
-        for j in range(max_steps):
-            if j + 2 > T.shape[0]:
-                T2 = np.zeros((2 * T.shape[0],) * 2, dtype=complex)
-                T2[:T.shape[0], :T.shape[0]] = T
-                T = T2
-            apply(Q[j].data_ptr(), w.data_ptr())
-            nq = j + 1
-            hbuf = self.ws.get("kry_h", 2 * nq + 8)
-            check(lib.ptn_dznrm2(w.data_ptr(), n, scal.data_ptr(), part.data_ptr(), stream), "dznrm2")
-            h1 = hbuf[0:nq]
-            h2 = hbuf[nq:2 * nq]
-            for h in (h1, h2):
-                check(lib.ptn_zdot_multi(Q.data_ptr(), n, nq, w.data_ptr(), n, h.data_ptr(), 0,
-                                         part.data_ptr(), stream), "zdot_multi")
-                check(lib.ptn_zaxpy_multi(Q.data_ptr(), n, nq, h.data_ptr(), w.data_ptr(), n, stream),
-                      "zaxpy_multi")
-            check(lib.ptn_dznrm2(w.data_ptr(), n, scal[1:].data_ptr(), part.data_ptr(), stream), "dznrm2")
-            # one synchronisation per step: projections, norms and the status
+        j = 0
+        done = False
+        while not done and j < max_steps:
+            batch = max(1, min(spec - j, max_steps - j)) if j < spec else 1
+            if j + batch + 1 > self._qcap:
+                self._ensure_Q(x, n, min(max_steps + 1, max(2 * self._qcap, j + batch + 1)))
+                Q = self.ws.bufs["kry_Q"][:self._qcap * n].view(self._qcap, n)
+            hs = self.ws.get("kry_hs", (j + batch) * 2 * (j + batch) + 8)
+            sc = self.ws.get("kry_sc", 2 * (j + batch) + 8, torch.float64)
+            for jj in range(j, j + batch):
+                apply(Q[jj].data_ptr(), w.data_ptr())
+                nq = jj + 1
+                base = hs[jj * 2 * (j + batch):]
+                check(lib.ptn_dznrm2(w.data_ptr(), n, sc[2 * jj:].data_ptr(), part.data_ptr(), stream), "dznrm2")
+                for h in (base[0:nq], base[nq:2 * nq]):
+                    check(lib.ptn_zdot_multi(Q.data_ptr(), n, nq, w.data_ptr(), n, h.data_ptr(), 0,
+                                             part.data_ptr(), stream), "zdot_multi")
+                    check(lib.ptn_zaxpy_multi(Q.data_ptr(), n, nq, h.data_ptr(), w.data_ptr(), n, stream),
+                          "zaxpy_multi")
+                check(lib.ptn_dznrm2(w.data_ptr(), n, sc[2 * jj + 1:].data_ptr(), part.data_ptr(), stream),
+                      "dznrm2")
+                if jj + 1 < self._qcap:
+                    check(lib.ptn_zscal_inv(w.data_ptr(), sc[2 * jj + 1:].data_ptr(), Q[jj + 1].data_ptr(), n,
+                                            stream), "zscal")
+            # one synchronisation per batch: coefficients, norms and the status
             # word go to pinned host memory asynchronously, then the stream syncs
-            hh_host, sc_host, st_host = self._pinned(2 * nq)
-            hh_host[:2 * nq].copy_(hbuf[:2 * nq], non_blocking=True)
-            sc_host.copy_(scal[:2], non_blocking=True)
+            nh = (j + batch) * 2 * (j + batch)
+            hh_host, sc_host, st_host = self._pinned(nh, 2 * (j + batch))
+            hh_host[:nh].copy_(hs[:nh], non_blocking=True)
+            sc_host[:2 * (j + batch)].copy_(sc[:2 * (j + batch)], non_blocking=True)
             st = self.ws.bufs.get("tc_status")
             if st is not None:
                 st_host.copy_(st[:1], non_blocking=True)
             if self.ws.device.type == "cuda":
                 torch.cuda.current_stream().synchronize()
-            hh = hh_host[:2 * nq].numpy()
-            sc = sc_host.numpy()
             if st is not None and int(st_host[0]) != 0:
                 code = int(st_host[0])
                 st.zero_()
                 raise _lib.PtnError(code, "tensor-core contraction inside the Krylov exponential")
-            w0, beta = float(sc[0]), float(sc[1])
-            T[:nq, j] = hh[:nq] + hh[nq:]
-            T[j + 1, j] = beta
-            m = j + 1
-            if not np.isfinite(beta):
-                raise _lib.PtnError(3, "Krylov exponential: non-finite vector")
-            if beta <= max(floor_abs, 1e-12 * w0):
-                break
-            if krylov_tol > 0.0:
-                col = small_propagator(self._proj(T, m, tridiagonal), dt, exp_factor, hermitian)
-                if beta0 * beta * abs(col[m - 1]) < krylov_tol:
+            hh_all = hh_host[:nh].numpy()
+            sc_all = sc_host[:2 * (j + batch)].numpy()
+            for jj in range(j, j + batch):
+                if jj + 2 > T.shape[0]:
+                    T2 = np.zeros((2 * T.shape[0],) * 2, dtype=complex)
+                    T2[:T.shape[0], :T.shape[0]] = T
+                    T = T2
+                nq = jj + 1
+                hh = hh_all[jj * 2 * (j + batch):jj * 2 * (j + batch) + 2 * nq]
+                w0, beta = float(sc_all[2 * jj]), float(sc_all[2 * jj + 1])
+                T[:nq, jj] = hh[:nq] + hh[nq:]
+                T[jj + 1, jj] = beta
+                m = jj + 1
+                if not np.isfinite(beta):
+                    raise _lib.PtnError(3, "Krylov exponential: non-finite vector")
+                if beta <= max(floor_abs, 1e-12 * w0):
+                    done = True
                     break
-            if j + 1 >= Q.shape[0]:
-                newcap = min(max_steps + 1, 2 * Q.shape[0])
-                Qn = torch.empty((newcap, n), dtype=CDT, device=x.device)
-                Qn[:Q.shape[0]].copy_(Q)
-                self.ws.bufs["kry_Q"] = Qn.view(-1)
-                Q = Qn
-            check(lib.ptn_zscal_inv(w.data_ptr(), scal[1:].data_ptr(), Q[j + 1].data_ptr(), n, stream),
-                  "zscal")
+                if krylov_tol > 0.0:
+                    col = small_propagator(self._proj(T, m, tridiagonal), dt, exp_factor, hermitian)
+                    if beta0 * beta * abs(col[m - 1]) < krylov_tol:
+                        done = True
+                        break
+                if jj + 1 >= self._qcap:
+                    done = True       # basis capacity reached (only with max_krylov_dim = capacity)
+                    break
+            j += batch
+        if n <= self.SPECULATE_MAX_N:
+            self._spec_depth[n] = m
         self.depths.append(m)
         c = beta0 * small_propagator(self._proj(T, m, tridiagonal), dt, exp_factor, hermitian)
         cdev = self.ws.get("kry_h", m + 8)[:m]

@@ -227,6 +227,29 @@ typedef struct {
 
 int ptn_zpermute(const ptn_permute_desc* d, void* stream);
 
+/* ---- Native executor ----------------------------------------------------------
+ * A contraction chain (one matvec, one environment update) as a list of the
+ * descriptors above whose operand pointers are filled in at run time from
+ * ptrs[]: op.a / op.b / op.c index the table for A / B (Bx) / C of a
+ * contraction or GEMM, and src (a) / dst (c) of a conversion (b = -1 when
+ * unused). The descriptors stay in host memory and are copied, so one plan can
+ * run with different vectors. Replaces the Python loop over np.tensordot calls
+ * of contract_ket_ham_with_envs / contract_any
+ * (contractions/state_operator_contraction.py:227-273, 407-694) with one call. */
+enum { PTN_OP_ZCONTRACT = 0, PTN_OP_CGEMM = 1, PTN_OP_TO_PLANES = 2, PTN_OP_EXPAND_B = 3 };
+typedef struct {
+  int32_t kind;
+  int32_t a, b, c;
+  const void* desc;
+} ptn_exec_op;
+int ptn_exec_ops(const ptn_exec_op* ops, int32_t nops, void* const* ptrs, int32_t nptrs, void* stream);
+
+/* One Gram-Schmidt step of krylov_exp_action (time_evolution/time_evolution.py:775-798):
+ * norms[0] = |w|, two passes h = Q^H w, w -= Q h (coefficients in h[0:nq] and
+ * h[nq:2nq]), norms[1] = |w|, and qnext = w / norms[1] when qnext is not null. */
+int ptn_krylov_gs_step(const void* Q, int64_t ldq, int32_t nq, void* w, int64_t n, void* h,
+                       void* partial, double* norms, void* qnext, void* stream);
+
 unsigned long long ptn_launch_counter(void);
 
 /* Scan a complex128 buffer for NaN/Inf; flag (device int32) is set to 1 if found. */

@@ -81,6 +81,13 @@ class PermuteDesc(ctypes.Structure):
                 ("scale", ctypes.c_void_p), ("scale_mode", ctypes.c_int32), ("pad_", ctypes.c_int32)]
 
 
+class ExecOp(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("a", ctypes.c_int32), ("b", ctypes.c_int32),
+                ("c", ctypes.c_int32), ("desc", ctypes.c_void_p)]
+
+
+OP_ZCONTRACT, OP_CGEMM, OP_TO_PLANES, OP_EXPAND_B = 0, 1, 2, 3
+
 _P = ctypes.c_void_p
 _I64 = ctypes.c_int64
 _I32 = ctypes.c_int32
@@ -107,6 +114,8 @@ SIGNATURES = {
     "ptn_zsvd_work_bytes": (_I64, [_I64, _I64]),
     "ptn_zsvd_jacobi": (ctypes.c_int, [ctypes.POINTER(SvdDesc), _P]),
     "ptn_zpermute": (ctypes.c_int, [ctypes.POINTER(PermuteDesc), _P]),
+    "ptn_exec_ops": (ctypes.c_int, [ctypes.POINTER(ExecOp), _I32, ctypes.POINTER(ctypes.c_void_p), _I32, _P]),
+    "ptn_krylov_gs_step": (ctypes.c_int, [_P, _I64, _I32, _P, _I64, _P, _P, _P, _P, _P]),
 }
 
 _lib = None

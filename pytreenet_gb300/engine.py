@@ -147,6 +147,48 @@ class Step:
             int(np.prod(col(B, nlab, "dims") or [1])) * int(np.prod(col(A, klabels, "dims") or [1]))
 
 
+class _NativeOps:
+    """A fixed list of descriptors run by ``ptn_exec_ops`` in one foreign call.
+    Operand references become indices into a pointer table filled per run:
+    0 = the input vector, 1 = the output, then each distinct fixed tensor or
+    workspace slot."""
+
+    def __init__(self, items):
+        slots: dict = {}
+        self.refs = [("in",), ("out",)]
+
+        def slot(ref):
+            if ref is None:
+                return -1
+            kind = ref[0]
+            if kind == "in":
+                return 0
+            if kind == "out":
+                return 1
+            key = (kind, id(ref[1])) if kind == "fixed" else (kind, ref[1])
+            if key not in slots:
+                slots[key] = len(self.refs)
+                self.refs.append(ref)
+            return slots[key]
+        self.descs = [d for _, d, _ in items]
+        self.ops = (_lib.ExecOp * max(len(items), 1))()
+        for i, (kind, d, refs) in enumerate(items):
+            a, b, c = refs
+            self.ops[i].kind = kind
+            self.ops[i].a, self.ops[i].b, self.ops[i].c = slot(a), slot(b), slot(c)
+            self.ops[i].desc = ctypes.addressof(d)
+        self.n = len(items)
+        self.ptrs = (ctypes.c_void_p * len(self.refs))()
+
+    def run(self, ws, x_ptr, y_ptr):
+        p = self.ptrs
+        p[0], p[1] = x_ptr or None, y_ptr or None
+        for i in range(2, len(self.refs)):
+            ref = self.refs[i]
+            p[i] = ref[1].data_ptr() if ref[0] == "fixed" else ws.ptr(ref[1])
+        check(_lib.load().ptn_exec_ops(self.ops, self.n, p, len(self.refs), _stream_ptr()), "ptn_exec_ops")
+
+
 class Plan:
     """A sequence of contraction steps with one dynamic input and output."""
 
@@ -157,24 +199,11 @@ class Plan:
         self.flops = sum(s.flops for s in steps)
 
     def run(self, x_ptr: int = 0, y_ptr: int = 0):
-        lib = _lib.load()
         for name, n in self.ws_sizes.items():
             self.ws.get(name, n)
-        stream = _stream_ptr()
-        for st in self.steps:
-            ptrs = []
-            for ref in st.refs:
-                kind = ref[0]
-                if kind == "fixed":
-                    ptrs.append(ref[1].data_ptr())
-                elif kind == "in":
-                    ptrs.append(x_ptr)
-                elif kind == "out":
-                    ptrs.append(y_ptr)
-                else:
-                    ptrs.append(self.ws.ptr(ref[1]))
-            st.desc.A, st.desc.B, st.desc.C = ptrs
-            check(lib.ptn_zcontract(ctypes.byref(st.desc), stream), "ptn_zcontract")
+        if not hasattr(self, "_exec"):
+            self._exec = _NativeOps([(_lib.OP_ZCONTRACT, st.desc, st.refs) for st in self.steps])
+        self._exec.run(self.ws, x_ptr, y_ptr)
 
 
 class ChainBuilder:
@@ -344,35 +373,24 @@ class MixedPlan:
         self.sizes[name] = max(self.sizes.get(name, 0), numel)
 
     def run(self, x_ptr: int = 0, y_ptr: int = 0):
-        lib = _lib.load()
         for name, n in self.sizes.items():
             self.ws.get(name, n + 64, torch.bfloat16)
         status = self.ws.bufs.get("tc_status")
         if status is None:
             status = torch.zeros(1, dtype=torch.int32, device=self.ws.device)
             self.ws.bufs["tc_status"] = status
-        stream = _stream_ptr()
-
-        def ptr(ref):
-            kind = ref[0]
-            if kind == "fixed":
-                return ref[1].data_ptr()
-            if kind == "in":
-                return x_ptr
-            if kind == "out":
-                return y_ptr
-            return self.ws.ptr(ref[1])
-        for kind, d, refs in self.ops:
-            if kind == "conv":
-                d.src, d.dst = ptr(refs[0]), ptr(refs[1])
-                check(lib.ptn_to_planes(ctypes.byref(d), stream), "ptn_to_planes")
-            elif kind == "expand":
-                d.src, d.dst = ptr(refs[0]), ptr(refs[1])
-                check(lib.ptn_expand_b(ctypes.byref(d), stream), "ptn_expand_b")
-            else:
-                d.A, d.Bx, d.C = ptr(refs[0]), ptr(refs[1]), ptr(refs[2])
-                d.status = status.data_ptr()
-                check(lib.ptn_cgemm_bf16x3(ctypes.byref(d), stream), "ptn_cgemm_bf16x3")
+        if not hasattr(self, "_exec"):
+            items = []
+            for kind, d, refs in self.ops:
+                if kind == "conv":
+                    items.append((_lib.OP_TO_PLANES, d, (refs[0], None, refs[1])))
+                elif kind == "expand":
+                    items.append((_lib.OP_EXPAND_B, d, (refs[0], None, refs[1])))
+                else:
+                    d.status = status.data_ptr()
+                    items.append((_lib.OP_CGEMM, d, tuple(refs)))
+            self._exec = _NativeOps(items)
+        self._exec.run(self.ws, x_ptr, y_ptr)
 
 
 # ----------------------------------------------------------------------------
@@ -491,17 +509,10 @@ class KrylovSolver:
                 apply(Q[jj].data_ptr(), w.data_ptr())
                 nq = jj + 1
                 base = hs[jj * 2 * (j + batch):]
-                check(lib.ptn_dznrm2(w.data_ptr(), n, sc[2 * jj:].data_ptr(), part.data_ptr(), stream), "dznrm2")
-                for h in (base[0:nq], base[nq:2 * nq]):
-                    check(lib.ptn_zdot_multi(Q.data_ptr(), n, nq, w.data_ptr(), n, h.data_ptr(), 0,
-                                             part.data_ptr(), stream), "zdot_multi")
-                    check(lib.ptn_zaxpy_multi(Q.data_ptr(), n, nq, h.data_ptr(), w.data_ptr(), n, stream),
-                          "zaxpy_multi")
-                check(lib.ptn_dznrm2(w.data_ptr(), n, sc[2 * jj + 1:].data_ptr(), part.data_ptr(), stream),
-                      "dznrm2")
-                if jj + 1 < self._qcap:
-                    check(lib.ptn_zscal_inv(w.data_ptr(), sc[2 * jj + 1:].data_ptr(), Q[jj + 1].data_ptr(), n,
-                                            stream), "zscal")
+                qnext = Q[jj + 1].data_ptr() if jj + 1 < self._qcap else None
+                # |w|, two Gram-Schmidt passes, |w|, next basis vector: one foreign call
+                check(lib.ptn_krylov_gs_step(Q.data_ptr(), n, nq, w.data_ptr(), n, base.data_ptr(), part.data_ptr(),
+                                             sc[2 * jj:].data_ptr(), qnext, stream), "krylov_gs_step")
             # one synchronisation per batch: coefficients, norms and the status
             # word go to pinned host memory asynchronously, then the stream syncs
             nh = (j + batch) * 2 * (j + batch)

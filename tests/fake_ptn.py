@@ -280,3 +280,42 @@ def _fake_permute(self, d_ref, stream):
 FakeLib.ptn_zsvd_work_bytes = _fake_svd_work_bytes
 FakeLib.ptn_zsvd_jacobi = _fake_svd
 FakeLib.ptn_zpermute = _fake_permute
+
+
+# ---- native executor -------------------------------------------------------------
+def _fake_exec_ops(self, ops, nops, ptrs, nptrs, stream):
+    import pytreenet_gb300._lib as L
+    for i in range(nops):
+        op = ops[i]
+        if op.kind == L.OP_ZCONTRACT:
+            d = L.ContractDesc.from_buffer_copy(ctypes.cast(op.desc, ctypes.POINTER(L.ContractDesc)).contents)
+            d.A, d.B, d.C = ptrs[op.a], (ptrs[op.b] if op.b >= 0 else None), ptrs[op.c]
+            self.ptn_zcontract(ctypes.byref(d), stream)
+        elif op.kind == L.OP_CGEMM:
+            d = L.CgemmDesc.from_buffer_copy(ctypes.cast(op.desc, ctypes.POINTER(L.CgemmDesc)).contents)
+            d.A, d.Bx, d.C = ptrs[op.a], (ptrs[op.b] if op.b >= 0 else None), ptrs[op.c]
+            self.ptn_cgemm_bf16x3(ctypes.byref(d), stream)
+        else:
+            d = L.ConvertDesc.from_buffer_copy(ctypes.cast(op.desc, ctypes.POINTER(L.ConvertDesc)).contents)
+            d.src, d.dst = ptrs[op.a], ptrs[op.c]
+            if op.kind == L.OP_TO_PLANES:
+                self.ptn_to_planes(ctypes.byref(d), stream)
+            else:
+                self.ptn_expand_b(ctypes.byref(d), stream)
+    return 0
+
+
+def _fake_gs_step(self, Q, ldq, nq, w, n, h, part, norms, qnext, stream):
+    self.ptn_dznrm2(w, n, norms, part, stream)
+    for off in (0, nq):
+        hp = int(h) + 16 * off
+        self.ptn_zdot_multi(Q, ldq, nq, w, n, hp, 0, part, stream)
+        self.ptn_zaxpy_multi(Q, ldq, nq, hp, w, n, stream)
+    self.ptn_dznrm2(w, n, int(norms) + 8, part, stream)
+    if qnext:
+        self.ptn_zscal_inv(w, int(norms) + 8, qnext, n, stream)
+    return 0
+
+
+FakeLib.ptn_exec_ops = _fake_exec_ops
+FakeLib.ptn_krylov_gs_step = _fake_gs_step

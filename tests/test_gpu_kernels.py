@@ -137,3 +137,43 @@ def test_qr_rank_deficient_exact_structure(lib):
     qn, rn = np.linalg.qr(B, mode="reduced")
     assert np.max(np.abs(q - qn)) < 1e-13
     assert np.all(q[4:, 4:] == qn[4:, 4:])
+
+
+@pytest.mark.parametrize("n,nq", [(1, 1), (1000, 3), (131072, 8), (70001, 16), (4097, 17)])
+def test_krylov_gs_step_matches_numpy(n, nq):
+    """One Gram-Schmidt step (fused cooperative kernel for nq <= 16, kernel
+    sequence above) against NumPy's two-pass classical Gram-Schmidt."""
+    import ctypes
+    from pytreenet_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(n + nq)
+    Qn = rng.normal(size=(nq, n)) + 1j * rng.normal(size=(nq, n))
+    for i in range(nq):                       # orthonormal rows, as in a Krylov basis
+        for j in range(i):
+            Qn[i] -= np.vdot(Qn[j], Qn[i]) * Qn[j]
+        Qn[i] /= np.linalg.norm(Qn[i])
+    wn = rng.normal(size=n) + 1j * rng.normal(size=n)
+    Q = torch.from_numpy(Qn).cuda()
+    w = torch.from_numpy(wn.copy()).cuda()
+    h = torch.zeros(2 * nq, dtype=torch.complex128, device="cuda")
+    part = torch.zeros(int(lib.ptn_krylov_partials(n)) + 8, dtype=torch.complex128, device="cuda")
+    norms = torch.zeros(2, dtype=torch.float64, device="cuda")
+    qn = torch.zeros(n, dtype=torch.complex128, device="cuda")
+    st = lib.ptn_krylov_gs_step(Q.data_ptr(), n, nq, w.data_ptr(), n, h.data_ptr(), part.data_ptr(),
+                                norms.data_ptr(), qn.data_ptr(),
+                                ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert st == 0
+    torch.cuda.synchronize()
+    w1 = wn.copy()
+    h1 = Qn.conj() @ w1
+    w1 = w1 - h1 @ Qn
+    h2 = Qn.conj() @ w1
+    w1 = w1 - h2 @ Qn
+    scale = np.linalg.norm(wn)
+    np.testing.assert_allclose(norms.cpu().numpy()[0], np.linalg.norm(wn), rtol=1e-13)
+    np.testing.assert_allclose(h.cpu().numpy(), np.concatenate([h1, h2]), atol=1e-12 * scale)
+    np.testing.assert_allclose(w.cpu().numpy(), w1, atol=1e-12 * scale)
+    b = np.linalg.norm(w1)
+    np.testing.assert_allclose(norms.cpu().numpy()[1], b, rtol=1e-10, atol=1e-13 * scale)
+    if b > 1e-8 * scale:
+        np.testing.assert_allclose(qn.cpu().numpy(), w1 / b, atol=1e-10)

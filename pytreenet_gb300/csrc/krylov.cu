@@ -7,9 +7,6 @@
 // shared-memory tree per CTA, then one CTA summing the per-CTA partials in a
 // fixed order, so repeated runs give identical bits.
 #include "ptn_common.cuh"
-#include "coop.cuh"
-
-#include <mutex>
 
 namespace {
 
@@ -144,146 +141,7 @@ unsigned long long g_ptn_launches = 0;
 
 extern "C" unsigned long long ptn_launch_counter(void) { return g_ptn_launches; }
 
-// ---- fused Gram-Schmidt step (one cooperative launch) ---------------------------------
-// Phase 1: |w|^2 and d_i = Q_i^H w; phase 2: w -= sum d_i Q_i and, in the same
-// pass, e_i = Q_i^H w; phase 3: w -= sum e_i Q_i and |w|^2; phase 4:
-// qnext = w / |w|. Every CTA writes its partial sums for a phase to its own
-// slot; after the grid barrier every CTA adds the slots in CTA order, so all
-// CTAs hold bit-identical totals (deterministic, like the multi-kernel path).
-// Consecutive phases use alternating slot sets: a CTA that runs ahead writes
-// the next phase's partials while others still read this phase's.
-constexpr int GS_MAXQ = 16;
-constexpr long long GS_WAIT_CYCLES = 4000000000LL;
-
-struct GsArgs {
-  const double2* Q;
-  int64_t ldq;
-  int nq;
-  double2* w;
-  int64_t n;
-  double2* h;        // [2 nq]
-  double* norms;     // [2]
-  double2* qnext;    // may be null
-  double2* slots;    // [2][G][GS_MAXQ + 1]
-  unsigned* ctrl;
-};
-
-// Block-reduce k complex values (thread-local v[0..k)) into out[0..k) (thread 0 writes).
-template <int K>
-__device__ __forceinline__ void block_reduce_store(double2 (&v)[K], int k, double2* out) {
-  __shared__ double2 red[RT / 32][K];
-  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-#pragma unroll
-  for (int i = 0; i < K; ++i) {
-    if (i < k) {
-      const double2 r = warp_sum2(v[i]);
-      if (lane == 0) red[wp][i] = r;
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x < k) {
-    double2 t = make_double2(0.0, 0.0);
-    for (int u = 0; u < RT / 32; ++u) t = cadd(t, red[u][threadIdx.x]);
-    out[threadIdx.x] = t;
-  }
-  __syncthreads();
-}
-
-__device__ __forceinline__ double2* slot_set(const GsArgs& a, int phase) {
-  return a.slots + (int64_t)(phase & 1) * gridDim.x * (GS_MAXQ + 1);
-}
-
-// Sum entries [0, k) of one slot set over CTAs in order, into shared tot[].
-__device__ __forceinline__ void gather_totals(const double2* set, int k, double2* tot) {
-  if (threadIdx.x < k) {
-    double2 t = make_double2(0.0, 0.0);
-    for (unsigned b = 0; b < gridDim.x; ++b) t = cadd(t, __ldcg(set + (int64_t)b * (GS_MAXQ + 1) + threadIdx.x));
-    tot[threadIdx.x] = t;
-  }
-  __syncthreads();
-}
-
-__global__ void __launch_bounds__(RT) zgs_step_kernel(GsArgs a) {
-  __shared__ double2 tot[GS_MAXQ + 1];
-  const int nq = a.nq;
-  const int64_t gt = (int64_t)blockIdx.x * RT + threadIdx.x, nt = (int64_t)gridDim.x * RT;
-  double2 acc[GS_MAXQ + 1];
-  // phase 1: slot[0..nq) = Q^H w, slot[nq] = (|w|^2, 0)
-#pragma unroll
-  for (int i = 0; i <= GS_MAXQ; ++i) acc[i] = make_double2(0.0, 0.0);
-  for (int64_t x = gt; x < a.n; x += nt) {
-    const double2 wx = a.w[x];
-    acc[GS_MAXQ].x += cabs2(wx);
-#pragma unroll
-    for (int i = 0; i < GS_MAXQ; ++i)
-      if (i < nq) acc[i] = cfmac(a.Q[(int64_t)i * a.ldq + x], wx, acc[i]);
-  }
-  acc[nq] = acc[GS_MAXQ];
-  block_reduce_store<GS_MAXQ + 1>(acc, nq + 1, slot_set(a, 0) + (int64_t)blockIdx.x * (GS_MAXQ + 1));
-  if (!ptn_grid_barrier(a.ctrl, GS_WAIT_CYCLES)) goto abort;
-  gather_totals(slot_set(a, 0), nq + 1, tot);
-  if (blockIdx.x == 0 && threadIdx.x < nq) a.h[threadIdx.x] = tot[threadIdx.x];
-  if (blockIdx.x == 0 && threadIdx.x == 0) a.norms[0] = sqrt(tot[nq].x);
-  // phase 2: w -= Q d, then slot[0..nq) = Q^H w
-  {
-    double2 d[GS_MAXQ];
-#pragma unroll
-    for (int i = 0; i < GS_MAXQ; ++i) d[i] = i < nq ? tot[i] : make_double2(0.0, 0.0);
-    __syncthreads();
-#pragma unroll
-    for (int i = 0; i <= GS_MAXQ; ++i) acc[i] = make_double2(0.0, 0.0);
-    for (int64_t x = gt; x < a.n; x += nt) {
-      double2 wx = a.w[x];
-      double2 qv[GS_MAXQ];
-#pragma unroll
-      for (int i = 0; i < GS_MAXQ; ++i)
-        if (i < nq) {
-          qv[i] = a.Q[(int64_t)i * a.ldq + x];
-          wx = csub(wx, cmul(d[i], qv[i]));
-        }
-#pragma unroll
-      for (int i = 0; i < GS_MAXQ; ++i)
-        if (i < nq) acc[i] = cfmac(qv[i], wx, acc[i]);
-      a.w[x] = wx;
-    }
-  }
-  block_reduce_store<GS_MAXQ + 1>(acc, nq, slot_set(a, 1) + (int64_t)blockIdx.x * (GS_MAXQ + 1));
-  if (!ptn_grid_barrier(a.ctrl, GS_WAIT_CYCLES)) goto abort;
-  gather_totals(slot_set(a, 1), nq, tot);
-  if (blockIdx.x == 0 && threadIdx.x < nq) a.h[nq + threadIdx.x] = tot[threadIdx.x];
-  // phase 3: w -= Q e, |w|^2
-  {
-    double2 e[GS_MAXQ];
-#pragma unroll
-    for (int i = 0; i < GS_MAXQ; ++i) e[i] = i < nq ? tot[i] : make_double2(0.0, 0.0);
-    __syncthreads();
-    double2 nrm[1] = {make_double2(0.0, 0.0)};
-    for (int64_t x = gt; x < a.n; x += nt) {
-      double2 wx = a.w[x];
-#pragma unroll
-      for (int i = 0; i < GS_MAXQ; ++i)
-        if (i < nq) wx = csub(wx, cmul(e[i], a.Q[(int64_t)i * a.ldq + x]));
-      a.w[x] = wx;
-      nrm[0].x += cabs2(wx);
-    }
-    block_reduce_store<1>(nrm, 1, slot_set(a, 2) + (int64_t)blockIdx.x * (GS_MAXQ + 1));
-  }
-  if (!ptn_grid_barrier(a.ctrl, GS_WAIT_CYCLES)) goto abort;
-  gather_totals(slot_set(a, 2), 1, tot);
-  {
-    const double beta = sqrt(tot[0].x);
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.norms[1] = beta;
-    if (a.qnext) {
-      const double inv = 1.0 / beta;
-      for (int64_t x = gt; x < a.n; x += nt) a.qnext[x] = cscale(a.w[x], inv);
-    }
-  }
-  return;
-abort:
-  if (threadIdx.x == 0) a.norms[1] = __longlong_as_double(0x7ff8000000000000LL);
-}
-
-extern "C" int64_t ptn_krylov_partials(int64_t n) { return nblocks_for(n) * 36 + 64; }
+extern "C" int64_t ptn_krylov_partials(int64_t n) { return nblocks_for(n) * MAXQ; }
 
 extern "C" int ptn_zdot_multi(const void* Q, int64_t ldq, int32_t nq, const void* w, int64_t n,
                               void* h, int32_t accumulate, void* partial, void* stream) {
@@ -367,57 +225,4 @@ extern "C" int ptn_check_finite(const void* x, int64_t n, int32_t* flag, void* s
   check_finite_kernel<<<(int)nblocks_for(n), RT, 0, ptn_stream(stream)>>>(
       static_cast<const double*>(x), 2 * n, flag);
   return ptn_launch_status();
-}
-
-// Fused Gram-Schmidt step for nq <= GS_MAXQ and n <= 2^21 (one cooperative launch); returns
-// PTN_ERR_UNSUPPORTED when it does not apply, so the caller runs the kernels
-// one by one.
-int ptn_gs_step_fused(const void* Q, int64_t ldq, int32_t nq, void* w, int64_t n, void* h, void* partial,
-                      double* norms, void* qnext, void* stream) {
-  static int cached[64] = {0};
-  static std::mutex mu;
-  // Long vectors keep the multi-kernel path: it runs ~8 CTAs per SM for
-  // bandwidth, this kernel one (its grid must be co-resident).
-  if (nq > GS_MAXQ || n > (int64_t(1) << 21)) return PTN_ERR_UNSUPPORTED;
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return PTN_ERR_UNSUPPORTED;
-  int maxb;
-  {
-    std::lock_guard<std::mutex> lock(mu);
-    if (cached[dev] == 0) {
-      int per_sm = 0, sms = 0, coop = 0;
-      if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) cached[dev] = -1;
-      else if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, zgs_step_kernel, RT, 0) != cudaSuccess ||
-               cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-        cached[dev] = -1;
-      else
-        cached[dev] = per_sm * sms;
-    }
-    maxb = cached[dev];
-  }
-  if (maxb <= 0) return PTN_ERR_UNSUPPORTED;
-  int64_t G = nblocks_for(n);
-  if (G > maxb) G = maxb;
-  if (G > 152) G = 152;
-  GsArgs a;
-  a.Q = static_cast<const double2*>(Q);
-  a.ldq = ldq;
-  a.nq = nq;
-  a.w = static_cast<double2*>(w);
-  a.n = n;
-  a.h = static_cast<double2*>(h);
-  a.norms = norms;
-  a.qnext = static_cast<double2*>(qnext);
-  a.slots = static_cast<double2*>(partial);
-  a.ctrl = reinterpret_cast<unsigned*>(a.slots + 2 * G * (GS_MAXQ + 1));
-  cudaStream_t s = ptn_stream(stream);
-  if (cudaMemsetAsync(a.ctrl, 0, 256, s) != cudaSuccess) return PTN_ERR_LAUNCH;
-  void* args[] = {&a};
-  PTN_COUNT(1);
-  if (cudaLaunchCooperativeKernel((const void*)zgs_step_kernel, dim3((unsigned)G), dim3(RT), args, 0, s) !=
-      cudaSuccess) {
-    cudaGetLastError();
-    return PTN_ERR_LAUNCH;
-  }
-  return PTN_OK;
 }

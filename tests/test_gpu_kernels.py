@@ -141,8 +141,8 @@ def test_qr_rank_deficient_exact_structure(lib):
 
 @pytest.mark.parametrize("n,nq", [(1, 1), (1000, 3), (131072, 8), (70001, 16), (4097, 17)])
 def test_krylov_gs_step_matches_numpy(n, nq):
-    """One Gram-Schmidt step (fused cooperative kernel for nq <= 16, kernel
-    sequence above) against NumPy's two-pass classical Gram-Schmidt."""
+    """One Gram-Schmidt step (ptn_krylov_gs_step) against NumPy's two-pass
+    classical Gram-Schmidt."""
     import ctypes
     from pytreenet_gb300 import _lib
     lib = _lib.load()

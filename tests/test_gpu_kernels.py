@@ -109,7 +109,8 @@ def _qr_case(lib, A, row_perm=None):
     return out, R.cpu().numpy()
 
 
-@pytest.mark.parametrize("m,k", [(6, 4), (300, 40), (2, 8), (2048, 64), (5, 5), (1, 3), (3000, 130)])
+@pytest.mark.parametrize("m,k", [(6, 4), (300, 40), (2, 8), (2048, 64), (5, 5), (1, 3), (3000, 130),
+                                 (512, 256), (768, 100), (64, 80), (700, 33), (769, 64)])
 def test_qr_matches_lapack_convention(lib, m, k):
     A = crandn(m, k)
     q, r = _qr_case(lib, A, row_perm=RNG.permutation(m))
@@ -135,6 +136,13 @@ def test_qr_rank_deficient_exact_structure(lib):
     B[:4, :] = crandn(4, k)
     q, r = _qr_case(lib, B)
     qn, rn = np.linalg.qr(B, mode="reduced")
+    assert np.max(np.abs(q - qn)) < 1e-13
+    assert np.all(q[4:, 4:] == qn[4:, 4:])
+    # the panel (blocked) path: rank 4 in a 256 x 64 matrix, exact identity complement
+    C = np.zeros((256, 64), dtype=complex)
+    C[:4, :] = crandn(4, 64)
+    q, r = _qr_case(lib, C)
+    qn, rn = np.linalg.qr(C, mode="reduced")
     assert np.max(np.abs(q - qn)) < 1e-13
     assert np.all(q[4:, 4:] == qn[4:, 4:])
 

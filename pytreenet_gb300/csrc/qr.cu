@@ -362,7 +362,7 @@ __global__ void __launch_bounds__(ST) hh_form_small(double2* __restrict__ A, con
 // and contributes a zero row and column to T.
 constexpr int QB = 16;
 constexpr int64_t QB_MAX_M = 768;
-constexpr int PT = 512;
+constexpr int PT = ST;  // block_sum and block_sum2 assume ST threads
 
 __device__ __forceinline__ double2 warp_sum2c(double2 v) { return warp_sum2(v); }
 

@@ -351,216 +351,6 @@ __global__ void __launch_bounds__(ST) hh_form_small(double2* __restrict__ A, con
   }
 }
 
-// ---- blocked path (m <= QB_MAX_M, at least 2 panels) ----------------------------------
-// The same Householder QR in panels of QB reflectors (the compact WY form
-// H_1 ... H_b = I - V T V^H of LAPACK's zgeqrf / zungqr): one CTA factorises a
-// panel held in shared memory (a warp per trailing panel column, so a
-// reflector step costs a few CTA barriers instead of a launch) and builds its
-// T; one launch applies the panel's block reflector to every trailing column
-// (a CTA per column). Q is formed panel by panel backwards the same way.
-// Exact zeros stay exact as in the per-step path: a zero reflector has tau = 0
-// and contributes a zero row and column to T.
-constexpr int QB = 16;
-constexpr int64_t QB_MAX_M = 768;
-constexpr int PT = ST;  // block_sum and block_sum2 assume ST threads
-
-__device__ __forceinline__ double2 warp_sum2c(double2 v) { return warp_sum2(v); }
-
-__global__ void __launch_bounds__(PT) qr_panel_fact(double2* __restrict__ A, const int64_t* __restrict__ rowoff,
-                                                    int64_t cs, int64_t m, int64_t p0, int b,
-                                                    double2* __restrict__ tau, double2* __restrict__ betas,
-                                                    double2* __restrict__ V, double2* __restrict__ Tb) {
-  extern __shared__ double2 P[];  // [b][len], column c at c * len
-  __shared__ double red[PT / 32 + 1];
-  __shared__ double2 sc[2];
-  __shared__ double2 G[QB][QB];
-  const int64_t len = m - p0;
-  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-  for (int64_t e = threadIdx.x; e < b * len; e += PT) {
-    const int64_t c = e / len, r = e - c * len;
-    P[e] = A[rowoff[p0 + r] + (p0 + c) * cs];
-  }
-  __syncthreads();
-  for (int jj = 0; jj < b; ++jj) {
-    double2* x = P + (int64_t)jj * len;
-    double acc = 0.0;
-    for (int64_t t = jj + 1 + threadIdx.x; t < len; t += PT) acc += cabs2(x[t]);
-    const double xn2 = block_sum(acc, red);
-    if (threadIdx.x == 0) {
-      const double2 alpha = x[jj];
-      const double xnorm = sqrt(xn2);
-      double2 t_, s_, b_;
-      if (xnorm == 0.0 && alpha.y == 0.0) {
-        t_ = make_double2(0.0, 0.0);
-        s_ = make_double2(0.0, 0.0);
-        b_ = alpha;
-      } else {
-        const double nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xnorm * xnorm);
-        const double beta = (alpha.x >= 0.0) ? -nrm : nrm;
-        t_ = make_double2((beta - alpha.x) / beta, -alpha.y / beta);
-        const double2 d = make_double2(alpha.x - beta, alpha.y);
-        const double den = d.x * d.x + d.y * d.y;
-        s_ = make_double2(d.x / den, -d.y / den);
-        b_ = make_double2(beta, 0.0);
-      }
-      sc[0] = t_;
-      sc[1] = s_;
-      tau[p0 + jj] = t_;
-      betas[p0 + jj] = b_;
-    }
-    __syncthreads();
-    const double2 s_ = sc[1];
-    const int64_t j = p0 + jj;
-    for (int64_t t = jj + threadIdx.x; t < len; t += PT) {
-      const double2 v = (t == jj) ? make_double2(1.0, 0.0) : cmul(x[t], s_);
-      x[t] = v;
-      V[j * m + j + (t - jj)] = v;
-    }
-    __syncthreads();
-    double2 f = sc[0];
-    f.y = -f.y;  // conj(tau): the factorisation applies H^H
-    for (int cc = jj + 1 + wp; cc < b; cc += PT / 32) {
-      double2* y = P + (int64_t)cc * len;
-      double2 w = make_double2(0.0, 0.0);
-      for (int64_t t = jj + lane; t < len; t += 32) w = cfmac(x[t], y[t], w);
-      w = warp_sum2c(w);
-      const double2 fw = cmul(f, w);
-      for (int64_t t = jj + lane; t < len; t += 32) y[t] = csub(y[t], cmul(x[t], fw));
-    }
-    __syncthreads();
-  }
-  // T (zlarft, forward, columnwise): T[i][i] = tau_i,
-  // T[0:i, i] = -tau_i T[0:i, 0:i] (V[:, 0:i]^H v_i).
-  for (int pr = wp; pr < b * b; pr += PT / 32) {
-    const int r = pr / b, i = pr - r * b;
-    if (r >= i) continue;
-    const double2* vr = P + (int64_t)r * len;
-    const double2* vi = P + (int64_t)i * len;
-    double2 w = make_double2(0.0, 0.0);
-    for (int64_t t = i + lane; t < len; t += 32) w = cfmac(vr[t], vi[t], w);
-    w = warp_sum2c(w);
-    if (lane == 0) G[r][i] = w;
-  }
-  __syncthreads();
-  __shared__ double2 Tl[QB][QB];
-  __shared__ double2 tmp[QB];
-  for (int e = threadIdx.x; e < QB * QB; e += PT) Tl[e / QB][e % QB] = make_double2(0.0, 0.0);
-  __syncthreads();
-  for (int i = 0; i < b; ++i) {
-    const double2 ti = tau[p0 + i];
-    if (threadIdx.x < i) {
-      const double2 g = G[threadIdx.x][i];
-      tmp[threadIdx.x] = make_double2(-(ti.x * g.x - ti.y * g.y), -(ti.x * g.y + ti.y * g.x));
-    }
-    __syncthreads();
-    if (threadIdx.x < i) {
-      const int r = threadIdx.x;
-      double2 a = make_double2(0.0, 0.0);
-      for (int q = r; q < i; ++q) a = cfma(Tl[r][q], tmp[q], a);
-      Tl[r][i] = a;
-    }
-    if (threadIdx.x == 0) Tl[i][i] = ti;
-    __syncthreads();
-  }
-  for (int e = threadIdx.x; e < QB * QB; e += PT) Tb[e] = Tl[e / QB][e % QB];
-  for (int64_t e = threadIdx.x; e < b * len; e += PT) {
-    const int64_t c = e / len, r = e - c * len;
-    A[rowoff[p0 + r] + (p0 + c) * cs] = P[e];
-  }
-}
-
-// Columns c0 + blockIdx.x, rows p0..m-1: c <- c - V op(T) V^H c with
-// op(T) = T^H (trans, factorisation: H^H) or T (Q formation: H).
-__global__ void __launch_bounds__(ST) qr_panel_apply(double2* __restrict__ A, const int64_t* __restrict__ rowoff,
-                                                     int64_t cs, int64_t m, int64_t p0, int b, int64_t c0,
-                                                     const double2* __restrict__ V, const double2* __restrict__ Tb,
-                                                     int trans) {
-  __shared__ double2 red[ST / 32][QB];
-  __shared__ double2 y[QB], z[QB];
-  const int64_t c = c0 + blockIdx.x;
-  const int64_t len = m - p0;
-  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-  double2 acc[QB];
-#pragma unroll
-  for (int l = 0; l < QB; ++l) acc[l] = make_double2(0.0, 0.0);
-  for (int64_t t = threadIdx.x; t < len; t += ST) {
-    const double2 a = A[rowoff[p0 + t] + c * cs];
-#pragma unroll
-    for (int l = 0; l < QB; ++l)
-      if (l < b && t >= l) acc[l] = cfmac(V[(p0 + l) * m + p0 + t], a, acc[l]);
-  }
-#pragma unroll
-  for (int l = 0; l < QB; ++l) {
-    const double2 r = warp_sum2(acc[l]);
-    if (lane == 0) red[wp][l] = r;
-  }
-  __syncthreads();
-  if (threadIdx.x < b) {
-    double2 t = make_double2(0.0, 0.0);
-    for (int u = 0; u < ST / 32; ++u) t = cadd(t, red[u][threadIdx.x]);
-    y[threadIdx.x] = t;
-  }
-  __syncthreads();
-  if (threadIdx.x < b) {
-    const int l = threadIdx.x;
-    double2 a = make_double2(0.0, 0.0);
-    if (trans) {
-      for (int r = 0; r <= l; ++r) a = cfmac(Tb[r * QB + l], y[r], a);   // conj(T[r][l]) y[r]
-    } else {
-      for (int r = l; r < b; ++r) a = cfma(Tb[l * QB + r], y[r], a);
-    }
-    z[l] = a;
-  }
-  __syncthreads();
-  for (int64_t t = threadIdx.x; t < len; t += ST) {
-    double2* q = A + rowoff[p0 + t] + c * cs;
-    double2 v = *q;
-#pragma unroll
-    for (int l = 0; l < QB; ++l)
-      if (l < b && t >= l) v = csub(v, cmul(V[(p0 + l) * m + p0 + t], z[l]));
-    *q = v;
-  }
-}
-
-// Q columns p0..p0+b-1 (zung2r on the panel, backwards), rows above p0 zeroed.
-__global__ void __launch_bounds__(PT) qr_panel_form(double2* __restrict__ A, const int64_t* __restrict__ rowoff,
-                                                    int64_t cs, int64_t m, int64_t p0, int b,
-                                                    const double2* __restrict__ tau,
-                                                    const double2* __restrict__ V) {
-  extern __shared__ double2 P[];
-  const int64_t len = m - p0;
-  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-  for (int jj = b - 1; jj >= 0; --jj) {
-    const int64_t j = p0 + jj;
-    const double2 t_ = tau[j];
-    const double2* v = V + j * m + j;       // v[t - jj] for local rows t >= jj
-    for (int cc = jj + 1 + wp; cc < b; cc += PT / 32) {
-      double2* y = P + (int64_t)cc * len;
-      double2 w = make_double2(0.0, 0.0);
-      for (int64_t t = jj + lane; t < len; t += 32) w = cfmac(v[t - jj], y[t], w);
-      w = warp_sum2c(w);
-      const double2 fw = cmul(t_, w);
-      for (int64_t t = jj + lane; t < len; t += 32) y[t] = csub(y[t], cmul(v[t - jj], fw));
-    }
-    double2* x = P + (int64_t)jj * len;
-    for (int64_t t = threadIdx.x; t < len; t += PT) {
-      double2 val;
-      if (t < jj) val = make_double2(0.0, 0.0);
-      else if (t == jj) val = make_double2(1.0 - t_.x, -t_.y);
-      else {
-        const double2 vi = v[t - jj];
-        val = make_double2(-(t_.x * vi.x - t_.y * vi.y), -(t_.x * vi.y + t_.y * vi.x));
-      }
-      x[t] = val;
-    }
-    __syncthreads();
-  }
-  for (int64_t e = threadIdx.x; e < b * m; e += PT) {
-    const int64_t c = e / m, r = e - c * m;
-    A[rowoff[r] + (p0 + c) * cs] = r < p0 ? make_double2(0.0, 0.0) : P[c * len + (r - p0)];
-  }
-}
-
 inline unsigned grid1(int64_t n) {
   int64_t b = (n + QT - 1) / QT;
   if (b < 1) b = 1;
@@ -573,50 +363,9 @@ inline unsigned grid1(int64_t n) {
 extern "C" int64_t ptn_zqr_work_bytes(int64_t m, int64_t k) {
   if (m <= QR_SMALL_M) {
     const int64_t p = m < k ? m : k;
-    const int64_t npan = (p + QB - 1) / QB;
-    return 16 * (2 * k + m * p + npan * QB * QB) + 256;   // tau, betas, V, panel T factors
+    return 16 * (2 * k + m * p) + 256;   // tau, betas, V
   }
   return 16 * (3 * k + (nrb_for(m) + 1) / 2 + 1 + nrb_for(m) * k) + 256;
-}
-
-static int zqr_keep_blocked(double2* A, const int64_t* rowoff, int64_t m, int64_t k, int64_t cs, double2* R,
-                            double2* tau, double2* betas, double2* V, double2* Tall, cudaStream_t s) {
-  const int64_t p = m < k ? m : k;
-  const size_t smem = (size_t)QB * m * sizeof(double2);
-  static bool attr_set = false;
-  if (!attr_set) {
-    if (cudaFuncSetAttribute(qr_panel_fact, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)(QB * QB_MAX_M * sizeof(double2))) != cudaSuccess ||
-        cudaFuncSetAttribute(qr_panel_form, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)(QB * QB_MAX_M * sizeof(double2))) != cudaSuccess)
-      return PTN_ERR_LAUNCH;
-    attr_set = true;
-  }
-  for (int64_t p0 = 0; p0 < p; p0 += QB) {
-    const int b = (int)(p - p0 < QB ? p - p0 : QB);
-    double2* Tb = Tall + (p0 / QB) * QB * QB;
-    PTN_COUNT(1);
-    qr_panel_fact<<<1, PT, smem, s>>>(A, rowoff, cs, m, p0, b, tau, betas, V, Tb);
-    if (p0 + b < k) {
-      PTN_COUNT(1);
-      qr_panel_apply<<<(unsigned)(k - p0 - b), ST, 0, s>>>(A, rowoff, cs, m, p0, b, p0 + b, V, Tb, 1);
-    }
-  }
-  PTN_COUNT(1);
-  extract_r_small<<<grid1(k * k), ST, 0, s>>>(A, rowoff, cs, k, p, betas, R);
-  const int64_t last = ((p - 1) / QB) * QB;
-  for (int64_t p0 = last; p0 >= 0; p0 -= QB) {
-    const int b = (int)(p - p0 < QB ? p - p0 : QB);
-    const double2* Tb = Tall + (p0 / QB) * QB * QB;
-    if (p0 + b < p) {
-      PTN_COUNT(1);
-      qr_panel_apply<<<(unsigned)(p - p0 - b), ST, 0, s>>>(A, rowoff, cs, m, p0, b, p0 + b, V, Tb, 0);
-    }
-    PTN_COUNT(1);
-    qr_panel_form<<<1, PT, (size_t)QB * (m - p0) * sizeof(double2), s>>>(A, rowoff, cs, m, p0, b, tau, V);
-  }
-  if (p < k) { PTN_COUNT(1); zero_cols_kernel<<<grid1(m * (k - p)), QT, 0, s>>>(A, rowoff, cs, m, k, p); }
-  return ptn_launch_status();
 }
 
 static int zqr_keep_small(double2* A, const int64_t* rowoff, int64_t m, int64_t k, int64_t cs, double2* R,
@@ -625,8 +374,6 @@ static int zqr_keep_small(double2* A, const int64_t* rowoff, int64_t m, int64_t 
   double2* betas = tau + k;
   double2* V = betas + k;
   const int64_t p = m < k ? m : k;
-  if (m <= QB_MAX_M && p >= 2 * QB)
-    return zqr_keep_blocked(A, rowoff, m, k, cs, R, tau, betas, V, V + m * p, s);
   for (int64_t j = 0; j < p; ++j) {
     const int64_t ncols = k - (j + 1);
     PTN_COUNT(1);

@@ -215,13 +215,14 @@ __global__ void zero_cols_kernel(double2* __restrict__ A, const int64_t* __restr
   }
 }
 
-// ---- small-m path (m <= QR_SMALL_M) ---------------------------------------------------
-// The reflectors go to a separate V buffer and the diagonal of R to `betas`,
-// so no CTA writes what another reads in the same launch.
+// ---- small-m path: one launch per Householder step ------------------------------------
+// For m <= QR_SMALL_M each step is one kernel: every CTA recomputes the
+// reflector from column j (a few KB, identical arithmetic in every CTA, so the
+// result is the same everywhere) and then owns one trailing column (dot and
+// update). The reflectors go to a separate V buffer and the diagonal of R to
+// `betas`, so no CTA writes what another reads in the same launch.
 constexpr int64_t QR_SMALL_M = 2048;
 constexpr int ST = 256;
-constexpr int QR_MULTI_MAX = 8;                   // reflectors per launch
-constexpr int64_t QR_MULTI_SMEM = 200 * 1024;     // dynamic shared memory budget
 
 __device__ __forceinline__ double block_sum(double v, double* red) {
   v = warp_sum(v);
@@ -245,6 +246,68 @@ __device__ __forceinline__ double2 block_sum2(double2 v, double* red) {
   return make_double2(re, im);
 }
 
+// Step j of the factorisation. grid = max(1, k - j - 1); CTA b owns column j+1+b.
+__global__ void __launch_bounds__(ST) hh_fact_small(double2* __restrict__ A, const int64_t* __restrict__ rowoff,
+                                                    int64_t cs, int64_t m, int64_t k, int64_t j,
+                                                    double2* __restrict__ tau, double2* __restrict__ betas,
+                                                    double2* __restrict__ V) {
+  __shared__ double2 vs[QR_SMALL_M];
+  __shared__ double red[ST / 32 + 1];
+  __shared__ double2 sc[3];  // tau, scal, w
+  const int64_t len = m - j;
+  double acc = 0.0;
+  for (int64_t t = threadIdx.x; t < len; t += ST) {
+    const double2 a = A[rowoff[j + t] + j * cs];
+    vs[t] = a;
+    if (t > 0) acc += cabs2(a);
+  }
+  const double xn2 = block_sum(acc, red);
+  if (threadIdx.x == 0) {
+    const double2 alpha = vs[0];
+    const double xnorm = sqrt(xn2);
+    double2 t_, s_, b_;
+    if (xnorm == 0.0 && alpha.y == 0.0) {
+      t_ = make_double2(0.0, 0.0);
+      s_ = make_double2(0.0, 0.0);
+      b_ = alpha;
+    } else {
+      const double nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xnorm * xnorm);
+      const double beta = (alpha.x >= 0.0) ? -nrm : nrm;
+      t_ = make_double2((beta - alpha.x) / beta, -alpha.y / beta);
+      const double2 d = make_double2(alpha.x - beta, alpha.y);
+      const double den = d.x * d.x + d.y * d.y;
+      s_ = make_double2(d.x / den, -d.y / den);
+      b_ = make_double2(beta, 0.0);
+    }
+    sc[0] = t_;
+    sc[1] = s_;
+    if (blockIdx.x == 0) {
+      tau[j] = t_;
+      betas[j] = b_;
+    }
+  }
+  __syncthreads();
+  const double2 s_ = sc[1];
+  for (int64_t t = threadIdx.x; t < len; t += ST) {
+    const double2 v = (t == 0) ? make_double2(1.0, 0.0) : cmul(vs[t], s_);
+    vs[t] = v;
+    if (blockIdx.x == 0) V[j * m + j + t] = v;
+  }
+  __syncthreads();
+  const int64_t c = j + 1 + blockIdx.x;
+  if (c >= k) return;
+  double2 w = make_double2(0.0, 0.0);
+  for (int64_t t = threadIdx.x; t < len; t += ST) w = cfmac(vs[t], A[rowoff[j + t] + c * cs], w);
+  w = block_sum2(w, red);
+  double2 f = sc[0];
+  f.y = -f.y;  // conj(tau): the factorisation applies H^H
+  const double2 fw = cmul(f, w);
+  for (int64_t t = threadIdx.x; t < len; t += ST) {
+    double2* p = A + rowoff[j + t] + c * cs;
+    *p = csub(*p, cmul(vs[t], fw));
+  }
+}
+
 // R[r][c]: strictly-upper part from A, diagonal from betas (rows < p), zero elsewhere.
 __global__ void extract_r_small(const double2* __restrict__ A, const int64_t* __restrict__ rowoff, int64_t cs,
                                 int64_t k, int64_t p, const double2* __restrict__ betas, double2* __restrict__ R) {
@@ -259,152 +322,33 @@ __global__ void extract_r_small(const double2* __restrict__ A, const int64_t* __
   }
 }
 
-// ---- several reflectors per launch (m <= QR_SMALL_M) ------------------------------------
-// Factorisation: every CTA factorises the ns-column panel j0..j0+ns-1
-// redundantly in shared memory (identical arithmetic, so identical reflectors
-// everywhere; the trailing panel columns are updated a warp per column), then
-// applies the ns reflectors to its own trailing column. CTA 0 writes the panel
-// back and stores the reflectors. ns launches' worth of dependent steps cost
-// one launch; GB300's per-SM FP64 rate keeps ns small (the panel work is
-// repeated on every SM).
-__global__ void __launch_bounds__(ST) hh_fact_multi(double2* __restrict__ A, const int64_t* __restrict__ rowoff,
-                                                    int64_t cs, int64_t m, int64_t k, int64_t j0, int ns,
-                                                    double2* __restrict__ tau, double2* __restrict__ betas,
-                                                    double2* __restrict__ V) {
-  extern __shared__ double2 P[];  // [ns][len] panel, then [len] own column
+// Step j of forming Q (zung2r): CTAs 0..ncols-1 apply H_j to columns j+1..p-1,
+// CTA ncols writes column j itself.
+__global__ void __launch_bounds__(ST) hh_form_small(double2* __restrict__ A, const int64_t* __restrict__ rowoff,
+                                                    int64_t cs, int64_t m, int64_t p, int64_t j,
+                                                    const double2* __restrict__ tau, const double2* __restrict__ V) {
   __shared__ double red[ST / 32 + 1];
-  __shared__ double2 sc[2];
-  __shared__ double2 taus[QR_MULTI_MAX];
-  const int64_t len = m - j0;
-  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-  double2* col = P + (int64_t)ns * len;
-  const int64_t c = j0 + ns + blockIdx.x;
-  const bool own = c < k;
-  for (int64_t e = threadIdx.x; e < ns * len; e += ST) {
-    const int64_t cc = e / len, r = e - cc * len;
-    P[e] = A[rowoff[j0 + r] + (j0 + cc) * cs];
+  const int64_t ncols = p - (j + 1);
+  const double2 t_ = tau[j];
+  const double2* v = V + j * m;
+  if (blockIdx.x == ncols) {
+    for (int64_t i = threadIdx.x; i < m; i += ST) {
+      double2* q = A + rowoff[i] + j * cs;
+      if (i < j) *q = make_double2(0.0, 0.0);
+      else if (i == j) *q = make_double2(1.0 - t_.x, -t_.y);
+      else *q = make_double2(-(t_.x * v[i].x - t_.y * v[i].y), -(t_.x * v[i].y + t_.y * v[i].x));
+    }
+    return;
   }
-  if (own)
-    for (int64_t t = threadIdx.x; t < len; t += ST) col[t] = A[rowoff[j0 + t] + c * cs];
-  __syncthreads();
-  for (int i = 0; i < ns; ++i) {
-    double2* x = P + (int64_t)i * len;
-    double acc = 0.0;
-    for (int64_t t = i + 1 + threadIdx.x; t < len; t += ST) acc += cabs2(x[t]);
-    const double xn2 = block_sum(acc, red);
-    if (threadIdx.x == 0) {
-      const double2 alpha = x[i];
-      const double xnorm = sqrt(xn2);
-      double2 t_, s_, b_;
-      if (xnorm == 0.0 && alpha.y == 0.0) {
-        t_ = make_double2(0.0, 0.0);
-        s_ = make_double2(0.0, 0.0);
-        b_ = alpha;
-      } else {
-        const double nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xnorm * xnorm);
-        const double beta = (alpha.x >= 0.0) ? -nrm : nrm;
-        t_ = make_double2((beta - alpha.x) / beta, -alpha.y / beta);
-        const double2 d = make_double2(alpha.x - beta, alpha.y);
-        const double den = d.x * d.x + d.y * d.y;
-        s_ = make_double2(d.x / den, -d.y / den);
-        b_ = make_double2(beta, 0.0);
-      }
-      sc[0] = t_;
-      sc[1] = s_;
-      taus[i] = t_;
-      if (blockIdx.x == 0) {
-        tau[j0 + i] = t_;
-        betas[j0 + i] = b_;
-      }
-    }
-    __syncthreads();
-    const double2 s_ = sc[1];
-    const int64_t j = j0 + i;
-    for (int64_t t = i + threadIdx.x; t < len; t += ST) {
-      const double2 v = (t == i) ? make_double2(1.0, 0.0) : cmul(x[t], s_);
-      x[t] = v;
-      if (blockIdx.x == 0) V[j * m + j0 + t] = v;
-    }
-    __syncthreads();
-    double2 f = sc[0];
-    f.y = -f.y;  // conj(tau): the factorisation applies H^H
-    for (int cc = i + 1 + wp; cc < ns; cc += ST / 32) {
-      double2* y = P + (int64_t)cc * len;
-      double2 w = make_double2(0.0, 0.0);
-      for (int64_t t = i + lane; t < len; t += 32) w = cfmac(x[t], y[t], w);
-      w = warp_sum2(w);
-      const double2 fw = cmul(f, w);
-      for (int64_t t = i + lane; t < len; t += 32) y[t] = csub(y[t], cmul(x[t], fw));
-    }
-    __syncthreads();
+  const int64_t c = j + 1 + blockIdx.x;
+  double2 w = make_double2(0.0, 0.0);
+  for (int64_t i = j + threadIdx.x; i < m; i += ST) w = cfmac(v[i], A[rowoff[i] + c * cs], w);
+  w = block_sum2(w, red);
+  const double2 fw = cmul(t_, w);
+  for (int64_t i = j + threadIdx.x; i < m; i += ST) {
+    double2* q = A + rowoff[i] + c * cs;
+    *q = csub(*q, cmul(v[i], fw));
   }
-  if (own) {
-    for (int i = 0; i < ns; ++i) {
-      const double2* v = P + (int64_t)i * len;
-      double2 w = make_double2(0.0, 0.0);
-      for (int64_t t = i + threadIdx.x; t < len; t += ST) w = cfmac(v[t], col[t], w);
-      w = block_sum2(w, red);
-      double2 f = taus[i];
-      f.y = -f.y;
-      const double2 fw = cmul(f, w);
-      for (int64_t t = i + threadIdx.x; t < len; t += ST) col[t] = csub(col[t], cmul(v[t], fw));
-      __syncthreads();
-    }
-    for (int64_t t = threadIdx.x; t < len; t += ST) A[rowoff[j0 + t] + c * cs] = col[t];
-  }
-  if (blockIdx.x == 0)
-    for (int64_t e = threadIdx.x; e < ns * len; e += ST) {
-      const int64_t cc = e / len, r = e - cc * len;
-      A[rowoff[j0 + r] + (j0 + cc) * cs] = P[e];
-    }
-}
-
-// Q formation for reflectors jlo..jhi-1 (zung2r order, descending) in one
-// launch: CTA b owns column c = jlo + b (< p). A column c >= jhi receives
-// H_{jhi-1} ... H_{jlo}; a panel column c < jhi is first formed from its own
-// reflector (rows above c zero) and then receives H_{c-1} ... H_{jlo}.
-__global__ void __launch_bounds__(ST) hh_form_multi(double2* __restrict__ A, const int64_t* __restrict__ rowoff,
-                                                    int64_t cs, int64_t m, int64_t jlo, int64_t jhi,
-                                                    const double2* __restrict__ tau,
-                                                    const double2* __restrict__ V) {
-  extern __shared__ double2 col[];  // rows jlo..m-1
-  __shared__ double red[ST / 32 + 1];
-  const int64_t c = jlo + blockIdx.x;
-  const int64_t len = m - jlo;
-  int64_t top;
-  if (c >= jhi) {
-    for (int64_t t = threadIdx.x; t < len; t += ST) col[t] = A[rowoff[jlo + t] + c * cs];
-    top = jhi - 1;
-  } else {
-    const double2 tc = tau[c];
-    const double2* vc = V + c * m;
-    for (int64_t t = threadIdx.x; t < len; t += ST) {
-      const int64_t row = jlo + t;
-      double2 val;
-      if (row < c) val = make_double2(0.0, 0.0);
-      else if (row == c) val = make_double2(1.0 - tc.x, -tc.y);
-      else {
-        const double2 vi = vc[row];
-        val = make_double2(-(tc.x * vi.x - tc.y * vi.y), -(tc.x * vi.y + tc.y * vi.x));
-      }
-      col[t] = val;
-    }
-    top = c - 1;
-  }
-  __syncthreads();
-  for (int64_t j = top; j >= jlo; --j) {
-    const double2 t_ = tau[j];
-    const double2* v = V + j * m;
-    double2 w = make_double2(0.0, 0.0);
-    for (int64_t row = j + threadIdx.x; row < m; row += ST) w = cfmac(v[row], col[row - jlo], w);
-    w = block_sum2(w, red);
-    const double2 fw = cmul(t_, w);
-    for (int64_t row = j + threadIdx.x; row < m; row += ST) col[row - jlo] = csub(col[row - jlo], cmul(v[row], fw));
-    __syncthreads();
-  }
-  for (int64_t t = threadIdx.x; t < len; t += ST) A[rowoff[jlo + t] + c * cs] = col[t];
-  if (c < jhi)
-    for (int64_t r = threadIdx.x; r < jlo; r += ST) A[rowoff[r] + c * cs] = make_double2(0.0, 0.0);
 }
 
 inline unsigned grid1(int64_t n) {
@@ -430,30 +374,16 @@ static int zqr_keep_small(double2* A, const int64_t* rowoff, int64_t m, int64_t 
   double2* betas = tau + k;
   double2* V = betas + k;
   const int64_t p = m < k ? m : k;
-  // reflectors per launch: the panel and one column must fit the smem budget
-  int64_t ns = QR_MULTI_SMEM / (16 * m) - 1;
-  if (ns > QR_MULTI_MAX) ns = QR_MULTI_MAX;
-  if (ns < 1) ns = 1;
-  static bool attr_set = false;
-  if (!attr_set) {
-    if (cudaFuncSetAttribute(hh_fact_multi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)QR_MULTI_SMEM) !=
-        cudaSuccess)
-      return PTN_ERR_LAUNCH;
-    attr_set = true;
-  }
-  for (int64_t j0 = 0; j0 < p; j0 += ns) {
-    const int64_t n_ = p - j0 < ns ? p - j0 : ns;
-    const int64_t ncols = k - j0 - n_;
+  for (int64_t j = 0; j < p; ++j) {
+    const int64_t ncols = k - (j + 1);
     PTN_COUNT(1);
-    hh_fact_multi<<<(unsigned)(ncols > 0 ? ncols : 1), ST, (size_t)(n_ + 1) * (m - j0) * 16, s>>>(
-        A, rowoff, cs, m, k, j0, (int)n_, tau, betas, V);
+    hh_fact_small<<<(unsigned)(ncols > 0 ? ncols : 1), ST, 0, s>>>(A, rowoff, cs, m, k, j, tau, betas, V);
   }
   PTN_COUNT(1);
   extract_r_small<<<grid1(k * k), ST, 0, s>>>(A, rowoff, cs, k, p, betas, R);
-  for (int64_t jhi = p; jhi > 0; jhi -= ns) {
-    const int64_t jlo = jhi - ns > 0 ? jhi - ns : 0;
+  for (int64_t j = p - 1; j >= 0; --j) {
     PTN_COUNT(1);
-    hh_form_multi<<<(unsigned)(p - jlo), ST, (size_t)(m - jlo) * 16, s>>>(A, rowoff, cs, m, jlo, jhi, tau, V);
+    hh_form_small<<<(unsigned)(p - j), ST, 0, s>>>(A, rowoff, cs, m, p, j, tau, V);
   }
   if (p < k) { PTN_COUNT(1); zero_cols_kernel<<<grid1(m * (k - p)), QT, 0, s>>>(A, rowoff, cs, m, k, p); }
   return ptn_launch_status();

@@ -208,6 +208,22 @@ class Clocks:
 
 
 # ----------------------------------------------------------------------------
+# replicas: whole-job rate over ranks
+# ----------------------------------------------------------------------------
+def aggregate_over_ranks(local_ms: float, steps: int, world: int, dist=None, device=None):
+    """Rate of N independent replicas (a TDVP sweep does not shard): every rank
+    advanced ``steps`` sweeps of its own realisation; the job took as long as
+    the slowest rank (all-reduce MAX). Returns (sweeps/s over all ranks, max ms)."""
+    import torch
+    t_max = float(local_ms)
+    if dist is not None and world > 1:
+        t = torch.tensor([t_max], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    return world * steps / (t_max / 1000.0), t_max
+
+
+# ----------------------------------------------------------------------------
 # GPU arm
 # ----------------------------------------------------------------------------
 def run_gb300(args, rank, world):
@@ -277,12 +293,7 @@ def run_gb300(args, rank, world):
     heff_ms = sum(a.elapsed_time(b) for a, b, _ in heff_events)
     heff_flops = sum(f for _, _, f in heff_events)
     n_heff = len(heff_events)
-    t_max = ms
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-    value = world * args.steps / (t_max / 1000.0)
+    value, t_max = aggregate_over_ranks(ms, args.steps, world, dist, "cuda")
 
     # -- end to end: state uploaded from pinned host memory, sweep, state read back
     e2e = None
@@ -304,12 +315,8 @@ def run_gb300(args, rank, world):
                 pinned[nid].copy_(t, non_blocking=True)
             torch.cuda.synchronize()
         w1 = time.perf_counter()
-        e2e_s = w1 - w0
-        if dist:
-            t = torch.tensor([e2e_s], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
-        e2e = {"value": world * args.steps / e2e_s, "unit": "sweeps/s",
+        e2e_value, _ = aggregate_over_ranks((w1 - w0) * 1000.0, args.steps, world, dist, "cuda")
+        e2e = {"value": e2e_value, "unit": "sweeps/s",
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes}
 
     achieved = heff_flops / (heff_ms / 1000.0) / 1e12 if heff_ms > 0 else None

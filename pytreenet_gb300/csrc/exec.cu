@@ -50,10 +50,15 @@ extern "C" int ptn_exec_ops(const ptn_exec_op* ops, int32_t nops, void* const* p
   return PTN_OK;
 }
 
+int ptn_gs_step_passes(const void* Q, int64_t ldq, int32_t nq, void* w, int64_t n, void* h, void* partial,
+                       double* norms, void* qnext, void* stream);
+
 extern "C" int ptn_krylov_gs_step(const void* Q, int64_t ldq, int32_t nq, void* w, int64_t n, void* h,
                                   void* partial, double* norms, void* qnext, void* stream) {
   if (!Q || !w || !h || !partial || !norms || nq < 1 || n < 1 || ldq < n) return PTN_ERR_ARG;
-  int st = ptn_dznrm2(w, n, norms, partial, stream);
+  int st = ptn_gs_step_passes(Q, ldq, nq, w, n, h, partial, norms, qnext, stream);
+  if (st != PTN_ERR_UNSUPPORTED) return st;
+  st = ptn_dznrm2(w, n, norms, partial, stream);
   if (st != PTN_OK) return st;
   double2* h1 = static_cast<double2*>(h);
   double2* h2 = h1 + nq;

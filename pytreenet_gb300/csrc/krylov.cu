@@ -141,7 +141,112 @@ unsigned long long g_ptn_launches = 0;
 
 extern "C" unsigned long long ptn_launch_counter(void) { return g_ptn_launches; }
 
-extern "C" int64_t ptn_krylov_partials(int64_t n) { return nblocks_for(n) * MAXQ; }
+// ---- Gram-Schmidt step in three passes ----------------------------------------------------
+// One pass over w per kernel; each CTA writes fixed-order partial sums, and
+// the last CTA to finish (atomic ticket, no waiting) adds them up in CTA
+// order, so the totals are deterministic. The last CTA also re-arms the
+// ticket for the next pass.
+//   mode 0: (Q^H w, |w|^2)            -> h[0..nq), norms[0] = |w|
+//   mode 1: w -= Q hin, then Q^H w    -> h[nq..2nq)
+//   mode 2: w -= Q hin, then |w|^2    -> norms[1] = |w|
+template <int NQ>
+__global__ void __launch_bounds__(RT) gs_pass_kernel(const double2* __restrict__ Q, int64_t ldq, int nq,
+                                                     double2* __restrict__ w, int64_t n,
+                                                     const double2* __restrict__ hin, double2* __restrict__ hout,
+                                                     double* __restrict__ nout, double2* __restrict__ partial,
+                                                     unsigned* __restrict__ ticket, int mode) {
+  __shared__ double2 hs[NQ];
+  __shared__ double2 red[RT / 32][NQ + 1];
+  __shared__ int last;
+  if (mode != 0 && threadIdx.x < nq) hs[threadIdx.x] = hin[threadIdx.x];
+  __syncthreads();
+  double2 acc[NQ];
+#pragma unroll
+  for (int i = 0; i < NQ; ++i) acc[i] = make_double2(0.0, 0.0);
+  double nacc = 0.0;
+  for (int64_t x = blockIdx.x * (int64_t)RT + threadIdx.x; x < n; x += (int64_t)gridDim.x * RT) {
+    double2 wv = w[x];
+    if (mode != 0) {
+      for (int i = 0; i < nq; ++i) wv = csub(wv, cmul(hs[i], Q[(int64_t)i * ldq + x]));
+      w[x] = wv;
+    }
+    if (mode != 2) {
+#pragma unroll
+      for (int i = 0; i < NQ; ++i)
+        if (i < nq) acc[i] = cfmac(Q[(int64_t)i * ldq + x], wv, acc[i]);
+    }
+    if (mode != 1) nacc += cabs2(wv);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < NQ; ++i) {
+    if (i >= nq) break;
+    const double2 v = warp_sum2(acc[i]);
+    if (lane == 0) red[warp][i] = v;
+  }
+  {
+    const double v = warp_sum(nacc);
+    if (lane == 0) red[warp][NQ] = make_double2(v, 0.0);
+  }
+  __syncthreads();
+  double2* mine = partial + (int64_t)blockIdx.x * (NQ + 1);
+  if (threadIdx.x < nq || threadIdx.x == NQ) {
+    double2 t = make_double2(0.0, 0.0);
+    for (int u = 0; u < RT / 32; ++u) t = cadd(t, red[u][threadIdx.x]);
+    mine[threadIdx.x] = t;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  if (threadIdx.x < nq || threadIdx.x == NQ) {
+    double2 t = make_double2(0.0, 0.0);
+    for (unsigned b = 0; b < gridDim.x; ++b) t = cadd(t, __ldcg(partial + (int64_t)b * (NQ + 1) + threadIdx.x));
+    if (threadIdx.x == NQ) {
+      if (mode != 1) nout[0] = sqrt(t.x);
+    } else if (mode != 2) {
+      hout[threadIdx.x] = t;
+    }
+  }
+  if (threadIdx.x == 0) *ticket = 0u;
+}
+
+template <int NQ>
+static int gs_step_passes(const double2* Q, int64_t ldq, int nq, double2* w, int64_t n, double2* h,
+                          double2* partial, double* norms, double2* qnext, cudaStream_t s) {
+  const int nb = (int)nblocks_for(n);
+  unsigned* ticket = reinterpret_cast<unsigned*>(partial + (int64_t)nb * (NQ + 1));
+  if (cudaMemsetAsync(ticket, 0, sizeof(unsigned), s) != cudaSuccess) return PTN_ERR_LAUNCH;
+  PTN_COUNT(3);
+  gs_pass_kernel<NQ><<<nb, RT, 0, s>>>(Q, ldq, nq, w, n, nullptr, h, norms, partial, ticket, 0);
+  gs_pass_kernel<NQ><<<nb, RT, 0, s>>>(Q, ldq, nq, w, n, h, h + nq, nullptr, partial, ticket, 1);
+  gs_pass_kernel<NQ><<<nb, RT, 0, s>>>(Q, ldq, nq, w, n, h + nq, nullptr, norms + 1, partial, ticket, 2);
+  if (qnext) {
+    PTN_COUNT(1);
+    zscal_inv_kernel<<<(int)nblocks_for(n), RT, 0, s>>>(w, norms + 1, qnext, n);
+  }
+  return ptn_launch_status();
+}
+
+// The Gram-Schmidt step as three passes for nq <= MAXQ (PTN_ERR_UNSUPPORTED
+// otherwise, and the caller runs the kernels one by one).
+int ptn_gs_step_passes(const void* Q, int64_t ldq, int32_t nq, void* w, int64_t n, void* h, void* partial,
+                       double* norms, void* qnext, void* stream) {
+  const double2* q = static_cast<const double2*>(Q);
+  double2* wv = static_cast<double2*>(w);
+  double2* hv = static_cast<double2*>(h);
+  double2* pv = static_cast<double2*>(partial);
+  double2* qn = static_cast<double2*>(qnext);
+  cudaStream_t s = ptn_stream(stream);
+  if (nq <= 4) return gs_step_passes<4>(q, ldq, nq, wv, n, hv, pv, norms, qn, s);
+  if (nq <= 8) return gs_step_passes<8>(q, ldq, nq, wv, n, hv, pv, norms, qn, s);
+  if (nq <= MAXQ) return gs_step_passes<MAXQ>(q, ldq, nq, wv, n, hv, pv, norms, qn, s);
+  return PTN_ERR_UNSUPPORTED;
+}
+
+extern "C" int64_t ptn_krylov_partials(int64_t n) { return nblocks_for(n) * (MAXQ + 1) + 16; }
 
 extern "C" int ptn_zdot_multi(const void* Q, int64_t ldq, int32_t nq, const void* w, int64_t n,
                               void* h, int32_t accumulate, void* partial, void* stream) {

@@ -12,7 +12,7 @@ namespace {
 
 constexpr int RT = 256;        // threads per CTA
 constexpr int MAXQ = 16;       // vectors per multi-dot launch
-constexpr int64_t CHUNK = 4096;
+constexpr int64_t CHUNK = 1024;   // elements per CTA: enough CTAs to keep HBM busy on 131k-entry vectors
 
 inline int64_t nblocks_for(int64_t n) {
   int64_t b = (n + CHUNK - 1) / CHUNK;

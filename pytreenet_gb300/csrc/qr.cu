@@ -222,46 +222,51 @@ __global__ void zero_cols_kernel(double2* __restrict__ A, const int64_t* __restr
 // update). The reflectors go to a separate V buffer and the diagonal of R to
 // `betas`, so no CTA writes what another reads in the same launch.
 constexpr int64_t QR_SMALL_M = 2048;
+constexpr int64_t QR_WARP_M = 512;
 constexpr int ST = 256;
 
+template <int NTH>
 __device__ __forceinline__ double block_sum(double v, double* red) {
   v = warp_sum(v);
+  if (NTH == 32) return v;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   if (lane == 0) red[w] = v;
   __syncthreads();
   double s = 0.0;
   if (threadIdx.x == 0) {
-    for (int i = 0; i < ST / 32; ++i) s += red[i];
-    red[ST / 32] = s;
+    for (int i = 0; i < NTH / 32; ++i) s += red[i];
+    red[NTH / 32] = s;
   }
   __syncthreads();
-  s = red[ST / 32];
+  s = red[NTH / 32];
   __syncthreads();
   return s;
 }
 
+template <int NTH>
 __device__ __forceinline__ double2 block_sum2(double2 v, double* red) {
-  double re = block_sum(v.x, red);
-  double im = block_sum(v.y, red);
+  double re = block_sum<NTH>(v.x, red);
+  double im = block_sum<NTH>(v.y, red);
   return make_double2(re, im);
 }
 
 // Step j of the factorisation. grid = max(1, k - j - 1); CTA b owns column j+1+b.
-__global__ void __launch_bounds__(ST) hh_fact_small(double2* __restrict__ A, const int64_t* __restrict__ rowoff,
+template <int NTH>
+__global__ void __launch_bounds__(NTH) hh_fact_small(double2* __restrict__ A, const int64_t* __restrict__ rowoff,
                                                     int64_t cs, int64_t m, int64_t k, int64_t j,
                                                     double2* __restrict__ tau, double2* __restrict__ betas,
                                                     double2* __restrict__ V) {
   __shared__ double2 vs[QR_SMALL_M];
-  __shared__ double red[ST / 32 + 1];
+  __shared__ double red[NTH / 32 + 1];
   __shared__ double2 sc[3];  // tau, scal, w
   const int64_t len = m - j;
   double acc = 0.0;
-  for (int64_t t = threadIdx.x; t < len; t += ST) {
+  for (int64_t t = threadIdx.x; t < len; t += NTH) {
     const double2 a = A[rowoff[j + t] + j * cs];
     vs[t] = a;
     if (t > 0) acc += cabs2(a);
   }
-  const double xn2 = block_sum(acc, red);
+  const double xn2 = block_sum<NTH>(acc, red);
   if (threadIdx.x == 0) {
     const double2 alpha = vs[0];
     const double xnorm = sqrt(xn2);
@@ -288,7 +293,7 @@ __global__ void __launch_bounds__(ST) hh_fact_small(double2* __restrict__ A, con
   }
   __syncthreads();
   const double2 s_ = sc[1];
-  for (int64_t t = threadIdx.x; t < len; t += ST) {
+  for (int64_t t = threadIdx.x; t < len; t += NTH) {
     const double2 v = (t == 0) ? make_double2(1.0, 0.0) : cmul(vs[t], s_);
     vs[t] = v;
     if (blockIdx.x == 0) V[j * m + j + t] = v;
@@ -297,12 +302,12 @@ __global__ void __launch_bounds__(ST) hh_fact_small(double2* __restrict__ A, con
   const int64_t c = j + 1 + blockIdx.x;
   if (c >= k) return;
   double2 w = make_double2(0.0, 0.0);
-  for (int64_t t = threadIdx.x; t < len; t += ST) w = cfmac(vs[t], A[rowoff[j + t] + c * cs], w);
-  w = block_sum2(w, red);
+  for (int64_t t = threadIdx.x; t < len; t += NTH) w = cfmac(vs[t], A[rowoff[j + t] + c * cs], w);
+  w = block_sum2<NTH>(w, red);
   double2 f = sc[0];
   f.y = -f.y;  // conj(tau): the factorisation applies H^H
   const double2 fw = cmul(f, w);
-  for (int64_t t = threadIdx.x; t < len; t += ST) {
+  for (int64_t t = threadIdx.x; t < len; t += NTH) {
     double2* p = A + rowoff[j + t] + c * cs;
     *p = csub(*p, cmul(vs[t], fw));
   }
@@ -324,15 +329,16 @@ __global__ void extract_r_small(const double2* __restrict__ A, const int64_t* __
 
 // Step j of forming Q (zung2r): CTAs 0..ncols-1 apply H_j to columns j+1..p-1,
 // CTA ncols writes column j itself.
-__global__ void __launch_bounds__(ST) hh_form_small(double2* __restrict__ A, const int64_t* __restrict__ rowoff,
+template <int NTH>
+__global__ void __launch_bounds__(NTH) hh_form_small(double2* __restrict__ A, const int64_t* __restrict__ rowoff,
                                                     int64_t cs, int64_t m, int64_t p, int64_t j,
                                                     const double2* __restrict__ tau, const double2* __restrict__ V) {
-  __shared__ double red[ST / 32 + 1];
+  __shared__ double red[NTH / 32 + 1];
   const int64_t ncols = p - (j + 1);
   const double2 t_ = tau[j];
   const double2* v = V + j * m;
   if (blockIdx.x == ncols) {
-    for (int64_t i = threadIdx.x; i < m; i += ST) {
+    for (int64_t i = threadIdx.x; i < m; i += NTH) {
       double2* q = A + rowoff[i] + j * cs;
       if (i < j) *q = make_double2(0.0, 0.0);
       else if (i == j) *q = make_double2(1.0 - t_.x, -t_.y);
@@ -342,10 +348,10 @@ __global__ void __launch_bounds__(ST) hh_form_small(double2* __restrict__ A, con
   }
   const int64_t c = j + 1 + blockIdx.x;
   double2 w = make_double2(0.0, 0.0);
-  for (int64_t i = j + threadIdx.x; i < m; i += ST) w = cfmac(v[i], A[rowoff[i] + c * cs], w);
-  w = block_sum2(w, red);
+  for (int64_t i = j + threadIdx.x; i < m; i += NTH) w = cfmac(v[i], A[rowoff[i] + c * cs], w);
+  w = block_sum2<NTH>(w, red);
   const double2 fw = cmul(t_, w);
-  for (int64_t i = j + threadIdx.x; i < m; i += ST) {
+  for (int64_t i = j + threadIdx.x; i < m; i += NTH) {
     double2* q = A + rowoff[i] + c * cs;
     *q = csub(*q, cmul(v[i], fw));
   }
@@ -374,16 +380,21 @@ static int zqr_keep_small(double2* A, const int64_t* rowoff, int64_t m, int64_t 
   double2* betas = tau + k;
   double2* V = betas + k;
   const int64_t p = m < k ? m : k;
+  // up to QR_WARP_M rows a single warp per column: no CTA barriers per step
+  const bool warp_cta = m <= QR_WARP_M;
   for (int64_t j = 0; j < p; ++j) {
     const int64_t ncols = k - (j + 1);
+    const unsigned g = (unsigned)(ncols > 0 ? ncols : 1);
     PTN_COUNT(1);
-    hh_fact_small<<<(unsigned)(ncols > 0 ? ncols : 1), ST, 0, s>>>(A, rowoff, cs, m, k, j, tau, betas, V);
+    if (warp_cta) hh_fact_small<32><<<g, 32, 0, s>>>(A, rowoff, cs, m, k, j, tau, betas, V);
+    else hh_fact_small<ST><<<g, ST, 0, s>>>(A, rowoff, cs, m, k, j, tau, betas, V);
   }
   PTN_COUNT(1);
   extract_r_small<<<grid1(k * k), ST, 0, s>>>(A, rowoff, cs, k, p, betas, R);
   for (int64_t j = p - 1; j >= 0; --j) {
     PTN_COUNT(1);
-    hh_form_small<<<(unsigned)(p - j), ST, 0, s>>>(A, rowoff, cs, m, p, j, tau, V);
+    if (warp_cta) hh_form_small<32><<<(unsigned)(p - j), 32, 0, s>>>(A, rowoff, cs, m, p, j, tau, V);
+    else hh_form_small<ST><<<(unsigned)(p - j), ST, 0, s>>>(A, rowoff, cs, m, p, j, tau, V);
   }
   if (p < k) { PTN_COUNT(1); zero_cols_kernel<<<grid1(m * (k - p)), QT, 0, s>>>(A, rowoff, cs, m, k, p); }
   return ptn_launch_status();

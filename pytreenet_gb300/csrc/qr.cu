@@ -222,7 +222,6 @@ __global__ void zero_cols_kernel(double2* __restrict__ A, const int64_t* __restr
 // update). The reflectors go to a separate V buffer and the diagonal of R to
 // `betas`, so no CTA writes what another reads in the same launch.
 constexpr int64_t QR_SMALL_M = 2048;
-constexpr int64_t QR_WARP_M = 512;
 constexpr int ST = 256;
 
 template <int NTH>
@@ -380,21 +379,17 @@ static int zqr_keep_small(double2* A, const int64_t* rowoff, int64_t m, int64_t 
   double2* betas = tau + k;
   double2* V = betas + k;
   const int64_t p = m < k ? m : k;
-  // up to QR_WARP_M rows a single warp per column: no CTA barriers per step
-  const bool warp_cta = m <= QR_WARP_M;
+  // (one warp per column measured slower than 256 threads at 512 x 256: 6.8 vs 4.2 ms)
   for (int64_t j = 0; j < p; ++j) {
     const int64_t ncols = k - (j + 1);
-    const unsigned g = (unsigned)(ncols > 0 ? ncols : 1);
     PTN_COUNT(1);
-    if (warp_cta) hh_fact_small<32><<<g, 32, 0, s>>>(A, rowoff, cs, m, k, j, tau, betas, V);
-    else hh_fact_small<ST><<<g, ST, 0, s>>>(A, rowoff, cs, m, k, j, tau, betas, V);
+    hh_fact_small<ST><<<(unsigned)(ncols > 0 ? ncols : 1), ST, 0, s>>>(A, rowoff, cs, m, k, j, tau, betas, V);
   }
   PTN_COUNT(1);
   extract_r_small<<<grid1(k * k), ST, 0, s>>>(A, rowoff, cs, k, p, betas, R);
   for (int64_t j = p - 1; j >= 0; --j) {
     PTN_COUNT(1);
-    if (warp_cta) hh_form_small<32><<<(unsigned)(p - j), 32, 0, s>>>(A, rowoff, cs, m, p, j, tau, V);
-    else hh_form_small<ST><<<(unsigned)(p - j), ST, 0, s>>>(A, rowoff, cs, m, p, j, tau, V);
+    hh_form_small<ST><<<(unsigned)(p - j), ST, 0, s>>>(A, rowoff, cs, m, p, j, tau, V);
   }
   if (p < k) { PTN_COUNT(1); zero_cols_kernel<<<grid1(m * (k - p)), QT, 0, s>>>(A, rowoff, cs, m, k, p); }
   return ptn_launch_status();

@@ -313,6 +313,9 @@ class TwoSiteTDVP(OneSiteTDVP):
             raise ValueError("Two-site TDVP cannot be used for systems with less than 2 sites!")
         if not hasattr(self.config, "max_bond_dim"):
             raise TypeError("two-site TDVP needs a TwoSiteTDVPConfig (truncation parameters)")
+        # bond dimensions change from step to step, so captured QR launch
+        # sequences would mostly be captured once and dropped: launch eagerly
+        self.net.use_graphs = False
         self.bond_dims_history: list[int] = []
 
     def _update_two_site_nodes(self, target_node_id, next_node_id, time_step_factor=1.0):

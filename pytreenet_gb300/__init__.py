@@ -14,6 +14,7 @@ from .tdvp import (TimeEvoMode, EvoDirection, PathFinderMode, TDVPConfig, Tensor
 from .truncation import SVDParameters, truncate_singular_values
 from .tebd import TEBD, TrotterStep, TrotterSplitting, NumericOperator
 from .operators import nearest_neighbour_ttno, tfim_ttno, heisenberg_ttno
+from .batch import run_realisations
 
 __all__ = [
     "Node", "TreeTensorNetworkState", "TreeTensorNetworkOperator", "TTNS", "TTNO",
@@ -22,5 +23,5 @@ __all__ = [
     "TwoSiteTDVPConfig", "FirstOrderTwoSiteTDVP", "SecondOrderTwoSiteTDVP",
     "SVDParameters", "truncate_singular_values", "TEBD", "TrotterStep", "TrotterSplitting",
     "NumericOperator",
-    "nearest_neighbour_ttno", "tfim_ttno", "heisenberg_ttno",
+    "nearest_neighbour_ttno", "tfim_ttno", "heisenberg_ttno", "run_realisations",
 ]

@@ -269,15 +269,16 @@ __global__ void __launch_bounds__(THREADS, 1)
 // cuTensorMapEncodeTiled is fetched through the runtime's driver entry point so
 // the library does not link libcuda (it still loads on a machine without a driver).
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  if (!fn) {
+  // initialised once, thread-safe (C++11 static initialisation)
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
     void* p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
             cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-  }
+      return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    return nullptr;
+  }();
   return fn;
 }
 
@@ -384,13 +385,10 @@ extern "C" int ptn_cgemm_smem_bytes(int32_t levels) { return levels == 3 ? Cfg<3
 
 template <int L>
 int launch_gemm(const CUtensorMap& ta, const CUtensorMap& tb, const GemmArgs& g, unsigned grid, cudaStream_t st) {
-  static bool attr_set = false;
-  if (!attr_set) {
-    if (cudaFuncSetAttribute(cgemm_bf16_kernel<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg<L>::SMEM) !=
-        cudaSuccess)
-      return PTN_ERR_LAUNCH;
-    attr_set = true;
-  }
+  // once per process, thread-safe; a failure is returned on every call
+  static const cudaError_t attr =
+      cudaFuncSetAttribute(cgemm_bf16_kernel<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg<L>::SMEM);
+  if (attr != cudaSuccess) return PTN_ERR_LAUNCH;
   PTN_COUNT(1);
   cgemm_bf16_kernel<L><<<grid, THREADS, Cfg<L>::SMEM, st>>>(ta, tb, g);
   return ptn_launch_status();

@@ -137,9 +137,9 @@ __global__ void check_finite_kernel(const double* __restrict__ x, int64_t n2, in
 
 }  // namespace
 
-unsigned long long g_ptn_launches = 0;
+std::atomic<unsigned long long> g_ptn_launches{0};
 
-extern "C" unsigned long long ptn_launch_counter(void) { return g_ptn_launches; }
+extern "C" unsigned long long ptn_launch_counter(void) { return g_ptn_launches.load(); }
 
 // ---- Gram-Schmidt step in three passes ----------------------------------------------------
 // One pass over w per kernel; each CTA writes fixed-order partial sums, and

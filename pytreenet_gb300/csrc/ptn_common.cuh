@@ -31,9 +31,12 @@ PTN_HD double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
 PTN_HD double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
 PTN_HD double cabs2(double2 a) { return fma(a.x, a.x, a.y * a.y); }
 
-// Host-side count of kernel launches issued by this library (ptn_launch_counter).
-extern unsigned long long g_ptn_launches;
-#define PTN_COUNT(n) (g_ptn_launches += (unsigned long long)(n))
+// Host-side count of kernel launches issued by this library (ptn_launch_counter);
+// atomic because independent realisations may drive the library from several
+// host threads.
+#include <atomic>
+extern std::atomic<unsigned long long> g_ptn_launches;
+#define PTN_COUNT(n) (g_ptn_launches.fetch_add((unsigned long long)(n), std::memory_order_relaxed))
 
 static inline int ptn_launch_status() {
   cudaError_t e = cudaGetLastError();

@@ -182,3 +182,25 @@ def ternary_saturated_state(depth: int = 3, chi: int = 64, seed: int = 0):
         t = rng.normal(size=shape) + 1j * rng.normal(size=shape)
         tensors[nid] = t / np.linalg.norm(t)
     return _build(spec, tensors), spec, tensors
+
+
+def binary_neel_random_field(n: int = 31, seed: int = 0, h: float = 2.0):
+    """Heap-ordered binary tree of ``n`` sites, Neel product state by depth
+    parity (every bond of dimension 1), Heisenberg couplings (Jxy = Jz = 1) and
+    random fields h_i ~ U[-h, h]. Returns (TTNS, TTNO, spec, tensors, W)."""
+    rng = np.random.default_rng(seed)
+    spec = binary_tree_spec(n)
+    nkids = {nid: 0 for nid, _ in spec}
+    depth = {}
+    for nid, p in spec:
+        depth[nid] = 0 if p is None else depth[p] + 1
+        if p is not None:
+            nkids[p] += 1
+    tensors = {}
+    for nid, p in spec:
+        v = np.array([1, 0], dtype=complex) if depth[nid] % 2 == 0 else np.array([0, 1], dtype=complex)
+        tensors[nid] = v.reshape([1] * (nkids[nid] + (0 if p is None else 1)) + [2])
+    st = _build(spec, tensors)
+    fields = {nid: rng.uniform(-h, h) for nid, _ in spec}
+    H = heisenberg_ttno(st, fields)
+    return st, H, spec, tensors, {nid: H.phys(nid) for nid in st._order}

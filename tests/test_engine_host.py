@@ -283,3 +283,27 @@ def test_engine_host_ttno_expectation(monkeypatch):
                                        config=P.TDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV))
         e = algo.evaluate_operator(H)
         assert abs(e - c["energy_final"]) < 1e-11 * max(1.0, abs(c["energy_final"]))
+
+
+def test_engine_host_realisations_concurrent_equals_sequential(monkeypatch):
+    """Independent realisations run by several worker threads give exactly the
+    results of running them one after the other."""
+    fake_ptn.install(monkeypatch)
+    import pytreenet_gb300 as P
+    from pytreenet_gb300.workloads import binary_neel_random_field
+
+    def make(i):
+        st, H, spec, _, _ = binary_neel_random_field(n=7, seed=i)
+        cfg = P.TwoSiteTDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV, max_bond_dim=4, rel_tol=1e-9,
+                                  total_tol=1e-9)
+        return P.SecondOrderTwoSiteTDVP(st, H, 0.05, 1.0, {}, config=cfg, solver_options={"krylov_tol": 1e-10})
+
+    def done(i, algo):
+        return (list(algo.bond_dims_history), {nid: algo.state.get_phys_numpy(nid).copy() for nid in algo.state._order})
+    seq = P.run_realisations(make, 5, 2, workers=1, on_done=done)
+    par = P.run_realisations(make, 5, 2, workers=3, on_done=done)
+    for (h1, s1), (h2, s2) in zip(seq, par):
+        assert h1 == h2
+        for nid in s1:
+            np.testing.assert_array_equal(s1[nid], s2[nid])
+    assert seq[0][0] != seq[1][0] or any(not np.array_equal(seq[0][1][k], seq[1][1][k]) for k in seq[0][1])

@@ -2,12 +2,13 @@
 
 A disorder average (for example many random-field realisations of a tree
 Hamiltonian) is a set of independent time evolutions. ``run_realisations``
-advances them concurrently: each worker thread owns a CUDA stream and a share
-of the realisations, builds their drivers on that stream and steps them. The
-library's foreign calls and the drivers' stream synchronisations release the
-interpreter lock, so one realisation's GPU work overlaps another's host-side
-work and the GPU is shared by several small problems at once. Realisations
-never exchange data.
+advances them with several worker threads: each owns a CUDA stream and a share
+of the realisations, builds their drivers on that stream and steps them.
+Realisations never exchange data. The library's foreign calls and the stream
+synchronisations release the interpreter lock, so GPU work of one realisation
+can overlap host work of another; when the drivers' Python work dominates
+(small trees), the interpreter lock serialises the workers and they run no
+faster than one.
 """
 from __future__ import annotations
 

@@ -181,6 +181,136 @@ __global__ void __launch_bounds__(SVD_THREADS) zsvd_jacobi_kernel(SvdArgs a) {
   }
 }
 
+// ---- small matrices: one CTA, everything in shared memory --------------------------------
+// For n <= SVD_SMALL_N columns and m <= SVD_SMALL_M rows the same sweeps run in
+// one CTA with CTA barriers between rounds (no cooperative launch, no global
+// traffic). Same pair schedule, rotation formula, thresholds and ordering as
+// the kernel above, one warp per pair, so the results are the same bit for bit.
+constexpr int64_t SVD_SMALL_N = 32, SVD_SMALL_M = 256;
+constexpr int SVD_SMALL_THREADS = 256;
+
+__device__ bool rotate_pair_smem(double2* A, double2* V, int64_t m, int64_t n, int64_t i, int64_t j, double tol,
+                                 double zero2, int lane) {
+  double2* ci = A + i * m;
+  double2* cj = A + j * m;
+  double al = 0.0, be = 0.0;
+  double2 ga = make_double2(0.0, 0.0);
+  for (int64_t k = lane; k < m; k += 32) {
+    const double2 x = ci[k], y = cj[k];
+    al += cabs2(x);
+    be += cabs2(y);
+    ga = cfmac(x, y, ga);
+  }
+  al = warp_sum(al);
+  be = warp_sum(be);
+  ga = warp_sum2(ga);
+  if (al <= zero2 || be <= zero2) return false;
+  const double g = hypot(ga.x, ga.y);
+  if (!(g > tol * sqrt(al) * sqrt(be))) return false;
+  const double zeta = (be - al) / (2.0 * g);
+  double t;
+  if (fabs(zeta) > 1e150) {
+    t = 0.5 / zeta;
+  } else {
+    t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+  }
+  const double c = 1.0 / sqrt(1.0 + t * t);
+  const double s = c * t;
+  const double2 e = make_double2(ga.x / g, ga.y / g);
+  const double2 s_em = make_double2(s * e.x, -s * e.y);
+  const double2 s_ep = make_double2(s * e.x, s * e.y);
+  for (int64_t k = lane; k < m; k += 32) {
+    const double2 x = ci[k], y = cj[k];
+    ci[k] = csub(cscale(x, c), cmul(s_em, y));
+    cj[k] = cadd(cmul(s_ep, x), cscale(y, c));
+  }
+  double2* vi = V + i * n;
+  double2* vj = V + j * n;
+  for (int64_t k = lane; k < n; k += 32) {
+    const double2 x = vi[k], y = vj[k];
+    vi[k] = csub(cscale(x, c), cmul(s_em, y));
+    vj[k] = cadd(cmul(s_ep, x), cscale(y, c));
+  }
+  return true;
+}
+
+__global__ void __launch_bounds__(SVD_SMALL_THREADS) zsvd_jacobi_small_kernel(SvdArgs a) {
+  extern __shared__ double2 sm[];
+  __shared__ double sig[SVD_SMALL_N];
+  __shared__ unsigned rot;
+  __shared__ double amax2s;
+  const int64_t m = a.m, n = a.n;
+  double2* A = sm;
+  double2* V = sm + m * n;
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  constexpr int NW = SVD_SMALL_THREADS / 32;
+  for (int64_t e = threadIdx.x; e < m * n; e += SVD_SMALL_THREADS) {
+    const int64_t i = e % m, j = e / m;
+    A[e] = a.src[i * a.rs + j * a.cs];
+  }
+  for (int64_t e = threadIdx.x; e < n * n; e += SVD_SMALL_THREADS) {
+    const int64_t i = e % n, j = e / n;
+    V[e] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+  }
+  __syncthreads();
+  for (int64_t j = wp; j < n; j += NW) {
+    double s2 = 0.0;
+    for (int64_t k = lane; k < m; k += 32) s2 += cabs2(A[j * m + k]);
+    s2 = warp_sum(s2);
+    if (lane == 0) sig[j] = s2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double mx = 0.0;
+    for (int64_t j = 0; j < n; ++j) mx = sig[j] > mx ? sig[j] : mx;
+    amax2s = mx;
+  }
+  __syncthreads();
+  const double zero2 = a.tol * a.tol * amax2s;
+  const int64_t np = (n + 1) & ~int64_t(1);
+  bool converged = (n < 2);
+  int sweep = 0;
+  for (; sweep < SVD_MAX_SWEEPS && !converged; ++sweep) {
+    if (threadIdx.x == 0) rot = 0u;
+    __syncthreads();
+    for (int64_t r = 0; r + 1 < np; ++r) {
+      for (int64_t p = wp; p < np / 2; p += NW) {
+        const int64_t x = p, y = np - 1 - p;
+        const int64_t i = (x == 0) ? 0 : 1 + (x - 1 + r) % (np - 1);
+        const int64_t j = 1 + (y - 1 + r) % (np - 1);
+        if (i >= n || j >= n) continue;
+        const bool did = rotate_pair_smem(A, V, m, n, i < j ? i : j, i < j ? j : i, a.tol, zero2, lane);
+        if (did && lane == 0) atomicAdd(&rot, 1u);
+      }
+      __syncthreads();
+    }
+    converged = (rot == 0u);
+    __syncthreads();
+  }
+  if (!converged && threadIdx.x == 0) atomicCAS(a.status, 0, PTN_ERR_NOCONVERGE);
+  for (int64_t j = wp; j < n; j += NW) {
+    double s2 = 0.0;
+    for (int64_t k = lane; k < m; k += 32) s2 += cabs2(A[j * m + k]);
+    s2 = warp_sum(s2);
+    if (lane == 0) sig[j] = sqrt(s2);
+  }
+  __syncthreads();
+  for (int64_t j = wp; j < n; j += NW) {
+    const double sj = sig[j];
+    int64_t cnt = 0;
+    for (int64_t i = lane; i < n; i += 32) {
+      const double si = sig[i];
+      cnt += (si > sj || (si == sj && i < j)) ? 1 : 0;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    const double inv = sj > 0.0 ? 1.0 / sj : 0.0;
+    for (int64_t k = lane; k < m; k += 32) a.U[cnt * a.ldu + k] = cscale(A[j * m + k], inv);
+    for (int64_t k = lane; k < n; k += 32) a.V[cnt * a.ldv + k] = V[j * n + k];
+    if (lane == 0) a.S[cnt] = sj;
+  }
+}
+
 int g_svd_max_blocks[64] = {0};
 std::mutex g_svd_mutex;
 
@@ -230,8 +360,6 @@ extern "C" int64_t ptn_zsvd_work_bytes(int64_t m, int64_t n) {
 extern "C" int ptn_zsvd_jacobi(const ptn_svd_desc* d, void* stream) {
   if (!d || !d->A || !d->U || !d->S || !d->V || !d->work || !d->status) return PTN_ERR_ARG;
   if (d->n < 1 || d->m < d->n || d->ldu < d->m || d->ldv < d->n) return PTN_ERR_ARG;
-  const int maxb = svd_max_blocks();
-  if (maxb <= 0) return PTN_ERR_LAUNCH;
   SvdArgs a;
   a.src = static_cast<const double2*>(d->A);
   a.rs = d->row_stride;
@@ -254,6 +382,18 @@ extern "C" int ptn_zsvd_jacobi(const ptn_svd_desc* d, void* stream) {
   a.tol = 8.0 * sqrt((double)d->m) * 1.1102230246251565e-16;
   a.status = d->status;
   cudaStream_t s = ptn_stream(stream);
+  if (d->n <= SVD_SMALL_N && d->m <= SVD_SMALL_M) {
+    static const cudaError_t attr = cudaFuncSetAttribute(
+        zsvd_jacobi_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (int)((SVD_SMALL_M * SVD_SMALL_N + SVD_SMALL_N * SVD_SMALL_N) * sizeof(double2)));
+    if (attr != cudaSuccess) return PTN_ERR_LAUNCH;
+    const size_t smem = (size_t)(d->m * d->n + d->n * d->n) * sizeof(double2);
+    PTN_COUNT(1);
+    zsvd_jacobi_small_kernel<<<1, SVD_SMALL_THREADS, smem, s>>>(a);
+    return ptn_launch_status();
+  }
+  const int maxb = svd_max_blocks();
+  if (maxb <= 0) return PTN_ERR_LAUNCH;
   if (cudaMemsetAsync(a.ctrl, 0, CTRL_BYTES, s) != cudaSuccess) return PTN_ERR_LAUNCH;
   const int64_t pairs = (((d->n + 1) & ~int64_t(1)) / 2);
   int64_t blocks = (pairs + SVD_WARPS - 1) / SVD_WARPS;

@@ -53,7 +53,8 @@ def _graded(rng, m, n, rank=None, spread=1e-12):
 @pytest.mark.parametrize("m,n,rank,spread,transpose", [
     (1, 1, None, 1.0, False), (7, 5, None, 1e-3, False), (64, 64, None, 1e-12, False),
     (200, 37, None, 1e-10, True), (96, 96, 10, 1e-6, False), (513, 129, None, 1e-13, False),
-    (300, 256, None, 1e-9, True)])
+    (300, 256, None, 1e-9, True), (256, 32, None, 1e-11, False), (100, 20, 6, 1e-8, True),
+    (257, 32, None, 1e-6, False), (40, 33, None, 1e-6, False)])
 def test_jacobi_svd_matches_lapack(m, n, rank, spread, transpose):
     rng = np.random.default_rng(m * 1000 + n)
     A, s_true = _graded(rng, m, n, rank, spread)

@@ -31,7 +31,9 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "TDVP sweeps/sec at chi=256 (one-site, 61-site T-tree, Heisenberg+fields)"
+def metric_name(args) -> str:
+    return (f"TDVP sweeps/sec at chi={args.chi} (one-site, {3 * args.arm + 1}-site T-tree, "
+            "Heisenberg+fields)")
 FP64_NOMINAL_TFLOPS = 1.25
 
 
@@ -345,7 +347,7 @@ def run_gb300(args, rank, world):
     if args.precision == "mixed" and not args.no_plain and rank == 0:
         plain = compare_with_plain(args, make)
         plain["speedup_mixed_over_plain"] = value / plain["sweeps_per_s"]
-    line = {"metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": world, "steps": args.steps,
+    line = {"metric": metric_name(args), "value": value, "unit": "sweeps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
             "dtype": "bf16x6 split (tcgen05, fp32 accumulate) contractions / f64 Krylov+QR" if args.precision == "mixed" else "c128 (fp64)",
@@ -404,7 +406,7 @@ def run_reference(args, rank, world):
           "sample": (f"NumPy oracle restatement of the reference algorithm; each step times one heff "
                      f"matvec, env update and QR per node degree at chi={args.chi} and weights them by "
                      f"one sweep's operation counts")}
-    return {"metric": METRIC, "value": v, "unit": "sweeps/s", "n_gpus": world, "steps": args.steps,
+    return {"metric": metric_name(args), "value": v, "unit": "sweeps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c128 (fp64)", "data": "synthetic",
             "config": config(args, "plain complex128 (CPU)"), "impl": "reference", "cpu_baseline": cb,

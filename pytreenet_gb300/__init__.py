@@ -15,6 +15,8 @@ from .truncation import SVDParameters, truncate_singular_values
 from .tebd import TEBD, TrotterStep, TrotterSplitting, NumericOperator
 from .operators import nearest_neighbour_ttno, tfim_ttno, heisenberg_ttno
 from .batch import run_realisations
+from .contractions import (SandwichCache, contract_ket_ham_with_envs, contract_any,
+                           effective_single_site_evolution)
 
 __all__ = [
     "Node", "TreeTensorNetworkState", "TreeTensorNetworkOperator", "TTNS", "TTNO",
@@ -24,4 +26,5 @@ __all__ = [
     "SVDParameters", "truncate_singular_values", "TEBD", "TrotterStep", "TrotterSplitting",
     "NumericOperator",
     "nearest_neighbour_ttno", "tfim_ttno", "heisenberg_ttno", "run_realisations",
+    "SandwichCache", "contract_ket_ham_with_envs", "contract_any", "effective_single_site_evolution",
 ]

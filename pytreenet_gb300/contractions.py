@@ -1,0 +1,126 @@
+"""PyTreeNet's contraction helpers on the GPU engine.
+
+Drop-in counterparts of the helpers a PyTreeNet user composes into custom
+algorithms: ``SandwichCache`` (``contractions/sandwich_caching.py:14-126``),
+``contract_ket_ham_with_envs`` (``contractions/state_operator_contraction.py:227-273``),
+``contract_any`` (``:407-461``) and ``effective_single_site_evolution``
+(``time_evolution/time_evo_util/effective_time_evolution.py:257-324``). Tensors
+come and go as NumPy arrays in the reference's leg conventions: a site tensor
+in its node's logical leg order (parent, children, physical), a cache entry
+E(node -> next) with legs (ket, ham, bra). The environments themselves stay on
+the device inside the cache; the contractions run through the same plans as
+the drivers.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from .engine import CDT, DeviceNetwork
+from .tdvp import EvoDirection, TimeEvoMode
+
+
+class SandwichCache:
+    """Environments of a TTNO sandwiched between a TTNS and its conjugate,
+    one device buffer per directed edge (``sandwich_caching.py:14-126``)."""
+
+    def __init__(self, state, hamiltonian, precision: str = "plain"):
+        self.state = state
+        self.hamiltonian = hamiltonian
+        self.net = DeviceNetwork(state, hamiltonian, precision=precision)
+        self._valid: set = set()
+
+    @classmethod
+    def init_cache_but_one(cls, state, hamiltonian, node_id: str, precision: str = "plain") -> "SandwichCache":
+        """Every environment pointing toward ``node_id`` (``sandwich_caching.py:97-126``)."""
+        cache = cls(state, hamiltonian, precision=precision)
+        cache.net.init_cache_but_one(node_id)
+
+        def rec(nid, toward):
+            for nb in cache.net.nbrs(nid):
+                if nb != toward:
+                    rec(nb, nid)
+            if toward is not None:
+                cache._valid.add((nid, toward))
+        rec(node_id, None)
+        return cache
+
+    def update_tree_cache(self, node_id: str, next_node_id: str):
+        """Recompute E(node_id -> next_node_id) from the current tensors
+        (``sandwich_caching.py:79-95``)."""
+        self.net.update_env(node_id, next_node_id)
+        self._valid.add((node_id, next_node_id))
+
+    def __contains__(self, key) -> bool:
+        return tuple(key) in self._valid
+
+    def get_entry(self, node_id: str, next_node_id: str) -> np.ndarray:
+        """E(node_id -> next_node_id) as a NumPy array with legs (ket, ham, bra)."""
+        if (node_id, next_node_id) not in self._valid:
+            raise KeyError(f"no cached environment from {node_id} to {next_node_id}")
+        return self.net.env_buf(node_id, next_node_id).detach().cpu().numpy()
+
+
+def _to_phys(state, nid, tensor) -> np.ndarray:
+    inv = np.argsort(state.logical_perm(nid))
+    return np.ascontiguousarray(np.transpose(np.asarray(tensor, dtype=np.complex128), inv))
+
+
+def _from_phys(state, nid, tensor) -> np.ndarray:
+    return np.transpose(tensor, state.logical_perm(nid))
+
+
+def _node_id(node) -> str:
+    return node if isinstance(node, str) else node.identifier
+
+
+def contract_ket_ham_with_envs(ket_node, ket_tensor, ham_node, ham_tensor, dictionary: SandwichCache) -> np.ndarray:
+    """H_eff applied to ``ket_tensor`` with the cached environments of all the
+    node's neighbours (``state_operator_contraction.py:227-273``). The TTNO
+    tensor is the cache's; the result has the ket tensor's leg order."""
+    nid = _node_id(ket_node)
+    net = dictionary.net
+    st = dictionary.state
+    x = torch.from_numpy(_to_phys(st, nid, ket_tensor)).to(net.device, CDT)
+    if list(x.shape) != net.shape(nid):
+        raise ValueError(f"tensor shape {tuple(x.shape)} does not match node {nid} {tuple(net.shape(nid))}")
+    y = torch.empty_like(x)
+    net.heff_plan(nid).run(x.data_ptr(), y.data_ptr())
+    return _from_phys(st, nid, y.cpu().numpy())
+
+
+def contract_any(node_id: str, next_node_id: str, state, operator, dictionary: SandwichCache,
+                 bra_state=None, bra_state_conjugated: bool = True, id_trafo_op=None, id_trafo_bra=None) -> np.ndarray:
+    """E(node_id -> next_node_id) from the node's current tensor and the cached
+    environments of its other neighbours (``state_operator_contraction.py:407-461``),
+    legs (ket, ham, bra). The bra is the conjugate of the ket state; other bras
+    and identifier transformations are not provided."""
+    if bra_state is not None or id_trafo_op is not None or id_trafo_bra is not None or not bra_state_conjugated:
+        raise NotImplementedError("contract_any on the GPU engine sandwiches the state with its own conjugate")
+    dictionary.update_tree_cache(node_id, next_node_id)
+    return dictionary.get_entry(node_id, next_node_id)
+
+
+def effective_single_site_evolution(state_tensor, state_node, hamiltonian_tensor, hamiltonian_node,
+                                    time_step_size: float, tensor_cache: SandwichCache,
+                                    mode: TimeEvoMode = TimeEvoMode.KRYLOV,
+                                    forward: EvoDirection = EvoDirection.FORWARD, **options) -> np.ndarray:
+    """exp(-i dt H_eff) applied to ``state_tensor`` (``effective_time_evolution.py:257-324``):
+    the matrix-free Krylov exponential (options ``krylov_tol``, ``max_krylov_dim``);
+    ``forward`` gives the sign of the exponent as in the reference. The dense
+    modes are not provided."""
+    if mode is not TimeEvoMode.KRYLOV:
+        raise NotImplementedError(f"time_evo_mode={mode}: the GPU engine runs the KRYLOV exponential only")
+    nid = _node_id(state_node)
+    net = tensor_cache.net
+    st = tensor_cache.state
+    x = torch.from_numpy(_to_phys(st, nid, state_tensor)).to(net.device, CDT)
+    p = net.heff_plan(nid)
+    exp_factor = forward.exp_factor() if isinstance(forward, EvoDirection) else (-1j if forward else 1j)
+
+    def apply(xp, yp):
+        p.run(xp, yp)
+    out = torch.empty_like(x)
+    net.krylov.expm(x, apply, time_step_size, exp_factor, options.get("krylov_tol", 1e-10),
+                    options.get("max_krylov_dim"), out=out, tridiagonal=net.levels > 0)
+    return _from_phys(st, nid, out.cpu().numpy())

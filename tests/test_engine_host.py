@@ -307,3 +307,39 @@ def test_engine_host_realisations_concurrent_equals_sequential(monkeypatch):
         for nid in s1:
             np.testing.assert_array_equal(s1[nid], s2[nid])
     assert seq[0][0] != seq[1][0] or any(not np.array_equal(seq[0][1][k], seq[1][1][k]) for k in seq[0][1])
+
+
+def test_contraction_helpers_match_oracle(monkeypatch):
+    """SandwichCache / contract_ket_ham_with_envs / contract_any /
+    effective_single_site_evolution in the reference's conventions, against the
+    oracle's restatement."""
+    fake_ptn.install(monkeypatch)
+    import pytreenet_gb300 as P
+    from pytreenet_gb300 import contractions as C
+    import oracle as O
+    c = load_case("ttree3_heis_chi6_o1")
+    st = build_ttn(P.TTNS, c["spec"], c["init"])
+    H = build_ttn(P.TTNO, c["spec"], c["ttno"])
+    ost = oracle_state(c)
+    center = "a0_1"
+    cache = C.SandwichCache.init_cache_but_one(st, H, center)
+    envs = O.init_cache_but_one(ost, c["ttno"], center)
+    for key, e in envs.items():
+        assert key in cache
+        np.testing.assert_allclose(cache.get_entry(*key), e, atol=1e-12)
+    # matvec in the node's logical leg order
+    x = st.tensors[center]
+    y = C.contract_ket_ham_with_envs(st.nodes[center], x, H.nodes[center], None, cache)
+    yo = O.heff_apply(ost.tensors[center], ost.tree, center, c["ttno"][center], envs)
+    np.testing.assert_allclose(y, np.transpose(yo, st.logical_perm(center)), atol=1e-12)
+    # environment recomputed toward a neighbour
+    e = C.contract_any(center, "a0_2", st, H, cache)
+    eo = O.env_update(ost.tree, center, "a0_2", ost.tensors[center], c["ttno"][center], envs)
+    np.testing.assert_allclose(e, eo, atol=1e-12)
+    # Krylov exponential of the site
+    z = C.effective_single_site_evolution(x, st.nodes[center], None, H.nodes[center], 0.05, cache,
+                                          mode=P.TimeEvoMode.KRYLOV, krylov_tol=1e-12)
+    zo = O.krylov_exp_action(ost.tensors[center], lambda v: O.heff_apply(v, ost.tree, center,
+                                                                         c["ttno"][center], envs),
+                             0.05, -1j, krylov_tol=1e-12)
+    np.testing.assert_allclose(z, np.transpose(zo, st.logical_perm(center)), atol=1e-11)

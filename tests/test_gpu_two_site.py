@@ -203,3 +203,27 @@ def test_gpu_ttno_expectation():
                                        config=P.TDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV))
         e = algo.evaluate_operator(H)
         assert abs(e - c["energy_final"]) < 1e-11 * max(1.0, abs(c["energy_final"]))
+
+
+def test_gpu_contraction_helpers_match_oracle():
+    """The contraction helpers on the real library against the oracle."""
+    import pytreenet_gb300 as P
+    from pytreenet_gb300 import contractions as C
+    c = load_case("ttree3_heis_chi6_o1")
+    st = build_ttn(P.TTNS, c["spec"], c["init"])
+    H = build_ttn(P.TTNO, c["spec"], c["ttno"])
+    ost = oracle_state(c)
+    center = "root"
+    cache = C.SandwichCache.init_cache_but_one(st, H, center)
+    envs = O.init_cache_but_one(ost, c["ttno"], center)
+    for key, e in envs.items():
+        np.testing.assert_allclose(cache.get_entry(*key), e, atol=1e-12)
+    x = st.tensors[center]
+    y = C.contract_ket_ham_with_envs(st.nodes[center], x, H.nodes[center], None, cache)
+    yo = O.heff_apply(ost.tensors[center], ost.tree, center, c["ttno"][center], envs)
+    np.testing.assert_allclose(y, np.transpose(yo, st.logical_perm(center)), atol=1e-12)
+    z = C.effective_single_site_evolution(x, st.nodes[center], None, H.nodes[center], 0.05, cache,
+                                          mode=P.TimeEvoMode.KRYLOV, krylov_tol=1e-12)
+    zo = O.krylov_exp_action(ost.tensors[center], lambda v: O.heff_apply(v, ost.tree, center, c["ttno"][center],
+                                                                         envs), 0.05, -1j, krylov_tol=1e-12)
+    np.testing.assert_allclose(z, np.transpose(zo, st.logical_perm(center)), atol=1e-11)

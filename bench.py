@@ -53,10 +53,14 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison sweep")
     ap.add_argument("--no-graphs", action="store_true",
                     help="launch the QR sequences eagerly instead of replaying CUDA graphs")
-    ap.add_argument("--workload", default="ttree", choices=["ttree", "ternary", "disorder"],
+    ap.add_argument("--workload", default="ttree", choices=["ttree", "ternary", "disorder", "gradient"],
                     help="ttree: one-site TDVP on the T-tree (headline); ternary: second-order "
                          "two-site TDVP on the depth-3 ternary tree (40 sites, XXZ) with truncation; "
-                         "disorder: many independent random-field realisations (binary tree, 31 sites)")
+                         "disorder: many independent random-field realisations (binary tree, 31 sites); "
+                         "gradient: d<Z_root>/d(g_i, J) after 30 one-site TDVP steps by the adjoint "
+                         "(binary tree, 31 sites, TFIM)")
+    ap.add_argument("--fd-params", type=int, default=3,
+                    help="gradient: parameters checked against central differences of the driver")
     ap.add_argument("--realisations", type=int, default=32, help="disorder: number of realisations")
     ap.add_argument("--workers", type=int, default=8, help="disorder: concurrent worker streams")
     ap.add_argument("--chi-max", type=int, default=64, help="ternary: max_bond_dim of the SVD split")
@@ -502,8 +506,84 @@ def run_disorder(args):
             "one_worker": out[1], "speedup_over_one_worker": out[args.workers] / out[1]}
 
 
+def run_gradient(args):
+    """Gradient of <Z_root>(T) after 30 first-order one-site TDVP steps (dt=0.02)
+    with respect to the 31 transverse fields g_i ~ U[0.3, 0.7] and J = 1 on the
+    31-site binary tree, bonds min(chi, subtree dimensions), random state scaled
+    to unit norm, complex128. One step
+    = one gradient evaluation (forward sweep, checkpointed backward sweep).
+    Also times one forward evolution through the driver and checks
+    ``--fd-params`` components against central differences (step 1e-5)."""
+    import torch
+    from pytreenet_gb300 import _lib
+    from pytreenet_gb300.adjoint import OneSiteTDVPAdjoint, coupling_gradient
+    from pytreenet_gb300.operators import tfim_ttno
+    from pytreenet_gb300.tdvp import FirstOrderOneSiteTDVP, TDVPConfig, TimeEvoMode, TensorProduct
+    from pytreenet_gb300.workloads import binary_tfim_random_state
+    lib = _lib.load()
+    chi, nsteps, dt, tol = args.chi, 30, 0.02, args.tol
+    st, spec, tensors, g, J = binary_tfim_random_state(n=31, chi=chi, seed=0)
+    theta = np.array([g[nid] for nid, _ in spec] + [J])
+    ops = {"s0": np.diag([1.0, -1.0]).astype(complex)}
+
+    def ham(th):
+        return tfim_ttno(st, J=float(th[-1]), g={nid: float(th[i]) for i, (nid, _) in enumerate(spec)})
+    adj = OneSiteTDVPAdjoint(st, ham(theta), dt, nsteps, krylov_tol=tol, normalise=True)
+    for _ in range(args.warmup):
+        coupling_gradient(adj, ham, theta, ops)
+    torch.cuda.synchronize()
+    l0 = lib.ptn_launch_counter()
+    t0 = time.perf_counter()
+    with Clocks(torch.cuda.current_device()) as clk:
+        for _ in range(args.steps):
+            val, grad = coupling_gradient(adj, ham, theta, ops)
+        torch.cuda.synchronize()
+    sec = (time.perf_counter() - t0) / args.steps
+    launches = int(lib.ptn_launch_counter() - l0) // args.steps
+
+    def run(th_):
+        s = st.copy_structure()
+        s._phys = {k: np.array(v, copy=True) for k, v in tensors.items()}
+        algo = FirstOrderOneSiteTDVP(s, ham(th_), dt, dt * nsteps, {},
+                                     config=TDVPConfig(time_evo_mode=TimeEvoMode.KRYLOV),
+                                     solver_options={"krylov_tol": tol})
+        algo.net.normalise_center()
+        for _ in range(nsteps):
+            algo.run_one_time_step()
+        return float(np.real(algo.evaluate_operator(TensorProduct(ops))))
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    v0 = run(theta)
+    torch.cuda.synchronize()
+    fwd = time.perf_counter() - t1
+    idx = [0, theta.size - 1, theta.size - 2][:max(0, args.fd_params)]
+    h = 1e-5
+    fd = {j: (run(theta + h * np.eye(theta.size)[j]) - run(theta - h * np.eye(theta.size)[j])) / (2 * h) for j in idx}
+    err = max((abs(grad[j] - fd[j]) for j in idx), default=None)
+    return {"metric": "gradient evaluations/sec (d<Z_root>/d(g_1..g_31, J), 30 one-site TDVP steps, "
+                      f"31-site binary tree, chi={chi})",
+            "value": 1.0 / sec, "unit": "gradients/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000 * sec, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c128 (fp64)", "data": "synthetic",
+            "config": {"workload": f"binary tree 31 sites, TFIM g_i~U[0.3,0.7], J=1, chi={chi} (bonds capped at the "
+                                   f"subtree dimensions), first-order 1TDVP, dt={dt}, {nsteps} steps, "
+                                   f"krylov_tol={tol}", "timing": "wall clock per gradient, forward + backward"},
+            "gpu_launches": launches, "clocks": clk.summary(), "value_Z_root": val,
+            "forward_seconds": fwd, "central_difference_seconds_estimate": 2 * theta.size * fwd,
+            "forward_matches_driver": abs(v0 - val),
+            "fd_check": {"params": idx, "adjoint": [float(grad[j]) for j in idx], "central": [fd[j] for j in idx],
+                         "max_abs_err": err, "grad_norm": float(np.linalg.norm(grad))}}
+
+
 def main():
     args = parse()
+    if args.workload == "gradient":
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        if args.chi == 256:
+            args.chi = 64
+        print(json.dumps(run_gradient(args)), flush=True)
+        return
     if args.workload == "disorder":
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))

@@ -463,12 +463,18 @@ class KrylovSolver:
 
     def expm(self, x: torch.Tensor, apply, dt: float, exp_factor: complex, krylov_tol=1e-10,
              max_krylov_dim=None, hermitian=True, out: torch.Tensor | None = None,
-             tridiagonal: bool = False) -> torch.Tensor:
+             tridiagonal: bool = False, basis: dict | None = None) -> torch.Tensor:
         """``tridiagonal``: project on the Lanczos tridiagonal (alpha_j, beta_j)
         only. Used with reduced-precision operators, whose rounding leaves
         entries far from the diagonal of the Arnoldi projection that the
         reference's full symmetrised projection would turn into a spurious
-        first-order coupling (the adaptive stop then never triggers)."""
+        first-order coupling (the adaptive stop then never triggers).
+
+        ``apply(xp, yp)`` gets device pointers, or the basis row and the output
+        as tensors when it carries ``takes_tensors = True``. ``basis``, when
+        given, receives the Krylov basis (``Q``: m x n copy), the m x m
+        projection used for the propagator (``T``) and the norm of x
+        (``beta0``); the adjoint of the exponential reuses them."""
         lib = _lib.load()
         stream = _stream_ptr()
         n = x.numel()
@@ -480,7 +486,10 @@ class KrylovSolver:
         if beta0 == 0.0:
             if out.data_ptr() != x.data_ptr():
                 out.copy_(x)
+            if basis is not None:
+                basis.update(Q=None, T=np.zeros((0, 0), dtype=complex), beta0=0.0, m=0)
             return out
+        tensor_apply = getattr(apply, "takes_tensors", False)
         max_steps = n if max_krylov_dim is None else min(n, int(max_krylov_dim))
         floor_abs = np.finfo(float).eps * max(n, 1)
         T = np.zeros((min(max_steps, 64) + 1,) * 2, dtype=complex)
@@ -506,7 +515,10 @@ class KrylovSolver:
             hs = self.ws.get("kry_hs", (j + batch) * 2 * (j + batch) + 8)
             sc = self.ws.get("kry_sc", 2 * (j + batch) + 8, torch.float64)
             for jj in range(j, j + batch):
-                apply(Q[jj].data_ptr(), w.data_ptr())
+                if tensor_apply:
+                    apply(Q[jj], w)
+                else:
+                    apply(Q[jj].data_ptr(), w.data_ptr())
                 nq = jj + 1
                 base = hs[jj * 2 * (j + batch):]
                 qnext = Q[jj + 1].data_ptr() if jj + 1 < self._qcap else None
@@ -558,6 +570,8 @@ class KrylovSolver:
         if n <= self.SPECULATE_MAX_N:
             self._spec_depth[n] = m
         self.depths.append(m)
+        if basis is not None:
+            basis.update(Q=Q[:m].clone(), T=self._proj(T, m, tridiagonal).copy(), beta0=beta0, m=m)
         c = beta0 * small_propagator(self._proj(T, m, tridiagonal), dt, exp_factor, hermitian)
         cdev = self.ws.get("kry_h", m + 8)[:m]
         cdev.copy_(torch.from_numpy(np.ascontiguousarray(c)).to(x.device))
@@ -577,6 +591,23 @@ class KrylovSolver:
 # ----------------------------------------------------------------------------
 # device network
 # ----------------------------------------------------------------------------
+def ttno_site_tensors(state, hamiltonian) -> dict:
+    """The TTNO's tensors as contiguous complex128 NumPy arrays with legs
+    (the state's physical neighbour order, out, in)."""
+    state._finalise()
+    hamiltonian._finalise()
+    out = {}
+    for nid in state._order:
+        Wn = hamiltonian.phys(nid)
+        hn = hamiltonian.nodes[nid]
+        order = state.nodes[nid].phys_neighbours()
+        hax = [hn.phys_neighbours().index(x) for x in order]
+        Wn = np.asarray(Wn.detach().cpu().numpy() if isinstance(Wn, torch.Tensor) else Wn)
+        Wn = np.transpose(Wn, hax + [Wn.ndim - 2, Wn.ndim - 1])
+        out[nid] = np.ascontiguousarray(Wn, dtype=np.complex128)
+    return out
+
+
 class DeviceNetwork:
     """Device copy of a TTNS (+ TTNO) with environment buffers and cached plans."""
 
@@ -607,16 +638,8 @@ class DeviceNetwork:
             state._phys[nid] = t
         self.W = {}
         if hamiltonian is not None:
-            hamiltonian._finalise()
-            for nid in state._order:
-                Wn = hamiltonian.phys(nid)
-                # TTNO legs are matched to the state's physical neighbour order
-                hn = hamiltonian.nodes[nid]
-                order = state.nodes[nid].phys_neighbours()
-                hax = [hn.phys_neighbours().index(x) for x in order]
-                Wn = np.asarray(Wn.detach().cpu().numpy() if isinstance(Wn, torch.Tensor) else Wn)
-                Wn = np.transpose(Wn, hax + [Wn.ndim - 2, Wn.ndim - 1])
-                self.W[nid] = torch.from_numpy(np.ascontiguousarray(Wn, dtype=np.complex128)).to(self.device)
+            self.W = {nid: torch.from_numpy(Wn).to(self.device)
+                      for nid, Wn in ttno_site_tensors(state, hamiltonian).items()}
         self.env: dict[tuple, torch.Tensor] = {}
         self.plans: dict = {}
         self.rowoff: dict = {}

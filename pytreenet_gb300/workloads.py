@@ -95,6 +95,35 @@ def binary_tfim_product_state(n: int = 15, chi: int = 8, seed: int = 0, J: float
     return st, H, spec, tensors
 
 
+def binary_tfim_random_state(n: int = 31, chi: int = 64, seed: int = 0, g_low: float = 0.3,
+                             g_high: float = 0.7, J: float = 1.0):
+    """Gradient workload: heap-ordered binary tree of ``n`` sites, Gaussian complex
+    tensors (unit Frobenius norm each) with the bond to a subtree of s sites of
+    dimension min(chi, 2^s, 2^(n-s)), so every QR split of a one-site sweep is
+    tall and of full rank; transverse fields g_i ~ U[g_low, g_high], coupling J.
+    Returns (TTNS, spec, tensors in physical layout, g dict, J)."""
+    rng = np.random.default_rng(seed)
+    spec = binary_tree_spec(n)
+    kids = {nid: [] for nid, _ in spec}
+    for nid, p in spec:
+        if p is not None:
+            kids[p].append(nid)
+    size = {}
+    for nid, _ in reversed(spec):
+        size[nid] = 1 + sum(size[c] for c in kids[nid])
+
+    def bond(c):
+        s = size[c]
+        return int(min(chi, 2 ** min(s, 60), 2 ** min(n - s, 60)))
+    tensors = {}
+    for nid, p in spec:
+        shape = ([bond(nid)] if p is not None else []) + [bond(c) for c in kids[nid]] + [2]
+        t = rng.standard_normal(size=shape) + 1j * rng.standard_normal(size=shape)
+        tensors[nid] = t / np.linalg.norm(t)
+    g = {nid: float(rng.uniform(g_low, g_high)) for nid, _ in spec}
+    return _build(spec, tensors), spec, tensors, g, J
+
+
 def ternary_spec(depth: int):
     """Complete ternary tree: t0 at the root, three children per internal node
     (1 + 3 + 9 + 27 = 40 sites for depth 3)."""

@@ -50,7 +50,10 @@ typedef struct {
  * strides used are stride_a (A) and stride_c (C); for N: stride_b, stride_c;
  * for K: stride_a, stride_b. opX = conjugate when conj_x != 0.
  * This is np.tensordot without the transposes: the strides address the legs
- * in place, and C may be written in any leg order. */
+ * in place, and C may be written in any leg order. Outputs of at most 38
+ * 64 x 64 tiles with K >= 2048 split K over several CTAs that add into C with
+ * atomics (C first scaled by beta), so their rounding can vary between runs;
+ * C must not overlap A or B. */
 typedef struct {
   const void* A;
   const void* B;

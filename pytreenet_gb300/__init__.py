@@ -4,7 +4,9 @@ Drop-in surface for the path (names as in PyTreeNet):
 TreeTensorNetworkState/TTNS, TreeTensorNetworkOperator/TTNO, Node,
 FirstOrderOneSiteTDVP, SecondOrderOneSiteTDVP, FirstOrderTwoSiteTDVP,
 SecondOrderTwoSiteTDVP, TDVPConfig, TwoSiteTDVPConfig, SVDParameters, TEBD,
-TrotterStep, TrotterSplitting, TimeEvoMode, EvoDirection, TensorProduct. Numerics run in libptn_gb300.so
+TrotterStep, TrotterSplitting, TimeEvoMode, EvoDirection, TensorProduct; plus
+gradients through a hand-written adjoint (OneSiteTDVPAdjoint,
+coupling_gradient). Numerics run in libptn_gb300.so
 (hand-written CUDA for sm_103a) through a C ABI; see include/ptn_gb300.h.
 """
 from .ttn import Node, TreeTensorNetworkState, TreeTensorNetworkOperator, TTNS, TTNO
@@ -17,6 +19,7 @@ from .operators import nearest_neighbour_ttno, tfim_ttno, heisenberg_ttno
 from .batch import run_realisations
 from .contractions import (SandwichCache, contract_ket_ham_with_envs, contract_any,
                            effective_single_site_evolution)
+from .adjoint import OneSiteTDVPAdjoint, coupling_gradient
 
 __all__ = [
     "Node", "TreeTensorNetworkState", "TreeTensorNetworkOperator", "TTNS", "TTNO",
@@ -27,4 +30,5 @@ __all__ = [
     "NumericOperator",
     "nearest_neighbour_ttno", "tfim_ttno", "heisenberg_ttno", "run_realisations",
     "SandwichCache", "contract_ket_ham_with_envs", "contract_any", "effective_single_site_evolution",
+    "OneSiteTDVPAdjoint", "coupling_gradient",
 ]

@@ -239,23 +239,25 @@ class _KrylovExp(torch.autograd.Function):
             raise ValueError("the adjoint needs an imaginary exponent factor (unitary evolution)")
         x = x.contiguous()
         y = torch.empty_like(x)
+        bx = {}
         _solver(x.device).expm(x.detach(), _tensor_apply(op, [p.detach() for p in params], x.shape),
-                               dt, c, tol, maxdim, out=y)
-        ctx.save_for_backward(x, *params)
-        ctx.meta = (op, dt, complex(c), tol, maxdim)
+                               dt, c, tol, maxdim, out=y, basis=bx)
+        # the basis of x is kept for the backward pass (under checkpointing it
+        # lives only while its step is being differentiated)
+        ctx.save_for_backward(x, bx["Q"] if bx["m"] else x.new_zeros(0), *params)
+        ctx.meta = (op, dt, complex(c), tol, maxdim, bx["T"], bx["beta0"], bx["m"])
         return y
 
     @staticmethod
     def backward(ctx, gy):
-        x, *params = ctx.saved_tensors
-        op, dt, c, tol, maxdim = ctx.meta
+        x, Qx, *params = ctx.saved_tensors
+        op, dt, c, tol, maxdim, Tx, beta_x, mx = ctx.meta
         gy = gy.contiguous()
         det = [p.detach() for p in params]
         ap = _tensor_apply(op, det, x.shape)
         solver = _solver(x.device)
-        bx, bw = {}, {}
-        scratch = torch.empty_like(x)
-        solver.expm(x.detach(), ap, dt, c, tol, maxdim, out=scratch, basis=bx)
+        bx = {"Q": Qx, "T": Tx, "beta0": beta_x, "m": mx}
+        bw = {}
         gx = torch.empty_like(x)
         solver.expm(gy, ap, dt, -c, tol, maxdim, out=gx, basis=bw)
         grads = [None] * len(params)
@@ -264,7 +266,9 @@ class _KrylovExp(torch.autograd.Function):
             z = c * dt
             M = coupling_matrix(bx["T"], bx["beta0"], bw["T"], bw["beta0"], z)
             U, sig, Yh = np.linalg.svd(M)
-            keep = int(np.sum(sig > 1e-15 * sig[0])) if sig[0] > 0 else 0
+            # M's singular values fall off geometrically; terms below 1e-13 of the
+            # largest change the gradient far below the Krylov tolerance
+            keep = int(np.sum(sig > 1e-13 * sig[0])) if sig[0] > 0 else 0
             if keep:
                 n = x.numel()
                 lib = _lib.load()

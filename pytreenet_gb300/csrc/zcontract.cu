@@ -10,6 +10,13 @@
 // threads with a 4 x 4 register tile each, K staged through shared memory in
 // steps of 8. Tile offsets of the M and N rows are decoded once per CTA; the K
 // offsets once per K step.
+//
+// Skinny outputs over a long K (an environment, or the gradient of one, is
+// chi x w x chi summed over everything else) would leave most SMs idle with
+// one CTA per output tile, so when there are few tiles the K range is split
+// over gridDim.y: a first kernel writes beta * C (or zero), and each split
+// adds alpha times its partial sums with double-precision atomics. The
+// summation order then varies between runs at the level of rounding.
 #include "ptn_common.cuh"
 
 namespace {
@@ -32,6 +39,8 @@ struct ContractArgs {
   int beta_zero;
   int64_t M, N, K;
   int64_t tiles_n;
+  int64_t k_chunk;  // K indices per split (the whole K when not split)
+  int split;        // accumulate with atomics into a pre-scaled C
   ModeDev m, n, k;  // m: (A, C) strides; n: (B, C); k: (A, B)
 };
 
@@ -82,12 +91,14 @@ __global__ void __launch_bounds__(256) zcontract_kernel(const ContractArgs a) {
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[i][j] = make_double2(0.0, 0.0);
 
-  for (int64_t k0 = 0; k0 < a.K; k0 += BK) {
+  const int64_t kbeg = (int64_t)blockIdx.y * a.k_chunk;
+  const int64_t kend = (kbeg + a.k_chunk < a.K) ? kbeg + a.k_chunk : a.K;
+  for (int64_t k0 = kbeg; k0 < kend; k0 += BK) {
     __syncthreads();
     if (tid < BK) {
       int64_t ki = k0 + tid;
       int64_t oa = -1, ob = -1;
-      if (ki < a.K) decode(a.k, ki, oa, ob);
+      if (ki < kend) decode(a.k, ki, oa, ob);
       offAk[tid] = oa;
       offBk[tid] = ob;
     }
@@ -136,9 +147,28 @@ __global__ void __launch_bounds__(256) zcontract_kernel(const ContractArgs a) {
       if (offCn[nn] < 0) continue;
       double2* p = a.C + offCm[mm] + offCn[nn];
       double2 v = cmul(a.alpha, acc[i][j]);
+      if (a.split) {
+        atomicAdd(&p->x, v.x);
+        atomicAdd(&p->y, v.y);
+        continue;
+      }
       if (!a.beta_zero) v = cfma(a.beta, *p, v);
       *p = v;
     }
+  }
+}
+
+// C <- beta * C (zero when beta == 0) over the M x N output positions.
+__global__ void __launch_bounds__(256) zcontract_scale_c(const ContractArgs a) {
+  const int64_t total = a.M * a.N;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t mi = i / a.N, ni = i - mi * a.N;
+    int64_t oa, ocm, ob, ocn;
+    decode(a.m, mi, oa, ocm);
+    decode(a.n, ni, ob, ocn);
+    double2* p = a.C + ocm + ocn;
+    *p = a.beta_zero ? make_double2(0.0, 0.0) : cmul(a.beta, *p);
   }
 }
 
@@ -184,7 +214,30 @@ extern "C" int ptn_zcontract(const ptn_contract_desc* d, void* stream) {
   a.tiles_n = tn;
   int64_t tiles = tm * tn;
   if (tiles > 0x7fffffffLL) return PTN_ERR_UNSUPPORTED;
+  // split K when the output tiles cover at most a quarter of the 152 SMs
+  int64_t splits = 1;
+  a.k_chunk = K;
+  if (tiles <= 38 && K >= 2048) {
+    int64_t want = (304 + tiles - 1) / tiles;
+    int64_t most = K / 256;
+    splits = want < most ? want : most;
+    if (splits >= 2) {
+      a.k_chunk = ((K + splits - 1) / splits + BK - 1) / BK * BK;
+      splits = (K + a.k_chunk - 1) / a.k_chunk;
+    } else {
+      splits = 1;
+    }
+  }
+  a.split = splits > 1;
+  cudaStream_t s = ptn_stream(stream);
+  if (a.split) {
+    int64_t total = M * N;
+    int64_t blocks = (total + 255) / 256;
+    if (blocks > 1024) blocks = 1024;
+    PTN_COUNT(1);
+    zcontract_scale_c<<<(unsigned)blocks, 256, 0, s>>>(a);
+  }
   PTN_COUNT(1);
-  zcontract_kernel<<<(unsigned)tiles, 256, 0, ptn_stream(stream)>>>(a);
+  zcontract_kernel<<<dim3((unsigned)tiles, (unsigned)splits), 256, 0, s>>>(a);
   return ptn_launch_status();
 }

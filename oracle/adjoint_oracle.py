@@ -106,6 +106,9 @@ class FirstOrderOneSiteTDVPTorch:
         self.tree = st.tree
         self.path = leaf_to_root_path(st.tree.copy())
         self.orth = orthogonalisation_paths(st.tree, self.path)
+        bp = list(reversed(self.path))
+        self.back_path = bp
+        self.back_orth = [st.tree.path_from_to(nid, bp[i + 2])[:-1] for i, nid in enumerate(bp[1:-1])] + [[bp[-1]]]
         canonical_form(st, self.path[0])
         self.A0 = {k: torch.from_numpy(np.ascontiguousarray(v)) for k, v in st.tensors.items()}
         self.nbrs = {k: st.tree.neighbours(k) for k in st.tensors}
@@ -158,3 +161,61 @@ class FirstOrderOneSiteTDVPTorch:
         for _ in range(steps):
             A = self.step(A, W)
         return expect_product(A, self.nbrs, self.tree.root, ops)
+
+
+class SecondOrderOneSiteTDVPTorch(FirstOrderOneSiteTDVPTorch):
+    """``SecondOrderOneSiteTDVPOracle`` (``secondorderonesite.py:60-193``) in torch;
+    the environments carried between steps by the reference are rebuilt from
+    the tensors at each step start (they point toward the centre and were
+    computed from the tensors as they are, so the two agree)."""
+
+    def _site(self, A, W, envs, nid, factor):
+        nb = self.nbrs[nid]
+        H = heff_matrix(list(A[nid].shape), [envs[(x, nid)] for x in nb], W[nid])
+        A[nid] = (torch.matrix_exp(-1j * self.dt * factor * H) @ A[nid].reshape(-1)).reshape(A[nid].shape)
+
+    def _link(self, A, W, envs, nid, nxt, factor):
+        Q, R = qr_split(A[nid], self.nbrs[nid].index(nxt))
+        A[nid] = Q
+        envs[(nid, nxt)] = self._env(A, W, envs, nid, nxt)
+        Hb = bond_matrix(envs[(nid, nxt)], envs[(nxt, nid)])
+        R = (torch.matrix_exp(1j * self.dt * factor * Hb) @ R.reshape(-1)).reshape(R.shape)
+        A[nxt] = absorb(R, A[nxt], self.nbrs[nxt].index(nid))
+
+    def _move(self, A, W, envs, path):
+        for prev, cur in zip(path[:-1], path[1:]):
+            self._hop(A, prev, cur)
+            envs[(prev, cur)] = self._env(A, W, envs, prev, cur)
+
+    def step(self, A, W):
+        A = dict(A)
+        envs = {}
+        path, op = self.path, self.orth
+
+        def rec(nid, toward):
+            for x in self.nbrs[nid]:
+                if x != toward:
+                    rec(x, nid)
+            if toward is not None:
+                envs[(nid, toward)] = self._env(A, W, envs, nid, toward)
+        rec(path[0], None)
+        for i, nid in enumerate(path[:-1]):
+            if i > 0:
+                self._move(A, W, envs, op[i - 1])
+            self._site(A, W, envs, nid, 0.5)
+            self._link(A, W, envs, nid, op[i][0], 0.5)
+        center = op[-1][0]
+        self._site(A, W, envs, path[-1], 1.0)
+        bp, bo = self.back_path, self.back_orth
+        self._link(A, W, envs, center, bp[1], 0.5)
+        center = bp[1]
+        for i, nid in enumerate(bp[1:-1]):
+            idx = i + 1
+            self._site(A, W, envs, nid, 0.5)
+            if bo[idx - 1]:
+                self._move(A, W, envs, bo[idx - 1])
+                center = bo[idx - 1][-1]
+            self._link(A, W, envs, center, bp[idx + 1], 0.5)
+            center = bp[idx + 1]
+        self._site(A, W, envs, bp[-1], 0.5)
+        return A

@@ -409,17 +409,19 @@ def expect_product(A: dict, nbrs: dict, root: str, ops: dict):
 # the differentiable sweep
 # ----------------------------------------------------------------------------
 class OneSiteTDVPAdjoint:
-    """First-order one-site TDVP (``FirstOrderOneSiteTDVP``) as a differentiable
+    """One-site TDVP (``FirstOrderOneSiteTDVP``, or ``SecondOrderOneSiteTDVP``
+    with ``second_order``) as a differentiable
     map (site tensors, TTNO tensors) -> site tensors after ``num_steps`` steps,
     with the observable <psi(T)| prod O_i |psi(T)> and its gradients.
 
     The initial state is brought into canonical form at the first site of the
-    update path by the engine (as the driver does); gradients with respect to
-    the state are gradients with respect to those canonical tensors."""
+    update path by the engine (as the driver does), and with ``normalise``
+    scaled to unit norm; gradients with respect to the state are gradients
+    with respect to those canonical tensors."""
 
     def __init__(self, initial_state, hamiltonian, time_step_size: float, num_steps: int,
                  krylov_tol: float = 1e-12, max_krylov_dim=None, use_checkpoint: bool = True,
-                 normalise: bool = False):
+                 normalise: bool = False, second_order: bool = False):
         from .tdvp import leaf_to_root_update_path
         if time_step_size <= 0 or num_steps <= 0:
             raise ValueError("time step and number of steps must be positive")
@@ -430,6 +432,10 @@ class OneSiteTDVPAdjoint:
         self.update_path = leaf_to_root_update_path(init)
         self.orth_paths = [st.path_from_to(self.update_path[i], self.update_path[i + 1])[1:]
                            for i in range(len(self.update_path) - 1)]
+        self.second_order = bool(second_order)
+        bp = list(reversed(self.update_path))
+        self.back_path = bp
+        self.back_orth = [st.path_from_to(nid, bp[i + 2])[:-1] for i, nid in enumerate(bp[1:-1])] + [[bp[-1]]]
         net = E.DeviceNetwork(st, None)
         if st.orthogonality_center_id is None:
             net.canonical_form(self.update_path[0])
@@ -468,12 +474,9 @@ class OneSiteTDVPAdjoint:
         A[a] = Q
         A[b] = absorb(R, A[b], self._ax(b, a))
 
-    def step(self, A: dict, W: dict) -> dict:
-        """One first-order step (``firstorderonesite.py:92-104``; site update
-        ``tdvp_algorithm.py:183-201``, link update ``onesitetdvp.py:103-127``,
-        then the orthogonality centre goes back to the first site)."""
-        A = dict(A)
-        path, op = self.update_path, self.orth_paths
+    # -- building blocks of the sweeps (functional counterparts of the driver's) --
+    def _envs_toward(self, A, W, center) -> dict:
+        """All environments pointing toward ``center`` (``init_cache_but_one``)."""
         envs = {}
 
         def rec(nid, toward):
@@ -482,28 +485,77 @@ class OneSiteTDVPAdjoint:
                     rec(x, nid)
             if toward is not None:
                 envs[(nid, toward)] = self._env(nid, toward, A, W, envs)
-        rec(path[0], None)
-        for i, nid in enumerate(path):
+        rec(center, None)
+        return envs
+
+    def _site(self, A, envs, W, nid, factor):
+        """``_update_site`` (``tdvp_algorithm.py:183-201``)."""
+        nb = self.nbrs[nid]
+        params = [envs[(x, nid)] for x in nb] + [W[nid]]
+        A[nid] = krylov_expm(A[nid], _SiteOp(len(nb)), params, self.dt * factor, -1j, self.tol, self.maxdim)
+
+    def _link(self, A, envs, W, nid, nxt, factor):
+        """``_update_link`` (``onesitetdvp.py:103-127``): QR split toward ``nxt``,
+        new environment, backward bond evolution, R absorbed into ``nxt``."""
+        Q, R = qr(A[nid], self._ax(nid, nxt))
+        A[nid] = Q
+        envs[(nid, nxt)] = self._env(nid, nxt, A, W, envs)
+        R = krylov_expm(R, _BondOp(), [envs[(nid, nxt)], envs[(nxt, nid)]], self.dt * factor, 1j,
+                        self.tol, self.maxdim)
+        A[nxt] = absorb(R, A[nxt], self._ax(nxt, nid))
+
+    def _move(self, A, envs, W, path):
+        """``_move_orth_and_update_cache_for_path`` (``tdvp_algorithm.py:203-221``)."""
+        for prev, cur in zip(path[:-1], path[1:]):
+            self._hop(A, prev, cur)
+            envs[(prev, cur)] = self._env(prev, cur, A, W, envs)
+
+    def step(self, A: dict, W: dict) -> dict:
+        """One time step. First order (``firstorderonesite.py:92-104``): every site
+        forward by dt with the links backward in between, then the
+        orthogonality centre goes back to the first site and the environments
+        are rebuilt. Second order (``secondorderonesite.py:101-193``): a
+        half-step sweep along the update path, the last site by dt, and a
+        half-step sweep back. Every step starts from environments rebuilt from
+        its input tensors; the second-order driver carries them over, and
+        they equal the rebuilt ones because each points toward the centre and
+        was computed from the tensors as they are."""
+        A = dict(A)
+        path, op = self.update_path, self.orth_paths
+        envs = self._envs_toward(A, W, path[0])
+        if not self.second_order:
+            for i, nid in enumerate(path):
+                if i > 0:
+                    self._move(A, envs, W, op[i - 1])
+                self._site(A, envs, W, nid, 1.0)
+                if i < len(path) - 1:
+                    self._link(A, envs, W, nid, op[i][0], 1.0)
+                else:
+                    back = self.tree.path_from_to(nid, path[0])
+                    for a, b in zip(back[:-1], back[1:]):
+                        self._hop(A, a, b)
+            return A
+        for i, nid in enumerate(path[:-1]):
             if i > 0:
-                sub = op[i - 1]
-                for prev, cur in zip(sub[:-1], sub[1:]):
-                    self._hop(A, prev, cur)
-                    envs[(prev, cur)] = self._env(prev, cur, A, W, envs)
-            nb = self.nbrs[nid]
-            params = [envs[(x, nid)] for x in nb] + [W[nid]]
-            A[nid] = krylov_expm(A[nid], _SiteOp(len(nb)), params, self.dt, -1j, self.tol, self.maxdim)
-            if i < len(path) - 1:
-                nxt = op[i][0]
-                Q, R = qr(A[nid], self._ax(nid, nxt))
-                A[nid] = Q
-                envs[(nid, nxt)] = self._env(nid, nxt, A, W, envs)
-                R = krylov_expm(R, _BondOp(), [envs[(nid, nxt)], envs[(nxt, nid)]], self.dt, 1j,
-                                self.tol, self.maxdim)
-                A[nxt] = absorb(R, A[nxt], self._ax(nxt, nid))
-            else:
-                back = self.tree.path_from_to(nid, path[0])
-                for a, b in zip(back[:-1], back[1:]):
-                    self._hop(A, a, b)
+                self._move(A, envs, W, op[i - 1])
+            self._site(A, envs, W, nid, 0.5)
+            self._link(A, envs, W, nid, op[i][0], 0.5)
+        center = op[len(path) - 2][0] if len(path) > 1 else path[0]
+        self._site(A, envs, W, path[-1], 1.0)
+        bp, bo = self.back_path, self.back_orth
+        if len(bp) > 1:
+            self._link(A, envs, W, center, bp[1], 0.5)
+            center = bp[1]
+            for i, nid in enumerate(bp[1:-1]):
+                idx = i + 1
+                self._site(A, envs, W, nid, 0.5)
+                sub = bo[idx - 1]
+                if sub:
+                    self._move(A, envs, W, sub)
+                    center = sub[-1]
+                self._link(A, envs, W, center, bp[idx + 1], 0.5)
+                center = bp[idx + 1]
+            self._site(A, envs, W, bp[-1], 0.5)
         return A
 
     def _step_flat(self, *flat):

@@ -194,3 +194,49 @@ def test_tdvp_state_gradient_matches_oracle(fake):
         assert torch.allclose(gA[k], g, atol=1e-9), k
     for k, g in zip(adj.order, grads[len(adj.order):]):
         assert torch.allclose(gW[k], g, atol=1e-9), k
+
+
+def test_second_order_tdvp_gradient_matches_oracle_and_fd(fake):
+    """The second-order schedule: coupling gradient against torch autograd
+    through the oracle's dense second-order sweep and against central
+    differences of the engine's SecondOrderOneSiteTDVP driver."""
+    import oracle as O
+    import oracle.adjoint_oracle as AO
+    from pytreenet_gb300.adjoint import OneSiteTDVPAdjoint, coupling_gradient
+    from pytreenet_gb300.tdvp import SecondOrderOneSiteTDVP, TDVPConfig, TimeEvoMode, TensorProduct
+    st, spec, tensors, theta, ham = _seven_site_problem(seed=6)
+    dt, steps = 0.1, 3
+    ops = {"s0": np.diag([1.0, -1.0]).astype(complex)}
+    adj = OneSiteTDVPAdjoint(st, ham(theta), dt, steps, krylov_tol=1e-14, second_order=True)
+    val, grad = coupling_gradient(adj, ham, theta, ops)
+    _, gW, gA = adj.expectation_and_gradient(ops, wrt_state=True)
+    tree = O.OTree()
+    for nid, p in spec:
+        tree.add_root(nid) if p is None else tree.add_child(nid, p)
+    otd = AO.SecondOrderOneSiteTDVPTorch(O.OState(tree, {k: v.copy() for k, v in tensors.items()}), dt)
+    A0 = {k: adj.A0[k].detach().clone().requires_grad_(True) for k in adj.order}
+    W0 = {k: adj.W0[k].detach().clone().requires_grad_(True) for k in adj.order}
+    ov = otd.expectation(A0, W0, steps, ops).real
+    ref = torch.autograd.grad(ov, [A0[k] for k in adj.order] + [W0[k] for k in adj.order])
+    assert abs(val - float(ov.detach())) < 1e-11
+    n = len(adj.order)
+    for k, r in zip(adj.order, ref[:n]):
+        assert torch.allclose(gA[k], r, atol=1e-9), k
+    for k, r in zip(adj.order, ref[n:]):
+        assert torch.allclose(gW[k], r, atol=1e-9), k
+
+    def run(th_):
+        s = st.copy_structure()
+        s._phys = {k: np.array(v, copy=True) for k, v in tensors.items()}
+        algo = SecondOrderOneSiteTDVP(s, ham(th_), dt, dt * steps, {},
+                                      config=TDVPConfig(time_evo_mode=TimeEvoMode.KRYLOV),
+                                      solver_options={"krylov_tol": 1e-14})
+        for _ in range(steps):
+            algo.run_one_time_step()
+        return float(np.real(algo.evaluate_operator(TensorProduct(ops))))
+    assert abs(run(theta) - val) < 1e-11
+    h = 1e-5
+    fd = np.array([(run(theta + h * np.eye(theta.size)[j]) - run(theta - h * np.eye(theta.size)[j])) / (2 * h)
+                   for j in range(theta.size)])
+    assert np.linalg.norm(grad) > 1e-4
+    assert np.linalg.norm(grad - fd) < 1e-6 * np.linalg.norm(grad)

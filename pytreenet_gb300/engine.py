@@ -662,6 +662,18 @@ class DeviceNetwork:
         self.qr_R = torch.zeros((kmax * kmax,), dtype=CDT, device=self.device)
         self.qr_work = torch.zeros(((wmax + 15) // 16,), dtype=CDT, device=self.device)
 
+    def refresh_hamiltonian(self, hamiltonian):
+        """Copy a changed TTNO's tensors into the device buffers in place (every
+        plan keeps pointing at them); the bond dimensions must not change."""
+        new = ttno_site_tensors(self.state, hamiltonian)
+        for nid, Wn in new.items():
+            if tuple(Wn.shape) != tuple(self.W[nid].shape):
+                raise ValueError(f"TTNO tensor of {nid} changed shape {tuple(self.W[nid].shape)} -> "
+                                 f"{tuple(Wn.shape)}; the environments would not fit")
+        for nid, Wn in new.items():
+            self.W[nid].copy_(torch.from_numpy(Wn))
+        self.ham = hamiltonian
+
     def _finish(self, cb: "ChainBuilder"):
         """The chain as a tensor-core plan on the reduced-precision paths, else FP64.
         (Small chains stay on the tensor cores too: the FP64 kernel's 64 x 64

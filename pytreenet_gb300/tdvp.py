@@ -83,6 +83,15 @@ class TDVPConfig(TTNTimeEvolutionConfig):
     main_path_mode: PathFinderMode = PathFinderMode.LeafToRoot
 
 
+def compute_num_time_steps(final_time: float, time_step_size: float) -> int:
+    """``TimeEvolution._compute_num_time_steps`` (``time_evolution/time_evolution.py:104-116``):
+    the integer part of final_time / dt, plus one when the fractional part is
+    at least 0.1 (so 0.3 / 0.05 = 5.999... gives 6, not 7)."""
+    import math
+    frac, whole = math.modf(final_time / time_step_size)
+    return int(whole) if frac < 0.1 else int(whole + 1)
+
+
 def _postorder(ttn, nid):
     node = ttn.nodes[nid]
     if node.is_leaf():
@@ -141,6 +150,10 @@ class OneSiteTDVP:
                  solver_options: dict[str, Any] | None = None, precision: str = "plain"):
         if len(initial_state.nodes) != len(hamiltonian.nodes):
             raise AssertionError("state and Hamiltonian must have the same nodes")
+        from .time_dep import AbstractTimeDepTTNO
+        if config is not None and config.time_dep and not isinstance(hamiltonian, AbstractTimeDepTTNO):
+            raise TypeError("The Hamiltonian must be from the AbstractTimeDepTTNO class "
+                            "if the time evolution is time-dependent!")
         if time_step_size <= 0 or final_time <= 0:
             raise ValueError("time step and final time must be positive")
         self.config = config if config is not None else self.config_class()
@@ -156,7 +169,7 @@ class OneSiteTDVP:
         self.solver_options = opts
         self.time_step_size = float(time_step_size)
         self.final_time = float(final_time)
-        self.num_time_steps = int(np.ceil(final_time / time_step_size))
+        self.num_time_steps = compute_num_time_steps(final_time, time_step_size)
         self.operators = operators if operators is not None else []
         self.hamiltonian = hamiltonian
         initial_state._finalise()
@@ -227,8 +240,21 @@ class OneSiteTDVP:
             ops = [ops]
         return np.array([self.evaluate_operator(o) for o in ops])
 
+    # -- time-dependent Hamiltonians (``ttn_time_evolution.py:266-280``) -----------
+    def update_hamiltonian(self):
+        """Advance a time-dependent TTNO by one step and copy its tensors into
+        the device buffers (the environments are kept, as in the reference)."""
+        self.hamiltonian.update(self.time_step_size)
+        self.hamiltonian.modify_state(self.state)
+        self.net.refresh_hamiltonian(self.hamiltonian)
+
+    def reset_hamiltonian(self):
+        self.hamiltonian.reset()
+        self.net.refresh_hamiltonian(self.hamiltonian)
+
     def run(self, evaluation_time: int = 1, pgbar: bool = False):
-        """``TimeEvolution.run`` (``time_evolution/time_evolution.py:346-368``)."""
+        """``TimeEvolution.run`` (``time_evolution/time_evolution.py:346-368``):
+        step, measure, then (``config.time_dep``) update the Hamiltonian."""
         res = [self.evaluate_operators()]
         self.times = [0.0]
         for i in range(self.num_time_steps):
@@ -236,6 +262,8 @@ class OneSiteTDVP:
             if evaluation_time != "inf" and (i + 1) % evaluation_time == 0:
                 res.append(self.evaluate_operators())
                 self.times.append((i + 1) * self.time_step_size)
+            if self.config.time_dep:
+                self.update_hamiltonian()
         self.results = np.array(res)
         return self.results
 

@@ -20,7 +20,7 @@ import scipy.linalg
 import torch
 
 from .engine import CDT, DeviceNetwork
-from .tdvp import TTNTimeEvolutionConfig, TensorProduct
+from .tdvp import TTNTimeEvolutionConfig, TensorProduct, compute_num_time_steps
 from .truncation import SVDParameters
 
 
@@ -82,7 +82,7 @@ class TEBD:
         self.svd_parameters = svd_parameters if svd_parameters is not None else SVDParameters()
         self.time_step_size = float(time_step_size)
         self.final_time = float(final_time)
-        self.num_time_steps = int(np.ceil(final_time / time_step_size))
+        self.num_time_steps = compute_num_time_steps(final_time, time_step_size)
         self.operators = operators if operators is not None else []
         initial_state._finalise()
         self.initial_state = initial_state

@@ -107,7 +107,8 @@ def phys_layout(ttn_node_parent, ttn_node_children, tensor, spec_children, nopen
     perm += [off + ttn_node_children.index(c) for c in spec_children]
     nv = off + len(ttn_node_children)
     perm += list(range(nv, nv + nopen))
-    return np.ascontiguousarray(np.transpose(tensor, perm))
+    # a copy: the reference updates time-dependent TTNO tensors in place
+    return np.array(np.transpose(tensor, perm), order="C", copy=True)
 
 
 def export_state(ttns, spec):
@@ -354,6 +355,66 @@ def unit_cases(ptn):
     print("units written")
 
 
+def run_case_time_dep(ptn, name, spec, tensors, dt, steps, order, tol, J=1.0, g0=0.5, amp=0.3, omega=5.0):
+    """TFIM with a driven field g(t) = g0 + amp sin(omega t) on every site, through
+    the reference's ``TimeDependentTTNO`` with one ``FactorUpdatable`` per node
+    (``ttno/time_dep_ttno.py:211-342, 370-470``) and ``TDVPConfig(time_dep=True)``.
+    The updatable of a node carries the difference of the TTNO tensors at
+    g0 + 1 and g0 (the TTNO is affine in g). The loop is the one of
+    ``TimeEvolution.run`` (``time_evolution/time_evolution.py:346-368``): step,
+    measure, update the Hamiltonian."""
+    from pytreenet.time_evolution.time_evolution import TimeEvoMode
+    from pytreenet.time_evolution.tdvp_algorithms.tdvp_algorithm import TDVPConfig
+    from pytreenet.ttno.time_dep_ttno import TimeDependentTTNO, FactorUpdatable
+    psi = build_reference_state(ptn, spec, tensors)
+    psi.canonical_form(spec[0][0])
+    psi.normalise()
+    tensors = export_state(psi, spec)
+    psi = build_reference_state(ptn, spec, tensors)
+    H0 = ptn.TTNO.from_hamiltonian(tfim(ptn, spec, J=J, g=g0), psi)
+    H1 = ptn.TTNO.from_hamiltonian(tfim(ptn, spec, J=J, g=g0 + 1.0), psi)
+    ups = []
+    for nid, _ in spec:
+        D = np.asarray(H1.tensors[nid]) - np.asarray(H0.tensors[nid])
+        idx = tuple(slice(0, d) for d in D.shape)
+        ups.append(FactorUpdatable(nid, idx, D, lambda t: amp * np.sin(omega * t)))
+    H = TimeDependentTTNO(ups, H0)
+    cls = ptn.FirstOrderOneSiteTDVP if order == 1 else ptn.SecondOrderOneSiteTDVP
+    ops = {nid: ptn.TensorProduct({nid: Z}) for nid, _ in spec}
+    algo = cls(psi, H, dt, dt * steps, ops,
+               config=TDVPConfig(time_evo_mode=TimeEvoMode.KRYLOV, time_dep=True),
+               solver_options={"krylov_tol": tol})
+    rec = {"spec_ids": np.array([s[0] for s in spec]),
+           "spec_parents": np.array(["" if s[1] is None else s[1] for s in spec]),
+           "dt": dt, "steps": steps, "order": order, "krylov_tol": tol,
+           "update_path": np.array(algo.update_path), "J": J, "g0": g0, "amp": amp, "omega": omega}
+    for nid, t in tensors.items():
+        rec[f"init/{nid}"] = t
+    for nid, t in export_ttno(H0, spec).items():
+        rec[f"ttno/{nid}"] = t
+    ch = children_of(spec)
+    for (nid, _), u in zip(spec, ups):
+        node = H0.nodes[nid]
+        rec[f"ttno_d/{nid}"] = phys_layout(node.parent, list(node.children), u.initial_values, ch[nid], 2)
+    zs = []
+    for step in range(steps):
+        algo.run_one_time_step()
+        zs.append([algo.state.operator_expectation_value(ops[nid]) for nid, _ in spec])
+        algo.update_hamiltonian()
+    rec["z"] = np.array(zs)
+    for nid, t in export_state(algo.state, spec).items():
+        rec[f"final/{nid}"] = t
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **rec)
+    print(name, "written")
+
+
+def time_dep_cases(ptn):
+    rng = np.random.default_rng(77)
+    spec = binary_tree(7)
+    run_case_time_dep(ptn, "binary7_tfim_driven_o1", spec, random_state_tensors(spec, rng, 3), 0.05, 6, 1, 1e-12)
+    run_case_time_dep(ptn, "binary7_tfim_driven_o2", spec, random_state_tensors(spec, rng, 3), 0.05, 5, 2, 1e-12)
+
+
 def main(ref_root):
     ptn = _import_reference(ref_root)
     rng = np.random.default_rng(1234)
@@ -402,6 +463,7 @@ def main(ref_root):
     run_case_tebd(ptn, "binary7_tfim_tebd", spec, random_state_tensors(spec, rng, 3), 0.05, 4,
                   (4, 1e-10, 1e-10, False))
     unit_cases(ptn)
+    time_dep_cases(ptn)
 
 
 if __name__ == "__main__":

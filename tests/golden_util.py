@@ -26,6 +26,10 @@ def load_case(name):
         "energy_final": complex(d["energy_final"]) if "energy_final" in d.files else None,
     }
     case["tebd"] = bool(int(d["tebd"])) if "tebd" in d.files else False
+    case["driven"] = "amp" in d.files
+    if case["driven"]:
+        case["ttno_d"] = {i: d[f"ttno_d/{i}"] for i in ids}
+        case["amp"], case["omega"] = float(d["amp"]), float(d["omega"])
     if case["tebd"]:
         case["gates"] = [(d[f"gate/{i}/op"], [str(x) for x in d[f"gate/{i}/ids"]]) for i in range(int(d["n_gates"]))]
     if case["two_site"] or case["tebd"]:
@@ -38,6 +42,14 @@ CASES = ["c1_binary15_tfim_chi8", "binary7_tfim_chi4_o2", "ttree3_heis_chi6_o1",
          "ttree3_heis_chi6_o2", "ternary2_xxz_chi4_o1"]
 TWO_SITE_CASES = ["ternary2_xxz_neel_2tdvp", "binary7_heis_2tdvp_trunc"]
 TEBD_CASES = ["binary7_tfim_tebd"]
+DRIVEN_CASES = ["binary7_tfim_driven_o1", "binary7_tfim_driven_o2"]
+
+
+def driven_ttno(case, t):
+    """TTNO tensors of a driven case at time t: base + amp sin(omega t) D."""
+    import numpy as np
+    f = case["amp"] * np.sin(case["omega"] * t)
+    return {k: case["ttno"][k] + f * case["ttno_d"][k] for k in case["ttno"]}
 
 
 def build_ttn(cls, spec, tensors):
@@ -105,3 +117,29 @@ def run_tebd_case(name, steps=None):
         zs.append([algo.evaluate_operator({nid: Zm}) for nid, _ in c["spec"]])
     out = {nid: algo.state.get_phys_numpy(nid) for nid, _ in c["spec"]}
     return c, O.OState(oracle_state(c).tree, out), np.array(zs), algo
+
+
+def run_driven_case(name, precision="plain"):
+    """Run the engine's one-site driver with a TimeDependentTTNO built from a
+    driven fixture through ``run()``; returns (case, oracle-state of the
+    result, <Z> rows after each step)."""
+    import numpy as np
+    import oracle as O
+    import pytreenet_gb300 as P
+    from pytreenet_gb300.time_dep import FactorUpdatable, TimeDependentTTNO
+    c = load_case(name)
+    st = build_ttn(P.TTNS, c["spec"], c["init"])
+    H0 = build_ttn(P.TTNO, c["spec"], {k: v.copy() for k, v in c["ttno"].items()})
+    amp, om = c["amp"], c["omega"]
+    ups = [FactorUpdatable(nid, tuple(slice(0, d) for d in c["ttno_d"][nid].shape), c["ttno_d"][nid],
+                           lambda t: amp * np.sin(om * t)) for nid, _ in c["spec"]]
+    H = TimeDependentTTNO(ups, H0)
+    Zm = np.diag([1.0, -1.0]).astype(complex)
+    ops = {nid: P.TensorProduct({nid: Zm}) for nid, _ in c["spec"]}
+    cls = P.FirstOrderOneSiteTDVP if c["order"] == 1 else P.SecondOrderOneSiteTDVP
+    algo = cls(st, H, c["dt"], c["dt"] * c["steps"], ops,
+               config=P.TDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV, time_dep=True),
+               solver_options={"krylov_tol": c["krylov_tol"]}, precision=precision)
+    res = algo.run()
+    out = {nid: algo.state.get_phys_numpy(nid) for nid, _ in c["spec"]}
+    return c, O.OState(oracle_state(c).tree, out), np.real(res[1:1 + c["steps"]])

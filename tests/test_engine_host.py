@@ -385,3 +385,59 @@ def test_finite_difference_gradient_matches_oracle(monkeypatch):
     ge = np.array([(exact(theta + 1e-5 * np.eye(4)[k]) - exact(theta - 1e-5 * np.eye(4)[k])) / 2e-5
                    for k in range(4)])
     assert np.max(np.abs(g - ge)) < 1e-5
+
+
+@pytest.mark.parametrize("name", ["binary7_tfim_driven_o1", "binary7_tfim_driven_o2"])
+def test_engine_host_time_dependent_hamiltonian(monkeypatch, name):
+    """Driven field through TimeDependentTTNO and config.time_dep: the engine's
+    run() reproduces the reference's <Z_i>(t) and final state."""
+    fake_ptn.install(monkeypatch)
+    from golden_util import run_driven_case
+    c, st, z = run_driven_case(name)
+    assert np.max(np.abs(z - c["z"].real)) < 1e-10
+    one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), st)
+    assert one_minus_f < 1e-12
+
+
+def test_time_dependent_ttno_api(monkeypatch):
+    """time_dep without a time-dependent TTNO raises TypeError (as the
+    reference); updates, resets and the discrete switcher act on the tensors
+    in the reference's leg order."""
+    fake_ptn.install(monkeypatch)
+    import pytreenet_gb300 as P
+    from pytreenet_gb300.time_dep import DiscreetTimeTTNO, FactorUpdatable, TimeDependentTTNO
+    c = load_case("binary7_tfim_driven_o1")
+    st = build_ttn(P.TTNS, c["spec"], c["init"])
+    H = build_ttn(P.TTNO, c["spec"], {k: v.copy() for k, v in c["ttno"].items()})
+    with pytest.raises(TypeError):
+        P.FirstOrderOneSiteTDVP(st, H, 0.1, 1.0, {}, config=P.TDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV,
+                                                                          time_dep=True))
+    base = H.get_tensor("s1").copy()
+    D = np.ones((1, 1, 1, 2, 2))
+    u = FactorUpdatable("s1", (0, 1, 2, slice(0, 2), slice(0, 2)), D, lambda t: 2.0 * t)
+    T = TimeDependentTTNO([u], H)
+    T.update(0.25)
+    T.update(0.25)
+    got = T.get_tensor("s1")
+    exp = base.copy()
+    exp[0, 1, 2] += 1.0
+    assert np.allclose(got, exp)
+    T.reset()
+    assert np.allclose(T.get_tensor("s1"), base)
+    H2 = build_ttn(P.TTNO, c["spec"], {k: 2 * v for k, v in c["ttno"].items()})
+    Dt = DiscreetTimeTTNO([H, H2], dt=0.5)
+    Dt.update(0.3)
+    assert np.allclose(Dt.get_tensor("s0"), H.get_tensor("s0"))
+    Dt.update(0.3)
+    assert np.allclose(Dt.get_tensor("s0"), H2.get_tensor("s0"))
+    Dt.reset()
+    assert np.allclose(Dt.get_tensor("s0"), H.get_tensor("s0"))
+
+
+def test_num_time_steps_rule():
+    """``_compute_num_time_steps``: floor when the fractional part is below 0.1."""
+    from pytreenet_gb300.tdvp import compute_num_time_steps
+    assert compute_num_time_steps(0.3, 0.05) == 6          # 5.999... and 6.000...1 both give 6
+    assert compute_num_time_steps(0.35, 0.1) == 4
+    assert compute_num_time_steps(1.0, 0.3) == 4           # 3.33: fraction 0.33 -> one more step
+    assert compute_num_time_steps(1.005, 0.1) == 10        # 10.05: fraction below 0.1 -> 10

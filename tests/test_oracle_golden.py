@@ -151,3 +151,29 @@ def test_oracle_ttno_expectation_matches_reference(name):
     c = load_case(name)
     e = O.ttno_expectation(oracle_state(c, "final"), c["ttno"])
     assert abs(e - c["energy_final"]) < 1e-12 * max(1.0, abs(c["energy_final"]))
+
+
+@pytest.mark.parametrize("name", ["binary7_tfim_driven_o1", "binary7_tfim_driven_o2"])
+def test_oracle_time_dependent_hamiltonian(name):
+    """A driven field g(t) through the reference's TimeDependentTTNO: the oracle
+    swaps in the TTNO tensors of the next time after every step, keeping the
+    environments it has (the reference does not rebuild them either)."""
+    from golden_util import driven_ttno
+    c = load_case(name)
+    st = oracle_state(c)
+    cls = O.FirstOrderOneSiteTDVPOracle if c["order"] == 1 else O.SecondOrderOneSiteTDVPOracle
+    algo = cls(st, driven_ttno(c, 0.0), c["dt"], krylov_tol=c["krylov_tol"])
+    static = cls(oracle_state(c), driven_ttno(c, 0.0), c["dt"], krylov_tol=c["krylov_tol"])
+    zerr, zstatic = 0.0, 0.0
+    for k in range(c["steps"]):
+        algo.run_one_time_step()
+        static.run_one_time_step()
+        z = np.array([O.expect_product(algo.state, {nid: Zm}) for nid, _ in c["spec"]])
+        zs = np.array([O.expect_product(static.state, {nid: Zm}) for nid, _ in c["spec"]])
+        zerr = max(zerr, float(np.max(np.abs(z - c["z"][k]))))
+        zstatic = max(zstatic, float(np.max(np.abs(zs - c["z"][k]))))
+        algo.W = driven_ttno(c, (k + 1) * c["dt"])
+    one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), algo.state)
+    assert zerr < 1e-10
+    assert one_minus_f < 1e-12
+    assert zstatic > 1e-4            # the drive matters at this resolution

@@ -212,6 +212,48 @@ class TreeTensorNetwork:
     def bond_dim(self, a, b) -> int:
         return self.phys(a).shape[self.phys_axis(a, b)]
 
+    # -- files (``core/ttn.py:1747-1838``) ------------------------------------------
+    def save(self, filepath: str):
+        """``{filepath}.npz`` with every tensor in its node's leg order (parent,
+        children in the node's order, open legs) and ``{filepath}.json`` with
+        the structure (root, orthogonality centre, and per node identifier,
+        parent, children, shape) -- PyTreeNet's format."""
+        import json
+        self._finalise()
+        tensors = {nid: np.ascontiguousarray(self.get_tensor(nid)) for nid in self._order}
+        np.savez(f"{filepath}.npz", **tensors)
+        data = {"root_id": self.root_id,
+                "orthogonality_center_id": self.orthogonality_center_id,
+                "nodes": {nid: {"identifier": nid, "parent": self.nodes[nid].parent,
+                                "children": list(self.nodes[nid].children),
+                                "shape": list(tensors[nid].shape)} for nid in self._order}}
+        with open(f"{filepath}.json", "w") as f:
+            json.dump(data, f, indent=2)
+
+    @classmethod
+    def load(cls, filepath: str):
+        """Read the two files written by :meth:`save` (or by PyTreeNet); every
+        tensor is taken to be in its node's leg order."""
+        import json
+        import os
+        if not (os.path.exists(f"{filepath}.npz") and os.path.exists(f"{filepath}.json")):
+            raise FileNotFoundError(f"Could not find required files at {filepath}!")
+        with open(f"{filepath}.json") as f:
+            data = json.load(f)
+        arrays = np.load(f"{filepath}.npz")
+        ttn = cls()
+        for nid, nd in data["nodes"].items():
+            node = Node(nd["identifier"], arrays[nid])
+            node.parent = nd["parent"]
+            node.children = list(nd["children"])
+            node.phys_children = list(nd["children"])
+            ttn.nodes[nid] = node
+            ttn._order.append(nid)
+            ttn._phys[nid] = np.ascontiguousarray(arrays[nid])
+        ttn.root_id = data["root_id"]
+        ttn.orthogonality_center_id = data["orthogonality_center_id"]
+        return ttn
+
     def copy_structure(self):
         """Deep copy of the structure (tensors are shared)."""
         import copy

@@ -408,6 +408,28 @@ def run_case_time_dep(ptn, name, spec, tensors, dt, steps, order, tol, J=1.0, g0
     print(name, "written")
 
 
+def saved_files(ptn):
+    """A TTNS and a TTNO written by the reference's ``TreeTensorNetwork.save``
+    (``core/ttn.py:1747-1780``), after a canonical form and a TDVP step have
+    reordered children, so the files carry non-trivial leg orders."""
+    from pytreenet.time_evolution.time_evolution import TimeEvoMode
+    from pytreenet.time_evolution.tdvp_algorithms.tdvp_algorithm import TDVPConfig
+    rng = np.random.default_rng(5)
+    spec = binary_tree(7)
+    psi = build_reference_state(ptn, spec, random_state_tensors(spec, rng, 2))
+    H = ptn.TTNO.from_hamiltonian(tfim(ptn, spec), psi)
+    algo = ptn.FirstOrderOneSiteTDVP(psi, H, 0.05, 0.1, {}, config=TDVPConfig(time_evo_mode=TimeEvoMode.KRYLOV))
+    algo.run_one_time_step()
+    algo.state.save(os.path.join(HERE, "saved_ttns"))
+    H.save(os.path.join(HERE, "saved_ttno"))
+    ids = [nid for nid, _ in spec]
+    rec = {"ids": np.array(ids),
+           "z": np.array([algo.state.operator_expectation_value(ptn.TensorProduct({nid: Z})) for nid in ids]),
+           "norm2": algo.state.scalar_product()}
+    np.savez_compressed(os.path.join(HERE, "saved_ttns_values.npz"), **rec)
+    print("saved files written")
+
+
 def time_dep_cases(ptn):
     rng = np.random.default_rng(77)
     spec = binary_tree(7)
@@ -464,6 +486,7 @@ def main(ref_root):
                   (4, 1e-10, 1e-10, False))
     unit_cases(ptn)
     time_dep_cases(ptn)
+    saved_files(ptn)
 
 
 if __name__ == "__main__":

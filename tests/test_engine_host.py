@@ -441,3 +441,40 @@ def test_num_time_steps_rule():
     assert compute_num_time_steps(0.35, 0.1) == 4
     assert compute_num_time_steps(1.0, 0.3) == 4           # 3.33: fraction 0.33 -> one more step
     assert compute_num_time_steps(1.005, 0.1) == 10        # 10.05: fraction below 0.1 -> 10
+
+
+def test_ttn_files_written_by_reference(monkeypatch, tmp_path):
+    """PyTreeNet's save format (``core/ttn.py:1747-1838``): files written by the
+    reference load into the engine's classes with the same values, and saving
+    them again reproduces the files."""
+    import json
+    import os
+    import pytreenet_gb300 as P
+    from golden_util import GOLDEN
+    st = P.TTNS.load(os.path.join(GOLDEN, "saved_ttns"))
+    H = P.TTNO.load(os.path.join(GOLDEN, "saved_ttno"))
+    vals = np.load(os.path.join(GOLDEN, "saved_ttns_values.npz"))
+    ids = [str(x) for x in vals["ids"]]
+    psi = st.to_dense(ids)
+    n = len(ids)
+    for i, nid in enumerate(ids):
+        zi = np.ones(1)
+        for j in range(n):
+            zi = np.kron(zi, np.array([1.0, -1.0]) if j == i else np.ones(2))
+        assert abs(np.vdot(psi, zi * psi) - vals["z"][i]) < 1e-12
+    assert abs(np.vdot(psi, psi) - vals["norm2"]) < 1e-12
+    assert st.orthogonality_center_id == "s3"
+    for obj, name in ((st, "saved_ttns"), (H, "saved_ttno")):
+        out = str(tmp_path / name)
+        obj.save(out)
+        with open(out + ".json") as f, open(os.path.join(GOLDEN, name + ".json")) as g:
+            assert json.load(f) == json.load(g)
+        a, b = np.load(out + ".npz"), np.load(os.path.join(GOLDEN, name + ".npz"))
+        assert sorted(a.files) == sorted(b.files)
+        for k in a.files:
+            assert np.array_equal(a[k], b[k])
+    # a loaded state and operator drive the engine
+    fake_ptn.install(monkeypatch)
+    algo = P.FirstOrderOneSiteTDVP(st, H, 0.05, 0.1, {}, config=P.TDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV))
+    algo.run_one_time_step()
+    assert abs(algo.evaluate_operator(P.TensorProduct({})) - vals["norm2"]) < 1e-10

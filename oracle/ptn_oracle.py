@@ -28,6 +28,7 @@ __all__ = [
     "scalar_product", "SVDParams", "truncate_singular_values", "two_site_merge",
     "two_site_heff_apply", "two_site_split", "SecondOrderTwoSiteTDVPOracle",
     "FirstOrderTwoSiteTDVPOracle", "tebd_apply_gate", "TEBDOracle", "ttno_expectation",
+    "fixed_bug_step",
 ]
 
 
@@ -530,6 +531,95 @@ class SecondOrderOneSiteTDVPOracle(_OneSiteBase):
             self.move_orth_and_update_cache(self.back_orth[idx - 1])
             self.update_link(self.state.orth_center, bp[idx + 1], 0.5)
         self.update_site(bp[-1], 0.5)
+
+
+# ----------------------------------------------------------------------------
+# fixed-rank BUG (basis update and Galerkin)
+# ----------------------------------------------------------------------------
+def _split_toward(A, ax):
+    """QR of A with leg ``ax`` as the column index: (Q with A's legs, R)."""
+    At = np.moveaxis(A, ax, -1)
+    k = At.shape[-1]
+    q, r = np.linalg.qr(At.reshape(-1, k), mode="reduced")
+    if q.shape[1] < k:
+        q = np.pad(q, [(0, 0), (0, k - q.shape[1])])
+        r = np.pad(r, [(0, k - r.shape[0]), (0, 0)])
+    return np.moveaxis(q.reshape(At.shape), -1, ax), r
+
+
+def _bug_basis(T):
+    """New basis of a non-root node: QR of its evolved tensor with the parent
+    leg (leg 0) as the column index, KEEP (``compute_fixed_size_new_basis_tensor``,
+    ``time_evo_util/bug_util.py:93-121``; leaf: ``common_bug.py:94-101``)."""
+    Q, _ = _split_toward(T, 0)
+    return Q
+
+
+def _in_new_child_bases(T, tree, nid, Ms):
+    """Contract each child's basis change tensor M_g (old, new) into T's leg
+    toward g (``contract_all_children``)."""
+    for g in tree.children[nid]:
+        a = tree.axis(nid, g)
+        T = np.moveaxis(np.tensordot(T, Ms[g], axes=([a], [0])), -1, a)
+    return T
+
+
+def _bug_update_node(c, P, envs_p, tree, W, dt, tol, child_tol):
+    """``update_node`` / ``update_leaf_node`` / ``update_non_leaf_node``
+    (``time_evo_util/common_bug.py:47-309``) with fixed rank. ``P`` has its
+    orthogonality centre at c's parent and ``envs_p`` all environments toward
+    it. Returns (new basis tensors of c's subtree, environment of c toward its
+    parent in the new basis, basis change tensor (old, new)). The reference
+    passes its solver options only to the root's children; deeper nodes run
+    with the defaults (``child_tol``)."""
+    p = tree.parent[c]
+    Q, R = _split_toward(P[p], tree.axis(p, c))
+    cur = dict(P)
+    cur[p] = Q
+    cur[c] = np.tensordot(R, P[c], axes=([1], [0]))
+    envs = dict(envs_p)
+    envs[(p, c)] = env_update(tree, p, c, cur[p], W[p], envs)
+    envs.pop((c, p), None)
+    new, Ms, blocks = {}, {}, {}
+    for g in tree.children[c]:
+        # every child starts from the environments as they were before any
+        # sibling was updated
+        sub, blocks[g], Ms[g] = _bug_update_node(g, cur, envs, tree, W, dt, child_tol, child_tol)
+        new.update(sub)
+    for g, b in blocks.items():
+        envs[(g, c)] = b
+    x = _in_new_child_bases(cur[c], tree, c, Ms)
+    upd = krylov_exp_action(x, lambda y: heff_apply(y, tree, c, W[c], envs), dt, -1j, krylov_tol=tol)
+    U = _bug_basis(upd)
+    old = _in_new_child_bases(P[c], tree, c, Ms)
+    legs = list(range(1, U.ndim))
+    M = np.tensordot(old, U.conj(), axes=(legs, legs))
+    new[c] = U
+    return new, env_update(tree, c, p, U, W[c], envs), M
+
+
+def fixed_bug_step(state: OState, W: dict, dt: float, krylov_tol=1e-10, default_tol=1e-10) -> OState:
+    """One step of ``FixedBUG`` (``time_evolution/fixed_bug.py:83-97``,
+    ``root_update`` in ``time_evo_util/common_bug.py:311-378``): every child of
+    the root updates its subtree recursively from the current state, then the
+    root tensor, expressed in the children's new bases, evolves by dt in the
+    new environments. The state must have its orthogonality centre at the root."""
+    tree = state.tree
+    root = tree.root
+    assert state.orth_center == root
+    envs = init_cache_but_one(state, W, root)
+    new, Ms, blocks = {}, {}, {}
+    for c in tree.children[root]:
+        sub, blocks[c], Ms[c] = _bug_update_node(c, state.tensors, envs, tree, W, dt, krylov_tol, default_tol)
+        new.update(sub)
+    for c, b in blocks.items():
+        envs[(c, root)] = b
+    x = _in_new_child_bases(state.tensors[root], tree, root, Ms)
+    new[root] = krylov_exp_action(x, lambda y: heff_apply(y, tree, root, W[root], envs), dt, -1j,
+                                  krylov_tol=krylov_tol)
+    out = OState(tree, new)
+    out.orth_center = root
+    return out
 
 
 # ----------------------------------------------------------------------------

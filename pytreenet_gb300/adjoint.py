@@ -316,22 +316,31 @@ def _rowoff(shape, ax, device):
     return _ROWOFF[key]
 
 
+def qr_keep_raw(A, ax):
+    """Householder QR (``ptn_zqr_keep``, KEEP: Q zero-padded when A is wide)
+    with leg ``ax`` as the column index: (Q with A's legs, R k x k)."""
+    shape = list(A.shape)
+    k = shape[ax]
+    m = A.numel() // k
+    lib = _lib.load()
+    Q = A.detach().contiguous().clone()
+    rowoff, cs = _rowoff(shape, ax, A.device)
+    R = torch.zeros((k, k), dtype=CDT, device=A.device)
+    work = torch.empty(((int(lib.ptn_zqr_work_bytes(m, k)) + 15) // 16,), dtype=CDT, device=A.device)
+    check(lib.ptn_zqr_keep(Q.data_ptr(), rowoff.data_ptr(), m, k, cs, R.data_ptr(), work.data_ptr(),
+                           E._stream_ptr()), "ptn_zqr_keep")
+    return Q, R
+
+
 class _QR(torch.autograd.Function):
     @staticmethod
     def forward(ctx, A, ax):
-        shape = list(A.shape)
-        k = shape[ax]
+        k = A.shape[ax]
         m = A.numel() // k
         if m < k:
             raise ValueError(f"QR split of a {m} x {k} matrix: the adjoint needs tall splits "
                              "(bond dimensions no larger than the subtree dimensions)")
-        lib = _lib.load()
-        Q = A.detach().contiguous().clone()
-        rowoff, cs = _rowoff(shape, ax, A.device)
-        R = torch.zeros((k, k), dtype=CDT, device=A.device)
-        work = torch.empty(((int(lib.ptn_zqr_work_bytes(m, k)) + 15) // 16,), dtype=CDT, device=A.device)
-        check(lib.ptn_zqr_keep(Q.data_ptr(), rowoff.data_ptr(), m, k, cs, R.data_ptr(), work.data_ptr(),
-                               E._stream_ptr()), "ptn_zqr_keep")
+        Q, R = qr_keep_raw(A, ax)
         ctx.save_for_backward(Q, R)
         ctx.ax = ax
         return Q, R

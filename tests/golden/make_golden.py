@@ -430,6 +430,71 @@ def saved_files(ptn):
     print("saved files written")
 
 
+def capped_state_tensors(spec, rng, chi):
+    """Gaussian tensors whose bond to a subtree of s sites has dimension
+    min(chi, 2^s, 2^(n-s)): every QR of a sweep is tall and of full rank."""
+    ch = children_of(spec)
+    n = len(spec)
+    size = {}
+    for nid, _ in reversed(spec):
+        size[nid] = 1 + sum(size[c] for c in ch[nid])
+
+    def bond(c):
+        return int(min(chi, 2 ** size[c], 2 ** (n - size[c])))
+    out = {}
+    for nid, p in spec:
+        shape = ([bond(nid)] if p is not None else []) + [bond(c) for c in ch[nid]] + [2]
+        out[nid] = (rng.normal(size=shape) + 1j * rng.normal(size=shape)) / np.sqrt(2)
+    return out
+
+
+def run_case_bug(ptn, name, spec, tensors, ham_fn, dt, steps, tol):
+    """The reference's fixed-rank BUG (``time_evolution/fixed_bug.py``,
+    ``time_evo_util/common_bug.py``) with KRYLOV local exponentials."""
+    from pytreenet.time_evolution.time_evolution import TimeEvoMode
+    from pytreenet.time_evolution.fixed_bug import FixedBUG, FixedBUGConfig
+    psi = build_reference_state(ptn, spec, tensors)
+    psi.canonical_form(spec[0][0])
+    psi.normalise()
+    tensors = export_state(psi, spec)
+    psi = build_reference_state(ptn, spec, tensors)
+    H = ptn.TTNO.from_hamiltonian(ham_fn(psi), psi)
+    ops = {nid: ptn.TensorProduct({nid: Z}) for nid, _ in spec}
+    algo = FixedBUG(psi, H, dt, dt * steps, ops, config=FixedBUGConfig(time_evo_mode=TimeEvoMode.KRYLOV),
+                    solver_options={"krylov_tol": tol})
+    rec = {"spec_ids": np.array([s[0] for s in spec]),
+           "spec_parents": np.array(["" if s[1] is None else s[1] for s in spec]),
+           "dt": dt, "steps": steps, "order": 1, "krylov_tol": tol, "bug": 1,
+           "update_path": np.array([])}
+    for nid, t in tensors.items():
+        rec[f"init/{nid}"] = t
+    for nid, t in export_ttno(H, spec).items():
+        rec[f"ttno/{nid}"] = t
+    zs = []
+    for step in range(steps):
+        algo.run_one_time_step()
+        zs.append([algo.state.operator_expectation_value(ops[nid]) for nid, _ in spec])
+    rec["z"] = np.array(zs)
+    for nid, t in export_state(algo.state, spec).items():
+        rec[f"final/{nid}"] = t
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **rec)
+    print(name, "written")
+
+
+def bug_cases(ptn):
+    rng = np.random.default_rng(31)
+    spec = binary_tree(15)
+    run_case_bug(ptn, "binary15_tfim_fixed_bug", spec, capped_state_tensors(spec, rng, 8),
+                 lambda psi: tfim(ptn, spec, g=0.7), 0.05, 4, 1e-12)
+    spec = ternary_tree(2)
+    ne = len(spec) - 1
+    jxy = rng.uniform(0.5, 1.5, size=ne)
+    jz = rng.uniform(0.5, 1.5, size=ne)
+    run_case_bug(ptn, "ternary2_xxz_fixed_bug", spec, capped_state_tensors(spec, rng, 4),
+                 lambda psi: heisenberg_fields(ptn, spec, rng.uniform(-1, 1, size=len(spec)), jxy, jz),
+                 0.05, 3, 1e-12)
+
+
 def time_dep_cases(ptn):
     rng = np.random.default_rng(77)
     spec = binary_tree(7)
@@ -487,6 +552,7 @@ def main(ref_root):
     unit_cases(ptn)
     time_dep_cases(ptn)
     saved_files(ptn)
+    bug_cases(ptn)
 
 
 if __name__ == "__main__":

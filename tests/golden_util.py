@@ -43,6 +43,7 @@ CASES = ["c1_binary15_tfim_chi8", "binary7_tfim_chi4_o2", "ttree3_heis_chi6_o1",
 TWO_SITE_CASES = ["ternary2_xxz_neel_2tdvp", "binary7_heis_2tdvp_trunc"]
 TEBD_CASES = ["binary7_tfim_tebd"]
 DRIVEN_CASES = ["binary7_tfim_driven_o1", "binary7_tfim_driven_o2"]
+BUG_CASES = ["binary15_tfim_fixed_bug", "ternary2_xxz_fixed_bug"]
 
 
 def driven_ttno(case, t):
@@ -143,3 +144,25 @@ def run_driven_case(name, precision="plain"):
     res = algo.run()
     out = {nid: algo.state.get_phys_numpy(nid) for nid, _ in c["spec"]}
     return c, O.OState(oracle_state(c).tree, out), np.real(res[1:1 + c["steps"]])
+
+
+def run_bug_case(name):
+    """Run the engine's FixedBUG on a BUG fixture; returns (case, oracle-state of
+    the result, <Z_i> after each step)."""
+    import numpy as np
+    import oracle as O
+    import pytreenet_gb300 as P
+    from pytreenet_gb300.bug import FixedBUG, FixedBUGConfig
+    c = load_case(name)
+    st = build_ttn(P.TTNS, c["spec"], c["init"])
+    H = build_ttn(P.TTNO, c["spec"], c["ttno"])
+    Zm = np.diag([1.0, -1.0]).astype(complex)
+    algo = FixedBUG(st, H, c["dt"], c["dt"] * c["steps"], {},
+                    config=FixedBUGConfig(time_evo_mode=P.TimeEvoMode.KRYLOV),
+                    solver_options={"krylov_tol": c["krylov_tol"]})
+    zs = []
+    for _ in range(c["steps"]):
+        algo.run_one_time_step()
+        zs.append([algo.evaluate_operator({nid: Zm}) for nid, _ in c["spec"]])
+    out = {nid: algo.state.get_phys_numpy(nid) for nid, _ in c["spec"]}
+    return c, O.OState(oracle_state(c).tree, out), np.array(zs)

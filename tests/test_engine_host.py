@@ -478,3 +478,14 @@ def test_ttn_files_written_by_reference(monkeypatch, tmp_path):
     algo = P.FirstOrderOneSiteTDVP(st, H, 0.05, 0.1, {}, config=P.TDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV))
     algo.run_one_time_step()
     assert abs(algo.evaluate_operator(P.TensorProduct({})) - vals["norm2"]) < 1e-10
+
+
+@pytest.mark.parametrize("name", ["binary15_tfim_fixed_bug", "ternary2_xxz_fixed_bug"])
+def test_engine_host_fixed_bug_matches_reference(monkeypatch, name):
+    """Fixed-rank BUG on the engine against the reference's FixedBUG."""
+    fake_ptn.install(monkeypatch)
+    from golden_util import run_bug_case
+    c, st, z = run_bug_case(name)
+    assert np.max(np.abs(z - c["z"])) < 1e-10
+    one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), st)
+    assert one_minus_f < 1e-12

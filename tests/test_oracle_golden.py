@@ -177,3 +177,19 @@ def test_oracle_time_dependent_hamiltonian(name):
     assert zerr < 1e-10
     assert one_minus_f < 1e-12
     assert zstatic > 1e-4            # the drive matters at this resolution
+
+
+@pytest.mark.parametrize("name", ["binary15_tfim_fixed_bug", "ternary2_xxz_fixed_bug"])
+def test_oracle_fixed_bug_matches_reference(name):
+    """Fixed-rank BUG: the oracle's step against the reference's FixedBUG."""
+    c = load_case(name)
+    st = oracle_state(c)
+    st.orth_center = c["spec"][0][0]
+    zerr = 0.0
+    for k in range(c["steps"]):
+        st = O.fixed_bug_step(st, c["ttno"], c["dt"], krylov_tol=c["krylov_tol"])
+        z = np.array([O.expect_product(st, {nid: Zm}) for nid, _ in c["spec"]])
+        zerr = max(zerr, float(np.max(np.abs(z - c["z"][k]))))
+    one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), st)
+    assert zerr < 1e-10
+    assert one_minus_f < 1e-12

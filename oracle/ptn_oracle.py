@@ -28,7 +28,7 @@ __all__ = [
     "scalar_product", "SVDParams", "truncate_singular_values", "two_site_merge",
     "two_site_heff_apply", "two_site_split", "SecondOrderTwoSiteTDVPOracle",
     "FirstOrderTwoSiteTDVPOracle", "tebd_apply_gate", "TEBDOracle", "ttno_expectation",
-    "fixed_bug_step",
+    "fixed_bug_step", "adaptive_bug_step", "svd_truncation", "leaf_to_leaf_path",
 ]
 
 
@@ -417,6 +417,49 @@ def leaf_to_root_path(tree: OTree):
     return path
 
 
+def leaf_to_leaf_path(tree: OTree):
+    """``TDVPUpdatePathFinder_LeafToLeaf.find_path`` (``update_path.py:255-396``):
+    the first pair of leaves at maximal distance (leaves in node order, the
+    root counted when it has one neighbour), the path between them, and every
+    off-path subtree visited children first just before the main-path node it
+    hangs from."""
+    leaves = [nid for nid in tree.nodes if tree.is_leaf(nid)]
+    if len(tree.lneighbours(tree.root)) == 1:
+        leaves.append(tree.root)
+    best, pair = -1, (leaves[0], leaves[0])
+    for i in range(len(leaves)):
+        di = tree.distance_to_node(leaves[i])
+        for j in range(i + 1, len(leaves)):
+            if di[leaves[j]] > best:
+                best, pair = di[leaves[j]], (leaves[i], leaves[j])
+    main = tree.path_from_to(*pair)
+    visited, path = set(), []
+
+    def sub(nid):
+        if nid in visited or nid in main:
+            return []
+        visited.add(nid)
+        out = []
+        p = tree.parent[nid]
+        if p is not None and p not in main and p not in visited:
+            out += sub(p)
+        for c in tree.lchildren[nid]:
+            if c not in main and c not in visited:
+                out += sub(c)
+        return out + [nid]
+    for origin in main:
+        p = tree.parent[origin]
+        if p is not None and p not in main and p not in visited:
+            path += sub(p)
+        for c in tree.lchildren[origin]:
+            if c not in main:
+                path += sub(c)
+        if origin not in visited:
+            visited.add(origin)
+            path.append(origin)
+    return path
+
+
 def orthogonalisation_paths(tree: OTree, path):
     """``find_orthogonalisation_path`` (``update_path.py:400-421``)."""
     return [tree.path_from_to(path[i], path[i + 1])[1:] for i in range(len(path) - 1)]
@@ -430,7 +473,7 @@ class _OneSiteBase:
     (``tdvp_algorithms/tdvp_algorithm.py:58-221``, ``onesitetdvp.py:17-134``)."""
 
     def __init__(self, state: OState, W: dict, dt: float, krylov_tol=1e-10,
-                 max_krylov_dim=None):
+                 max_krylov_dim=None, path_mode: str = "LeafToRoot"):
         self.state = state.copy()
         self.W = W
         self.dt = dt
@@ -438,7 +481,7 @@ class _OneSiteBase:
         self.maxdim = max_krylov_dim
         self.krylov_dims = []
         init_tree = state.tree.copy()
-        self.update_path = leaf_to_root_path(init_tree)
+        self.update_path = leaf_to_leaf_path(init_tree) if path_mode == "LeafToLeaf" else leaf_to_root_path(init_tree)
         self.orth_paths = orthogonalisation_paths(init_tree, self.update_path)
         if self.state.orth_center is None:
             canonical_form(self.state, self.update_path[0])
@@ -596,6 +639,108 @@ def _bug_update_node(c, P, envs_p, tree, W, dt, tol, child_tol):
     M = np.tensordot(old, U.conj(), axes=(legs, legs))
     new[c] = U
     return new, env_update(tree, c, p, U, W[c], envs), M
+
+
+def _split_reduced(A, ax):
+    """QR with SplitMode.REDUCED: the bond shrinks to the row count when A is wide."""
+    At = np.moveaxis(A, ax, -1)
+    k = At.shape[-1]
+    q, r = np.linalg.qr(At.reshape(-1, k), mode="reduced")
+    return np.moveaxis(q.reshape(At.shape[:-1] + (q.shape[1],)), -1, ax), r
+
+
+def _move_center(state: OState, target: str, reduced: bool):
+    tree = state.tree
+    path = tree.path_from_to(state.orth_center, target)
+    for a, b in zip(path[:-1], path[1:]):
+        split = _split_reduced if reduced else _split_toward
+        Q, R = split(state.tensors[a], tree.axis(a, b))
+        state.tensors[a] = Q
+        ax = tree.axis(b, a)
+        state.tensors[b] = np.moveaxis(np.tensordot(R, state.tensors[b], axes=([1], [ax])), 0, ax)
+    state.orth_center = target
+
+
+def svd_truncation(state: OState, params: SVDParams) -> OState:
+    """``svd_truncation`` with one-site compressions (``core/truncation/svd_truncation.py``):
+    along the leaf-to-leaf path, the centre moves to each non-root node (REDUCED
+    QR) and the bond to its parent is cut by a truncated SVD, U staying at the
+    node and S V^H going into the parent (``compress_parent_leg``)."""
+    tree = state.tree
+    path = leaf_to_leaf_path(tree)
+    _move_center(state, path[0], reduced=True)
+    for nid in path:
+        if nid == tree.root:
+            continue
+        _move_center(state, nid, reduced=True)
+        T = state.tensors[nid]
+        k = T.shape[0]
+        u, s, vh = np.linalg.svd(T.reshape(k, -1).T, full_matrices=False)
+        r, new_s = truncate_singular_values(s, params)
+        state.tensors[nid] = u[:, :r].T.reshape((r,) + T.shape[1:])
+        p = tree.parent[nid]
+        ax = tree.axis(p, nid)
+        svh = new_s[:, None] * vh[:r]
+        state.tensors[p] = np.moveaxis(np.tensordot(svh, state.tensors[p], axes=([1], [ax])), 0, ax)
+        state.orth_center = p
+    return state
+
+
+def _adaptive_bug_update_node(c, P, envs_p, tree, W, dt, tol, child_tol):
+    """``update_node`` of the rank-adaptive BUG (``common_bug.py:47-309`` with
+    ``fixed_rank=False``): REDUCED moves, and the new basis spans the old and
+    the evolved tensor (``compute_new_basis_tensor``, ``bug_util.py:123-157``;
+    a leaf concatenates its old basis tensor, an inner node its old centre
+    tensor in the children's new bases)."""
+    p = tree.parent[c]
+    Q, R = _split_reduced(P[p], tree.axis(p, c))
+    cur = dict(P)
+    cur[p] = Q
+    cur[c] = np.tensordot(R, P[c], axes=([1], [0]))
+    envs = dict(envs_p)
+    envs[(p, c)] = env_update(tree, p, c, cur[p], W[p], envs)
+    envs.pop((c, p), None)
+    new, Ms, blocks = {}, {}, {}
+    for g in tree.children[c]:
+        sub, blocks[g], Ms[g] = _adaptive_bug_update_node(g, cur, envs, tree, W, dt, child_tol, child_tol)
+        new.update(sub)
+    for g, b in blocks.items():
+        envs[(g, c)] = b
+    x = _in_new_child_bases(cur[c], tree, c, Ms)
+    upd = krylov_exp_action(x, lambda y: heff_apply(y, tree, c, W[c], envs), dt, -1j, krylov_tol=tol)
+    old = _in_new_child_bases(P[c], tree, c, Ms)
+    first = old if not tree.children[c] else x
+    U, _ = _split_reduced(np.concatenate([first, upd], axis=0), 0)
+    legs = list(range(1, U.ndim))
+    M = np.tensordot(old, U.conj(), axes=(legs, legs))
+    new[c] = U
+    return new, env_update(tree, c, p, U, W[c], envs), M
+
+
+def adaptive_bug_step(state: OState, W: dict, dt: float, svd: SVDParams, krylov_tol=1e-10,
+                      default_tol=1e-10) -> OState:
+    """One step of the rank-adaptive ``BUG`` (``time_evolution/bug.py:84-117``):
+    the augmented-basis root update, then ``svd_truncation`` and the centre
+    back at the root."""
+    tree = state.tree
+    root = tree.root
+    assert state.orth_center == root
+    envs = init_cache_but_one(state, W, root)
+    new, Ms, blocks = {}, {}, {}
+    for c in tree.children[root]:
+        sub, blocks[c], Ms[c] = _adaptive_bug_update_node(c, state.tensors, envs, tree, W, dt, krylov_tol,
+                                                          default_tol)
+        new.update(sub)
+    for c, b in blocks.items():
+        envs[(c, root)] = b
+    x = _in_new_child_bases(state.tensors[root], tree, root, Ms)
+    new[root] = krylov_exp_action(x, lambda y: heff_apply(y, tree, root, W[root], envs), dt, -1j,
+                                  krylov_tol=krylov_tol)
+    out = OState(tree, new)
+    out.orth_center = root
+    svd_truncation(out, svd)
+    _move_center(out, root, reduced=False)
+    return out
 
 
 def fixed_bug_step(state: OState, W: dict, dt: float, krylov_tol=1e-10, default_tol=1e-10) -> OState:

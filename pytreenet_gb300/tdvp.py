@@ -135,6 +135,58 @@ def leaf_to_root_update_path(ttn) -> list[str]:
     return path
 
 
+def leaf_to_leaf_update_path(ttn) -> list[str]:
+    """``TDVPUpdatePathFinder_LeafToLeaf.find_path``
+    (``time_evolution/time_evo_util/update_path.py:255-396``): the first pair of
+    leaves at maximal distance (leaves in node order, the root included when it
+    has a single neighbour), the path between them, and every off-path subtree,
+    children first, just before the main-path node it hangs from."""
+    leaves = [nid for nid in ttn._order if ttn.nodes[nid].is_leaf()]
+    if ttn.nodes[ttn.root_id].nneighbours() == 1:
+        leaves.append(ttn.root_id)
+    best, pair = -1, (leaves[0], leaves[0])
+    for i in range(len(leaves)):
+        di = ttn.distance_to_node(leaves[i])
+        for j in range(i + 1, len(leaves)):
+            if di[leaves[j]] > best:
+                best, pair = di[leaves[j]], (leaves[i], leaves[j])
+    main = ttn.path_from_to(*pair)
+    on_main = set(main)
+    visited: set = set()
+    path: list[str] = []
+
+    def subtree(nid):
+        if nid in visited or nid in on_main:
+            return []
+        visited.add(nid)
+        node = ttn.nodes[nid]
+        out = []
+        if node.parent is not None and node.parent not in on_main and node.parent not in visited:
+            out += subtree(node.parent)
+        for c in node.children:
+            if c not in on_main and c not in visited:
+                out += subtree(c)
+        return out + [nid]
+    for origin in main:
+        node = ttn.nodes[origin]
+        if node.parent is not None and node.parent not in on_main and node.parent not in visited:
+            path += subtree(node.parent)
+        for c in node.children:
+            if c not in on_main:
+                path += subtree(c)
+        if origin not in visited:
+            visited.add(origin)
+            path.append(origin)
+    return path
+
+
+def find_update_path(ttn, mode: "PathFinderMode") -> list[str]:
+    """``find_path`` (``update_path.py:15-31``) for the two path modes."""
+    if mode is PathFinderMode.LeafToLeaf:
+        return leaf_to_leaf_update_path(ttn)
+    return leaf_to_root_update_path(ttn)
+
+
 class TensorProduct(dict):
     """Single-site operators keyed by node id (``operators/tensorproduct.py:33``)."""
 
@@ -175,7 +227,7 @@ class OneSiteTDVP:
         initial_state._finalise()
         self._initial_state = initial_state.copy_structure()
         self.state = initial_state.copy_structure()
-        self.update_path = leaf_to_root_update_path(self._initial_state)
+        self.update_path = find_update_path(self._initial_state, self.config.main_path_mode)
         self.orthogonalization_path = [self.state.path_from_to(self.update_path[i], self.update_path[i + 1])[1:]
                                        for i in range(len(self.update_path) - 1)]
         self.precision = precision

@@ -182,9 +182,10 @@ def heisenberg_fields(ptn, spec, fields, jxy=None, jz=None):
     return ptn.Hamiltonian(terms, conv)
 
 
-def run_case(ptn, name, spec, tensors, ham_fn, dt, steps, order, tol, canonical_random=False):
+def run_case(ptn, name, spec, tensors, ham_fn, dt, steps, order, tol, canonical_random=False, path_mode=None):
     from pytreenet.time_evolution.time_evolution import TimeEvoMode
     from pytreenet.time_evolution.tdvp_algorithms.tdvp_algorithm import TDVPConfig
+    from pytreenet.time_evolution.time_evo_util import PathFinderMode
     psi = build_reference_state(ptn, spec, tensors)
     if canonical_random:
         psi.canonical_form(spec[0][0])
@@ -194,13 +195,16 @@ def run_case(ptn, name, spec, tensors, ham_fn, dt, steps, order, tol, canonical_
     H = ptn.TTNO.from_hamiltonian(ham_fn(psi), psi)
     cls = ptn.FirstOrderOneSiteTDVP if order == 1 else ptn.SecondOrderOneSiteTDVP
     ops = {nid: ptn.TensorProduct({nid: Z}) for nid, _ in spec}
-    algo = cls(psi, H, dt, dt * steps, ops,
-               config=TDVPConfig(time_evo_mode=TimeEvoMode.KRYLOV),
-               solver_options={"krylov_tol": tol})
+    cfg = TDVPConfig(time_evo_mode=TimeEvoMode.KRYLOV)
+    if path_mode is not None:
+        cfg = TDVPConfig(time_evo_mode=TimeEvoMode.KRYLOV, main_path_mode=PathFinderMode[path_mode])
+    algo = cls(psi, H, dt, dt * steps, ops, config=cfg, solver_options={"krylov_tol": tol})
     rec = {"spec_ids": np.array([s[0] for s in spec]),
            "spec_parents": np.array(["" if s[1] is None else s[1] for s in spec]),
            "dt": dt, "steps": steps, "order": order, "krylov_tol": tol,
            "update_path": np.array(algo.update_path)}
+    if path_mode is not None:
+        rec["path_mode"] = path_mode
     for nid, t in tensors.items():
         rec[f"init/{nid}"] = t
     for nid, t in export_ttno(H, spec).items():
@@ -481,6 +485,42 @@ def run_case_bug(ptn, name, spec, tensors, ham_fn, dt, steps, tol):
     print(name, "written")
 
 
+def run_case_adaptive_bug(ptn, name, spec, tensors, ham_fn, dt, steps, tol, svd):
+    """The reference's rank-adaptive BUG (``time_evolution/bug.py``): bases
+    augmented with the evolved tensors, then ``svd_truncation``. The bond cap
+    does not bind, so the truncation keeps every singular value above the
+    tolerances and its visiting order (which in the reference follows the
+    node dictionary order) cannot change the result beyond them."""
+    from pytreenet.time_evolution.time_evolution import TimeEvoMode
+    from pytreenet.time_evolution.bug import BUG, BUGConfig
+    psi = build_reference_state(ptn, spec, tensors)
+    H = ptn.TTNO.from_hamiltonian(ham_fn(psi), psi)
+    ops = {nid: ptn.TensorProduct({nid: Z}) for nid, _ in spec}
+    maxd, rel, tot = svd
+    cfg = BUGConfig(time_evo_mode=TimeEvoMode.KRYLOV, max_bond_dim=maxd, rel_tol=rel, total_tol=tot)
+    algo = BUG(psi, H, dt, dt * steps, ops, config=cfg, solver_options={"krylov_tol": tol})
+    rec = {"spec_ids": np.array([s[0] for s in spec]),
+           "spec_parents": np.array(["" if s[1] is None else s[1] for s in spec]),
+           "dt": dt, "steps": steps, "order": 1, "krylov_tol": tol, "bug": 2,
+           "update_path": np.array([]), "svd_max_bond_dim": maxd, "svd_rel_tol": rel, "svd_total_tol": tot,
+           "svd_renorm": 0}
+    for nid, t in tensors.items():
+        rec[f"init/{nid}"] = t
+    for nid, t in export_ttno(H, spec).items():
+        rec[f"ttno/{nid}"] = t
+    zs, bonds = [], []
+    for step in range(steps):
+        algo.run_one_time_step()
+        zs.append([algo.state.operator_expectation_value(ops[nid]) for nid, _ in spec])
+        bonds.append([algo.state.tensors[nid].shape[0] for nid, p in spec if p is not None])
+    rec["z"] = np.array(zs)
+    rec["bonds"] = np.array(bonds)
+    for nid, t in export_state(algo.state, spec).items():
+        rec[f"final/{nid}"] = t
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **rec)
+    print(name, "written; bonds", bonds[-1])
+
+
 def bug_cases(ptn):
     rng = np.random.default_rng(31)
     spec = binary_tree(15)
@@ -493,6 +533,28 @@ def bug_cases(ptn):
     run_case_bug(ptn, "ternary2_xxz_fixed_bug", spec, capped_state_tensors(spec, rng, 4),
                  lambda psi: heisenberg_fields(ptn, spec, rng.uniform(-1, 1, size=len(spec)), jxy, jz),
                  0.05, 3, 1e-12)
+    spec = binary_tree(7)
+    run_case_adaptive_bug(ptn, "binary7_tfim_bug", spec, capped_state_tensors(spec, rng, 1),
+                          lambda psi: tfim(ptn, spec, g=0.8), 0.05, 4, 1e-12, (100, 1e-10, 1e-10))
+    spec = ternary_tree(2)
+    run_case_adaptive_bug(ptn, "ternary2_xxz_bug", spec, neel_state_tensors(spec),
+                          lambda psi: heisenberg_fields(ptn, spec, np.zeros(len(spec)), jxy, jz),
+                          0.05, 3, 1e-12, (100, 1e-10, 1e-10))
+
+
+def leaf_to_leaf_cases(ptn):
+    """One-site TDVP on the leaf-to-leaf update path
+    (``PathFinderMode.LeafToLeaf``, ``update_path.py:255-396``)."""
+    rng = np.random.default_rng(41)
+    spec = t_tree(3)
+    h = rng.uniform(-1, 1, size=len(spec))
+    run_case(ptn, "ttree3_heis_l2l_o1", spec, capped_state_tensors(spec, rng, 6),
+             lambda psi: heisenberg_fields(ptn, spec, h), 0.02, 3, 1, 1e-12, canonical_random=True,
+             path_mode="LeafToLeaf")
+    spec = binary_tree(15)
+    run_case(ptn, "binary15_tfim_l2l_o2", spec, capped_state_tensors(spec, rng, 6),
+             lambda psi: tfim(ptn, spec, g=0.6), 0.02, 3, 2, 1e-12, canonical_random=True,
+             path_mode="LeafToLeaf")
 
 
 def time_dep_cases(ptn):
@@ -553,6 +615,7 @@ def main(ref_root):
     time_dep_cases(ptn)
     saved_files(ptn)
     bug_cases(ptn)
+    leaf_to_leaf_cases(ptn)
 
 
 if __name__ == "__main__":

@@ -25,6 +25,7 @@ def load_case(name):
         "two_site": bool(int(d["two_site"])) if "two_site" in d.files else False,
         "energy_final": complex(d["energy_final"]) if "energy_final" in d.files else None,
     }
+    case["path_mode"] = str(d["path_mode"]) if "path_mode" in d.files else "LeafToRoot"
     case["tebd"] = bool(int(d["tebd"])) if "tebd" in d.files else False
     case["driven"] = "amp" in d.files
     if case["driven"]:
@@ -44,6 +45,8 @@ TWO_SITE_CASES = ["ternary2_xxz_neel_2tdvp", "binary7_heis_2tdvp_trunc"]
 TEBD_CASES = ["binary7_tfim_tebd"]
 DRIVEN_CASES = ["binary7_tfim_driven_o1", "binary7_tfim_driven_o2"]
 BUG_CASES = ["binary15_tfim_fixed_bug", "ternary2_xxz_fixed_bug"]
+ADAPTIVE_BUG_CASES = ["binary7_tfim_bug", "ternary2_xxz_bug"]
+L2L_CASES = ["ttree3_heis_l2l_o1", "binary15_tfim_l2l_o2"]
 
 
 def driven_ttno(case, t):
@@ -166,3 +169,28 @@ def run_bug_case(name):
         zs.append([algo.evaluate_operator({nid: Zm}) for nid, _ in c["spec"]])
     out = {nid: algo.state.get_phys_numpy(nid) for nid, _ in c["spec"]}
     return c, O.OState(oracle_state(c).tree, out), np.array(zs)
+
+
+def run_one_site_case(name, precision="plain"):
+    """The engine's one-site driver on a fixture, honouring its path mode;
+    returns (case, oracle-state of the result, max |<Z_i> - reference| over steps)."""
+    import numpy as np
+    import oracle as O
+    import pytreenet_gb300 as P
+    c = load_case(name)
+    st = build_ttn(P.TTNS, c["spec"], c["init"])
+    H = build_ttn(P.TTNO, c["spec"], c["ttno"])
+    cls = P.FirstOrderOneSiteTDVP if c["order"] == 1 else P.SecondOrderOneSiteTDVP
+    algo = cls(st, H, c["dt"], c["dt"] * c["steps"], {},
+               config=P.TDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV,
+                                   main_path_mode=P.PathFinderMode[c["path_mode"]]),
+               solver_options={"krylov_tol": c["krylov_tol"]}, precision=precision)
+    assert algo.update_path == c["update_path"]
+    Zm = np.diag([1.0, -1.0]).astype(complex)
+    zerr = 0.0
+    for k in range(c["steps"]):
+        algo.run_one_time_step()
+        z = np.array([algo.evaluate_operator({nid: Zm}) for nid, _ in c["spec"]])
+        zerr = max(zerr, float(np.max(np.abs(z - c["z"][k]))))
+    out = {nid: algo.state.get_phys_numpy(nid) for nid, _ in c["spec"]}
+    return c, O.OState(oracle_state(c).tree, out), zerr

@@ -489,3 +489,14 @@ def test_engine_host_fixed_bug_matches_reference(monkeypatch, name):
     assert np.max(np.abs(z - c["z"])) < 1e-10
     one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), st)
     assert one_minus_f < 1e-12
+
+
+@pytest.mark.parametrize("name", ["ttree3_heis_l2l_o1", "binary15_tfim_l2l_o2"])
+def test_engine_host_leaf_to_leaf_path(monkeypatch, name):
+    """TDVPConfig(main_path_mode=LeafToLeaf): the reference's path and results."""
+    fake_ptn.install(monkeypatch)
+    from golden_util import run_one_site_case
+    c, st, zerr = run_one_site_case(name)
+    one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), st)
+    assert zerr < 1e-10
+    assert one_minus_f < 1e-12

@@ -64,3 +64,13 @@ def test_gpu_tdvp_ttree_chi16_vs_oracle():
     got = O.OState(tree, {nid: algo.state.get_phys_numpy(nid) for nid, _ in spec})
     one_minus_f, dist = fidelity_and_dist(ora.state, got)
     assert one_minus_f < 1e-12
+
+
+@pytest.mark.parametrize("name", ["ttree3_heis_l2l_o1", "binary15_tfim_l2l_o2"])
+def test_gpu_leaf_to_leaf_path(name):
+    """TDVPConfig(main_path_mode=LeafToLeaf) on the GB300 against the reference."""
+    from golden_util import run_one_site_case
+    c, st, zerr = run_one_site_case(name)
+    one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), st)
+    assert zerr < 1e-10
+    assert one_minus_f < 1e-12

@@ -11,7 +11,7 @@ Zm = np.diag([1.0, -1.0]).astype(complex)
 def _run(c, steps=None):
     st = oracle_state(c)
     cls = O.FirstOrderOneSiteTDVPOracle if c["order"] == 1 else O.SecondOrderOneSiteTDVPOracle
-    algo = cls(st, c["ttno"], c["dt"], krylov_tol=c["krylov_tol"])
+    algo = cls(st, c["ttno"], c["dt"], krylov_tol=c["krylov_tol"], path_mode=c["path_mode"])
     assert algo.update_path == c["update_path"]
     zerr = 0.0
     for k in range(c["steps"] if steps is None else steps):
@@ -191,5 +191,38 @@ def test_oracle_fixed_bug_matches_reference(name):
         z = np.array([O.expect_product(st, {nid: Zm}) for nid, _ in c["spec"]])
         zerr = max(zerr, float(np.max(np.abs(z - c["z"][k]))))
     one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), st)
+    assert zerr < 1e-10
+    assert one_minus_f < 1e-12
+
+
+@pytest.mark.parametrize("name", ["binary7_tfim_bug", "ternary2_xxz_bug"])
+def test_oracle_adaptive_bug_matches_reference(name):
+    """Rank-adaptive BUG with SVD truncation: the oracle against the reference's
+    BUG, including the bond dimensions after every step."""
+    d = np.load(f"{GOLDEN}/{name}.npz")
+    c = load_case(name)
+    params = O.SVDParams(max_bond_dim=int(d["svd_max_bond_dim"]), rel_tol=float(d["svd_rel_tol"]),
+                         total_tol=float(d["svd_total_tol"]), renorm=False)
+    st = oracle_state(c)
+    st.orth_center = None
+    O.canonical_form(st, c["spec"][0][0])
+    zerr = 0.0
+    for k in range(c["steps"]):
+        st = O.adaptive_bug_step(st, c["ttno"], c["dt"], params, krylov_tol=c["krylov_tol"])
+        z = np.array([O.expect_product(st, {nid: Zm}) for nid, _ in c["spec"]])
+        zerr = max(zerr, float(np.max(np.abs(z - c["z"][k]))))
+        bonds = [st.tensors[nid].shape[0] for nid, p in c["spec"] if p is not None]
+        assert bonds == list(d["bonds"][k])
+    one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), st)
+    assert zerr < 1e-9
+    assert one_minus_f < 1e-11
+
+
+@pytest.mark.parametrize("name", ["ttree3_heis_l2l_o1", "binary15_tfim_l2l_o2"])
+def test_oracle_leaf_to_leaf_path(name):
+    """One-site TDVP on PathFinderMode.LeafToLeaf: same path and results as the reference."""
+    c = load_case(name)
+    algo, zerr = _run(c)
+    one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), algo.state)
     assert zerr < 1e-10
     assert one_minus_f < 1e-12

@@ -6,7 +6,7 @@ FirstOrderOneSiteTDVP, SecondOrderOneSiteTDVP, FirstOrderTwoSiteTDVP,
 SecondOrderTwoSiteTDVP, TDVPConfig, TwoSiteTDVPConfig, SVDParameters, TEBD,
 TrotterStep, TrotterSplitting, TimeEvoMode, EvoDirection, TensorProduct; plus
 gradients through a hand-written adjoint (OneSiteTDVPAdjoint,
-coupling_gradient), the fixed-rank BUG integrator (FixedBUG) and
+coupling_gradient), the BUG integrators (FixedBUG, rank-adaptive BUG) and
 time-dependent TTNOs. Numerics run in libptn_gb300.so
 (hand-written CUDA for sm_103a) through a C ABI; see include/ptn_gb300.h.
 """
@@ -21,7 +21,7 @@ from .batch import run_realisations
 from .contractions import (SandwichCache, contract_ket_ham_with_envs, contract_any,
                            effective_single_site_evolution)
 from .adjoint import OneSiteTDVPAdjoint, coupling_gradient
-from .bug import FixedBUG, FixedBUGConfig
+from .bug import BUG, BUGConfig, FixedBUG, FixedBUGConfig
 from .time_dep import TimeDependentTTNO, FactorUpdatable, DiscreetTimeTTNO
 
 __all__ = [
@@ -33,6 +33,6 @@ __all__ = [
     "NumericOperator",
     "nearest_neighbour_ttno", "tfim_ttno", "heisenberg_ttno", "run_realisations",
     "SandwichCache", "contract_ket_ham_with_envs", "contract_any", "effective_single_site_evolution",
-    "OneSiteTDVPAdjoint", "coupling_gradient", "FixedBUG", "FixedBUGConfig",
+    "OneSiteTDVPAdjoint", "coupling_gradient", "FixedBUG", "FixedBUGConfig", "BUG", "BUGConfig",
     "TimeDependentTTNO", "FactorUpdatable", "DiscreetTimeTTNO",
 ]

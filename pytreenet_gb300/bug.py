@@ -27,9 +27,15 @@ from typing import Any
 import numpy as np
 import torch
 
+import ctypes
+
+from . import _lib
+from . import engine as E
 from .adjoint import (_SiteOp, _raw_contract, _solver, _tensor_apply, absorb, env_apply, qr_keep_raw)
-from .engine import DeviceNetwork
-from .tdvp import (TTNTimeEvolutionConfig, TensorProduct, TimeEvoMode, compute_num_time_steps)
+from .engine import CDT, DeviceNetwork, check
+from .tdvp import (TTNTimeEvolutionConfig, TensorProduct, TimeEvoMode, compute_num_time_steps,
+                   leaf_to_leaf_update_path)
+from .truncation import SVDParameters, truncate_singular_values
 
 DEFAULT_KRYLOV_TOL = 1e-10
 
@@ -48,6 +54,51 @@ class FixedBUGConfig(CommonBUGConfig):
 
     def __post_init__(self):
         self.fixed_rank = True
+
+
+@dataclass
+class BUGConfig(CommonBUGConfig, SVDParameters):
+    """``bug.py:15-27``: the BUG options and the truncation of ``svd_truncation``."""
+
+    def __post_init__(self):
+        SVDParameters.__post_init__(self)
+        assert self.fixed_rank is False, "Fixed rank is not supported for BUG!"
+
+
+def qr_split(A, ax, reduced: bool):
+    """QR with leg ``ax`` as the column index; ``reduced`` (SplitMode.REDUCED)
+    shrinks that leg to the row count when A is wide, else it is kept."""
+    Q, R = qr_keep_raw(A, ax)
+    k = A.shape[ax]
+    m = A.numel() // k
+    if reduced and m < k:
+        Q = Q.narrow(ax, 0, m).contiguous()
+        R = R[:m].contiguous()
+    return Q, R
+
+
+def small_svd(R: torch.Tensor):
+    """Jacobi SVD (``ptn_zsvd_jacobi``) of a k x k device matrix: returns U and V
+    as k x k tensors whose row j holds column j (U = Ut^T, V = Vt^T) and S on
+    the host, with R = U diag(S) V^H."""
+    lib = _lib.load()
+    k = R.shape[0]
+    R = R.contiguous()
+    Ut = torch.empty((k, k), dtype=CDT, device=R.device)
+    Vt = torch.empty((k, k), dtype=CDT, device=R.device)
+    Sb = torch.zeros((k + 2,), dtype=torch.float64, device=R.device)
+    work = torch.empty(((int(lib.ptn_zsvd_work_bytes(k, k)) + 15) // 16,), dtype=CDT, device=R.device)
+    d = _lib.SvdDesc()
+    d.A, d.m, d.n, d.row_stride, d.col_stride = R.data_ptr(), k, k, k, 1
+    d.U, d.ldu, d.S, d.V, d.ldv = Ut.data_ptr(), k, Sb.data_ptr(), Vt.data_ptr(), k
+    d.work = work.data_ptr()
+    d.status = Sb[k:].data_ptr()
+    check(lib.ptn_zsvd_jacobi(ctypes.byref(d), E._stream_ptr()), "ptn_zsvd_jacobi")
+    host = Sb.cpu()
+    code = int(host[k:k + 1].view(torch.int32)[0])
+    if code != 0:
+        raise _lib.PtnError(code, "Jacobi SVD")
+    return Ut, Vt, host[:k].numpy().copy()
 
 
 class FixedBUG:
@@ -113,10 +164,12 @@ class FixedBUG:
             T = _raw_contract(T, lT, Ms[g], [lT[ax], "new"], lout, [lT[ax]])
         return T
 
+    _adaptive = False
+
     def _update_node(self, c, P, envs_p, tol):
         """``update_node`` + ``update_leaf_node`` / ``update_non_leaf_node``."""
         p = self.parent[c]
-        Q, R = qr_keep_raw(P[p], self._ax(p, c))
+        Q, R = qr_split(P[p], self._ax(p, c), reduced=self._adaptive)
         cur = dict(P)
         cur[p] = Q
         cur[c] = absorb(R, P[c], self._ax(c, p))
@@ -128,9 +181,17 @@ class FixedBUG:
             sub, blocks[g], Ms[g] = self._update_node(g, cur, envs, DEFAULT_KRYLOV_TOL)
             new.update(sub)
         envs.update({(g, c): b for g, b in blocks.items()})
-        upd = self._evolve(c, self._in_new_child_bases(cur[c], c, Ms), envs, tol)
-        U, _ = qr_keep_raw(upd, 0)
+        x = self._in_new_child_bases(cur[c], c, Ms)
+        upd = self._evolve(c, x, envs, tol)
         old = self._in_new_child_bases(P[c], c, Ms)
+        if self._adaptive:
+            # the new basis spans the old and the evolved tensor
+            # (``compute_new_basis_tensor``, ``bug_util.py:123-157``): a leaf
+            # stacks its old basis tensor, an inner node its old centre tensor
+            first = old if not self.children[c] else x
+            U, _ = qr_split(torch.cat([first, upd], dim=0), 0, reduced=True)
+        else:
+            U, _ = qr_keep_raw(upd, 0)
         legs = [f"i{j}" for j in range(1, U.dim())]
         M = _raw_contract(old, ["p"] + legs, U, ["q"] + legs, ["p", "q"], legs, conj_b=True)
         new[c] = U
@@ -157,13 +218,19 @@ class FixedBUG:
         new[root] = self._evolve(root, self._in_new_child_bases(A[root], root, Ms), envs, tol)
         return new
 
+    def _store(self, new: dict):
+        for nid, t in new.items():
+            if tuple(t.shape) == tuple(self.net.t[nid].shape):
+                self.net.t[nid].copy_(t)
+            else:
+                self.net._forget_node(nid)
+                self.net._set_node_tensor(nid, t.contiguous())
+        self.state.orthogonality_center_id = self.root
+
     # -- driver API ------------------------------------------------------------------
     def run_one_time_step(self, **kwargs):
         with torch.no_grad():
-            new = self._root_update(dict(self.net.t))
-            for nid, t in new.items():
-                self.net.t[nid].copy_(t)
-        self.state.orthogonality_center_id = self.root
+            self._store(self._root_update(dict(self.net.t)))
 
     def evaluate_operator(self, operator) -> complex:
         from .ttn import TreeTensorNetworkOperator
@@ -190,3 +257,59 @@ class FixedBUG:
                 self.times.append((i + 1) * self.time_step_size)
         self.results = np.array(res)
         return self.results
+
+
+class BUG(FixedBUG):
+    """Rank-adaptive BUG (``time_evolution/bug.py:30-117``): every basis is
+    augmented with the evolved tensor (bond dimensions up to double), the
+    centre moves with REDUCED QRs, and after the root update ``svd_truncation``
+    (``core/truncation/svd_truncation.py``) cuts every bond by a truncated SVD
+    along the leaf-to-leaf path: the centre moves to each non-root node, its
+    parent leg is factored (Householder QR, then Jacobi SVD of the k x k R),
+    U stays and S V^H goes into the parent, with the rule of
+    ``truncate_singular_values`` (``BUGConfig``'s SVD fields). The centre then
+    returns to the root. The reference orders that path by its node
+    dictionary, which its BUG update rebuilds in a hash-dependent order; a bond
+    cap that binds can therefore make its result depend on the process, while
+    tolerance-limited truncations agree to the tolerance."""
+
+    config_class = BUGConfig
+    _adaptive = True
+
+    def _move(self, A, center, target, reduced):
+        path = self.state.path_from_to(center, target)
+        for a, b in zip(path[:-1], path[1:]):
+            Q, R = qr_split(A[a], self._ax(a, b), reduced=reduced)
+            A[a] = Q
+            A[b] = absorb(R, A[b], self._ax(b, a))
+        return target
+
+    def _compress_parent_leg(self, A, nid):
+        """``compress_parent_leg`` (``svd_truncation.py``)."""
+        T = A[nid]
+        Q, R = qr_keep_raw(T, 0)
+        Ut, Vt, s = small_svd(R)
+        new_s, _ = truncate_singular_values(s, self.config)
+        r = len(new_s)
+        A[nid] = absorb(Ut[:r].contiguous(), Q, 0)
+        p = self.parent[nid]
+        svh = new_s[:, None] * Vt[:r].cpu().numpy().conj()
+        A[p] = absorb(torch.from_numpy(np.ascontiguousarray(svh)).to(T.device), A[p], self._ax(p, nid))
+        return p
+
+    def truncation(self, A):
+        path = leaf_to_leaf_update_path(self.state)
+        center = self._move(A, self.root, path[0], True)
+        for nid in path:
+            if nid == self.root:
+                continue
+            center = self._move(A, center, nid, True)
+            center = self._compress_parent_leg(A, nid)
+        self._move(A, center, self.root, False)
+        return A
+
+    def run_one_time_step(self, **kwargs):
+        with torch.no_grad():
+            A = dict(self.net.t)
+            A.update(self._root_update(A))
+            self._store(self.truncation(A))

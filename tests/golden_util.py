@@ -194,3 +194,27 @@ def run_one_site_case(name, precision="plain"):
         zerr = max(zerr, float(np.max(np.abs(z - c["z"][k]))))
     out = {nid: algo.state.get_phys_numpy(nid) for nid, _ in c["spec"]}
     return c, O.OState(oracle_state(c).tree, out), zerr
+
+
+def run_adaptive_bug_case(name):
+    """The engine's rank-adaptive BUG on a fixture; returns (case, oracle-state of
+    the result, <Z_i> after each step, bond dimensions after each step)."""
+    import numpy as np
+    import oracle as O
+    import pytreenet_gb300 as P
+    from pytreenet_gb300.bug import BUG, BUGConfig
+    d = np.load(os.path.join(GOLDEN, name + ".npz"))
+    c = load_case(name)
+    st = build_ttn(P.TTNS, c["spec"], c["init"])
+    H = build_ttn(P.TTNO, c["spec"], c["ttno"])
+    Zm = np.diag([1.0, -1.0]).astype(complex)
+    cfg = BUGConfig(time_evo_mode=P.TimeEvoMode.KRYLOV, max_bond_dim=int(d["svd_max_bond_dim"]),
+                    rel_tol=float(d["svd_rel_tol"]), total_tol=float(d["svd_total_tol"]))
+    algo = BUG(st, H, c["dt"], c["dt"] * c["steps"], {}, config=cfg, solver_options={"krylov_tol": c["krylov_tol"]})
+    zs, bonds = [], []
+    for _ in range(c["steps"]):
+        algo.run_one_time_step()
+        zs.append([algo.evaluate_operator({nid: Zm}) for nid, _ in c["spec"]])
+        bonds.append([algo.state.phys(nid).shape[0] for nid, p in c["spec"] if p is not None])
+    out = {nid: algo.state.get_phys_numpy(nid) for nid, _ in c["spec"]}
+    return c, O.OState(oracle_state(c).tree, out), np.array(zs), np.array(bonds), d["bonds"]

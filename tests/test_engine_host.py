@@ -500,3 +500,16 @@ def test_engine_host_leaf_to_leaf_path(monkeypatch, name):
     one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), st)
     assert zerr < 1e-10
     assert one_minus_f < 1e-12
+
+
+@pytest.mark.parametrize("name", ["binary7_tfim_bug", "ternary2_xxz_bug"])
+def test_engine_host_adaptive_bug_matches_reference(monkeypatch, name):
+    """Rank-adaptive BUG on the engine against the reference's BUG, bond
+    dimensions included."""
+    fake_ptn.install(monkeypatch)
+    from golden_util import run_adaptive_bug_case
+    c, st, z, bonds, ref_bonds = run_adaptive_bug_case(name)
+    assert np.array_equal(bonds, ref_bonds)
+    assert np.max(np.abs(z - c["z"])) < 1e-9
+    one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), st)
+    assert one_minus_f < 1e-11

@@ -15,7 +15,7 @@ from .tdvp import (TimeEvoMode, EvoDirection, PathFinderMode, TDVPConfig, Tensor
                    FirstOrderOneSiteTDVP, SecondOrderOneSiteTDVP, leaf_to_root_update_path,
                    TwoSiteTDVPConfig, FirstOrderTwoSiteTDVP, SecondOrderTwoSiteTDVP)
 from .truncation import SVDParameters, truncate_singular_values
-from .tebd import TEBD, TrotterStep, TrotterSplitting, NumericOperator
+from .tebd import TEBD, TrotterStep, TrotterSplitting, NumericOperator, SWAPlist, swap_gate
 from .operators import nearest_neighbour_ttno, tfim_ttno, heisenberg_ttno
 from .batch import run_realisations
 from .contractions import (SandwichCache, contract_ket_ham_with_envs, contract_any,
@@ -30,7 +30,7 @@ __all__ = [
     "FirstOrderOneSiteTDVP", "SecondOrderOneSiteTDVP", "leaf_to_root_update_path",
     "TwoSiteTDVPConfig", "FirstOrderTwoSiteTDVP", "SecondOrderTwoSiteTDVP",
     "SVDParameters", "truncate_singular_values", "TEBD", "TrotterStep", "TrotterSplitting",
-    "NumericOperator",
+    "NumericOperator", "SWAPlist", "swap_gate",
     "nearest_neighbour_ttno", "tfim_ttno", "heisenberg_ttno", "run_realisations",
     "SandwichCache", "contract_ket_ham_with_envs", "contract_any", "effective_single_site_evolution",
     "OneSiteTDVPAdjoint", "coupling_gradient", "FixedBUG", "FixedBUGConfig", "BUG", "BUGConfig",

@@ -7,9 +7,10 @@ svd_parameters=None, config=None)`` with ``exponents``, ``trotter_splitting``,
 ``exponentiate_splitting(delta_time, ttn)`` returning operators that carry
 ``.operator`` (legs: outputs, then inputs) and ``.node_identifiers`` can be
 passed as the splitting -- PyTreeNet's own ``TrotterSplitting`` included. The
-module's ``TrotterStep`` / ``TrotterSplitting`` cover one- and two-site terms
-on neighbouring nodes (``time_evolution/trotter.py:105-322``, without the SWAP
-bookkeeping that non-neighbouring terms need).
+module's ``SWAPlist`` / ``TrotterStep`` / ``TrotterSplitting``
+(``time_evolution/trotter.py:15-322``) build the gate list, with SWAP gates
+before and after a step to bring the sites of a non-neighbouring term next to
+each other.
 """
 from __future__ import annotations
 
@@ -32,15 +33,63 @@ class NumericOperator:
     node_identifiers: list
 
 
+def swap_gate(dimension: int = 2) -> np.ndarray:
+    """SWAP of two sites of dimension d as a d^2 x d^2 matrix: |i j> -> |j i>."""
+    d = int(dimension)
+    m = np.zeros((d * d, d * d), dtype=complex)
+    for i in range(d):
+        for j in range(d):
+            m[j * d + i, i * d + j] = 1.0
+    return m
+
+
+def _open_dimension(ttn, nid) -> int:
+    return int(ttn.phys(nid).shape[-1])
+
+
+class SWAPlist(list):
+    """``time_evolution/trotter.py:15-103``: SWAP gates of neighbouring nodes,
+    each pair in the leg order of its gate."""
+
+    def __init__(self, swap_list=None):
+        swap_list = [] if swap_list is None else list(swap_list)
+        for pair in swap_list:
+            if len(pair) != 2:
+                raise ValueError("SWAPs can only happen between exactly two nodes!")
+        super().__init__(swap_list)
+
+    def is_compatible_with_ttn(self, ttn) -> bool:
+        for a, b in self:
+            if a not in ttn.nodes:
+                return False
+            if b not in ttn.nodes[a].neighbouring_nodes():
+                return False
+            if _open_dimension(ttn, a) != _open_dimension(ttn, b):
+                return False
+        return True
+
+    def into_operators(self, ttn=None, dim=None) -> list:
+        if ttn is None and dim is None and len(self) != 0:
+            raise ValueError("`ttn` and `dim` cannot both be `None`!")
+        out = []
+        for a, b in self:
+            d = _open_dimension(ttn, a) if ttn is not None else dim
+            out.append(NumericOperator(swap_gate(d).reshape(d, d, d, d), [a, b]))
+        return out
+
+
 class TrotterStep:
     """``time_evolution/trotter.py:105-194``: a tensor product of one-site
-    operators and the factor of its exponent."""
+    operators, the factor of its exponent, and SWAP gates applied before and
+    after the exponentiated operator."""
 
-    def __init__(self, operator: TensorProduct | dict, factor: float):
+    def __init__(self, operator: TensorProduct | dict, factor: float, swaps_before=None, swaps_after=None):
         self.operator = dict(operator)
         self.factor = factor
+        self.swaps_before = SWAPlist() if swaps_before is None else SWAPlist(swaps_before)
+        self.swaps_after = SWAPlist() if swaps_after is None else SWAPlist(swaps_after)
 
-    def exponentiate_operator(self, delta_time: float) -> NumericOperator:
+    def exponentiate_operator(self, delta_time: float, ttn=None, dim=None) -> NumericOperator:
         """exp(-i factor dt (A_1 x A_2 x ...)) with the factors in the tensor
         product's order, reshaped to (out_1, ..., out_n, in_1, ..., in_n)."""
         ids = list(self.operator)
@@ -52,20 +101,40 @@ class TrotterStep:
         dims = [m.shape[0] for m in mats]
         return NumericOperator(u.reshape(dims + dims), ids)
 
+    def realise_swaps(self, ttn=None, dim=None):
+        return self.swaps_before.into_operators(ttn, dim), self.swaps_after.into_operators(ttn, dim)
+
 
 class TrotterSplitting(list):
-    """``time_evolution/trotter.py:196-322`` for neighbouring terms: the
-    exponentiated steps in order."""
+    """``time_evolution/trotter.py:196-322``: the Trotter steps in order."""
+
+    def __init__(self, trotter_steps=None):
+        super().__init__([] if trotter_steps is None else trotter_steps)
+
+    @classmethod
+    def from_lists(cls, tensor_products, splitting=None, swaps_before=None, swaps_after=None):
+        """Steps from a list of tensor products: ``splitting`` gives (index,
+        factor) pairs (or bare indices, factor 1; default: every product once
+        in order); the SWAP lists are indexed like the products."""
+        if splitting is None:
+            splitting = [(i, 1) for i in range(len(tensor_products))]
+        steps = []
+        for split in splitting:
+            index, factor = (split, 1) if isinstance(split, (int, np.integer)) else (split[0], split[1])
+            steps.append(TrotterStep(tensor_products[index], factor,
+                                     swaps_before=None if swaps_before is None else swaps_before[index],
+                                     swaps_after=None if swaps_after is None else swaps_after[index]))
+        return cls(steps)
 
     def exponentiate_splitting(self, delta_time: float, ttn=None, dim=None) -> list:
+        """The gates of one time step: for every step its SWAPs before, the
+        exponentiated operator, its SWAPs after."""
         out = []
         for step in self:
-            ids = list(step.operator)
-            if len(ids) == 2 and ttn is not None:
-                a, b = ids
-                if ttn.nodes[a].parent != b and ttn.nodes[b].parent != a:
-                    raise NotImplementedError("two-site terms on non-neighbouring nodes need SWAP gates")
-            out.append(step.exponentiate_operator(delta_time))
+            before, after = step.realise_swaps(ttn=ttn, dim=dim)
+            out.extend(before)
+            out.append(step.exponentiate_operator(delta_time, ttn=ttn, dim=dim))
+            out.extend(after)
         return out
 
 
@@ -113,7 +182,10 @@ class TEBD:
         if len(ids) == 1:
             self.net.apply_single_site_gate(ids[0], self._dev_ops[index])
         elif len(ids) == 2:
-            self.net.apply_two_site_gate(ids[0], ids[1], self._dev_ops[index], self.svd_parameters)
+            a, b = ids
+            if self.state.nodes[a].parent != b and self.state.nodes[b].parent != a:
+                raise ValueError(f"nodes {a} and {b} are not neighbours; bring them together with SWAP gates")
+            self.net.apply_two_site_gate(a, b, self._dev_ops[index], self.svd_parameters)
         else:
             raise NotImplementedError("More than two-site interactions are not implemented.")
 

@@ -310,6 +310,62 @@ def run_case_tebd(ptn, name, spec, tensors, dt, steps, svd, J=1.0, g=0.7):
     print(name, "written; max bond", tebd.state.max_bond_dim())
 
 
+def run_case_tebd_swaps(ptn, name, spec, tensors, dt, steps, svd, J=1.0, g=0.7, K=0.4):
+    """TEBD whose splitting (``TrotterSplitting.from_lists``, ``trotter.py:218-283``)
+    also carries a next-nearest-neighbour term -K Z_s3 Z_s0: s3 and s1 are
+    swapped before the exponentiated (s1, s0) term and swapped back after it
+    (``SWAPlist``, ``trotter.py:15-103``). The splitting's definition and the
+    gates the reference applies are stored."""
+    from pytreenet.time_evolution.trotter import SWAPlist
+    psi = build_reference_state(ptn, spec, tensors)
+    tps = [ptn.TensorProduct({p: -J * Z, nid: Z}) for nid, p in spec if p is not None]
+    tps += [ptn.TensorProduct({nid: -g * X}) for nid, _ in spec]
+    tps.append(ptn.TensorProduct({"s1": -K * Z, "s0": Z}))
+    n = len(tps)
+    before = [SWAPlist() for _ in range(n)]
+    after = [SWAPlist() for _ in range(n)]
+    before[-1] = SWAPlist([("s3", "s1")])
+    after[-1] = SWAPlist([("s3", "s1")])
+    split = ptn.TrotterSplitting.from_lists(tps, swaps_before=before, swaps_after=after)
+    maxd, rel, tot, renorm = svd
+    params = ptn.SVDParameters(max_bond_dim=maxd, rel_tol=rel, total_tol=tot, renorm=renorm)
+    ops = {nid: ptn.TensorProduct({nid: Z}) for nid, _ in spec}
+    tebd = ptn.TEBD(psi, split, dt, dt * steps, ops, svd_parameters=params)
+    rec = {"spec_ids": np.array([s[0] for s in spec]),
+           "spec_parents": np.array(["" if s[1] is None else s[1] for s in spec]),
+           "dt": dt, "steps": steps, "order": 0, "krylov_tol": 0.0, "tebd": 1,
+           "svd_max_bond_dim": maxd, "svd_rel_tol": rel, "svd_total_tol": tot, "svd_renorm": int(renorm),
+           "update_path": np.array([s[0] for s in spec]), "n_gates": len(tebd.exponents), "n_terms": n}
+    for i, u in enumerate(tebd.exponents):
+        rec[f"gate/{i}/op"] = np.asarray(u.operator)
+        rec[f"gate/{i}/ids"] = np.array(list(u.node_identifiers))
+    for i, tp in enumerate(tps):
+        rec[f"term/{i}/ids"] = np.array(list(tp.keys()))
+        rec[f"term/{i}/ops"] = np.array([tp[k] for k in tp.keys()])
+        rec[f"term/{i}/before"] = np.array(list(before[i]), dtype=str).reshape(-1, 2)
+        rec[f"term/{i}/after"] = np.array(list(after[i]), dtype=str).reshape(-1, 2)
+    for nid, t in tensors.items():
+        rec[f"init/{nid}"] = t
+    for nid, _ in spec:
+        rec[f"ttno/{nid}"] = np.zeros(1)
+    zs = []
+    for step in range(steps):
+        tebd.run_one_time_step()
+        zs.append([tebd.state.operator_expectation_value(ops[nid]) for nid, _ in spec])
+    rec["z"] = np.array(zs)
+    for nid, t in export_state(tebd.state, spec).items():
+        rec[f"final/{nid}"] = t
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **rec)
+    print(name, "written; gates", len(tebd.exponents))
+
+
+def tebd_swap_cases(ptn):
+    rng = np.random.default_rng(53)
+    spec = binary_tree(7)
+    run_case_tebd_swaps(ptn, "binary7_tfim_tebd_swaps", spec, random_state_tensors(spec, rng, 2), 0.05, 4,
+                        (6, 1e-10, 1e-10, False))
+
+
 def svd_cases():
     """Truncation known answers: the reference's own truncation of fixed spectra."""
     from pytreenet.util.tensor_splitting import SVDParameters, truncate_singular_values
@@ -616,6 +672,7 @@ def main(ref_root):
     saved_files(ptn)
     bug_cases(ptn)
     leaf_to_leaf_cases(ptn)
+    tebd_swap_cases(ptn)
 
 
 if __name__ == "__main__":

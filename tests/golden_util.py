@@ -42,7 +42,7 @@ def load_case(name):
 CASES = ["c1_binary15_tfim_chi8", "binary7_tfim_chi4_o2", "ttree3_heis_chi6_o1",
          "ttree3_heis_chi6_o2", "ternary2_xxz_chi4_o1"]
 TWO_SITE_CASES = ["ternary2_xxz_neel_2tdvp", "binary7_heis_2tdvp_trunc"]
-TEBD_CASES = ["binary7_tfim_tebd"]
+TEBD_CASES = ["binary7_tfim_tebd", "binary7_tfim_tebd_swaps"]
 DRIVEN_CASES = ["binary7_tfim_driven_o1", "binary7_tfim_driven_o2"]
 BUG_CASES = ["binary15_tfim_fixed_bug", "ternary2_xxz_fixed_bug"]
 ADAPTIVE_BUG_CASES = ["binary7_tfim_bug", "ternary2_xxz_bug"]
@@ -218,3 +218,20 @@ def run_adaptive_bug_case(name):
         bonds.append([algo.state.phys(nid).shape[0] for nid, p in c["spec"] if p is not None])
     out = {nid: algo.state.get_phys_numpy(nid) for nid, _ in c["spec"]}
     return c, O.OState(oracle_state(c).tree, out), np.array(zs), np.array(bonds), d["bonds"]
+
+
+def swap_splitting(name):
+    """The engine's TrotterSplitting.from_lists rebuilt from a fixture's stored
+    definition (tensor products and SWAP lists)."""
+    import numpy as np
+    import pytreenet_gb300 as P
+    d = np.load(os.path.join(GOLDEN, name + ".npz"))
+    n = int(d["n_terms"])
+    tps, before, after = [], [], []
+    for i in range(n):
+        ids = [str(x) for x in d[f"term/{i}/ids"]]
+        ops = d[f"term/{i}/ops"]
+        tps.append(P.TensorProduct({k: ops[j] for j, k in enumerate(ids)}))
+        before.append(P.SWAPlist([tuple(str(y) for y in x) for x in d[f"term/{i}/before"]]))
+        after.append(P.SWAPlist([tuple(str(y) for y in x) for x in d[f"term/{i}/after"]]))
+    return P.TrotterSplitting.from_lists(tps, swaps_before=before, swaps_after=after)

@@ -513,3 +513,29 @@ def test_engine_host_adaptive_bug_matches_reference(monkeypatch, name):
     assert np.max(np.abs(z - c["z"])) < 1e-9
     one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), st)
     assert one_minus_f < 1e-11
+
+
+def test_engine_host_swap_splitting_matches_reference(monkeypatch):
+    """TrotterSplitting.from_lists with SWAP lists: the same gate sequence as
+    the reference's (SWAPs before, the exponentiated term, SWAPs after), and
+    TEBD driven by it reproduces the reference's run."""
+    fake_ptn.install(monkeypatch)
+    import pytreenet_gb300 as P
+    from golden_util import swap_splitting
+    c = load_case("binary7_tfim_tebd_swaps")
+    split = swap_splitting("binary7_tfim_tebd_swaps")
+    st = build_ttn(P.TTNS, c["spec"], c["init"])
+    assert split[-1].swaps_before.is_compatible_with_ttn(st)
+    gates = split.exponentiate_splitting(c["dt"], ttn=st)
+    assert len(gates) == len(c["gates"])
+    for g, (op, ids) in zip(gates, c["gates"]):
+        assert list(g.node_identifiers) == ids
+        assert np.allclose(g.operator, op, atol=1e-14)
+    algo = P.TEBD(st, split, c["dt"], c["dt"] * c["steps"], {}, svd_parameters=P.SVDParameters(**c["svd"]))
+    for k in range(c["steps"]):
+        algo.run_one_time_step()
+        z = np.array([algo.evaluate_operator({nid: Zm}) for nid, _ in c["spec"]])
+        assert np.max(np.abs(z - c["z"][k])) < 1e-12 * np.max(np.abs(c["z"]))
+    with pytest.raises(ValueError):
+        bad = P.TrotterSplitting([P.TrotterStep({"s3": Zm, "s0": Zm}, 1.0)])
+        P.TEBD(build_ttn(P.TTNS, c["spec"], c["init"]), bad, 0.1, 0.1, {}).run_one_time_step()

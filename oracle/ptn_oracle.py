@@ -28,7 +28,7 @@ __all__ = [
     "scalar_product", "SVDParams", "truncate_singular_values", "two_site_merge",
     "two_site_heff_apply", "two_site_split", "SecondOrderTwoSiteTDVPOracle",
     "FirstOrderTwoSiteTDVPOracle", "tebd_apply_gate", "TEBDOracle", "ttno_expectation",
-    "fixed_bug_step", "adaptive_bug_step", "svd_truncation", "leaf_to_leaf_path",
+    "fixed_bug_step", "adaptive_bug_step", "svd_truncation", "leaf_to_leaf_path", "dense_exp_action",
 ]
 
 
@@ -377,6 +377,20 @@ def krylov_exp_action(psi, action, dt, exp_factor, krylov_tol=1e-10,
 # ----------------------------------------------------------------------------
 # update paths
 # ----------------------------------------------------------------------------
+def dense_exp_action(psi, action, dt, exp_factor):
+    """exp(exp_factor dt H) psi with H formed column by column from ``action``
+    and exponentiated by ``scipy.linalg.expm`` (the exact modes of
+    ``TimeEvoMode``, ``time_evolution.py:621-655``; small tensors only)."""
+    import scipy.linalg
+    n = psi.size
+    H = np.empty((n, n), dtype=complex)
+    for i in range(n):
+        e = np.zeros(n, dtype=complex)
+        e[i] = 1.0
+        H[:, i] = np.asarray(action(e.reshape(psi.shape))).reshape(-1)
+    return (scipy.linalg.expm(exp_factor * dt * H) @ psi.reshape(-1)).reshape(psi.shape)
+
+
 def _postorder(tree: OTree, nid):
     if tree.is_leaf(nid):
         return [nid]
@@ -473,7 +487,8 @@ class _OneSiteBase:
     (``tdvp_algorithms/tdvp_algorithm.py:58-221``, ``onesitetdvp.py:17-134``)."""
 
     def __init__(self, state: OState, W: dict, dt: float, krylov_tol=1e-10,
-                 max_krylov_dim=None, path_mode: str = "LeafToRoot"):
+                 max_krylov_dim=None, path_mode: str = "LeafToRoot", exact: bool = False):
+        self.exact = exact
         self.state = state.copy()
         self.W = W
         self.dt = dt
@@ -490,6 +505,8 @@ class _OneSiteBase:
         self.envs = init_cache_but_one(self.state, W, self.update_path[0])
 
     def _krylov(self, x, action, factor, exp_factor):
+        if self.exact:
+            return dense_exp_action(x, action, self.dt * factor, exp_factor)
         return krylov_exp_action(x, action, self.dt * factor, exp_factor,
                                  krylov_tol=self.tol, max_krylov_dim=self.maxdim,
                                  stats=self.krylov_dims)

@@ -33,8 +33,8 @@ from . import _lib
 from . import engine as E
 from .adjoint import (_SiteOp, _raw_contract, _solver, _tensor_apply, absorb, env_apply, qr_keep_raw)
 from .engine import CDT, DeviceNetwork, check
-from .tdvp import (TTNTimeEvolutionConfig, TensorProduct, TimeEvoMode, compute_num_time_steps,
-                   leaf_to_leaf_update_path)
+from .tdvp import (TTNTimeEvolutionConfig, TensorProduct, TimeEvoMode, check_time_evo_mode,
+                   compute_num_time_steps, leaf_to_leaf_update_path)
 from .truncation import SVDParameters, truncate_singular_values
 
 DEFAULT_KRYLOV_TOL = 1e-10
@@ -111,15 +111,11 @@ class FixedBUG:
         if time_step_size <= 0 or final_time <= 0:
             raise ValueError("time step and final time must be positive")
         self.config = config if config is not None else self.config_class()
-        if self.config.time_evo_mode is not TimeEvoMode.KRYLOV:
-            raise NotImplementedError(
-                f"time_evo_mode={self.config.time_evo_mode}: the GPU engine runs the matrix-free "
-                "KRYLOV exponential only")
-        opts = dict(solver_options or {})
-        bad = set(opts) - TimeEvoMode.valid_solver_options(TimeEvoMode.KRYLOV)
-        if bad:
-            raise ValueError(f"solver options {sorted(bad)} are not valid for KRYLOV")
-        self.solver_options = opts
+        self.solver_options = check_time_evo_mode(self.config.time_evo_mode, solver_options)
+        # the reference hands its options to the root and its children only;
+        # deeper nodes run the mode's defaults (the exact modes need no options)
+        self._deep_tol = (self.solver_options["krylov_tol"] if self.config.time_evo_mode.is_exact()
+                          else DEFAULT_KRYLOV_TOL)
         self.time_step_size = float(time_step_size)
         self.final_time = float(final_time)
         self.num_time_steps = compute_num_time_steps(final_time, time_step_size)
@@ -178,7 +174,7 @@ class FixedBUG:
         envs.pop((c, p), None)
         new, Ms, blocks = {}, {}, {}
         for g in self.children[c]:
-            sub, blocks[g], Ms[g] = self._update_node(g, cur, envs, DEFAULT_KRYLOV_TOL)
+            sub, blocks[g], Ms[g] = self._update_node(g, cur, envs, self._deep_tol)
             new.update(sub)
         envs.update({(g, c): b for g, b in blocks.items()})
         x = self._in_new_child_bases(cur[c], c, Ms)

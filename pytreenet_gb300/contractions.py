@@ -106,11 +106,11 @@ def effective_single_site_evolution(state_tensor, state_node, hamiltonian_tensor
                                     mode: TimeEvoMode = TimeEvoMode.KRYLOV,
                                     forward: EvoDirection = EvoDirection.FORWARD, **options) -> np.ndarray:
     """exp(-i dt H_eff) applied to ``state_tensor`` (``effective_time_evolution.py:257-324``):
-    the matrix-free Krylov exponential (options ``krylov_tol``, ``max_krylov_dim``);
-    ``forward`` gives the sign of the exponent as in the reference. The dense
-    modes are not provided."""
-    if mode is not TimeEvoMode.KRYLOV:
-        raise NotImplementedError(f"time_evo_mode={mode}: the GPU engine runs the KRYLOV exponential only")
+    the matrix-free Krylov exponential (options ``krylov_tol``, ``max_krylov_dim``;
+    the exact modes run it to machine precision); ``forward`` gives the sign of
+    the exponent as in the reference."""
+    from .tdvp import check_time_evo_mode
+    options = check_time_evo_mode(mode, options, tensor_cache.net.precision)
     nid = _node_id(state_node)
     net = tensor_cache.net
     st = tensor_cache.state

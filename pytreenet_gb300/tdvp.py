@@ -23,9 +23,12 @@ from .ttn import TreeTensorNetworkOperator, TreeTensorNetworkState
 class TimeEvoMode(Enum):
     """Local exponential method (``time_evolution/time_evolution.py:431-655``).
 
-    Only KRYLOV (matrix-free Lanczos, the GPU path) is executed by this engine.
-    FASTEST maps to the dense CHEBYSHEV path in the reference, which builds the
-    N x N effective Hamiltonian; it is not ported."""
+    KRYLOV is the matrix-free Lanczos exponential with the adaptive stop at
+    ``krylov_tol``. The exact modes (FASTEST, which the reference maps to
+    CHEBYSHEV, EXPM, CHEBYSHEV, SPARSE) build the N x N effective Hamiltonian
+    in the reference; here they compute the same exp(-i dt H_eff) x
+    matrix-free, with the Krylov stop at 1e-14 (1e-11 on the reduced-precision
+    path) and at most 64 vectors. The SciPy ODE modes are not provided."""
     FASTEST = "fastest"
     EXPM = "expm"
     CHEBYSHEV = "chebyshev"
@@ -48,7 +51,44 @@ class TimeEvoMode(Enum):
     def valid_solver_options(mode) -> set:
         if mode is TimeEvoMode.KRYLOV:
             return {"krylov_tol", "max_krylov_dim", "hermitian", "exp_factor"}
+        if mode in TimeEvoMode.scipy_modes():
+            return {"atol", "rtol", "max_step", "first_step", "jac", "jac_sparsity",
+                    "lband", "uband", "min_step", "hermitian", "exp_factor"}
         return {"exp_factor"}
+
+    @staticmethod
+    def scipy_modes() -> list:
+        return [TimeEvoMode.RK45, TimeEvoMode.RK23, TimeEvoMode.DOP853, TimeEvoMode.BDF]
+
+    @staticmethod
+    def fastest_equivalent() -> "TimeEvoMode":
+        return TimeEvoMode.CHEBYSHEV
+
+    def is_exact(self) -> bool:
+        """The matrix-exponential modes (everything but KRYLOV and the ODE solvers)."""
+        return self is not TimeEvoMode.KRYLOV and self not in TimeEvoMode.scipy_modes()
+
+
+# the exact modes run the Krylov exponential to these stops
+EXACT_KRYLOV_TOL = {"plain": 1e-14, "reduced": 1e-11}
+EXACT_MAX_KRYLOV_DIM = 64
+
+
+def check_time_evo_mode(mode, solver_options, precision: str = "plain"):
+    """Validate the mode and options as the reference does and return the
+    options the engine's Krylov exponential runs with."""
+    if mode in TimeEvoMode.scipy_modes():
+        raise NotImplementedError(
+            f"time_evo_mode={mode}: the SciPy ODE solvers are not provided; use KRYLOV or an exact mode")
+    opts = TimeEvoMode.default_solver_options(mode)
+    opts.update(solver_options or {})
+    bad = set(opts) - TimeEvoMode.valid_solver_options(mode)
+    if bad:
+        raise ValueError(f"solver options {sorted(bad)} are not valid for {mode}")
+    if mode.is_exact():
+        opts = dict(opts, krylov_tol=EXACT_KRYLOV_TOL["plain" if precision == "plain" else "reduced"],
+                    max_krylov_dim=EXACT_MAX_KRYLOV_DIM)
+    return opts
 
 
 class EvoDirection(Enum):
@@ -209,16 +249,7 @@ class OneSiteTDVP:
         if time_step_size <= 0 or final_time <= 0:
             raise ValueError("time step and final time must be positive")
         self.config = config if config is not None else self.config_class()
-        if self.config.time_evo_mode is not TimeEvoMode.KRYLOV:
-            raise NotImplementedError(
-                f"time_evo_mode={self.config.time_evo_mode}: the GPU engine runs the matrix-free "
-                "KRYLOV exponential only (the dense modes build the full effective Hamiltonian)")
-        opts = TimeEvoMode.default_solver_options(TimeEvoMode.KRYLOV)
-        opts.update(solver_options or {})
-        bad = set(opts) - TimeEvoMode.valid_solver_options(TimeEvoMode.KRYLOV)
-        if bad:
-            raise ValueError(f"solver options {sorted(bad)} are not valid for KRYLOV")
-        self.solver_options = opts
+        self.solver_options = check_time_evo_mode(self.config.time_evo_mode, solver_options, precision)
         self.time_step_size = float(time_step_size)
         self.final_time = float(final_time)
         self.num_time_steps = compute_num_time_steps(final_time, time_step_size)

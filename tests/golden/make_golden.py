@@ -182,7 +182,8 @@ def heisenberg_fields(ptn, spec, fields, jxy=None, jz=None):
     return ptn.Hamiltonian(terms, conv)
 
 
-def run_case(ptn, name, spec, tensors, ham_fn, dt, steps, order, tol, canonical_random=False, path_mode=None):
+def run_case(ptn, name, spec, tensors, ham_fn, dt, steps, order, tol, canonical_random=False, path_mode=None,
+             default_mode=False):
     from pytreenet.time_evolution.time_evolution import TimeEvoMode
     from pytreenet.time_evolution.tdvp_algorithms.tdvp_algorithm import TDVPConfig
     from pytreenet.time_evolution.time_evo_util import PathFinderMode
@@ -198,13 +199,19 @@ def run_case(ptn, name, spec, tensors, ham_fn, dt, steps, order, tol, canonical_
     cfg = TDVPConfig(time_evo_mode=TimeEvoMode.KRYLOV)
     if path_mode is not None:
         cfg = TDVPConfig(time_evo_mode=TimeEvoMode.KRYLOV, main_path_mode=PathFinderMode[path_mode])
-    algo = cls(psi, H, dt, dt * steps, ops, config=cfg, solver_options={"krylov_tol": tol})
+    if default_mode:
+        # TDVPConfig() runs the reference's default local exponential (FASTEST -> CHEBYSHEV)
+        algo = cls(psi, H, dt, dt * steps, ops, config=TDVPConfig())
+    else:
+        algo = cls(psi, H, dt, dt * steps, ops, config=cfg, solver_options={"krylov_tol": tol})
     rec = {"spec_ids": np.array([s[0] for s in spec]),
            "spec_parents": np.array(["" if s[1] is None else s[1] for s in spec]),
            "dt": dt, "steps": steps, "order": order, "krylov_tol": tol,
            "update_path": np.array(algo.update_path)}
     if path_mode is not None:
         rec["path_mode"] = path_mode
+    if default_mode:
+        rec["time_evo_mode"] = str(algo.config.time_evo_mode.name)
     for nid, t in tensors.items():
         rec[f"init/{nid}"] = t
     for nid, t in export_ttno(H, spec).items():
@@ -613,6 +620,20 @@ def leaf_to_leaf_cases(ptn):
              path_mode="LeafToLeaf")
 
 
+def default_mode_cases(ptn):
+    """TDVP with the reference's default configuration (time_evo_mode FASTEST,
+    a dense exponential of the effective Hamiltonian)."""
+    rng = np.random.default_rng(61)
+    spec = t_tree(3)
+    h = rng.uniform(-1, 1, size=len(spec))
+    run_case(ptn, "ttree3_heis_fastest_o1", spec, capped_state_tensors(spec, rng, 6),
+             lambda psi: heisenberg_fields(ptn, spec, h), 0.05, 3, 1, 0.0, canonical_random=True,
+             default_mode=True)
+    spec = binary_tree(7)
+    run_case(ptn, "binary7_tfim_fastest_o2", spec, capped_state_tensors(spec, rng, 4),
+             lambda psi: tfim(ptn, spec, g=0.9), 0.05, 3, 2, 0.0, canonical_random=True, default_mode=True)
+
+
 def time_dep_cases(ptn):
     rng = np.random.default_rng(77)
     spec = binary_tree(7)
@@ -673,6 +694,7 @@ def main(ref_root):
     bug_cases(ptn)
     leaf_to_leaf_cases(ptn)
     tebd_swap_cases(ptn)
+    default_mode_cases(ptn)
 
 
 if __name__ == "__main__":

@@ -26,6 +26,7 @@ def load_case(name):
         "energy_final": complex(d["energy_final"]) if "energy_final" in d.files else None,
     }
     case["path_mode"] = str(d["path_mode"]) if "path_mode" in d.files else "LeafToRoot"
+    case["time_evo_mode"] = str(d["time_evo_mode"]) if "time_evo_mode" in d.files else "KRYLOV"
     case["tebd"] = bool(int(d["tebd"])) if "tebd" in d.files else False
     case["driven"] = "amp" in d.files
     if case["driven"]:
@@ -47,6 +48,7 @@ DRIVEN_CASES = ["binary7_tfim_driven_o1", "binary7_tfim_driven_o2"]
 BUG_CASES = ["binary15_tfim_fixed_bug", "ternary2_xxz_fixed_bug"]
 ADAPTIVE_BUG_CASES = ["binary7_tfim_bug", "ternary2_xxz_bug"]
 L2L_CASES = ["ttree3_heis_l2l_o1", "binary15_tfim_l2l_o2"]
+DEFAULT_MODE_CASES = ["ttree3_heis_fastest_o1", "binary7_tfim_fastest_o2"]
 
 
 def driven_ttno(case, t):
@@ -181,10 +183,11 @@ def run_one_site_case(name, precision="plain"):
     st = build_ttn(P.TTNS, c["spec"], c["init"])
     H = build_ttn(P.TTNO, c["spec"], c["ttno"])
     cls = P.FirstOrderOneSiteTDVP if c["order"] == 1 else P.SecondOrderOneSiteTDVP
+    mode = P.TimeEvoMode[c["time_evo_mode"]]
+    opts = {"krylov_tol": c["krylov_tol"]} if mode is P.TimeEvoMode.KRYLOV else None
     algo = cls(st, H, c["dt"], c["dt"] * c["steps"], {},
-               config=P.TDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV,
-                                   main_path_mode=P.PathFinderMode[c["path_mode"]]),
-               solver_options={"krylov_tol": c["krylov_tol"]}, precision=precision)
+               config=P.TDVPConfig(time_evo_mode=mode, main_path_mode=P.PathFinderMode[c["path_mode"]]),
+               solver_options=opts, precision=precision)
     assert algo.update_path == c["update_path"]
     Zm = np.diag([1.0, -1.0]).astype(complex)
     zerr = 0.0

@@ -539,3 +539,16 @@ def test_engine_host_swap_splitting_matches_reference(monkeypatch):
     with pytest.raises(ValueError):
         bad = P.TrotterSplitting([P.TrotterStep({"s3": Zm, "s0": Zm}, 1.0)])
         P.TEBD(build_ttn(P.TTNS, c["spec"], c["init"]), bad, 0.1, 0.1, {}).run_one_time_step()
+
+
+@pytest.mark.parametrize("name", ["ttree3_heis_fastest_o1", "binary7_tfim_fastest_o2"])
+def test_engine_host_default_mode(monkeypatch, name):
+    """TDVPConfig(time_evo_mode=FASTEST), the reference's default: the engine's
+    matrix-free exponential at its exact-mode stop reproduces the reference's
+    dense exponential."""
+    fake_ptn.install(monkeypatch)
+    from golden_util import run_one_site_case
+    c, st, zerr = run_one_site_case(name)
+    one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), st)
+    assert zerr < 1e-11
+    assert one_minus_f < 1e-12

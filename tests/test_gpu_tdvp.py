@@ -74,3 +74,13 @@ def test_gpu_leaf_to_leaf_path(name):
     one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), st)
     assert zerr < 1e-10
     assert one_minus_f < 1e-12
+
+
+@pytest.mark.parametrize("name", ["ttree3_heis_fastest_o1", "binary7_tfim_fastest_o2"])
+def test_gpu_default_mode(name):
+    """TDVPConfig() (FASTEST) on the GB300 against the reference's dense exponential."""
+    from golden_util import run_one_site_case
+    c, st, zerr = run_one_site_case(name)
+    one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), st)
+    assert zerr < 1e-11
+    assert one_minus_f < 1e-12

@@ -11,7 +11,8 @@ Zm = np.diag([1.0, -1.0]).astype(complex)
 def _run(c, steps=None):
     st = oracle_state(c)
     cls = O.FirstOrderOneSiteTDVPOracle if c["order"] == 1 else O.SecondOrderOneSiteTDVPOracle
-    algo = cls(st, c["ttno"], c["dt"], krylov_tol=c["krylov_tol"], path_mode=c["path_mode"])
+    algo = cls(st, c["ttno"], c["dt"], krylov_tol=c["krylov_tol"], path_mode=c["path_mode"],
+               exact=c["time_evo_mode"] != "KRYLOV")
     assert algo.update_path == c["update_path"]
     zerr = 0.0
     for k in range(c["steps"] if steps is None else steps):
@@ -226,3 +227,15 @@ def test_oracle_leaf_to_leaf_path(name):
     one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), algo.state)
     assert zerr < 1e-10
     assert one_minus_f < 1e-12
+
+
+@pytest.mark.parametrize("name", ["ttree3_heis_fastest_o1", "binary7_tfim_fastest_o2"])
+def test_oracle_default_mode_matches_reference(name):
+    """TDVPConfig() (FASTEST, a dense exponential): the oracle's dense
+    exponential reproduces the reference."""
+    c = load_case(name)
+    assert c["time_evo_mode"] == "FASTEST"
+    algo, zerr = _run(c)
+    one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), algo.state)
+    assert zerr < 1e-12
+    assert one_minus_f < 1e-13

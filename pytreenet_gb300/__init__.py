@@ -19,7 +19,8 @@ from .tebd import TEBD, TrotterStep, TrotterSplitting, NumericOperator, SWAPlist
 from .operators import nearest_neighbour_ttno, tfim_ttno, heisenberg_ttno
 from .batch import run_realisations
 from .contractions import (SandwichCache, contract_ket_ham_with_envs, contract_any,
-                           effective_single_site_evolution)
+                           effective_single_site_evolution, get_effective_single_site_hamiltonian,
+                           get_effective_single_site_hamiltonian_nodes)
 from .adjoint import OneSiteTDVPAdjoint, coupling_gradient
 from .bug import BUG, BUGConfig, FixedBUG, FixedBUGConfig
 from .time_dep import TimeDependentTTNO, FactorUpdatable, DiscreetTimeTTNO
@@ -33,6 +34,7 @@ __all__ = [
     "NumericOperator", "SWAPlist", "swap_gate",
     "nearest_neighbour_ttno", "tfim_ttno", "heisenberg_ttno", "run_realisations",
     "SandwichCache", "contract_ket_ham_with_envs", "contract_any", "effective_single_site_evolution",
+    "get_effective_single_site_hamiltonian", "get_effective_single_site_hamiltonian_nodes",
     "OneSiteTDVPAdjoint", "coupling_gradient", "FixedBUG", "FixedBUGConfig", "BUG", "BUGConfig",
     "TimeDependentTTNO", "FactorUpdatable", "DiscreetTimeTTNO",
 ]

@@ -3,8 +3,10 @@
 Drop-in counterparts of the helpers a PyTreeNet user composes into custom
 algorithms: ``SandwichCache`` (``contractions/sandwich_caching.py:14-126``),
 ``contract_ket_ham_with_envs`` (``contractions/state_operator_contraction.py:227-273``),
-``contract_any`` (``:407-461``) and ``effective_single_site_evolution``
-(``time_evolution/time_evo_util/effective_time_evolution.py:257-324``). Tensors
+``contract_any`` (``:407-461``), ``effective_single_site_evolution``
+(``time_evolution/time_evo_util/effective_time_evolution.py:257-324``) and the
+dense ``get_effective_single_site_hamiltonian(_nodes)``
+(``contractions/effective_hamiltonians.py:109-157``). Tensors
 come and go as NumPy arrays in the reference's leg conventions: a site tensor
 in its node's logical leg order (parent, children, physical), a cache entry
 E(node -> next) with legs (ket, ham, bra). The environments themselves stay on
@@ -124,3 +126,42 @@ def effective_single_site_evolution(state_tensor, state_node, hamiltonian_tensor
     net.krylov.expm(x, apply, time_step_size, exp_factor, options.get("krylov_tol", 1e-10),
                     options.get("max_krylov_dim"), out=out, tridiagonal=net.levels > 0)
     return _from_phys(st, nid, out.cpu().numpy())
+
+
+def _dense_site_hamiltonian(cache: SandwichCache, nid: str, W=None) -> np.ndarray:
+    from .adjoint import site_apply
+    net = cache.net
+    shape = net.shape(nid)
+    N = int(np.prod(shape))
+    eye = torch.eye(N, dtype=CDT, device=net.device).reshape([N] + shape)
+    envs = [net.env_buf(x, nid) for x in net.nbrs(nid)]
+    Y = site_apply(eye, envs, net.W[nid] if W is None else W, batch=True)
+    H_phys = Y.reshape(N, N).transpose(0, 1).cpu().numpy()      # column r = H e_r
+    P = np.arange(N).reshape(shape).transpose(cache.state.logical_perm(nid)).reshape(-1)
+    return H_phys[np.ix_(P, P)]
+
+
+def get_effective_single_site_hamiltonian(node_id: str, state, hamiltonian, tensor_cache: SandwichCache) -> np.ndarray:
+    """H_eff of a site as an N x N matrix acting on the site tensor flattened in
+    its leg order (``get_effective_single_site_hamiltonian``,
+    ``contractions/effective_hamiltonians.py:133-157``). The matrix is built on
+    the device by applying the matvec chain to the N unit vectors at once;
+    meant for small sites, as in the reference."""
+    return _dense_site_hamiltonian(tensor_cache, node_id)
+
+
+def get_effective_single_site_hamiltonian_nodes(state_node, hamiltonian_node, hamiltonian_tensor,
+                                                tensor_cache: SandwichCache) -> np.ndarray:
+    """As :func:`get_effective_single_site_hamiltonian`, with the TTNO tensor given
+    in ``hamiltonian_node``'s leg order (``effective_hamiltonians.py:109-131``)."""
+    nid = _node_id(state_node)
+    W = None
+    if hamiltonian_tensor is not None:
+        net = tensor_cache.net
+        order = tensor_cache.state.nodes[nid].phys_neighbours()
+        hn = hamiltonian_node.neighbouring_nodes()
+        n = len(hn)
+        perm = [hn.index(x) for x in order] + [n, n + 1]
+        Wn = np.transpose(np.asarray(hamiltonian_tensor, dtype=np.complex128), perm)
+        W = torch.from_numpy(np.ascontiguousarray(Wn)).to(net.device)
+    return _dense_site_hamiltonian(tensor_cache, nid, W)

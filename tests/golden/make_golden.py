@@ -634,6 +634,33 @@ def default_mode_cases(ptn):
              lambda psi: tfim(ptn, spec, g=0.9), 0.05, 3, 2, 0.0, canonical_random=True, default_mode=True)
 
 
+def heff_cases(ptn):
+    """Dense effective site Hamiltonians from the reference's
+    ``get_effective_single_site_hamiltonian`` (``contractions/effective_hamiltonians.py:133-157``)
+    with ``SandwichCache.init_cache_but_one`` environments, on a T-tree state."""
+    from pytreenet.contractions.sandwich_caching import SandwichCache
+    from pytreenet.contractions.effective_hamiltonians import get_effective_single_site_hamiltonian
+    rng = np.random.default_rng(71)
+    spec = t_tree(2)
+    h = rng.uniform(-1, 1, size=len(spec))
+    tensors = random_state_tensors(spec, rng, 3)
+    psi = build_reference_state(ptn, spec, tensors)
+    H = ptn.TTNO.from_hamiltonian(heisenberg_fields(ptn, spec, h), psi)
+    rec = {"spec_ids": np.array([s[0] for s in spec]),
+           "spec_parents": np.array(["" if s[1] is None else s[1] for s in spec])}
+    for nid, t in tensors.items():
+        rec[f"init/{nid}"] = t
+    for nid, t in export_ttno(H, spec).items():
+        rec[f"ttno/{nid}"] = t
+    nodes = ["root", "a0_0", "a1_1"]
+    for nid in nodes:
+        cache = SandwichCache.init_cache_but_one(psi, H, nid)
+        rec[f"heff/{nid}"] = get_effective_single_site_hamiltonian(nid, psi, H, cache)
+    rec["heff_nodes"] = np.array(nodes)
+    np.savez_compressed(os.path.join(HERE, "ttree2_heis_heff.npz"), **rec)
+    print("heff written", {n: rec[f"heff/{n}"].shape for n in nodes})
+
+
 def time_dep_cases(ptn):
     rng = np.random.default_rng(77)
     spec = binary_tree(7)
@@ -695,6 +722,7 @@ def main(ref_root):
     leaf_to_leaf_cases(ptn)
     tebd_swap_cases(ptn)
     default_mode_cases(ptn)
+    heff_cases(ptn)
 
 
 if __name__ == "__main__":

@@ -238,3 +238,23 @@ def swap_splitting(name):
         before.append(P.SWAPlist([tuple(str(y) for y in x) for x in d[f"term/{i}/before"]]))
         after.append(P.SWAPlist([tuple(str(y) for y in x) for x in d[f"term/{i}/after"]]))
     return P.TrotterSplitting.from_lists(tps, swaps_before=before, swaps_after=after)
+
+
+def check_heff_fixture(tol=1e-12):
+    """Dense effective site Hamiltonians of the engine against the reference's
+    ``get_effective_single_site_hamiltonian`` (fixture ``ttree2_heis_heff``)."""
+    import numpy as np
+    import pytreenet_gb300 as P
+    d = np.load(os.path.join(GOLDEN, "ttree2_heis_heff.npz"))
+    ids = [str(x) for x in d["spec_ids"]]
+    spec = list(zip(ids, [str(x) or None for x in d["spec_parents"]]))
+    for nid in [str(x) for x in d["heff_nodes"]]:
+        st = build_ttn(P.TTNS, spec, {i: d[f"init/{i}"] for i in ids})
+        H = build_ttn(P.TTNO, spec, {i: d[f"ttno/{i}"] for i in ids})
+        cache = P.SandwichCache.init_cache_but_one(st, H, nid)
+        got = P.get_effective_single_site_hamiltonian(nid, st, H, cache)
+        ref = d[f"heff/{nid}"]
+        assert got.shape == ref.shape
+        assert np.max(np.abs(got - ref)) < tol * max(1.0, np.max(np.abs(ref))), nid
+        got2 = P.get_effective_single_site_hamiltonian_nodes(st.nodes[nid], H.nodes[nid], H.get_tensor(nid), cache)
+        assert np.max(np.abs(got2 - ref)) < tol * max(1.0, np.max(np.abs(ref))), nid

@@ -552,3 +552,10 @@ def test_engine_host_default_mode(monkeypatch, name):
     one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), st)
     assert zerr < 1e-11
     assert one_minus_f < 1e-12
+
+
+def test_engine_host_dense_effective_hamiltonian(monkeypatch):
+    """get_effective_single_site_hamiltonian(_nodes) against the reference."""
+    fake_ptn.install(monkeypatch)
+    from golden_util import check_heff_fixture
+    check_heff_fixture()

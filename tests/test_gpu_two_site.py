@@ -227,3 +227,9 @@ def test_gpu_contraction_helpers_match_oracle():
     zo = O.krylov_exp_action(ost.tensors[center], lambda v: O.heff_apply(v, ost.tree, center, c["ttno"][center],
                                                                          envs), 0.05, -1j, krylov_tol=1e-12)
     np.testing.assert_allclose(z, np.transpose(zo, st.logical_perm(center)), atol=1e-11)
+
+
+def test_gpu_dense_effective_hamiltonian():
+    """get_effective_single_site_hamiltonian(_nodes) on the GB300 against the reference."""
+    from golden_util import check_heff_fixture
+    check_heff_fixture()

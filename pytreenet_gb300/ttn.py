@@ -297,6 +297,76 @@ class TreeTensorNetworkState(TreeTensorNetwork):
         T, sites = rec(self.root_id, None)
         return np.transpose(T, [sites.index(s) for s in site_order]).reshape(-1)
 
+    # -- overlaps and expectation values on the engine (``ttns/ttns.py:49-297``) ------
+    def _device(self):
+        from .engine import DeviceNetwork
+        return DeviceNetwork(self)
+
+    def to_vector(self, to_copy: bool = False) -> tuple:
+        """The dense state vector and the node order of its factors (small trees)."""
+        return self.to_dense(list(self._order)), list(self._order)
+
+    def scalar_product(self, other: "TreeTensorNetworkState | None" = None,
+                       use_orthogonal_center: bool = True) -> complex:
+        """sum self * conj(other) over all legs, i.e. <other|self>; <self|self>
+        without ``other`` (``ttns.py:65-89``)."""
+        mine = self._device()
+        if other is None:
+            return mine.expect_local({})
+        return other._device().overlap(mine)
+
+    def norm(self) -> float:
+        return float(np.sqrt(self.scalar_product().real))
+
+    def normalise(self, norm: float | None = None) -> float:
+        """Divide the orthogonality centre (else the root) by the norm; returns the
+        norm before (``ttns.py:91-125``)."""
+        if norm is None:
+            norm = self.norm()
+        nid = self.orthogonality_center_id if self.orthogonality_center_id is not None else self.root_id
+        if nid is None:
+            raise ValueError("Cannot normalise TTNS without nodes!")
+        self._phys[nid] = self.phys(nid) / norm
+        return norm
+
+    def normalize(self, norm: float | None = None) -> float:
+        return self.normalise(norm)
+
+    def distance(self, other: "TreeTensorNetworkState", normalise: bool = False) -> float:
+        """||A - B|| with <A|B> taken in absolute value (``ttns.py:140-166``)."""
+        a = self.scalar_product().real
+        b = other.scalar_product().real
+        dist = a - 2 * abs(self.scalar_product(other)) + b
+        if dist < 0:
+            assert dist > -1e-8 * min(a, b), f"Distance is negative! {dist}"
+            dist = abs(dist)
+        if normalise:
+            dist *= 2 / (a + b)
+        return float(np.sqrt(dist))
+
+    def infidelity(self, other: "TreeTensorNetworkState") -> float:
+        return 1 - self.distance(other, normalise=True)
+
+    def single_site_operator_expectation_value(self, node_id: str, operator, move_orth_center: bool = False) -> complex:
+        return self.tensor_product_expectation_value({node_id: operator})
+
+    def tensor_product_expectation_value(self, operator) -> complex:
+        """<psi| prod_i O_i |psi> (``ttns.py:240-264``)."""
+        if len(operator) == 0:
+            return self.scalar_product()
+        return self._device().expect_local(dict(operator))
+
+    def ttno_expectation_value(self, operator) -> complex:
+        return self._device().expect_ttno(operator)
+
+    def operator_expectation_value(self, operator) -> complex:
+        """A TensorProduct (any mapping node -> matrix) or a TTNO (``ttns.py:278-297``)."""
+        if isinstance(operator, TreeTensorNetworkOperator):
+            return self.ttno_expectation_value(operator)
+        if isinstance(operator, Mapping):
+            return self.tensor_product_expectation_value(operator)
+        raise TypeError("Operator must be a TensorProduct or a TTNO!")
+
     def get_phys_numpy(self, nid):
         t = self.phys(nid)
         return t if isinstance(t, np.ndarray) else t.detach().cpu().numpy()

@@ -559,3 +559,37 @@ def test_engine_host_dense_effective_hamiltonian(monkeypatch):
     fake_ptn.install(monkeypatch)
     from golden_util import check_heff_fixture
     check_heff_fixture()
+
+
+def test_ttns_observable_methods_match_reference(monkeypatch):
+    """TTNS.scalar_product / norm / normalise / operator_expectation_value /
+    distance on the engine against values the reference computed."""
+    import os
+    import oracle as O
+    import pytreenet_gb300 as P
+    from golden_util import GOLDEN
+    fake_ptn.install(monkeypatch)
+    st = P.TTNS.load(os.path.join(GOLDEN, "saved_ttns"))
+    vals = np.load(os.path.join(GOLDEN, "saved_ttns_values.npz"))
+    assert abs(st.scalar_product() - vals["norm2"]) < 1e-12
+    for i, nid in enumerate(str(x) for x in vals["ids"]):
+        assert abs(st.operator_expectation_value(P.TensorProduct({nid: Zm})) - vals["z"][i]) < 1e-12
+        assert abs(st.single_site_operator_expectation_value(nid, Zm) - vals["z"][i]) < 1e-12
+    # energy of a reference final state under its TTNO
+    c = load_case("ttree3_heis_chi6_o1")
+    fin = build_ttn(P.TTNS, c["spec"], c["final"])
+    H = build_ttn(P.TTNO, c["spec"], c["ttno"])
+    assert abs(fin.operator_expectation_value(H) - c["energy_final"]) < 1e-10
+    # overlaps between two states, against the oracle
+    a = build_ttn(P.TTNS, c["spec"], c["init"])
+    b = build_ttn(P.TTNS, c["spec"], c["final"])
+    ref = O.scalar_product(oracle_state(c, "final"), oracle_state(c, "init"))   # sum init * conj(final)
+    assert abs(a.scalar_product(b) - ref) < 1e-12 * max(1.0, abs(ref))
+    d = a.distance(b)
+    na, nb = O.scalar_product(oracle_state(c), oracle_state(c)).real, \
+        O.scalar_product(oracle_state(c, "final"), oracle_state(c, "final")).real
+    assert abs(d - np.sqrt(abs(na - 2 * abs(ref) + nb))) < 1e-10
+    n0 = a.normalise()
+    assert abs(n0 - np.sqrt(na)) < 1e-12 and abs(a.norm() - 1.0) < 1e-12
+    with pytest.raises(TypeError):
+        a.operator_expectation_value(3)

@@ -233,3 +233,21 @@ def test_gpu_dense_effective_hamiltonian():
     """get_effective_single_site_hamiltonian(_nodes) on the GB300 against the reference."""
     from golden_util import check_heff_fixture
     check_heff_fixture()
+
+
+def test_gpu_ttns_observable_methods():
+    """TTNS.scalar_product / operator_expectation_value on the GB300 against
+    values the reference computed."""
+    import os
+    import pytreenet_gb300 as P
+    from golden_util import GOLDEN
+    Zm = np.diag([1.0, -1.0]).astype(complex)
+    st = P.TTNS.load(os.path.join(GOLDEN, "saved_ttns"))
+    vals = np.load(os.path.join(GOLDEN, "saved_ttns_values.npz"))
+    assert abs(st.scalar_product() - vals["norm2"]) < 1e-12
+    for i, nid in enumerate(str(x) for x in vals["ids"]):
+        assert abs(st.operator_expectation_value(P.TensorProduct({nid: Zm})) - vals["z"][i]) < 1e-12
+    c = load_case("ttree3_heis_chi6_o1")
+    fin = build_ttn(P.TTNS, c["spec"], c["final"])
+    H = build_ttn(P.TTNO, c["spec"], c["ttno"])
+    assert abs(fin.operator_expectation_value(H) - c["energy_final"]) < 1e-10

@@ -17,6 +17,7 @@ from .tdvp import (TimeEvoMode, EvoDirection, PathFinderMode, TDVPConfig, Tensor
 from .truncation import SVDParameters, truncate_singular_values
 from .tebd import TEBD, TrotterStep, TrotterSplitting, NumericOperator, SWAPlist, swap_gate
 from .operators import nearest_neighbour_ttno, tfim_ttno, heisenberg_ttno
+from .hamiltonian import Hamiltonian
 from .batch import run_realisations
 from .contractions import (SandwichCache, contract_ket_ham_with_envs, contract_any,
                            effective_single_site_evolution, get_effective_single_site_hamiltonian,
@@ -32,7 +33,7 @@ __all__ = [
     "TwoSiteTDVPConfig", "FirstOrderTwoSiteTDVP", "SecondOrderTwoSiteTDVP",
     "SVDParameters", "truncate_singular_values", "TEBD", "TrotterStep", "TrotterSplitting",
     "NumericOperator", "SWAPlist", "swap_gate",
-    "nearest_neighbour_ttno", "tfim_ttno", "heisenberg_ttno", "run_realisations",
+    "nearest_neighbour_ttno", "tfim_ttno", "heisenberg_ttno", "run_realisations", "Hamiltonian",
     "SandwichCache", "contract_ket_ham_with_envs", "contract_any", "effective_single_site_evolution",
     "get_effective_single_site_hamiltonian", "get_effective_single_site_hamiltonian_nodes",
     "OneSiteTDVPAdjoint", "coupling_gradient", "FixedBUG", "FixedBUGConfig", "BUG", "BUGConfig",

@@ -377,6 +377,15 @@ class TreeTensorNetworkOperator(TreeTensorNetwork):
 
     n_open = 2
 
+    @classmethod
+    def from_hamiltonian(cls, hamiltonian, reference_tree, method=None, dtype=complex):
+        """``TTNO.from_hamiltonian`` (``ttno/ttno_class.py:60-97``): the TTNO of a
+        symbolic ``Hamiltonian`` on ``reference_tree``'s structure. ``method``
+        (the reference's state-diagram finder) is accepted and not used: the
+        construction of ``hamiltonian.ttno_from_hamiltonian`` is exact."""
+        from .hamiltonian import ttno_from_hamiltonian
+        return ttno_from_hamiltonian(hamiltonian, reference_tree, dtype=dtype)
+
 
 TTNS = TreeTensorNetworkState
 TTNO = TreeTensorNetworkOperator

@@ -258,3 +258,4 @@ def check_heff_fixture(tol=1e-12):
         assert np.max(np.abs(got - ref)) < tol * max(1.0, np.max(np.abs(ref))), nid
         got2 = P.get_effective_single_site_hamiltonian_nodes(st.nodes[nid], H.nodes[nid], H.get_tensor(nid), cache)
         assert np.max(np.abs(got2 - ref)) < tol * max(1.0, np.max(np.abs(ref))), nid
+

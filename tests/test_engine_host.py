@@ -593,3 +593,76 @@ def test_ttns_observable_methods_match_reference(monkeypatch):
     assert abs(n0 - np.sqrt(na)) < 1e-12 and abs(a.norm() - 1.0) < 1e-12
     with pytest.raises(TypeError):
         a.operator_expectation_value(3)
+
+
+def _symbolic_tfim(spec, J, g):
+    import pytreenet_gb300 as P
+    X = np.array([[0, 1], [1, 0]], dtype=complex)
+    conv = {"mJZ": -J * Zm, "Z": Zm, "mgX": -g * X}
+    terms = [P.TensorProduct({p: "mJZ", nid: "Z"}) for nid, p in spec if p is not None]
+    terms += [P.TensorProduct({nid: "mgX"}) for nid, _ in spec]
+    return P.Hamiltonian(terms, conv)
+
+
+def test_ttno_from_hamiltonian_is_the_reference_operator():
+    """TTNO.from_hamiltonian builds the same operator as the reference's TTNO
+    (expectation values on random states with full bond dimensions), with the
+    reference's bond dimension for nearest-neighbour models."""
+    import oracle as O
+    import pytreenet_gb300 as P
+    c = load_case("binary7_tfim_fastest_o2")          # TFIM, J = 1, g = 0.9
+    st = build_ttn(P.TTNS, c["spec"], c["init"])
+    H = P.TTNO.from_hamiltonian(_symbolic_tfim(c["spec"], 1.0, 0.9), st)
+    W = {nid: H.phys(nid) for nid, _ in c["spec"]}
+    assert max(max(w.shape[:-2], default=0) for w in W.values()) == 3
+    rng = np.random.default_rng(0)
+    from pytreenet_gb300.workloads import binary_tfim_random_state
+    for _ in range(4):
+        s, spec, tens, _, _ = binary_tfim_random_state(n=7, chi=8, seed=int(rng.integers(1 << 30)))
+        ost = O.OState(oracle_state(c).tree, tens)
+        a = O.ttno_expectation(ost, W)
+        b = O.ttno_expectation(ost, c["ttno"])
+        assert abs(a - b) < 1e-12 * max(1.0, abs(b))
+    # a long-range, multi-site, symbolic-coefficient Hamiltonian against a dense sum
+    from fractions import Fraction
+    X = np.array([[0, 1], [1, 0]], dtype=complex)
+    Y = np.array([[0, -1j], [1j, 0]], dtype=complex)
+    terms = [(Fraction(1, 2), "K", P.TensorProduct({"s3": "X", "s6": "Y", "s0": "Z"})),
+             (Fraction(1), "1", P.TensorProduct({"s4": "Z", "s5": "Z"})),
+             P.TensorProduct({"s2": X}), (Fraction(3), "K", P.TensorProduct({"s3": "X", "s6": "Y"}))]
+    Hs = P.Hamiltonian(terms, {"X": X, "Y": Y, "Z": Zm}, {"K": 0.7})
+    Ht = P.TTNO.from_hamiltonian(Hs, st)
+    Wt = {nid: Ht.phys(nid) for nid, _ in c["spec"]}
+    ids = [n for n, _ in c["spec"]]
+
+    def dense(ops):
+        mats = [ops.get(n, np.eye(2)) for n in ids]
+        out = mats[0]
+        for m in mats[1:]:
+            out = np.kron(out, m)
+        return out
+    Hd = 0.35 * dense({"s3": X, "s6": Y, "s0": Zm}) + dense({"s4": Zm, "s5": Zm}) + dense({"s2": X}) \
+        + 2.1 * dense({"s3": X, "s6": Y})
+    for _ in range(3):
+        s, spec, tens, _, _ = binary_tfim_random_state(n=7, chi=8, seed=int(rng.integers(1 << 30)))
+        ost = O.OState(oracle_state(c).tree, tens)
+        v = O.state_vector(ost, ids)
+        assert abs(O.ttno_expectation(ost, Wt) - np.vdot(v, Hd @ v)) < 1e-12 * max(1.0, np.linalg.norm(v) ** 2)
+
+
+def test_ttno_from_hamiltonian_drives_tdvp(monkeypatch):
+    """One-site TDVP with a TTNO from TTNO.from_hamiltonian reproduces the
+    reference's run, which used the reference's own TTNO."""
+    fake_ptn.install(monkeypatch)
+    import pytreenet_gb300 as P
+    c = load_case("binary15_tfim_l2l_o2")              # TFIM, J = 1, g = 0.6
+    st = build_ttn(P.TTNS, c["spec"], c["init"])
+    H = P.TTNO.from_hamiltonian(_symbolic_tfim(c["spec"], 1.0, 0.6), st)
+    algo = P.SecondOrderOneSiteTDVP(st, H, c["dt"], c["dt"] * c["steps"], {},
+                                    config=P.TDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV,
+                                                        main_path_mode=P.PathFinderMode.LeafToLeaf),
+                                    solver_options={"krylov_tol": c["krylov_tol"]})
+    for k in range(c["steps"]):
+        algo.run_one_time_step()
+        z = np.array([algo.evaluate_operator({nid: Zm}) for nid, _ in c["spec"]])
+        assert np.max(np.abs(z - c["z"][k])) < 1e-10

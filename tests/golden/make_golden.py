@@ -661,6 +661,38 @@ def heff_cases(ptn):
     print("heff written", {n: rec[f"heff/{n}"].shape for n in nodes})
 
 
+def exact_cases(ptn):
+    """``ExactTimeEvolution`` (``time_evolution/exact_time_evolution.py``) on a
+    random 6-site Hermitian H: a closed run (state vector) and an open one (a
+    vectorised density matrix under a 64 x 64 generator)."""
+    from pytreenet.time_evolution.exact_time_evolution import ExactTimeEvolution, ExactTimeEvolutionConfig
+    rng = np.random.default_rng(83)
+    n = 64
+    a = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
+    H = (a + a.conj().T) / 4
+    psi = rng.normal(size=n) + 1j * rng.normal(size=n)
+    psi /= np.linalg.norm(psi)
+    ops = [np.diag(rng.normal(size=n)).astype(complex), (lambda b: (b + b.conj().T) / 2)(rng.normal(size=(n, n)) + 0j)]
+    rec = {"H": H, "psi": psi, "op0": ops[0], "op1": ops[1], "dt": 0.05, "final": 0.2}
+    m = 8
+    L = rng.normal(size=(m * m, m * m)) + 1j * rng.normal(size=(m * m, m * m))
+    L = (L + L.conj().T) / 8
+    rho = np.eye(m, dtype=complex).reshape(-1) / m
+    O = np.diag(np.arange(m)).astype(complex)
+    ev2 = ExactTimeEvolution(rho, L, 0.05, 0.2, [O], config=ExactTimeEvolutionConfig(open=True))
+    for _ in range(4):
+        ev2.run_one_time_step()
+    rec.update(L=L, rho=rho, O=O, open_final=ev2.evaluate_operator(O))
+    ev3 = ExactTimeEvolution(psi, H, 0.05, 0.2, ops)
+    vals = []
+    for _ in range(4):
+        ev3.run_one_time_step()
+        vals.append([ev3.evaluate_operator(o) for o in ops])
+    rec["closed_values"] = np.array(vals)
+    np.savez_compressed(os.path.join(HERE, "exact_evolution.npz"), **rec)
+    print("exact written")
+
+
 def time_dep_cases(ptn):
     rng = np.random.default_rng(77)
     spec = binary_tree(7)
@@ -723,6 +755,7 @@ def main(ref_root):
     tebd_swap_cases(ptn)
     default_mode_cases(ptn)
     heff_cases(ptn)
+    exact_cases(ptn)
 
 
 if __name__ == "__main__":

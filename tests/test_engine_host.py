@@ -666,3 +666,26 @@ def test_ttno_from_hamiltonian_drives_tdvp(monkeypatch):
         algo.run_one_time_step()
         z = np.array([algo.evaluate_operator({nid: Zm}) for nid, _ in c["spec"]])
         assert np.max(np.abs(z - c["z"][k])) < 1e-10
+
+
+def test_exact_time_evolution_matches_reference(monkeypatch):
+    """ExactTimeEvolution (closed and open) against the reference's run."""
+    import os
+    fake_ptn.install(monkeypatch)
+    from golden_util import GOLDEN
+    from pytreenet_gb300.exact import ExactTimeEvolution, ExactTimeEvolutionConfig
+    d = np.load(os.path.join(GOLDEN, "exact_evolution.npz"))
+    ops = [d["op0"], d["op1"]]
+    ev = ExactTimeEvolution(d["psi"], d["H"], float(d["dt"]), float(d["final"]), ops)
+    assert ev.num_time_steps == 4
+    for k in range(4):
+        ev.run_one_time_step()
+        got = [ev.evaluate_operator(o) for o in ops]
+        assert np.max(np.abs(np.array(got) - d["closed_values"][k])) < 1e-12
+    res = ExactTimeEvolution(d["psi"], d["H"], float(d["dt"]), float(d["final"]), ops).run()
+    assert np.max(np.abs(res[1:] - d["closed_values"])) < 1e-12
+    ev2 = ExactTimeEvolution(d["rho"], d["L"], float(d["dt"]), float(d["final"]), [d["O"]],
+                             config=ExactTimeEvolutionConfig(open=True))
+    for _ in range(4):
+        ev2.run_one_time_step()
+    assert abs(ev2.evaluate_operator(d["O"]) - d["open_final"]) < 1e-12

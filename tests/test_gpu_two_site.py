@@ -251,3 +251,19 @@ def test_gpu_ttns_observable_methods():
     fin = build_ttn(P.TTNS, c["spec"], c["final"])
     H = build_ttn(P.TTNO, c["spec"], c["ttno"])
     assert abs(fin.operator_expectation_value(H) - c["energy_final"]) < 1e-10
+
+
+def test_gpu_exact_time_evolution():
+    """ExactTimeEvolution on the GB300 against the reference's run."""
+    import os
+    from golden_util import GOLDEN
+    from pytreenet_gb300.exact import ExactTimeEvolution, ExactTimeEvolutionConfig
+    d = np.load(os.path.join(GOLDEN, "exact_evolution.npz"))
+    ops = [d["op0"], d["op1"]]
+    res = ExactTimeEvolution(d["psi"], d["H"], float(d["dt"]), float(d["final"]), ops).run()
+    assert np.max(np.abs(res[1:] - d["closed_values"])) < 1e-12
+    ev2 = ExactTimeEvolution(d["rho"], d["L"], float(d["dt"]), float(d["final"]), [d["O"]],
+                             config=ExactTimeEvolutionConfig(open=True))
+    for _ in range(4):
+        ev2.run_one_time_step()
+    assert abs(ev2.evaluate_operator(d["O"]) - d["open_final"]) < 1e-12

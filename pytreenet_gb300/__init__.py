@@ -19,6 +19,7 @@ from .tebd import TEBD, TrotterStep, TrotterSplitting, NumericOperator, SWAPlist
 from .operators import nearest_neighbour_ttno, tfim_ttno, heisenberg_ttno
 from .hamiltonian import Hamiltonian
 from .exact import ExactTimeEvolution, ExactTimeEvolutionConfig
+from .application import ApplicationMethod, apply_ttno_to_ttns
 from .batch import run_realisations
 from .contractions import (SandwichCache, contract_ket_ham_with_envs, contract_any,
                            effective_single_site_evolution, get_effective_single_site_hamiltonian,
@@ -35,7 +36,7 @@ __all__ = [
     "SVDParameters", "truncate_singular_values", "TEBD", "TrotterStep", "TrotterSplitting",
     "NumericOperator", "SWAPlist", "swap_gate",
     "nearest_neighbour_ttno", "tfim_ttno", "heisenberg_ttno", "run_realisations", "Hamiltonian",
-    "ExactTimeEvolution", "ExactTimeEvolutionConfig",
+    "ExactTimeEvolution", "ExactTimeEvolutionConfig", "ApplicationMethod", "apply_ttno_to_ttns",
     "SandwichCache", "contract_ket_ham_with_envs", "contract_any", "effective_single_site_evolution",
     "get_effective_single_site_hamiltonian", "get_effective_single_site_hamiltonian_nodes",
     "OneSiteTDVPAdjoint", "coupling_gradient", "FixedBUG", "FixedBUGConfig", "BUG", "BUGConfig",

@@ -367,6 +367,12 @@ class TreeTensorNetworkState(TreeTensorNetwork):
             return self.tensor_product_expectation_value(operator)
         raise TypeError("Operator must be a TensorProduct or a TTNO!")
 
+    def apply_operator(self, operator):
+        """Absorb every one-site operator of a TensorProduct into its node
+        (``ttns.py:329-337``), on the device."""
+        from .application import apply_operator_in_place
+        apply_operator_in_place(self, operator)
+
     def get_phys_numpy(self, nid):
         t = self.phys(nid)
         return t if isinstance(t, np.ndarray) else t.detach().cpu().numpy()

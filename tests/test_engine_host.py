@@ -689,3 +689,37 @@ def test_exact_time_evolution_matches_reference(monkeypatch):
     for _ in range(4):
         ev2.run_one_time_step()
     assert abs(ev2.evaluate_operator(d["O"]) - d["open_final"]) < 1e-12
+
+
+def test_direct_ttno_application(monkeypatch):
+    """apply_ttno_to_ttns (DIRECT) and TTNS.apply_operator against dense H|psi>."""
+    fake_ptn.install(monkeypatch)
+    import oracle as O
+    import pytreenet_gb300 as P
+    from fractions import Fraction
+    from pytreenet_gb300.workloads import binary_tfim_random_state
+    X = np.array([[0, 1], [1, 0]], dtype=complex)
+    Y = np.array([[0, -1j], [1j, 0]], dtype=complex)
+    st, spec, tens, _, _ = binary_tfim_random_state(n=7, chi=8, seed=9)
+    ids = [n for n, _ in spec]
+    terms = [(Fraction(1, 2), "K", P.TensorProduct({"s3": "X", "s6": "Y", "s0": "Z"})),
+             P.TensorProduct({"s4": "Z", "s5": "Z"}), P.TensorProduct({"s2": X})]
+    H = P.TTNO.from_hamiltonian(P.Hamiltonian(terms, {"X": X, "Y": Y, "Z": Zm}, {"K": 0.7}), st)
+
+    def dense(ops):
+        mats = [ops.get(n, np.eye(2)) for n in ids]
+        out = mats[0]
+        for m in mats[1:]:
+            out = np.kron(out, m)
+        return out
+    Hd = 0.35 * dense({"s3": X, "s6": Y, "s0": Zm}) + dense({"s4": Zm, "s5": Zm}) + dense({"s2": X})
+    psi = st.to_dense(ids)
+    out = P.apply_ttno_to_ttns(st, H)
+    got = out.to_dense(ids)
+    assert np.max(np.abs(got - Hd @ psi)) < 1e-12 * np.max(np.abs(Hd @ psi))
+    assert out.phys("s1").shape[0] == st.phys("s1").shape[0] * H.phys("s1").shape[0]
+    st2, _, _, _, _ = binary_tfim_random_state(n=7, chi=8, seed=9)
+    st2.apply_operator(P.TensorProduct({"s2": X, "s5": Zm}))
+    assert np.max(np.abs(st2.to_dense(ids) - dense({"s2": X, "s5": Zm}) @ psi)) < 1e-12
+    with pytest.raises(NotImplementedError):
+        P.apply_ttno_to_ttns(st, H, method=P.ApplicationMethod.ZIPUP)

@@ -267,3 +267,26 @@ def test_gpu_exact_time_evolution():
     for _ in range(4):
         ev2.run_one_time_step()
     assert abs(ev2.evaluate_operator(d["O"]) - d["open_final"]) < 1e-12
+
+
+def test_gpu_direct_ttno_application():
+    """apply_ttno_to_ttns (DIRECT) on the GB300 against dense H|psi>."""
+    import pytreenet_gb300 as P
+    from pytreenet_gb300.workloads import binary_tfim_random_state
+    X = np.array([[0, 1], [1, 0]], dtype=complex)
+    Zm = np.diag([1.0, -1.0]).astype(complex)
+    st, spec, tens, _, _ = binary_tfim_random_state(n=7, chi=8, seed=9)
+    ids = [n for n, _ in spec]
+    H = P.TTNO.from_hamiltonian(P.Hamiltonian([P.TensorProduct({"s3": X, "s0": Zm}),
+                                               P.TensorProduct({"s2": X})]), st)
+
+    def dense(ops):
+        mats = [ops.get(n, np.eye(2)) for n in ids]
+        out = mats[0]
+        for m in mats[1:]:
+            out = np.kron(out, m)
+        return out
+    psi = st.to_dense(ids)
+    ref = (dense({"s3": X, "s0": Zm}) + dense({"s2": X})) @ psi
+    got = P.apply_ttno_to_ttns(st, H).to_dense(ids)
+    assert np.max(np.abs(got - ref)) < 1e-12 * np.max(np.abs(ref))

@@ -34,8 +34,9 @@ from . import engine as E
 from .adjoint import (_SiteOp, _raw_contract, _solver, _tensor_apply, absorb, env_apply, qr_keep_raw)
 from .engine import CDT, DeviceNetwork, check
 from .tdvp import (TTNTimeEvolutionConfig, TensorProduct, TimeEvoMode, check_time_evo_mode,
-                   compute_num_time_steps, leaf_to_leaf_update_path)
-from .truncation import SVDParameters, truncate_singular_values
+                   compute_num_time_steps)
+from .svd_truncation import TreeOps, move_center, qr_split, truncate_tensors
+from .truncation import SVDParameters
 
 DEFAULT_KRYLOV_TOL = 1e-10
 
@@ -63,18 +64,6 @@ class BUGConfig(CommonBUGConfig, SVDParameters):
     def __post_init__(self):
         SVDParameters.__post_init__(self)
         assert self.fixed_rank is False, "Fixed rank is not supported for BUG!"
-
-
-def qr_split(A, ax, reduced: bool):
-    """QR with leg ``ax`` as the column index; ``reduced`` (SplitMode.REDUCED)
-    shrinks that leg to the row count when A is wide, else it is kept."""
-    Q, R = qr_keep_raw(A, ax)
-    k = A.shape[ax]
-    m = A.numel() // k
-    if reduced and m < k:
-        Q = Q.narrow(ax, 0, m).contiguous()
-        R = R[:m].contiguous()
-    return Q, R
 
 
 def small_svd(R: torch.Tensor):
@@ -272,36 +261,10 @@ class BUG(FixedBUG):
     config_class = BUGConfig
     _adaptive = True
 
-    def _move(self, A, center, target, reduced):
-        path = self.state.path_from_to(center, target)
-        for a, b in zip(path[:-1], path[1:]):
-            Q, R = qr_split(A[a], self._ax(a, b), reduced=reduced)
-            A[a] = Q
-            A[b] = absorb(R, A[b], self._ax(b, a))
-        return target
-
-    def _compress_parent_leg(self, A, nid):
-        """``compress_parent_leg`` (``svd_truncation.py``)."""
-        T = A[nid]
-        Q, R = qr_keep_raw(T, 0)
-        Ut, Vt, s = small_svd(R)
-        new_s, _ = truncate_singular_values(s, self.config)
-        r = len(new_s)
-        A[nid] = absorb(Ut[:r].contiguous(), Q, 0)
-        p = self.parent[nid]
-        svh = new_s[:, None] * Vt[:r].cpu().numpy().conj()
-        A[p] = absorb(torch.from_numpy(np.ascontiguousarray(svh)).to(T.device), A[p], self._ax(p, nid))
-        return p
-
     def truncation(self, A):
-        path = leaf_to_leaf_update_path(self.state)
-        center = self._move(A, self.root, path[0], True)
-        for nid in path:
-            if nid == self.root:
-                continue
-            center = self._move(A, center, nid, True)
-            center = self._compress_parent_leg(A, nid)
-        self._move(A, center, self.root, False)
+        ops = TreeOps(self.state)
+        center = truncate_tensors(ops, A, self.root, self.config)
+        move_center(ops, A, center, self.root, False)
         return A
 
     def run_one_time_step(self, **kwargs):

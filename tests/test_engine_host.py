@@ -723,3 +723,31 @@ def test_direct_ttno_application(monkeypatch):
     assert np.max(np.abs(st2.to_dense(ids) - dense({"s2": X, "s5": Zm}) @ psi)) < 1e-12
     with pytest.raises(NotImplementedError):
         P.apply_ttno_to_ttns(st, H, method=P.ApplicationMethod.ZIPUP)
+
+
+def test_apply_and_truncate_matches_oracle(monkeypatch):
+    """apply_and_truncate(DIRECT, SVD): the engine's truncated H|psi> equals the
+    oracle's svd_truncation of the same state (a binding bond cap), and without
+    a cap the truncation only removes the zero directions."""
+    fake_ptn.install(monkeypatch)
+    import oracle as O
+    import pytreenet_gb300 as P
+    from pytreenet_gb300.workloads import binary_tfim_random_state
+    X = np.array([[0, 1], [1, 0]], dtype=complex)
+    st, spec, tens, _, _ = binary_tfim_random_state(n=7, chi=2, seed=4)
+    ids = [n for n, _ in spec]
+    H = P.TTNO.from_hamiltonian(_symbolic_tfim(spec, 1.0, 0.7), st)
+    full = P.apply_ttno_to_ttns(st, H)
+    ref_vec = full.to_dense(ids)
+    loose = P.apply_and_truncate(st, H, P.ApplicationMethod.DIRECT, P.TruncationMethod.SVD,
+                                 trunc_args=(P.SVDParameters(max_bond_dim=100, rel_tol=1e-13, total_tol=1e-13),))
+    assert np.max(np.abs(loose.to_dense(ids) - ref_vec)) < 1e-11 * np.max(np.abs(ref_vec))
+    params = P.SVDParameters(max_bond_dim=3, rel_tol=1e-10, total_tol=1e-10)
+    tight = P.apply_and_truncate(st, H, P.ApplicationMethod.DIRECT, P.TruncationMethod.SVD, trunc_args=(params,))
+    assert max(tight.phys(n).shape[0] for n in ids if n != "s0") <= 3
+    ost = O.OState(oracle_state(load_case("binary7_tfim_fastest_o2")).tree,
+                   {n: full.get_phys_numpy(n) for n in ids})
+    O.canonical_form(ost, O.leaf_to_leaf_path(ost.tree)[0])
+    O.svd_truncation(ost, O.SVDParams(max_bond_dim=3, rel_tol=1e-10, total_tol=1e-10))
+    a, b = tight.to_dense(ids), O.state_vector(ost, ids)
+    assert np.max(np.abs(a - b)) < 1e-10 * np.max(np.abs(b))

@@ -290,3 +290,24 @@ def test_gpu_direct_ttno_application():
     ref = (dense({"s3": X, "s0": Zm}) + dense({"s2": X})) @ psi
     got = P.apply_ttno_to_ttns(st, H).to_dense(ids)
     assert np.max(np.abs(got - ref)) < 1e-12 * np.max(np.abs(ref))
+
+
+def test_gpu_apply_and_truncate():
+    """apply_and_truncate(DIRECT, SVD) on the GB300: a tolerance-only truncation
+    keeps H|psi>, a bond cap of 3 is respected."""
+    import pytreenet_gb300 as P
+    from pytreenet_gb300.workloads import binary_tfim_random_state
+    X = np.array([[0, 1], [1, 0]], dtype=complex)
+    Zm = np.diag([1.0, -1.0]).astype(complex)
+    st, spec, tens, _, _ = binary_tfim_random_state(n=7, chi=2, seed=4)
+    ids = [n for n, _ in spec]
+    terms = [P.TensorProduct({p: -Zm, n: Zm}) for n, p in spec if p is not None]
+    terms += [P.TensorProduct({n: -0.7 * X}) for n, _ in spec]
+    H = P.TTNO.from_hamiltonian(P.Hamiltonian(terms), st)
+    ref = P.apply_ttno_to_ttns(st, H).to_dense(ids)
+    loose = P.apply_and_truncate(st, H, P.ApplicationMethod.DIRECT, P.TruncationMethod.SVD,
+                                 trunc_args=(P.SVDParameters(max_bond_dim=100, rel_tol=1e-13, total_tol=1e-13),))
+    assert np.max(np.abs(loose.to_dense(ids) - ref)) < 1e-11 * np.max(np.abs(ref))
+    tight = P.apply_and_truncate(st, H, P.ApplicationMethod.DIRECT, P.TruncationMethod.SVD,
+                                 trunc_args=(P.SVDParameters(max_bond_dim=3, rel_tol=1e-10, total_tol=1e-10),))
+    assert max(tight.phys(n).shape[0] for n in ids if n != "s0") <= 3

@@ -33,8 +33,9 @@ from . import _lib
 from . import engine as E
 from .adjoint import (_SiteOp, _raw_contract, _solver, _tensor_apply, absorb, env_apply, qr_keep_raw)
 from .engine import CDT, DeviceNetwork, check
-from .tdvp import (TTNTimeEvolutionConfig, TensorProduct, TimeEvoMode, check_time_evo_mode,
+from .tdvp import (TTNTimeEvolutionConfig, TensorProduct, TimeEvoMode, _tensor_copy, check_time_evo_mode,
                    compute_num_time_steps)
+from .results import RunLoop, init_operators
 from .svd_truncation import TreeOps, move_center, qr_split, truncate_tensors
 from .truncation import SVDParameters
 
@@ -90,7 +91,7 @@ def small_svd(R: torch.Tensor):
     return Ut, Vt, host[:k].numpy().copy()
 
 
-class FixedBUG:
+class FixedBUG(RunLoop):
     """Fixed-rank BUG driver with PyTreeNet's constructor and stepping API."""
 
     config_class = FixedBUGConfig
@@ -108,9 +109,10 @@ class FixedBUG:
         self.time_step_size = float(time_step_size)
         self.final_time = float(final_time)
         self.num_time_steps = compute_num_time_steps(final_time, time_step_size)
-        self.operators = operators if operators is not None else []
+        self.operators = init_operators(operators)
         self.hamiltonian = hamiltonian
         initial_state._finalise()
+        self._loschmidt_state = _tensor_copy(initial_state) if getattr(self.config, "record_loschmidt_amplitude", False) else None
         self.state = initial_state.copy_structure()
         self.net = DeviceNetwork(self.state, hamiltonian)
         root = self.state.root_id
@@ -203,6 +205,12 @@ class FixedBUG:
         new[root] = self._evolve(root, self._in_new_child_bases(A[root], root, Ms), envs, tol)
         return new
 
+    def update_hamiltonian(self):
+        """A time-dependent TTNO advanced by one step and copied to the device."""
+        self.hamiltonian.update(self.time_step_size)
+        self.hamiltonian.modify_state(self.state)
+        self.net.refresh_hamiltonian(self.hamiltonian)
+
     def _store(self, new: dict):
         for nid, t in new.items():
             if tuple(t.shape) == tuple(self.net.t[nid].shape):
@@ -222,27 +230,6 @@ class FixedBUG:
         if isinstance(operator, TreeTensorNetworkOperator):
             return self.net.expect_ttno(operator)
         return self.net.expect_local(dict(operator))
-
-    def evaluate_operators(self):
-        ops = self.operators
-        if isinstance(ops, dict):
-            ops = list(ops.values())
-        elif isinstance(ops, TensorProduct):
-            ops = [ops]
-        return np.array([self.evaluate_operator(o) for o in ops])
-
-    def run(self, evaluation_time: int = 1, pgbar: bool = False):
-        """``TimeEvolution.run`` (``time_evolution/time_evolution.py:346-368``)."""
-        res = [self.evaluate_operators()]
-        self.times = [0.0]
-        for i in range(self.num_time_steps):
-            self.run_one_time_step()
-            if evaluation_time != "inf" and (i + 1) % evaluation_time == 0:
-                res.append(self.evaluate_operators())
-                self.times.append((i + 1) * self.time_step_size)
-        self.results = np.array(res)
-        return self.results
-
 
 class BUG(FixedBUG):
     """Rank-adaptive BUG (``time_evolution/bug.py:30-117``): every basis is

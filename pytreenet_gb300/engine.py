@@ -1428,16 +1428,21 @@ class DeviceNetwork:
 
     # -- observables ------------------------------------------------------------------
     def overlap(self, other: "DeviceNetwork") -> complex:
-        """<self|other> for two states on the same tree (``contract_two_ttns``,
-        ``contractions/state_state_contraction.py:29-66``)."""
+        """<self|other> for two states on the same tree, bond dimensions free to
+        differ (``contract_two_ttns``, ``contractions/state_state_contraction.py:29-66``).
+        Each environment has legs (other's bond, self's bond)."""
         st = self.state
+        if other.nbrs(st.root_id) != self.nbrs(st.root_id):
+            raise ValueError("the two states must share the tree and its leg layout")
 
         def rec(nid, toward):
-            shape = self.shape(nid)
-            n = len(shape) - 1
+            ks, bs = other.shape(nid), self.shape(nid)
+            if ks[-1] != bs[-1]:
+                raise ValueError(f"physical dimensions of {nid} differ")
+            n = len(bs) - 1
             nb = self.nbrs(nid)
             cb = ChainBuilder(self.ws)
-            T = Operand.contiguous(("fixed", other.t[nid]), [f"a{k}" for k in range(n)] + ["s"], shape)
+            T = Operand.contiguous(("fixed", other.t[nid]), [f"a{k}" for k in range(n)] + ["s"], ks)
             for k, x in enumerate(nb):
                 if x == toward:
                     continue
@@ -1445,16 +1450,16 @@ class DeviceNetwork:
                 T = cb.contract(T, Operand.contiguous(("fixed", sub), [f"a{k}", f"c{k}"], list(sub.shape)),
                                 [f"a{k}"])
             B = Operand.contiguous(("fixed", self.t[nid]),
-                                   [f"c{k}" if nb[k] != toward else "z" for k in range(n)] + ["s"], shape)
+                                   [f"c{k}" if nb[k] != toward else "z" for k in range(n)] + ["s"], bs)
             if toward is None:
                 res = torch.zeros((1,), dtype=CDT, device=self.device)
                 cb.contract(T, B, [f"c{k}" for k in range(n)] + ["s"], out=Operand(("fixed", res), [], [], []),
                             conj_b=True)
             else:
                 k0 = nb.index(toward)
-                res = torch.zeros((shape[k0], shape[k0]), dtype=CDT, device=self.device)
+                res = torch.zeros((ks[k0], bs[k0]), dtype=CDT, device=self.device)
                 cb.contract(T, B, [f"c{k}" for k in range(n) if k != k0] + ["s"],
-                            out=Operand.contiguous(("fixed", res), [f"a{k0}", "z"], [shape[k0]] * 2), conj_b=True)
+                            out=Operand.contiguous(("fixed", res), [f"a{k0}", "z"], [ks[k0], bs[k0]]), conj_b=True)
             cb.plan().run()
             return res
         return complex(rec(st.root_id, None).cpu().numpy()[0])

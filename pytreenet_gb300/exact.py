@@ -19,6 +19,7 @@ import torch
 from . import engine as E
 from .adjoint import _raw_contract
 from .engine import CDT
+from .results import RunLoop, init_operators
 from .tdvp import compute_num_time_steps
 
 
@@ -28,7 +29,7 @@ class ExactTimeEvolutionConfig:
     open: bool = False
 
 
-class ExactTimeEvolution:
+class ExactTimeEvolution(RunLoop):
     """``ExactTimeEvolution(initial_state, hamiltonian, time_step_size, final_time,
     operators, config=None, solver_options=None)`` with ``run_one_time_step``,
     ``evaluate_operator`` and ``run``."""
@@ -47,7 +48,7 @@ class ExactTimeEvolution:
         self.time_step_size = float(time_step_size)
         self.final_time = float(final_time)
         self.num_time_steps = compute_num_time_steps(final_time, time_step_size)
-        self.operators = operators if operators is not None else []
+        self.operators = init_operators(operators)
         self.hamiltonian = np.asarray(hamiltonian, dtype=complex)
         u = scipy.linalg.expm(-1j * self.time_step_size * self.hamiltonian)
         self._u = torch.from_numpy(np.ascontiguousarray(u)).to(self.device, CDT)
@@ -79,22 +80,3 @@ class ExactTimeEvolution:
             return complex(_raw_contract(O, ["i", "j"], rho, ["j", "i"], [], ["i", "j"]).item())
         opsi = _raw_contract(O, ["i", "j"], self._psi, ["j"], ["i"], ["j"])
         return complex(_raw_contract(self._psi, ["i"], opsi, ["i"], [], ["i"], conj_a=True).item())
-
-    def evaluate_operators(self):
-        ops = self.operators
-        if isinstance(ops, dict):
-            ops = list(ops.values())
-        elif isinstance(ops, np.ndarray):
-            ops = [ops]
-        return np.array([self.evaluate_operator(o) for o in ops])
-
-    def run(self, evaluation_time: int = 1, pgbar: bool = False):
-        res = [self.evaluate_operators()]
-        self.times = [0.0]
-        for i in range(self.num_time_steps):
-            self.run_one_time_step()
-            if evaluation_time != "inf" and (i + 1) % evaluation_time == 0:
-                res.append(self.evaluate_operators())
-                self.times.append((i + 1) * self.time_step_size)
-        self.results = np.array(res)
-        return self.results

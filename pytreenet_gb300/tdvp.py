@@ -17,6 +17,7 @@ import numpy as np
 
 from .engine import DeviceNetwork
 from .truncation import SVDParameters
+from .results import RunLoop, init_operators
 from .ttn import TreeTensorNetworkOperator, TreeTensorNetworkState
 
 
@@ -121,6 +122,13 @@ class TDVPConfig(TTNTimeEvolutionConfig):
     """``tdvp_algorithms/tdvp_algorithm.py:23-34``."""
     time_evo_mode: TimeEvoMode = TimeEvoMode.FASTEST
     main_path_mode: PathFinderMode = PathFinderMode.LeafToRoot
+
+
+def _tensor_copy(ttn):
+    """A TTN sharing no tensor with ``ttn`` (the state at time zero)."""
+    out = ttn.copy_structure()
+    out._phys = {k: (v.copy() if isinstance(v, np.ndarray) else v.clone()) for k, v in out._phys.items()}
+    return out
 
 
 def compute_num_time_steps(final_time: float, time_step_size: float) -> int:
@@ -231,7 +239,7 @@ class TensorProduct(dict):
     """Single-site operators keyed by node id (``operators/tensorproduct.py:33``)."""
 
 
-class OneSiteTDVP:
+class OneSiteTDVP(RunLoop):
     """Common machinery of the one-site TDVP drivers
     (``tdvp_algorithms/tdvp_algorithm.py:37-221``, ``onesitetdvp.py:17-134``)."""
 
@@ -253,9 +261,10 @@ class OneSiteTDVP:
         self.time_step_size = float(time_step_size)
         self.final_time = float(final_time)
         self.num_time_steps = compute_num_time_steps(final_time, time_step_size)
-        self.operators = operators if operators is not None else []
+        self.operators = init_operators(operators)
         self.hamiltonian = hamiltonian
         initial_state._finalise()
+        self._loschmidt_state = _tensor_copy(initial_state) if self.config.record_loschmidt_amplitude else None
         self._initial_state = initial_state.copy_structure()
         self.state = initial_state.copy_structure()
         self.update_path = find_update_path(self._initial_state, self.config.main_path_mode)
@@ -315,15 +324,6 @@ class OneSiteTDVP:
             return self.net.expect_ttno(operator)
         return self.net.expect_local(dict(operator))
 
-    def evaluate_operators(self):
-        ops = self.operators
-        if isinstance(ops, dict):
-            ops = list(ops.values())
-        elif isinstance(ops, TensorProduct):
-            ops = [ops]
-        return np.array([self.evaluate_operator(o) for o in ops])
-
-    # -- time-dependent Hamiltonians (``ttn_time_evolution.py:266-280``) -----------
     def update_hamiltonian(self):
         """Advance a time-dependent TTNO by one step and copy its tensors into
         the device buffers (the environments are kept, as in the reference)."""
@@ -334,22 +334,6 @@ class OneSiteTDVP:
     def reset_hamiltonian(self):
         self.hamiltonian.reset()
         self.net.refresh_hamiltonian(self.hamiltonian)
-
-    def run(self, evaluation_time: int = 1, pgbar: bool = False):
-        """``TimeEvolution.run`` (``time_evolution/time_evolution.py:346-368``):
-        step, measure, then (``config.time_dep``) update the Hamiltonian."""
-        res = [self.evaluate_operators()]
-        self.times = [0.0]
-        for i in range(self.num_time_steps):
-            self.run_one_time_step()
-            if evaluation_time != "inf" and (i + 1) % evaluation_time == 0:
-                res.append(self.evaluate_operators())
-                self.times.append((i + 1) * self.time_step_size)
-            if self.config.time_dep:
-                self.update_hamiltonian()
-        self.results = np.array(res)
-        return self.results
-
 
 class FirstOrderOneSiteTDVP(OneSiteTDVP):
     """``tdvp_algorithms/firstorderonesite.py:7-104``."""

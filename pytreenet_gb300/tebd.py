@@ -21,7 +21,8 @@ import scipy.linalg
 import torch
 
 from .engine import CDT, DeviceNetwork
-from .tdvp import TTNTimeEvolutionConfig, TensorProduct, compute_num_time_steps
+from .results import RunLoop, init_operators
+from .tdvp import TTNTimeEvolutionConfig, TensorProduct, _tensor_copy, compute_num_time_steps
 from .truncation import SVDParameters
 
 
@@ -138,7 +139,7 @@ class TrotterSplitting(list):
         return out
 
 
-class TEBD:
+class TEBD(RunLoop):
     """``time_evolution/tebd.py:18-155``."""
 
     def __init__(self, initial_state, trotter_splitting, time_step_size: float, final_time: float,
@@ -152,8 +153,9 @@ class TEBD:
         self.time_step_size = float(time_step_size)
         self.final_time = float(final_time)
         self.num_time_steps = compute_num_time_steps(final_time, time_step_size)
-        self.operators = operators if operators is not None else []
+        self.operators = init_operators(operators)
         initial_state._finalise()
+        self._loschmidt_state = _tensor_copy(initial_state) if getattr(self.config, "record_loschmidt_amplitude", False) else None
         self.initial_state = initial_state
         self.state = initial_state.copy_structure()
         self.state.orthogonality_center_id = None
@@ -201,23 +203,3 @@ class TEBD:
         if isinstance(operator, TreeTensorNetworkOperator):
             return self.net.expect_ttno(operator)
         return self.net.expect_local(dict(operator))
-
-    def evaluate_operators(self):
-        ops = self.operators
-        if isinstance(ops, dict) and not isinstance(ops, TensorProduct):
-            ops = list(ops.values())
-        elif isinstance(ops, TensorProduct):
-            ops = [ops]
-        return np.array([self.evaluate_operator(o) for o in ops])
-
-    def run(self, evaluation_time: int = 1, pgbar: bool = False):
-        """``TimeEvolution.run`` (``time_evolution/time_evolution.py:346-368``)."""
-        res = [self.evaluate_operators()]
-        self.times = [0.0]
-        for i in range(self.num_time_steps):
-            self.run_one_time_step()
-            if evaluation_time != "inf" and (i + 1) % evaluation_time == 0:
-                res.append(self.evaluate_operators())
-                self.times.append((i + 1) * self.time_step_size)
-        self.results = np.array(res)
-        return self.results

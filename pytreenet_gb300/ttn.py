@@ -212,6 +212,24 @@ class TreeTensorNetwork:
     def bond_dim(self, a, b) -> int:
         return self.phys(a).shape[self.phys_axis(a, b)]
 
+    def bond_dims(self) -> dict:
+        """(parent, child) -> bond dimension (``core/ttn.py:754-768``)."""
+        return {(self.nodes[n].parent, n): self.bond_dim(n, self.nodes[n].parent)
+                for n in self._order if self.nodes[n].parent is not None}
+
+    def max_bond_dim(self) -> int:
+        dims = self.bond_dims()
+        if not dims:
+            raise ValueError("This TTN has no virtual bond dimension!")
+        return max(dims.values())
+
+    def avg_bond_dim(self) -> float:
+        dims = self.bond_dims()
+        return sum(dims.values()) / len(dims)
+
+    def size(self) -> int:
+        return int(sum(int(np.prod(self.phys(n).shape)) for n in self._order))
+
     # -- files (``core/ttn.py:1747-1838``) ------------------------------------------
     def save(self, filepath: str):
         """``{filepath}.npz`` with every tensor in its node's leg order (parent,

@@ -693,6 +693,40 @@ def exact_cases(ptn):
     print("exact written")
 
 
+def run_results_case(ptn):
+    """``run(evaluation_time=2)`` of the reference's two-site TDVP with every
+    ``record_*`` flag set (``time_evolution.py:346-368``,
+    ``ttn_time_evolution.py:88-211``): the whole Results content is stored."""
+    from pytreenet.time_evolution.time_evolution import TimeEvoMode
+    from pytreenet.time_evolution.tdvp_algorithms.twositetdvp import TwoSiteTDVPConfig
+    rng = np.random.default_rng(97)
+    spec = binary_tree(7)
+    tensors = neel_state_tensors(spec)
+    psi = build_reference_state(ptn, spec, tensors)
+    h = rng.uniform(-1, 1, size=len(spec))
+    H = ptn.TTNO.from_hamiltonian(heisenberg_fields(ptn, spec, h), psi)
+    cfg = TwoSiteTDVPConfig(time_evo_mode=TimeEvoMode.KRYLOV, max_bond_dim=4, rel_tol=1e-10, total_tol=1e-10,
+                            record_bond_dim=True, record_max_bdim=True, record_average_bdim=True,
+                            record_total_size=True, record_norm=True, record_loschmidt_amplitude=True)
+    ops = {"z0": ptn.TensorProduct({"s0": Z}), "x3": ptn.TensorProduct({"s3": X})}
+    algo = ptn.SecondOrderTwoSiteTDVP(psi, H, 0.05, 0.05 * 6, ops, config=cfg, solver_options={"krylov_tol": 1e-12})
+    algo.run(evaluation_time=2, pgbar=False)
+    rec = {"spec_ids": np.array([s[0] for s in spec]),
+           "spec_parents": np.array(["" if s[1] is None else s[1] for s in spec]), "h": h}
+    for nid, t in tensors.items():
+        rec[f"init/{nid}"] = t
+    for nid, t in export_ttno(H, spec).items():
+        rec[f"ttno/{nid}"] = t
+    keys = []
+    for k, v in algo.results.results.items():
+        name = "bond/" + "/".join(k) if isinstance(k, tuple) else str(k)
+        rec["res/" + name] = np.asarray(v)
+        keys.append(name)
+    rec["res_keys"] = np.array(keys)
+    np.savez_compressed(os.path.join(HERE, "binary7_heis_2tdvp_results.npz"), **rec)
+    print("results written", keys)
+
+
 def time_dep_cases(ptn):
     rng = np.random.default_rng(77)
     spec = binary_tree(7)
@@ -756,6 +790,7 @@ def main(ref_root):
     default_mode_cases(ptn)
     heff_cases(ptn)
     exact_cases(ptn)
+    run_results_case(ptn)
 
 
 if __name__ == "__main__":

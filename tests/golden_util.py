@@ -259,3 +259,27 @@ def check_heff_fixture(tol=1e-12):
         got2 = P.get_effective_single_site_hamiltonian_nodes(st.nodes[nid], H.nodes[nid], H.get_tensor(nid), cache)
         assert np.max(np.abs(got2 - ref)) < tol * max(1.0, np.max(np.abs(ref))), nid
 
+
+
+def run_recorded_case(precision="plain"):
+    """The engine's SecondOrderTwoSiteTDVP.run(evaluation_time=2) with every
+    record flag, on the inputs of ``binary7_heis_2tdvp_results``; returns
+    (engine Results, reference arrays by name)."""
+    import numpy as np
+    import pytreenet_gb300 as P
+    d = np.load(os.path.join(GOLDEN, "binary7_heis_2tdvp_results.npz"))
+    ids = [str(x) for x in d["spec_ids"]]
+    spec = list(zip(ids, [str(x) or None for x in d["spec_parents"]]))
+    st = build_ttn(P.TTNS, spec, {i: d[f"init/{i}"] for i in ids})
+    H = build_ttn(P.TTNO, spec, {i: d[f"ttno/{i}"] for i in ids})
+    X = np.array([[0, 1], [1, 0]], dtype=complex)
+    Zm = np.diag([1.0, -1.0]).astype(complex)
+    cfg = P.TwoSiteTDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV, max_bond_dim=4, rel_tol=1e-10, total_tol=1e-10,
+                              record_bond_dim=True, record_max_bdim=True, record_average_bdim=True,
+                              record_total_size=True, record_norm=True, record_loschmidt_amplitude=True)
+    ops = {"z0": P.TensorProduct({"s0": Zm}), "x3": P.TensorProduct({"s3": X})}
+    algo = P.SecondOrderTwoSiteTDVP(st, H, 0.05, 0.05 * 6, ops, config=cfg, solver_options={"krylov_tol": 1e-12},
+                                    precision=precision)
+    algo.run(evaluation_time=2)
+    ref = {str(k): d["res/" + str(k)] for k in d["res_keys"]}
+    return algo.results, ref

@@ -751,3 +751,19 @@ def test_apply_and_truncate_matches_oracle(monkeypatch):
     O.svd_truncation(ost, O.SVDParams(max_bond_dim=3, rel_tol=1e-10, total_tol=1e-10))
     a, b = tight.to_dense(ids), O.state_vector(ost, ids)
     assert np.max(np.abs(a - b)) < 1e-10 * np.max(np.abs(b))
+
+
+def test_run_results_match_reference(monkeypatch):
+    """run(evaluation_time=2) with every record flag: the Results entries
+    (times, operators, bond dimensions, their maximum and average, total size,
+    norm, Loschmidt amplitude) equal the reference's."""
+    fake_ptn.install(monkeypatch)
+    from golden_util import run_recorded_case
+    res, ref = run_recorded_case()
+    for name, arr in ref.items():
+        key = tuple(name.split("/")[1:]) if name.startswith("bond/") else name
+        got = res.operator_result(key) if key != "times" else res.times()
+        assert got.shape == arr.shape, name
+        assert np.max(np.abs(got - arr)) < 1e-9 * max(1.0, np.max(np.abs(arr))), name
+    assert set(res.get_results().keys()) == {tuple(n.split("/")[1:]) if n.startswith("bond/") else n
+                                              for n in ref if n != "times"}

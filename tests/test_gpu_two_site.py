@@ -311,3 +311,14 @@ def test_gpu_apply_and_truncate():
     tight = P.apply_and_truncate(st, H, P.ApplicationMethod.DIRECT, P.TruncationMethod.SVD,
                                  trunc_args=(P.SVDParameters(max_bond_dim=3, rel_tol=1e-10, total_tol=1e-10),))
     assert max(tight.phys(n).shape[0] for n in ids if n != "s0") <= 3
+
+
+def test_gpu_recorded_run_matches_reference():
+    """run(evaluation_time=2) with every record flag on the GB300 against the
+    reference's Results (operators, bond dimensions, norm, Loschmidt amplitude)."""
+    from golden_util import run_recorded_case
+    res, ref = run_recorded_case()
+    for name, arr in ref.items():
+        key = tuple(name.split("/")[1:]) if name.startswith("bond/") else name
+        got = res.operator_result(key) if key != "times" else res.times()
+        assert np.max(np.abs(got - arr)) < 1e-9 * max(1.0, np.max(np.abs(arr))), name

@@ -21,7 +21,9 @@ class SVDParameters:
     Keep s > max(rel_tol * s_0, total_tol) (or, with ``sum_trunc``, drop the
     tail whose squared sum is below total_tol^2), at most ``max_bond_dim``
     values and at least one; ``renorm`` rescales the kept values to the 2-norm
-    of all of them. ``random`` (randomised SVD) is not provided by the engine."""
+    of all of them. With ``random`` the reference factors by a randomised SVD
+    and keeps exactly ``max_bond_dim`` values; the engine keeps the same number
+    of exact leading values."""
     max_bond_dim: int = 100
     rel_tol: float = 1e-15
     total_tol: float = 1e-15
@@ -43,8 +45,8 @@ class SVDParameters:
             raise ValueError("'rel_tol' has to be positive or -inf.")
         if self.total_tol < 0 and self.total_tol != float("-inf"):
             raise ValueError("'total_tol' has to be positive or -inf.")
-        if self.random:
-            raise NotImplementedError("randomised SVD is not provided by the GPU engine")
+        if self.random and self.max_bond_dim == float("inf"):
+            raise ValueError("a randomised SVD needs a finite 'max_bond_dim' (its rank)")
 
 
 def renormalise_singular_values(s: np.ndarray, new_s: np.ndarray) -> np.ndarray:
@@ -71,6 +73,13 @@ def truncate_singular_values(s: np.ndarray, svd_params) -> tuple[np.ndarray, np.
     s = np.asarray(s, dtype=float)
     if len(s) == 0:
         raise ValueError("No singular values to truncate!")
+    if getattr(svd_params, "random", False):
+        # ``truncated_tensor_svd`` with ``random`` keeps the max_bond_dim leading
+        # values of its randomised factorisation and applies no tolerance
+        # (``util/tensor_splitting.py:488-527``); the engine factors exactly and
+        # keeps the same number
+        k = min(int(svd_params.max_bond_dim), len(s))
+        return s[:k].copy(), s[k:]
     if getattr(svd_params, "sum_trunc", False):
         s_temp = s[:_sum_truncation_index(s, svd_params.total_tol, getattr(svd_params, "sum_renorm", False))]
     else:

@@ -172,6 +172,12 @@ def test_svd_parameters_validation():
             warnings.simplefilter("ignore")
             new_s, _ = P.truncate_singular_values(d[f"svd/{i}/s"], p)
         np.testing.assert_allclose(new_s, d[f"svd/{i}/out"], rtol=1e-15, atol=0)
+    # random=True: the reference keeps exactly max_bond_dim values, no tolerance
+    s = np.array([3.0, 1.0, 1e-12, 1e-14])
+    kept, cut = P.truncate_singular_values(s, P.SVDParameters(max_bond_dim=3, rel_tol=1e-3, random=True))
+    assert list(kept) == [3.0, 1.0, 1e-12] and list(cut) == [1e-14]
+    with pytest.raises(ValueError):
+        P.SVDParameters(random=True, max_bond_dim=float("inf"))
 
 
 def _two_site_vs_oracle(chi, max_bond_dim, steps=2):

@@ -29,6 +29,7 @@ __all__ = [
     "two_site_heff_apply", "two_site_split", "SecondOrderTwoSiteTDVPOracle",
     "FirstOrderTwoSiteTDVPOracle", "tebd_apply_gate", "TEBDOracle", "ttno_expectation",
     "fixed_bug_step", "adaptive_bug_step", "svd_truncation", "leaf_to_leaf_path", "dense_exp_action",
+    "zipup_apply",
 ]
 
 
@@ -781,6 +782,41 @@ def fixed_bug_step(state: OState, W: dict, dt: float, krylov_tol=1e-10, default_
                                   krylov_tol=krylov_tol)
     out = OState(tree, new)
     out.orth_center = root
+    return out
+
+
+# ----------------------------------------------------------------------------
+# zip-up application of a TTNO
+# ----------------------------------------------------------------------------
+def zipup_apply(state: OState, W: dict, params: SVDParams) -> OState:
+    """Non-canonical zip-up (``ttns/ttns_ttno/zipup.py:55-105,191-253``): from
+    the leaves up, each node's state tensor, its TTNO tensor and the blocks of
+    its children are contracted and split by a truncated SVD, the node keeping
+    U (new bond toward the parent) and the parent receiving S V^H with legs
+    (state bond, operator bond, new bond); the root keeps everything."""
+    tree = state.tree
+    order = _postorder(tree, tree.root)
+    cache, new = {}, {}
+    for v in order:
+        nb = tree.neighbours(v)
+        n = len(nb)
+        T = np.tensordot(state.tensors[v], W[v], axes=([n], [n + 1]))
+        legs = [("a", k) for k in range(n)] + [("b", k) for k in range(n)] + ["t"]
+        kids = [k for k, x in enumerate(nb) if x != tree.parent[v]]
+        for k in kids:
+            T = np.tensordot(T, cache.pop(nb[k]), axes=([legs.index(("a", k)), legs.index(("b", k))], [0, 1]))
+            legs = [l for l in legs if l not in (("a", k), ("b", k))] + [("n", k)]
+        if tree.parent[v] is None:
+            new[v] = np.transpose(T, [legs.index(("n", k)) for k in kids] + [legs.index("t")])
+            continue
+        order_legs = [("n", k) for k in kids] + ["t", ("a", 0), ("b", 0)]
+        T = np.transpose(T, [legs.index(l) for l in order_legs])
+        rows, cp, wp = T.shape[:-2], T.shape[-2], T.shape[-1]
+        u, sv, vh = np.linalg.svd(T.reshape(-1, cp * wp), full_matrices=False)
+        r, new_s = truncate_singular_values(sv, params)
+        new[v] = np.moveaxis(u[:, :r].reshape(rows + (r,)), -1, 0)
+        cache[v] = np.transpose((new_s[:, None] * vh[:r]).reshape(r, cp, wp), (1, 2, 0))
+    out = OState(tree, new)
     return out
 
 

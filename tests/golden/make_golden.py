@@ -727,6 +727,32 @@ def run_results_case(ptn):
     print("results written", keys)
 
 
+def zipup_cases(ptn):
+    """The reference's non-canonical zip-up application of a TTNO
+    (``ttns/ttns_ttno/zipup.py:22-105``) with a bond cap that binds and with
+    tolerances only."""
+    from pytreenet.ttns.ttns_ttno.zipup import zipup
+    rng = np.random.default_rng(101)
+    spec = binary_tree(7)
+    tensors = capped_state_tensors(spec, rng, 3)
+    psi = build_reference_state(ptn, spec, tensors)
+    H = ptn.TTNO.from_hamiltonian(tfim(ptn, spec, g=0.6), psi)
+    rec = {"spec_ids": np.array([s[0] for s in spec]),
+           "spec_parents": np.array(["" if s[1] is None else s[1] for s in spec])}
+    for nid, t in tensors.items():
+        rec[f"init/{nid}"] = t
+    for nid, t in export_ttno(H, spec).items():
+        rec[f"ttno/{nid}"] = t
+    for tag, (maxd, tol) in {"cap": (4, 1e-10), "tol": (100, 1e-12)}.items():
+        out = zipup(H, build_reference_state(ptn, spec, tensors),
+                    svd_params=ptn.SVDParameters(max_bond_dim=maxd, rel_tol=tol, total_tol=tol))
+        rec[f"{tag}/params"] = np.array([maxd, tol])
+        for nid, t in export_state(out, spec).items():
+            rec[f"{tag}/final/{nid}"] = t
+    np.savez_compressed(os.path.join(HERE, "binary7_tfim_zipup.npz"), **rec)
+    print("zipup written")
+
+
 def time_dep_cases(ptn):
     rng = np.random.default_rng(77)
     spec = binary_tree(7)
@@ -791,6 +817,7 @@ def main(ref_root):
     heff_cases(ptn)
     exact_cases(ptn)
     run_results_case(ptn)
+    zipup_cases(ptn)
 
 
 if __name__ == "__main__":

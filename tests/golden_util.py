@@ -283,3 +283,26 @@ def run_recorded_case(precision="plain"):
     algo.run(evaluation_time=2)
     ref = {str(k): d["res/" + str(k)] for k in d["res_keys"]}
     return algo.results, ref
+
+
+def check_zipup_fixture(tag, tol=1e-12):
+    """The engine's zip-up against the reference's on ``binary7_tfim_zipup``."""
+    import numpy as np
+    import oracle as O
+    import pytreenet_gb300 as P
+    d = np.load(os.path.join(GOLDEN, "binary7_tfim_zipup.npz"))
+    ids = [str(x) for x in d["spec_ids"]]
+    spec = list(zip(ids, [str(x) or None for x in d["spec_parents"]]))
+    st = build_ttn(P.TTNS, spec, {i: d[f"init/{i}"] for i in ids})
+    H = build_ttn(P.TTNO, spec, {i: d[f"ttno/{i}"] for i in ids})
+    maxd, t = d[f"{tag}/params"]
+    out = P.apply_ttno_to_ttns(st, H, P.ApplicationMethod.ZIPUP,
+                               P.SVDParameters(max_bond_dim=int(maxd), rel_tol=t, total_tol=t))
+    tree = O.OTree()
+    for nid, p in spec:
+        tree.add_root(nid) if p is None else tree.add_child(nid, p)
+    for i in ids:
+        assert tuple(out.phys(i).shape) == d[f"{tag}/final/{i}"].shape, i
+    a = O.state_vector(O.OState(tree, {i: out.get_phys_numpy(i) for i in ids}), ids)
+    b = O.state_vector(O.OState(tree, {i: d[f"{tag}/final/{i}"] for i in ids}), ids)
+    assert np.max(np.abs(a - b)) < tol * np.max(np.abs(b))

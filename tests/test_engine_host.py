@@ -773,3 +773,10 @@ def test_run_results_match_reference(monkeypatch):
         assert np.max(np.abs(got - arr)) < 1e-9 * max(1.0, np.max(np.abs(arr))), name
     assert set(res.get_results().keys()) == {tuple(n.split("/")[1:]) if n.startswith("bond/") else n
                                               for n in ref if n != "times"}
+
+
+@pytest.mark.parametrize("tag", ["cap", "tol"])
+def test_engine_zipup_matches_reference(monkeypatch, tag):
+    fake_ptn.install(monkeypatch)
+    from golden_util import check_zipup_fixture
+    check_zipup_fixture(tag)

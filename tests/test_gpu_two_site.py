@@ -322,3 +322,10 @@ def test_gpu_recorded_run_matches_reference():
         key = tuple(name.split("/")[1:]) if name.startswith("bond/") else name
         got = res.operator_result(key) if key != "times" else res.times()
         assert np.max(np.abs(got - arr)) < 1e-9 * max(1.0, np.max(np.abs(arr))), name
+
+
+@pytest.mark.parametrize("tag", ["cap", "tol"])
+def test_gpu_zipup_matches_reference(tag):
+    """Zip-up TTNO application on the GB300 against the reference's zipup."""
+    from golden_util import check_zipup_fixture
+    check_zipup_fixture(tag)

@@ -239,3 +239,22 @@ def test_oracle_default_mode_matches_reference(name):
     one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), algo.state)
     assert zerr < 1e-12
     assert one_minus_f < 1e-13
+
+
+@pytest.mark.parametrize("tag", ["cap", "tol"])
+def test_oracle_zipup_matches_reference(tag):
+    """Non-canonical zip-up: the oracle against the reference's zipup."""
+    d = np.load(f"{GOLDEN}/binary7_tfim_zipup.npz")
+    ids = [str(x) for x in d["spec_ids"]]
+    spec = list(zip(ids, [str(x) or None for x in d["spec_parents"]]))
+    tree = O.OTree()
+    for nid, p in spec:
+        tree.add_root(nid) if p is None else tree.add_child(nid, p)
+    maxd, tol = d[f"{tag}/params"]
+    out = O.zipup_apply(O.OState(tree, {i: d[f"init/{i}"] for i in ids}), {i: d[f"ttno/{i}"] for i in ids},
+                        O.SVDParams(max_bond_dim=int(maxd), rel_tol=tol, total_tol=tol))
+    ref = O.OState(tree, {i: d[f"{tag}/final/{i}"] for i in ids})
+    for i in ids:
+        assert out.tensors[i].shape == ref.tensors[i].shape, i
+    a, b = O.state_vector(out, ids), O.state_vector(ref, ids)
+    assert np.max(np.abs(a - b)) < 1e-12 * np.max(np.abs(b))

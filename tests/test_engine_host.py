@@ -728,7 +728,7 @@ def test_direct_ttno_application(monkeypatch):
     st2.apply_operator(P.TensorProduct({"s2": X, "s5": Zm}))
     assert np.max(np.abs(st2.to_dense(ids) - dense({"s2": X, "s5": Zm}) @ psi)) < 1e-12
     with pytest.raises(NotImplementedError):
-        P.apply_ttno_to_ttns(st, H, method=P.ApplicationMethod.ZIPUP)
+        P.apply_ttno_to_ttns(st, H, method=P.ApplicationMethod.VARIATIONAL)
 
 
 def test_apply_and_truncate_matches_oracle(monkeypatch):

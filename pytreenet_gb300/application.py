@@ -22,7 +22,8 @@ from .ttn import Node, TreeTensorNetworkState
 
 
 class ApplicationMethod(Enum):
-    """``ttns_ttno/application.py:23-98`` (DIRECT and ZIPUP run)."""
+    """``ttns_ttno/application.py:23-98`` (DIRECT, ZIPUP, DIRECT_TRUNCATE and
+    DIRECT_TRUNCATE_RANDOM run)."""
     DIRECT = "direct"
     DENSITY_MATRIX = "density_matrix"
     HALF_DENSITY_MATRIX = "half_density_matrix"
@@ -48,8 +49,21 @@ def apply_ttno_to_ttns(ttns: TreeTensorNetworkState, ttno, method: ApplicationMe
     DIRECT, or ZIPUP with ``svd_params`` (positional or keyword)."""
     if method is ApplicationMethod.ZIPUP:
         return zipup(ttno, ttns, *args, device=device, **kwargs)
+    if method in (ApplicationMethod.DIRECT_TRUNCATE, ApplicationMethod.DIRECT_TRUNCATE_RANDOM):
+        # ``application.py:67-85``: DIRECT followed by the SVD truncation; the
+        # random variant sets ``params.random`` (the engine's rank rule for it)
+        from .svd_truncation import TruncationMethod, apply_and_truncate
+        if method is ApplicationMethod.DIRECT_TRUNCATE_RANDOM:
+            from .truncation import SVDParameters
+            kwargs = dict(kwargs)
+            params = kwargs.get("params", SVDParameters())
+            params.random = True
+            kwargs["params"] = params
+        return apply_and_truncate(ttns, ttno, ApplicationMethod.DIRECT, TruncationMethod.SVD,
+                                  trunc_args=args, trunc_kwargs=kwargs)
     if method is not ApplicationMethod.DIRECT:
-        raise NotImplementedError(f"TTNO application method {method} is not provided (DIRECT, ZIPUP)")
+        raise NotImplementedError(f"TTNO application method {method} is not provided "
+                                  "(DIRECT, ZIPUP, DIRECT_TRUNCATE, DIRECT_TRUNCATE_RANDOM)")
     if not torch.cuda.is_available():
         raise RuntimeError("pytreenet_gb300 needs a CUDA device (no CPU fallback)")
     dev = torch.device(device or E.DEFAULT_DEVICE)

@@ -780,3 +780,21 @@ def test_engine_zipup_matches_reference(monkeypatch, tag):
     fake_ptn.install(monkeypatch)
     from golden_util import check_zipup_fixture
     check_zipup_fixture(tag)
+
+
+def test_direct_truncate_methods(monkeypatch):
+    """DIRECT_TRUNCATE = DIRECT + SVD truncation; the random variant keeps
+    exactly max_bond_dim values per bond (when the bond allows)."""
+    fake_ptn.install(monkeypatch)
+    import pytreenet_gb300 as P
+    from pytreenet_gb300.workloads import binary_tfim_random_state
+    st, spec, tens, _, _ = binary_tfim_random_state(n=7, chi=2, seed=4)
+    ids = [n for n, _ in spec]
+    H = P.TTNO.from_hamiltonian(_symbolic_tfim(spec, 1.0, 0.7), st)
+    ref = P.apply_ttno_to_ttns(st, H).to_dense(ids)
+    a = P.apply_ttno_to_ttns(st, H, P.ApplicationMethod.DIRECT_TRUNCATE,
+                             P.SVDParameters(max_bond_dim=100, rel_tol=1e-13, total_tol=1e-13))
+    assert np.max(np.abs(a.to_dense(ids) - ref)) < 1e-11 * np.max(np.abs(ref))
+    b = P.apply_ttno_to_ttns(st, H, P.ApplicationMethod.DIRECT_TRUNCATE_RANDOM,
+                             params=P.SVDParameters(max_bond_dim=2))
+    assert all(b.phys(n).shape[0] == 2 for n in ids if n != "s0")

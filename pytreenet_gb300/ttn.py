@@ -374,6 +374,33 @@ class TreeTensorNetworkState(TreeTensorNetwork):
             return self.scalar_product()
         return self._device().expect_local(dict(operator))
 
+    def multi_single_site_expectation_value(self, operators, move_orth: bool = False) -> dict:
+        """node -> [<psi|O|psi> for each one-site operator on that node]
+        (``ttns/ttns_util.py:25-175``): a TensorProduct is split into its
+        one-site factors, a list groups single-site TensorProducts by node, a
+        dict maps node -> TensorProduct or list of them. One device network
+        serves all the contractions."""
+        from .tdvp import TensorProduct
+
+        def single(op):
+            if len(op) != 1:
+                raise ValueError("every operator must act on exactly one site")
+            return op
+        if isinstance(operators, TensorProduct):
+            prepared = {n: [TensorProduct({n: o})] for n, o in operators.items()}
+        elif isinstance(operators, list):
+            prepared = {}
+            for op in operators:
+                n = next(iter(single(op)))
+                prepared.setdefault(n, []).append(op)
+        elif isinstance(operators, dict):
+            prepared = {n: ([single(o) for o in op] if isinstance(op, list) else [single(op)])
+                        for n, op in operators.items()}
+        else:
+            raise TypeError("Invalid input type of operators!")
+        net = self._device()
+        return {n: [net.expect_local(dict(op)) for op in ops] for n, ops in prepared.items()}
+
     def ttno_expectation_value(self, operator) -> complex:
         return self._device().expect_ttno(operator)
 

@@ -798,3 +798,24 @@ def test_direct_truncate_methods(monkeypatch):
     b = P.apply_ttno_to_ttns(st, H, P.ApplicationMethod.DIRECT_TRUNCATE_RANDOM,
                              params=P.SVDParameters(max_bond_dim=2))
     assert all(b.phys(n).shape[0] == 2 for n in ids if n != "s0")
+
+
+def test_multi_single_site_expectation_value(monkeypatch):
+    """TTNS.multi_single_site_expectation_value in its three input forms against
+    the reference's values on its saved state."""
+    import os
+    import pytreenet_gb300 as P
+    from golden_util import GOLDEN
+    fake_ptn.install(monkeypatch)
+    st = P.TTNS.load(os.path.join(GOLDEN, "saved_ttns"))
+    vals = np.load(os.path.join(GOLDEN, "saved_ttns_values.npz"))
+    ids = [str(x) for x in vals["ids"]]
+    z = dict(zip(ids, vals["z"]))
+    out = st.multi_single_site_expectation_value(P.TensorProduct({n: Zm for n in ids}))
+    assert all(abs(out[n][0] - z[n]) < 1e-12 for n in ids)
+    out = st.multi_single_site_expectation_value([P.TensorProduct({"s1": Zm}), P.TensorProduct({"s1": 2 * Zm})])
+    assert abs(out["s1"][0] - z["s1"]) < 1e-12 and abs(out["s1"][1] - 2 * z["s1"]) < 1e-12
+    out = st.multi_single_site_expectation_value({"s4": [P.TensorProduct({"s4": Zm})], "s5": P.TensorProduct({"s5": Zm})})
+    assert abs(out["s4"][0] - z["s4"]) < 1e-12 and abs(out["s5"][0] - z["s5"]) < 1e-12
+    with pytest.raises(TypeError):
+        st.multi_single_site_expectation_value(3)

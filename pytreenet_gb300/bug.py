@@ -113,19 +113,35 @@ class FixedBUG(RunLoop):
         self.hamiltonian = hamiltonian
         initial_state._finalise()
         self._loschmidt_state = _tensor_copy(initial_state) if getattr(self.config, "record_loschmidt_amplitude", False) else None
-        self.state = initial_state.copy_structure()
-        self.net = DeviceNetwork(self.state, hamiltonian)
-        root = self.state.root_id
-        if self.state.orthogonality_center_id is None:
-            self.net.canonical_form(root)
-        else:
-            self.net.move_orth_center(root)
-        self.root = root
+        self._initial_state = initial_state.copy_structure()
+        self._setup_state()
+        root = self.root
         self.nbrs = {nid: list(self.net.nbrs(nid)) for nid in self.state._order}
         self.children = {nid: list(self.state.nodes[nid].phys_children) for nid in self.state._order}
         self.parent = {nid: self.state.nodes[nid].parent for nid in self.state._order}
         self.results = None
         self.times = []
+
+    def _setup_state(self):
+        self.state = self._initial_state.copy_structure()
+        self.net = DeviceNetwork(self.state, self.hamiltonian)
+        self.root = self.state.root_id
+        if self.state.orthogonality_center_id is None:
+            self.net.canonical_form(self.root)
+        else:
+            self.net.move_orth_center(self.root)
+        self.results = None
+        self.times = []
+
+    @property
+    def initial_state(self):
+        return self._initial_state
+
+    def reset_to_initial_state(self):
+        """``TimeEvolution.reset_to_initial_state``."""
+        if getattr(self.config, "time_dep", False):
+            self.hamiltonian.reset()
+        self._setup_state()
 
     # -- local pieces --------------------------------------------------------------
     def _ax(self, u, v):

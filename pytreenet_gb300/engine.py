@@ -632,7 +632,10 @@ class DeviceNetwork:
         for nid in state._order:
             t = state._phys[nid]
             if isinstance(t, np.ndarray):
-                t = torch.from_numpy(np.ascontiguousarray(t, dtype=np.complex128))
+                host = t
+                t = torch.from_numpy(np.ascontiguousarray(t, dtype=np.complex128)).to(self.device, CDT)
+                if t.device.type == "cpu" and np.shares_memory(t.numpy(), host):
+                    t = t.clone()            # never evolve the caller's arrays in place
             t = t.to(self.device, CDT).contiguous()
             self.t[nid] = t
             state._phys[nid] = t

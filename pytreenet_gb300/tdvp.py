@@ -266,12 +266,19 @@ class OneSiteTDVP(RunLoop):
         initial_state._finalise()
         self._loschmidt_state = _tensor_copy(initial_state) if self.config.record_loschmidt_amplitude else None
         self._initial_state = initial_state.copy_structure()
-        self.state = initial_state.copy_structure()
         self.update_path = find_update_path(self._initial_state, self.config.main_path_mode)
-        self.orthogonalization_path = [self.state.path_from_to(self.update_path[i], self.update_path[i + 1])[1:]
+        self.orthogonalization_path = [self._initial_state.path_from_to(self.update_path[i],
+                                                                        self.update_path[i + 1])[1:]
                                        for i in range(len(self.update_path) - 1)]
         self.precision = precision
-        self.net = DeviceNetwork(self.state, hamiltonian, precision=precision)
+        self._setup_state()
+
+    def _setup_state(self):
+        """The working state from the initial one: a device copy in canonical
+        form at the first site of the update path, environments toward it
+        (``tdvp_algorithm.py:58-163``)."""
+        self.state = self._initial_state.copy_structure()
+        self.net = DeviceNetwork(self.state, self.hamiltonian, precision=self.precision)
         if self.state.orthogonality_center_id is None:
             self.net.canonical_form(self.update_path[0])
         else:
@@ -279,6 +286,19 @@ class OneSiteTDVP(RunLoop):
         self.net.init_cache_but_one(self.update_path[0])
         self.results = None
         self.times = []
+
+    @property
+    def initial_state(self):
+        return self._initial_state
+
+    def reset_to_initial_state(self):
+        """``TimeEvolution.reset_to_initial_state`` (``time_evolution.py:370-390``):
+        the state back to the initial one, results cleared, a time-dependent
+        Hamiltonian reset. The initial tensors must not have been modified
+        (the engine evolves device copies)."""
+        if self.config.time_dep:
+            self.hamiltonian.reset()
+        self._setup_state()
 
     # -- Krylov options ------------------------------------------------------------
     def _kry(self):
@@ -408,10 +428,14 @@ class TwoSiteTDVP(OneSiteTDVP):
             raise ValueError("Two-site TDVP cannot be used for systems with less than 2 sites!")
         if not hasattr(self.config, "max_bond_dim"):
             raise TypeError("two-site TDVP needs a TwoSiteTDVPConfig (truncation parameters)")
+        self.bond_dims_history: list[int] = []
+
+    def _setup_state(self):
+        super()._setup_state()
         # bond dimensions change from step to step, so captured QR launch
         # sequences would mostly be captured once and dropped: launch eagerly
         self.net.use_graphs = False
-        self.bond_dims_history: list[int] = []
+        self.bond_dims_history = []
 
     def _update_two_site_nodes(self, target_node_id, next_node_id, time_step_factor=1.0):
         """``_update_two_site_nodes`` (``twositetdvp.py:89-125``)."""

@@ -166,6 +166,15 @@ class TEBD(RunLoop):
         self.results = None
         self.times = []
 
+    def reset_to_initial_state(self):
+        """``TimeEvolution.reset_to_initial_state``: a fresh device copy of the
+        initial state, results cleared."""
+        self.state = self.initial_state.copy_structure()
+        self.state.orthogonality_center_id = None
+        self.net = DeviceNetwork(self.state, None, precision=self.net.precision)
+        self.results = None
+        self.times = []
+
     @property
     def exponents(self) -> list:
         return self._exponents

@@ -819,3 +819,42 @@ def test_multi_single_site_expectation_value(monkeypatch):
     assert abs(out["s4"][0] - z["s4"]) < 1e-12 and abs(out["s5"][0] - z["s5"]) < 1e-12
     with pytest.raises(TypeError):
         st.multi_single_site_expectation_value(3)
+
+
+def test_reset_to_initial_state(monkeypatch):
+    """reset_to_initial_state: the same evolution twice gives the same results."""
+    fake_ptn.install(monkeypatch)
+    import pytreenet_gb300 as P
+    c = load_case("ttree3_heis_chi6_o1")
+    st = build_ttn(P.TTNS, c["spec"], {k: v.copy() for k, v in c["init"].items()})
+    H = build_ttn(P.TTNO, c["spec"], c["ttno"])
+    ops = {"z": P.TensorProduct({c["spec"][0][0]: Zm})}
+    algo = P.FirstOrderOneSiteTDVP(st, H, c["dt"], c["dt"] * 2, ops,
+                                   config=P.TDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV),
+                                   solver_options={"krylov_tol": 1e-12})
+    first = algo.run()
+    algo.reset_to_initial_state()
+    assert algo.results is None
+    second = algo.run()
+    assert np.max(np.abs(first - second)) < 1e-13
+
+
+def test_reset_bug_and_tebd(monkeypatch):
+    """reset_to_initial_state for BUG and TEBD repeats the run exactly."""
+    fake_ptn.install(monkeypatch)
+    import pytreenet_gb300 as P
+    from golden_util import FixedSplitting
+    c = load_case("binary15_tfim_fixed_bug")
+    st = build_ttn(P.TTNS, c["spec"], c["init"])
+    H = build_ttn(P.TTNO, c["spec"], c["ttno"])
+    ops = {"z": P.TensorProduct({"s0": Zm})}
+    algo = P.FixedBUG(st, H, c["dt"], c["dt"] * 2, ops, config=P.FixedBUGConfig(time_evo_mode=P.TimeEvoMode.KRYLOV))
+    a = algo.run()
+    algo.reset_to_initial_state()
+    assert np.max(np.abs(algo.run() - a)) < 1e-13
+    t = load_case("binary7_tfim_tebd")
+    st = build_ttn(P.TTNS, t["spec"], t["init"])
+    tebd = P.TEBD(st, FixedSplitting(t["gates"]), t["dt"], t["dt"] * 2, ops, svd_parameters=P.SVDParameters(**t["svd"]))
+    a = tebd.run()
+    tebd.reset_to_initial_state()
+    assert np.max(np.abs(tebd.run() - a)) < 1e-13

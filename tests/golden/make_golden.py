@@ -242,7 +242,8 @@ def neel_state_tensors(spec):
     return out
 
 
-def run_case_two_site(ptn, name, spec, tensors, ham_fn, dt, steps, tol, svd, canonical_random=False):
+def run_case_two_site(ptn, name, spec, tensors, ham_fn, dt, steps, tol, svd, canonical_random=False,
+                      path_mode=None):
     """Second-order two-site TDVP (``secondordertwosite.py``) with truncation ``svd``
     = (max_bond_dim, rel_tol, total_tol, renorm)."""
     from pytreenet.time_evolution.time_evolution import TimeEvoMode
@@ -257,8 +258,12 @@ def run_case_two_site(ptn, name, spec, tensors, ham_fn, dt, steps, tol, svd, can
     H = ptn.TTNO.from_hamiltonian(ham_fn(psi), psi)
     ops = {nid: ptn.TensorProduct({nid: Z}) for nid, _ in spec}
     maxd, rel, tot, renorm = svd
+    extra = {}
+    if path_mode is not None:
+        from pytreenet.time_evolution.time_evo_util import PathFinderMode
+        extra["main_path_mode"] = PathFinderMode[path_mode]
     cfg = TwoSiteTDVPConfig(time_evo_mode=TimeEvoMode.KRYLOV, max_bond_dim=maxd, rel_tol=rel,
-                            total_tol=tot, renorm=renorm)
+                            total_tol=tot, renorm=renorm, **extra)
     algo = SecondOrderTwoSiteTDVP(psi, H, dt, dt * steps, ops, config=cfg,
                                   solver_options={"krylov_tol": tol})
     rec = {"spec_ids": np.array([s[0] for s in spec]),
@@ -266,6 +271,8 @@ def run_case_two_site(ptn, name, spec, tensors, ham_fn, dt, steps, tol, svd, can
            "dt": dt, "steps": steps, "order": 2, "krylov_tol": tol,
            "two_site": 1, "svd_max_bond_dim": maxd, "svd_rel_tol": rel, "svd_total_tol": tot,
            "svd_renorm": int(renorm), "update_path": np.array(algo.update_path)}
+    if path_mode is not None:
+        rec["path_mode"] = path_mode
     for nid, t in tensors.items():
         rec[f"init/{nid}"] = t
     for nid, t in export_ttno(H, spec).items():
@@ -605,6 +612,17 @@ def bug_cases(ptn):
                           0.05, 3, 1e-12, (100, 1e-10, 1e-10))
 
 
+def leaf_to_leaf_two_site_cases(ptn):
+    """Second-order two-site TDVP on the leaf-to-leaf path, bonds growing
+    from a Neel state."""
+    rng = np.random.default_rng(107)
+    spec = binary_tree(7)
+    h = rng.uniform(-1, 1, size=len(spec))
+    run_case_two_site(ptn, "binary7_heis_2tdvp_l2l", spec, neel_state_tensors(spec),
+                      lambda psi: heisenberg_fields(ptn, spec, h), 0.05, 3, 1e-12, (6, 1e-10, 1e-10, False),
+                      path_mode="LeafToLeaf")
+
+
 def leaf_to_leaf_cases(ptn):
     """One-site TDVP on the leaf-to-leaf update path
     (``PathFinderMode.LeafToLeaf``, ``update_path.py:255-396``)."""
@@ -818,6 +836,7 @@ def main(ref_root):
     exact_cases(ptn)
     run_results_case(ptn)
     zipup_cases(ptn)
+    leaf_to_leaf_two_site_cases(ptn)
 
 
 if __name__ == "__main__":

@@ -42,7 +42,7 @@ def load_case(name):
 
 CASES = ["c1_binary15_tfim_chi8", "binary7_tfim_chi4_o2", "ttree3_heis_chi6_o1",
          "ttree3_heis_chi6_o2", "ternary2_xxz_chi4_o1"]
-TWO_SITE_CASES = ["ternary2_xxz_neel_2tdvp", "binary7_heis_2tdvp_trunc"]
+TWO_SITE_CASES = ["ternary2_xxz_neel_2tdvp", "binary7_heis_2tdvp_trunc", "binary7_heis_2tdvp_l2l"]
 TEBD_CASES = ["binary7_tfim_tebd", "binary7_tfim_tebd_swaps"]
 DRIVEN_CASES = ["binary7_tfim_driven_o1", "binary7_tfim_driven_o2"]
 BUG_CASES = ["binary15_tfim_fixed_bug", "ternary2_xxz_fixed_bug"]

@@ -109,7 +109,8 @@ def _run_two_site(name, precision="plain", order=2, dt=None, steps=None):
     c = load_case(name)
     st = build_ttn(P.TTNS, c["spec"], c["init"])
     H = build_ttn(P.TTNO, c["spec"], c["ttno"])
-    cfg = P.TwoSiteTDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV, **c["svd"])
+    cfg = P.TwoSiteTDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV, main_path_mode=P.PathFinderMode[c["path_mode"]],
+                              **c["svd"])
     cls = P.SecondOrderTwoSiteTDVP if order == 2 else P.FirstOrderTwoSiteTDVP
     dt = c["dt"] if dt is None else dt
     algo = cls(st, H, dt, dt * c["steps"], {}, config=cfg,

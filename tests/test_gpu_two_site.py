@@ -97,7 +97,8 @@ def _run_two_site(name, precision="plain"):
     c = load_case(name)
     st = build_ttn(P.TTNS, c["spec"], c["init"])
     H = build_ttn(P.TTNO, c["spec"], c["ttno"])
-    cfg = P.TwoSiteTDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV, **c["svd"])
+    cfg = P.TwoSiteTDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV, main_path_mode=P.PathFinderMode[c["path_mode"]],
+                              **c["svd"])
     algo = P.SecondOrderTwoSiteTDVP(st, H, c["dt"], c["dt"] * c["steps"], {}, config=cfg,
                                     solver_options={"krylov_tol": c["krylov_tol"]}, precision=precision)
     zs = []

@@ -24,16 +24,15 @@ from __future__ import annotations
 from dataclasses import dataclass
 from typing import Any
 
-import numpy as np
-import torch
-
 import ctypes
+
+import torch
 
 from . import _lib
 from . import engine as E
 from .adjoint import (_SiteOp, _raw_contract, _solver, _tensor_apply, absorb, env_apply, qr_keep_raw)
 from .engine import CDT, DeviceNetwork, check
-from .tdvp import (TTNTimeEvolutionConfig, TensorProduct, TimeEvoMode, _tensor_copy, check_time_evo_mode,
+from .tdvp import (TTNTimeEvolutionConfig, TimeEvoMode, _tensor_copy, check_time_evo_mode,
                    compute_num_time_steps)
 from .results import RunLoop, init_operators
 from .svd_truncation import TreeOps, move_center, qr_split, truncate_tensors

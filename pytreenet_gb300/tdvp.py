@@ -8,8 +8,7 @@ config=None, solver_options=None)``, ``run_one_time_step()``, ``run()``,
 """
 from __future__ import annotations
 
-import copy
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 from enum import Enum
 from typing import Any
 

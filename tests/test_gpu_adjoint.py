@@ -56,3 +56,33 @@ def test_gpu_tdvp_gradient_matches_oracle_and_fd():
                    for j in range(theta.size)])
     assert np.linalg.norm(grad) > 1e-4
     assert np.linalg.norm(grad - fd) < 1e-6 * np.linalg.norm(grad)
+
+
+def test_gpu_second_order_tdvp_gradient_matches_oracle():
+    """The second-order adjoint on the GB300 against torch autograd through the
+    oracle's dense second-order sweep."""
+    import oracle as O
+    import oracle.adjoint_oracle as AO
+    from pytreenet_gb300.adjoint import OneSiteTDVPAdjoint
+    from pytreenet_gb300.workloads import binary_tfim_random_state
+    from pytreenet_gb300.operators import tfim_ttno
+    st, spec, tensors, g, J = binary_tfim_random_state(n=7, chi=4, seed=6)
+    H = tfim_ttno(st, J=J, g=g)
+    dt, steps = 0.1, 3
+    ops = {"s0": np.diag([1.0, -1.0]).astype(complex)}
+    adj = OneSiteTDVPAdjoint(st, H, dt, steps, krylov_tol=1e-14, second_order=True)
+    val, gW, gA = adj.expectation_and_gradient(ops, wrt_state=True)
+    tree = O.OTree()
+    for nid, p in spec:
+        tree.add_root(nid) if p is None else tree.add_child(nid, p)
+    otd = AO.SecondOrderOneSiteTDVPTorch(O.OState(tree, {k: v.copy() for k, v in tensors.items()}), dt)
+    A0 = {k: adj.A0[k].cpu().clone().requires_grad_(True) for k in adj.order}
+    W0 = {k: adj.W0[k].cpu().clone().requires_grad_(True) for k in adj.order}
+    ov = otd.expectation(A0, W0, steps, ops).real
+    ref = torch.autograd.grad(ov, [A0[k] for k in adj.order] + [W0[k] for k in adj.order])
+    assert abs(val - float(ov.detach())) < 1e-11
+    n = len(adj.order)
+    for k, r in zip(adj.order, ref[:n]):
+        assert torch.allclose(gA[k].cpu(), r, atol=1e-9), k
+    for k, r in zip(adj.order, ref[n:]):
+        assert torch.allclose(gW[k].cpu(), r, atol=1e-9), k

@@ -20,7 +20,7 @@ from .operators import nearest_neighbour_ttno, tfim_ttno, heisenberg_ttno
 from .hamiltonian import Hamiltonian
 from .exact import ExactTimeEvolution, ExactTimeEvolutionConfig
 from .application import ApplicationMethod, apply_ttno_to_ttns
-from .svd_truncation import TruncationMethod, apply_and_truncate, svd_truncation
+from .svd_truncation import SplitMode, TruncationMethod, apply_and_truncate, svd_truncation
 from .batch import run_realisations
 from .contractions import (SandwichCache, contract_ket_ham_with_envs, contract_any,
                            effective_single_site_evolution, get_effective_single_site_hamiltonian,
@@ -38,7 +38,7 @@ __all__ = [
     "NumericOperator", "SWAPlist", "swap_gate",
     "nearest_neighbour_ttno", "tfim_ttno", "heisenberg_ttno", "run_realisations", "Hamiltonian",
     "ExactTimeEvolution", "ExactTimeEvolutionConfig", "ApplicationMethod", "apply_ttno_to_ttns",
-    "TruncationMethod", "apply_and_truncate", "svd_truncation",
+    "SplitMode", "TruncationMethod", "apply_and_truncate", "svd_truncation",
     "SandwichCache", "contract_ket_ham_with_envs", "contract_any", "effective_single_site_evolution",
     "get_effective_single_site_hamiltonian", "get_effective_single_site_hamiltonian_nodes",
     "OneSiteTDVPAdjoint", "coupling_gradient", "FixedBUG", "FixedBUGConfig", "BUG", "BUGConfig",

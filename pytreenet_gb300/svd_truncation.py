@@ -18,6 +18,14 @@ from .adjoint import absorb, qr_keep_raw
 from .truncation import truncate_singular_values
 
 
+class SplitMode(Enum):
+    """``util/tensor_splitting.py:23-50``: REDUCED shrinks a bond to the row
+    count of a wide split, KEEP keeps it (zero-padded Q); FULL is not provided."""
+    FULL = "full"
+    REDUCED = "reduced"
+    KEEP = "keep"
+
+
 class TruncationMethod(Enum):
     """``core/truncation/truncating.py:14-60`` (SVD and NONE run here)."""
     RECURSIVE = "recursive"

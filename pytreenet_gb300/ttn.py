@@ -374,6 +374,64 @@ class TreeTensorNetworkState(TreeTensorNetwork):
             return self.scalar_product()
         return self._device().expect_local(dict(operator))
 
+    # -- canonical forms on the device (``core/ttn.py:1530-1700``) -------------------
+    def _orthogonalise(self, target: str, mode, full: bool):
+        from .svd_truncation import SplitMode, TreeOps, canonical_form, move_center
+        from .application import _device_tensor
+        from . import engine as E
+        import torch
+        if not torch.cuda.is_available():
+            raise RuntimeError("pytreenet_gb300 needs a CUDA device (no CPU fallback)")
+        name = "REDUCED" if mode is None else getattr(mode, "name", str(mode)).upper()
+        if name == "FULL":
+            raise NotImplementedError("SplitMode.FULL is not provided")
+        mode = SplitMode[name]
+        dev = torch.device(E.DEFAULT_DEVICE)
+        ops = TreeOps(self)
+        with torch.no_grad():
+            A = {n: _device_tensor(self.phys(n), dev) for n in self._order}
+            if full or self.orthogonality_center_id is None:
+                canonical_form(ops, A, target, reduced=mode is SplitMode.REDUCED)
+            else:
+                move_center(ops, A, self.orthogonality_center_id, target, reduced=mode is SplitMode.REDUCED)
+        for n, t in A.items():
+            self._phys[n] = t
+            self.nodes[n].shape = tuple(t.shape)
+        self.orthogonality_center_id = target
+
+    def canonical_form(self, orthogonality_center_id: str, mode=None):
+        """``TreeTensorNetwork.canonical_form``: moves an existing centre, else
+        brings the whole network into canonical form (QR splits, ``mode``
+        SplitMode.REDUCED by default or KEEP)."""
+        self._orthogonalise(orthogonality_center_id, mode, full=False)
+
+    def orthogonalize(self, orthogonality_center_id: str, mode=None):
+        """Canonical form from scratch, whatever the current centre."""
+        self._orthogonalise(orthogonality_center_id, mode, full=True)
+
+    def move_orthogonalization_center(self, new_center_id: str, mode=None):
+        if self.orthogonality_center_id is None:
+            raise AssertionError("The TTN is not in canonical form, so the orth. center cannot be moved!")
+        self._orthogonalise(new_center_id, mode, full=False)
+
+    def ensure_orth_center(self, node_id: str, mode=None) -> bool:
+        was = self.orthogonality_center_id == node_id
+        if not was:
+            self.canonical_form(node_id, mode)
+        return was
+
+    def ensure_root_orth_center(self, mode=None) -> bool:
+        return self.ensure_orth_center(self.root_id, mode)
+
+    def is_in_canonical_form(self, node_id: str | None = None) -> bool:
+        """<psi|psi> equals the squared norm of the centre tensor (``ttns.py:299-327``)."""
+        node_id = self.orthogonality_center_id if node_id is None else node_id
+        if node_id is None:
+            return False
+        t = self.phys(node_id)
+        t = t.detach().cpu().numpy() if not isinstance(t, np.ndarray) else t
+        return bool(np.allclose(self.scalar_product(), np.vdot(t, t)))
+
     def multi_single_site_expectation_value(self, operators, move_orth: bool = False) -> dict:
         """node -> [<psi|O|psi> for each one-site operator on that node]
         (``ttns/ttns_util.py:25-175``): a TensorProduct is split into its

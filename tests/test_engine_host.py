@@ -859,3 +859,26 @@ def test_reset_bug_and_tebd(monkeypatch):
     a = tebd.run()
     tebd.reset_to_initial_state()
     assert np.max(np.abs(tebd.run() - a)) < 1e-13
+
+
+def test_ttns_canonical_form_methods(monkeypatch):
+    """canonical_form / move_orthogonalization_center / is_in_canonical_form on
+    the device: the state is unchanged, the centre carries the norm, REDUCED
+    shrinks wide bonds and KEEP keeps them."""
+    fake_ptn.install(monkeypatch)
+    import pytreenet_gb300 as P
+    c = load_case("binary7_tfim_chi4_o2")            # zero-padded product state, bonds 4
+    ids = [n for n, _ in c["spec"]]
+    st = build_ttn(P.TTNS, c["spec"], {k: v.copy() for k, v in c["init"].items()})
+    v0 = st.to_dense(ids)
+    assert not st.is_in_canonical_form()
+    st.canonical_form("s3", mode=P.SplitMode.KEEP)
+    assert st.orthogonality_center_id == "s3" and st.is_in_canonical_form()
+    assert np.max(np.abs(st.to_dense(ids) - v0)) < 1e-12
+    assert st.phys("s4").shape[0] == 4                  # KEEP: the leaf bond stays 4
+    st.move_orthogonalization_center("s6")
+    assert st.is_in_canonical_form() and np.max(np.abs(st.to_dense(ids) - v0)) < 1e-12
+    st2 = build_ttn(P.TTNS, c["spec"], {k: v.copy() for k, v in c["init"].items()})
+    st2.canonical_form("s0")                            # REDUCED: a leaf bond cannot exceed 2
+    assert st2.phys("s4").shape[0] == 2 and np.max(np.abs(st2.to_dense(ids) - v0)) < 1e-12
+    assert st2.ensure_root_orth_center() is True

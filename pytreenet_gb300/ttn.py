@@ -212,6 +212,35 @@ class TreeTensorNetwork:
     def bond_dim(self, a, b) -> int:
         return self.phys(a).shape[self.phys_axis(a, b)]
 
+    def pad_bond_dimension(self, node1_id: str, node2_id: str, new_bond_dim: int):
+        """Zero-pad the bond between two neighbours to ``new_bond_dim`` (the old
+        entries first), as ``core/ttn.py:792-836`` does with its projectors."""
+        old = self.bond_dim(node1_id, node2_id)
+        if new_bond_dim <= old:
+            return
+        for a, b in ((node1_id, node2_id), (node2_id, node1_id)):
+            t = self.phys(a)
+            ax = self.phys_axis(a, b)
+            shape = list(t.shape)
+            shape[ax] = new_bond_dim
+            idx = tuple(slice(0, old) if i == ax else slice(None) for i in range(len(shape)))
+            if isinstance(t, np.ndarray):
+                out = np.zeros(shape, dtype=t.dtype)
+            else:
+                import torch
+                out = torch.zeros(shape, dtype=t.dtype, device=t.device)
+            out[idx] = t
+            self._phys[a] = out
+            self.nodes[a].shape = tuple(shape)
+
+    def pad_bond_dimensions(self, new_bond_dim: int):
+        """Every bond smaller than ``new_bond_dim`` padded to it (``core/ttn.py:838-863``)."""
+        self._finalise()
+        for n in self._order:
+            p = self.nodes[n].parent
+            if p is not None and self.bond_dim(n, p) < new_bond_dim:
+                self.pad_bond_dimension(p, n, new_bond_dim)
+
     def bond_dims(self) -> dict:
         """(parent, child) -> bond dimension (``core/ttn.py:754-768``)."""
         return {(self.nodes[n].parent, n): self.bond_dim(n, self.nodes[n].parent)

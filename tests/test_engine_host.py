@@ -882,3 +882,18 @@ def test_ttns_canonical_form_methods(monkeypatch):
     st2.canonical_form("s0")                            # REDUCED: a leaf bond cannot exceed 2
     assert st2.phys("s4").shape[0] == 2 and np.max(np.abs(st2.to_dense(ids) - v0)) < 1e-12
     assert st2.ensure_root_orth_center() is True
+
+
+def test_pad_bond_dimensions_reproduces_c1_fixture():
+    """pad_bond_dimensions of a bond-1 product state gives the zero-padded
+    tensors the C1 fixture was built from (same values, same leg layout)."""
+    import pytreenet_gb300 as P
+    c = load_case("c1_binary15_tfim_chi8")
+    small = {}
+    for nid, t in c["init"].items():
+        small[nid] = t[tuple(slice(0, 1) for _ in range(t.ndim - 1)) + (slice(None),)].copy()
+    st = build_ttn(P.TTNS, c["spec"], small)
+    st.pad_bond_dimensions(8)
+    for nid, t in c["init"].items():
+        assert np.array_equal(st.phys(nid), t), nid
+    assert st.max_bond_dim() == 8

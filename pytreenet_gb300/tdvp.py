@@ -235,7 +235,112 @@ def find_update_path(ttn, mode: "PathFinderMode") -> list[str]:
 
 
 class TensorProduct(dict):
-    """Single-site operators keyed by node id (``operators/tensorproduct.py:33``)."""
+    """Single-site operators keyed by node id (``operators/tensorproduct.py:33-430``),
+    numeric or symbolic (strings resolved through a conversion dictionary)."""
+
+    @classmethod
+    def from_operators(cls, operators) -> "TensorProduct":
+        out = cls()
+        for op in operators:
+            assert len(op.node_identifiers) == 1
+            out[op.node_identifiers[0]] = op.operator
+        return out
+
+    def add_operator(self, node_id: str, operator):
+        self[node_id] = operator
+
+    def add_suffix(self, suffix: str) -> "TensorProduct":
+        return TensorProduct({k + suffix: v for k, v in self.items()})
+
+    def num_sites(self) -> int:
+        return len(self)
+
+    def allclose(self, other) -> bool:
+        return len(self) == len(other) and all(k in other and np.allclose(v, other[k]) for k, v in self.items())
+
+    def pad_with_identities(self, ttn, symbolic: bool = False) -> "TensorProduct":
+        """Identities on every node of ``ttn`` without an operator."""
+        missing = set(self) - set(ttn.nodes)
+        if missing:
+            raise KeyError("Single site operators in this tensor product are applied to nodes "
+                           "that do not exist in the TTN!")
+        out = TensorProduct(self)
+        for nid in ttn.nodes:
+            if nid not in out:
+                d = int(ttn.phys(nid).shape[-1])
+                out[nid] = f"I{d}" if symbolic else np.eye(d)
+        return out
+
+    def into_operator(self, conversion_dict=None, order=None):
+        """The Kronecker product of the factors (``order`` defaults to the keys)."""
+        from .tebd import NumericOperator
+        order = list(self.keys()) if order is None else order
+        total = np.ones((1, 1), dtype=complex)
+        for nid in order:
+            op = self[nid]
+            if isinstance(op, str):
+                if conversion_dict is None:
+                    raise TypeError("If the tensor_product contains symbolic operators, there must be a "
+                                    "dictionary for conversion!")
+                op = conversion_dict[op]
+            total = np.kron(total, np.asarray(op))
+        return NumericOperator(total, list(order))
+
+    def exp(self, factor=1):
+        """exp(factor * A_1 x A_2 x ...)."""
+        import scipy.linalg
+        from .tebd import NumericOperator
+        op = self.into_operator()
+        return NumericOperator(scipy.linalg.expm(factor * op.operator), op.node_identifiers)
+
+    def _local(self, fn, invariance=None, suffix=""):
+        out = TensorProduct()
+        for k, v in self.items():
+            if isinstance(v, str):
+                out[k] = v if (invariance is not None and invariance.get(v)) else v + suffix
+            else:
+                out[k] = fn(np.asarray(v))
+        return out
+
+    def transpose(self, sym_dict=None, transpose_suffix: str = "_T") -> "TensorProduct":
+        return self._local(np.transpose, sym_dict, transpose_suffix)
+
+    def conjugate(self, real_dict=None, conjugate_suffix: str = "_conj") -> "TensorProduct":
+        return self._local(np.conjugate, real_dict, conjugate_suffix)
+
+    def conjugate_transpose(self, herm_dict=None, herm_suffix: str = "_H") -> "TensorProduct":
+        return self._local(lambda a: a.conj().T, herm_dict, herm_suffix)
+
+    def otimes(self, other, to_copy: bool = True) -> "TensorProduct":
+        out = TensorProduct(self) if to_copy else self
+        for k, v in other.items():
+            if k in out:
+                raise ValueError("The tensor products have a common identifier!")
+            out[k] = v
+        return out
+
+    def multiply(self, other, identity_dict=None, conversion_dict=None, multi_inset: str = "_mult_"):
+        """Site-wise matrix products (numeric factors; symbolic ones need the
+        conversion dictionary, into which the products are entered)."""
+        out = TensorProduct()
+        for k in set(self) | set(other):
+            if k in self and k in other:
+                a, b = self[k], other[k]
+                if isinstance(a, str) or isinstance(b, str):
+                    if conversion_dict is None:
+                        raise TypeError("symbolic factors need a conversion dictionary")
+                    name = f"{a}{multi_inset}{b}"
+                    conversion_dict[name] = np.asarray(conversion_dict[a] if isinstance(a, str) else a) @ \
+                        np.asarray(conversion_dict[b] if isinstance(b, str) else b)
+                    out[k] = name
+                else:
+                    out[k] = np.asarray(a) @ np.asarray(b)
+            else:
+                out[k] = self[k] if k in self else other[k]
+        return out
+
+    def __matmul__(self, other):
+        return self.multiply(other)
 
 
 class OneSiteTDVP(RunLoop):

@@ -897,3 +897,25 @@ def test_pad_bond_dimensions_reproduces_c1_fixture():
     for nid, t in c["init"].items():
         assert np.array_equal(st.phys(nid), t), nid
     assert st.max_bond_dim() == 8
+
+
+def test_tensor_product_methods():
+    import pytreenet_gb300 as P
+    X = np.array([[0, 1], [1, 0]], dtype=complex)
+    Y = np.array([[0, -1j], [1j, 0]], dtype=complex)
+    tp = P.TensorProduct({"a": X, "b": Zm})
+    op = tp.into_operator()
+    assert np.allclose(op.operator, np.kron(X, Zm)) and op.node_identifiers == ["a", "b"]
+    import scipy.linalg
+    assert np.allclose(tp.exp(-0.3j).operator, scipy.linalg.expm(-0.3j * np.kron(X, Zm)))
+    assert (tp @ P.TensorProduct({"a": Y}))["a"].tolist() == (X @ Y).tolist()
+    assert tp.otimes(P.TensorProduct({"c": Y})).num_sites() == 3
+    with pytest.raises(ValueError):
+        tp.otimes(P.TensorProduct({"a": Y}))
+    assert np.allclose(P.TensorProduct({"a": Y}).conjugate_transpose()["a"], Y.conj().T)
+    assert P.TensorProduct({"a": "X"}).transpose()["a"] == "X_T"
+    c = load_case("binary7_tfim_tebd")
+    st = build_ttn(P.TTNS, c["spec"], c["init"])
+    padded = P.TensorProduct({"s1": X}).pad_with_identities(st)
+    assert padded.num_sites() == 7 and np.allclose(padded["s0"], np.eye(2))
+    assert P.TensorProduct({"a": X}).allclose(P.TensorProduct({"a": X.copy()}))

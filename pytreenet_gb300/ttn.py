@@ -515,6 +515,52 @@ class TreeTensorNetworkOperator(TreeTensorNetwork):
 
     n_open = 2
 
+    def as_matrix(self, order: list | None = None):
+        """The operator as a dense matrix and the node order of its factors
+        (``ttno/ttno_class.py:44-58``); the contractions run on the device, for
+        small trees only."""
+        import torch
+        from .adjoint import _raw_contract
+        from .application import _device_tensor
+        from . import engine as E
+        if not torch.cuda.is_available():
+            raise RuntimeError("pytreenet_gb300 needs a CUDA device (no CPU fallback)")
+        dev = torch.device(E.DEFAULT_DEVICE)
+        self._finalise()
+
+        def rec(nid):
+            node = self.nodes[nid]
+            T = _device_tensor(self.phys(nid), dev)
+            has_p = node.parent is not None
+            kids = list(node.phys_children)
+            n = T.dim() - 2
+            labels = (["p"] if has_p else []) + [f"c{k}" for k in range(len(kids))] + ["t", "s"]
+            sites = [nid]
+            outs, ins = ["t"], ["s"]
+            for k, c in enumerate(kids):
+                sub, subsites = rec(c)
+                new_labels = [l for l in labels if l != f"c{k}"] + [f"O{k}", f"I{k}"]
+                T = _raw_contract(T, labels, sub, [f"c{k}", f"O{k}", f"I{k}"], new_labels, [f"c{k}"])
+                labels = new_labels
+                sites += subsites
+                outs.append(f"O{k}")
+                ins.append(f"I{k}")
+            final = (["p"] if has_p else []) + outs + ins
+            T = _raw_contract(T, labels, torch.ones((), dtype=T.dtype, device=dev), [], final, [])
+            dim = int(np.prod([int(self.phys(x).shape[-1]) for x in sites]))
+            shape = ([T.shape[0]] if has_p else []) + [dim, dim]
+            return T.reshape(shape), sites
+        mat, sites = rec(self.root_id)
+        mat = mat.cpu().numpy()
+        if order is None:
+            return mat, sites
+        dims = [int(self.phys(x).shape[-1]) for x in sites]
+        perm = [sites.index(x) for x in order]
+        nsite = len(sites)
+        full = mat.reshape(dims + dims).transpose(perm + [nsite + i for i in perm])
+        D = int(np.prod(dims))
+        return full.reshape(D, D), list(order)
+
     @classmethod
     def from_hamiltonian(cls, hamiltonian, reference_tree, method=None, dtype=complex):
         """``TTNO.from_hamiltonian`` (``ttno/ttno_class.py:60-97``): the TTNO of a

@@ -919,3 +919,30 @@ def test_tensor_product_methods():
     padded = P.TensorProduct({"s1": X}).pad_with_identities(st)
     assert padded.num_sites() == 7 and np.allclose(padded["s0"], np.eye(2))
     assert P.TensorProduct({"a": X}).allclose(P.TensorProduct({"a": X.copy()}))
+
+
+def test_ttno_as_matrix(monkeypatch):
+    """TTNO.as_matrix (device contractions) equals the dense operator."""
+    fake_ptn.install(monkeypatch)
+    import pytreenet_gb300 as P
+    from fractions import Fraction
+    from pytreenet_gb300.workloads import binary_tfim_random_state
+    X = np.array([[0, 1], [1, 0]], dtype=complex)
+    Y = np.array([[0, -1j], [1j, 0]], dtype=complex)
+    st, spec, tens, _, _ = binary_tfim_random_state(n=7, chi=2, seed=1)
+    ids = [n for n, _ in spec]
+    terms = [(Fraction(1, 2), "K", P.TensorProduct({"s3": "X", "s6": "Y", "s0": "Z"})),
+             P.TensorProduct({"s4": "Z", "s5": "Z"}), P.TensorProduct({"s2": X})]
+    H = P.TTNO.from_hamiltonian(P.Hamiltonian(terms, {"X": X, "Y": Y, "Z": Zm}, {"K": 0.7}), st)
+
+    def dense(ops):
+        mats = [ops.get(n, np.eye(2)) for n in ids]
+        out = mats[0]
+        for m in mats[1:]:
+            out = np.kron(out, m)
+        return out
+    Hd = 0.35 * dense({"s3": X, "s6": Y, "s0": Zm}) + dense({"s4": Zm, "s5": Zm}) + dense({"s2": X})
+    M, order = H.as_matrix(order=ids)
+    assert order == ids and np.max(np.abs(M - Hd)) < 1e-12
+    M2, sites = H.as_matrix()
+    assert sorted(sites) == sorted(ids) and M2.shape == (128, 128)

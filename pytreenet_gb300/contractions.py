@@ -117,6 +117,8 @@ def effective_single_site_evolution(state_tensor, state_node, hamiltonian_tensor
     net = tensor_cache.net
     st = tensor_cache.state
     x = torch.from_numpy(_to_phys(st, nid, state_tensor)).to(net.device, CDT)
+    if list(x.shape) != net.shape(nid):
+        raise ValueError(f"tensor shape {tuple(x.shape)} does not match node {nid} {tuple(net.shape(nid))}")
     p = net.heff_plan(nid)
     exp_factor = forward.exp_factor() if isinstance(forward, EvoDirection) else (-1j if forward else 1j)
 

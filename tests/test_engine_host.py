@@ -350,6 +350,11 @@ def test_contraction_helpers_match_oracle(monkeypatch):
                                                                          c["ttno"][center], envs),
                              0.05, -1j, krylov_tol=1e-12)
     np.testing.assert_allclose(z, np.transpose(zo, st.logical_perm(center)), atol=1e-11)
+    # a tensor of another shape is refused before anything runs on the device
+    with pytest.raises(ValueError):
+        C.effective_single_site_evolution(x[..., :1], st.nodes[center], None, H.nodes[center], 0.05, cache)
+    with pytest.raises(ValueError):
+        C.contract_ket_ham_with_envs(st.nodes[center], x[..., :1], H.nodes[center], None, cache)
 
 
 def test_finite_difference_gradient_matches_oracle(monkeypatch):

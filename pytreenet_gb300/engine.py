@@ -135,6 +135,13 @@ class Step:
         for l in klabels:
             if A.dims[A.labels.index(l)] != B.dims[B.labels.index(l)]:
                 raise ValueError(f"dimension mismatch on leg {l}")
+        # the output's legs must have the sizes of the operand legs they come
+        # from: the kernel writes through C's strides over A's and B's ranges
+        for op, labs in ((A, mlab), (B, nlab)):
+            for l in labs:
+                if C.dims[C.labels.index(l)] != op.dims[op.labels.index(l)]:
+                    raise ValueError(f"output leg {l} has size {C.dims[C.labels.index(l)]}, "
+                                     f"the operand's has {op.dims[op.labels.index(l)]}")
         _fill(d.m, col(A, mlab, "dims"), col(A, mlab, "strides"), col(C, mlab, "strides"), "m")
         _fill(d.n, col(B, nlab, "dims"), col(B, nlab, "strides"), col(C, nlab, "strides"), "n")
         _fill(d.k, col(A, klabels, "dims"), col(A, klabels, "strides"), col(B, klabels, "strides"), "k")

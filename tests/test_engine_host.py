@@ -951,3 +951,21 @@ def test_ttno_as_matrix(monkeypatch):
     assert order == ids and np.max(np.abs(M - Hd)) < 1e-12
     M2, sites = H.as_matrix()
     assert sorted(sites) == sorted(ids) and M2.shape == (128, 128)
+
+
+def test_plans_refuse_mismatched_output_legs(monkeypatch):
+    """A gate whose output dimension differs from the site's is refused when the
+    plan is built (the kernel would otherwise write past the output buffer)."""
+    fake_ptn.install(monkeypatch)
+    import torch
+    import pytreenet_gb300 as P
+    from pytreenet_gb300.engine import DeviceNetwork, Operand, Step
+    c = load_case("binary7_tfim_tebd")
+    st = build_ttn(P.TTNS, c["spec"], c["init"])
+    net = DeviceNetwork(st, None)
+    with pytest.raises(ValueError):
+        net.apply_single_site_gate("s1", torch.zeros((3, 2), dtype=torch.complex128))
+    A = Operand.contiguous(("fixed", None), ["i", "k"], [4, 5])
+    B = Operand.contiguous(("fixed", None), ["k", "j"], [5, 6])
+    with pytest.raises(ValueError):
+        Step(A, B, ["k"], Operand.contiguous(("fixed", None), ["i", "j"], [4, 7]))

@@ -70,6 +70,8 @@ def _raw_contract(a, la, b, lb, lc, klabels, conj_a=False, conj_b=False, out=Non
         if beta != 0.0:
             raise ValueError("beta needs an output tensor")
         out = torch.empty(shape_c, dtype=CDT, device=a.device)
+    elif list(out.shape) != shape_c or not out.is_contiguous() or out.dtype != CDT:
+        raise ValueError(f"output tensor {tuple(out.shape)} does not match the contraction's {tuple(shape_c)}")
     key = (tuple(la), tuple(a.shape), tuple(lb), tuple(b.shape), tuple(lc), tuple(klabels),
            bool(conj_a), bool(conj_b), complex(beta))
     ent = _DESCS.get(key)

@@ -59,6 +59,10 @@ _DESCS: dict = {}
 
 def _raw_contract(a, la, b, lb, lc, klabels, conj_a=False, conj_b=False, out=None, beta=0.0):
     """C[lc] = beta C + sum_k op(A)[la] op(B)[lb] in one ``ptn_exec_ops`` call."""
+    if a.dtype != CDT or b.dtype != CDT:
+        raise TypeError("contractions take complex128 tensors")
+    if a.dim() != len(la) or b.dim() != len(lb):
+        raise ValueError("one label per leg")
     a = a.contiguous()
     b = b.contiguous()
     dims = dict(zip(la, a.shape))

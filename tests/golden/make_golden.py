@@ -781,7 +781,7 @@ def time_dep_cases(ptn):
 def main(ref_root):
     ptn = _import_reference(ref_root)
     rng = np.random.default_rng(1234)
-    # C1 as specified: 15-node binary TFIM, padded product state chi=8, 50 steps.
+    # 15-node binary TFIM, Bloch-sphere product state zero-padded to chi=8, 50 steps.
     spec = binary_tree(15)
     run_case(ptn, "c1_binary15_tfim_chi8", spec, product_state_tensors(spec, rng, 8),
              lambda psi: tfim(ptn, spec), 0.01, 50, 1, 1e-12)
@@ -789,7 +789,7 @@ def main(ref_root):
     spec = binary_tree(7)
     run_case(ptn, "binary7_tfim_chi4_o2", spec, product_state_tensors(spec, rng, 4),
              lambda psi: tfim(ptn, spec), 0.02, 8, 2, 1e-12)
-    # T-tree, random canonicalised state, Heisenberg + fields (C3 shape, small).
+    # T-tree, random canonicalised state, Heisenberg + fields (root + three arms, small).
     spec = t_tree(3)
     h = rng.uniform(-1, 1, size=len(spec))
     run_case(ptn, "ttree3_heis_chi6_o1", spec, random_state_tensors(spec, rng, 6),

@@ -891,7 +891,7 @@ def test_ttns_canonical_form_methods(monkeypatch):
 
 def test_pad_bond_dimensions_reproduces_c1_fixture():
     """pad_bond_dimensions of a bond-1 product state gives the zero-padded
-    tensors the C1 fixture was built from (same values, same leg layout)."""
+    tensors the padded binary-tree fixture was built from (same values, same leg layout)."""
     import pytreenet_gb300 as P
     c = load_case("c1_binary15_tfim_chi8")
     small = {}

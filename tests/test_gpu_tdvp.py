@@ -37,7 +37,7 @@ def test_gpu_tdvp_full_rank_cases(name):
 
 
 def test_gpu_tdvp_c1_padded():
-    """C1 at full length (50 steps); bounded by the reference's own rounding floor."""
+    """15-node binary TFIM from a zero-padded product state, 50 steps; bounded by the reference's own rounding floor."""
     c, got, zerr = _run("c1_binary15_tfim_chi8")
     ids = [s[0] for s in c["spec"]]
     a = O.state_vector(got, ids)
@@ -47,7 +47,7 @@ def test_gpu_tdvp_c1_padded():
 
 
 def test_gpu_tdvp_ttree_chi16_vs_oracle():
-    """C3 shape (root + 3 arms) at reduced size against the oracle: own TTNO builder."""
+    """A T-tree (root + 3 arms) at reduced size against the oracle: own TTNO builder."""
     import pytreenet_gb300 as P
     from pytreenet_gb300.workloads import t_tree_state, t_tree_heisenberg
     st, spec, tensors = t_tree_state(arm_len=5, chi=16, seed=5)

@@ -32,7 +32,7 @@ def test_oracle_full_rank_cases(name):
 
 
 def test_oracle_c1_padded_product_state():
-    """C1 (15-node binary TFIM, chi=8 zero-padded product state, 50 steps).
+    """15-node binary TFIM, chi=8 zero-padded product state, 50 steps.
     The reference's own result moves by ~2e-6 (state) / 5e-9 (<Z>) under a
     1e-15 relative input perturbation, because some QRs see noise-level
     rank deficiency; parity is asserted at that floor."""

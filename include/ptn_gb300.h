@@ -71,6 +71,11 @@ typedef struct {
  * and contract_nodes (contractions/node_contraction.py:62-86). */
 int ptn_zcontract(const ptn_contract_desc* d, void* stream);
 
+/* The K split ptn_zcontract uses for an output of `tiles` 64 x 64 tiles and a
+ * K range of K: returns the number of splits and sets *k_chunk (K indices per
+ * split). Host-only arithmetic. No counterpart in the reference. */
+int64_t ptn_zcontract_splits(int64_t tiles, int64_t K, int64_t* k_chunk);
+
 /* ---- Krylov (Lanczos/Arnoldi) vector kernels, complex128 -------------------
  * Replace the np.vdot / np.linalg.norm / axpy loop of krylov_exp_action
  * (time_evolution/time_evolution.py:721-821). Vectors q_i are rows of a

@@ -93,6 +93,7 @@ _I64 = ctypes.c_int64
 _I32 = ctypes.c_int32
 SIGNATURES = {
     "ptn_zcontract": (ctypes.c_int, [ctypes.POINTER(ContractDesc), _P]),
+    "ptn_zcontract_splits": (_I64, [_I64, _I64, ctypes.POINTER(ctypes.c_int64)]),
     "ptn_krylov_partials": (_I64, [_I64]),
     "ptn_zdot_multi": (ctypes.c_int, [_P, _I64, _I32, _P, _I64, _P, _I32, _P, _P]),
     "ptn_zaxpy_multi": (ctypes.c_int, [_P, _I64, _I32, _P, _P, _I64, _P]),

@@ -192,6 +192,20 @@ int fill_modes(const ptn_modes& src, ModeDev& dst, int which, int64_t& total) {
 
 }  // namespace
 
+// Split K when the output tiles cover at most a quarter of the 152 SMs: about
+// 304 CTAs in all, each split at least 256 K indices long, chunks a multiple
+// of the K step; the chunks cover [0, K) exactly once.
+extern "C" int64_t ptn_zcontract_splits(int64_t tiles, int64_t K, int64_t* k_chunk) {
+  *k_chunk = K;
+  if (tiles > 38 || K < 2048) return 1;
+  int64_t want = (304 + tiles - 1) / tiles;
+  int64_t most = K / 256;
+  int64_t splits = want < most ? want : most;
+  if (splits < 2) return 1;
+  *k_chunk = ((K + splits - 1) / splits + BK - 1) / BK * BK;
+  return (K + *k_chunk - 1) / *k_chunk;
+}
+
 extern "C" int ptn_zcontract(const ptn_contract_desc* d, void* stream) {
   if (!d || !d->A || !d->B || !d->C) return PTN_ERR_ARG;
   ContractArgs a;
@@ -214,20 +228,7 @@ extern "C" int ptn_zcontract(const ptn_contract_desc* d, void* stream) {
   a.tiles_n = tn;
   int64_t tiles = tm * tn;
   if (tiles > 0x7fffffffLL) return PTN_ERR_UNSUPPORTED;
-  // split K when the output tiles cover at most a quarter of the 152 SMs
-  int64_t splits = 1;
-  a.k_chunk = K;
-  if (tiles <= 38 && K >= 2048) {
-    int64_t want = (304 + tiles - 1) / tiles;
-    int64_t most = K / 256;
-    splits = want < most ? want : most;
-    if (splits >= 2) {
-      a.k_chunk = ((K + splits - 1) / splits + BK - 1) / BK * BK;
-      splits = (K + a.k_chunk - 1) / a.k_chunk;
-    } else {
-      splits = 1;
-    }
-  }
+  int64_t splits = ptn_zcontract_splits(tiles, K, &a.k_chunk);
   a.split = splits > 1;
   cudaStream_t s = ptn_stream(stream);
   if (a.split) {

@@ -373,11 +373,56 @@ def run_case_tebd_swaps(ptn, name, spec, tensors, dt, steps, svd, J=1.0, g=0.7, 
     print(name, "written; gates", len(tebd.exponents))
 
 
+def run_case_tebd_strang(ptn, name, spec, tensors, dt, steps, svd, J=1.0, g=0.7):
+    """TEBD with a symmetric (Strang) splitting from ``TrotterSplitting.from_lists``:
+    the field terms by dt/2, the edge terms by dt, the field terms by dt/2."""
+    psi = build_reference_state(ptn, spec, tensors)
+    tps = [ptn.TensorProduct({p: -J * Z, nid: Z}) for nid, p in spec if p is not None]
+    ne = len(tps)
+    tps += [ptn.TensorProduct({nid: -g * X}) for nid, _ in spec]
+    fields = list(range(ne, len(tps)))
+    splitting = [(i, 0.5) for i in fields] + [(i, 1) for i in range(ne)] + [(i, 0.5) for i in fields]
+    split = ptn.TrotterSplitting.from_lists(tps, splitting=splitting)
+    maxd, rel, tot, renorm = svd
+    params = ptn.SVDParameters(max_bond_dim=maxd, rel_tol=rel, total_tol=tot, renorm=renorm)
+    ops = {nid: ptn.TensorProduct({nid: Z}) for nid, _ in spec}
+    tebd = ptn.TEBD(psi, split, dt, dt * steps, ops, svd_parameters=params)
+    rec = {"spec_ids": np.array([s[0] for s in spec]),
+           "spec_parents": np.array(["" if s[1] is None else s[1] for s in spec]),
+           "dt": dt, "steps": steps, "order": 0, "krylov_tol": 0.0, "tebd": 1,
+           "svd_max_bond_dim": maxd, "svd_rel_tol": rel, "svd_total_tol": tot, "svd_renorm": int(renorm),
+           "update_path": np.array([s[0] for s in spec]), "n_gates": len(tebd.exponents), "n_terms": len(tps),
+           "splitting": np.array(splitting, dtype=float)}
+    for i, u in enumerate(tebd.exponents):
+        rec[f"gate/{i}/op"] = np.asarray(u.operator)
+        rec[f"gate/{i}/ids"] = np.array(list(u.node_identifiers))
+    for i, tp in enumerate(tps):
+        rec[f"term/{i}/ids"] = np.array(list(tp.keys()))
+        rec[f"term/{i}/ops"] = np.array([tp[k] for k in tp.keys()])
+        rec[f"term/{i}/before"] = np.zeros((0, 2), dtype=str)
+        rec[f"term/{i}/after"] = np.zeros((0, 2), dtype=str)
+    for nid, t in tensors.items():
+        rec[f"init/{nid}"] = t
+    for nid, _ in spec:
+        rec[f"ttno/{nid}"] = np.zeros(1)
+    zs = []
+    for step in range(steps):
+        tebd.run_one_time_step()
+        zs.append([tebd.state.operator_expectation_value(ops[nid]) for nid, _ in spec])
+    rec["z"] = np.array(zs)
+    for nid, t in export_state(tebd.state, spec).items():
+        rec[f"final/{nid}"] = t
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **rec)
+    print(name, "written; gates", len(tebd.exponents))
+
+
 def tebd_swap_cases(ptn):
     rng = np.random.default_rng(53)
     spec = binary_tree(7)
     run_case_tebd_swaps(ptn, "binary7_tfim_tebd_swaps", spec, random_state_tensors(spec, rng, 2), 0.05, 4,
                         (6, 1e-10, 1e-10, False))
+    run_case_tebd_strang(ptn, "binary7_tfim_tebd_strang", spec, random_state_tensors(spec, rng, 2), 0.05, 4,
+                         (6, 1e-10, 1e-10, False))
 
 
 def svd_cases():

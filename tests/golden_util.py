@@ -43,7 +43,7 @@ def load_case(name):
 CASES = ["c1_binary15_tfim_chi8", "binary7_tfim_chi4_o2", "ttree3_heis_chi6_o1",
          "ttree3_heis_chi6_o2", "ternary2_xxz_chi4_o1"]
 TWO_SITE_CASES = ["ternary2_xxz_neel_2tdvp", "binary7_heis_2tdvp_trunc", "binary7_heis_2tdvp_l2l"]
-TEBD_CASES = ["binary7_tfim_tebd", "binary7_tfim_tebd_swaps"]
+TEBD_CASES = ["binary7_tfim_tebd", "binary7_tfim_tebd_swaps", "binary7_tfim_tebd_strang"]
 DRIVEN_CASES = ["binary7_tfim_driven_o1", "binary7_tfim_driven_o2"]
 BUG_CASES = ["binary15_tfim_fixed_bug", "ternary2_xxz_fixed_bug"]
 ADAPTIVE_BUG_CASES = ["binary7_tfim_bug", "ternary2_xxz_bug"]
@@ -237,7 +237,10 @@ def swap_splitting(name):
         tps.append(P.TensorProduct({k: ops[j] for j, k in enumerate(ids)}))
         before.append(P.SWAPlist([tuple(str(y) for y in x) for x in d[f"term/{i}/before"]]))
         after.append(P.SWAPlist([tuple(str(y) for y in x) for x in d[f"term/{i}/after"]]))
-    return P.TrotterSplitting.from_lists(tps, swaps_before=before, swaps_after=after)
+    splitting = None
+    if "splitting" in d.files:
+        splitting = [(int(i), float(f)) for i, f in d["splitting"]]
+    return P.TrotterSplitting.from_lists(tps, splitting=splitting, swaps_before=before, swaps_after=after)
 
 
 def check_heff_fixture(tol=1e-12):

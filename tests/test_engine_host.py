@@ -527,15 +527,16 @@ def test_engine_host_adaptive_bug_matches_reference(monkeypatch, name):
     assert one_minus_f < 1e-11
 
 
-def test_engine_host_swap_splitting_matches_reference(monkeypatch):
-    """TrotterSplitting.from_lists with SWAP lists: the same gate sequence as
-    the reference's (SWAPs before, the exponentiated term, SWAPs after), and
+@pytest.mark.parametrize("name", ["binary7_tfim_tebd_swaps", "binary7_tfim_tebd_strang"])
+def test_engine_host_swap_splitting_matches_reference(monkeypatch, name):
+    """TrotterSplitting.from_lists with SWAP lists or with a symmetric
+    (Strang) order of factors: the same gate sequence as the reference's, and
     TEBD driven by it reproduces the reference's run."""
     fake_ptn.install(monkeypatch)
     import pytreenet_gb300 as P
     from golden_util import swap_splitting
-    c = load_case("binary7_tfim_tebd_swaps")
-    split = swap_splitting("binary7_tfim_tebd_swaps")
+    c = load_case(name)
+    split = swap_splitting(name)
     st = build_ttn(P.TTNS, c["spec"], c["init"])
     assert split[-1].swaps_before.is_compatible_with_ttn(st)
     gates = split.exponentiate_splitting(c["dt"], ttn=st)

@@ -808,14 +808,15 @@ class DeviceNetwork:
         rec(left_out, None)
 
     # -- local evolutions ------------------------------------------------------------
-    def evolve_site(self, nid, dt, exp_factor, tol, maxdim):
+    def evolve_site(self, nid, dt, exp_factor, tol, maxdim, hermitian: bool = True):
         p = self.heff_plan(nid)
 
         def apply(xp, yp):
             p.run(xp, yp)
             self.flops += p.flops
         x = self.t[nid]
-        self.krylov.expm(x, apply, dt, exp_factor, tol, maxdim, out=x, tridiagonal=self.levels > 0)
+        self.krylov.expm(x, apply, dt, exp_factor, tol, maxdim, hermitian=hermitian, out=x,
+                         tridiagonal=self.levels > 0)
         self.check_device_status()
 
     def check_device_status(self):
@@ -825,13 +826,14 @@ class DeviceNetwork:
             st.zero_()
             raise _lib.PtnError(code, "tensor-core contraction")
 
-    def evolve_bond(self, r: torch.Tensor, nid, nxt, dt, exp_factor, tol, maxdim):
+    def evolve_bond(self, r: torch.Tensor, nid, nxt, dt, exp_factor, tol, maxdim, hermitian: bool = True):
         p = self.bond_plan(nid, nxt)
 
         def apply(xp, yp):
             p.run(xp, yp)
             self.flops += p.flops
-        return self.krylov.expm(r, apply, dt, exp_factor, tol, maxdim, out=r, tridiagonal=self.levels > 0)
+        return self.krylov.expm(r, apply, dt, exp_factor, tol, maxdim, hermitian=hermitian, out=r,
+                                tridiagonal=self.levels > 0)
 
     # -- QR split and R absorption ---------------------------------------------------
     CHOLQR_MIN_ROWS = 8192
@@ -1351,7 +1353,7 @@ class DeviceNetwork:
             nv_.children = [u] + [c for c in nv_.children if c != u]
         return new_s
 
-    def evolve_two_site(self, u, v, dt, exp_factor, tol, maxdim, svd) -> np.ndarray:
+    def evolve_two_site(self, u, v, dt, exp_factor, tol, maxdim, svd, hermitian: bool = True) -> np.ndarray:
         """Two-site update of (u, v) with u the orthogonality centre: merge,
         Krylov exponential of the pair's H_eff, truncated SVD split, centre to
         v, environment E(u -> v) (``TwoSiteTDVP._update_two_site_nodes``,
@@ -1366,7 +1368,8 @@ class DeviceNetwork:
         def apply(xp, yp):
             hp.run(xp, yp)
             self.flops += hp.flops
-        self.krylov.expm(x2, apply, dt, exp_factor, tol, maxdim, out=x2, tridiagonal=self.levels > 0)
+        self.krylov.expm(x2, apply, dt, exp_factor, tol, maxdim, hermitian=hermitian, out=x2,
+                         tridiagonal=self.levels > 0)
         self.check_device_status()
         s = self.svd_split(u, v, x2, svd)
         self.state.orthogonality_center_id = v

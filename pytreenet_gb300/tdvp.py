@@ -418,7 +418,8 @@ class OneSiteTDVP(RunLoop):
     # -- building blocks --------------------------------------------------------------
     def _update_site(self, node_id, time_step_factor=1.0):
         tol, maxdim = self._kry()
-        self.net.evolve_site(node_id, self.time_step_size * time_step_factor, self._factor(True), tol, maxdim)
+        self.net.evolve_site(node_id, self.time_step_size * time_step_factor, self._factor(True), tol, maxdim,
+                             hermitian=self.solver_options.get("hermitian", True))
 
     def _update_link(self, node_id, next_node_id, time_step_factor=1.0):
         st = self.state
@@ -427,7 +428,7 @@ class OneSiteTDVP(RunLoop):
         self.net.update_env(node_id, next_node_id)
         tol, maxdim = self._kry()
         self.net.evolve_bond(R, node_id, next_node_id, self.time_step_size * time_step_factor,
-                             self._factor(False), tol, maxdim)
+                             self._factor(False), tol, maxdim, hermitian=self.solver_options.get("hermitian", True))
         self.net.absorb(R, node_id, next_node_id, link_variant=True)
         st.orthogonality_center_id = next_node_id
 
@@ -545,7 +546,8 @@ class TwoSiteTDVP(OneSiteTDVP):
         """``_update_two_site_nodes`` (``twositetdvp.py:89-125``)."""
         tol, maxdim = self._kry()
         s = self.net.evolve_two_site(target_node_id, next_node_id, self.time_step_size * time_step_factor,
-                                     self._factor(True), tol, maxdim, self.config)
+                                     self._factor(True), tol, maxdim, self.config,
+                                     hermitian=self.solver_options.get("hermitian", True))
         self.bond_dims_history.append(len(s))
 
     def _single_site_backwards_update(self, node_id, time_step_factor=1.0):

@@ -970,3 +970,20 @@ def test_plans_refuse_mismatched_output_legs(monkeypatch):
     B = Operand.contiguous(("fixed", None), ["k", "j"], [5, 6])
     with pytest.raises(ValueError):
         Step(A, B, ["k"], Operand.contiguous(("fixed", None), ["i", "j"], [4, 7]))
+
+
+def test_solver_option_hermitian_false(monkeypatch):
+    """solver_options hermitian=False (the Arnoldi projection exponentiated as
+    it is) reproduces the reference's run of a Hermitian problem."""
+    fake_ptn.install(monkeypatch)
+    import pytreenet_gb300 as P
+    c = load_case("ttree3_heis_chi6_o1")
+    st = build_ttn(P.TTNS, c["spec"], c["init"])
+    H = build_ttn(P.TTNO, c["spec"], c["ttno"])
+    algo = P.FirstOrderOneSiteTDVP(st, H, c["dt"], c["dt"] * c["steps"], {},
+                                   config=P.TDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV),
+                                   solver_options={"krylov_tol": c["krylov_tol"], "hermitian": False})
+    for k in range(c["steps"]):
+        algo.run_one_time_step()
+        z = np.array([algo.evaluate_operator({nid: Zm}) for nid, _ in c["spec"]])
+        assert np.max(np.abs(z - c["z"][k])) < 1e-10

@@ -241,6 +241,60 @@ class TreeTensorNetwork:
             if p is not None and self.bond_dim(n, p) < new_bond_dim:
                 self.pad_bond_dimension(p, n, new_bond_dim)
 
+    @property
+    def root(self):
+        """(root node, root tensor in its leg order) (``core/ttn.py:165-180``)."""
+        if self.root_id is None:
+            raise KeyError("There is no root in the TTN.")
+        return self.nodes[self.root_id], self.get_tensor(self.root_id)
+
+    def num_nodes(self) -> int:
+        return len(self._order)
+
+    def linearise(self, mode: str = "children_first") -> list:
+        """Node order with every node after its children (or, with
+        ``parents_first``, before them) (``core/tree_structure.py:653-690``)."""
+        name = getattr(mode, "name", str(mode)).lower()
+        out = []
+
+        def rec(n):
+            if name == "parents_first":
+                out.append(n)
+            for c in self.nodes[n].children:
+                rec(c)
+            if name != "parents_first":
+                out.append(n)
+        rec(self.root_id)
+        return out
+
+    def replace_tensor(self, node_id: str, new_tensor, permutation=None, new_shape: bool = False):
+        """Set a node's tensor, given in its leg order (or permuted into it by
+        ``permutation``) (``core/ttn.py:981-1010``)."""
+        t = np.asarray(new_tensor) if not hasattr(new_tensor, "detach") else new_tensor.detach().cpu().numpy()
+        if permutation is not None:
+            t = np.transpose(t, permutation)
+        if not new_shape and tuple(t.shape) != tuple(self.get_tensor(node_id).shape):
+            raise ValueError("the new tensor does not fit the node (pass new_shape=True)")
+        self.set_tensor(node_id, t)
+        self.nodes[node_id].shape = tuple(self._phys[node_id].shape)
+
+    def conjugate(self):
+        """A copy with every tensor complex-conjugated (``core/ttn.py:681-690``)."""
+        out = self.copy_structure()
+        out._phys = {k: (np.conj(v) if isinstance(v, np.ndarray) else v.conj().resolve_conj())
+                     for k, v in self._phys.items()}
+        return out
+
+    def completely_contract_tree(self, to_copy: bool = False, order: list | None = None):
+        """The whole network as one tensor and the node order of its open legs
+        (states only: one physical leg per node; small trees)."""
+        if not hasattr(self, "to_dense"):
+            raise NotImplementedError("a TTNO contracts to a matrix with as_matrix()")
+        order = list(self._order) if order is None else list(order)
+        vec = self.to_dense(order)
+        dims = [int(self.phys(n).shape[-1]) for n in order]
+        return vec.reshape(dims), order
+
     def bond_dims(self) -> dict:
         """(parent, child) -> bond dimension (``core/ttn.py:754-768``)."""
         return {(self.nodes[n].parent, n): self.bond_dim(n, self.nodes[n].parent)

@@ -987,3 +987,27 @@ def test_solver_option_hermitian_false(monkeypatch):
         algo.run_one_time_step()
         z = np.array([algo.evaluate_operator({nid: Zm}) for nid, _ in c["spec"]])
         assert np.max(np.abs(z - c["z"][k])) < 1e-10
+
+
+def test_ttn_structure_methods():
+    import pytreenet_gb300 as P
+    c = load_case("ttree3_heis_chi6_o1")
+    st = build_ttn(P.TTNS, c["spec"], {k: v.copy() for k, v in c["init"].items()})
+    node, t = st.root
+    assert node.identifier == c["spec"][0][0] and st.num_nodes() == len(c["spec"])
+    lin = st.linearise()
+    assert lin[-1] == st.root_id and set(lin) == set(st.nodes)
+    for n in lin:                                  # children before parents
+        p = st.nodes[n].parent
+        assert p is None or lin.index(p) > lin.index(n)
+    assert st.linearise("parents_first")[0] == st.root_id
+    ids = [n for n, _ in c["spec"]]
+    v = st.to_dense(ids)
+    assert np.allclose(st.conjugate().to_dense(ids), v.conj())
+    full, order = st.completely_contract_tree(order=ids)
+    assert np.allclose(full.reshape(-1), v) and order == ids
+    leaf = ids[-1]
+    st.replace_tensor(leaf, 2 * st.get_tensor(leaf))
+    assert np.allclose(st.to_dense(ids), 2 * v)
+    with pytest.raises(ValueError):
+        st.replace_tensor(leaf, np.zeros((1, 1)))

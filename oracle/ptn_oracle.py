@@ -392,6 +392,20 @@ def dense_exp_action(psi, action, dt, exp_factor):
     return (scipy.linalg.expm(exp_factor * dt * H) @ psi.reshape(-1)).reshape(psi.shape)
 
 
+def ode_exp_action(psi, action, dt, exp_factor, method="RK45", **options):
+    """The ODE modes of ``TimeEvoMode.time_evolve_action``
+    (``time_evolution.py:595-615``): ``scipy.integrate.solve_ivp`` on
+    y' = exp_factor H y over (0, dt), read at t_eval = [dt]."""
+    from scipy.integrate import solve_ivp
+    shape = psi.shape
+
+    def rhs(t, y):
+        return exp_factor * np.asarray(action(y.reshape(shape))).reshape(-1)
+    res = solve_ivp(rhs, (0, dt), np.asarray(psi, dtype=complex).reshape(-1), method=method,
+                    t_eval=[dt], **options)
+    return res.y[:, 0].reshape(shape)
+
+
 def _postorder(tree: OTree, nid):
     if tree.is_leaf(nid):
         return [nid]
@@ -488,8 +502,10 @@ class _OneSiteBase:
     (``tdvp_algorithms/tdvp_algorithm.py:58-221``, ``onesitetdvp.py:17-134``)."""
 
     def __init__(self, state: OState, W: dict, dt: float, krylov_tol=1e-10,
-                 max_krylov_dim=None, path_mode: str = "LeafToRoot", exact: bool = False):
+                 max_krylov_dim=None, path_mode: str = "LeafToRoot", exact: bool = False,
+                 ode: dict | None = None):
         self.exact = exact
+        self.ode = ode
         self.state = state.copy()
         self.W = W
         self.dt = dt
@@ -506,6 +522,8 @@ class _OneSiteBase:
         self.envs = init_cache_but_one(self.state, W, self.update_path[0])
 
     def _krylov(self, x, action, factor, exp_factor):
+        if self.ode is not None:
+            return ode_exp_action(x, action, self.dt * factor, exp_factor, **self.ode)
         if self.exact:
             return dense_exp_action(x, action, self.dt * factor, exp_factor)
         return krylov_exp_action(x, action, self.dt * factor, exp_factor,

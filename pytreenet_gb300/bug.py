@@ -17,7 +17,7 @@ local exponential the engine's Krylov solver; tensors keep the engine's
 physical leg layout, so the reference's basis-change nodes become
 contractions on a leg in place. As in the reference, the solver options
 reach the root and its children only; deeper nodes use the default Krylov
-tolerance 1e-10.
+tolerance 1e-10 (an ODE mode there runs at ``solve_ivp``'s own tolerances).
 """
 from __future__ import annotations
 
@@ -32,8 +32,9 @@ from . import _lib
 from . import engine as E
 from .adjoint import (_SiteOp, _raw_contract, _solver, _tensor_apply, absorb, env_apply, qr_keep_raw)
 from .engine import CDT, DeviceNetwork, check
+from .ode import RungeKuttaSolver
 from .tdvp import (TTNTimeEvolutionConfig, TimeEvoMode, _tensor_copy, check_time_evo_mode,
-                   compute_num_time_steps)
+                   compute_num_time_steps, ode_options)
 from .results import RunLoop, init_operators
 from .svd_truncation import TreeOps, move_center, qr_split, truncate_tensors
 from .truncation import SVDParameters
@@ -103,8 +104,13 @@ class FixedBUG(RunLoop):
         self.solver_options = check_time_evo_mode(self.config.time_evo_mode, solver_options)
         # the reference hands its options to the root and its children only;
         # deeper nodes run the mode's defaults (the exact modes need no options)
-        self._deep_tol = (self.solver_options["krylov_tol"] if self.config.time_evo_mode.is_exact()
-                          else DEFAULT_KRYLOV_TOL)
+        mode = self.config.time_evo_mode
+        exact = mode.is_exact()
+        # local solver settings (Krylov stop, Krylov dimension cap, ODE options)
+        self._top = (self.solver_options.get("krylov_tol", DEFAULT_KRYLOV_TOL),
+                     self.solver_options.get("max_krylov_dim"), ode_options(mode, self.solver_options))
+        self._deep = (self.solver_options["krylov_tol"] if exact else DEFAULT_KRYLOV_TOL,
+                      self.solver_options.get("max_krylov_dim") if exact else None, ode_options(mode, {}))
         self.time_step_size = float(time_step_size)
         self.final_time = float(final_time)
         self.num_time_steps = compute_num_time_steps(final_time, time_step_size)
@@ -150,12 +156,18 @@ class FixedBUG(RunLoop):
         ev = [envs[(x, nid)] if x != nxt else None for x in self.nbrs[nid]]
         return env_apply(A, ev, self.net.W[nid], self._ax(nid, nxt))
 
-    def _evolve(self, nid, x, envs, tol):
+    def _evolve(self, nid, x, envs, setting):
+        tol, maxdim, ode = setting
         nb = self.nbrs[nid]
         params = [envs[(v, nid)] for v in nb] + [self.net.W[nid]]
         y = torch.empty_like(x)
-        _solver(x.device).expm(x.contiguous(), _tensor_apply(_SiteOp(len(nb)), params, x.shape), self.time_step_size,
-                               -1j, tol, self.solver_options.get("max_krylov_dim"), out=y)
+        apply = _tensor_apply(_SiteOp(len(nb)), params, x.shape)
+        if ode is not None:
+            if self._rk is None:
+                self._rk = RungeKuttaSolver(_solver(x.device).ws)
+            self._rk.integrate(x.contiguous(), apply, self.time_step_size, -1j, out=y, **ode)
+        else:
+            _solver(x.device).expm(x.contiguous(), apply, self.time_step_size, -1j, tol, maxdim, out=y)
         return y
 
     def _in_new_child_bases(self, T, nid, Ms):
@@ -167,8 +179,9 @@ class FixedBUG(RunLoop):
         return T
 
     _adaptive = False
+    _rk = None
 
-    def _update_node(self, c, P, envs_p, tol):
+    def _update_node(self, c, P, envs_p, setting):
         """``update_node`` + ``update_leaf_node`` / ``update_non_leaf_node``."""
         p = self.parent[c]
         Q, R = qr_split(P[p], self._ax(p, c), reduced=self._adaptive)
@@ -180,11 +193,11 @@ class FixedBUG(RunLoop):
         envs.pop((c, p), None)
         new, Ms, blocks = {}, {}, {}
         for g in self.children[c]:
-            sub, blocks[g], Ms[g] = self._update_node(g, cur, envs, self._deep_tol)
+            sub, blocks[g], Ms[g] = self._update_node(g, cur, envs, self._deep)
             new.update(sub)
         envs.update({(g, c): b for g, b in blocks.items()})
         x = self._in_new_child_bases(cur[c], c, Ms)
-        upd = self._evolve(c, x, envs, tol)
+        upd = self._evolve(c, x, envs, setting)
         old = self._in_new_child_bases(P[c], c, Ms)
         if self._adaptive:
             # the new basis spans the old and the evolved tensor
@@ -211,13 +224,12 @@ class FixedBUG(RunLoop):
             if toward is not None:
                 envs[(nid, toward)] = self._env(nid, toward, A[nid], envs)
         rec(root, None)
-        tol = self.solver_options.get("krylov_tol", DEFAULT_KRYLOV_TOL)
         new, Ms, blocks = {}, {}, {}
         for c in self.children[root]:
-            sub, blocks[c], Ms[c] = self._update_node(c, A, envs, tol)
+            sub, blocks[c], Ms[c] = self._update_node(c, A, envs, self._top)
             new.update(sub)
         envs.update({(c, root): b for c, b in blocks.items()})
-        new[root] = self._evolve(root, self._in_new_child_bases(A[root], root, Ms), envs, tol)
+        new[root] = self._evolve(root, self._in_new_child_bases(A[root], root, Ms), envs, self._top)
         return new
 
     def update_hamiltonian(self):

@@ -108,10 +108,12 @@ def effective_single_site_evolution(state_tensor, state_node, hamiltonian_tensor
                                     mode: TimeEvoMode = TimeEvoMode.KRYLOV,
                                     forward: EvoDirection = EvoDirection.FORWARD, **options) -> np.ndarray:
     """exp(-i dt H_eff) applied to ``state_tensor`` (``effective_time_evolution.py:257-324``):
-    the matrix-free Krylov exponential (options ``krylov_tol``, ``max_krylov_dim``;
-    the exact modes run it to machine precision); ``forward`` gives the sign of
-    the exponent as in the reference."""
-    from .tdvp import check_time_evo_mode
+    the matrix-free Krylov exponential (options ``krylov_tol``, ``max_krylov_dim``,
+    ``hermitian``; the exact modes run it to machine precision), or for RK45,
+    RK23 and DOP853 the adaptive Runge-Kutta integration with ``solve_ivp``'s
+    options. ``forward`` gives the sign of the exponent as in the reference;
+    ``exp_factor`` replaces the forward factor -i (backward: its negation)."""
+    from .tdvp import check_time_evo_mode, ode_options
     options = check_time_evo_mode(mode, options, tensor_cache.net.precision)
     nid = _node_id(state_node)
     net = tensor_cache.net
@@ -120,13 +122,24 @@ def effective_single_site_evolution(state_tensor, state_node, hamiltonian_tensor
     if list(x.shape) != net.shape(nid):
         raise ValueError(f"tensor shape {tuple(x.shape)} does not match node {nid} {tuple(net.shape(nid))}")
     p = net.heff_plan(nid)
-    exp_factor = forward.exp_factor() if isinstance(forward, EvoDirection) else (-1j if forward else 1j)
+    is_forward = forward is EvoDirection.FORWARD if isinstance(forward, EvoDirection) else bool(forward)
+    override = options.get("exp_factor")
+    if override is None:
+        exp_factor = -1j if is_forward else 1j
+    else:
+        exp_factor = override if is_forward else -override
 
     def apply(xp, yp):
         p.run(xp, yp)
     out = torch.empty_like(x)
-    net.krylov.expm(x, apply, time_step_size, exp_factor, options.get("krylov_tol", 1e-10),
-                    options.get("max_krylov_dim"), out=out, tridiagonal=net.levels > 0)
+    ode = ode_options(mode, options)
+    if ode is not None:
+        from .ode import RungeKuttaSolver
+        RungeKuttaSolver(net.ws).integrate(x, apply, time_step_size, exp_factor, out=out, **ode)
+    else:
+        net.krylov.expm(x, apply, time_step_size, exp_factor, options.get("krylov_tol", 1e-10),
+                        options.get("max_krylov_dim"), hermitian=options.get("hermitian", True), out=out,
+                        tridiagonal=net.levels > 0)
     return _from_phys(st, nid, out.cpu().numpy())
 
 

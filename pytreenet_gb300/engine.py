@@ -634,6 +634,10 @@ class DeviceNetwork:
         self.ham = hamiltonian
         self.ws = Workspace(self.device)
         self.krylov = KrylovSolver(self.ws)
+        # explicit Runge-Kutta options ({"method": "RK45", "atol": ..., ...})
+        # when the local equations are integrated instead of exponentiated
+        self.ode: dict | None = None
+        self._rk = None
         state._finalise()
         self.t = {}
         for nid in state._order:
@@ -815,9 +819,20 @@ class DeviceNetwork:
             p.run(xp, yp)
             self.flops += p.flops
         x = self.t[nid]
-        self.krylov.expm(x, apply, dt, exp_factor, tol, maxdim, hermitian=hermitian, out=x,
-                         tridiagonal=self.levels > 0)
+        self.local_exp(x, apply, dt, exp_factor, tol, maxdim, hermitian, out=x)
         self.check_device_status()
+
+    def local_exp(self, x, apply, dt, exp_factor, tol, maxdim, hermitian=True, out=None):
+        """exp(exp_factor dt H) x for the operator ``apply``: the Krylov
+        exponential, or the adaptive Runge-Kutta integration of
+        y' = exp_factor H y when ``self.ode`` names an ODE method."""
+        if self.ode is not None:
+            if self._rk is None:
+                from .ode import RungeKuttaSolver
+                self._rk = RungeKuttaSolver(self.ws)
+            return self._rk.integrate(x, apply, dt, exp_factor, out=out, **self.ode)
+        return self.krylov.expm(x, apply, dt, exp_factor, tol, maxdim, hermitian=hermitian, out=out,
+                                tridiagonal=self.levels > 0)
 
     def check_device_status(self):
         st = self.ws.bufs.get("tc_status")
@@ -832,8 +847,7 @@ class DeviceNetwork:
         def apply(xp, yp):
             p.run(xp, yp)
             self.flops += p.flops
-        return self.krylov.expm(r, apply, dt, exp_factor, tol, maxdim, hermitian=hermitian, out=r,
-                                tridiagonal=self.levels > 0)
+        return self.local_exp(r, apply, dt, exp_factor, tol, maxdim, hermitian, out=r)
 
     # -- QR split and R absorption ---------------------------------------------------
     CHOLQR_MIN_ROWS = 8192
@@ -1368,8 +1382,7 @@ class DeviceNetwork:
         def apply(xp, yp):
             hp.run(xp, yp)
             self.flops += hp.flops
-        self.krylov.expm(x2, apply, dt, exp_factor, tol, maxdim, hermitian=hermitian, out=x2,
-                         tridiagonal=self.levels > 0)
+        self.local_exp(x2, apply, dt, exp_factor, tol, maxdim, hermitian, out=x2)
         self.check_device_status()
         s = self.svd_split(u, v, x2, svd)
         self.state.orthogonality_center_id = v

@@ -28,7 +28,10 @@ class TimeEvoMode(Enum):
     CHEBYSHEV, EXPM, CHEBYSHEV, SPARSE) build the N x N effective Hamiltonian
     in the reference; here they compute the same exp(-i dt H_eff) x
     matrix-free, with the Krylov stop at 1e-14 (1e-11 on the reduced-precision
-    path) and at most 64 vectors. The SciPy ODE modes are not provided."""
+    path) and at most 64 vectors. RK45, RK23 and DOP853 integrate the local
+    equation with the same adaptive explicit Runge-Kutta pairs and step
+    control as ``solve_ivp``, on device vectors (``ode.py``); BDF (implicit,
+    needs the N x N Jacobian) is not provided."""
     FASTEST = "fastest"
     EXPM = "expm"
     CHEBYSHEV = "chebyshev"
@@ -77,10 +80,13 @@ EXACT_MAX_KRYLOV_DIM = 64
 def check_time_evo_mode(mode, solver_options, precision: str = "plain"):
     """Validate the mode and options as the reference does and return the
     options the engine's Krylov exponential runs with."""
-    if mode in TimeEvoMode.scipy_modes():
+    if mode is TimeEvoMode.BDF:
         raise NotImplementedError(
-            f"time_evo_mode={mode}: the SciPy ODE solvers are not provided; use KRYLOV or an exact mode")
-    opts = TimeEvoMode.default_solver_options(mode)
+            f"time_evo_mode={mode}: the implicit BDF solver is not provided; use RK45, RK23, DOP853, "
+            "KRYLOV or an exact mode")
+    # the drivers hand the caller's options to the solver as they are: an ODE
+    # mode given none runs at solve_ivp's own tolerances (``ode_options``)
+    opts = {} if mode in TimeEvoMode.scipy_modes() else TimeEvoMode.default_solver_options(mode)
     opts.update(solver_options or {})
     bad = set(opts) - TimeEvoMode.valid_solver_options(mode)
     if bad:
@@ -88,6 +94,26 @@ def check_time_evo_mode(mode, solver_options, precision: str = "plain"):
     if mode.is_exact():
         opts = dict(opts, krylov_tol=EXACT_KRYLOV_TOL["plain" if precision == "plain" else "reduced"],
                     max_krylov_dim=EXACT_MAX_KRYLOV_DIM)
+    return opts
+
+
+ODE_OPTIONS = ("atol", "rtol", "max_step", "first_step")
+# solve_ivp's tolerances when the caller sets none
+ODE_DEFAULT_TOLERANCES = {"atol": 1e-6, "rtol": 1e-3}
+
+
+def ode_options(mode, solver_options) -> dict | None:
+    """The Runge-Kutta settings of an ODE mode (None for the exponential
+    modes): the method and the ``solve_ivp`` options that explicit methods
+    read (``jac``, ``lband`` and the like have no effect on them). The
+    reference's drivers pass their options to ``solve_ivp`` unchanged
+    (``time_evolution.py:595-615``), so tolerances not given are
+    ``solve_ivp``'s: atol 1e-6, rtol 1e-3."""
+    if mode not in TimeEvoMode.scipy_modes():
+        return None
+    opts = dict(ODE_DEFAULT_TOLERANCES)
+    opts.update({k: v for k, v in (solver_options or {}).items() if k in ODE_OPTIONS})
+    opts["method"] = mode.value
     return opts
 
 
@@ -383,6 +409,7 @@ class OneSiteTDVP(RunLoop):
         (``tdvp_algorithm.py:58-163``)."""
         self.state = self._initial_state.copy_structure()
         self.net = DeviceNetwork(self.state, self.hamiltonian, precision=self.precision)
+        self.net.ode = ode_options(self.config.time_evo_mode, self.solver_options)
         if self.state.orthogonality_center_id is None:
             self.net.canonical_form(self.update_path[0])
         else:

@@ -183,7 +183,7 @@ def heisenberg_fields(ptn, spec, fields, jxy=None, jz=None):
 
 
 def run_case(ptn, name, spec, tensors, ham_fn, dt, steps, order, tol, canonical_random=False, path_mode=None,
-             default_mode=False):
+             default_mode=False, ode_mode=None, ode_options=None):
     from pytreenet.time_evolution.time_evolution import TimeEvoMode
     from pytreenet.time_evolution.tdvp_algorithms.tdvp_algorithm import TDVPConfig
     from pytreenet.time_evolution.time_evo_util import PathFinderMode
@@ -202,6 +202,10 @@ def run_case(ptn, name, spec, tensors, ham_fn, dt, steps, order, tol, canonical_
     if default_mode:
         # TDVPConfig() runs the reference's default local exponential (FASTEST -> CHEBYSHEV)
         algo = cls(psi, H, dt, dt * steps, ops, config=TDVPConfig())
+    elif ode_mode is not None:
+        # a solve_ivp mode; ode_options None = the solver's own tolerances
+        algo = cls(psi, H, dt, dt * steps, ops, config=TDVPConfig(time_evo_mode=TimeEvoMode[ode_mode]),
+                   solver_options=None if ode_options is None else dict(ode_options))
     else:
         algo = cls(psi, H, dt, dt * steps, ops, config=cfg, solver_options={"krylov_tol": tol})
     rec = {"spec_ids": np.array([s[0] for s in spec]),
@@ -210,8 +214,10 @@ def run_case(ptn, name, spec, tensors, ham_fn, dt, steps, order, tol, canonical_
            "update_path": np.array(algo.update_path)}
     if path_mode is not None:
         rec["path_mode"] = path_mode
-    if default_mode:
+    if default_mode or ode_mode is not None:
         rec["time_evo_mode"] = str(algo.config.time_evo_mode.name)
+    for k, v in (ode_options or {}).items():
+        rec[f"solver_options/{k}"] = v
     for nid, t in tensors.items():
         rec[f"init/{nid}"] = t
     for nid, t in export_ttno(H, spec).items():
@@ -697,6 +703,24 @@ def default_mode_cases(ptn):
              lambda psi: tfim(ptn, spec, g=0.9), 0.05, 3, 2, 0.0, canonical_random=True, default_mode=True)
 
 
+def ode_cases(ptn):
+    """TDVP with the solve_ivp modes of ``TimeEvoMode`` (``time_evolution.py:595-615``):
+    RK45 at tight tolerances, DOP853 with no options (solve_ivp's rtol 1e-3,
+    atol 1e-6), RK23 at 1e-8."""
+    rng = np.random.default_rng(67)
+    spec = t_tree(3)
+    h = rng.uniform(-1, 1, size=len(spec))
+    run_case(ptn, "ttree3_heis_rk45_o1", spec, capped_state_tensors(spec, rng, 6),
+             lambda psi: heisenberg_fields(ptn, spec, h), 0.05, 3, 1, 0.0, canonical_random=True,
+             ode_mode="RK45", ode_options={"atol": 1e-10, "rtol": 1e-10})
+    spec = binary_tree(7)
+    run_case(ptn, "binary7_tfim_dop853_o2", spec, capped_state_tensors(spec, rng, 4),
+             lambda psi: tfim(ptn, spec, g=0.9), 0.3, 2, 2, 0.0, canonical_random=True, ode_mode="DOP853")
+    run_case(ptn, "binary7_tfim_rk23_o1", spec, capped_state_tensors(spec, rng, 4),
+             lambda psi: tfim(ptn, spec, g=0.7), 0.04, 2, 1, 0.0, canonical_random=True, ode_mode="RK23",
+             ode_options={"atol": 1e-8, "rtol": 1e-8})
+
+
 def heff_cases(ptn):
     """Dense effective site Hamiltonians from the reference's
     ``get_effective_single_site_hamiltonian`` (``contractions/effective_hamiltonians.py:133-157``)
@@ -882,6 +906,7 @@ def main(ref_root):
     run_results_case(ptn)
     zipup_cases(ptn)
     leaf_to_leaf_two_site_cases(ptn)
+    ode_cases(ptn)
 
 
 if __name__ == "__main__":

@@ -27,6 +27,7 @@ def load_case(name):
     }
     case["path_mode"] = str(d["path_mode"]) if "path_mode" in d.files else "LeafToRoot"
     case["time_evo_mode"] = str(d["time_evo_mode"]) if "time_evo_mode" in d.files else "KRYLOV"
+    case["solver_options"] = {k.split("/", 1)[1]: float(d[k]) for k in d.files if k.startswith("solver_options/")}
     case["tebd"] = bool(int(d["tebd"])) if "tebd" in d.files else False
     case["driven"] = "amp" in d.files
     if case["driven"]:
@@ -49,6 +50,8 @@ BUG_CASES = ["binary15_tfim_fixed_bug", "ternary2_xxz_fixed_bug"]
 ADAPTIVE_BUG_CASES = ["binary7_tfim_bug", "ternary2_xxz_bug"]
 L2L_CASES = ["ttree3_heis_l2l_o1", "binary15_tfim_l2l_o2"]
 DEFAULT_MODE_CASES = ["ttree3_heis_fastest_o1", "binary7_tfim_fastest_o2"]
+# TDVP with the solve_ivp modes (RK45, DOP853 with solve_ivp's own tolerances, RK23)
+ODE_CASES = ["ttree3_heis_rk45_o1", "binary7_tfim_dop853_o2", "binary7_tfim_rk23_o1"]
 
 
 def driven_ttno(case, t):
@@ -184,7 +187,7 @@ def run_one_site_case(name, precision="plain"):
     H = build_ttn(P.TTNO, c["spec"], c["ttno"])
     cls = P.FirstOrderOneSiteTDVP if c["order"] == 1 else P.SecondOrderOneSiteTDVP
     mode = P.TimeEvoMode[c["time_evo_mode"]]
-    opts = {"krylov_tol": c["krylov_tol"]} if mode is P.TimeEvoMode.KRYLOV else None
+    opts = {"krylov_tol": c["krylov_tol"]} if mode is P.TimeEvoMode.KRYLOV else (c["solver_options"] or None)
     algo = cls(st, H, c["dt"], c["dt"] * c["steps"], {},
                config=P.TDVPConfig(time_evo_mode=mode, main_path_mode=P.PathFinderMode[c["path_mode"]]),
                solver_options=opts, precision=precision)

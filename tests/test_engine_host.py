@@ -1011,3 +1011,50 @@ def test_ttn_structure_methods():
     assert np.allclose(st.to_dense(ids), 2 * v)
     with pytest.raises(ValueError):
         st.replace_tensor(leaf, np.zeros((1, 1)))
+
+
+@pytest.mark.parametrize("method", ["RK45", "RK23", "DOP853"])
+def test_engine_host_runge_kutta_matches_solve_ivp(monkeypatch, method):
+    """The device Runge-Kutta integration takes the same steps as
+    scipy.integrate.solve_ivp (same number of right-hand-side evaluations,
+    DOP853 less the three of its dense output) and lands on the same point,
+    forward and backward, at tight and at loose tolerances with a step cap."""
+    import torch
+    from scipy.integrate import solve_ivp
+    from pytreenet_gb300.engine import Workspace
+    from pytreenet_gb300.ode import RungeKuttaSolver
+    fake_ptn.install(monkeypatch)
+    rng = np.random.default_rng(5)
+    n = 40
+    A = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    Hm = (A + A.conj().T) / 2
+    x0 = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    Ht = torch.from_numpy(Hm)
+
+    def ap(a, b):
+        b.copy_(Ht @ a)
+    ap.takes_tensors = True
+    for ef, dt in ((-1j, 0.05), (1j, 0.2)):
+        for opts in ({"atol": 1e-10, "rtol": 1e-10}, {"atol": 1e-6, "rtol": 1e-3, "max_step": 0.02}):
+            ref = solve_ivp(lambda t, y: ef * (Hm @ y), (0, dt), x0, method=method, t_eval=[dt], **opts)
+            solver = RungeKuttaSolver(Workspace(torch.device("cpu")))
+            y = solver.integrate(torch.from_numpy(x0.copy()), ap, dt, ef, method, **opts).numpy()
+            assert np.abs(y - ref.y[:, 0]).max() < 1e-13 * np.abs(ref.y[:, 0]).max()
+            assert solver.evaluations[-1] == ref.nfev - (3 if method == "DOP853" else 0)
+
+
+def test_engine_host_ode_options_follow_the_reference():
+    """ODE modes: options pass through as given (solve_ivp's tolerances when
+    none), solver-only keys are dropped, BDF is refused."""
+    from pytreenet_gb300.tdvp import TimeEvoMode, check_time_evo_mode, ode_options
+    assert ode_options(TimeEvoMode.KRYLOV, {"krylov_tol": 1e-9}) is None
+    opts = check_time_evo_mode(TimeEvoMode.RK45, None)
+    assert opts == {}
+    assert ode_options(TimeEvoMode.RK45, opts) == {"atol": 1e-6, "rtol": 1e-3, "method": "RK45"}
+    o = ode_options(TimeEvoMode.DOP853, check_time_evo_mode(TimeEvoMode.DOP853, {"rtol": 1e-9, "jac": None,
+                                                                                 "hermitian": True}))
+    assert o == {"atol": 1e-6, "rtol": 1e-9, "method": "DOP853"}
+    with pytest.raises(NotImplementedError):
+        check_time_evo_mode(TimeEvoMode.BDF, None)
+    with pytest.raises(ValueError):
+        check_time_evo_mode(TimeEvoMode.RK23, {"krylov_tol": 1e-9})

@@ -76,6 +76,18 @@ def test_gpu_leaf_to_leaf_path(name):
     assert one_minus_f < 1e-12
 
 
+@pytest.mark.parametrize("name", ["ttree3_heis_rk45_o1", "binary7_tfim_dop853_o2", "binary7_tfim_rk23_o1"])
+def test_gpu_ode_modes(name):
+    """RK45 / DOP853 / RK23 (the solve_ivp modes) on the GB300 against the
+    reference: the same adaptive steps on device vectors. The exact evolution
+    differs from these fixtures by 1e-9 to 1e-7 in <Z>, far above the bound."""
+    from golden_util import run_one_site_case
+    c, st, zerr = run_one_site_case(name)
+    one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), st)
+    assert zerr < 1e-11
+    assert one_minus_f < 1e-12
+
+
 @pytest.mark.parametrize("name", ["ttree3_heis_fastest_o1", "binary7_tfim_fastest_o2"])
 def test_gpu_default_mode(name):
     """TDVPConfig() (FASTEST) on the GB300 against the reference's dense exponential."""

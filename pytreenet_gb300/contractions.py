@@ -47,18 +47,32 @@ class SandwichCache:
         rec(node_id, None)
         return cache
 
+    @classmethod
+    def of_network(cls, net: DeviceNetwork, hamiltonian=None) -> "SandwichCache":
+        """The environments a driver's device network holds, as a cache (the
+        drivers' ``partial_tree_cache``); no buffers are copied."""
+        cache = cls.__new__(cls)
+        cache.state = net.state
+        cache.hamiltonian = hamiltonian
+        cache.net = net
+        cache._valid = None
+        return cache
+
     def update_tree_cache(self, node_id: str, next_node_id: str):
         """Recompute E(node_id -> next_node_id) from the current tensors
         (``sandwich_caching.py:79-95``)."""
         self.net.update_env(node_id, next_node_id)
-        self._valid.add((node_id, next_node_id))
+        if self._valid is not None:
+            self._valid.add((node_id, next_node_id))
 
     def __contains__(self, key) -> bool:
+        if self._valid is None:
+            return tuple(key) in self.net.env
         return tuple(key) in self._valid
 
     def get_entry(self, node_id: str, next_node_id: str) -> np.ndarray:
         """E(node_id -> next_node_id) as a NumPy array with legs (ket, ham, bra)."""
-        if (node_id, next_node_id) not in self._valid:
+        if (node_id, next_node_id) not in self:
             raise KeyError(f"no cached environment from {node_id} to {next_node_id}")
         return self.net.env_buf(node_id, next_node_id).detach().cpu().numpy()
 

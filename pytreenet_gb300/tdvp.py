@@ -431,6 +431,19 @@ class OneSiteTDVP(RunLoop):
             self.hamiltonian.reset()
         self._setup_state()
 
+    @property
+    def partial_tree_cache(self):
+        """The environments of the sweep (``TDVPAlgorithm.partial_tree_cache``,
+        ``tdvp_algorithm.py:108,156-163``) as a ``SandwichCache`` over the
+        device buffers."""
+        from .contractions import SandwichCache
+        return SandwichCache.of_network(self.net, self.hamiltonian)
+
+    def update_tree_cache(self, node_id: str, next_node_id: str):
+        """``TDVPAlgorithm.update_tree_cache`` (``tdvp_algorithm.py:165-182``):
+        E(node_id -> next_node_id) from the current tensors."""
+        self.net.update_env(node_id, next_node_id)
+
     # -- Krylov options ------------------------------------------------------------
     def _kry(self):
         o = self.solver_options

@@ -1058,3 +1058,32 @@ def test_engine_host_ode_options_follow_the_reference():
         check_time_evo_mode(TimeEvoMode.BDF, None)
     with pytest.raises(ValueError):
         check_time_evo_mode(TimeEvoMode.RK23, {"krylov_tol": 1e-9})
+
+
+def test_engine_host_partial_tree_cache_matches_oracle(monkeypatch):
+    """``partial_tree_cache`` exposes the sweep's environments: after a
+    first-order step every environment the oracle's sweep holds is there, legs
+    (ket, ham, bra), equal to rounding; ``update_tree_cache`` recomputes one."""
+    import oracle as O
+    from golden_util import build_ttn, load_case, oracle_state
+    fake_ptn.install(monkeypatch)
+    import pytreenet_gb300 as P
+    c = load_case("ttree3_heis_chi6_o1")
+    st = build_ttn(P.TTNS, c["spec"], c["init"])
+    H = build_ttn(P.TTNO, c["spec"], c["ttno"])
+    algo = P.FirstOrderOneSiteTDVP(st, H, c["dt"], c["dt"], {}, config=P.TDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV),
+                                   solver_options={"krylov_tol": c["krylov_tol"]})
+    ref = O.FirstOrderOneSiteTDVPOracle(oracle_state(c), c["ttno"], c["dt"], krylov_tol=c["krylov_tol"])
+    algo.run_one_time_step()
+    ref.run_one_time_step()
+    cache = algo.partial_tree_cache
+    assert len(ref.envs) > 0
+    for (u, v), E in ref.envs.items():
+        assert (u, v) in cache
+        got = cache.get_entry(u, v)
+        assert got.shape == E.shape
+        assert np.abs(got - E).max() < 1e-10 * max(1.0, np.abs(E).max())
+    u, v = next(iter(ref.envs))
+    before = cache.get_entry(u, v)
+    algo.update_tree_cache(u, v)
+    assert np.abs(cache.get_entry(u, v) - before).max() < 1e-10 * max(1.0, np.abs(before).max())

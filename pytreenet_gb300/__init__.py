@@ -27,7 +27,14 @@ from .contractions import (SandwichCache, contract_ket_ham_with_envs, contract_a
                            get_effective_single_site_hamiltonian_nodes)
 from .adjoint import OneSiteTDVPAdjoint, coupling_gradient
 from .bug import BUG, BUGConfig, FixedBUG, FixedBUGConfig
-from .time_dep import TimeDependentTTNO, FactorUpdatable, DiscreetTimeTTNO
+from .time_dep import AbstractTimeDepTTNO, TimeDependentTTNO, FactorUpdatable, DiscreetTimeTTNO
+from .tdvp import OneSiteTDVP, TwoSiteTDVP, TTNTimeEvolutionConfig
+from .results import Results
+from .application import zipup
+from .local_evolution import krylov_exp_action, time_evolve
+from .functions import (TDVPUpdatePathFinder, bosonic_operators, canonical_form, completely_contract_tree,
+                        contract_two_ttns, expectation_value, hadamard, multi_single_site_expectation_value,
+                        pauli_matrices, spin_jumps)
 
 __all__ = [
     "Node", "TreeTensorNetworkState", "TreeTensorNetworkOperator", "TTNS", "TTNO",
@@ -42,5 +49,9 @@ __all__ = [
     "SandwichCache", "contract_ket_ham_with_envs", "contract_any", "effective_single_site_evolution",
     "get_effective_single_site_hamiltonian", "get_effective_single_site_hamiltonian_nodes",
     "OneSiteTDVPAdjoint", "coupling_gradient", "FixedBUG", "FixedBUGConfig", "BUG", "BUGConfig",
-    "TimeDependentTTNO", "FactorUpdatable", "DiscreetTimeTTNO",
+    "AbstractTimeDepTTNO", "TimeDependentTTNO", "FactorUpdatable", "DiscreetTimeTTNO",
+    "OneSiteTDVP", "TwoSiteTDVP", "TTNTimeEvolutionConfig", "Results", "zipup",
+    "krylov_exp_action", "time_evolve", "TDVPUpdatePathFinder", "bosonic_operators", "canonical_form",
+    "completely_contract_tree", "contract_two_ttns", "expectation_value", "hadamard",
+    "multi_single_site_expectation_value", "pauli_matrices", "spin_jumps",
 ]

@@ -1087,3 +1087,78 @@ def test_engine_host_partial_tree_cache_matches_oracle(monkeypatch):
     before = cache.get_entry(u, v)
     algo.update_tree_cache(u, v)
     assert np.abs(cache.get_entry(u, v) - before).max() < 1e-10 * max(1.0, np.abs(before).max())
+
+
+def test_engine_host_time_evolve_and_krylov_exp_action(monkeypatch):
+    """``time_evolve`` on a dense matrix in every mode family against SciPy
+    (expm for the exact and Krylov modes, solve_ivp with the mode defaults for
+    RK45), forward and backward; ``krylov_exp_action`` with a NumPy action
+    and with a torch action."""
+    import scipy.linalg
+    import torch
+    from scipy.integrate import solve_ivp
+    fake_ptn.install(monkeypatch)
+    from pytreenet_gb300.local_evolution import krylov_exp_action, time_evolve
+    from pytreenet_gb300.tdvp import EvoDirection, TimeEvoMode
+    rng = np.random.default_rng(9)
+    n = 30
+    A = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    H = (A + A.conj().T) / 2
+    psi = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    psi /= np.linalg.norm(psi)
+    dt = 0.1
+    for fwd, f in ((EvoDirection.FORWARD, -1j), (EvoDirection.BACKWARD, 1j)):
+        exact = scipy.linalg.expm(f * dt * H) @ psi
+        for mode in (TimeEvoMode.FASTEST, TimeEvoMode.EXPM, TimeEvoMode.SPARSE):
+            assert np.abs(time_evolve(psi, H, dt, forward=fwd, mode=mode) - exact).max() < 1e-12
+        got = time_evolve(psi, H, dt, forward=fwd, mode=TimeEvoMode.KRYLOV, krylov_tol=1e-13)
+        assert np.abs(got - exact).max() < 1e-11
+        ref = solve_ivp(lambda t, y: f * (H @ y), (0, dt), psi, method="RK45", t_eval=[dt],
+                        atol=1e-10, rtol=1e-10).y[:, 0]
+        assert np.abs(time_evolve(psi, H, dt, forward=fwd, mode=TimeEvoMode.RK45) - ref).max() < 1e-13
+    # a real exp_factor override: a diffusion-like flow exp(-dt H)
+    got = time_evolve(psi, H, dt, mode=TimeEvoMode.EXPM, exp_factor=-1.0)
+    assert np.abs(got - scipy.linalg.expm(-dt * H) @ psi).max() < 1e-12
+    exact = scipy.linalg.expm(-1j * dt * H) @ psi
+    got = krylov_exp_action(psi.reshape(5, 6), lambda y: (H @ y.reshape(-1)).reshape(5, 6), dt, -1j,
+                            krylov_tol=1e-13)
+    assert got.shape == (5, 6) and np.abs(got.reshape(-1) - exact).max() < 1e-11
+    Ht = torch.from_numpy(H)
+    got = krylov_exp_action(torch.from_numpy(psi.copy()), lambda y: Ht @ y, dt, -1j, krylov_tol=1e-13)
+    assert isinstance(got, torch.Tensor) and np.abs(got.numpy() - exact).max() < 1e-11
+    with pytest.raises(ValueError):
+        time_evolve(psi, H[:5, :5], dt)
+    with pytest.raises(NotImplementedError):
+        time_evolve(psi, H, dt, mode=TimeEvoMode.BDF)
+
+
+def test_engine_host_module_functions(monkeypatch):
+    """Module-level functions with PyTreeNet's names: expectation_value gives
+    the reference's final energy, contract_two_ttns is the bilinear product
+    of the dense vectors, TDVPUpdatePathFinder's default (LeafToLeaf) gives the
+    reference's leaf-to-leaf path, the operator helpers their matrices."""
+    from golden_util import build_ttn, load_case
+    fake_ptn.install(monkeypatch)
+    import pytreenet_gb300 as P
+    c = load_case("ttree3_heis_chi6_o1")
+    final = build_ttn(P.TTNS, c["spec"], c["final"])
+    H = build_ttn(P.TTNO, c["spec"], c["ttno"])
+    assert abs(P.expectation_value(final, H) - c["energy_final"]) < 1e-10
+    a = build_ttn(P.TTNS, c["spec"], c["init"])
+    b = build_ttn(P.TTNS, c["spec"], c["final"])
+    order = [nid for nid, _ in c["spec"]]
+    va, vb = a.to_dense(order), b.to_dense(order)
+    assert abs(P.contract_two_ttns(a, b) - np.sum(va * vb)) < 1e-12
+    assert abs(P.contract_two_ttns(a, b) - a.scalar_product(b)) > 1e-3   # no conjugation
+    l2l = load_case("ttree3_heis_l2l_o1")
+    st = build_ttn(P.TTNS, l2l["spec"], l2l["init"])
+    assert P.TDVPUpdatePathFinder(st).find_path() == l2l["update_path"]
+    assert P.TDVPUpdatePathFinder(st, P.PathFinderMode.LeafToRoot).find_path() == \
+        P.leaf_to_root_update_path(st)
+    X, Y, Z = P.pauli_matrices()
+    assert np.allclose(X @ Y, 1j * Z)
+    sp, sm = P.spin_jumps()
+    assert np.allclose(sp, [[0, 1], [0, 0]]) and np.allclose(sm, [[0, 0], [1, 0]])
+    cr, an, num = P.bosonic_operators(4)
+    assert np.allclose(np.diag(num), [0, 1, 2, 3]) and np.isclose(cr[2, 1], np.sqrt(2)) and np.allclose(an, cr.T)
+    assert np.allclose(P.hadamard() @ P.hadamard(), np.eye(2))

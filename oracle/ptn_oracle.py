@@ -1022,8 +1022,8 @@ class _TwoSiteBase(_OneSiteBase):
     """``TwoSiteTDVP`` (``tdvp_algorithms/twositetdvp.py:29-146``)."""
 
     def __init__(self, state: OState, W: dict, dt: float, svd: SVDParams, krylov_tol=1e-10,
-                 max_krylov_dim=None, path_mode: str = "LeafToRoot"):
-        super().__init__(state, W, dt, krylov_tol, max_krylov_dim, path_mode=path_mode)
+                 max_krylov_dim=None, path_mode: str = "LeafToRoot", ode: dict | None = None):
+        super().__init__(state, W, dt, krylov_tol, max_krylov_dim, path_mode=path_mode, ode=ode)
         self.svd = svd
         self.bond_history = []
 

@@ -131,10 +131,13 @@ class RungeKuttaSolver:
                 out.copy_(x)
             return out
         ef = complex(exp_factor)
+        # a negative dt integrates backward from 0 to dt, as solve_ivp does
+        direction = 1.0 if t_bound > 0 else -1.0
+        interval = abs(t_bound)
         H(S[0], S[1])
         # initial step (Hairer, Norsett & Wanner II.4; SciPy's select_initial_step)
         if first_step is not None:
-            if first_step <= 0 or first_step > abs(t_bound):
+            if first_step <= 0 or first_step > interval:
                 raise ValueError("`first_step` must be positive and not exceed the interval")
             h_abs = float(first_step)
         else:
@@ -143,24 +146,26 @@ class RungeKuttaSolver:
             scale = atol + y0.abs() * rtol
             d0, d1 = self._rms(y0, scale), self._rms(f0, scale)
             h0 = 1e-6 if (d0 < 1e-5 or d1 < 1e-5) else 0.01 * d0 / d1
-            h0 = min(h0, t_bound)
-            self._combine(S[:2], [1.0, h0 * ef], tmp)
+            h0 = min(h0, interval)
+            self._combine(S[:2], [1.0, h0 * direction * ef], tmp)
             H(tmp, ynew)
             d2 = self._rms((ynew - S[1]) * ef, scale) / h0
             if d1 <= 1e-15 and d2 <= 1e-15:
                 h1 = max(1e-6, h0 * 1e-3)
             else:
                 h1 = (0.01 / max(d1, d2)) ** (1.0 / (tab.order + 1))
-            h_abs = min(100 * h0, h1, t_bound, max_step)
+            h_abs = min(100 * h0, h1, interval, max_step)
         accepted_steps = 0
-        while t < t_bound:
-            min_step = 10 * abs(np.nextafter(t, np.inf) - t)
+        while direction * (t - t_bound) < 0:
+            min_step = 10 * abs(np.nextafter(t, direction * np.inf) - t)
             h_abs = min(max(h_abs, min_step), max_step)
             rejected = False
             while True:
                 if h_abs < min_step:
                     raise _lib.PtnError(3, f"{method}: required step size is less than spacing between numbers")
-                t_new = min(t + h_abs, t_bound)
+                t_new = t + h_abs * direction
+                if direction * (t_new - t_bound) > 0:
+                    t_new = t_bound
                 h = t_new - t
                 h_abs = abs(h)
                 for i in range(1, s):

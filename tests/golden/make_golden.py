@@ -249,7 +249,7 @@ def neel_state_tensors(spec):
 
 
 def run_case_two_site(ptn, name, spec, tensors, ham_fn, dt, steps, tol, svd, canonical_random=False,
-                      path_mode=None):
+                      path_mode=None, ode_mode=None, ode_options=None):
     """Second-order two-site TDVP (``secondordertwosite.py``) with truncation ``svd``
     = (max_bond_dim, rel_tol, total_tol, renorm)."""
     from pytreenet.time_evolution.time_evolution import TimeEvoMode
@@ -268,10 +268,12 @@ def run_case_two_site(ptn, name, spec, tensors, ham_fn, dt, steps, tol, svd, can
     if path_mode is not None:
         from pytreenet.time_evolution.time_evo_util import PathFinderMode
         extra["main_path_mode"] = PathFinderMode[path_mode]
-    cfg = TwoSiteTDVPConfig(time_evo_mode=TimeEvoMode.KRYLOV, max_bond_dim=maxd, rel_tol=rel,
+    mode = TimeEvoMode.KRYLOV if ode_mode is None else TimeEvoMode[ode_mode]
+    cfg = TwoSiteTDVPConfig(time_evo_mode=mode, max_bond_dim=maxd, rel_tol=rel,
                             total_tol=tot, renorm=renorm, **extra)
     algo = SecondOrderTwoSiteTDVP(psi, H, dt, dt * steps, ops, config=cfg,
-                                  solver_options={"krylov_tol": tol})
+                                  solver_options={"krylov_tol": tol} if ode_mode is None else
+                                  (None if ode_options is None else dict(ode_options)))
     rec = {"spec_ids": np.array([s[0] for s in spec]),
            "spec_parents": np.array(["" if s[1] is None else s[1] for s in spec]),
            "dt": dt, "steps": steps, "order": 2, "krylov_tol": tol,
@@ -279,6 +281,10 @@ def run_case_two_site(ptn, name, spec, tensors, ham_fn, dt, steps, tol, svd, can
            "svd_renorm": int(renorm), "update_path": np.array(algo.update_path)}
     if path_mode is not None:
         rec["path_mode"] = path_mode
+    if ode_mode is not None:
+        rec["time_evo_mode"] = ode_mode
+    for k, v in (ode_options or {}).items():
+        rec[f"solver_options/{k}"] = v
     for nid, t in tensors.items():
         rec[f"init/{nid}"] = t
     for nid, t in export_ttno(H, spec).items():
@@ -719,6 +725,11 @@ def ode_cases(ptn):
     run_case(ptn, "binary7_tfim_rk23_o1", spec, capped_state_tensors(spec, rng, 4),
              lambda psi: tfim(ptn, spec, g=0.7), 0.04, 2, 1, 0.0, canonical_random=True, ode_mode="RK23",
              ode_options={"atol": 1e-8, "rtol": 1e-8})
+    # second-order two-site TDVP with RK45 and bond growth under truncation
+    h = rng.uniform(-1, 1, size=len(spec))
+    run_case_two_site(ptn, "binary7_heis_2tdvp_rk45", spec, random_state_tensors(spec, rng, 2),
+                      lambda psi: heisenberg_fields(ptn, spec, h), 0.05, 2, 0.0, (6, 1e-10, 1e-10, False),
+                      canonical_random=True, ode_mode="RK45", ode_options={"atol": 1e-10, "rtol": 1e-10})
 
 
 def heff_cases(ptn):

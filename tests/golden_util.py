@@ -43,7 +43,24 @@ def load_case(name):
 
 CASES = ["c1_binary15_tfim_chi8", "binary7_tfim_chi4_o2", "ttree3_heis_chi6_o1",
          "ttree3_heis_chi6_o2", "ternary2_xxz_chi4_o1"]
-TWO_SITE_CASES = ["ternary2_xxz_neel_2tdvp", "binary7_heis_2tdvp_trunc", "binary7_heis_2tdvp_l2l"]
+TWO_SITE_CASES = ["ternary2_xxz_neel_2tdvp", "binary7_heis_2tdvp_trunc", "binary7_heis_2tdvp_l2l",
+                  "binary7_heis_2tdvp_rk45"]
+ODE_MODES = ("RK45", "RK23", "DOP853")
+
+
+def case_solver(c, P):
+    """(TimeEvoMode, solver_options) of a fixture for the engine's drivers."""
+    mode = P.TimeEvoMode[c["time_evo_mode"]]
+    if mode is P.TimeEvoMode.KRYLOV:
+        return mode, {"krylov_tol": c["krylov_tol"]}
+    return mode, (c["solver_options"] or None)
+
+
+def oracle_ode(c):
+    """The oracle's ``ode`` argument for a fixture run with a solve_ivp mode."""
+    if c["time_evo_mode"] not in ODE_MODES:
+        return None
+    return dict(c["solver_options"], method=c["time_evo_mode"])
 TEBD_CASES = ["binary7_tfim_tebd", "binary7_tfim_tebd_swaps", "binary7_tfim_tebd_strang"]
 DRIVEN_CASES = ["binary7_tfim_driven_o1", "binary7_tfim_driven_o2"]
 BUG_CASES = ["binary15_tfim_fixed_bug", "ternary2_xxz_fixed_bug"]

@@ -101,7 +101,7 @@ def test_engine_host_cholqr2_split(monkeypatch):
 # ---------------------------------------------------------------------------
 # two-site TDVP (truncated SVD split) on the fake library
 # ---------------------------------------------------------------------------
-from golden_util import TWO_SITE_CASES  # noqa: E402
+from golden_util import TWO_SITE_CASES, case_solver  # noqa: E402
 
 
 def _run_two_site(name, precision="plain", order=2, dt=None, steps=None):
@@ -109,12 +109,12 @@ def _run_two_site(name, precision="plain", order=2, dt=None, steps=None):
     c = load_case(name)
     st = build_ttn(P.TTNS, c["spec"], c["init"])
     H = build_ttn(P.TTNO, c["spec"], c["ttno"])
-    cfg = P.TwoSiteTDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV, main_path_mode=P.PathFinderMode[c["path_mode"]],
+    mode, opts = case_solver(c, P)
+    cfg = P.TwoSiteTDVPConfig(time_evo_mode=mode, main_path_mode=P.PathFinderMode[c["path_mode"]],
                               **c["svd"])
     cls = P.SecondOrderTwoSiteTDVP if order == 2 else P.FirstOrderTwoSiteTDVP
     dt = c["dt"] if dt is None else dt
-    algo = cls(st, H, dt, dt * c["steps"], {}, config=cfg,
-               solver_options={"krylov_tol": c["krylov_tol"]}, precision=precision)
+    algo = cls(st, H, dt, dt * c["steps"], {}, config=cfg, solver_options=opts, precision=precision)
     assert algo.update_path == c["update_path"]
     zs = []
     for k in range(c["steps"] if steps is None else steps):
@@ -1018,7 +1018,9 @@ def test_engine_host_runge_kutta_matches_solve_ivp(monkeypatch, method):
     """The device Runge-Kutta integration takes the same steps as
     scipy.integrate.solve_ivp (same number of right-hand-side evaluations,
     DOP853 less the three of its dense output) and lands on the same point,
-    forward and backward, at tight and at loose tolerances with a step cap."""
+    for either sign of the exponent factor and of dt (a negative dt integrates
+    backward, as the two-site sweeps' backward site updates do), at tight and
+    at loose tolerances with a step cap."""
     import torch
     from scipy.integrate import solve_ivp
     from pytreenet_gb300.engine import Workspace
@@ -1034,7 +1036,7 @@ def test_engine_host_runge_kutta_matches_solve_ivp(monkeypatch, method):
     def ap(a, b):
         b.copy_(Ht @ a)
     ap.takes_tensors = True
-    for ef, dt in ((-1j, 0.05), (1j, 0.2)):
+    for ef, dt in ((-1j, 0.05), (1j, 0.2), (-1j, -0.1)):
         for opts in ({"atol": 1e-10, "rtol": 1e-10}, {"atol": 1e-6, "rtol": 1e-3, "max_step": 0.02}):
             ref = solve_ivp(lambda t, y: ef * (Hm @ y), (0, dt), x0, method=method, t_eval=[dt], **opts)
             solver = RungeKuttaSolver(Workspace(torch.device("cpu")))

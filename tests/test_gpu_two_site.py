@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from golden_util import TWO_SITE_CASES, build_ttn, load_case, oracle_state, fidelity_and_dist
+from golden_util import TWO_SITE_CASES, build_ttn, case_solver, load_case, oracle_state, fidelity_and_dist
 
 pytestmark = pytest.mark.gpu
 Zm = np.diag([1.0, -1.0]).astype(complex)
@@ -97,10 +97,11 @@ def _run_two_site(name, precision="plain"):
     c = load_case(name)
     st = build_ttn(P.TTNS, c["spec"], c["init"])
     H = build_ttn(P.TTNO, c["spec"], c["ttno"])
-    cfg = P.TwoSiteTDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV, main_path_mode=P.PathFinderMode[c["path_mode"]],
+    mode, opts = case_solver(c, P)
+    cfg = P.TwoSiteTDVPConfig(time_evo_mode=mode, main_path_mode=P.PathFinderMode[c["path_mode"]],
                               **c["svd"])
     algo = P.SecondOrderTwoSiteTDVP(st, H, c["dt"], c["dt"] * c["steps"], {}, config=cfg,
-                                    solver_options={"krylov_tol": c["krylov_tol"]}, precision=precision)
+                                    solver_options=opts, precision=precision)
     zs = []
     for k in range(c["steps"]):
         algo.run_one_time_step()

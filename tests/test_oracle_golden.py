@@ -72,7 +72,7 @@ def test_update_path_and_orth_paths():
 # ---------------------------------------------------------------------------
 # two-site TDVP and truncation
 # ---------------------------------------------------------------------------
-from golden_util import TWO_SITE_CASES  # noqa: E402
+from golden_util import TWO_SITE_CASES, oracle_ode  # noqa: E402
 
 
 def test_oracle_truncation_known_answers():
@@ -94,7 +94,7 @@ def test_oracle_two_site_cases(name):
     c = load_case(name)
     st = oracle_state(c)
     algo = O.SecondOrderTwoSiteTDVPOracle(st, c["ttno"], c["dt"], O.SVDParams(**c["svd"]),
-                                          krylov_tol=c["krylov_tol"], path_mode=c["path_mode"])
+                                          krylov_tol=c["krylov_tol"], path_mode=c["path_mode"], ode=oracle_ode(c))
     assert algo.update_path == c["update_path"]
     zerr = 0.0
     for k in range(c["steps"]):

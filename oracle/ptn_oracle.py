@@ -643,6 +643,14 @@ def _in_new_child_bases(T, tree, nid, Ms):
     return T
 
 
+def _bug_exp(x, action, dt, setting):
+    """exp(-i dt H) x for a BUG node: ``setting`` is a Krylov tolerance, or
+    the ``solve_ivp`` arguments (method and options) of an ODE mode."""
+    if isinstance(setting, dict):
+        return ode_exp_action(x, action, dt, -1j, **setting)
+    return krylov_exp_action(x, action, dt, -1j, krylov_tol=setting)
+
+
 def _bug_update_node(c, P, envs_p, tree, W, dt, tol, child_tol):
     """``update_node`` / ``update_leaf_node`` / ``update_non_leaf_node``
     (``time_evo_util/common_bug.py:47-309``) with fixed rank. ``P`` has its
@@ -668,7 +676,7 @@ def _bug_update_node(c, P, envs_p, tree, W, dt, tol, child_tol):
     for g, b in blocks.items():
         envs[(g, c)] = b
     x = _in_new_child_bases(cur[c], tree, c, Ms)
-    upd = krylov_exp_action(x, lambda y: heff_apply(y, tree, c, W[c], envs), dt, -1j, krylov_tol=tol)
+    upd = _bug_exp(x, lambda y: heff_apply(y, tree, c, W[c], envs), dt, tol)
     U = _bug_basis(upd)
     old = _in_new_child_bases(P[c], tree, c, Ms)
     legs = list(range(1, U.ndim))
@@ -779,12 +787,17 @@ def adaptive_bug_step(state: OState, W: dict, dt: float, svd: SVDParams, krylov_
     return out
 
 
-def fixed_bug_step(state: OState, W: dict, dt: float, krylov_tol=1e-10, default_tol=1e-10) -> OState:
+def fixed_bug_step(state: OState, W: dict, dt: float, krylov_tol=1e-10, default_tol=1e-10,
+                   ode: dict | None = None) -> OState:
     """One step of ``FixedBUG`` (``time_evolution/fixed_bug.py:83-97``,
     ``root_update`` in ``time_evo_util/common_bug.py:311-378``): every child of
     the root updates its subtree recursively from the current state, then the
     root tensor, expressed in the children's new bases, evolves by dt in the
-    new environments. The state must have its orthogonality centre at the root."""
+    new environments. The state must have its orthogonality centre at the root.
+    ``ode`` (``solve_ivp`` method and options) selects an ODE mode; nodes below
+    the root's children then run it with ``solve_ivp``'s own tolerances."""
+    if ode is not None:
+        krylov_tol, default_tol = ode, {"method": ode["method"]}
     tree = state.tree
     root = tree.root
     assert state.orth_center == root
@@ -796,8 +809,7 @@ def fixed_bug_step(state: OState, W: dict, dt: float, krylov_tol=1e-10, default_
     for c, b in blocks.items():
         envs[(c, root)] = b
     x = _in_new_child_bases(state.tensors[root], tree, root, Ms)
-    new[root] = krylov_exp_action(x, lambda y: heff_apply(y, tree, root, W[root], envs), dt, -1j,
-                                  krylov_tol=krylov_tol)
+    new[root] = _bug_exp(x, lambda y: heff_apply(y, tree, root, W[root], envs), dt, krylov_tol)
     out = OState(tree, new)
     out.orth_center = root
     return out

@@ -579,9 +579,10 @@ def capped_state_tensors(spec, rng, chi):
     return out
 
 
-def run_case_bug(ptn, name, spec, tensors, ham_fn, dt, steps, tol):
+def run_case_bug(ptn, name, spec, tensors, ham_fn, dt, steps, tol, ode_mode=None, ode_options=None):
     """The reference's fixed-rank BUG (``time_evolution/fixed_bug.py``,
-    ``time_evo_util/common_bug.py``) with KRYLOV local exponentials."""
+    ``time_evo_util/common_bug.py``) with KRYLOV local exponentials, or a
+    solve_ivp mode (``ode_mode``) with ``ode_options``."""
     from pytreenet.time_evolution.time_evolution import TimeEvoMode
     from pytreenet.time_evolution.fixed_bug import FixedBUG, FixedBUGConfig
     psi = build_reference_state(ptn, spec, tensors)
@@ -591,12 +592,20 @@ def run_case_bug(ptn, name, spec, tensors, ham_fn, dt, steps, tol):
     psi = build_reference_state(ptn, spec, tensors)
     H = ptn.TTNO.from_hamiltonian(ham_fn(psi), psi)
     ops = {nid: ptn.TensorProduct({nid: Z}) for nid, _ in spec}
-    algo = FixedBUG(psi, H, dt, dt * steps, ops, config=FixedBUGConfig(time_evo_mode=TimeEvoMode.KRYLOV),
-                    solver_options={"krylov_tol": tol})
+    if ode_mode is None:
+        algo = FixedBUG(psi, H, dt, dt * steps, ops, config=FixedBUGConfig(time_evo_mode=TimeEvoMode.KRYLOV),
+                        solver_options={"krylov_tol": tol})
+    else:
+        algo = FixedBUG(psi, H, dt, dt * steps, ops, config=FixedBUGConfig(time_evo_mode=TimeEvoMode[ode_mode]),
+                        solver_options=None if ode_options is None else dict(ode_options))
     rec = {"spec_ids": np.array([s[0] for s in spec]),
            "spec_parents": np.array(["" if s[1] is None else s[1] for s in spec]),
            "dt": dt, "steps": steps, "order": 1, "krylov_tol": tol, "bug": 1,
            "update_path": np.array([])}
+    if ode_mode is not None:
+        rec["time_evo_mode"] = ode_mode
+    for k, v in (ode_options or {}).items():
+        rec[f"solver_options/{k}"] = v
     for nid, t in tensors.items():
         rec[f"init/{nid}"] = t
     for nid, t in export_ttno(H, spec).items():
@@ -730,6 +739,12 @@ def ode_cases(ptn):
     run_case_two_site(ptn, "binary7_heis_2tdvp_rk45", spec, random_state_tensors(spec, rng, 2),
                       lambda psi: heisenberg_fields(ptn, spec, h), 0.05, 2, 0.0, (6, 1e-10, 1e-10, False),
                       canonical_random=True, ode_mode="RK45", ode_options={"atol": 1e-10, "rtol": 1e-10})
+    # fixed-rank BUG with RK45: the root and its children at 1e-10, deeper
+    # nodes at solve_ivp's own tolerances (the reference passes no options there)
+    spec = binary_tree(15)
+    run_case_bug(ptn, "binary15_tfim_fixed_bug_rk45", spec, capped_state_tensors(spec, rng, 4),
+                 lambda psi: tfim(ptn, spec, g=0.6), 0.1, 2, 0.0, ode_mode="RK45",
+                 ode_options={"atol": 1e-10, "rtol": 1e-10})
 
 
 def heff_cases(ptn):

@@ -63,7 +63,7 @@ def oracle_ode(c):
     return dict(c["solver_options"], method=c["time_evo_mode"])
 TEBD_CASES = ["binary7_tfim_tebd", "binary7_tfim_tebd_swaps", "binary7_tfim_tebd_strang"]
 DRIVEN_CASES = ["binary7_tfim_driven_o1", "binary7_tfim_driven_o2"]
-BUG_CASES = ["binary15_tfim_fixed_bug", "ternary2_xxz_fixed_bug"]
+BUG_CASES = ["binary15_tfim_fixed_bug", "ternary2_xxz_fixed_bug", "binary15_tfim_fixed_bug_rk45"]
 ADAPTIVE_BUG_CASES = ["binary7_tfim_bug", "ternary2_xxz_bug"]
 L2L_CASES = ["ttree3_heis_l2l_o1", "binary15_tfim_l2l_o2"]
 DEFAULT_MODE_CASES = ["ttree3_heis_fastest_o1", "binary7_tfim_fastest_o2"]
@@ -182,9 +182,9 @@ def run_bug_case(name):
     st = build_ttn(P.TTNS, c["spec"], c["init"])
     H = build_ttn(P.TTNO, c["spec"], c["ttno"])
     Zm = np.diag([1.0, -1.0]).astype(complex)
-    algo = FixedBUG(st, H, c["dt"], c["dt"] * c["steps"], {},
-                    config=FixedBUGConfig(time_evo_mode=P.TimeEvoMode.KRYLOV),
-                    solver_options={"krylov_tol": c["krylov_tol"]})
+    mode, opts = case_solver(c, P)
+    algo = FixedBUG(st, H, c["dt"], c["dt"] * c["steps"], {}, config=FixedBUGConfig(time_evo_mode=mode),
+                    solver_options=opts)
     zs = []
     for _ in range(c["steps"]):
         algo.run_one_time_step()

@@ -17,6 +17,8 @@ PyTreeNet's module functions ``time_evolve`` and ``krylov_exp_action``
   one of the same shape. A NumPy action is the caller's host code (each
   Krylov step copies the vector to the host and back); an action written on
   torch tensors runs where they live and no copy is made.
+* ``TimeEvoMode.time_evolve_action`` / ``TimeEvoMode.time_evolve``: the
+  enum's methods, with the caller's options only.
 
 NumPy inputs give NumPy results, device tensors device tensors.
 """
@@ -77,24 +79,60 @@ def krylov_exp_action(psi, action, time_difference: float, exp_factor: complex, 
     return out.cpu().numpy() if was_numpy else out
 
 
-def time_evolve(psi, hamiltonian, time_difference: float, forward=EvoDirection.FORWARD,
-                mode: TimeEvoMode = TimeEvoMode.FASTEST, **options):
-    """psi(t +/- dt) = exp(-/+ i H dt) psi for a dense matrix H
-    (``time_evolve``, ``time_evolution.py:657-694``)."""
+def _exp_factor(forward, override) -> complex:
+    if isinstance(forward, bool):
+        forward = EvoDirection.from_bool(forward)
+    if override is None:
+        return forward.exp_factor()
+    return override if forward is EvoDirection.FORWARD else -override
+
+
+def time_evolve_action(mode: TimeEvoMode, psi, time_evo_action, time_difference: float,
+                       forward=EvoDirection.FORWARD, **options):
+    """``TimeEvoMode.time_evolve_action`` (``time_evolution.py:536-615``):
+    psi evolved under y' = c A(t) y with A given as ``time_evo_action(t, y)``
+    (NumPy or torch, as for ``krylov_exp_action``). KRYLOV calls it at t = 0;
+    the Runge-Kutta modes at their stage times. ``exp_factor`` and
+    ``hermitian`` are read here; options the mode does not read are ignored."""
+    options = dict(options)
+    exp_factor = _exp_factor(forward, options.pop("exp_factor", None))
+    hermitian = options.pop("hermitian", True)
+    if mode is TimeEvoMode.KRYLOV:
+        return krylov_exp_action(psi, lambda y: time_evo_action(0.0, y), time_difference, exp_factor,
+                                 krylov_tol=options.get("krylov_tol", 1e-10),
+                                 max_krylov_dim=options.get("max_krylov_dim"), hermitian=hermitian)
+    if not mode.is_scipy():
+        raise NotImplementedError("The time evolution via action is not implemented for this mode: "
+                                  + str(mode.value))
+    if mode is TimeEvoMode.BDF:
+        raise NotImplementedError("the implicit BDF solver is not provided")
+    x, was_numpy = _to_device(psi)
+    shape = tuple(x.shape)
+    _, rk = _solvers(x.device)
+    if was_numpy:
+        def ap(t, xq, w):
+            y = np.asarray(time_evo_action(t, xq.detach().cpu().numpy().reshape(shape)), dtype=np.complex128)
+            w.copy_(torch.from_numpy(np.ascontiguousarray(y).reshape(-1)).to(w.device))
+    else:
+        def ap(t, xq, w):
+            w.copy_(time_evo_action(t, xq.view(shape)).reshape(-1))
+    ap.takes_time = True
+    _tensor_action(ap)
+    out = torch.empty_like(x)
+    rk.integrate(x.reshape(-1), ap, time_difference, exp_factor, out=out.view(-1), **ode_options(mode, options))
+    return out.cpu().numpy() if was_numpy else out
+
+
+def evolve_dense(mode: TimeEvoMode, psi, hamiltonian, time_difference: float, forward, options: dict):
+    """``TimeEvoMode.time_evolve`` (``time_evolution.py:617-655``) for a dense
+    H with exactly the caller's options (an ODE mode given none runs at
+    ``solve_ivp``'s own tolerances); options the mode does not read are
+    ignored, as in the reference."""
     from .adjoint import _raw_contract
     if mode is TimeEvoMode.BDF:
         raise NotImplementedError("the implicit BDF solver is not provided")
-    opts = TimeEvoMode.default_solver_options(mode)
-    opts.update(options)
-    bad = set(opts) - TimeEvoMode.valid_solver_options(mode)
-    if bad:
-        raise ValueError(f"solver options {sorted(bad)} are not valid for {mode}")
-    is_forward = forward is EvoDirection.FORWARD if isinstance(forward, EvoDirection) else bool(forward)
-    override = opts.get("exp_factor")
-    if override is None:
-        exp_factor = -1j if is_forward else 1j
-    else:
-        exp_factor = override if is_forward else -override
+    opts = dict(options)
+    exp_factor = _exp_factor(forward, opts.pop("exp_factor", None))
     x, was_numpy = _to_device(psi)
     n = x.numel()
     Hd, _ = _to_device(hamiltonian)
@@ -121,3 +159,13 @@ def time_evolve(psi, hamiltonian, time_difference: float, forward=EvoDirection.F
                  None, hermitian=False, out=out)
     out = out.view(x.shape)
     return out.cpu().numpy() if was_numpy else out
+
+
+def time_evolve(psi, hamiltonian, time_difference: float, forward=EvoDirection.FORWARD,
+                mode: TimeEvoMode = TimeEvoMode.FASTEST, **options):
+    """psi(t +/- dt) = exp(-/+ i H dt) psi for a dense matrix H
+    (``time_evolve``, ``time_evolution.py:657-694``): the mode's default
+    options laid under the caller's."""
+    opts = TimeEvoMode.default_solver_options(mode)
+    opts.update(options)
+    return evolve_dense(mode, psi, hamiltonian, time_difference, forward, opts)

@@ -99,8 +99,10 @@ class RungeKuttaSolver:
                   first_step: float | None = None, out: torch.Tensor | None = None, **ignored) -> torch.Tensor:
         """y(dt) for y' = exp_factor H y, y(0) = x, where ``apply(xp, yp)``
         writes H applied to the vector at ``xp`` into ``yp`` (device pointers,
-        or tensors when ``apply.takes_tensors``). Options that SciPy ignores
-        for explicit methods (``jac``, ``lband``, ...) are accepted and ignored."""
+        or tensors when ``apply.takes_tensors``; with ``apply.takes_time`` it
+        is called as ``apply(t, xp, yp)`` for an operator H(t)). Options that
+        SciPy ignores for explicit methods (``jac``, ``lband``, ...) are
+        accepted and ignored."""
         tab = tableau(method)
         if rtol < 100 * np.finfo(float).eps:
             rtol = 100 * np.finfo(float).eps
@@ -114,15 +116,17 @@ class RungeKuttaSolver:
         tmp = self.ws.get("ode_tmp", n)[:n]
         ynew = self.ws.get("ode_ynew", n)[:n]
         tensor_apply = getattr(apply, "takes_tensors", False)
+        timed = getattr(apply, "takes_time", False)
         evals = 0
 
-        def H(src: torch.Tensor, dst: torch.Tensor):
+        def H(src: torch.Tensor, dst: torch.Tensor, at: float):
             nonlocal evals
             evals += 1
-            if tensor_apply:
-                apply(src, dst)
+            a, b = (src, dst) if tensor_apply else (src.data_ptr(), dst.data_ptr())
+            if timed:
+                apply(at, a, b)
             else:
-                apply(src.data_ptr(), dst.data_ptr())
+                apply(a, b)
 
         S[0].copy_(x.reshape(-1))
         t, t_bound = 0.0, float(dt)
@@ -134,7 +138,7 @@ class RungeKuttaSolver:
         # a negative dt integrates backward from 0 to dt, as solve_ivp does
         direction = 1.0 if t_bound > 0 else -1.0
         interval = abs(t_bound)
-        H(S[0], S[1])
+        H(S[0], S[1], t)
         # initial step (Hairer, Norsett & Wanner II.4; SciPy's select_initial_step)
         if first_step is not None:
             if first_step <= 0 or first_step > interval:
@@ -148,7 +152,7 @@ class RungeKuttaSolver:
             h0 = 1e-6 if (d0 < 1e-5 or d1 < 1e-5) else 0.01 * d0 / d1
             h0 = min(h0, interval)
             self._combine(S[:2], [1.0, h0 * direction * ef], tmp)
-            H(tmp, ynew)
+            H(tmp, ynew, t + h0 * direction)
             d2 = self._rms((ynew - S[1]) * ef, scale) / h0
             if d1 <= 1e-15 and d2 <= 1e-15:
                 h1 = max(1e-6, h0 * 1e-3)
@@ -170,9 +174,9 @@ class RungeKuttaSolver:
                 h_abs = abs(h)
                 for i in range(1, s):
                     self._combine(S[:1 + i], [1.0] + [h * ef * a for a in tab.A[i, :i]], tmp)
-                    H(tmp, S[1 + i])
+                    H(tmp, S[1 + i], t + tab.C[i] * h)
                 self._combine(S[:1 + s], [1.0] + [h * ef * b for b in tab.B], ynew)
-                H(ynew, S[1 + s])
+                H(ynew, S[1 + s], t + h)
                 scale = atol + torch.maximum(S[0].abs(), ynew.abs()) * rtol
                 if tab.E is not None:
                     self._combine(S[1:2 + s], [h * ef * e for e in tab.E], tmp)

@@ -71,6 +71,31 @@ class TimeEvoMode(Enum):
         """The matrix-exponential modes (everything but KRYLOV and the ODE solvers)."""
         return self is not TimeEvoMode.KRYLOV and self not in TimeEvoMode.scipy_modes()
 
+    def is_scipy(self) -> bool:
+        """A ``solve_ivp`` mode (FASTEST counts as its equivalent, CHEBYSHEV)."""
+        if self is TimeEvoMode.FASTEST:
+            return TimeEvoMode.fastest_equivalent().is_scipy()
+        return self in TimeEvoMode.scipy_modes()
+
+    def action_evolvable(self) -> bool:
+        """Modes that evolve through an action instead of a dense matrix."""
+        return self.is_scipy() or self is TimeEvoMode.KRYLOV
+
+    def time_evolve_action(self, psi, time_evo_action, time_difference: float, forward=None, **options):
+        """psi evolved by y' = c A(t) y on the device, A given as
+        ``time_evo_action(t, y)`` (``time_evolution.py:536-615``); see
+        ``local_evolution.time_evolve_action``."""
+        from .local_evolution import time_evolve_action
+        return time_evolve_action(self, psi, time_evo_action, time_difference,
+                                  EvoDirection.FORWARD if forward is None else forward, **options)
+
+    def time_evolve(self, psi, hamiltonian, time_difference: float, forward=None, **options):
+        """psi evolved by a dense Hamiltonian with the caller's options only
+        (``time_evolution.py:617-655``); see ``local_evolution``."""
+        from .local_evolution import evolve_dense
+        return evolve_dense(self, psi, hamiltonian, time_difference,
+                            EvoDirection.FORWARD if forward is None else forward, options)
+
 
 # the exact modes run the Krylov exponential to these stops
 EXACT_KRYLOV_TOL = {"plain": 1e-14, "reduced": 1e-11}
@@ -121,6 +146,13 @@ class EvoDirection(Enum):
     """``time_evolution/time_evolution.py:384-429``: FORWARD = exp(-i H t)."""
     FORWARD = -1
     BACKWARD = 1
+
+    @staticmethod
+    def from_bool(forward: bool) -> "EvoDirection":
+        return EvoDirection.FORWARD if forward else EvoDirection.BACKWARD
+
+    def exp_sign(self) -> int:
+        return self.value
 
     def exp_factor(self) -> complex:
         return 1.0j * self.value

@@ -1164,3 +1164,68 @@ def test_engine_host_module_functions(monkeypatch):
     cr, an, num = P.bosonic_operators(4)
     assert np.allclose(np.diag(num), [0, 1, 2, 3]) and np.isclose(cr[2, 1], np.sqrt(2)) and np.allclose(an, cr.T)
     assert np.allclose(P.hadamard() @ P.hadamard(), np.eye(2))
+
+
+def test_engine_host_time_evo_mode_methods(monkeypatch):
+    """TimeEvoMode / EvoDirection helpers and the enum's evolution methods
+    with the checks of the reference's own mode tests (a random Hermitian
+    24 x 24 generator on a (2, 3, 4) tensor, dt = 0.1, against expm): the
+    action form for the solve_ivp modes at atol = rtol = 1e-9, the dense form
+    for the exact and solve_ivp modes, the module function's mode defaults at
+    dt = 1, and a time-dependent action against solve_ivp's own integration."""
+    import scipy.linalg
+    from scipy.integrate import solve_ivp
+    fake_ptn.install(monkeypatch)
+    from pytreenet_gb300.local_evolution import time_evolve
+    from pytreenet_gb300.tdvp import EvoDirection, TimeEvoMode
+    assert EvoDirection.from_bool(True) is EvoDirection.FORWARD
+    assert EvoDirection.from_bool(False) is EvoDirection.BACKWARD
+    assert EvoDirection.FORWARD.exp_sign() == -1 and EvoDirection.BACKWARD.exp_sign() == 1
+    assert EvoDirection.FORWARD.exp_factor() == -1j and EvoDirection.BACKWARD.exp_factor() == 1j
+    assert TimeEvoMode.fastest_equivalent() is TimeEvoMode.CHEBYSHEV
+    for m, exp in ((TimeEvoMode.EXPM, False), (TimeEvoMode.CHEBYSHEV, False), (TimeEvoMode.SPARSE, False),
+                   (TimeEvoMode.FASTEST, False), (TimeEvoMode.RK45, True), (TimeEvoMode.RK23, True),
+                   (TimeEvoMode.DOP853, True), (TimeEvoMode.BDF, True)):
+        assert m.is_scipy() is exp
+        assert m.action_evolvable() is exp
+    assert TimeEvoMode.KRYLOV.action_evolvable()
+    rng = np.random.default_rng(21)
+    shape = (2, 3, 4)
+    n = 24
+    A = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    Hm = (A + A.conj().T) / 2
+    psi = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    Ht = Hm.reshape(2 * list(shape))
+
+    def action(_, x):
+        return np.tensordot(Ht, x, axes=([3, 4, 5], [0, 1, 2]))
+    dt = 0.1
+    ref = scipy.linalg.expm(-1j * Hm * dt) @ psi.reshape(-1)
+    for m in (TimeEvoMode.RK45, TimeEvoMode.RK23, TimeEvoMode.DOP853):
+        got = m.time_evolve_action(psi, action, dt, atol=1e-9, rtol=1e-9)
+        assert got.shape == shape
+        np.testing.assert_allclose(got.reshape(-1), ref)
+    got = TimeEvoMode.KRYLOV.time_evolve_action(psi, action, dt, krylov_tol=1e-12)
+    np.testing.assert_allclose(got.reshape(-1), ref)
+    with pytest.raises(NotImplementedError):
+        TimeEvoMode.EXPM.time_evolve_action(psi, action, dt)
+    for m in (TimeEvoMode.EXPM, TimeEvoMode.CHEBYSHEV, TimeEvoMode.SPARSE, TimeEvoMode.RK45,
+              TimeEvoMode.RK23, TimeEvoMode.DOP853):
+        got = m.time_evolve(psi, Hm, dt, atol=1e-9, rtol=1e-9)
+        assert got.shape == shape
+        np.testing.assert_allclose(got.reshape(-1), ref)
+    with pytest.raises(NotImplementedError):
+        TimeEvoMode.BDF.time_evolve(psi, Hm, dt)
+    ref1 = scipy.linalg.expm(-1j * Hm) @ psi.reshape(-1)
+    for m in (TimeEvoMode.RK45, TimeEvoMode.RK23, TimeEvoMode.DOP853):
+        # the module function lays the mode's 1e-10 defaults under the options;
+        # the enum method alone runs at solve_ivp's 1e-3 and misses by far more
+        np.testing.assert_allclose(time_evolve(psi, Hm, 1.0, mode=m).reshape(-1), ref1, atol=1e-6)
+        assert np.abs(m.time_evolve(psi, Hm, 1.0).reshape(-1) - ref1).max() > 1e-6
+    # H(t) = (1 + t) H: the stage times reach the action
+    got = TimeEvoMode.RK45.time_evolve_action(psi, lambda t, x: (1 + t) * action(t, x), 0.3, atol=1e-10, rtol=1e-10)
+    sol = solve_ivp(lambda t, y: -1j * (1 + t) * (Hm @ y), (0, 0.3), psi.reshape(-1), method="RK45",
+                    t_eval=[0.3], atol=1e-10, rtol=1e-10).y[:, 0]
+    assert np.abs(got.reshape(-1) - sol).max() < 1e-13
+    exact = scipy.linalg.expm(-1j * (0.3 + 0.045) * Hm) @ psi.reshape(-1)
+    assert np.abs(got.reshape(-1) - exact).max() < 1e-7

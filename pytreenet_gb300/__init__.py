@@ -24,7 +24,10 @@ from .svd_truncation import SplitMode, TruncationMethod, apply_and_truncate, svd
 from .batch import run_realisations
 from .contractions import (SandwichCache, contract_ket_ham_with_envs, contract_any,
                            effective_single_site_evolution, get_effective_single_site_hamiltonian,
-                           get_effective_single_site_hamiltonian_nodes)
+                           get_effective_single_site_hamiltonian_nodes, PartialTreeCachDict,
+                           contract_bond_tensor, effective_bond_evolution, bond_time_evolution,
+                           single_site_time_evolution, get_effective_bond_hamiltonian,
+                           get_effective_bond_hamiltonian_nodes, get_effective_bond_hamiltonian_tensor)
 from .adjoint import OneSiteTDVPAdjoint, coupling_gradient
 from .bug import BUG, BUGConfig, FixedBUG, FixedBUGConfig
 from .time_dep import AbstractTimeDepTTNO, TimeDependentTTNO, FactorUpdatable, DiscreetTimeTTNO
@@ -54,4 +57,7 @@ __all__ = [
     "krylov_exp_action", "time_evolve", "TDVPUpdatePathFinder", "bosonic_operators", "canonical_form",
     "completely_contract_tree", "contract_two_ttns", "expectation_value", "hadamard",
     "multi_single_site_expectation_value", "pauli_matrices", "spin_jumps",
+    "PartialTreeCachDict", "contract_bond_tensor", "effective_bond_evolution", "bond_time_evolution",
+    "single_site_time_evolution", "get_effective_bond_hamiltonian", "get_effective_bond_hamiltonian_nodes",
+    "get_effective_bond_hamiltonian_tensor",
 ]

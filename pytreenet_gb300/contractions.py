@@ -119,7 +119,7 @@ def contract_any(node_id: str, next_node_id: str, state, operator, dictionary: S
 
 def effective_single_site_evolution(state_tensor, state_node, hamiltonian_tensor, hamiltonian_node,
                                     time_step_size: float, tensor_cache: SandwichCache,
-                                    mode: TimeEvoMode = TimeEvoMode.KRYLOV,
+                                    mode: TimeEvoMode = TimeEvoMode.FASTEST,
                                     forward: EvoDirection = EvoDirection.FORWARD, **options) -> np.ndarray:
     """exp(-i dt H_eff) applied to ``state_tensor`` (``effective_time_evolution.py:257-324``):
     the matrix-free Krylov exponential (options ``krylov_tol``, ``max_krylov_dim``,
@@ -194,3 +194,136 @@ def get_effective_single_site_hamiltonian_nodes(state_node, hamiltonian_node, ha
         Wn = np.transpose(np.asarray(hamiltonian_tensor, dtype=np.complex128), perm)
         W = torch.from_numpy(np.ascontiguousarray(Wn)).to(net.device)
     return _dense_site_hamiltonian(tensor_cache, nid, W)
+
+
+# ----------------------------------------------------------------------------
+# bond pieces with a plain environment dictionary
+# ----------------------------------------------------------------------------
+class PartialTreeCachDict(dict):
+    """Environment tensors keyed by (node, next node), legs (ket, ham, bra)
+    (``contractions/tree_cach_dict.py:16-150``); values may be NumPy arrays
+    or device tensors."""
+
+    def get_entry(self, node_id: str, next_node_id: str):
+        return self[(node_id, next_node_id)]
+
+    def add_entry(self, node_id: str, next_node_id: str, tensor):
+        self[(node_id, next_node_id)] = tensor
+
+    def delete_entry(self, node_id: str, next_node_id: str):
+        del self[(node_id, next_node_id)]
+
+    def contains(self, node_id: str, next_node_id: str) -> bool:
+        return (node_id, next_node_id) in self
+
+    def change_next_id_for_entry(self, node_id: str, old_next_id: str, new_next_id: str):
+        self[(node_id, new_next_id)] = self.pop((node_id, old_next_id))
+
+    def num_legs(self, node_id: str, next_node_id: str) -> int:
+        return len(self[(node_id, next_node_id)].shape)
+
+    def copy(self) -> "PartialTreeCachDict":
+        return PartialTreeCachDict(self)
+
+    def close_to(self, other: "PartialTreeCachDict") -> bool:
+        if set(self) != set(other):
+            return False
+        return all(np.allclose(np.asarray(_host(self[k])), np.asarray(_host(other[k]))) for k in self)
+
+
+def _host(t):
+    return t.detach().cpu().numpy() if isinstance(t, torch.Tensor) else t
+
+
+def _dev(t) -> torch.Tensor:
+    from . import engine as E
+    if isinstance(t, torch.Tensor):
+        return t.to(E.DEFAULT_DEVICE if t.device.type == "cpu" else t.device, CDT).contiguous()
+    return torch.from_numpy(np.ascontiguousarray(np.asarray(t, dtype=np.complex128))).to(E.DEFAULT_DEVICE)
+
+
+def _bond_envs(state_node, tensor_cache):
+    """(E_parent, E_child) of a bond node: the parent's environment toward the
+    child and the child's toward the parent."""
+    parent = state_node.parent
+    children = list(state_node.children)
+    if parent is None or len(children) != 1:
+        raise ValueError("The node must have exactly two neighbours (a parent and one child) "
+                         "to represent a bond!")
+    return tensor_cache.get_entry(parent, children[0]), tensor_cache.get_entry(children[0], parent)
+
+
+def _bond_apply(r: torch.Tensor, ep: torch.Tensor, ec: torch.Tensor, out: torch.Tensor | None = None):
+    from .adjoint import _raw_contract
+    t = _raw_contract(ep, ["a", "b", "p"], r, ["a", "c"], ["b", "p", "c"], ["a"])
+    return _raw_contract(t, ["b", "p", "c"], ec, ["c", "b", "q"], ["p", "q"], ["b", "c"], out=out)
+
+
+def contract_bond_tensor(tensor, state_node, tensor_cache) -> np.ndarray:
+    """H_eff applied to a bond tensor (legs: parent side, child side)
+    (``contract_bond_tensor``, ``state_operator_contraction.py:984-1040``):
+    y[a', c'] = sum E_p[a, b, a'] x[a, c] E_c[c, b, c'], two device contractions."""
+    ep, ec = _bond_envs(state_node, tensor_cache)
+    y = _bond_apply(_dev(tensor), _dev(ep), _dev(ec))
+    return y if isinstance(tensor, torch.Tensor) else y.cpu().numpy()
+
+
+def get_effective_bond_hamiltonian_tensor(state_node, tensor_cache) -> np.ndarray:
+    """H[a', c', a, c] = sum_b E_p[a, b, a'] E_c[c, b, c']
+    (``effective_hamiltonians.py:159-206``), one device contraction."""
+    from .adjoint import _raw_contract
+    ep, ec = _bond_envs(state_node, tensor_cache)
+    h = _raw_contract(_dev(ep), ["a", "b", "p"], _dev(ec), ["c", "b", "q"], ["p", "q", "a", "c"], ["b"])
+    return h.cpu().numpy()
+
+
+def get_effective_bond_hamiltonian_nodes(state_node, tensor_cache) -> np.ndarray:
+    """The bond Hamiltonian as a matrix (output legs rows, input legs columns)."""
+    h = get_effective_bond_hamiltonian_tensor(state_node, tensor_cache)
+    d = h.shape[0] * h.shape[1]
+    return h.reshape(d, d)
+
+
+def get_effective_bond_hamiltonian(bond_node_id: str, state, tensor_cache) -> np.ndarray:
+    return get_effective_bond_hamiltonian_nodes(state.nodes[bond_node_id], tensor_cache)
+
+
+def effective_bond_evolution(state_tensor, state_node, time_step_size: float, tensor_cache,
+                             mode: TimeEvoMode = TimeEvoMode.FASTEST,
+                             forward: EvoDirection = EvoDirection.FORWARD, **options) -> np.ndarray:
+    """A bond tensor evolved by its effective Hamiltonian
+    (``effective_time_evolution.py:205-255``): the action modes (KRYLOV, the
+    solve_ivp modes) apply the bond matvec on the device; the exact modes
+    evolve by the dense bond Hamiltonian, on the device as well."""
+    ep, ec = _bond_envs(state_node, tensor_cache)
+    ep, ec = _dev(ep), _dev(ec)
+    x = _dev(state_tensor)
+    if mode.action_evolvable():
+        def action(t, y):
+            return _bond_apply(y, ep, ec)
+        out = mode.time_evolve_action(x, action, time_step_size, forward=forward, **options)
+    else:
+        h = get_effective_bond_hamiltonian_nodes(state_node, tensor_cache)
+        out = mode.time_evolve(x, h, time_step_size, forward=forward, **options)
+    return out if isinstance(state_tensor, torch.Tensor) else out.cpu().numpy()
+
+
+def bond_time_evolution(node_id: str, state, time_step_size: float, tensor_cache,
+                        forward: EvoDirection = EvoDirection.FORWARD, mode: TimeEvoMode = TimeEvoMode.FASTEST,
+                        solver_options: dict | None = None) -> np.ndarray:
+    """``bond_time_evolution`` (``effective_time_evolution.py:28-68``)."""
+    node = state.nodes[node_id]
+    return effective_bond_evolution(state.tensors[node_id], node, time_step_size, tensor_cache, mode=mode,
+                                    forward=forward, **(solver_options or {}))
+
+
+def single_site_time_evolution(node_id: str, state, hamiltonian, time_step_size: float,
+                               tensor_cache: SandwichCache, forward: EvoDirection = EvoDirection.FORWARD,
+                               mode: TimeEvoMode = TimeEvoMode.FASTEST,
+                               solver_options: dict | None = None) -> np.ndarray:
+    """``single_site_time_evolution`` (``effective_time_evolution.py:70-115``):
+    the node's tensor evolved by its effective Hamiltonian with the cache's
+    environments."""
+    return effective_single_site_evolution(state.tensors[node_id], state.nodes[node_id], None,
+                                           hamiltonian.nodes[node_id], time_step_size, tensor_cache,
+                                           mode=mode, forward=forward, **(solver_options or {}))

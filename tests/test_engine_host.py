@@ -350,6 +350,11 @@ def test_contraction_helpers_match_oracle(monkeypatch):
                                                                          c["ttno"][center], envs),
                              0.05, -1j, krylov_tol=1e-12)
     np.testing.assert_allclose(z, np.transpose(zo, st.logical_perm(center)), atol=1e-11)
+    # the node-id form with the default mode (FASTEST: exact) against the dense exponential
+    zf = C.single_site_time_evolution(center, st, H, 0.05, cache)
+    zd = O.dense_exp_action(ost.tensors[center], lambda v: O.heff_apply(v, ost.tree, center, c["ttno"][center],
+                                                                        envs), 0.05, -1j)
+    np.testing.assert_allclose(zf, np.transpose(zd, st.logical_perm(center)), atol=1e-12)
     # a tensor of another shape is refused before anything runs on the device
     with pytest.raises(ValueError):
         C.effective_single_site_evolution(x[..., :1], st.nodes[center], None, H.nodes[center], 0.05, cache)
@@ -1229,3 +1234,47 @@ def test_engine_host_time_evo_mode_methods(monkeypatch):
     assert np.abs(got.reshape(-1) - sol).max() < 1e-13
     exact = scipy.linalg.expm(-1j * (0.3 + 0.045) * Hm) @ psi.reshape(-1)
     assert np.abs(got.reshape(-1) - exact).max() < 1e-7
+
+
+def test_engine_host_effective_bond_evolution(monkeypatch):
+    """``effective_bond_evolution`` as the reference's own bond tests run it:
+    a (4, 5) bond tensor between random non-Hermitian environments (4, 6, 4)
+    and (5, 6, 5) in a ``PartialTreeCachDict``, every action mode (KRYLOV
+    with hermitian=False and no early stop, the solve_ivp modes at 1e-10)
+    and every exact mode against expm of the dense bond Hamiltonian, which
+    itself matches a NumPy restatement."""
+    import scipy.linalg
+    fake_ptn.install(monkeypatch)
+    import pytreenet_gb300 as P
+    from pytreenet_gb300.contractions import (PartialTreeCachDict, contract_bond_tensor,
+                                              effective_bond_evolution, get_effective_bond_hamiltonian_nodes)
+    rng = np.random.default_rng(17)
+
+    def crandn(*s):
+        return rng.standard_normal(s) + 1j * rng.standard_normal(s)
+    node = P.Node("state_node")
+    node.parent, node.children = "parent_node", ["child_node"]
+    x = crandn(4, 5)
+    cache = PartialTreeCachDict()
+    ep, ec = crandn(4, 6, 4), crandn(5, 6, 5)
+    cache.add_entry("parent_node", "child_node", ep)
+    cache.add_entry("child_node", "parent_node", ec)
+    H = np.einsum("abp,cbq->pqac", ep, ec).reshape(20, 20)
+    np.testing.assert_allclose(get_effective_bond_hamiltonian_nodes(node, cache), H, rtol=1e-13)
+    np.testing.assert_allclose(contract_bond_tensor(x, node, cache), (H @ x.reshape(-1)).reshape(4, 5), rtol=1e-13)
+    dt = 0.1
+    ref = (scipy.linalg.expm(-1j * dt * H) @ x.reshape(-1)).reshape(4, 5)
+    for mode in (P.TimeEvoMode.RK45, P.TimeEvoMode.RK23, P.TimeEvoMode.DOP853):
+        np.testing.assert_allclose(effective_bond_evolution(x, node, dt, cache, mode=mode, rtol=1e-10, atol=1e-10),
+                                   ref)
+    np.testing.assert_allclose(effective_bond_evolution(x, node, dt, cache, mode=P.TimeEvoMode.KRYLOV,
+                                                        krylov_tol=0.0, hermitian=False), ref)
+    for mode in (P.TimeEvoMode.FASTEST, P.TimeEvoMode.EXPM, P.TimeEvoMode.CHEBYSHEV, P.TimeEvoMode.SPARSE):
+        np.testing.assert_allclose(effective_bond_evolution(x, node, dt, cache, mode=mode), ref)
+    back = effective_bond_evolution(x, node, dt, cache, mode=P.TimeEvoMode.EXPM, forward=P.EvoDirection.BACKWARD)
+    np.testing.assert_allclose(back, (scipy.linalg.expm(1j * dt * H) @ x.reshape(-1)).reshape(4, 5))
+    assert cache.contains("parent_node", "child_node") and cache.num_legs("child_node", "parent_node") == 3
+    bad = P.Node("leaf")
+    bad.parent, bad.children = "parent_node", []
+    with pytest.raises(ValueError):
+        contract_bond_tensor(x, bad, cache)

@@ -1034,8 +1034,9 @@ class _TwoSiteBase(_OneSiteBase):
     """``TwoSiteTDVP`` (``tdvp_algorithms/twositetdvp.py:29-146``)."""
 
     def __init__(self, state: OState, W: dict, dt: float, svd: SVDParams, krylov_tol=1e-10,
-                 max_krylov_dim=None, path_mode: str = "LeafToRoot", ode: dict | None = None):
-        super().__init__(state, W, dt, krylov_tol, max_krylov_dim, path_mode=path_mode, ode=ode)
+                 max_krylov_dim=None, path_mode: str = "LeafToRoot", ode: dict | None = None,
+                 exact: bool = False):
+        super().__init__(state, W, dt, krylov_tol, max_krylov_dim, path_mode=path_mode, ode=ode, exact=exact)
         self.svd = svd
         self.bond_history = []
 

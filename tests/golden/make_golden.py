@@ -745,6 +745,13 @@ def ode_cases(ptn):
     run_case_bug(ptn, "binary15_tfim_fixed_bug_rk45", spec, capped_state_tensors(spec, rng, 4),
                  lambda psi: tfim(ptn, spec, g=0.6), 0.1, 2, 0.0, ode_mode="RK45",
                  ode_options={"atol": 1e-10, "rtol": 1e-10})
+    # second-order two-site TDVP with the default mode (FASTEST: dense two-site
+    # effective Hamiltonians in the reference)
+    spec = binary_tree(7)
+    h = rng.uniform(-1, 1, size=len(spec))
+    run_case_two_site(ptn, "binary7_heis_2tdvp_fastest", spec, random_state_tensors(spec, rng, 2),
+                      lambda psi: heisenberg_fields(ptn, spec, h), 0.05, 2, 0.0, (5, 1e-10, 1e-10, False),
+                      canonical_random=True, ode_mode="FASTEST")
 
 
 def heff_cases(ptn):

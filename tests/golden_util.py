@@ -44,7 +44,7 @@ def load_case(name):
 CASES = ["c1_binary15_tfim_chi8", "binary7_tfim_chi4_o2", "ttree3_heis_chi6_o1",
          "ttree3_heis_chi6_o2", "ternary2_xxz_chi4_o1"]
 TWO_SITE_CASES = ["ternary2_xxz_neel_2tdvp", "binary7_heis_2tdvp_trunc", "binary7_heis_2tdvp_l2l",
-                  "binary7_heis_2tdvp_rk45"]
+                  "binary7_heis_2tdvp_rk45", "binary7_heis_2tdvp_fastest"]
 ODE_MODES = ("RK45", "RK23", "DOP853")
 
 

@@ -94,7 +94,8 @@ def test_oracle_two_site_cases(name):
     c = load_case(name)
     st = oracle_state(c)
     algo = O.SecondOrderTwoSiteTDVPOracle(st, c["ttno"], c["dt"], O.SVDParams(**c["svd"]),
-                                          krylov_tol=c["krylov_tol"], path_mode=c["path_mode"], ode=oracle_ode(c))
+                                          krylov_tol=c["krylov_tol"], path_mode=c["path_mode"], ode=oracle_ode(c),
+                                          exact=c["time_evo_mode"] not in ("KRYLOV", "RK45", "RK23", "DOP853"))
     assert algo.update_path == c["update_path"]
     zerr = 0.0
     for k in range(c["steps"]):

@@ -33,6 +33,7 @@ from .bug import BUG, BUGConfig, FixedBUG, FixedBUGConfig
 from .time_dep import AbstractTimeDepTTNO, TimeDependentTTNO, FactorUpdatable, DiscreetTimeTTNO
 from .tdvp import OneSiteTDVP, TwoSiteTDVP, TTNTimeEvolutionConfig
 from .results import Results
+from .ttno_decomposition import Decomposition
 from .application import zipup
 from .local_evolution import krylov_exp_action, time_evolve
 from .functions import (TDVPUpdatePathFinder, bosonic_operators, canonical_form, completely_contract_tree,
@@ -59,5 +60,5 @@ __all__ = [
     "multi_single_site_expectation_value", "pauli_matrices", "spin_jumps",
     "PartialTreeCachDict", "contract_bond_tensor", "effective_bond_evolution", "bond_time_evolution",
     "single_site_time_evolution", "get_effective_bond_hamiltonian", "get_effective_bond_hamiltonian_nodes",
-    "get_effective_bond_hamiltonian_tensor",
+    "get_effective_bond_hamiltonian_tensor", "Decomposition",
 ]

@@ -624,6 +624,14 @@ class TreeTensorNetworkOperator(TreeTensorNetwork):
         from .hamiltonian import ttno_from_hamiltonian
         return ttno_from_hamiltonian(hamiltonian, reference_tree, dtype=dtype)
 
+    @classmethod
+    def from_tensor(cls, reference_tree, tensor, leg_dict: dict, mode=None):
+        """``TTNO.from_tensor`` (``ttno/ttno_class.py:163-298``): the TTNO of a
+        dense operator tensor (legs out_1..out_n, in_1..in_n; ``leg_dict``
+        maps node -> out leg) by successive device QR (default) or SVD splits."""
+        from .ttno_decomposition import Decomposition, ttno_from_tensor
+        return ttno_from_tensor(reference_tree, tensor, leg_dict, Decomposition.QR if mode is None else mode)
+
 
 TTNS = TreeTensorNetworkState
 TTNO = TreeTensorNetworkOperator

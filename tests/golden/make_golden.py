@@ -754,6 +754,42 @@ def ode_cases(ptn):
                       canonical_random=True, ode_mode="FASTEST")
 
 
+def from_tensor_cases(ptn):
+    """``TTNO.from_tensor`` (``ttno/ttno_class.py:163-298``, QR mode) on a
+    4-node tree and a 6-node tree with mixed physical dimensions: the input
+    operator tensor, its leg dictionary and the reference's node tensors in
+    the reference's node leg order."""
+    rng = np.random.default_rng(83)
+    rec = {}
+    cases = [("t4", [("root", None), ("a", "root"), ("b", "root"), ("c", "a")],
+              {"root": 2, "a": 0, "b": 3, "c": 1}, {"root": 2, "a": 2, "b": 2, "c": 2}),
+             ("t6", [("r", None), ("x", "r"), ("y", "r"), ("z", "r"), ("u", "y"), ("v", "y")],
+              {"r": 5, "x": 0, "y": 1, "z": 4, "u": 2, "v": 3}, {"r": 2, "x": 3, "y": 2, "z": 2, "u": 2, "v": 3})]
+    for tag, spec, leg_dict, dims in cases:
+        ch = children_of(spec)
+        tensors = {}
+        for nid, p in spec:
+            nv = len(ch[nid]) + (0 if p is None else 1)
+            tensors[nid] = np.ones([1] * nv + [dims[nid]], dtype=complex)
+        psi = build_reference_state(ptn, spec, tensors)
+        out_dims = [0] * len(spec)
+        for nid, leg in leg_dict.items():
+            out_dims[leg] = dims[nid]
+        shape = out_dims + out_dims
+        op = rng.normal(size=shape) + 1j * rng.normal(size=shape)
+        ttno = ptn.TTNO.from_tensor(psi, op, leg_dict)
+        rec[f"{tag}/spec_ids"] = np.array([x[0] for x in spec])
+        rec[f"{tag}/spec_parents"] = np.array(["" if x[1] is None else x[1] for x in spec])
+        rec[f"{tag}/op"] = op
+        for nid, _ in spec:
+            rec[f"{tag}/init/{nid}"] = tensors[nid]
+            rec[f"{tag}/leg/{nid}"] = leg_dict[nid]
+            rec[f"{tag}/ttno/{nid}"] = np.asarray(ttno.tensors[nid])
+            rec[f"{tag}/children/{nid}"] = np.array(list(ttno.nodes[nid].children), dtype=str)
+    np.savez_compressed(os.path.join(HERE, "ttno_from_tensor.npz"), **rec)
+    print("ttno_from_tensor written")
+
+
 def heff_cases(ptn):
     """Dense effective site Hamiltonians from the reference's
     ``get_effective_single_site_hamiltonian`` (``contractions/effective_hamiltonians.py:133-157``)
@@ -940,6 +976,7 @@ def main(ref_root):
     zipup_cases(ptn)
     leaf_to_leaf_two_site_cases(ptn)
     ode_cases(ptn)
+    from_tensor_cases(ptn)
 
 
 if __name__ == "__main__":

@@ -1278,3 +1278,36 @@ def test_engine_host_effective_bond_evolution(monkeypatch):
     bad.parent, bad.children = "parent_node", []
     with pytest.raises(ValueError):
         contract_bond_tensor(x, bad, cache)
+
+
+@pytest.mark.parametrize("tag", ["t4", "t6"])
+def test_engine_host_ttno_from_tensor(monkeypatch, tag):
+    """``TTNO.from_tensor``: in QR mode the node tensors equal the reference's
+    (same leg bookkeeping, Householder signs); the SVD modes give the same
+    operator (as_matrix against the input tensor)."""
+    from golden_util import GOLDEN, build_ttn
+    fake_ptn.install(monkeypatch)
+    import pytreenet_gb300 as P
+    from pytreenet_gb300.ttno_decomposition import Decomposition
+    d = np.load(f"{GOLDEN}/ttno_from_tensor.npz")
+    ids = [str(x) for x in d[f"{tag}/spec_ids"]]
+    spec = list(zip(ids, [str(x) or None for x in d[f"{tag}/spec_parents"]]))
+    tree = build_ttn(P.TTNS, spec, {nid: d[f"{tag}/init/{nid}"] for nid in ids})
+    leg_dict = {nid: int(d[f"{tag}/leg/{nid}"]) for nid in ids}
+    op = d[f"{tag}/op"]
+    ttno = P.TTNO.from_tensor(tree, op, leg_dict)
+    for nid in ids:
+        ref = d[f"{tag}/ttno/{nid}"]
+        got = np.asarray(ttno.tensors[nid])
+        assert got.shape == ref.shape, nid
+        assert np.abs(got - ref).max() < 1e-12 * max(1.0, np.abs(ref).max()), nid
+        assert list(ttno.nodes[nid].children) == [str(x) for x in d[f"{tag}/children/{nid}"]]
+    half = op.ndim // 2
+    order = ids
+    perm = [leg_dict[n] for n in order] + [half + leg_dict[n] for n in order]
+    dim = int(np.prod([op.shape[leg_dict[n]] for n in order]))
+    dense = np.transpose(op, perm).reshape(dim, dim)
+    for mode in (Decomposition.QR, Decomposition.SVD, Decomposition.tSVD):
+        m, got_order = P.TTNO.from_tensor(tree, op, leg_dict, mode=mode).as_matrix(order)
+        assert list(got_order) == order
+        assert np.abs(m - dense).max() < 1e-11 * np.abs(dense).max(), mode

@@ -331,3 +331,30 @@ def test_gpu_zipup_matches_reference(tag):
     """Zip-up TTNO application on the GB300 against the reference's zipup."""
     from golden_util import check_zipup_fixture
     check_zipup_fixture(tag)
+
+
+@pytest.mark.parametrize("tag", ["t4", "t6"])
+def test_gpu_ttno_from_tensor(tag):
+    """TTNO.from_tensor on the GB300: QR-mode node tensors equal the
+    reference's; the SVD modes give the same operator."""
+    import pytreenet_gb300 as P
+    from golden_util import GOLDEN
+    d = np.load(f"{GOLDEN}/ttno_from_tensor.npz")
+    ids = [str(x) for x in d[f"{tag}/spec_ids"]]
+    spec = list(zip(ids, [str(x) or None for x in d[f"{tag}/spec_parents"]]))
+    tree = build_ttn(P.TTNS, spec, {nid: d[f"{tag}/init/{nid}"] for nid in ids})
+    leg_dict = {nid: int(d[f"{tag}/leg/{nid}"]) for nid in ids}
+    op = d[f"{tag}/op"]
+    ttno = P.TTNO.from_tensor(tree, op, leg_dict)
+    for nid in ids:
+        ref = d[f"{tag}/ttno/{nid}"]
+        got = np.asarray(ttno.tensors[nid])
+        assert got.shape == ref.shape, nid
+        assert np.abs(got - ref).max() < 1e-12 * max(1.0, np.abs(ref).max()), nid
+    half = op.ndim // 2
+    perm = [leg_dict[n] for n in ids] + [half + leg_dict[n] for n in ids]
+    dim = int(np.prod([op.shape[leg_dict[n]] for n in ids]))
+    dense = np.transpose(op, perm).reshape(dim, dim)
+    for mode in (P.Decomposition.SVD, P.Decomposition.tSVD):
+        m, _ = P.TTNO.from_tensor(tree, op, leg_dict, mode=mode).as_matrix(ids)
+        assert np.abs(m - dense).max() < 1e-11 * np.abs(dense).max(), mode

@@ -285,15 +285,39 @@ class TreeTensorNetwork:
                      for k, v in self._phys.items()}
         return out
 
+    def _preorder(self) -> list:
+        """Root first, then every child's subtree in the children's order."""
+        self._finalise()
+        out = []
+
+        def rec(n):
+            out.append(n)
+            for c in self.nodes[n].children:
+                rec(c)
+        rec(self.root_id)
+        return out
+
     def completely_contract_tree(self, to_copy: bool = False, order: list | None = None):
         """The whole network as one tensor and the node order of its open legs
-        (states only: one physical leg per node; small trees)."""
-        if not hasattr(self, "to_dense"):
-            raise NotImplementedError("a TTNO contracts to a matrix with as_matrix()")
-        order = list(self._order) if order is None else list(order)
-        vec = self.to_dense(order)
-        dims = [int(self.phys(n).shape[-1]) for n in order]
-        return vec.reshape(dims), order
+        (``contractions/tree_contraction.py:20-62``): by default the nodes in
+        the order the reference contracts them (root, then each child's subtree
+        in turn); a state has one leg per node, an operator its (out, in) pair
+        per node. Small trees only."""
+        default = self._preorder()
+        if order is None:
+            order = default
+        elif set(order) != set(default):
+            raise ValueError("The order is inconsistent with the structure of the tree!")
+        order = list(order)
+        if hasattr(self, "to_dense"):
+            vec = self.to_dense(order)
+            dims = [int(self.phys(n).shape[-1]) for n in order]
+            return vec.reshape(dims), order
+        mat, _ = self.as_matrix(order)
+        dims = [int(self.phys(n).shape[-2]) for n in order]
+        n = len(order)
+        pairs = [i for k in range(n) for i in (k, n + k)]
+        return np.transpose(np.asarray(mat).reshape(dims + dims), pairs), order
 
     def bond_dims(self) -> dict:
         """(parent, child) -> bond dimension (``core/ttn.py:754-768``)."""

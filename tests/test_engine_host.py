@@ -1311,3 +1311,37 @@ def test_engine_host_ttno_from_tensor(monkeypatch, tag):
         m, got_order = P.TTNO.from_tensor(tree, op, leg_dict, mode=mode).as_matrix(order)
         assert list(got_order) == order
         assert np.abs(m - dense).max() < 1e-11 * np.abs(dense).max(), mode
+
+
+def test_engine_host_from_tensor_root_is_leaf(monkeypatch):
+    """The reference's root-is-leaf case of ``from_tensor``: a 7-node tree whose
+    root has one child, built with ``add_child_to_parent`` on chosen legs; the
+    completely contracted TTNO (legs (out, in) per node, root first, then each
+    child's subtree) equals the input tensor with its legs in that order."""
+    fake_ptn.install(monkeypatch)
+    import pytreenet_gb300 as P
+    rng = np.random.default_rng(3)
+
+    def crandn(shape):
+        return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    shapes = [(1, 1, 1, 2), (1, 1, 1, 2), (1, 2), (1, 2), (1, 2), (1, 1, 2), (1, 2)]
+    t = [crandn(s) for s in shapes]
+    tree = P.TTNS()
+    tree.add_root("node4", t[4])
+    tree.add_child_to_parent("node0", t[0], 0, "node4", 0)
+    tree.add_child_to_parent("node1", t[1], 0, "node0", 1)
+    tree.add_child_to_parent("node2", t[2], 0, "node1", 1)
+    tree.add_child_to_parent("node3", t[3], 0, "node1", 2)
+    tree.add_child_to_parent("node5", t[5], 0, "node0", 2)
+    tree.add_child_to_parent("node6", t[6], 0, "node5", 1)
+    n = len(shapes)
+    start = crandn(2 * n * [2])
+    leg_dict = {f"node{i}": i for i in range(n)}
+    ttno = P.TTNO.from_tensor(tree, start.copy(), leg_dict)
+    contracted, order = ttno.completely_contract_tree(to_copy=True)
+    assert order == ["node4", "node0", "node1", "node2", "node3", "node5", "node6"]
+    perm = [i for nid in order for i in (leg_dict[nid], leg_dict[nid] + n)]
+    assert np.allclose(start.transpose(perm), contracted)
+    # a state contracts to one leg per node in the same order
+    vec, sorder = tree.completely_contract_tree()
+    assert sorder == order and vec.shape == (2,) * n

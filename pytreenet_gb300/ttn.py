@@ -206,8 +206,64 @@ class TreeTensorNetwork:
             rec(nb, center, 1)
         return out
 
-    def get_leaves(self) -> list[str]:
-        return [nid for nid in self._order if self.nodes[nid].is_leaf()]
+    def get_leaves(self, include_root: bool = True) -> list[str]:
+        """Leaf identifiers; with ``include_root`` a root with one neighbour
+        counts too (``core/tree_structure.py:201-216``)."""
+        leaves = [nid for nid in self._order if self.nodes[nid].is_leaf()]
+        if include_root and self.root_id is not None and self.nodes[self.root_id].nneighbours() == 1:
+            leaves.append(self.root_id)
+        return leaves
+
+    def get_leafs(self, include_root: bool = True) -> list[str]:
+        return self.get_leaves(include_root=include_root)
+
+    def find_subtree_of_node(self, node_id: str) -> dict:
+        """node id -> node for ``node_id`` and everything below it
+        (``core/tree_structure.py:433-457``)."""
+        out = {}
+
+        def rec(n):
+            out[n] = self.nodes[n]
+            for c in self.nodes[n].children:
+                rec(c)
+        rec(node_id)
+        return out
+
+    def find_subtree_size_of_node(self, node_id: str) -> int:
+        return len(self.find_subtree_of_node(node_id))
+
+    def leaves_under_node(self, node_id: str) -> dict:
+        """The leaves of ``node_id``'s subtree (``core/tree_structure.py:459-477``)."""
+        return {n: node for n, node in self.find_subtree_of_node(node_id).items() if node.is_leaf()}
+
+    def find_pairs_of_distance(self, distance: int, consider_open: bool = False) -> set:
+        """Unordered pairs of nodes ``distance`` edges apart
+        (``core/tree_structure.py:273-309``); with ``consider_open`` only nodes
+        with an open leg of dimension above one count, and the distance is
+        measured over those nodes alone."""
+        def counts(n):
+            return (not consider_open) or int(self.phys(n).shape[-1]) > 1
+        if distance < 0:
+            raise ValueError("distance must be non-negative")
+        if distance == 0:
+            return {frozenset([n]) for n in self._order if counts(n)}
+        pairs = set()
+        for a in self._order:
+            if not counts(a):
+                continue
+            for b, d in self.distance_to_node(a).items():
+                if b == a or not counts(b):
+                    continue
+                if consider_open:
+                    path = self.path_from_to(a, b)
+                    d = sum(1 for x in path[1:] if counts(x))
+                if d == distance:
+                    pairs.add(frozenset((a, b)))
+        return pairs
+
+    def nearest_neighbours(self, consider_open: bool = False) -> list:
+        """Nearest-neighbour pairs (``core/tree_structure.py:187-199``)."""
+        return [tuple(p) for p in self.find_pairs_of_distance(1, consider_open=consider_open)]
 
     def bond_dim(self, a, b) -> int:
         return self.phys(a).shape[self.phys_axis(a, b)]

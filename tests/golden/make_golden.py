@@ -790,6 +790,42 @@ def from_tensor_cases(ptn):
     print("ttno_from_tensor written")
 
 
+PATH_TREES = {
+    "rootleaf7": ("node4", [("node0", "node4", 0), ("node1", "node0", 1), ("node2", "node1", 1),
+                            ("node3", "node1", 2), ("node5", "node0", 2), ("node6", "node5", 1)]),
+    "chainroot": ("r", [("a", "r", 0), ("b", "a", 1), ("c", "b", 1)]),
+    "rootleafT": ("r", [("a", "r", 0), ("b", "a", 1), ("c", "a", 2), ("d", "b", 1), ("e", "c", 1)]),
+    "wide": ("r", [("a", "r", 0), ("b", "r", 1), ("c", "r", 2), ("d", "a", 1), ("e", "a", 2), ("f", "c", 1),
+                   ("g", "f", 1)]),
+}
+
+
+def path_cases(ptn):
+    """Update paths of ``TDVPUpdatePathFinder`` (both modes) on trees built
+    with ``add_child_to_parent`` on chosen legs, roots with one child included."""
+    from pytreenet.time_evolution.time_evo_util.update_path import TDVPUpdatePathFinder, PathFinderMode
+    from pytreenet.core.node import Node as RNode
+    rec = {}
+    for name, (root, edges) in PATH_TREES.items():
+        nch = {root: 0}
+        for c, p, _ in edges:
+            nch[p] = nch.get(p, 0) + 1
+            nch.setdefault(c, 0)
+
+        def ones(n, is_root):
+            return np.ones([1] * (nch[n] + (0 if is_root else 1)) + [2], dtype=complex)
+        t = ptn.TreeTensorNetworkState()
+        t.add_root(RNode(identifier=root), ones(root, True))
+        for c, p, leg in edges:
+            t.add_child_to_parent(RNode(identifier=c), ones(c, False), 0, p, leg)
+        rec[f"{name}/edges"] = np.array([[c, p, str(leg)] for c, p, leg in edges])
+        rec[f"{name}/root"] = root
+        for mode in ("LeafToRoot", "LeafToLeaf"):
+            rec[f"{name}/{mode}"] = np.array(TDVPUpdatePathFinder(t, PathFinderMode[mode]).find_path())
+    np.savez_compressed(os.path.join(HERE, "update_paths.npz"), **rec)
+    print("update_paths written")
+
+
 def heff_cases(ptn):
     """Dense effective site Hamiltonians from the reference's
     ``get_effective_single_site_hamiltonian`` (``contractions/effective_hamiltonians.py:133-157``)
@@ -977,6 +1013,7 @@ def main(ref_root):
     leaf_to_leaf_two_site_cases(ptn)
     ode_cases(ptn)
     from_tensor_cases(ptn)
+    path_cases(ptn)
 
 
 if __name__ == "__main__":

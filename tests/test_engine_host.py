@@ -1345,3 +1345,54 @@ def test_engine_host_from_tensor_root_is_leaf(monkeypatch):
     # a state contracts to one leg per node in the same order
     vec, sorder = tree.completely_contract_tree()
     assert sorder == order and vec.shape == (2,) * n
+
+
+def test_update_paths_match_reference():
+    """``TDVPUpdatePathFinder`` in both modes gives the reference's paths on
+    trees built leg by leg, including roots with a single child (which count
+    as leaves, as in the reference's ``get_leaves``)."""
+    from golden_util import GOLDEN
+    import pytreenet_gb300 as P
+    d = np.load(f"{GOLDEN}/update_paths.npz")
+    names = sorted({k.split("/")[0] for k in d.files})
+    assert len(names) >= 4
+    for name in names:
+        root = str(d[f"{name}/root"])
+        edges = [(str(c), str(p), int(leg)) for c, p, leg in d[f"{name}/edges"]]
+        nch = {root: 0}
+        for c, p, _ in edges:
+            nch[p] = nch.get(p, 0) + 1
+            nch.setdefault(c, 0)
+
+        def ones(n, is_root):
+            return np.ones([1] * (nch[n] + (0 if is_root else 1)) + [2], dtype=complex)
+        t = P.TTNS()
+        t.add_root(root, ones(root, True))
+        for c, p, leg in edges:
+            t.add_child_to_parent(c, ones(c, False), 0, p, leg)
+        for mode in ("LeafToRoot", "LeafToLeaf"):
+            want = [str(x) for x in d[f"{name}/{mode}"]]
+            assert P.TDVPUpdatePathFinder(t, P.PathFinderMode[mode]).find_path() == want, (name, mode)
+    leaves = t.get_leaves(include_root=False)
+    assert root not in leaves and set(leaves) <= set(nch)
+
+
+def test_tree_structure_queries():
+    """Leaves, subtrees and pairs at a distance (``core/tree_structure.py``):
+    a node whose open leg is trivial is skipped when ``consider_open``."""
+    import pytreenet_gb300 as P
+    t = P.TTNS()
+    t.add_root("r", np.ones((1, 1, 2), dtype=complex))
+    t.add_child_to_parent("a", np.ones((1, 1, 1), dtype=complex), 0, "r", 0)   # trivial open leg
+    t.add_child_to_parent("b", np.ones((1, 2), dtype=complex), 0, "r", 1)
+    t.add_child_to_parent("c", np.ones((1, 2), dtype=complex), 0, "a", 1)
+    assert sorted(t.get_leaves()) == ["b", "c"]
+    assert set(t.find_subtree_of_node("a")) == {"a", "c"} and t.find_subtree_size_of_node("r") == 4
+    assert set(t.leaves_under_node("a")) == {"c"}
+    assert t.find_pairs_of_distance(1) == {frozenset(p) for p in [("r", "a"), ("r", "b"), ("a", "c")]}
+    assert t.find_pairs_of_distance(2) == {frozenset(p) for p in [("a", "b"), ("r", "c")]}
+    assert t.find_pairs_of_distance(1, consider_open=True) == {frozenset(p) for p in [("r", "b"), ("r", "c")]}
+    assert t.find_pairs_of_distance(0, consider_open=True) == {frozenset([n]) for n in ("r", "b", "c")}
+    assert sorted(tuple(sorted(p)) for p in t.nearest_neighbours()) == [("a", "c"), ("a", "r"), ("b", "r")]
+    with pytest.raises(ValueError):
+        t.find_pairs_of_distance(-1)

@@ -334,6 +334,24 @@ class TreeTensorNetwork:
         self.set_tensor(node_id, t)
         self.nodes[node_id].shape = tuple(self._phys[node_id].shape)
 
+    def scale(self, factor, inplace: bool = True):
+        """The network times ``factor``: the orthogonality centre's tensor (or
+        the root's) is scaled, so a canonical form stays intact
+        (``core/ttn.py:692-720``)."""
+        ttn = self if inplace else self.copy_structure()
+        if not inplace:
+            ttn._phys = {k: (v.copy() if isinstance(v, np.ndarray) else v.clone()) for k, v in self._phys.items()}
+        nid = ttn.orthogonality_center_id if ttn.orthogonality_center_id is not None else ttn.root_id
+        if nid is None:
+            raise AssertionError("Cannot scale an empty TTN!")
+        ttn._phys[nid] = ttn._phys[nid] * factor
+        return ttn
+
+    def assert_orth_center(self, node_id: str, object_name: str = "tree tensor network"):
+        """Raise unless ``node_id`` is the orthogonality centre (``core/ttn.py:1585-1600``)."""
+        if self.orthogonality_center_id != node_id:
+            raise AssertionError(f"The {object_name} has no orthogonality center at {node_id}!")
+
     def conjugate(self):
         """A copy with every tensor complex-conjugated (``core/ttn.py:681-690``)."""
         out = self.copy_structure()

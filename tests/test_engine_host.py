@@ -1396,3 +1396,20 @@ def test_tree_structure_queries():
     assert sorted(tuple(sorted(p)) for p in t.nearest_neighbours()) == [("a", "c"), ("a", "r"), ("b", "r")]
     with pytest.raises(ValueError):
         t.find_pairs_of_distance(-1)
+
+
+def test_ttn_scale_and_orth_assertion():
+    """``scale`` multiplies the centre's tensor (the root's without a centre),
+    in place or on a copy; ``assert_orth_center`` checks the centre."""
+    import pytreenet_gb300 as P
+    t = P.TTNS()
+    t.add_root("r", np.ones((1, 2), dtype=complex))
+    t.add_child_to_parent("a", np.full((1, 2), 2.0, dtype=complex), 0, "r", 0)
+    c = t.scale(3.0, inplace=False)
+    assert np.allclose(c.tensors["r"], 3.0) and np.allclose(t.tensors["r"], 1.0)
+    t.orthogonality_center_id = "a"
+    t.scale(0.5)
+    assert np.allclose(t.tensors["a"], 1.0) and np.allclose(t.tensors["r"], 1.0)
+    t.assert_orth_center("a")
+    with pytest.raises(AssertionError):
+        t.assert_orth_center("r")

@@ -590,6 +590,16 @@ class TreeTensorNetworkState(TreeTensorNetwork):
         """Canonical form from scratch, whatever the current centre."""
         self._orthogonalise(orthogonality_center_id, mode, full=True)
 
+    def orthogonalize_root(self, mode=None):
+        """Canonical form with the centre at the root (``core/ttn.py:1652-1664``)."""
+        if self.root_id is None:
+            raise ValueError("The TTN has no root node!")
+        self.canonical_form(self.root_id, mode=mode)
+
+    def transpose_all_tensors(self):
+        """Tensors are always served in their nodes' leg order; nothing to do
+        (``core/ttn.py:1741-1746``)."""
+
     def move_orthogonalization_center(self, new_center_id: str, mode=None):
         if self.orthogonality_center_id is None:
             raise AssertionError("The TTN is not in canonical form, so the orth. center cannot be moved!")

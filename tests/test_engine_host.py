@@ -893,6 +893,10 @@ def test_ttns_canonical_form_methods(monkeypatch):
     st2.canonical_form("s0")                            # REDUCED: a leaf bond cannot exceed 2
     assert st2.phys("s4").shape[0] == 2 and np.max(np.abs(st2.to_dense(ids) - v0)) < 1e-12
     assert st2.ensure_root_orth_center() is True
+    st3 = build_ttn(P.TTNS, c["spec"], {k: v.copy() for k, v in c["init"].items()})
+    st3.orthogonalize_root()
+    assert st3.orthogonality_center_id == st3.root_id and st3.is_in_canonical_form()
+    assert np.max(np.abs(st3.to_dense(ids) - v0)) < 1e-12
 
 
 def test_pad_bond_dimensions_reproduces_c1_fixture():

@@ -217,6 +217,41 @@ class TreeTensorNetwork:
     def get_leafs(self, include_root: bool = True) -> list[str]:
         return self.get_leaves(include_root=include_root)
 
+    def same_connectivity_as(self, other) -> bool:
+        """Same node ids, same neighbours (``core/tree_structure.py:389-408``)."""
+        if set(self.nodes) != set(other.nodes):
+            return False
+        return all(set(self.nodes[n].neighbouring_nodes()) == set(other.nodes[n].neighbouring_nodes())
+                   for n in self.nodes)
+
+    def same_hierarchy_as(self, other) -> bool:
+        """Same parents and children (``core/tree_structure.py:410-431``)."""
+        if set(self.nodes) != set(other.nodes):
+            return False
+        return all(self.nodes[n].parent == other.nodes[n].parent
+                   and set(self.nodes[n].children) == set(other.nodes[n].children) for n in self.nodes)
+
+    def _open_dims(self, nid) -> tuple:
+        shape = self.phys(nid).shape
+        return tuple(int(d) for d in shape[len(shape) - self.n_open:])
+
+    def same_open_dimensions_as(self, other) -> bool:
+        """Same open-leg dimensions on every node (``core/ttn.py:381-400``)."""
+        if set(self.nodes) != set(other.nodes):
+            return False
+        return all(self._open_dims(n) == other._open_dims(n) for n in self.nodes)
+
+    def same_structure_as(self, other) -> bool:
+        """Same hierarchy and open dimensions (``core/ttn.py:338-356``)."""
+        return self.same_hierarchy_as(other) and self.same_open_dimensions_as(other)
+
+    def same_bond_dimensions_as(self, other) -> bool:
+        """Same bond dimension on every edge (``core/ttn.py:358-379``)."""
+        if not self.same_connectivity_as(other):
+            return False
+        return all(self.bond_dim(n, x) == other.bond_dim(n, x)
+                   for n in self.nodes for x in self.nodes[n].neighbouring_nodes())
+
     def find_subtree_of_node(self, node_id: str) -> dict:
         """node id -> node for ``node_id`` and everything below it
         (``core/tree_structure.py:433-457``)."""

@@ -1417,3 +1417,25 @@ def test_ttn_scale_and_orth_assertion():
     t.assert_orth_center("a")
     with pytest.raises(AssertionError):
         t.assert_orth_center("r")
+
+
+def test_ttn_structure_comparisons():
+    """same_connectivity_as / same_hierarchy_as / same_structure_as /
+    same_open_dimensions_as / same_bond_dimensions_as."""
+    import pytreenet_gb300 as P
+
+    def tree(bond, phys):
+        t = P.TTNS()
+        t.add_root("r", np.ones((bond, 1, phys), dtype=complex))
+        t.add_child_to_parent("a", np.ones((bond, phys), dtype=complex), 0, "r", 0)
+        t.add_child_to_parent("b", np.ones((1, 2), dtype=complex), 0, "r", 1)
+        return t
+    a, b, c, d = tree(2, 2), tree(2, 2), tree(3, 2), tree(2, 3)
+    assert a.same_connectivity_as(b) and a.same_hierarchy_as(b) and a.same_structure_as(b)
+    assert a.same_bond_dimensions_as(b) and not a.same_bond_dimensions_as(c)
+    assert a.same_structure_as(c) and not a.same_structure_as(d) and not a.same_open_dimensions_as(d)
+    e = P.TTNS()
+    e.add_root("a", np.ones((2, 1, 2), dtype=complex))
+    e.add_child_to_parent("r", np.ones((2, 1, 2), dtype=complex), 0, "a", 0)
+    e.add_child_to_parent("b", np.ones((1, 2), dtype=complex), 0, "r", 1)
+    assert a.same_connectivity_as(e) and not a.same_hierarchy_as(e)   # same edges, other root

@@ -217,6 +217,13 @@ class TreeTensorNetwork:
     def get_leafs(self, include_root: bool = True) -> list[str]:
         return self.get_leaves(include_root=include_root)
 
+    def is_child_of(self, pot_child: str, pot_parent: str) -> bool:
+        """(``core/tree_structure.py:501-515``)"""
+        return self.nodes[pot_child].parent == pot_parent
+
+    def is_parent_of(self, pot_parent: str, pot_child: str) -> bool:
+        return self.is_child_of(pot_child, pot_parent)
+
     def same_connectivity_as(self, other) -> bool:
         """Same node ids, same neighbours (``core/tree_structure.py:389-408``)."""
         if set(self.nodes) != set(other.nodes):
@@ -505,6 +512,16 @@ class TreeTensorNetworkState(TreeTensorNetwork):
     """TTNS: one open (physical) leg per node (``ttns/ttns.py:18-444``)."""
 
     n_open = 1
+
+    def to_complex(self, precision: int = 128) -> "TreeTensorNetworkState":
+        """Stored tensors cast to complex128 (or complex64) (``ttns/ttns.py:423-444``);
+        the engine computes in complex128 whatever the stored type."""
+        if precision not in (64, 128):
+            raise ValueError("Precision must be either 64 or 128!")
+        dtype = np.complex128 if precision == 128 else np.complex64
+        for nid, t in list(self._phys.items()):
+            self._phys[nid] = np.asarray(t.detach().cpu().numpy() if hasattr(t, "detach") else t).astype(dtype)
+        return self
 
     def to_dense(self, site_order=None) -> np.ndarray:
         """Contract to a dense state vector (small trees only)."""

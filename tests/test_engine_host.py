@@ -1439,3 +1439,16 @@ def test_ttn_structure_comparisons():
     e.add_child_to_parent("r", np.ones((2, 1, 2), dtype=complex), 0, "a", 0)
     e.add_child_to_parent("b", np.ones((1, 2), dtype=complex), 0, "r", 1)
     assert a.same_connectivity_as(e) and not a.same_hierarchy_as(e)   # same edges, other root
+
+
+def test_ttn_parentage_and_to_complex():
+    import pytreenet_gb300 as P
+    t = P.TTNS()
+    t.add_root("r", np.ones((1, 2)))
+    t.add_child_to_parent("a", np.ones((1, 2)), 0, "r", 0)
+    assert t.is_child_of("a", "r") and t.is_parent_of("r", "a") and not t.is_child_of("r", "a")
+    assert t.to_complex() is t and t.tensors["a"].dtype == np.complex128
+    t.to_complex(64)
+    assert t.tensors["r"].dtype == np.complex64
+    with pytest.raises(ValueError):
+        t.to_complex(32)

@@ -42,6 +42,9 @@ class TimeEvoMode(Enum):
     BDF = "BDF"
     KRYLOV = "krylov"
 
+    def __str__(self) -> str:
+        return self.value
+
     @staticmethod
     def default_solver_options(mode) -> dict:
         if mode is TimeEvoMode.KRYLOV:

@@ -8,7 +8,11 @@ one sweep (run_one_time_step). Inputs are larger than L2 (the root tensor alone
 is 537 MB in complex128), so no L2 flush is needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--chi 256] [--arm 20]
+                  [--chi 256] [--arm 20] [--precision mixed|plain]
+  python bench.py --breakdown            # time per engine operation of one sweep
+  python bench.py --fidelity-sweeps 20   # mixed vs plain complex128 over 20 sweeps
+  python bench.py --impl reference --full-sweep   # one complete CPU oracle sweep
+  python bench.py --workload ternary|disorder|gradient   # the other configurations
 
 Multi-GPU: replicas only (a sweep is sequential); each rank advances its own
 realisation and ``value`` is the sum of sweeps over ranks / max time.
@@ -31,9 +35,12 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+
 def metric_name(args) -> str:
     return (f"TDVP sweeps/sec at chi={args.chi} (one-site, {3 * args.arm + 1}-site T-tree, "
             "Heisenberg+fields)")
+
+
 FP64_NOMINAL_TFLOPS = 1.25
 
 
@@ -53,6 +60,13 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison sweep")
     ap.add_argument("--no-graphs", action="store_true",
                     help="launch the QR sequences eagerly instead of replaying CUDA graphs")
+    ap.add_argument("--breakdown", action="store_true",
+                    help="time every engine operation of one sweep (synchronised) instead of the bench")
+    ap.add_argument("--fidelity-sweeps", type=int, default=0,
+                    help="run this many sweeps on the mixed and the plain path from one state and "
+                         "report fidelity and energy error after each")
+    ap.add_argument("--full-sweep", action="store_true",
+                    help="reference arm: time one complete oracle sweep and compare the per-operation model")
     ap.add_argument("--workload", default="ttree", choices=["ttree", "ternary", "disorder", "gradient"],
                     help="ttree: one-site TDVP on the T-tree (headline); ternary: second-order "
                          "two-site TDVP on the depth-3 ternary tree (40 sites, XXZ) with truncation; "
@@ -76,14 +90,17 @@ def config(args, precision):
 
 
 # ----------------------------------------------------------------------------
-# CPU baseline: the NumPy oracle on a bounded sample, extrapolated to a sweep
+# CPU baseline: the NumPy oracle, per-operation model of one sweep
 # ----------------------------------------------------------------------------
+# Operation classes of one oracle sweep: H_eff matvecs, environment updates, QR
+# splits and R absorptions by node degree, bond matvecs, and the Krylov vector
+# work (Gram-Schmidt step) by vector length. Counted in a dry run of the oracle
+# driver at chi=8 (the schedule and the Krylov depths do not depend on chi in
+# any material way), timed at the bench's chi.
 def oracle_schedule_counts(arm, tol, dt):
-    """Operation counts of one sweep, from a dry run of the oracle driver at chi=8
-    (the schedule and Krylov depths do not depend on chi in any material way)."""
     import oracle as O
     import oracle.ptn_oracle as OP
-    from pytreenet_gb300.workloads import t_tree_state, t_tree_heisenberg, t_tree_spec
+    from pytreenet_gb300.workloads import t_tree_state, t_tree_heisenberg
     st, spec, tensors = t_tree_state(arm_len=arm, chi=8, seed=0)
     H, W = t_tree_heisenberg(st, seed=1)
     tree = O.OTree()
@@ -92,16 +109,34 @@ def oracle_schedule_counts(arm, tol, dt):
     counts = {}
     deg = {nid: len(tree.neighbours(nid)) for nid, _ in spec}
 
-    def wrap(name, fn, key):
+    def bump(key):
+        counts[key] = counts.get(key, 0) + 1
+
+    def wrap(fn, key):
         def w(*a, **k):
-            nid = key(*a)
-            counts[(name, deg[nid])] = counts.get((name, deg[nid]), 0) + 1
+            bump(key(*a))
             return fn(*a, **k)
         return w
-    saved = (OP.heff_apply, OP.env_update, OP.qr_keep_split)
-    OP.heff_apply = wrap("heff", OP.heff_apply, lambda x, tree, nid, *r: nid)
-    OP.env_update = wrap("env", OP.env_update, lambda tree, nid, *r: nid)
-    OP.qr_keep_split = wrap("qr", OP.qr_keep_split, lambda state, nid, *r: nid)
+    saved = (OP.heff_apply, OP.env_update, OP.qr_keep_split, OP.bond_apply, OP.absorb_r, OP.krylov_exp_action)
+    OP.heff_apply = wrap(OP.heff_apply, lambda x, tree, nid, *r: ("heff", deg[nid]))
+    OP.env_update = wrap(OP.env_update, lambda tree, nid, *r: ("env", deg[nid]))
+    OP.qr_keep_split = wrap(OP.qr_keep_split, lambda state, nid, *r: ("qr", deg[nid]))
+    OP.bond_apply = wrap(OP.bond_apply, lambda *r: ("bond", 0))
+    OP.absorb_r = wrap(OP.absorb_r, lambda state, r, src, dst, *x: ("absorb", deg[dst]))
+    orig_kry = OP.krylov_exp_action
+
+    def kry(psi, action, *a, stats=None, **k):
+        # one Gram-Schmidt step per matvec; keyed by the vector's node class
+        n = psi.size
+        cls = 0 if psi.ndim == 2 and psi.shape[0] == psi.shape[1] and psi.shape[0] > 2 else psi.ndim - 1
+        local = []
+        out = orig_kry(psi, action, *a, stats=local, **k)
+        for m in local:
+            counts[("gs", cls)] = counts.get(("gs", cls), 0) + int(m)
+        if stats is not None:
+            stats.extend(local)
+        return out
+    OP.krylov_exp_action = kry
     try:
         algo = O.FirstOrderOneSiteTDVPOracle(O.OState(tree, tensors), W, dt, krylov_tol=tol)
         c0 = algo.state.orth_center
@@ -109,20 +144,53 @@ def oracle_schedule_counts(arm, tol, dt):
         counts.clear()
         algo.run_one_time_step()
     finally:
-        OP.heff_apply, OP.env_update, OP.qr_keep_split = saved
+        (OP.heff_apply, OP.env_update, OP.qr_keep_split, OP.bond_apply, OP.absorb_r,
+         OP.krylov_exp_action) = saved
     return counts
 
 
-def oracle_op_times(chi, reps=1):
-    """Seconds per oracle operation at this chi, by node degree (bounded sample)."""
+# classes timed in one sample: node degree 1, 2, 3, and the bond (0)
+OP_CLASSES = (1, 2, 3, 0)
+
+
+def oracle_op_times(chi, classes=OP_CLASSES, depth=4):
+    """Seconds per oracle operation at this chi for the given classes (one
+    timing each). ``gs`` is one Gram-Schmidt step of the oracle's Krylov
+    loop (norms, two passes over ``depth`` basis vectors: the mean over the
+    steps of a solve of depth ~7) at that vector length."""
     import oracle as O
+    import oracle.ptn_oracle as OP
     rng = np.random.default_rng(0)
     w, d = 5, 2
 
     def c(*s):
         return (rng.standard_normal(s) + 1j * rng.standard_normal(s)) / np.sqrt(2)
+
+    def timed(fn, *a):
+        t0 = time.perf_counter()
+        fn(*a)
+        return time.perf_counter() - t0
+
+    def gs_step(n):
+        Q = [c(n) for _ in range(depth)]
+        wv = c(n)
+
+        def run():
+            x = wv
+            np.linalg.norm(x)
+            for _ in range(2):
+                for q in Q:
+                    h = np.vdot(q, x)
+                    x = x - h * q
+            np.linalg.norm(x)
+        return timed(run)
     times = {}
-    for degn in (1, 2, 3):
+    for degn in classes:
+        if degn == 0:
+            r, eq, en = c(chi, chi), c(chi, w, chi), c(chi, w, chi)
+            times[("bond", 0)] = timed(OP.bond_apply, r, eq, en)
+            times[("gs", 0)] = gs_step(chi * chi)
+            continue
         tree = O.OTree()
         tree.add_root("v")
         for i in range(degn):
@@ -131,39 +199,35 @@ def oracle_op_times(chi, reps=1):
         x = c(*shape)
         W = c(*([w] * degn + [d, d]))
         envs = {(f"u{i}", "v"): c(chi, w, chi) for i in range(degn)}
-        t0 = time.perf_counter()
-        for _ in range(reps):
-            O.heff_apply(x, tree, "v", W, envs)
-        times[("heff", degn)] = (time.perf_counter() - t0) / reps
-        t0 = time.perf_counter()
-        for _ in range(reps):
-            O.env_update(tree, "v", "u0", x, W, envs)
-        times[("env", degn)] = (time.perf_counter() - t0) / reps
-        mat = x.reshape(-1, chi)
-        t0 = time.perf_counter()
-        for _ in range(reps):
-            np.linalg.qr(mat)
-        times[("qr", degn)] = (time.perf_counter() - t0) / reps
+        times[("heff", degn)] = timed(O.heff_apply, x, tree, "v", W, envs)
+        times[("env", degn)] = timed(O.env_update, tree, "v", "u0", x, W, envs)
+        state = O.OState(tree, {"v": x.copy(), **{f"u{i}": c(chi, d) for i in range(degn)}})
+        times[("qr", degn)] = timed(OP.qr_keep_split, state, "v", "u0")
+        times[("absorb", degn)] = timed(OP.absorb_r, state, c(chi, chi), "u0", "v", True)
+        times[("gs", degn)] = gs_step(x.size)
     return times
 
 
-def cpu_sweeps_per_s(args):
-    t0 = time.perf_counter()
-    counts = oracle_schedule_counts(args.arm, args.tol, args.dt)
-    times = oracle_op_times(args.chi)
-    sweep = sum(n * times.get(k, 0.0) for k, n in counts.items())
-    wall = time.perf_counter() - t0
-    return 1.0 / sweep, {"counts": {f"{a}/deg{b}": n for (a, b), n in sorted(counts.items())},
-                         "sample_seconds": round(wall, 2)}
+def model_sweep_seconds(counts, times):
+    missing = sorted({k for k in counts if k not in times})
+    if missing:
+        raise KeyError(f"no timing for {missing}")
+    return sum(n * times[k] for k, n in counts.items())
 
 
 def cpu_baseline_obj(args):
-    v, info = cpu_sweeps_per_s(args)
-    return {"value": v, "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
-            "sample": (f"NumPy oracle (OpenBLAS, all host threads): one heff matvec, env update and QR per "
-                       f"node degree at chi={args.chi}, weighted by the operation counts of one oracle sweep "
-                       f"(from a chi=8 dry run); {info['sample_seconds']} s of CPU work"),
-            "detail": info}
+    t0 = time.perf_counter()
+    counts = oracle_schedule_counts(args.arm, args.tol, args.dt)
+    times = oracle_op_times(args.chi)
+    sweep = model_sweep_seconds(counts, times)
+    wall = time.perf_counter() - t0
+    return {"value": 1.0 / sweep, "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": (f"NumPy oracle (OpenBLAS, all host threads): one H_eff matvec, environment update, "
+                       f"QR split and R absorption per node degree, one bond matvec and one Gram-Schmidt "
+                       f"step per vector length, at chi={args.chi}, weighted by the operation counts of "
+                       f"one oracle sweep (chi=8 dry run); {wall:.1f} s of CPU work"),
+            "detail": {"counts": {f"{a}/{b}": n for (a, b), n in sorted(counts.items())},
+                       "seconds_each": {f"{a}/{b}": t for (a, b), t in sorted(times.items())}}}
 
 
 # ----------------------------------------------------------------------------
@@ -235,27 +299,50 @@ def aggregate_over_ranks(local_ms: float, steps: int, world: int, dist=None, dev
 # ----------------------------------------------------------------------------
 # GPU arm
 # ----------------------------------------------------------------------------
+def _make_ttree(args, precision, seed, steps_total):
+    import pytreenet_gb300 as P
+    from pytreenet_gb300.workloads import t_tree_state, t_tree_heisenberg
+    st, spec, _ = t_tree_state(arm_len=args.arm, chi=args.chi, seed=seed)
+    H, _ = t_tree_heisenberg(st, seed=1000 + seed)
+    a = P.FirstOrderOneSiteTDVP(st, H, args.dt, args.dt * steps_total, {},
+                                config=P.TDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV),
+                                solver_options={"krylov_tol": args.tol}, precision=precision)
+    a.net.normalise_center()
+    a.net.use_graphs = not args.no_graphs
+    return a, H
+
+
+def _measured_peak(kind: str):
+    """Roofline denominator from MEASURED_PEAKS.json. The heff chain is timed
+    inside a sweep of about a second, so the sustained tensor figure applies."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(path))
+        if kind == "tensor":
+            return float(d["bf16_tflops_sustained"]), "MEASURED_PEAKS.json bf16_tflops_sustained (cuBLAS, of measured)"
+        return float(d["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (copy, of measured)"
+    except Exception:
+        if kind == "tensor":
+            return 1700.0, "fallback 1.7 PFLOP/s bf16 sustained (MEASURED_PEAKS.json absent), of fallback"
+        return 6800.0, "fallback 6.8 TB/s (MEASURED_PEAKS.json absent), of fallback"
+
+
+# DRAM bytes per launch of the root-matvec tensor-core steps, from the ncu
+# capture summarised in profiles/cgemm_bf16x6_root_matvec_chi256.md (filled in
+# once that capture exists; None until then).
+ROOT_MATVEC_DRAM_BYTES = None
+
+
 def run_gb300(args, rank, world):
     import torch
-    import pytreenet_gb300 as P
     from pytreenet_gb300 import _lib
-    from pytreenet_gb300.workloads import t_tree_state, t_tree_heisenberg
     dist = None
     if world > 1:
         import torch.distributed as dist
     lib = _lib.load()
-    def make(precision):
-        st, spec, _ = t_tree_state(arm_len=args.arm, chi=args.chi, seed=rank)
-        H, _ = t_tree_heisenberg(st, seed=1000 + rank)
-        total = args.warmup + 2 * args.steps + 1
-        a = P.FirstOrderOneSiteTDVP(st, H, args.dt, args.dt * total, {},
-                                    config=P.TDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV),
-                                    solver_options={"krylov_tol": args.tol}, precision=precision)
-        a.net.normalise_center()
-        return a
-    algo = make(args.precision)
+    total = args.warmup + 2 * args.steps + 1
+    algo, H = _make_ttree(args, args.precision, rank, total)
     net = algo.net
-    net.use_graphs = not args.no_graphs
     for _ in range(args.warmup):
         algo.run_one_time_step()
     torch.cuda.synchronize()
@@ -274,7 +361,7 @@ def run_gb300(args, rank, world):
             e0.record()
             run(xp, yp)
             e1.record()
-            heff_events.append((e0, e1, p.flops))
+            heff_events.append((e0, e1, p.flops, nid))
         p.run = run_timed
         try:
             return orig(nid, *a, **k)
@@ -285,6 +372,7 @@ def run_gb300(args, rank, world):
         dist.barrier()
     torch.cuda.synchronize()
     l0 = lib.ptn_launch_counter() + net.graph_launches
+    c0 = (net.cholqr_count, net.householder_count, net.qr_rows_skipped, len(net.krylov.depths))
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with Clocks(torch.cuda.current_device()) as clk:
         torch.cuda.nvtx.range_push("timed_region")
@@ -299,122 +387,237 @@ def run_gb300(args, rank, world):
     launches = int(lib.ptn_launch_counter() + net.graph_launches - l0)
     net.evolve_site = orig
     ms = start.elapsed_time(stop)
-    heff_ms = sum(a.elapsed_time(b) for a, b, _ in heff_events)
-    heff_flops = sum(f for _, _, f in heff_events)
+    heff_ms = sum(a.elapsed_time(b) for a, b, _, _ in heff_events)
+    heff_flops = sum(f for _, _, f, _ in heff_events)
+    root_ev = [(a.elapsed_time(b), f) for a, b, f, nid in heff_events if nid == "root"]
     n_heff = len(heff_events)
     value, t_max = aggregate_over_ranks(ms, args.steps, world, dist, "cuda")
+    qr_stats = {"cholqr2_splits": (net.cholqr_count - c0[0]) / args.steps,
+                "householder_splits": (net.householder_count - c0[1]) / args.steps,
+                "zero_rows_skipped": (net.qr_rows_skipped - c0[2]) / args.steps,
+                "cholqr2_rejected_keys": len(net.cholqr_fails), "per": "sweep"}
+    depths = net.krylov.depths[c0[3]:]
 
-    # -- end to end: state uploaded from pinned host memory, sweep, state read back
+    # -- end to end through the public API: every sweep the caller's state goes
+    # up from host memory (TTNS.tensors[node] = array, written into the running
+    # driver's device buffers) and comes back (TTNS.tensors[node] -> NumPy)
     e2e = None
     if not args.no_e2e:
-        pinned = {nid: torch.empty(net.t[nid].shape, dtype=net.t[nid].dtype, pin_memory=True)
-                  for nid in net.t}
-        for nid, t in net.t.items():
-            pinned[nid].copy_(t)
-        nbytes = sum(t.numel() * t.element_size() for t in net.t.values())
+        st = algo.state
+        host = {nid: np.array(st.tensors[nid]) for nid in st._order}
+        nbytes = sum(a.nbytes for a in host.values())
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
         w0 = time.perf_counter()
         for _ in range(args.steps):
-            for nid, t in net.t.items():
-                t.copy_(pinned[nid], non_blocking=True)
+            for nid, a in host.items():
+                st.tensors[nid] = a
             algo.run_one_time_step()
-            for nid, t in net.t.items():
-                pinned[nid].copy_(t, non_blocking=True)
-            torch.cuda.synchronize()
+            host = {nid: st.tensors[nid] for nid in st._order}
+        torch.cuda.synchronize()
         w1 = time.perf_counter()
         e2e_value, _ = aggregate_over_ranks((w1 - w0) * 1000.0, args.steps, world, dist, "cuda")
-        e2e = {"value": e2e_value, "unit": "sweeps/s",
-               "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes}
+        e2e = {"value": e2e_value, "unit": "sweeps/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+               "how": "TTNS.tensors[node] = host array before each sweep, TTNS.tensors[node] after it "
+                      "(run_one_time_step on the public driver)"}
 
     achieved = heff_flops / (heff_ms / 1000.0) / 1e12 if heff_ms > 0 else None
     if args.precision == "mixed":
-        peak, peak_src = _measured_bf16_peak()
-        # algorithmic complex flops (8 per complex MAC); the BF16x3 split issues 3x that on the pipe
-        roof = {"bound": "tensor", "kernel": "ptn_cgemm_bf16x3 (heff matvec chain, tcgen05, 3 split levels)",
+        peak, peak_src = _measured_peak("tensor")
+        roof = {"bound": "tensor", "kernel": "H_eff matvec chain: cgemm_bf16_kernel<3> (tcgen05, BF16x6) + "
+                                             "operand conversions",
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": (achieved / peak) if achieved else None,
-                "peak_source": peak_src + "; achieved counts algorithmic complex flops, the BF16x6 "
-                               "split issues 6x as many tensor flops",
-                "traffic": None}
+                "peak_source": peak_src + "; achieved counts algorithmic complex flops (8 per complex MAC); "
+                               "the BF16x6 split issues 6x as many tensor flops",
+                "traffic": ROOT_MATVEC_DRAM_BYTES}
     else:
-        roof = {"bound": "tensor", "kernel": "ptn_zcontract (heff matvec chain, FP64)",
+        roof = {"bound": "tensor", "kernel": "H_eff matvec chain: zcontract_kernel (FP64)",
                 "achieved": achieved, "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
                 "frac": (achieved / FP64_NOMINAL_TFLOPS) if achieved else None,
                 "peak_source": "nominal GB300 FP64 (1.25 TFLOP/s); FP64 is not in MEASURED_PEAKS.json",
                 "traffic": None}
     roof.update({
-            "algorithmic_flops_per_matvec": heff_flops / max(n_heff, 1),
-            "matvecs_timed": n_heff, "matvec_ms_total": heff_ms, "share_of_step": heff_ms / ms})
+        "algorithmic_flops_per_matvec": heff_flops / max(n_heff, 1),
+        "matvecs_timed": n_heff, "matvec_ms_total": heff_ms, "share_of_step": heff_ms / ms})
+    if root_ev:
+        rt = sum(t for t, _ in root_ev)
+        roof["root_matvec"] = {"count": len(root_ev), "ms_each": rt / len(root_ev),
+                               "tflops_algorithmic": sum(f for _, f in root_ev) / (rt / 1000.0) / 1e12}
     plain = None
     if args.precision == "mixed" and not args.no_plain and rank == 0:
-        plain = compare_with_plain(args, make)
+        plain = compare_with_plain(args, 1)
         plain["speedup_mixed_over_plain"] = value / plain["sweeps_per_s"]
     line = {"metric": metric_name(args), "value": value, "unit": "sweeps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
             "dtype": "bf16x6 split (tcgen05, fp32 accumulate) contractions / f64 Krylov+QR" if args.precision == "mixed" else "c128 (fp64)",
             "data": "synthetic",
-            "config": config(args, "mixed: BF16x6 (3-level split) tcgen05 contractions, FP32 accumulate, FP64 Krylov/QR/norm"
+            "config": config(args, "mixed: BF16x6 (3-level split) tcgen05 contractions, FP32 accumulate, FP64 Krylov; "
+                                   "CholeskyQR2 (tensor-core Gram, FP32 device Cholesky) for full-rank splits, "
+                                   "FP64 Householder otherwise"
                              if args.precision == "mixed" else "plain complex128"),
-            "roofline": roof, "e2e": e2e, "plain_fp64": plain,
+            "roofline": roof, "e2e": e2e, "plain_fp64": plain, "qr": qr_stats,
             "gpu_launches": launches, "clocks": clk.summary(),
-            "krylov_depth_mean": float(np.mean(net.krylov.depths[-n_heff:])) if n_heff else None}
+            "krylov_depth_mean": float(np.mean(depths)) if depths else None}
     return line
 
 
-def _measured_bf16_peak():
-    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    try:
-        d = json.load(open(path))
-        return float(d["bf16_tflops"]), "MEASURED_PEAKS.json bf16_tflops (burst, cuBLAS), of measured"
-    except Exception:
-        return 1900.0, "fallback 1.9 PFLOP/s bf16 (MEASURED_PEAKS.json absent), of fallback"
-
-
-def compare_with_plain(args, make):
-    """One sweep on the plain complex128 path from the same initial state as one
-    sweep on the mixed path: plain sweep time and the fidelity error of the
-    mixed result (1 - |<mixed|plain>| / (|mixed| |plain|))."""
+def compare_with_plain(args, sweeps: int):
+    """``sweeps`` sweeps on the plain complex128 path and on the mixed path
+    from the same initial state: plain sweep time, the fidelity error
+    1 - |<mixed|plain>| / (|mixed| |plain|) after each sweep, and (last sweep)
+    the energy <H> of both states evaluated in complex128."""
     import torch
-    a_m = make("mixed")
-    a_m.run_one_time_step()
-    a_p = make("plain")
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    a_p.run_one_time_step()
-    e1.record()
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    ov = a_m.net.overlap(a_p.net)
-    nm = a_m.net.overlap(a_m.net).real
-    npl = a_p.net.overlap(a_p.net).real
-    err = 1.0 - abs(ov) / np.sqrt(nm * npl)
-    t = args.dt
-    return {"sweeps_per_s": 1000.0 / ms, "ms_per_sweep": ms, "fidelity_error_one_sweep": err,
-            "fidelity_error_per_unit_time": err / t, "sweeps_compared": 1}
+    a_m, H = _make_ttree(args, "mixed", 0, sweeps + 2)
+    a_p, _ = _make_ttree(args, "plain", 0, sweeps + 2)
+    hist = []
+    ms_p = 0.0
+    for i in range(sweeps):
+        a_m.run_one_time_step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        a_p.run_one_time_step()
+        e1.record()
+        torch.cuda.synchronize()
+        ms_p += e0.elapsed_time(e1)
+        ov = a_m.net.overlap(a_p.net)
+        nm = a_m.net.overlap(a_m.net).real
+        npl = a_p.net.overlap(a_p.net).real
+        hist.append(float(1.0 - abs(ov) / np.sqrt(nm * npl)))
+    e_m = a_m.net.expect_ttno(H).real / a_m.net.overlap(a_m.net).real
+    e_p = a_p.net.expect_ttno(H).real / a_p.net.overlap(a_p.net).real
+    t = args.dt * sweeps
+    return {"sweeps_per_s": 1000.0 * sweeps / ms_p, "ms_per_sweep": ms_p / sweeps,
+            "sweeps_compared": sweeps, "fidelity_error": hist[-1], "fidelity_error_history": hist,
+            "fidelity_error_per_unit_time": hist[-1] / t, "energy_mixed": e_m, "energy_plain": e_p,
+            "energy_error": abs(e_m - e_p), "energy_error_relative": abs(e_m - e_p) / abs(e_p),
+            "reference": "the plain complex128 GPU path (FP64 contractions, Householder QR), "
+                         "from the same initial state"}
+
+
+def run_breakdown(args):
+    """Time of every engine operation of one sweep, each bracketed by device
+    synchronisations (two warm sweeps first: plans built, QR graphs captured)."""
+    import torch
+    from collections import defaultdict
+    from pytreenet_gb300 import engine as E
+    acc, cnt = defaultdict(float), defaultdict(int)
+    algo, _ = _make_ttree(args, args.precision, 0, 10)
+    last = f"_{args.arm - 1}"
+
+    def cls(nid):
+        return "root" if nid == "root" else ("leaf" if nid.endswith(last) else "arm")
+    saved = {}
+
+    def wrap(name, key):
+        orig = getattr(E.DeviceNetwork, name)
+        saved[name] = orig
+
+        def timed(self, *a, **kw):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            r = orig(self, *a, **kw)
+            torch.cuda.synchronize()
+            k = f"{name}:{key(*a)}"
+            acc[k] += time.perf_counter() - t
+            cnt[k] += 1
+            return r
+        setattr(E.DeviceNetwork, name, timed)
+    wrap("evolve_site", lambda nid, *r: cls(nid))
+    wrap("evolve_bond", lambda r, nid, *x: cls(nid))
+    wrap("update_env", lambda nid, *x: cls(nid))
+    wrap("qr_split", lambda nid, *x: cls(nid))
+    wrap("absorb", lambda R, src, dst, *x: cls(dst))
+    try:
+        for _ in range(2):
+            algo.run_one_time_step()
+        acc.clear()
+        cnt.clear()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        algo.run_one_time_step()
+        torch.cuda.synchronize()
+        total = time.perf_counter() - t
+    finally:
+        for name, orig in saved.items():
+            setattr(E.DeviceNetwork, name, orig)
+    rows = {k: {"ms": acc[k] * 1e3, "share": acc[k] / total, "calls": cnt[k],
+                "ms_each": acc[k] * 1e3 / max(cnt[k], 1)} for k in sorted(acc, key=lambda k: -acc[k])}
+    for k, r in rows.items():
+        print(f"{k:24s} {r['ms']:9.1f} ms  {100 * r['share']:5.1f} %  n={r['calls']:4d}  {r['ms_each']:8.3f} ms each",
+              file=sys.stderr)
+    return {"metric": "per-operation time of one sweep (synchronised)", "workload": config(args, args.precision),
+            "sweep_ms": total * 1e3, "operations": rows,
+            "qr": {"cholqr2": algo.net.cholqr_count, "householder": algo.net.householder_count}}
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the NumPy oracle's per-operation model of one sweep
+    (see oracle_op_times), each step re-timing one operation class in turn
+    (degree 1, 2, 3 nodes, the bond) so the run ends in minutes; the warm-up
+    steps time every class once."""
     if rank != 0:
         return None
+    counts = oracle_schedule_counts(args.arm, args.tol, args.dt)
+    times = {}
     samples = []
     for i in range(args.warmup + args.steps):
-        v, info = cpu_sweeps_per_s(args)
+        classes = OP_CLASSES if i == 0 else (OP_CLASSES[i % len(OP_CLASSES)],)
+        times.update(oracle_op_times(args.chi, classes))
         if i >= args.warmup:
-            samples.append(1.0 / v)
+            samples.append(model_sweep_seconds(counts, times))
     v = 1.0 / float(np.mean(samples))
     cb = {"value": v, "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
-          "sample": (f"NumPy oracle restatement of the reference algorithm; each step times one heff "
-                     f"matvec, env update and QR per node degree at chi={args.chi} and weights them by "
-                     f"one sweep's operation counts")}
+          "sample": (f"NumPy oracle restatement of the reference algorithm, all host threads: per-operation "
+                     f"model of one sweep at chi={args.chi} (H_eff matvecs, environment updates, QR splits, R "
+                     f"absorptions, bond matvecs, Gram-Schmidt steps, weighted by one oracle sweep's counts); "
+                     f"each step re-times one operation class")}
     return {"metric": metric_name(args), "value": v, "unit": "sweeps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c128 (fp64)", "data": "synthetic",
             "config": config(args, "plain complex128 (CPU)"), "impl": "reference", "cpu_baseline": cb,
             "e2e": {"value": v, "unit": "sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def run_reference_full_sweep(args):
+    """One complete sweep of the NumPy oracle at the bench's config (canonical
+    form and initial environments untimed), beside the per-operation model's
+    prediction for the same sweep."""
+    import oracle as O
+    from pytreenet_gb300.workloads import t_tree_state, t_tree_heisenberg
+    st, spec, tensors = t_tree_state(arm_len=args.arm, chi=args.chi, seed=0)
+    H, W = t_tree_heisenberg(st, seed=1000)
+    tree = O.OTree()
+    for nid, p in spec:
+        tree.add_root(nid) if p is None else tree.add_child(nid, p)
+    t0 = time.perf_counter()
+    algo = O.FirstOrderOneSiteTDVPOracle(O.OState(tree, tensors), W, args.dt, krylov_tol=args.tol)
+    c0 = algo.state.orth_center
+    algo.state.tensors[c0] = algo.state.tensors[c0] / np.linalg.norm(algo.state.tensors[c0])
+    setup = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    algo.run_one_time_step()
+    sweep = time.perf_counter() - t0
+    counts = oracle_schedule_counts(args.arm, args.tol, args.dt)
+    times = oracle_op_times(args.chi)
+    model = model_sweep_seconds(counts, times)
+    return {"metric": metric_name(args) + " -- one complete oracle sweep", "value": 1.0 / sweep,
+            "unit": "sweeps/s", "seconds": sweep, "setup_seconds": setup, "model_seconds": model,
+            "model_error_relative": (model - sweep) / sweep, "cores": os.cpu_count(),
+            "krylov_depth_mean": float(np.mean(algo.krylov_dims)) if algo.krylov_dims else None,
+            "impl": "reference", "config": config(args, "plain complex128 (CPU)")}
+
+
+def run_fidelity(args):
+    import torch
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    r = compare_with_plain(args, args.fidelity_sweeps)
+    r.update({"metric": f"mixed vs plain complex128 over {args.fidelity_sweeps} sweeps",
+              "config": config(args, "mixed (BF16x6) vs plain (complex128)")})
+    return r
 
 
 def run_two_site(args):
@@ -454,7 +657,7 @@ def run_two_site(args):
     ms = start.elapsed_time(stop)
     launches = int(lib.ptn_launch_counter() + algo.net.graph_launches - l0)
     bonds = sorted({int(x) for x in algo.bond_dims_history[-20:]})
-    return {"metric": f"two-site TDVP steps/sec (ternary depth 3, 40 sites, XXZ, chi_max={args.chi_max})",
+    line = {"metric": f"two-site TDVP steps/sec (ternary depth 3, 40 sites, XXZ, chi_max={args.chi_max})",
             "value": args.steps / (ms / 1000.0), "unit": "steps/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
@@ -466,6 +669,19 @@ def run_two_site(args):
                        "start": "random state at the saturated bond dimensions"},
             "gpu_launches": launches, "clocks": clk.summary(), "recent_bond_dims": bonds,
             "krylov_depth_mean": float(np.mean(algo.net.krylov.depths)) if algo.net.krylov.depths else None}
+    if args.precision == "mixed" and not args.no_plain:
+        # the same number of steps on the plain path from the same state
+        ref = make("plain")
+        other = make("mixed")
+        for _ in range(args.steps):
+            ref.run_one_time_step()
+            other.run_one_time_step()
+        ov = other.net.overlap(ref.net)
+        f = 1.0 - abs(ov) / np.sqrt(other.net.overlap(other.net).real * ref.net.overlap(ref.net).real)
+        line["plain_fp64"] = {"steps_compared": args.steps, "fidelity_error": float(f),
+                              "fidelity_error_per_unit_time": float(f) / (0.02 * args.steps),
+                              "same_bond_dims": list(ref.bond_dims_history) == list(other.bond_dims_history)}
+    return line
 
 
 def run_disorder(args):
@@ -577,22 +793,22 @@ def run_gradient(args):
 
 def main():
     args = parse()
-    if args.workload == "gradient":
+    if args.impl == "reference" and args.full_sweep:
+        print(json.dumps(run_reference_full_sweep(args)), flush=True)
+        return
+    single = {"gradient": run_gradient, "disorder": run_disorder, "ternary": run_two_site}
+    if args.impl == "gb300" and (args.workload in single or args.breakdown or args.fidelity_sweeps):
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
-        if args.chi == 256:
+        if args.workload == "gradient" and args.chi == 256:
             args.chi = 64
-        print(json.dumps(run_gradient(args)), flush=True)
-        return
-    if args.workload == "disorder":
-        import torch
-        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
-        print(json.dumps(run_disorder(args)), flush=True)
-        return
-    if args.workload == "ternary":
-        import torch
-        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
-        print(json.dumps(run_two_site(args)), flush=True)
+        if args.breakdown:
+            fn = run_breakdown
+        elif args.fidelity_sweeps:
+            fn = run_fidelity
+        else:
+            fn = single[args.workload]
+        print(json.dumps(fn(args)), flush=True)
         return
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))

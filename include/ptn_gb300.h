@@ -119,6 +119,55 @@ int64_t ptn_zqr_work_bytes(int64_t m, int64_t k);
 int ptn_zqr_keep(void* A, const int64_t* rowoff, int64_t m, int64_t k, int64_t colstride,
                  void* R, void* work, void* stream);
 
+/* Same result as ptn_zqr_keep on the m x k matrix when its rows m_used..m-1
+ * (in rowoff order) are exactly zero: the factorisation runs on the first
+ * m_used rows with the kernel sequence of the m-row problem (so the same
+ * rounding), and the steps that would meet a zero column are written directly
+ * (R rows zero, Q column j = e_j for m_used <= j < min(m, k)). Replaces the
+ * same np.linalg.qr call as ptn_zqr_keep; the zero rows are the padded bond
+ * indices a KEEP split leaves behind, so near-leaf splits of a padded or
+ * low-rank state skip most of their Householder steps. */
+int ptn_zqr_keep_rows(void* A, const int64_t* rowoff, int64_t m, int64_t m_used, int64_t k, int64_t colstride,
+                      void* R, void* work, void* stream);
+
+/* out[0] (device int64) = 1 + the largest row index i (in rowoff order) with a
+ * nonzero entry of the m x k matrix, 0 for a zero matrix: the m_used that
+ * ptn_zqr_keep_rows may be given. No counterpart in the reference. */
+int ptn_znonzero_rows(const void* A, const int64_t* rowoff, int64_t m, int64_t k, int64_t colstride,
+                      int64_t* out, void* stream);
+
+/* ---- CholeskyQR2 factors (mixed-precision QR split) ---------------------------
+ * The mixed-precision path splits tall full-rank site matrices (the QR of
+ * tensor_qr_decomposition, util/tensor_splitting.py:60-107) by CholeskyQR2:
+ * Gram matrices and products with R^{-1} on the tensor cores, and these k x k
+ * steps on the device, so no host round trip sits between them.
+ *
+ * G (k x k, row-major, leading dimension ldg, Hermitian up to rounding; its
+ * Hermitian part is used) = R^H R with R upper triangular: writes R and R^{-1}
+ * (k x k row-major, zero below the diagonal). Computed in FP32 on one CTA.
+ * status (device int32) is set to PTN_ERR_NOCONVERGE when a pivot is not
+ * positive or the smallest diagonal entry of R is not above pivot_ratio times
+ * the largest (the matrix is not of full numerical rank; the caller falls back
+ * to Householder). series != 0: when ||G - I||_F <= series_tol the first-order
+ * factor R = I + U, R^{-1} = I - U (U = strict upper part of G - I plus half
+ * its diagonal) is written instead (second pass of CholeskyQR2, whose Gram
+ * matrix is the identity up to the first pass's rounding). work:
+ * ptn_zchol_work_bytes(k) bytes (16-byte aligned); k <= ptn_zchol_max_k(). */
+int64_t ptn_zchol_work_bytes(int64_t k);
+int64_t ptn_zchol_max_k(void);
+int ptn_zchol_upper(const void* G, int64_t ldg, int64_t k, void* R, void* Rinv, double pivot_ratio,
+                    int32_t series, double series_tol, int32_t* status, void* work, void* stream);
+
+/* C = A B for upper-triangular k x k row-major A, B (C must not alias them),
+ * in FP64: X = R1^{-1} R2^{-1} and R2 R1 of CholeskyQR2. */
+int ptn_ztri_mul_upper(const void* A, const void* B, void* C, int64_t k, void* stream);
+
+/* R = R0 (2I - X R0) in FP64 for upper-triangular k x k X, R0 (one Newton step
+ * toward X^{-1}; work: k x k complex128). CholeskyQR2 writes Q = A X and
+ * returns this R, so that Q R reproduces A to FP64 rounding whatever the
+ * FP32 error of the factors. No argument may alias another. */
+int ptn_ztri_inv_newton(const void* X, const void* R0, void* R, void* work, int64_t k, void* stream);
+
 /* ---- Mixed precision (tcgen05 tensor cores, BF16x3, FP32 accumulation) -------
  * C[m, n] = sum_k A[m, k] * B[n, k] over complex numbers; A and B are given as
  * `levels` BF16 pieces (2: ~16-bit mantissa, products i+j<2 = "BF16x3";
@@ -161,11 +210,6 @@ typedef struct {
 } ptn_convert_desc;
 int ptn_to_planes(const ptn_convert_desc* d, void* stream);
 int ptn_expand_b(const ptn_convert_desc* d, void* stream);
-
-/* Self-test of the tcgen05 descriptors: D[128][128] (fp32) = A[128][64] * B[128][64]^T
- * for bf16 A, B (K contiguous); one CTA; sw64 != 0 stages K as two 64-byte-swizzled
- * tiles instead of one 128-byte-swizzled tile. */
-int ptn_tc_selftest(const void* A, const void* B, void* D, int32_t* status, int32_t sw64, void* stream);
 
 /* Same as ptn_zqr_keep, but without a caller-provided work buffer. This entry
  * point has no counterpart in the reference. It is meant for callers that

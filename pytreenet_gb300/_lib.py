@@ -107,11 +107,18 @@ SIGNATURES = {
     "ptn_launch_counter": (ctypes.c_ulonglong, []),
     "ptn_zqr_noalloc_max_bytes": (_I64, []),
     "ptn_zqr_keep_noalloc": (ctypes.c_int, [_P, _P, _I64, _I64, _I64, _P, _P]),
+    "ptn_zqr_keep_rows": (ctypes.c_int, [_P, _P, _I64, _I64, _I64, _I64, _P, _P, _P]),
+    "ptn_znonzero_rows": (ctypes.c_int, [_P, _P, _I64, _I64, _I64, _P, _P]),
+    "ptn_zchol_work_bytes": (_I64, [_I64]),
+    "ptn_zchol_max_k": (_I64, []),
+    "ptn_zchol_upper": (ctypes.c_int, [_P, _I64, _I64, _P, _P, ctypes.c_double, _I32, ctypes.c_double, _P, _P,
+                                       _P]),
+    "ptn_ztri_mul_upper": (ctypes.c_int, [_P, _P, _P, _I64, _P]),
+    "ptn_ztri_inv_newton": (ctypes.c_int, [_P, _P, _P, _P, _I64, _P]),
     "ptn_cgemm_bf16x3": (ctypes.c_int, [ctypes.POINTER(CgemmDesc), _P]),
     "ptn_cgemm_smem_bytes": (ctypes.c_int, [_I32]),
     "ptn_to_planes": (ctypes.c_int, [ctypes.POINTER(ConvertDesc), _P]),
     "ptn_expand_b": (ctypes.c_int, [ctypes.POINTER(ConvertDesc), _P]),
-    "ptn_tc_selftest": (ctypes.c_int, [_P, _P, _P, _P, _I32, _P]),
     "ptn_zsvd_work_bytes": (_I64, [_I64, _I64]),
     "ptn_zsvd_jacobi": (ctypes.c_int, [ctypes.POINTER(SvdDesc), _P]),
     "ptn_zpermute": (ctypes.c_int, [ctypes.POINTER(PermuteDesc), _P]),

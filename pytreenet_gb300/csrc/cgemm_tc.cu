@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   constexpr uint32_t ACC_COLS = 2 * NT;          // one accumulator: [Re | Im]
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  __shared__ uint64_t full_bar[STAGES], empty_bar[STAGES], tfull_bar[2], tempty_bar[2];
+  __shared__ uint64_t full_bar[STAGES], empty_bar[STAGES], tfull_bar[2], tempty_bar[2], drain_bar;
   __shared__ uint32_t tmem_base;
   __shared__ int64_t noff[NT];
   __shared__ int s_abort;
@@ -108,6 +108,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       tc::mbar_init(&tfull_bar[b], 1);
       tc::mbar_init(&tempty_bar[b], 4);   // one arrival per epilogue warp
     }
+    tc::mbar_init(&drain_bar, 1);
     tc::fence_mbar_init();
   }
   if (warp == 1) {
@@ -129,11 +130,14 @@ __global__ void __launch_bounds__(THREADS, 1)
     if (lane == 0) {
       tc::prefetch_tmap(&tmA);
       tc::prefetch_tmap(&tmB);
+      int issued = 0;
+      bool aborted = false;
       for (int kt = 0; kt < ktiles; ++kt) {
         const int s = kt % STAGES;
         const int use = kt / STAGES;
         if (use > 0 && !tc::mbar_wait_abortable(&empty_bar[s], (use - 1) & 1, WAIT_CYCLES, vstatus)) {
           atomicExch(g.status, PTN_ERR_TIMEOUT);
+          aborted = true;
           break;
         }
         uint8_t* st = smem + s * STAGE_BYTES;
@@ -143,6 +147,17 @@ __global__ void __launch_bounds__(THREADS, 1)
           tc::tma_load_3d(st + p * A_PLANE_BYTES, &tmA, &full_bar[s], kx, (int)m0, p);
         for (int b = 0; b < 3 * L; ++b)
           tc::tma_load_3d(st + A_STAGE_BYTES + b * B_BLOCK_BYTES, &tmB, &full_bar[s], kx, (int)n0, b);
+        ++issued;
+      }
+      if (aborted) {
+        // Drain before the CTA gives up its shared memory: wait (bounded) for
+        // the last load issued into each stage. A stage's phase for its last
+        // use is the only one still to complete, so a completed one returns
+        // at once.
+        for (int s = 0; s < STAGES && s < issued; ++s) {
+          const int kt_last = s + ((issued - 1 - s) / STAGES) * STAGES;
+          tc::mbar_wait(&full_bar[s], (uint32_t)((kt_last / STAGES) & 1), WAIT_CYCLES);
+        }
       }
     }
   } else if (warp == 1) {
@@ -153,17 +168,21 @@ __global__ void __launch_bounds__(THREADS, 1)
     // accumulations it absorbs, so this bounds that loss to one tile.
     if (lane == 0) {
       const uint32_t idesc = tc::idesc_bf16(MT, 2 * NT);
+      bool aborted = false, any_mma = false;
       for (int kt = 0; kt < ktiles; ++kt) {
         const int s = kt % STAGES;
         const int b = kt & 1, ub = kt >> 1;
         if (ub > 0 && !tc::mbar_wait_abortable(&tempty_bar[b], (ub - 1) & 1, WAIT_CYCLES, vstatus)) {
           atomicExch(g.status, PTN_ERR_TIMEOUT);
+          aborted = true;
           break;
         }
         if (!tc::mbar_wait_abortable(&full_bar[s], (kt / STAGES) & 1, WAIT_CYCLES, vstatus)) {
           atomicExch(g.status, PTN_ERR_TIMEOUT);
+          aborted = true;
           break;
         }
+        any_mma = true;
         tc::fence_after();
         const uint32_t sa = tc::smem_u32(smem + s * STAGE_BYTES);
         const uint32_t sb = sa + A_STAGE_BYTES;
@@ -192,6 +211,11 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
         tc::mma_commit(&empty_bar[s]);
         tc::mma_commit(&tfull_bar[b]);
+      }
+      if (aborted && any_mma) {
+        // every MMA this thread issued completes before TMEM is freed
+        tc::mma_commit(&drain_bar);
+        tc::mbar_wait(&drain_bar, 0, WAIT_CYCLES);
       }
     }
   } else {

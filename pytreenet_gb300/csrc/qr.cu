@@ -395,13 +395,48 @@ static int zqr_keep_small(double2* A, const int64_t* rowoff, int64_t m, int64_t 
   return ptn_launch_status();
 }
 
+// Q[j, j] = 1 for j in [lo, hi): the columns that Householder steps with an
+// exactly-zero remaining column (tau = 0) leave as unit vectors.
+__global__ void unit_diag_kernel(double2* __restrict__ A, const int64_t* __restrict__ rowoff, int64_t cs,
+                                 int64_t lo, int64_t hi) {
+  const int64_t j = lo + blockIdx.x * (int64_t)QT + threadIdx.x;
+  if (j < hi) A[rowoff[j] + j * cs] = make_double2(1.0, -0.0);
+}
+
+static int zqr_keep_impl(double2* A, const int64_t* rowoff, int64_t m_path, int64_t m, int64_t k, int64_t cs,
+                         double2* R, void* work, cudaStream_t s);
+
 extern "C" int ptn_zqr_keep(void* Av, const int64_t* rowoff, int64_t m, int64_t k, int64_t cs, void* Rv,
                             void* work, void* stream) {
   if (!Av || !rowoff || !Rv || !work || m < 1 || k < 1 || cs < 1) return PTN_ERR_ARG;
+  return zqr_keep_impl(static_cast<double2*>(Av), rowoff, m, m, k, cs, static_cast<double2*>(Rv), work,
+                       ptn_stream(stream));
+}
+
+extern "C" int ptn_zqr_keep_rows(void* Av, const int64_t* rowoff, int64_t m, int64_t m_used, int64_t k, int64_t cs,
+                                 void* Rv, void* work, void* stream) {
+  if (!Av || !rowoff || !Rv || !work || m < 1 || k < 1 || cs < 1 || m_used < 1 || m_used > m) return PTN_ERR_ARG;
   cudaStream_t s = ptn_stream(stream);
   double2* A = static_cast<double2*>(Av);
-  double2* R = static_cast<double2*>(Rv);
-  if (m <= QR_SMALL_M) return zqr_keep_small(A, rowoff, m, k, cs, R, work, s);
+  int st = zqr_keep_impl(A, rowoff, m, m_used, k, cs, static_cast<double2*>(Rv), work, s);
+  if (st != PTN_OK) return st;
+  // Rows m_used.. are zero, so every step j >= m_used of the full factorisation
+  // meets a zero column (tau = 0, beta = 0): R keeps zero rows there and Q the
+  // unit vector e_j in column j (up to min(m, k)); columns past min(m, k) stay
+  // zero (KEEP padding), as the call on m_used rows already left them.
+  const int64_t hi = m < k ? m : k;
+  if (m_used < hi) {
+    PTN_COUNT(1);
+    unit_diag_kernel<<<(unsigned)((hi - m_used + QT - 1) / QT), QT, 0, s>>>(A, rowoff, cs, m_used, hi);
+  }
+  return ptn_launch_status();
+}
+
+// Householder QR of the first m rows, with the kernel sequence (and so the
+// rounding) of an m_path-row problem.
+static int zqr_keep_impl(double2* A, const int64_t* rowoff, int64_t m_path, int64_t m, int64_t k, int64_t cs,
+                         double2* R, void* work, cudaStream_t s) {
+  if (m_path <= QR_SMALL_M) return zqr_keep_small(A, rowoff, m, k, cs, R, work, s);
   QRWork q = carve(work, m, k);
   const int64_t p = m < k ? m : k;
   // factorisation

@@ -665,6 +665,9 @@ class DeviceNetwork:
         self.qr_graphs: dict = {}
         self.qr_seen: set = set()
         self.cholqr_fails: set = set()
+        self.cholqr_count = 0          # splits done by CholeskyQR2
+        self.householder_count = 0     # splits done by Householder QR
+        self.qr_rows_skipped = 0       # zero trailing rows the Householder QRs skipped
         self.graph_launches = 0
         lib = _lib.load()
         kmax, wmax = 1, 1
@@ -730,10 +733,11 @@ class DeviceNetwork:
         T = cb.contract(T, Wop, [f"b{k}" for k in ks[:half]] + ["s"])
         return T, ks[half:], nb
 
-    def heff_plan(self, nid) -> Plan:
+    def heff_plan(self, nid, fp64: bool = False) -> Plan:
         """y = H_eff x (``contract_ket_ham_with_envs``,
-        ``contractions/state_operator_contraction.py:227-273``)."""
-        key = ("heff", nid)
+        ``contractions/state_operator_contraction.py:227-273``); ``fp64`` forces
+        the complex128 chain on the reduced-precision path."""
+        key = ("heff", nid) if not fp64 else ("heff", nid, "fp64")
         if key in self.plans:
             return self.plans[key]
         cb = ChainBuilder(self.ws)
@@ -750,7 +754,7 @@ class DeviceNetwork:
                 T = cb.contract(T, E, [f"a{k}", f"b{k}"])
         if not rest:
             raise RuntimeError("site without neighbours")
-        p = self._finish(cb)
+        p = cb.plan() if fp64 else self._finish(cb)
         self.plans[key] = p
         return p
 
@@ -850,59 +854,90 @@ class DeviceNetwork:
         return self.local_exp(r, apply, dt, exp_factor, tol, maxdim, hermitian, out=r)
 
     # -- QR split and R absorption ---------------------------------------------------
-    CHOLQR_MIN_ROWS = 8192
+    # Reduced-precision path: tall splits (m >= 2k, k <= ptn_zchol_max_k) try
+    # CholeskyQR2 first; the pivot test on the device decides, and a split that
+    # is not of full numerical rank takes the Householder path.
+    CHOLQR_MIN_ROWS = 64
+    # Splits with at least this many entries are scanned for exactly-zero
+    # trailing rows, which the Householder QR then skips (ptn_zqr_keep_rows).
+    QR_SCAN_MIN = 1 << 15
+    CHOLQR_PIVOT_RATIO = 1e-3
+    # second pass: first-order factor when ||Q1^H Q1 - I||_F is at most this
+    CHOLQR_SERIES_TOL = 3e-4
 
-    def _cholqr2(self, nid, row_axes, col_axis) -> torch.Tensor | None:
-        """Mixed path, tall full-rank matrices: CholeskyQR2 with the Gram matrices
-        and the triangular solves on the tensor cores (BF16x6, FP32-level) and the
-        k x k Cholesky factorisations on the host. Returns R, or None when the
-        matrix is too ill-conditioned (then the caller falls back to Householder).
-        Q differs from the Householder Q only by a diagonal phase, which the
-        one-site TDVP absorbs as a gauge transformation."""
+    def _qr_words(self):
+        """Device words written by the split probe ([0] rows in use, [1] the
+        Cholesky status as int32) and their pinned host copy."""
+        w = self.ws.bufs.get("qr_words")
+        if w is None:
+            w = torch.zeros(2, dtype=torch.int64, device=self.device)
+            self.ws.bufs["qr_words"] = w
+            self._qr_words_host = torch.zeros(2, dtype=torch.int64, pin_memory=self.device.type == "cuda")
+        return w, self._qr_words_host
+
+    def _cholqr_plans(self, nid, row_axes, col_axis):
+        """Tensor-core plans of CholeskyQR2 for one split: the Gram matrix of the
+        site matrix A, A times a k x k matrix B (into the ``cholqr_out`` slot),
+        and the Gram matrix of that product. ``bufs``: k x k complex128 slots
+        [G, B, R1, R2, R2^-1, X, R0]."""
         shape = self.shape(nid)
         n = len(shape) - 1
         labels = [f"a{i}" for i in range(n)] + ["s"]
         rows = [labels[a] for a in row_axes]
         col = labels[col_axis]
         k = shape[col_axis]
-        key = ("cholqr", nid, tuple(row_axes), col_axis)
+        key = ("cholqr", nid, tuple(shape), tuple(row_axes), col_axis)
         if key not in self.plans:
-            Gt = torch.zeros((k, k), dtype=CDT, device=self.device)
-            Rinv = torch.zeros((k, k), dtype=CDT, device=self.device)
+            bufs = torch.zeros((7, k, k), dtype=CDT, device=self.device)
+            lp = [l if l != col else "p" for l in labels]
+            lq = [l if l != col else "q" for l in labels]
+            G = Operand.contiguous(("fixed", bufs[0]), ["p", "q"], [k, k])
             cb = ChainBuilder(self.ws)
-            A1 = Operand.contiguous(("fixed", self.t[nid]), [l if l != col else "p" for l in labels], shape)
-            A2 = Operand.contiguous(("fixed", self.t[nid]), [l if l != col else "q" for l in labels], shape)
-            cb.contract(A1, A2, rows, out=Operand.contiguous(("fixed", Gt), ["p", "q"], [k, k]), conj_a=True)
-            gram = cb.mixed_plan(self.levels)
+            cb.contract(Operand.contiguous(("fixed", self.t[nid]), lp, shape),
+                        Operand.contiguous(("fixed", self.t[nid]), lq, shape), rows, out=G, conj_a=True)
+            gram_a = cb.mixed_plan(self.levels)
             cb = ChainBuilder(self.ws)
-            A = Operand.contiguous(("fixed", self.t[nid]), [l if l != col else "p" for l in labels], shape)
-            Ri = Operand.contiguous(("fixed", Rinv), ["p", "q"], [k, k])
-            out = Operand.contiguous(("ws", "cholqr_out"), [l if l != col else "q" for l in labels], shape)
-            cb.contract(A, Ri, ["p"], out=out)
-            apply = cb.mixed_plan(self.levels)
-            self.plans[key] = (gram, apply, Gt, Rinv)
-        gram, apply, Gt, Rinv = self.plans[key]
-        Rtot = None
-        for _ in range(2):
-            gram.run()
-            G = Gt.cpu().numpy()
-            G = 0.5 * (G + G.conj().T)
-            try:
-                Lc = np.linalg.cholesky(G)
-            except np.linalg.LinAlgError:
-                return None
-            d = np.abs(np.diag(Lc))
-            if d.min() <= 1e-3 * d.max():
-                return None
-            R = Lc.conj().T                         # G = R^H R, R upper triangular
-            Rinv.copy_(torch.from_numpy(np.ascontiguousarray(np.linalg.inv(R))).to(self.device))
-            self.ws.get("cholqr_out", self.t[nid].numel())
-            apply.run()
-            self.t[nid].view(-1).copy_(self.ws.bufs["cholqr_out"][:self.t[nid].numel()])
-            Rtot = R if Rtot is None else R @ Rtot
-            self.flops += gram.flops + apply.flops
+            cb.contract(Operand.contiguous(("fixed", self.t[nid]), lp, shape),
+                        Operand.contiguous(("fixed", bufs[1]), ["p", "q"], [k, k]), ["p"],
+                        out=Operand.contiguous(("ws", "cholqr_out"), lq, shape))
+            apply_a = cb.mixed_plan(self.levels)
+            cb = ChainBuilder(self.ws)
+            cb.contract(Operand.contiguous(("ws", "cholqr_out"), lp, shape),
+                        Operand.contiguous(("ws", "cholqr_out"), lq, shape), rows, out=G, conj_a=True)
+            gram_q = cb.mixed_plan(self.levels)
+            self.plans[key] = (gram_a, apply_a, gram_q, bufs)
+        return self.plans[key]
+
+    def _cholqr_finish(self, nid, gram_a, apply_a, gram_q, bufs, k) -> torch.Tensor:
+        """CholeskyQR2 once the first factor R1 (of G1 = A^H A) passed its test:
+        Q1 = A R1^-1, G2 = Q1^H Q1 = R2^H R2, X = R1^-1 R2^-1, Q = A X written
+        over the site tensor, and R = X^-1 from R2 R1 by one FP64 Newton step,
+        so that Q R = A to FP64 rounding plus the one tensor-core product A X
+        (the FP32 error of the Cholesky factors only moves Q's gauge and its
+        orthonormality). No host round trip."""
+        lib = _lib.load()
+        stream = _stream_ptr()
+        numel = self.t[nid].numel()
+        G, B, R1, R2, R2i, X, R0 = (bufs[i] for i in range(7))
+        self.ws.get("cholqr_out", numel)
+        apply_a.run()                                   # Q1 = A R1^-1 (B holds R1^-1)
+        gram_q.run()                                    # G = Q1^H Q1
+        # a failure here (not expected after the first pass) lands in the
+        # tensor-core status word, which the next status check reports
+        st = self.ws.bufs.get("tc_status")
+        work = self.ws.get("chol_work", (int(lib.ptn_zchol_work_bytes(k)) + 15) // 16)
+        check(lib.ptn_zchol_upper(G.data_ptr(), k, k, R2.data_ptr(), R2i.data_ptr(), 0.0, 1,
+                                  self.CHOLQR_SERIES_TOL, st.data_ptr(), work.data_ptr(), stream), "zchol_upper")
+        check(lib.ptn_ztri_mul_upper(B.data_ptr(), R2i.data_ptr(), X.data_ptr(), k, stream), "ztri_mul_upper")
+        check(lib.ptn_ztri_mul_upper(R2.data_ptr(), R1.data_ptr(), R0.data_ptr(), k, stream), "ztri_mul_upper")
+        B.copy_(X)
         Rd = self.qr_R[:k * k].view(k, k)
-        Rd.copy_(torch.from_numpy(np.ascontiguousarray(Rtot)).to(self.device))
+        check(lib.ptn_ztri_inv_newton(X.data_ptr(), R0.data_ptr(), Rd.data_ptr(), G.data_ptr(), k, stream),
+              "ztri_inv_newton")
+        apply_a.run()                                   # Q = A X
+        self.t[nid].view(-1).copy_(self.ws.bufs["cholqr_out"][:numel])
+        self.flops += 2 * gram_a.flops + 2 * apply_a.flops
+        self.cholqr_count += 1
         return Rd
 
     def qr_split(self, nid, nbr) -> torch.Tensor:
@@ -929,29 +964,61 @@ class DeviceNetwork:
         m = rowoff.numel()
         k = shape[col_axis]
         lib = _lib.load()
+        stream = _stream_ptr()
         # two-site splits change bond dimensions, and with them the row count of
         # every other split of the two nodes: size R and the work area for this one
         self._ensure_qr_buffers(m, k)
-        ckey = (nid, tuple(row_axes), col_axis)
-        if self.levels and m >= self.CHOLQR_MIN_ROWS and m >= 2 * k and ckey not in self.cholqr_fails:
-            backup = self.ws.get("cholqr_backup", self.t[nid].numel())
-            backup.copy_(self.t[nid].view(-1))
-            R = self._cholqr2(nid, row_axes, col_axis)
-            if R is not None:
-                if node.parent != nbr:
-                    node.children = [nbr] + [c for c in node.children if c != nbr]
-                return R
-            # rank-deficient (e.g. zero-padded bonds): keep LAPACK's Householder
-            # complement, which the one-site TDVP result depends on
-            self.cholqr_fails.add(ckey)
-            self.t[nid].view(-1).copy_(backup)
+        ckey = (nid, tuple(shape), tuple(row_axes), col_axis)
+        use_chol = bool(self.levels) and m >= self.CHOLQR_MIN_ROWS and m >= 2 * k and \
+            k <= int(lib.ptn_zchol_max_k()) and ckey not in self.cholqr_fails
+        scan = m * k >= self.QR_SCAN_MIN and self.device.type == "cuda"
+        m_used = m
+        if use_chol or scan:
+            # one probe, one synchronisation: the rows in use and, for a tall
+            # split, the first Cholesky factor of the Gram matrix with its pivot test
+            words, host = self._qr_words()
+            words.zero_()
+            A = self.t[nid]
+            if scan:
+                check(lib.ptn_znonzero_rows(A.data_ptr(), rowoff.data_ptr(), m, k, strides[col_axis],
+                                            words.data_ptr(), stream), "znonzero_rows")
+            if use_chol:
+                gram_a, apply_a, gram_q, bufs = self._cholqr_plans(nid, row_axes, col_axis)
+                gram_a.run()
+                if self.ws.bufs.get("tc_status") is None:
+                    self.ws.bufs["tc_status"] = torch.zeros(1, dtype=torch.int32, device=self.device)
+                work = self.ws.get("chol_work", (int(lib.ptn_zchol_work_bytes(k)) + 15) // 16)
+                check(lib.ptn_zchol_upper(bufs[0].data_ptr(), k, k, bufs[2].data_ptr(), bufs[1].data_ptr(),
+                                          self.CHOLQR_PIVOT_RATIO, 0, 0.0, words.data_ptr() + 8,
+                                          work.data_ptr(), stream), "zchol_upper")
+            host.copy_(words, non_blocking=True)
+            if self.device.type == "cuda":
+                torch.cuda.current_stream().synchronize()
+            if scan:
+                m_used = max(1, int(host[0]))
+            if use_chol:
+                if int(host[1]) == 0:
+                    R = self._cholqr_finish(nid, gram_a, apply_a, gram_q, bufs, k)
+                    if node.parent != nbr:
+                        node.children = [nbr] + [c for c in node.children if c != nbr]
+                    return R
+                # not of full numerical rank (e.g. zero-padded bonds): keep
+                # LAPACK's Householder complement, which one-site TDVP depends on
+                self.cholqr_fails.add(ckey)
         R = self.qr_R[:k * k].view(k, k)
         work = self.qr_work
+        if m_used < m:
+            self.qr_rows_skipped += m - m_used
 
         def launch():
-            check(lib.ptn_zqr_keep(self.t[nid].data_ptr(), rowoff.data_ptr(), m, k, strides[col_axis],
-                                   R.data_ptr(), work.data_ptr(), _stream_ptr()), "ptn_zqr_keep")
-        gkey = (nid, nbr, key)
+            if m_used < m:
+                check(lib.ptn_zqr_keep_rows(self.t[nid].data_ptr(), rowoff.data_ptr(), m, m_used, k,
+                                            strides[col_axis], R.data_ptr(), work.data_ptr(), _stream_ptr()),
+                      "ptn_zqr_keep_rows")
+            else:
+                check(lib.ptn_zqr_keep(self.t[nid].data_ptr(), rowoff.data_ptr(), m, k, strides[col_axis],
+                                       R.data_ptr(), work.data_ptr(), _stream_ptr()), "ptn_zqr_keep")
+        gkey = (nid, nbr, key, m_used)
         if not self.use_graphs or self.device.type != "cuda":
             launch()
         elif gkey in self.qr_graphs:
@@ -972,7 +1039,8 @@ class DeviceNetwork:
             launch()
         if node.parent != nbr:
             node.children = [nbr] + [c for c in node.children if c != nbr]
-        self.flops += 8 * 2 * m * k * k
+        self.flops += 8 * 2 * m_used * k * k
+        self.householder_count += 1
         return R
 
     def absorb(self, R: torch.Tensor, src, dst, link_variant: bool, precise: bool = False):
@@ -1453,6 +1521,26 @@ class DeviceNetwork:
         st.orthogonality_center_id = center
 
     # -- observables ------------------------------------------------------------------
+    def center_energy(self) -> float:
+        """<psi|H|psi> / <psi|psi> from the orthogonality centre and the cached
+        environments pointing to it (valid whenever those are current, as after
+        every one-site TDVP time step): one complex128 H_eff application and
+        two dot products, instead of a contraction of the whole network."""
+        c = self.state.orthogonality_center_id
+        x = self.t[c]
+        y = self.ws.get("energy_y", x.numel())
+        self.heff_plan(c, fp64=True).run(x.data_ptr(), y.data_ptr())
+        lib = _lib.load()
+        n = x.numel()
+        part = self.ws.get("kry_part", int(lib.ptn_krylov_partials(n)) * 2 + 8)
+        h = self.ws.get("energy_h", 2)
+        check(lib.ptn_zdot_multi(x.data_ptr(), n, 1, y.data_ptr(), n, h[0:].data_ptr(), 0, part.data_ptr(),
+                                 _stream_ptr()), "zdot_multi")
+        check(lib.ptn_zdot_multi(x.data_ptr(), n, 1, x.data_ptr(), n, h[1:].data_ptr(), 0, part.data_ptr(),
+                                 _stream_ptr()), "zdot_multi")
+        v = h.cpu().numpy()
+        return float(v[0].real / v[1].real)
+
     def overlap(self, other: "DeviceNetwork") -> complex:
         """<self|other> for two states on the same tree, bond dimensions free to
         differ (``contract_two_ttns``, ``contractions/state_state_contraction.py:29-66``).

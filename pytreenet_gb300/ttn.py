@@ -163,9 +163,21 @@ class TreeTensorNetwork:
         return np.transpose(t, self.logical_perm(nid))
 
     def set_tensor(self, nid, value):
-        """Set a tensor given in the node's logical leg order."""
+        """Set a tensor given in the node's logical leg order. A node whose
+        tensor lives on the device (the state of a running driver) is
+        overwritten in place when the shape matches, so the engine's buffers
+        keep their addresses (the drivers mutate their state in place, as in
+        the reference)."""
         self._finalise()
-        inv = np.argsort(self.logical_perm(nid))
+        inv = [int(i) for i in np.argsort(self.logical_perm(nid))]
+        cur = self._phys.get(nid)
+        if cur is not None and not isinstance(cur, np.ndarray) and getattr(cur, "is_cuda", False):
+            import torch
+            src = value.permute(*inv) if isinstance(value, torch.Tensor) else \
+                torch.from_numpy(np.ascontiguousarray(np.transpose(np.asarray(value), inv)))
+            if tuple(src.shape) == tuple(cur.shape):
+                cur.copy_(src)
+                return
         self._phys[nid] = np.ascontiguousarray(np.transpose(np.asarray(value), inv))
 
     def __getitem__(self, nid):
@@ -520,7 +532,12 @@ class TreeTensorNetworkState(TreeTensorNetwork):
             raise ValueError("Precision must be either 64 or 128!")
         dtype = np.complex128 if precision == 128 else np.complex64
         for nid, t in list(self._phys.items()):
-            self._phys[nid] = np.asarray(t.detach().cpu().numpy() if hasattr(t, "detach") else t).astype(dtype)
+            if hasattr(t, "detach"):
+                import torch
+                # device tensors stay where they are; only the dtype changes
+                self._phys[nid] = t.to(torch.complex128 if precision == 128 else torch.complex64)
+            else:
+                self._phys[nid] = np.asarray(t).astype(dtype)
         return self
 
     def to_dense(self, site_order=None) -> np.ndarray:
@@ -639,7 +656,13 @@ class TreeTensorNetworkState(TreeTensorNetwork):
         self._orthogonalise(orthogonality_center_id, mode, full=False)
 
     def orthogonalize(self, orthogonality_center_id: str, mode=None):
-        """Canonical form from scratch, whatever the current centre."""
+        """``TreeTensorNetwork.orthogonalize`` (``core/ttn.py:1699-1715``): a
+        wrapper of ``canonical_form`` (moves an existing centre, else brings the
+        whole network into canonical form)."""
+        self.canonical_form(orthogonality_center_id, mode=mode)
+
+    def orthogonalize_from_scratch(self, orthogonality_center_id: str, mode=None):
+        """Canonical form by QR splits of every node, whatever the current centre."""
         self._orthogonalise(orthogonality_center_id, mode, full=True)
 
     def orthogonalize_root(self, mode=None):

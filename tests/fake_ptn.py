@@ -319,3 +319,83 @@ def _fake_gs_step(self, Q, ldq, nq, w, n, h, part, norms, qnext, stream):
 
 FakeLib.ptn_exec_ops = _fake_exec_ops
 FakeLib.ptn_krylov_gs_step = _fake_gs_step
+
+
+# ---- CholeskyQR2 factors and the zero-row scan --------------------------------------
+def _fake_chol_upper(self, G, ldg, k, R, Rinv, ratio, series, series_tol, status, work, stream):
+    g = _view(G, (k - 1) * ldg + k).copy()
+    g = np.stack([g[i * ldg:i * ldg + k] for i in range(k)])
+    g = 0.5 * (g + g.conj().T)
+    if series and np.linalg.norm(g - np.eye(k)) <= series_tol:
+        e = g - np.eye(k)
+        u = np.triu(e, 1) + 0.5 * np.diag(np.diag(e).real)
+        _view(R, k * k)[:] = (np.eye(k) + u).reshape(-1)
+        _view(Rinv, k * k)[:] = (np.eye(k) - u).reshape(-1)
+        return 0
+    try:
+        lc = np.linalg.cholesky(g)
+    except np.linalg.LinAlgError:
+        _view(status, 1, np.int32)[0] = 5
+        return 0
+    d = np.abs(np.diag(lc))
+    if not d.min() > ratio * d.max():
+        _view(status, 1, np.int32)[0] = 5
+        return 0
+    r = lc.conj().T
+    _view(R, k * k)[:] = r.reshape(-1)
+    _view(Rinv, k * k)[:] = np.triu(np.linalg.inv(r)).reshape(-1)
+    return 0
+
+
+def _fake_tri_mul(self, A, B, C, k, stream):
+    a = _view(A, k * k).reshape(k, k)
+    b = _view(B, k * k).reshape(k, k)
+    _view(C, k * k)[:] = np.triu(np.triu(a) @ np.triu(b)).reshape(-1)
+    return 0
+
+
+def _fake_nonzero_rows(self, A, rowoff, m, k, cs, out, stream):
+    ro = _view(rowoff, m, np.int64)
+    ext = int(ro.max()) + (k - 1) * cs + 1
+    mat = _view(A, ext)[ro[:, None] + np.arange(k)[None, :] * cs]
+    nz = np.nonzero(np.any(mat != 0, axis=1))[0]
+    _view(out, 1, np.int64)[0] = int(nz[-1]) + 1 if nz.size else 0
+    return 0
+
+
+def _fake_qr_keep_rows(self, A, rowoff, m, m_used, k, cs, R, work, stream):
+    ro = _view(rowoff, m, np.int64)
+    ext = int(ro.max()) + (k - 1) * cs + 1
+    a = _view(A, ext)
+    idx = ro[:, None] + np.arange(k)[None, :] * cs
+    mat = a[idx]
+    assert not np.any(mat[m_used:]), "rows past m_used must be zero"
+    p = min(m, k)
+    q = np.zeros((m, k), dtype=complex)
+    r = np.zeros((k, k), dtype=complex)
+    qs, rs = np.linalg.qr(mat[:m_used], mode="reduced")
+    q[:m_used, :qs.shape[1]] = qs
+    r[:rs.shape[0], :] = rs
+    for j in range(min(m_used, k), p):
+        q[j, j] = 1.0
+    a[idx] = q
+    _view(R, k * k)[:] = r.reshape(-1)
+    return 0
+
+
+FakeLib.ptn_zchol_work_bytes = lambda self, k: 16
+FakeLib.ptn_zchol_max_k = lambda self: 256
+FakeLib.ptn_zchol_upper = _fake_chol_upper
+FakeLib.ptn_ztri_mul_upper = _fake_tri_mul
+
+
+def _fake_tri_inv_newton(self, X, R0, R, work, k, stream):
+    x = np.triu(_view(X, k * k).reshape(k, k))
+    r0 = np.triu(_view(R0, k * k).reshape(k, k))
+    _view(R, k * k)[:] = np.triu(r0 @ (2 * np.eye(k) - x @ r0)).reshape(-1)
+    return 0
+
+
+FakeLib.ptn_ztri_inv_newton = _fake_tri_inv_newton
+FakeLib.ptn_znonzero_rows = _fake_nonzero_rows
+FakeLib.ptn_zqr_keep_rows = _fake_qr_keep_rows

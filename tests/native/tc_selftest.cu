@@ -4,8 +4,13 @@
 // layout. One CTA computes D = A * B^T for a 128 x 64 A and a 128 x 64 B
 // (bf16, K contiguous) with four K=16 MMAs and writes the 128 x 128 FP32
 // accumulator. Every wait is bounded; a timeout sets *status = 1.
+//
+// Test-only: built into its own library by tests/test_gpu_mixed.py, not part
+// of libptn_gb300.
 #include "ptn_common.cuh"
 #include "tc_ptx.cuh"
+
+std::atomic<unsigned long long> g_ptn_launches{0};
 
 namespace {
 
@@ -71,7 +76,7 @@ __global__ void __launch_bounds__(128) tc_selftest_kernel(const uint16_t* __rest
 
 }  // namespace
 
-extern "C" int ptn_tc_selftest(const void* A, const void* B, void* D, int32_t* status, int32_t sw64,
+extern "C" int tc_selftest(const void* A, const void* B, void* D, int32_t* status, int32_t sw64,
                                void* stream) {
   if (!A || !B || !D || !status) return PTN_ERR_ARG;
   PTN_COUNT(1);

@@ -22,16 +22,37 @@ def _bf16_round(x):
     return torch.from_numpy(np.ascontiguousarray(x, dtype=np.float32)).to(torch.bfloat16)
 
 
+@pytest.fixture(scope="module")
+def selftest_lib(lib):
+    """The descriptor self-test kernel, built into a test-only library."""
+    import ctypes
+    import os
+    import subprocess
+    from pytreenet_gb300 import build
+    here = os.path.dirname(os.path.abspath(__file__))
+    out_dir = os.path.join(here, "native", "_build")
+    os.makedirs(out_dir, exist_ok=True)
+    so = os.path.join(out_dir, "libtc_selftest.so")
+    cmd = [build.nvcc(), *build.ARCH, *build.NVCC_FLAGS, "-shared", "-I", build.CSRC,
+           os.path.join(here, "native", "tc_selftest.cu"), "-o", so]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    t = ctypes.CDLL(so)
+    t.tc_selftest.restype = ctypes.c_int
+    t.tc_selftest.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_int32, ctypes.c_void_p]
+    return t
+
+
 @pytest.mark.parametrize("sw64", [0, 1])
-def test_tcgen05_descriptor_selftest(lib, sw64):
+def test_tcgen05_descriptor_selftest(selftest_lib, sw64):
     from pytreenet_gb300.engine import _stream_ptr
     A = _bf16_round(RNG.normal(size=(128, 64)))
     B = _bf16_round(RNG.normal(size=(128, 64)))
     D = torch.zeros((128, 128), dtype=torch.float32, device="cuda")
     st = torch.zeros(1, dtype=torch.int32, device="cuda")
     Ad, Bd = A.cuda(), B.cuda()
-    assert lib.ptn_tc_selftest(Ad.data_ptr(), Bd.data_ptr(), D.data_ptr(), st.data_ptr(), sw64,
-                               _stream_ptr()) == 0
+    assert selftest_lib.tc_selftest(Ad.data_ptr(), Bd.data_ptr(), D.data_ptr(), st.data_ptr(), sw64,
+                                    _stream_ptr()) == 0
     torch.cuda.synchronize()
     assert int(st.item()) == 0
     ref = A.float().numpy() @ B.float().numpy().T
@@ -145,3 +166,42 @@ def test_gpu_qr_graph_replay_matches_eager():
     for (r0, q0), (r1, q1) in zip(outs[0], outs[1]):
         assert torch.equal(r0, r1) and torch.equal(q0, q1)
     assert net.qr_graphs, "the multi-kernel split was not captured"
+
+
+def test_cgemm_abort_mid_kernel_drains_and_recovers(lib):
+    """A nonzero status word written from another stream while tensor-core
+    GEMMs run makes them stop early: the running CTAs leave their waits, drain
+    the loads and MMAs they issued, free TMEM and exit; later launches see the
+    word and skip. The status stays nonzero, and once it is cleared the same
+    GEMM runs again and reproduces its earlier output exactly."""
+    from pytreenet_gb300.engine import Operand, ChainBuilder, Workspace
+    M, N, K = 65536, 512, 2048
+    g = torch.Generator(device="cuda").manual_seed(5)
+    Ad = torch.randn((M, K), dtype=torch.complex128, device="cuda", generator=g)
+    Bd = torch.randn((N, K), dtype=torch.complex128, device="cuda", generator=g)
+    C = torch.zeros((M, N), dtype=torch.complex128, device="cuda")
+    ws = Workspace("cuda")
+    cb = ChainBuilder(ws)
+    cb.contract(Operand.contiguous(("fixed", Ad), ["m", "k"], [M, K]),
+                Operand.contiguous(("fixed", Bd), ["n", "k"], [N, K]), ["k"],
+                out=Operand.contiguous(("fixed", C), ["m", "n"], [M, N]))
+    p = cb.mixed_plan(3)
+    p.run()
+    torch.cuda.synchronize()
+    status = ws.bufs["tc_status"]
+    assert int(status.item()) == 0
+    C_ok = C.clone()
+    side = torch.cuda.Stream()
+    for _ in range(8):
+        p.run()
+    with torch.cuda.stream(side):
+        torch.cuda._sleep(2_000_000)          # ~1 ms, while the GEMMs above run
+        status.fill_(99)
+    torch.cuda.synchronize()
+    assert int(status.item()) != 0
+    status.zero_()
+    C.zero_()
+    p.run()
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    assert torch.equal(C, C_ok)

@@ -861,7 +861,11 @@ class DeviceNetwork:
     # Splits with at least this many entries are scanned for exactly-zero
     # trailing rows, which the Householder QR then skips (ptn_zqr_keep_rows).
     QR_SCAN_MIN = 1 << 15
-    CHOLQR_PIVOT_RATIO = 1e-3
+    # CholeskyQR2 writes Q = A X with one tensor-core product, whose FP32
+    # rounding (relative to |A||X|) puts ~6e-8 kappa(A) into Q R - A; splits
+    # whose first Cholesky factor has a diagonal ratio below this (kappa above
+    # ~10) take the backward-stable Householder path instead
+    CHOLQR_PIVOT_RATIO = 0.1
     # second pass: first-order factor when ||Q1^H Q1 - I||_F is at most this
     CHOLQR_SERIES_TOL = 3e-4
 

@@ -221,7 +221,9 @@ def _fake_cgemm(self, d_ref, stream):
     def blk(i):
         return _bf16_val(b[i * N * d.ldb:(i + 1) * N * d.ldb].reshape(N, d.ldb)[:, :K])
     B = sum(blk(3 * lv + 1) + 1j * blk(3 * lv + 2) for lv in range(L))
-    C = A @ B.T
+    # FP32 accumulation, as the tensor cores: the rounding error scales with
+    # sum |a||b|, not with |C|
+    C = (A.astype(np.complex64) @ B.T.astype(np.complex64)).astype(np.complex128)
     md, ms = _modes(d.m_out, "stride_c")
     nd, ns = _modes(d.n_out, "stride_c")
     off = _offsets(md, ms)[:, None] + _offsets(nd, ns)[None, :]

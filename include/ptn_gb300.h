@@ -192,9 +192,19 @@ typedef struct {
   int64_t c_plane;
   ptn_modes m_out, n_out;
   int32_t* status;
+  void* partial;            /* split-K scratch (8-byte aligned), or null   */
+  int64_t partial_bytes;
 } ptn_cgemm_desc;
 int ptn_cgemm_bf16x3(const ptn_cgemm_desc* d, void* stream);
 int ptn_cgemm_smem_bytes(int32_t levels);
+
+/* Scratch that ptn_cgemm_bf16x3 uses to split the K range of an M x N x K
+ * product whose output has too few 128 x 64 tiles to fill the GPU (0 when it
+ * does not split). With at least this many bytes at d->partial, the K range
+ * is cut into pieces whose FP32 partial sums a second kernel adds in FP64, in
+ * a fixed order, before writing the output; with less (or null) the product
+ * runs unsplit. No counterpart in the reference. */
+int64_t ptn_cgemm_partial_bytes(int64_t M, int64_t N, int64_t K);
 
 /* Gather a complex128 tensor into the split BF16 operand layouts above.
  * rows / cols: source mode groups (dims + stride_a); element (r, c) of the
@@ -221,7 +231,10 @@ int ptn_expand_b(const ptn_convert_desc* d, void* stream);
  * ptn_zqr_work_bytes(m, k) exceeds it are rejected with PTN_ERR_UNSUPPORTED
  * before anything is launched. The first call on each device looks up the
  * array's device address (with that device current), so make one call on a
- * device before capturing a stream that uses it. All calls share the one
+ * device before capturing a stream that uses it. The address is cached for the
+ * life of the process: after cudaDeviceReset (or anything else that destroys
+ * the device's primary context) it is stale, so do not call this entry point
+ * on that device again in the same process. All calls share the one
  * array: calls that can overlap on the GPU (different streams, or different
  * host threads) race on it, so serialise them. Nothing in the scratch needs
  * to start at zero; each call writes every entry it later reads. */
@@ -292,6 +305,8 @@ enum { PTN_OP_ZCONTRACT = 0, PTN_OP_CGEMM = 1, PTN_OP_TO_PLANES = 2, PTN_OP_EXPA
 typedef struct {
   int32_t kind;
   int32_t a, b, c;
+  int32_t d;                /* PTN_OP_CGEMM: table index of the split-K scratch, or -1 */
+  int32_t pad_;
   const void* desc;
 } ptn_exec_op;
 int ptn_exec_ops(const ptn_exec_op* ops, int32_t nops, void* const* ptrs, int32_t nptrs, void* stream);

@@ -971,6 +971,11 @@ def two_site_merge(state: OState, u: str, v: str):
     return T.out([f"u:{x}" for x in nu] + ["su"] + [f"v:{x}" for x in nv] + ["sv"]), nu, nv
 
 
+# Largest intermediate (elements) for which the two-site H_eff follows the
+# reference's contraction order.
+TWO_SITE_REFERENCE_ORDER_MAX = 10 ** 8
+
+
 def two_site_heff_apply(x, nu, nv, u, v, Wu, Wv, tree: OTree, envs):
     """H_eff of the merged pair applied to ``x`` (legs as ``two_site_merge``)
     (``effective_two_site_evolution``, ``time_evo_util/effective_time_evolution.py:326-410``:
@@ -978,14 +983,36 @@ def two_site_heff_apply(x, nu, nv, u, v, Wu, Wv, tree: OTree, envs):
     contraction of ``contract_ket_ham_with_envs``)."""
     lab_x = [f"au{k}" for k in range(len(nu))] + ["su"] + [f"av{k}" for k in range(len(nv))] + ["sv"]
     T = _L(x, lab_x)
-    for k, nb in enumerate(nu):
-        T = T.dot(_L(envs[(nb, u)], [f"au{k}", f"bu{k}", f"cu{k}"]), [f"au{k}"])
-    wl_u = [f"bu{nu.index(x)}" if x != v else "bw" for x in tree.neighbours(u)] + ["tu", "su"]
-    T = T.dot(_L(Wu, wl_u), [f"bu{k}" for k in range(len(nu))] + ["su"])
-    for k, nb in enumerate(nv):
-        T = T.dot(_L(envs[(nb, v)], [f"av{k}", f"bv{k}", f"cv{k}"]), [f"av{k}"])
-    wl_v = [f"bv{nv.index(x)}" if x != u else "bw" for x in tree.neighbours(v)] + ["tv", "sv"]
-    T = T.dot(_L(Wv, wl_v), [f"bv{k}" for k in range(len(nv))] + ["bw", "sv"])
+    wl_u = [f"bu{nu.index(y)}" if y != v else "bw" for y in tree.neighbours(u)] + ["tu", "su"]
+    wl_v = [f"bv{nv.index(y)}" if y != u else "bw" for y in tree.neighbours(v)] + ["tv", "sv"]
+    wu = [envs[(nb, u)].shape[1] for nb in nu]
+    wv = [envs[(nb, v)].shape[1] for nb in nv]
+    w_bw = Wu.shape[tree.neighbours(u).index(v)]
+    peak = x.size * max(int(np.prod(wu)), w_bw * int(np.prod(wv)))
+    if peak <= TWO_SITE_REFERENCE_ORDER_MAX:
+        # the reference's order: every environment of a side, then its TTNO tensor
+        for k, nb in enumerate(nu):
+            T = T.dot(_L(envs[(nb, u)], [f"au{k}", f"bu{k}", f"cu{k}"]), [f"au{k}"])
+        T = T.dot(_L(Wu, wl_u), [f"bu{k}" for k in range(len(nu))] + ["su"])
+        for k, nb in enumerate(nv):
+            T = T.dot(_L(envs[(nb, v)], [f"av{k}", f"bv{k}", f"cv{k}"]), [f"av{k}"])
+        T = T.dot(_L(Wv, wl_v), [f"bv{k}" for k in range(len(nv))] + ["bw", "sv"])
+    else:
+        # too large for that order (the TTNO bond legs of a whole side pile
+        # up): each side in the single-site order instead (half of its
+        # environments, its TTNO tensor, the rest) -- the same sum
+        hu = len(nu) // 2
+        for k in range(hu):
+            T = T.dot(_L(envs[(nu[k], u)], [f"au{k}", f"bu{k}", f"cu{k}"]), [f"au{k}"])
+        T = T.dot(_L(Wu, wl_u), [f"bu{k}" for k in range(hu)] + ["su"])
+        for k in range(hu, len(nu)):
+            T = T.dot(_L(envs[(nu[k], u)], [f"au{k}", f"bu{k}", f"cu{k}"]), [f"au{k}", f"bu{k}"])
+        hv = len(nv) // 2
+        for k in range(hv):
+            T = T.dot(_L(envs[(nv[k], v)], [f"av{k}", f"bv{k}", f"cv{k}"]), [f"av{k}"])
+        T = T.dot(_L(Wv, wl_v), [f"bv{k}" for k in range(hv)] + ["bw", "sv"])
+        for k in range(hv, len(nv)):
+            T = T.dot(_L(envs[(nv[k], v)], [f"av{k}", f"bv{k}", f"cv{k}"]), [f"av{k}", f"bv{k}"])
     return T.out([f"cu{k}" for k in range(len(nu))] + ["tu"] + [f"cv{k}" for k in range(len(nv))] + ["tv"])
 
 

@@ -57,7 +57,8 @@ class CgemmDesc(ctypes.Structure):
                 ("M", ctypes.c_int64), ("K", ctypes.c_int64), ("Bx", ctypes.c_void_p),
                 ("ldb", ctypes.c_int64), ("N", ctypes.c_int64), ("out_kind", ctypes.c_int32),
                 ("levels", ctypes.c_int32), ("C", ctypes.c_void_p), ("c_plane", ctypes.c_int64),
-                ("m_out", Modes), ("n_out", Modes), ("status", ctypes.c_void_p)]
+                ("m_out", Modes), ("n_out", Modes), ("status", ctypes.c_void_p),
+                ("partial", ctypes.c_void_p), ("partial_bytes", ctypes.c_int64)]
 
 
 class ConvertDesc(ctypes.Structure):
@@ -83,7 +84,8 @@ class PermuteDesc(ctypes.Structure):
 
 class ExecOp(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int32), ("a", ctypes.c_int32), ("b", ctypes.c_int32),
-                ("c", ctypes.c_int32), ("desc", ctypes.c_void_p)]
+                ("c", ctypes.c_int32), ("d", ctypes.c_int32), ("pad_", ctypes.c_int32),
+                ("desc", ctypes.c_void_p)]
 
 
 OP_ZCONTRACT, OP_CGEMM, OP_TO_PLANES, OP_EXPAND_B = 0, 1, 2, 3
@@ -117,6 +119,7 @@ SIGNATURES = {
     "ptn_ztri_inv_newton": (ctypes.c_int, [_P, _P, _P, _P, _I64, _P]),
     "ptn_cgemm_bf16x3": (ctypes.c_int, [ctypes.POINTER(CgemmDesc), _P]),
     "ptn_cgemm_smem_bytes": (ctypes.c_int, [_I32]),
+    "ptn_cgemm_partial_bytes": (_I64, [_I64, _I64, _I64]),
     "ptn_to_planes": (ctypes.c_int, [ctypes.POINTER(ConvertDesc), _P]),
     "ptn_expand_b": (ctypes.c_int, [ctypes.POINTER(ConvertDesc), _P]),
     "ptn_zsvd_work_bytes": (_I64, [_I64, _I64]),

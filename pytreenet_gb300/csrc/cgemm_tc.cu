@@ -61,7 +61,17 @@ struct GemmArgs {
   OutModes mo, no;
   int32_t* status;
   int64_t tiles_n;
+  int64_t tiles;             // output tiles (tiles_m * tiles_n)
+  int32_t splits;            // K ranges per tile (1: no split)
+  int32_t ksplit;            // K tiles per range
+  float2* partial;           // [splits][M][N] FP32 partial sums when splits > 1
 };
+
+// Split-K: outputs with fewer tiles than this many CTAs get their K range
+// split so the launch fills the GPU (one CTA per SM, 152 SMs, two waves);
+// each range keeps at least SPLIT_MIN_KT K tiles.
+constexpr int64_t SPLIT_TARGET_CTAS = 304;
+constexpr int64_t SPLIT_MIN_KT = 4;
 
 __device__ __forceinline__ int64_t decode_off(const OutModes& md, int64_t idx) {
   int64_t o = 0;
@@ -94,10 +104,13 @@ __global__ void __launch_bounds__(THREADS, 1)
   if (s_abort != 0) return;  // an earlier CTA failed: skip the work
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t tile = blockIdx.x;
+  const int64_t tile = blockIdx.x % g.tiles;
+  const int split = (int)(blockIdx.x / g.tiles);
   const int64_t tm = tile / g.tiles_n, tn = tile - tm * g.tiles_n;
   const int64_t m0 = tm * MT, n0 = tn * NT;
-  const int ktiles = (int)((g.K + KT - 1) / KT);
+  const int kt_all = (int)((g.K + KT - 1) / KT);
+  const int kt0 = split * g.ksplit;
+  const int ktiles = min(kt_all, kt0 + g.ksplit) - kt0;    // K tiles of this CTA's range
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -142,7 +155,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
         uint8_t* st = smem + s * STAGE_BYTES;
         tc::mbar_arrive_expect_tx(&full_bar[s], STAGE_BYTES);
-        const int kx = kt * KT;
+        const int kx = (kt0 + kt) * KT;
         for (int p = 0; p < 2 * L; ++p)
           tc::tma_load_3d(st + p * A_PLANE_BYTES, &tmA, &full_bar[s], kx, (int)m0, p);
         for (int b = 0; b < 3 * L; ++b)
@@ -253,6 +266,12 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
     if (!ok) {
       if (lane == 0) atomicExch(g.status, PTN_ERR_TIMEOUT);
+    } else if (m < g.M && g.splits > 1) {
+      // this K range's FP32 partial sums; splitk_reduce_kernel adds the ranges
+      float2* P = g.partial + ((int64_t)split * g.M + m) * g.N + n0;
+#pragma unroll
+      for (int i = 0; i < NT; ++i)
+        if (n0 + i < g.N) P[i] = make_float2(acc_re[i], acc_im[i]);
     } else if (m < g.M) {
       const int64_t moff = decode_off(g.mo, m);
       if (g.out_kind == 0) {
@@ -372,6 +391,59 @@ __global__ void expand_b_kernel(const double2* __restrict__ src, OutModes nm, Ou
   }
 }
 
+// Sum of the split-K partial sums (FP64, ranges in order: deterministic),
+// written like the GEMM epilogue: complex128 through the output modes, or as
+// BF16 level planes.
+__global__ void splitk_reduce_kernel(const float2* __restrict__ partial, int splits, int64_t M, int64_t N,
+                                     OutModes mo, OutModes no, int out_kind, void* C, int64_t c_plane, int L,
+                                     const int32_t* __restrict__ status) {
+  if (*status != 0) return;
+  const int64_t total = M * N;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t m = e / N, n = e - (e / N) * N;
+    double re = 0.0, im = 0.0;
+    for (int s = 0; s < splits; ++s) {
+      const float2 p = partial[((int64_t)s * M + m) * N + n];
+      re += (double)p.x;
+      im += (double)p.y;
+    }
+    const int64_t o = decode_off(mo, m) + decode_off(no, n);
+    if (out_kind == 0) {
+      static_cast<double2*>(C)[o] = make_double2(re, im);
+    } else {
+      __nv_bfloat16* Cb = static_cast<__nv_bfloat16*>(C);
+      for (int lv = 0; lv < L; ++lv) {
+        const __nv_bfloat16 rb = __double2bfloat16(re);
+        const __nv_bfloat16 ib = __double2bfloat16(im);
+        Cb[(2 * lv) * c_plane + o] = rb;
+        Cb[(2 * lv + 1) * c_plane + o] = ib;
+        re -= (double)__bfloat162float(rb);
+        im -= (double)__bfloat162float(ib);
+      }
+    }
+  }
+}
+
+// Split of the K range for an M x N x K product: (splits, K tiles per split).
+void split_plan(int64_t M, int64_t N, int64_t K, int64_t& splits, int64_t& ksplit) {
+  const int64_t tiles = ((M + MT - 1) / MT) * ((N + NT - 1) / NT);
+  const int64_t kt_all = (K + KT - 1) / KT;
+  splits = 1;
+  ksplit = kt_all;
+  if (tiles >= SPLIT_TARGET_CTAS / 2) return;
+  int64_t s = (SPLIT_TARGET_CTAS + tiles - 1) / tiles;
+  const int64_t smax = kt_all / SPLIT_MIN_KT;
+  if (s > smax) s = smax;
+  if (s < 2) return;
+  ksplit = (kt_all + s - 1) / s;
+  splits = (kt_all + ksplit - 1) / ksplit;
+  if (splits < 2) {
+    splits = 1;
+    ksplit = kt_all;
+  }
+}
+
 int fill_out(const ptn_modes& src, OutModes& dst) {
   if (src.n < 0 || src.n > PTN_MAX_MODES) return PTN_ERR_ARG;
   dst.n = src.n;
@@ -407,6 +479,13 @@ unsigned grid_for(int64_t n) {
 
 extern "C" int ptn_cgemm_smem_bytes(int32_t levels) { return levels == 3 ? Cfg<3>::SMEM : Cfg<2>::SMEM; }
 
+extern "C" int64_t ptn_cgemm_partial_bytes(int64_t M, int64_t N, int64_t K) {
+  if (M < 1 || N < 1 || K < 1) return 0;
+  int64_t splits, ksplit;
+  split_plan(M, N, K, splits, ksplit);
+  return splits > 1 ? splits * M * N * (int64_t)sizeof(float2) : 0;
+}
+
 template <int L>
 int launch_gemm(const CUtensorMap& ta, const CUtensorMap& tb, const GemmArgs& g, unsigned grid, cudaStream_t st) {
   // once per process, thread-safe; a failure is returned on every call
@@ -415,6 +494,11 @@ int launch_gemm(const CUtensorMap& ta, const CUtensorMap& tb, const GemmArgs& g,
   if (attr != cudaSuccess) return PTN_ERR_LAUNCH;
   PTN_COUNT(1);
   cgemm_bf16_kernel<L><<<grid, THREADS, Cfg<L>::SMEM, st>>>(ta, tb, g);
+  if (g.splits > 1) {
+    PTN_COUNT(1);
+    splitk_reduce_kernel<<<grid_for(g.M * g.N), 256, 0, st>>>(g.partial, g.splits, g.M, g.N, g.mo, g.no,
+                                                              g.out_kind, g.C, g.c_plane, L, g.status);
+  }
   return ptn_launch_status();
 }
 
@@ -445,8 +529,22 @@ extern "C" int ptn_cgemm_bf16x3(const ptn_cgemm_desc* d, void* stream) {
     return PTN_ERR_ARG;
   const int64_t tm = (d->M + MT - 1) / MT, tn = (d->N + NT - 1) / NT;
   g.tiles_n = tn;
-  if (tm * tn > 0x7fffffffLL) return PTN_ERR_UNSUPPORTED;
-  const unsigned grid = (unsigned)(tm * tn);
+  g.tiles = tm * tn;
+  int64_t splits = 1, ksplit = (d->K + KT - 1) / KT;
+  if (d->partial) {
+    int64_t s_, k_;
+    split_plan(d->M, d->N, d->K, s_, k_);
+    if (s_ > 1 && s_ * d->M * d->N * (int64_t)sizeof(float2) <= d->partial_bytes &&
+        !(reinterpret_cast<uintptr_t>(d->partial) & 7)) {
+      splits = s_;
+      ksplit = k_;
+    }
+  }
+  g.splits = (int32_t)splits;
+  g.ksplit = (int32_t)ksplit;
+  g.partial = static_cast<float2*>(d->partial);
+  if (tm * tn * splits > 0x7fffffffLL) return PTN_ERR_UNSUPPORTED;
+  const unsigned grid = (unsigned)(tm * tn * splits);
   return L == 3 ? launch_gemm<3>(ta, tb, g, grid, ptn_stream(stream)) : launch_gemm<2>(ta, tb, g, grid, ptn_stream(stream));
 }
 

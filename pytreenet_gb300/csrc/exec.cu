@@ -14,7 +14,8 @@ extern "C" int ptn_exec_ops(const ptn_exec_op* ops, int32_t nops, void* const* p
   if (!ops || nops < 0 || (nops > 0 && (!ptrs || nptrs < 1))) return PTN_ERR_ARG;
   for (int32_t i = 0; i < nops; ++i) {
     const ptn_exec_op& op = ops[i];
-    if (!op.desc || op.a < 0 || op.a >= nptrs || op.b < -1 || op.b >= nptrs || op.c < 0 || op.c >= nptrs)
+    if (!op.desc || op.a < 0 || op.a >= nptrs || op.b < -1 || op.b >= nptrs || op.c < 0 || op.c >= nptrs ||
+        op.d < -1 || op.d >= nptrs)
       return PTN_ERR_ARG;
     int st;
     switch (op.kind) {
@@ -31,6 +32,7 @@ extern "C" int ptn_exec_ops(const ptn_exec_op* ops, int32_t nops, void* const* p
         d.A = ptrs[op.a];
         d.Bx = op.b >= 0 ? ptrs[op.b] : nullptr;
         d.C = ptrs[op.c];
+        if (op.d >= 0) d.partial = ptrs[op.d];
         st = ptn_cgemm_bf16x3(&d, stream);
         break;
       }

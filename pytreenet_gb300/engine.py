@@ -180,9 +180,10 @@ class _NativeOps:
         self.descs = [d for _, d, _ in items]
         self.ops = (_lib.ExecOp * max(len(items), 1))()
         for i, (kind, d, refs) in enumerate(items):
-            a, b, c = refs
+            a, b, c = refs[:3]
             self.ops[i].kind = kind
             self.ops[i].a, self.ops[i].b, self.ops[i].c = slot(a), slot(b), slot(c)
+            self.ops[i].d = slot(refs[3]) if len(refs) > 3 else -1
             self.ops[i].desc = ctypes.addressof(d)
         self.n = len(items)
         self.ptrs = (ctypes.c_void_p * len(self.refs))()
@@ -289,7 +290,8 @@ class MixedPlan:
         self.ws = ws
         self.levels = L = int(levels)
         self.ops = []            # ("conv"|"expand"|"gemm", desc, refs)
-        self.sizes = {}          # ws name -> (numel, dtype)
+        self.sizes = {}          # ws name -> numel (bf16 planes)
+        self.byte_sizes = {}     # ws name -> bytes (complex128 slots)
         self.flops = 0
         nsteps = len(logical)
         info = []
@@ -358,6 +360,11 @@ class MixedPlan:
             g = CgemmDesc()
             g.lda, g.a_plane, g.M, g.K, g.ldb, g.N = lda, plane, M, K, ldb, N
             g.levels = L
+            # split-K scratch for outputs with few tiles (one shared slot)
+            pb = int(_lib.load().ptn_cgemm_partial_bytes(M, N, K))
+            g.partial_bytes = pb
+            if pb:
+                self._need_bytes("tc_partial", pb)
             ost = out_stride[i]
             if i < nsteps - 1:
                 nrows, ncols, nlda, _ = A_layout[i + 1]
@@ -379,9 +386,14 @@ class MixedPlan:
     def _need(self, name, numel):
         self.sizes[name] = max(self.sizes.get(name, 0), numel)
 
+    def _need_bytes(self, name, nbytes):
+        self.byte_sizes[name] = max(self.byte_sizes.get(name, 0), int(nbytes))
+
     def run(self, x_ptr: int = 0, y_ptr: int = 0):
         for name, n in self.sizes.items():
             self.ws.get(name, n + 64, torch.bfloat16)
+        for name, nb in self.byte_sizes.items():
+            self.ws.get(name, (nb + 15) // 16, CDT)
         status = self.ws.bufs.get("tc_status")
         if status is None:
             status = torch.zeros(1, dtype=torch.int32, device=self.ws.device)
@@ -395,7 +407,8 @@ class MixedPlan:
                     items.append((_lib.OP_EXPAND_B, d, (refs[0], None, refs[1])))
                 else:
                     d.status = status.data_ptr()
-                    items.append((_lib.OP_CGEMM, d, tuple(refs)))
+                    part = ("ws", "tc_partial") if d.partial_bytes else None
+                    items.append((_lib.OP_CGEMM, d, tuple(refs) + (part,)))
             self._exec = _NativeOps(items)
         self._exec.run(self.ws, x_ptr, y_ptr)
 

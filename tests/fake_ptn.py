@@ -401,3 +401,5 @@ def _fake_tri_inv_newton(self, X, R0, R, work, k, stream):
 FakeLib.ptn_ztri_inv_newton = _fake_tri_inv_newton
 FakeLib.ptn_znonzero_rows = _fake_nonzero_rows
 FakeLib.ptn_zqr_keep_rows = _fake_qr_keep_rows
+# the stand-in GEMM never splits K
+FakeLib.ptn_cgemm_partial_bytes = lambda self, M, N, K: 0

@@ -205,3 +205,53 @@ def test_cgemm_abort_mid_kernel_drains_and_recovers(lib):
     torch.cuda.synchronize()
     assert int(status.item()) == 0
     assert torch.equal(C, C_ok)
+
+
+@pytest.mark.parametrize("M,N,K", [(256, 256, 16384), (200, 70, 4096), (1280, 256, 2048)])
+def test_cgemm_split_k_matches_complex128(lib, M, N, K):
+    """Few output tiles and a long K: the product is split over K (FP32
+    partial sums added in FP64) and matches complex128 at the BF16x6 level."""
+    from pytreenet_gb300.engine import Operand, ChainBuilder, Workspace
+    assert lib.ptn_cgemm_partial_bytes(M, N, K) > 0
+    A, B = crandn(M, K), crandn(N, K)
+    Ad, Bd = torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()
+    C = torch.zeros((M, N), dtype=torch.complex128, device="cuda")
+    ws = Workspace("cuda")
+    cb = ChainBuilder(ws)
+    cb.contract(Operand.contiguous(("fixed", Ad), ["m", "k"], [M, K]),
+                Operand.contiguous(("fixed", Bd), ["n", "k"], [N, K]), ["k"],
+                out=Operand.contiguous(("fixed", C), ["m", "n"], [M, N]))
+    p = cb.mixed_plan(3)
+    p.run()
+    torch.cuda.synchronize()
+    assert int(ws.bufs["tc_status"].item()) == 0
+    assert "tc_partial" in ws.bufs
+    err = np.max(np.abs(C.cpu().numpy() - A @ B.T)) / np.sqrt(K)
+    assert err < 2e-6, err
+    # deterministic: a second run gives the same bits
+    C0 = C.clone()
+    p.run()
+    torch.cuda.synchronize()
+    assert torch.equal(C, C0)
+
+
+def test_cgemm_split_k_into_planes(lib):
+    """A split first step writes its sum as BF16 planes for the next step."""
+    from pytreenet_gb300.engine import Operand, ChainBuilder, Workspace
+    M, K, N, P = 200, 8192, 100, 60
+    assert lib.ptn_cgemm_partial_bytes(M, N, K) > 0
+    A, B, D = crandn(M, K), crandn(N, K), crandn(N, P)
+    Ad, Bd, Dd = (torch.from_numpy(x).cuda() for x in (A, B, D))
+    C = torch.zeros((M, P), dtype=torch.complex128, device="cuda")
+    ws = Workspace("cuda")
+    cb = ChainBuilder(ws)
+    T = cb.contract(Operand.contiguous(("fixed", Ad), ["m", "k"], [M, K]),
+                    Operand.contiguous(("fixed", Bd), ["n", "k"], [N, K]), ["k"])
+    cb.contract(T, Operand.contiguous(("fixed", Dd), ["n", "p"], [N, P]), ["n"],
+                out=Operand.contiguous(("fixed", C), ["m", "p"], [M, P]))
+    cb.mixed_plan(3).run()
+    torch.cuda.synchronize()
+    assert int(ws.bufs["tc_status"].item()) == 0
+    ref = (A @ B.T) @ D
+    err = np.max(np.abs(C.cpu().numpy() - ref)) / (np.sqrt(K) * np.sqrt(N))
+    assert err < 2e-6, err

@@ -119,6 +119,19 @@ int64_t ptn_zqr_work_bytes(int64_t m, int64_t k);
 int ptn_zqr_keep(void* A, const int64_t* rowoff, int64_t m, int64_t k, int64_t colstride,
                  void* R, void* work, void* stream);
 
+/* How ptn_zqr_keep runs an m x k problem on the current device: 1 = one
+ * cooperative launch (m <= 2048 and the columns fit in shared memory; each
+ * reflector is handed from CTA to CTA through a flag, no launch per step),
+ * 0 = a launch sequence per Householder step. Both give the same bits. A
+ * caller that records launch sequences into CUDA graphs uses this to record
+ * only the sequences. No counterpart in the reference. */
+int ptn_zqr_path(int64_t m, int64_t k);
+
+/* ptn_zqr_keep, always as the launch sequence (path 0): the same result, for
+ * callers that record the launches into a CUDA graph or compare the paths. */
+int ptn_zqr_keep_steps(void* A, const int64_t* rowoff, int64_t m, int64_t k, int64_t colstride,
+                       void* R, void* work, void* stream);
+
 /* Same result as ptn_zqr_keep on the m x k matrix when its rows m_used..m-1
  * (in rowoff order) are exactly zero: the factorisation runs on the first
  * m_used rows with the kernel sequence of the m-row problem (so the same

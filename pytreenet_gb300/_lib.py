@@ -105,6 +105,8 @@ SIGNATURES = {
     "ptn_zscal_ratio": (ctypes.c_int, [_P, _P, _P, _P, _I64, _P]),
     "ptn_zqr_work_bytes": (_I64, [_I64, _I64]),
     "ptn_zqr_keep": (ctypes.c_int, [_P, _P, _I64, _I64, _I64, _P, _P, _P]),
+    "ptn_zqr_path": (ctypes.c_int, [_I64, _I64]),
+    "ptn_zqr_keep_steps": (ctypes.c_int, [_P, _P, _I64, _I64, _I64, _P, _P, _P]),
     "ptn_check_finite": (ctypes.c_int, [_P, _I64, _P, _P]),
     "ptn_launch_counter": (ctypes.c_ulonglong, []),
     "ptn_zqr_noalloc_max_bytes": (_I64, []),

@@ -363,14 +363,272 @@ inline unsigned grid1(int64_t n) {
   return (unsigned)b;
 }
 
+// ---- small m, one cooperative launch ---------------------------------------------------
+// The same Householder steps as hh_fact_small / extract_r_small / hh_form_small,
+// with the same arithmetic per column (thread-to-row map, reduction tree,
+// scalar formulas), so the results are the same bits; but all of them run in
+// one launch. CTA b owns a few columns (snake order, so the Q formation work
+// -- column c needs c + 1 reflectors -- is balanced) and keeps them in shared
+// memory. Reflector j is computed once, by the owner of column j, as soon as
+// column j has received reflectors 0 .. j-1, and published through V, tau and
+// a flag; every CTA waits for the flag (bounded), then applies the reflector
+// to its own columns. The owner of column j + 1 updates that column first and
+// publishes reflector j + 1 right away, so the chain of dependent steps costs
+// one flag hand-over each instead of one kernel launch.
+constexpr long long HP_WAIT_CYCLES = 4000000000LL;   // ~2 s at 2 GHz
+
+struct HPArgs {
+  double2* A;
+  const int64_t* rowoff;
+  int64_t cs, m, k, p;
+  double2* tau;
+  double2* betas;
+  double2* V;
+  double2* R;
+  int* ready;     // [p], zero on entry; ready[j] = 1 once reflector j is published
+  int* status;    // nonzero: a wait ran out (every CTA stops)
+  int G;          // CTAs
+  int cpc;        // columns per CTA (upper bound)
+};
+
+// i-th column of CTA b (increasing in i)
+__device__ __forceinline__ int64_t hp_col(int b, int i, int G) {
+  return (int64_t)i * G + ((i & 1) ? (G - 1 - b) : b);
+}
+__device__ __forceinline__ int hp_owner(int64_t c, int G) {
+  const int64_t i = c / G, r = c - i * G;
+  return (int)((i & 1) ? (G - 1 - r) : r);
+}
+
+__global__ void __launch_bounds__(ST) hh_persistent_kernel(HPArgs a) {
+  extern __shared__ double2 hsm[];           // [cpc][m] own columns, then [m] reflector
+  __shared__ double red[ST / 32 + 1];
+  __shared__ double2 sc[2];
+  __shared__ int abort_s;
+  const int b = blockIdx.x, tid = threadIdx.x, G = a.G;
+  const int64_t m = a.m, k = a.k, p = a.p, cs = a.cs;
+  double2* vs = hsm + (int64_t)a.cpc * m;
+  int nown = 0;
+  while (nown < a.cpc && hp_col(b, nown, G) < k) ++nown;
+  for (int i = 0; i < nown; ++i) {
+    const int64_t c = hp_col(b, i, G);
+    for (int64_t t = tid; t < m; t += ST) hsm[i * m + t] = a.A[a.rowoff[t] + c * cs];
+  }
+  if (tid == 0) abort_s = 0;
+  __syncthreads();
+
+  // zlarfg on column j (own slot col) and publication of v_j, tau_j, beta_j
+  auto publish = [&](int64_t j, const double2* col) {
+    const int64_t len = m - j;
+    double acc = 0.0;
+    for (int64_t t = tid; t < len; t += ST)
+      if (t > 0) acc += cabs2(col[j + t]);
+    const double xn2 = block_sum<ST>(acc, red);
+    if (tid == 0) {
+      const double2 alpha = col[j];
+      const double xnorm = sqrt(xn2);
+      double2 t_, s_, b_;
+      if (xnorm == 0.0 && alpha.y == 0.0) {
+        t_ = make_double2(0.0, 0.0);
+        s_ = make_double2(0.0, 0.0);
+        b_ = alpha;
+      } else {
+        const double nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xnorm * xnorm);
+        const double beta = (alpha.x >= 0.0) ? -nrm : nrm;
+        t_ = make_double2((beta - alpha.x) / beta, -alpha.y / beta);
+        const double2 d = make_double2(alpha.x - beta, alpha.y);
+        const double den = d.x * d.x + d.y * d.y;
+        s_ = make_double2(d.x / den, -d.y / den);
+        b_ = make_double2(beta, 0.0);
+      }
+      sc[1] = s_;
+      a.tau[j] = t_;
+      a.betas[j] = b_;
+    }
+    __syncthreads();
+    const double2 s_ = sc[1];
+    for (int64_t t = tid; t < len; t += ST)
+      a.V[j * m + j + t] = (t == 0) ? make_double2(1.0, 0.0) : cmul(col[j + t], s_);
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) atomicExch(a.ready + j, 1);
+  };
+
+  if (p > 0 && hp_owner(0, G) == b) publish(0, hsm);      // column 0 is this CTA's slot 0
+  for (int64_t j = 0; j < p; ++j) {
+    if (tid == 0) {
+      const volatile int* flag = a.ready + j;
+      const volatile int* st = a.status;
+      const long long t0 = clock64();
+      for (unsigned it = 0;; ++it) {
+        if (*flag != 0) break;
+        if ((it & 255u) == 0u && *st != 0) { abort_s = 1; break; }
+        if (clock64() - t0 > HP_WAIT_CYCLES) {
+          atomicExch(a.status, PTN_ERR_TIMEOUT);
+          abort_s = 1;
+          break;
+        }
+      }
+      __threadfence();
+      if (!abort_s) sc[0] = __ldcg(a.tau + j);
+    }
+    __syncthreads();
+    if (abort_s) break;
+    const int64_t len = m - j;
+    for (int64_t t = tid; t < len; t += ST) vs[t] = __ldcg(a.V + j * m + j + t);
+    __syncthreads();
+    double2 f = sc[0];
+    f.y = -f.y;  // conj(tau): the factorisation applies H^H
+    for (int i = 0; i < nown; ++i) {
+      const int64_t c = hp_col(b, i, G);
+      if (c <= j) continue;
+      double2* col = hsm + i * m;
+      double2 w = make_double2(0.0, 0.0);
+      for (int64_t t = tid; t < len; t += ST) w = cfmac(vs[t], col[j + t], w);
+      w = block_sum2<ST>(w, red);
+      const double2 fw = cmul(f, w);
+      for (int64_t t = tid; t < len; t += ST) col[j + t] = csub(col[j + t], cmul(vs[t], fw));
+      __syncthreads();
+      if (c == j + 1 && j + 1 < p) publish(j + 1, col);
+    }
+    __syncthreads();
+  }
+  if (abort_s) {
+    if (b == 0 && tid == 0) a.R[0] = make_double2(NAN, NAN);   // the result is not usable
+    return;
+  }
+  // R (rows < p: beta on the diagonal, the stored upper part above it), then Q
+  // (zung2r: column c = H_0 ... H_c e_c), KEEP padding past p
+  for (int i = 0; i < nown; ++i) {
+    const int64_t c = hp_col(b, i, G);
+    double2* col = hsm + i * m;
+    for (int64_t r = tid; r < k; r += ST) {
+      double2 v = make_double2(0.0, 0.0);
+      if (r < p) {
+        if (c == r) v = a.betas[r];
+        else if (c > r) v = col[r];
+      }
+      a.R[r * k + c] = v;
+    }
+    __syncthreads();
+    if (c >= p) {
+      for (int64_t t = tid; t < m; t += ST) a.A[a.rowoff[t] + c * cs] = make_double2(0.0, 0.0);
+      continue;
+    }
+    // reflectors come from other CTAs: read them through L2
+    const double2 tc = __ldcg(a.tau + c);
+    const double2* vc = a.V + c * m;
+    for (int64_t t = tid; t < m; t += ST) {
+      if (t < c) {
+        col[t] = make_double2(0.0, 0.0);
+      } else if (t == c) {
+        col[t] = make_double2(1.0 - tc.x, -tc.y);
+      } else {
+        const double2 vt = __ldcg(vc + t);
+        col[t] = make_double2(-(tc.x * vt.x - tc.y * vt.y), -(tc.x * vt.y + tc.y * vt.x));
+      }
+    }
+    __syncthreads();
+    for (int64_t j = c - 1; j >= 0; --j) {
+      const double2 t_ = __ldcg(a.tau + j);
+      const double2* v = a.V + j * m;
+      double2 w = make_double2(0.0, 0.0);
+      for (int64_t t = j + tid; t < m; t += ST) w = cfmac(__ldcg(v + t), col[t], w);
+      w = block_sum2<ST>(w, red);
+      const double2 fw = cmul(t_, w);
+      for (int64_t t = j + tid; t < m; t += ST) col[t] = csub(col[t], cmul(__ldcg(v + t), fw));
+      __syncthreads();
+    }
+    for (int64_t t = tid; t < m; t += ST) a.A[a.rowoff[t] + c * cs] = col[t];
+  }
+}
+
 }  // namespace
 
 extern "C" int64_t ptn_zqr_work_bytes(int64_t m, int64_t k) {
   if (m <= QR_SMALL_M) {
     const int64_t p = m < k ? m : k;
-    return 16 * (2 * k + m * p) + 256;   // tau, betas, V
+    return 16 * (2 * k + m * p) + 4 * (p + 1) + 512;   // tau, betas, V, flags, status
   }
   return 16 * (3 * k + (nrb_for(m) + 1) / 2 + 1 + nrb_for(m) * k) + 256;
+}
+
+// Launch shape of the one-launch path for an m x k problem (m <= QR_SMALL_M):
+// CTAs, columns per CTA and dynamic shared memory; false when it does not fit
+// (columns too many for shared memory, or more CTAs than can be co-resident).
+static bool hp_shape(int64_t m, int64_t k, int& G, int& cpc, size_t& smem) {
+  // device properties and the kernel's shared-memory limit: once per process
+  // (thread-safe static initialisation; the engine drives one device)
+  struct Dev {
+    int n_sm = 0;
+    size_t dyn_max = 0;
+  };
+  static const Dev dv = []() {
+    Dev d;
+    int dev = 0;
+    cudaDeviceProp pr;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&pr, dev) != cudaSuccess ||
+        !pr.cooperativeLaunch)
+      return d;
+    const size_t dyn = pr.sharedMemPerBlockOptin - 1024;    // room for the static shared memory
+    if (cudaFuncSetAttribute(hh_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn) !=
+        cudaSuccess)
+      return d;
+    d.n_sm = pr.multiProcessorCount;
+    d.dyn_max = dyn;
+    return d;
+  }();
+  if (dv.n_sm <= 0 || m < 1 || k < 1 || m > QR_SMALL_M) return false;
+  int64_t g = (k + 1) / 2;                           // two columns per CTA
+  if (g > dv.n_sm) g = dv.n_sm;
+  const int64_t c = (k + g - 1) / g;
+  const size_t bytes = (size_t)(c + 1) * (size_t)m * sizeof(double2);
+  if (bytes > dv.dyn_max) return false;
+  int max_per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, hh_persistent_kernel, ST, bytes) != cudaSuccess ||
+      (int64_t)max_per_sm * dv.n_sm < g)
+    return false;
+  G = (int)g;
+  cpc = (int)c;
+  smem = bytes;
+  return true;
+}
+
+extern "C" int ptn_zqr_path(int64_t m, int64_t k) {
+  int G, cpc;
+  size_t smem;
+  if (m <= QR_SMALL_M && hp_shape(m, k, G, cpc, smem)) return 1;
+  return 0;
+}
+
+static int zqr_keep_persistent(double2* A, const int64_t* rowoff, int64_t m, int64_t k, int64_t cs, double2* R,
+                               void* work, cudaStream_t s) {
+  int G, cpc;
+  size_t smem;
+  if (!hp_shape(m, k, G, cpc, smem)) return PTN_ERR_UNSUPPORTED;
+  const int64_t p = m < k ? m : k;
+  HPArgs a;
+  a.A = A;
+  a.rowoff = rowoff;
+  a.cs = cs;
+  a.m = m;
+  a.k = k;
+  a.p = p;
+  a.tau = static_cast<double2*>(work);
+  a.betas = a.tau + k;
+  a.V = a.betas + k;
+  a.ready = reinterpret_cast<int*>(a.V + m * p);
+  a.status = a.ready + p;
+  a.R = R;
+  a.G = G;
+  a.cpc = cpc;
+  if (cudaMemsetAsync(a.ready, 0, sizeof(int) * (size_t)(p + 1), s) != cudaSuccess) return PTN_ERR_LAUNCH;
+  void* args[] = {&a};
+  PTN_COUNT(1);
+  if (cudaLaunchCooperativeKernel((const void*)hh_persistent_kernel, dim3((unsigned)G), dim3(ST), args, smem, s) !=
+      cudaSuccess)
+    return PTN_ERR_LAUNCH;
+  return ptn_launch_status();
 }
 
 static int zqr_keep_small(double2* A, const int64_t* rowoff, int64_t m, int64_t k, int64_t cs, double2* R,
@@ -413,6 +671,16 @@ extern "C" int ptn_zqr_keep(void* Av, const int64_t* rowoff, int64_t m, int64_t 
                        ptn_stream(stream));
 }
 
+extern "C" int ptn_zqr_keep_steps(void* Av, const int64_t* rowoff, int64_t m, int64_t k, int64_t cs, void* Rv,
+                                  void* work, void* stream) {
+  if (!Av || !rowoff || !Rv || !work || m < 1 || k < 1 || cs < 1) return PTN_ERR_ARG;
+  if (m > QR_SMALL_M)
+    return zqr_keep_impl(static_cast<double2*>(Av), rowoff, m, m, k, cs, static_cast<double2*>(Rv), work,
+                         ptn_stream(stream));
+  return zqr_keep_small(static_cast<double2*>(Av), rowoff, m, k, cs, static_cast<double2*>(Rv), work,
+                        ptn_stream(stream));
+}
+
 extern "C" int ptn_zqr_keep_rows(void* Av, const int64_t* rowoff, int64_t m, int64_t m_used, int64_t k, int64_t cs,
                                  void* Rv, void* work, void* stream) {
   if (!Av || !rowoff || !Rv || !work || m < 1 || k < 1 || cs < 1 || m_used < 1 || m_used > m) return PTN_ERR_ARG;
@@ -436,7 +704,11 @@ extern "C" int ptn_zqr_keep_rows(void* Av, const int64_t* rowoff, int64_t m, int
 // rounding) of an m_path-row problem.
 static int zqr_keep_impl(double2* A, const int64_t* rowoff, int64_t m_path, int64_t m, int64_t k, int64_t cs,
                          double2* R, void* work, cudaStream_t s) {
-  if (m_path <= QR_SMALL_M) return zqr_keep_small(A, rowoff, m, k, cs, R, work, s);
+  if (m_path <= QR_SMALL_M) {
+    const int st = zqr_keep_persistent(A, rowoff, m, k, cs, R, work, s);
+    if (st != PTN_ERR_UNSUPPORTED) return st;
+    return zqr_keep_small(A, rowoff, m, k, cs, R, work, s);
+  }
   QRWork q = carve(work, m, k);
   const int64_t p = m < k ? m : k;
   // factorisation

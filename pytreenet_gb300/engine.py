@@ -1036,7 +1036,10 @@ class DeviceNetwork:
                 check(lib.ptn_zqr_keep(self.t[nid].data_ptr(), rowoff.data_ptr(), m, k, strides[col_axis],
                                        R.data_ptr(), work.data_ptr(), _stream_ptr()), "ptn_zqr_keep")
         gkey = (nid, nbr, key, m_used)
-        if not self.use_graphs or self.device.type != "cuda":
+        # small splits run as one cooperative launch (ptn_zqr_path 1): nothing
+        # to replay; the per-step launch sequences of larger ones are recorded
+        one_launch = m <= 2048 and int(lib.ptn_zqr_path(m_used, k)) == 1
+        if not self.use_graphs or self.device.type != "cuda" or one_launch:
             launch()
         elif gkey in self.qr_graphs:
             g, nlaunch = self.qr_graphs[gkey]

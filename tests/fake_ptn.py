@@ -403,3 +403,4 @@ FakeLib.ptn_znonzero_rows = _fake_nonzero_rows
 FakeLib.ptn_zqr_keep_rows = _fake_qr_keep_rows
 # the stand-in GEMM never splits K
 FakeLib.ptn_cgemm_partial_bytes = lambda self, M, N, K: 0
+FakeLib.ptn_zqr_path = lambda self, m, k: 0

@@ -199,3 +199,36 @@ def test_engine_rank_deficient_split_takes_householder(lib):
     assert outs[1][2].cholqr_count == 0 and outs[1][2].householder_count == 1
     assert outs[1][2].qr_rows_skipped == 256 - 6
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+
+
+@pytest.mark.parametrize("shape,pad", [((256, 256, 2), 0), ((256, 256, 2), 100), ((24, 24, 2), 0),
+                                       ((40, 7, 2), 0), ((8, 300, 2), 0), ((64, 1000, 2), 0), ((3, 1, 2), 0),
+                                       ((512, 100, 2), 0)])
+def test_zqr_one_launch_path_equals_launch_sequence(lib, shape, pad):
+    """The one-launch Householder QR (reflectors handed between CTAs through
+    flags) returns the same bits as the per-step launch sequence, full-rank
+    and with zero-padded columns (KEEP complements), tall and wide."""
+    from pytreenet_gb300.engine import _stream_ptr
+    T = crandn(*shape)
+    if pad:
+        T[:, shape[1] - pad:, :] = 0.0           # the trailing child indices unused: rank-deficient rows
+    idx, strides = _rowoff(shape, [1, 2])
+    k, m = shape[0], idx.size
+    if m <= 2048:
+        assert lib.ptn_zqr_path(m, k) == 1
+    ro = dev(idx)
+    w = torch.zeros((int(lib.ptn_zqr_work_bytes(m, k)) + 15) // 16, dtype=torch.complex128, device="cuda")
+    out = []
+    for fn in (lib.ptn_zqr_keep, lib.ptn_zqr_keep_steps):
+        A = dev(T.copy())
+        R = torch.zeros(k * k, dtype=torch.complex128, device="cuda")
+        assert fn(A.data_ptr(), ro.data_ptr(), m, k, strides[0], R.data_ptr(), w.data_ptr(), _stream_ptr()) == 0
+        torch.cuda.synchronize()
+        out.append((A.cpu().numpy(), R.cpu().numpy()))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+    # and it is a QR: Q R = A
+    mat = T.reshape(-1)[idx[:, None] + np.arange(k)[None, :] * strides[0]]
+    q = out[0][0].reshape(-1)[idx[:, None] + np.arange(k)[None, :] * strides[0]]
+    r = out[0][1].reshape(k, k)
+    assert np.max(np.abs(q @ r - mat)) < 1e-12 * max(1.0, np.max(np.abs(mat)))

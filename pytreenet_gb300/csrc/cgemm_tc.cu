@@ -72,6 +72,10 @@ struct GemmArgs {
 // each range keeps at least SPLIT_MIN_KT K tiles.
 constexpr int64_t SPLIT_TARGET_CTAS = 304;
 constexpr int64_t SPLIT_MIN_KT = 4;
+// Products with fewer K tiles than this are not split: measured on GB300, the
+// partial-sum pass costs more than the parallelism gains below K = 1024
+// (512 x 1280 x 256: 70 us split, 47 us not; 256 x 256 x 1280: 54 vs 84 us).
+constexpr int64_t SPLIT_MIN_KT_TOTAL = 32;
 
 __device__ __forceinline__ int64_t decode_off(const OutModes& md, int64_t idx) {
   int64_t o = 0;
@@ -391,6 +395,82 @@ __global__ void expand_b_kernel(const double2* __restrict__ src, OutModes nm, Ou
   }
 }
 
+// ---- skinny products on the CUDA cores ----------------------------------------------
+// A product with K <= SMALLK_MAX_K (one 32-wide K tile) and N <= SMALLK_MAX_N
+// (the contraction with a TTNO tensor over its bond and physical legs, K =
+// w d = 10) does too little arithmetic per output for a tensor-core tile
+// pipeline: its set-up per CTA dominates (65536 x 10 x 10 measured 60 us).
+// Here one thread owns one row: it rebuilds A's row from the BF16 level planes,
+// B (same operand layout, staged in shared memory) likewise, accumulates in
+// FP32 as the tensor cores do, and writes through the same output modes; the
+// cost is the operand traffic.
+constexpr int64_t SMALLK_MAX_K = 32;
+constexpr int64_t SMALLK_MAX_N = 128;
+constexpr int SMALLK_T = 128;
+
+__global__ void __launch_bounds__(SMALLK_T)
+    cgemm_smallk_kernel(const __nv_bfloat16* __restrict__ A, int64_t lda, int64_t a_plane,
+                        const __nv_bfloat16* __restrict__ Bx, int64_t ldb, GemmArgs g, int L) {
+  __shared__ float2 sB[SMALLK_MAX_N * SMALLK_MAX_K];
+  __shared__ int64_t noff[SMALLK_MAX_N];
+  if (*(volatile int32_t*)g.status != 0) return;
+  const int N = (int)g.N, K = (int)g.K;
+  const int64_t blk = (int64_t)N * ldb;
+  for (int e = threadIdx.x; e < N * K; e += SMALLK_T) {
+    const int n = e / K, kk = e - n * K;
+    float re = 0.f, im = 0.f;
+    for (int lv = 0; lv < L; ++lv) {
+      re += __bfloat162float(Bx[(3 * lv + 1) * blk + (int64_t)n * ldb + kk]);
+      im += __bfloat162float(Bx[(3 * lv + 2) * blk + (int64_t)n * ldb + kk]);
+    }
+    sB[n * SMALLK_MAX_K + kk] = make_float2(re, im);
+  }
+  for (int n = threadIdx.x; n < N; n += SMALLK_T) noff[n] = decode_off(g.no, n);
+  __syncthreads();
+  for (int64_t m = blockIdx.x * (int64_t)SMALLK_T + threadIdx.x; m < g.M; m += (int64_t)gridDim.x * SMALLK_T) {
+    float2 a[SMALLK_MAX_K];
+#pragma unroll
+    for (int kk = 0; kk < SMALLK_MAX_K; ++kk) {
+      float re = 0.f, im = 0.f;
+      if (kk < K) {
+        for (int lv = 0; lv < L; ++lv) {
+          re += __bfloat162float(A[(2 * lv) * a_plane + m * lda + kk]);
+          im += __bfloat162float(A[(2 * lv + 1) * a_plane + m * lda + kk]);
+        }
+      }
+      a[kk] = make_float2(re, im);
+    }
+    const int64_t moff = decode_off(g.mo, m);
+    for (int n = 0; n < N; ++n) {
+      float cr = 0.f, ci = 0.f;
+#pragma unroll
+      for (int kk = 0; kk < SMALLK_MAX_K; ++kk) {
+        if (kk < K) {
+          const float2 b = sB[n * SMALLK_MAX_K + kk];
+          cr = fmaf(a[kk].x, b.x, cr);
+          cr = fmaf(-a[kk].y, b.y, cr);
+          ci = fmaf(a[kk].x, b.y, ci);
+          ci = fmaf(a[kk].y, b.x, ci);
+        }
+      }
+      const int64_t o = moff + noff[n];
+      if (g.out_kind == 0) {
+        static_cast<double2*>(g.C)[o] = make_double2((double)cr, (double)ci);
+      } else {
+        __nv_bfloat16* C = static_cast<__nv_bfloat16*>(g.C);
+        for (int lv = 0; lv < L; ++lv) {
+          const __nv_bfloat16 rb = __float2bfloat16_rn(cr);
+          const __nv_bfloat16 ib = __float2bfloat16_rn(ci);
+          C[(2 * lv) * g.c_plane + o] = rb;
+          C[(2 * lv + 1) * g.c_plane + o] = ib;
+          cr -= __bfloat162float(rb);
+          ci -= __bfloat162float(ib);
+        }
+      }
+    }
+  }
+}
+
 // Sum of the split-K partial sums (FP64, ranges in order: deterministic),
 // written like the GEMM epilogue: complex128 through the output modes, or as
 // BF16 level planes.
@@ -431,7 +511,7 @@ void split_plan(int64_t M, int64_t N, int64_t K, int64_t& splits, int64_t& kspli
   const int64_t kt_all = (K + KT - 1) / KT;
   splits = 1;
   ksplit = kt_all;
-  if (tiles >= SPLIT_TARGET_CTAS / 2) return;
+  if (tiles >= SPLIT_TARGET_CTAS / 2 || kt_all < SPLIT_MIN_KT_TOTAL) return;
   int64_t s = (SPLIT_TARGET_CTAS + tiles - 1) / tiles;
   const int64_t smax = kt_all / SPLIT_MIN_KT;
   if (s > smax) s = smax;
@@ -519,6 +599,15 @@ extern "C" int ptn_cgemm_bf16x3(const ptn_cgemm_desc* d, void* stream) {
   g.c_plane = d->c_plane;
   g.status = d->status;
   if (fill_out(d->m_out, g.mo) || fill_out(d->n_out, g.no)) return PTN_ERR_ARG;
+  if (d->K <= SMALLK_MAX_K && d->N <= SMALLK_MAX_N) {
+    int64_t blocks = (d->M + SMALLK_T - 1) / SMALLK_T;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    PTN_COUNT(1);
+    cgemm_smallk_kernel<<<(unsigned)blocks, SMALLK_T, 0, ptn_stream(stream)>>>(
+        static_cast<const __nv_bfloat16*>(d->A), d->lda, d->a_plane, static_cast<const __nv_bfloat16*>(d->Bx),
+        d->ldb, g, d->levels);
+    return ptn_launch_status();
+  }
   CUtensorMap ta, tb;
   const int L = d->levels;
   if (make_map_3d(&ta, d->A, (uint64_t)d->K, (uint64_t)d->M, 2 * L, (uint64_t)d->lda * 2,

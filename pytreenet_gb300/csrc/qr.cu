@@ -249,6 +249,30 @@ __device__ __forceinline__ double2 block_sum2(double2 v, double* red) {
   return make_double2(re, im);
 }
 
+// block_sum2 in one pass: both parts reduced with block_sum's tree (same warp
+// shuffles, warp partials added in warp order by thread 0), so the same bits,
+// with half the barriers. red2: NTH / 32 + 1 entries.
+template <int NTH>
+__device__ __forceinline__ double2 block_sum2_fused(double2 v, double2* red2) {
+  v.x = warp_sum(v.x);
+  v.y = warp_sum(v.y);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) red2[w] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sx = 0.0, sy = 0.0;
+    for (int i = 0; i < NTH / 32; ++i) {
+      sx += red2[i].x;
+      sy += red2[i].y;
+    }
+    red2[NTH / 32] = make_double2(sx, sy);
+  }
+  __syncthreads();
+  const double2 s = red2[NTH / 32];
+  __syncthreads();
+  return s;
+}
+
 // Step j of the factorisation. grid = max(1, k - j - 1); CTA b owns column j+1+b.
 template <int NTH>
 __global__ void __launch_bounds__(NTH) hh_fact_small(double2* __restrict__ A, const int64_t* __restrict__ rowoff,
@@ -403,6 +427,7 @@ __device__ __forceinline__ int hp_owner(int64_t c, int G) {
 __global__ void __launch_bounds__(ST) hh_persistent_kernel(HPArgs a) {
   extern __shared__ double2 hsm[];           // [cpc][m] own columns, then [m] reflector
   __shared__ double red[ST / 32 + 1];
+  __shared__ double2 red2[ST / 32 + 1];
   __shared__ double2 sc[2];
   __shared__ int abort_s;
   const int b = blockIdx.x, tid = threadIdx.x, G = a.G;
@@ -485,7 +510,7 @@ __global__ void __launch_bounds__(ST) hh_persistent_kernel(HPArgs a) {
       double2* col = hsm + i * m;
       double2 w = make_double2(0.0, 0.0);
       for (int64_t t = tid; t < len; t += ST) w = cfmac(vs[t], col[j + t], w);
-      w = block_sum2<ST>(w, red);
+      w = block_sum2_fused<ST>(w, red2);
       const double2 fw = cmul(f, w);
       for (int64_t t = tid; t < len; t += ST) col[j + t] = csub(col[j + t], cmul(vs[t], fw));
       __syncthreads();
@@ -534,7 +559,7 @@ __global__ void __launch_bounds__(ST) hh_persistent_kernel(HPArgs a) {
       const double2* v = a.V + j * m;
       double2 w = make_double2(0.0, 0.0);
       for (int64_t t = j + tid; t < m; t += ST) w = cfmac(__ldcg(v + t), col[t], w);
-      w = block_sum2<ST>(w, red);
+      w = block_sum2_fused<ST>(w, red2);
       const double2 fw = cmul(t_, w);
       for (int64_t t = j + tid; t < m; t += ST) col[t] = csub(col[t], cmul(__ldcg(v + t), fw));
       __syncthreads();

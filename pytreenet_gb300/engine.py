@@ -240,8 +240,8 @@ class ChainBuilder:
     def plan(self) -> Plan:
         return Plan(self.ws, self.steps, self.sizes)
 
-    def mixed_plan(self, levels: int = 3) -> "MixedPlan":
-        return MixedPlan(self.ws, self.logical, levels)
+    def mixed_plan(self, levels: int = 3, own_fixed: bool = False) -> "MixedPlan":
+        return MixedPlan(self.ws, self.logical, levels, own_fixed)
 
 
 def _modes_single(dims, strides):
@@ -285,11 +285,18 @@ class MixedPlan:
     ``ptn_expand_b``; the first operand is gathered by ``ptn_to_planes``.
     """
 
-    def __init__(self, ws: Workspace, logical, levels: int = 3):
+    def __init__(self, ws: Workspace, logical, levels: int = 3, own_fixed: bool = False):
+        """``own_fixed``: operands that are fixed tensors (environments, TTNO
+        tensors) are split into BF16 planes held by the plan and converted by
+        ``prepare()`` only; a plan run many times on the same operands (the
+        H_eff of one Krylov solve) then converts only the moving vector."""
         from ._lib import CgemmDesc, ConvertDesc
         self.ws = ws
         self.levels = L = int(levels)
         self.ops = []            # ("conv"|"expand"|"gemm", desc, refs)
+        self.prep = []           # conversions of fixed operands into plan-owned planes
+        self.owned = []          # plan-owned plane buffers
+        self.hold = False        # True: run() skips the prep conversions (operands unchanged)
         self.sizes = {}          # ws name -> numel (bf16 planes)
         self.byte_sizes = {}     # ws name -> bytes (complex128 slots)
         self.flops = 0
@@ -348,15 +355,31 @@ class MixedPlan:
                 _set_modes(d.rows, [dims[l] for l in rows], [A.strides[A.labels.index(l)] for l in rows], "stride_a")
                 _set_modes(d.cols, [dims[l] for l in cols], [A.strides[A.labels.index(l)] for l in cols], "stride_a")
                 d.ld, d.plane, d.conj, d.levels = lda, plane, int(kw.get("conj_a", False)), L
-                self.ops.append(("conv", d, (A.ref, ("ws", aslot))))
-                self._need(aslot, 2 * L * plane)
+                if own_fixed and A.ref[0] == "fixed":
+                    buf = torch.empty(2 * L * plane + 64, dtype=torch.bfloat16, device=ws.device)
+                    self.owned.append(buf)
+                    aref = ("fixed", buf)
+                    self.prep.append(("conv", d, (A.ref, aref)))
+                else:
+                    aref = ("ws", aslot)
+                    self.ops.append(("conv", d, (A.ref, aref)))
+                    self._need(aslot, 2 * L * plane)
+            else:
+                aref = ("ws", aslot)
             ldb = _round8(K)
             d = ConvertDesc()
             _set_modes(d.rows, [dims[l] for l in nlab], [B.strides[B.labels.index(l)] for l in nlab], "stride_a")
             _set_modes(d.cols, [dims[l] for l in cols], [B.strides[B.labels.index(l)] for l in cols], "stride_a")
             d.ld, d.plane, d.conj, d.levels = ldb, 0, int(kw.get("conj_b", False)), L
-            self.ops.append(("expand", d, (B.ref, ("ws", "bx"))))
-            self._need("bx", 3 * L * N * ldb)
+            if own_fixed and B.ref[0] == "fixed":
+                buf = torch.empty(3 * L * N * ldb + 64, dtype=torch.bfloat16, device=ws.device)
+                self.owned.append(buf)
+                bref = ("fixed", buf)
+                self.prep.append(("expand", d, (B.ref, bref)))
+            else:
+                bref = ("ws", "bx")
+                self.ops.append(("expand", d, (B.ref, bref)))
+                self._need("bx", 3 * L * N * ldb)
             g = CgemmDesc()
             g.lda, g.a_plane, g.M, g.K, g.ldb, g.N = lda, plane, M, K, ldb, N
             g.levels = L
@@ -375,13 +398,13 @@ class MixedPlan:
                 self._need(cslot, 2 * L * nM * nlda)
                 _set_modes(g.m_out, [dims[l] for l in rows], [ost[l] for l in rows], "stride_c")
                 _set_modes(g.n_out, [dims[l] for l in nlab], [ost[l] for l in nlab], "stride_c")
-                self.ops.append(("gemm", g, (("ws", aslot), ("ws", "bx"), ("ws", cslot))))
+                self.ops.append(("gemm", g, (aref, bref, ("ws", cslot))))
             else:
                 g.out_kind = 0
                 g.c_plane = 0
                 _set_modes(g.m_out, [dims[l] for l in rows], [ost[l] for l in rows], "stride_c")
                 _set_modes(g.n_out, [dims[l] for l in nlab], [ost[l] for l in nlab], "stride_c")
-                self.ops.append(("gemm", g, (("ws", aslot), ("ws", "bx"), out.ref)))
+                self.ops.append(("gemm", g, (aref, bref, out.ref)))
 
     def _need(self, name, numel):
         self.sizes[name] = max(self.sizes.get(name, 0), numel)
@@ -389,7 +412,7 @@ class MixedPlan:
     def _need_bytes(self, name, nbytes):
         self.byte_sizes[name] = max(self.byte_sizes.get(name, 0), int(nbytes))
 
-    def run(self, x_ptr: int = 0, y_ptr: int = 0):
+    def _build_exec(self):
         for name, n in self.sizes.items():
             self.ws.get(name, n + 64, torch.bfloat16)
         for name, nb in self.byte_sizes.items():
@@ -410,7 +433,21 @@ class MixedPlan:
                     part = ("ws", "tc_partial") if d.partial_bytes else None
                     items.append((_lib.OP_CGEMM, d, tuple(refs) + (part,)))
             self._exec = _NativeOps(items)
+            self._prep_exec = _NativeOps([(_lib.OP_TO_PLANES if kind == "conv" else _lib.OP_EXPAND_B, d,
+                                           (refs[0], None, refs[1])) for kind, d, refs in self.prep])
+
+    def run(self, x_ptr: int = 0, y_ptr: int = 0):
+        self._build_exec()
+        if self.prep and not self.hold:
+            self._prep_exec.run(self.ws, 0, 0)
         self._exec.run(self.ws, x_ptr, y_ptr)
+
+    def prepare(self):
+        """Convert the fixed operands into the plan's own planes now; runs
+        made while ``hold`` is set reuse them."""
+        self._build_exec()
+        if self.prep:
+            self._prep_exec.run(self.ws, 0, 0)
 
 
 # ----------------------------------------------------------------------------
@@ -704,12 +741,14 @@ class DeviceNetwork:
             self.W[nid].copy_(torch.from_numpy(Wn))
         self.ham = hamiltonian
 
-    def _finish(self, cb: "ChainBuilder"):
+    def _finish(self, cb: "ChainBuilder", own_fixed: bool = False):
         """The chain as a tensor-core plan on the reduced-precision paths, else FP64.
         (Small chains stay on the tensor cores too: the FP64 kernel's 64 x 64
         tiles leave most of the GPU idle on skinny shapes such as a leaf's
-        2 x 256 x 1280 step, measured 16x slower than the tensor-core plan.)"""
-        return cb.mixed_plan(self.levels) if self.levels else cb.plan()
+        2 x 256 x 1280 step, measured 16x slower than the tensor-core plan.)
+        ``own_fixed``: the plan keeps its fixed operands converted (see
+        ``MixedPlan``), for the operators of a Krylov solve."""
+        return cb.mixed_plan(self.levels, own_fixed) if self.levels else cb.plan()
 
     # -- shapes ------------------------------------------------------------------
     def nbrs(self, nid):
@@ -767,7 +806,7 @@ class DeviceNetwork:
                 T = cb.contract(T, E, [f"a{k}", f"b{k}"])
         if not rest:
             raise RuntimeError("site without neighbours")
-        p = cb.plan() if fp64 else self._finish(cb)
+        p = cb.plan() if fp64 else self._finish(cb, own_fixed=True)
         self.plans[key] = p
         return p
 
@@ -807,7 +846,7 @@ class DeviceNetwork:
         y = Operand.contiguous(("out",), ["x", "y"], [chi_q, chi_n])
         T = cb.contract(eq, r, ["a"])
         cb.contract(T, en, ["c", "b"], out=y)
-        p = self._finish(cb)
+        p = self._finish(cb, own_fixed=True)
         self.plans[key] = p
         return p
 
@@ -829,6 +868,19 @@ class DeviceNetwork:
         rec(left_out, None)
 
     # -- local evolutions ------------------------------------------------------------
+    @staticmethod
+    def _held(p, fn):
+        """Run ``fn`` with plan ``p``'s fixed operands converted once (its
+        environments and TTNO tensor do not change during one local solve)."""
+        if not isinstance(p, MixedPlan) or not p.prep:
+            return fn()
+        p.prepare()
+        p.hold = True
+        try:
+            return fn()
+        finally:
+            p.hold = False
+
     def evolve_site(self, nid, dt, exp_factor, tol, maxdim, hermitian: bool = True):
         p = self.heff_plan(nid)
 
@@ -836,7 +888,7 @@ class DeviceNetwork:
             p.run(xp, yp)
             self.flops += p.flops
         x = self.t[nid]
-        self.local_exp(x, apply, dt, exp_factor, tol, maxdim, hermitian, out=x)
+        self._held(p, lambda: self.local_exp(x, apply, dt, exp_factor, tol, maxdim, hermitian, out=x))
         self.check_device_status()
 
     def local_exp(self, x, apply, dt, exp_factor, tol, maxdim, hermitian=True, out=None):
@@ -864,7 +916,7 @@ class DeviceNetwork:
         def apply(xp, yp):
             p.run(xp, yp)
             self.flops += p.flops
-        return self.local_exp(r, apply, dt, exp_factor, tol, maxdim, hermitian, out=r)
+        return self._held(p, lambda: self.local_exp(r, apply, dt, exp_factor, tol, maxdim, hermitian, out=r))
 
     # -- QR split and R absorption ---------------------------------------------------
     # Reduced-precision path: tall splits (m >= 2k, k <= ptn_zchol_max_k) try

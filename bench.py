@@ -13,6 +13,7 @@ is 537 MB in complex128), so no L2 flush is needed between steps.
   python bench.py --fidelity-sweeps 20   # mixed vs plain complex128 over 20 sweeps
   python bench.py --impl reference --full-sweep   # one complete CPU oracle sweep
   python bench.py --workload ternary|disorder|gradient   # the other configurations
+  python bench.py --workload matvec --arm 2   # root H_eff matvec + Gram-Schmidt step (ncu target)
 
 Multi-GPU: replicas only (a sweep is sequential); each rank advances its own
 realisation and ``value`` is the sum of sweeps over ranks / max time.
@@ -67,7 +68,9 @@ def parse():
                          "report fidelity and energy error after each")
     ap.add_argument("--full-sweep", action="store_true",
                     help="reference arm: time one complete oracle sweep and compare the per-operation model")
-    ap.add_argument("--workload", default="ttree", choices=["ttree", "ternary", "disorder", "gradient"],
+    ap.add_argument("--entries", type=int, default=1 << 24, help="gram_schmidt: vector length")
+    ap.add_argument("--workload", default="ttree",
+                    choices=["ttree", "ternary", "disorder", "gradient", "matvec", "gram_schmidt"],
                     help="ttree: one-site TDVP on the T-tree (headline); ternary: second-order "
                          "two-site TDVP on the depth-3 ternary tree (40 sites, XXZ) with truncation; "
                          "disorder: many independent random-field realisations (binary tree, 31 sites); "
@@ -620,6 +623,112 @@ def run_fidelity(args):
     return r
 
 
+def run_matvec(args):
+    """The root's H_eff matvec of the T-tree at --chi (arms of --arm sites,
+    canonical form, environments toward the root), and the Gram-Schmidt step
+    of the Krylov loop on vectors of the root's size: achieved algorithmic
+    TFLOP/s of the matvec (8 flop per complex MAC), achieved GB/s of the
+    Gram-Schmidt kernels ((3 nq + 5) vector passes of 16 bytes per entry:
+    three passes over w and nq basis vectors, two of them writing w). The
+    target of the ncu captures in profiles/."""
+    import torch
+    from pytreenet_gb300 import _lib
+    from pytreenet_gb300.engine import DeviceNetwork, _stream_ptr
+    from pytreenet_gb300.workloads import t_tree_state, t_tree_heisenberg
+    lib = _lib.load()
+    st, spec, _ = t_tree_state(arm_len=args.arm, chi=args.chi, seed=0)
+    H, _ = t_tree_heisenberg(st, seed=1000)
+    net = DeviceNetwork(st, H, precision=args.precision)
+    net.canonical_form("root")
+    net.normalise_center()
+    net.init_cache_but_one("root")
+    p = net.heff_plan("root")
+    x = net.t["root"]
+    y = torch.empty_like(x)
+    reps = max(args.steps, 1)
+
+    def timed(fn, n):
+        for _ in range(max(args.warmup, 1)):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(n):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / n
+    torch.cuda.nvtx.range_push("matvec")
+    ms = net._held(p, lambda: timed(lambda: p.run(x.data_ptr(), y.data_ptr()), reps))
+    torch.cuda.nvtx.range_pop()
+    n = x.numel()
+    gs = {}
+    torch.cuda.nvtx.range_push("gram_schmidt")
+    for nq in (4, 8):
+        Q = torch.randn((nq, n), dtype=torch.complex128, device="cuda")
+        w = torch.randn(n, dtype=torch.complex128, device="cuda")
+        h = torch.zeros(2 * nq + 8, dtype=torch.complex128, device="cuda")
+        part = torch.zeros(int(lib.ptn_krylov_partials(n)) * (nq + 2) + 64, dtype=torch.complex128, device="cuda")
+        norms = torch.zeros(4, dtype=torch.float64, device="cuda")
+
+        def step():
+            lib.ptn_krylov_gs_step(Q.data_ptr(), n, nq, w.data_ptr(), n, h.data_ptr(), part.data_ptr(),
+                                   norms.data_ptr(), None, _stream_ptr())
+        t = timed(step, reps)
+        nbytes = (3 * nq + 5) * n * 16
+        gs[nq] = {"ms": t, "bytes": nbytes, "GB_s": nbytes / (t / 1000.0) / 1e9}
+        del Q, w
+    torch.cuda.nvtx.range_pop()
+    peak_t, src_t = _measured_peak("tensor")
+    peak_h, src_h = _measured_peak("hbm")
+    tf = p.flops / (ms / 1000.0) / 1e12
+    return {"metric": f"root H_eff matvec and Gram-Schmidt step at chi={args.chi}", "precision": args.precision,
+            "matvec_ms": ms, "matvec_algorithmic_flops": p.flops, "matvec_tflops": tf,
+            "matvec_frac_of_bf16_sustained": tf / peak_t, "peak_tensor_source": src_t,
+            "gram_schmidt": {str(k): dict(v, frac_of_hbm=v["GB_s"] / peak_h) for k, v in gs.items()},
+            "peak_hbm_source": src_h, "vector_entries": n}
+
+
+def run_gram_schmidt(args):
+    """The Gram-Schmidt step of the Krylov loop (ptn_krylov_gs_step: |w|, two
+    passes of h = Q^H w, w -= Q h, |w|) on --entries complex128 entries with
+    nq = 4 and 8 basis vectors: achieved GB/s against MEASURED_PEAKS.json
+    hbm_gbs, algorithmic bytes (3 nq + 5) x entries x 16 per step."""
+    import torch
+    from pytreenet_gb300 import _lib
+    from pytreenet_gb300.engine import _stream_ptr
+    lib = _lib.load()
+    n = args.entries
+    peak_h, src_h = _measured_peak("hbm")
+    out = {}
+    for nq in (4, 8):
+        Q = torch.randn((nq, n), dtype=torch.complex128, device="cuda")
+        w = torch.randn(n, dtype=torch.complex128, device="cuda")
+        h = torch.zeros(2 * nq + 8, dtype=torch.complex128, device="cuda")
+        part = torch.zeros(int(lib.ptn_krylov_partials(n)) * (nq + 2) + 64, dtype=torch.complex128, device="cuda")
+        norms = torch.zeros(4, dtype=torch.float64, device="cuda")
+
+        def step():
+            lib.ptn_krylov_gs_step(Q.data_ptr(), n, nq, w.data_ptr(), n, h.data_ptr(), part.data_ptr(),
+                                   norms.data_ptr(), None, _stream_ptr())
+        for _ in range(max(args.warmup, 1)):
+            step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(max(args.steps, 1)):
+            step()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / max(args.steps, 1)
+        nbytes = (3 * nq + 5) * n * 16
+        out[str(nq)] = {"ms": ms, "bytes": nbytes, "GB_s": nbytes / (ms / 1000.0) / 1e9,
+                        "frac_of_hbm": nbytes / (ms / 1000.0) / 1e9 / peak_h}
+        del Q, w
+    return {"metric": f"Gram-Schmidt step GB/s ({n} complex128 entries per vector)", "results": out,
+            "peak_source": src_h, "kernels": "gs_pass_kernel (3 passes) + partial-sum finish in the last CTA"}
+
+
 def run_two_site(args):
     """Second-order two-site TDVP on the depth-3 ternary tree (40 sites), XXZ with
     per-edge couplings U[0.5, 1.5], truncation max_bond_dim=chi_max with
@@ -796,7 +905,8 @@ def main():
     if args.impl == "reference" and args.full_sweep:
         print(json.dumps(run_reference_full_sweep(args)), flush=True)
         return
-    single = {"gradient": run_gradient, "disorder": run_disorder, "ternary": run_two_site}
+    single = {"gradient": run_gradient, "disorder": run_disorder, "ternary": run_two_site, "matvec": run_matvec,
+              "gram_schmidt": run_gram_schmidt}
     if args.impl == "gb300" and (args.workload in single or args.breakdown or args.fidelity_sweeps):
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))

@@ -495,11 +495,12 @@ __global__ void __launch_bounds__(ST) hh_persistent_kernel(HPArgs a) {
         }
       }
       __threadfence();
-      if (!abort_s) sc[0] = __ldcg(a.tau + j);
     }
     __syncthreads();
     if (abort_s) break;
     const int64_t len = m - j;
+    // v_j and tau_j in one round trip to L2
+    if (tid == 0) sc[0] = __ldcg(a.tau + j);
     for (int64_t t = tid; t < len; t += ST) vs[t] = __ldcg(a.V + j * m + j + t);
     __syncthreads();
     double2 f = sc[0];
@@ -554,14 +555,41 @@ __global__ void __launch_bounds__(ST) hh_persistent_kernel(HPArgs a) {
       }
     }
     __syncthreads();
+    // H_{c-1}, ..., H_0 in turn; each step stages its reflector in shared
+    // memory, and the next one is fetched while this one is applied
+    constexpr int PF = QR_SMALL_M / ST;                // rows per thread
+    double2 pre[PF];
+    double2 tpre = make_double2(0.0, 0.0);
+    if (c > 0) {
+      const double2* v = a.V + (c - 1) * m;
+#pragma unroll
+      for (int q = 0; q < PF; ++q) {
+        const int64_t t = (c - 1) + tid + (int64_t)q * ST;
+        pre[q] = t < m ? __ldcg(v + t) : make_double2(0.0, 0.0);
+      }
+      tpre = __ldcg(a.tau + (c - 1));
+    }
     for (int64_t j = c - 1; j >= 0; --j) {
-      const double2 t_ = __ldcg(a.tau + j);
-      const double2* v = a.V + j * m;
+#pragma unroll
+      for (int q = 0; q < PF; ++q) {
+        const int64_t t = j + tid + (int64_t)q * ST;
+        if (t < m) vs[t] = pre[q];
+      }
+      const double2 t_ = tpre;
+      if (j > 0) {
+        const double2* vn = a.V + (j - 1) * m;
+#pragma unroll
+        for (int q = 0; q < PF; ++q) {
+          const int64_t t = (j - 1) + tid + (int64_t)q * ST;
+          pre[q] = t < m ? __ldcg(vn + t) : make_double2(0.0, 0.0);
+        }
+        tpre = __ldcg(a.tau + (j - 1));
+      }
       double2 w = make_double2(0.0, 0.0);
-      for (int64_t t = j + tid; t < m; t += ST) w = cfmac(__ldcg(v + t), col[t], w);
+      for (int64_t t = j + tid; t < m; t += ST) w = cfmac(vs[t], col[t], w);
       w = block_sum2_fused<ST>(w, red2);
       const double2 fw = cmul(t_, w);
-      for (int64_t t = j + tid; t < m; t += ST) col[t] = csub(col[t], cmul(__ldcg(v + t), fw));
+      for (int64_t t = j + tid; t < m; t += ST) col[t] = csub(col[t], cmul(vs[t], fw));
       __syncthreads();
     }
     for (int64_t t = tid; t < m; t += ST) a.A[a.rowoff[t] + c * cs] = col[t];

@@ -92,7 +92,7 @@ def test_permute_kernel():
     np.testing.assert_array_equal(dst.cpu().numpy(), ref)
 
 
-def _run_two_site(name, precision="plain"):
+def _run_two_site(name, precision="plain", with_algo=False):
     import pytreenet_gb300 as P
     c = load_case(name)
     st = build_ttn(P.TTNS, c["spec"], c["init"])
@@ -107,7 +107,46 @@ def _run_two_site(name, precision="plain"):
         algo.run_one_time_step()
         zs.append([algo.evaluate_operator({nid: Zm}) for nid, _ in c["spec"]])
     out = {nid: algo.state.get_phys_numpy(nid) for nid, _ in c["spec"]}
+    if with_algo:
+        return c, O.OState(oracle_state(c).tree, out), np.array(zs), algo
     return c, O.OState(oracle_state(c).tree, out), np.array(zs)
+
+
+C2 = "c2_ternary3_xxz_neel_chi16"
+
+
+def _c2_bond_history():
+    import os
+    from golden_util import GOLDEN
+    return [int(x) for x in np.load(os.path.join(GOLDEN, C2 + ".npz"))["bond_history"]]
+
+
+def test_gpu_c2_ternary_depth3_chi16_plain_matches_oracle():
+    """Config 2 at full tree size: second-order two-site TDVP on the ternary
+    tree of depth 3 (40 sites), XXZ, Neel start, max_bond_dim 16, cutoff
+    1e-10, 10 steps of dt = 0.02, complex128 on the GPU against the oracle
+    (tests/golden/make_oracle_fixtures.py; the reference's order cannot run
+    this size): the same bond dimension after every one of the 780 splits,
+    fidelity error below 1e-10 and <Z_i> to 1e-8 after every step."""
+    c, got, zs, algo = _run_two_site(C2, with_algo=True)
+    assert list(algo.bond_dims_history) == _c2_bond_history()
+    fin = oracle_state(c, "final")
+    for nid in fin.tensors:
+        assert fin.tensors[nid].shape == got.tensors[nid].shape, nid
+    one_minus_f, _ = fidelity_and_dist(fin, got)
+    assert one_minus_f < 1e-10
+    assert np.max(np.abs(zs - c["z"])) < 1e-8
+
+
+def test_gpu_c2_ternary_depth3_chi16_mixed_matches_oracle():
+    """The same run with BF16x6 tensor-core contractions (FP64 Krylov, SVD and
+    truncation): bond dimensions as the complex128 oracle's, fidelity error
+    below 1e-11 per unit time (2e-12 over the 0.2 time units), <Z_i> to 2e-6."""
+    c, got, zs, algo = _run_two_site(C2, precision="mixed", with_algo=True)
+    assert list(algo.bond_dims_history) == _c2_bond_history()
+    one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), got)
+    assert one_minus_f < 2e-12
+    assert np.max(np.abs(zs - c["z"])) < 2e-6
 
 
 @pytest.mark.parametrize("name", TWO_SITE_CASES)

@@ -57,8 +57,50 @@ from .engine import CDT, KrylovSolver, Operand, Step, Workspace, check, ttno_sit
 _DESCS: dict = {}
 
 
+# Contraction precision of the adjoint: 0 = complex128 (ptn_zcontract), 3 =
+# BF16x6 tensor-core products with FP32 accumulation (ptn_cgemm_bf16x3). Set
+# by OneSiteTDVPAdjoint around its forward and backward passes; the Krylov
+# exponentials, QR splits and the phi-function integral stay in FP64.
+_LEVELS = {"levels": 0}
+_MIXED_PLANS: dict = {}
+_MIXED_WS: dict = {}
+
+
+class _Ptr:
+    """A plan operand whose device address is set before each run."""
+
+    def __init__(self):
+        self.p = 0
+
+    def data_ptr(self):
+        return self.p
+
+
+def _mixed_contract(a, la, b, lb, lc, klabels, conj_a, conj_b, out, levels):
+    key = (tuple(la), tuple(a.shape), tuple(lb), tuple(b.shape), tuple(lc), tuple(klabels),
+           bool(conj_a), bool(conj_b), levels)
+    ent = _MIXED_PLANS.get(key)
+    if ent is None:
+        dev = str(a.device)
+        ws = _MIXED_WS.setdefault(dev, Workspace(a.device))
+        holder = _Ptr()
+        dims = {**dict(zip(la, a.shape)), **dict(zip(lb, b.shape))}
+        cb = E.ChainBuilder(ws)
+        cb.contract(Operand.contiguous(("in",), list(la), list(a.shape)),
+                    Operand.contiguous(("fixed", holder), list(lb), list(b.shape)), list(klabels),
+                    out=Operand.contiguous(("out",), list(lc), [dims[l] for l in lc]),
+                    conj_a=conj_a, conj_b=conj_b)
+        ent = (cb.mixed_plan(levels), holder, ws)
+        _MIXED_PLANS[key] = ent
+    plan, holder, ws = ent
+    holder.p = b.data_ptr()
+    plan.run(a.data_ptr(), out.data_ptr())
+    return out
+
+
 def _raw_contract(a, la, b, lb, lc, klabels, conj_a=False, conj_b=False, out=None, beta=0.0):
-    """C[lc] = beta C + sum_k op(A)[la] op(B)[lb] in one ``ptn_exec_ops`` call."""
+    """C[lc] = beta C + sum_k op(A)[la] op(B)[lb] in one ``ptn_exec_ops`` call
+    (on the tensor cores when the adjoint runs in mixed precision and beta = 0)."""
     if a.dtype != CDT or b.dtype != CDT:
         raise TypeError("contractions take complex128 tensors")
     if a.dim() != len(la) or b.dim() != len(lb):
@@ -76,6 +118,8 @@ def _raw_contract(a, la, b, lb, lc, klabels, conj_a=False, conj_b=False, out=Non
         out = torch.empty(shape_c, dtype=CDT, device=a.device)
     elif list(out.shape) != shape_c or not out.is_contiguous() or out.dtype != CDT:
         raise ValueError(f"output tensor {tuple(out.shape)} does not match the contraction's {tuple(shape_c)}")
+    if _LEVELS["levels"] and beta == 0.0 and klabels:
+        return _mixed_contract(a, la, b, lb, lc, klabels, conj_a, conj_b, out, _LEVELS["levels"])
     key = (tuple(la), tuple(a.shape), tuple(lb), tuple(b.shape), tuple(lc), tuple(klabels),
            bool(conj_a), bool(conj_b), complex(beta))
     ent = _DESCS.get(key)
@@ -423,6 +467,29 @@ def expect_product(A: dict, nbrs: dict, root: str, ops: dict):
 # ----------------------------------------------------------------------------
 # the differentiable sweep
 # ----------------------------------------------------------------------------
+class _precision:
+    """Contraction precision of the adjoint for the duration of a block (the
+    backward pass runs inside ``expectation_and_gradient``'s block)."""
+
+    def __init__(self, levels):
+        self.levels = levels
+
+    def __enter__(self):
+        self.saved = _LEVELS["levels"]
+        _LEVELS["levels"] = self.levels
+
+    def __exit__(self, *a):
+        _LEVELS["levels"] = self.saved
+        if self.levels and a[0] is None:
+            # a bounded wait that ran out inside a tensor-core product
+            for ws in _MIXED_WS.values():
+                st = ws.bufs.get("tc_status")
+                if st is not None and int(st.item()) != 0:
+                    code = int(st.item())
+                    st.zero_()
+                    raise _lib.PtnError(code, "tensor-core contraction in the adjoint")
+
+
 class OneSiteTDVPAdjoint:
     """One-site TDVP (``FirstOrderOneSiteTDVP``, or ``SecondOrderOneSiteTDVP``
     with ``second_order``) as a differentiable
@@ -436,8 +503,15 @@ class OneSiteTDVPAdjoint:
 
     def __init__(self, initial_state, hamiltonian, time_step_size: float, num_steps: int,
                  krylov_tol: float = 1e-12, max_krylov_dim=None, use_checkpoint: bool = True,
-                 normalise: bool = False, second_order: bool = False):
+                 normalise: bool = False, second_order: bool = False, precision: str = "plain"):
+        """``precision``: "plain" (complex128 contractions) or "mixed" (every
+        contraction of the forward and backward passes as BF16x6 tensor-core
+        products with FP32 accumulation; Krylov vectors, QR, the small
+        exponentials and the phi-function integral stay FP64)."""
         from .tdvp import leaf_to_root_update_path
+        if precision not in ("plain", "mixed"):
+            raise ValueError("precision must be 'plain' or 'mixed'")
+        self.levels = 3 if precision == "mixed" else 0
         if time_step_size <= 0 or num_steps <= 0:
             raise ValueError("time step and number of steps must be positive")
         initial_state._finalise()
@@ -583,11 +657,12 @@ class OneSiteTDVPAdjoint:
     def evolve(self, A: dict, W: dict) -> dict:
         flat = tuple(A[nid] for nid in self.order)
         Wl = tuple(W[nid] for nid in self.order)
-        for _ in range(self.num_steps):
-            if self.use_checkpoint and torch.is_grad_enabled():
-                flat = checkpoint(self._step_flat, *flat, *Wl, use_reentrant=False)
-            else:
-                flat = self._step_flat(*flat, *Wl)
+        with _precision(self.levels):
+            for _ in range(self.num_steps):
+                if self.use_checkpoint and torch.is_grad_enabled():
+                    flat = checkpoint(self._step_flat, *flat, *Wl, use_reentrant=False)
+                else:
+                    flat = self._step_flat(*flat, *Wl)
         return dict(zip(self.order, flat))
 
     def expectation_and_gradient(self, ops: dict, W: dict | None = None, wrt_state: bool = False):
@@ -597,7 +672,7 @@ class OneSiteTDVPAdjoint:
         W = self.W0 if W is None else W
         Wl = {nid: W[nid].detach().clone().requires_grad_(True) for nid in self.order}
         A = {nid: self.A0[nid].detach().clone().requires_grad_(wrt_state) for nid in self.order}
-        with torch.enable_grad():
+        with torch.enable_grad(), _precision(self.levels):
             At = self.evolve(A, Wl)
             val = expect_product(At, self.nbrs, self.root, ops)
             loss = val.real.sum()

@@ -240,3 +240,18 @@ def test_second_order_tdvp_gradient_matches_oracle_and_fd(fake):
                    for j in range(theta.size)])
     assert np.linalg.norm(grad) > 1e-4
     assert np.linalg.norm(grad - fd) < 1e-6 * np.linalg.norm(grad)
+
+
+def test_mixed_precision_adjoint_close_to_fp64(fake):
+    """The adjoint with every contraction (forward and backward) as BF16-split
+    tensor-core products, the stand-in accumulating in FP32: value and coupling
+    gradient within the FP32 level of the complex128 adjoint's."""
+    from pytreenet_gb300.adjoint import OneSiteTDVPAdjoint, coupling_gradient
+    st, spec, tensors, theta, ham = _seven_site_problem()
+    ops = {"s0": np.diag([1.0, -1.0]).astype(complex)}
+    adj = OneSiteTDVPAdjoint(st, ham(theta), 0.05, 3, krylov_tol=1e-14)
+    val, grad = coupling_gradient(adj, ham, theta, ops)
+    adj_m = OneSiteTDVPAdjoint(st, ham(theta), 0.05, 3, krylov_tol=1e-14, precision="mixed")
+    val_m, grad_m = coupling_gradient(adj_m, ham, theta, ops)
+    assert abs(val_m - val) < 1e-6
+    assert 0 < np.linalg.norm(grad_m - grad) < 1e-5 * np.linalg.norm(grad)

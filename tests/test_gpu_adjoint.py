@@ -125,3 +125,11 @@ def test_gpu_gradient_31_sites_chi16_matches_central_differences():
                    for j in idx])
     assert np.linalg.norm(grad) > 1e-3
     assert np.max(np.abs(grad[idx] - fd)) < 1e-6 * np.linalg.norm(grad), (grad[idx], fd)
+    # the mixed-precision adjoint (BF16x6 tensor-core contractions forward and
+    # backward; FP64 Krylov, QR and phi-integral) against the same FP64
+    # central differences
+    adj_m = OneSiteTDVPAdjoint(st, ham(theta), dt, steps, krylov_tol=tol, normalise=True, precision="mixed")
+    val_m, grad_m = coupling_gradient(adj_m, ham, theta, ops)
+    assert abs(val_m - val) < 1e-7
+    assert np.max(np.abs(grad_m[idx] - fd)) < 1e-6 * np.linalg.norm(grad), (grad_m[idx], fd)
+    assert np.linalg.norm(grad_m - grad) < 1e-6 * np.linalg.norm(grad)

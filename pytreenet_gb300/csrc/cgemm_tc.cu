@@ -15,7 +15,8 @@
 // Operands (both K-major, K contiguous):
 //   A: 2L bf16 planes (Ar_0, Ai_0, Ar_1, Ai_1, ...), each [M][lda]
 //   Bx: bf16 [level][block(-Bi, Br, Bi)][N][ldb]
-// Tiles are staged by TMA (64-byte swizzle, K=32 per stage) through an mbarrier ring;
+// Tiles are staged by TMA (32-byte swizzle, K=16 per stage, up to 8 stages)
+// through an mbarrier ring; two stages make one 32-wide accumulation round;
 // one warp issues TMA, one warp issues MMA and owns the TMEM allocation, four
 // warps run the epilogue (TMEM -> registers -> global, strided by output mode
 // tables so the result lands directly in the layout the next step reads).
@@ -31,18 +32,23 @@ namespace {
 
 constexpr int MT = 128;         // rows of C per CTA
 constexpr int NT = 64;          // complex columns of C per CTA (MMA N = 2*NT)
-constexpr int KT = 32;          // K per stage (one 64-byte swizzle row)
-constexpr int A_PLANE_BYTES = MT * 64;             // 8 KB
-constexpr int B_BLOCK_BYTES = NT * 64;             // 4 KB
+constexpr int KT = 32;          // K per accumulation round (the unit of the K split)
+constexpr int KS = 16;          // K per shared-memory stage (one 32-byte swizzle row, one MMA K)
+constexpr int A_PLANE_BYTES = MT * 2 * KS;         // 4 KB
+constexpr int B_BLOCK_BYTES = NT * 2 * KS;         // 2 KB
 constexpr int SMEM_LIMIT = 227 * 1024;
 constexpr int THREADS = 192;
 
+// Stages of KS: as many as fit (at most 8). Two stages make one accumulation
+// round, so the TMEM partial sums still cover 32 K values; the deeper ring
+// hides the TMA latency that two 84 KB stages of 32 K values left exposed
+// (ncu at the chi=128 root: tensor pipe 39 % active, long-scoreboard stalls).
 template <int L>
 struct Cfg {
   static constexpr int A_STAGE = 2 * L * A_PLANE_BYTES;
   static constexpr int B_STAGE = 3 * L * B_BLOCK_BYTES;
   static constexpr int STAGE = A_STAGE + B_STAGE;
-  static constexpr int STAGES = (SMEM_LIMIT - 2048) / STAGE > 4 ? 4 : (SMEM_LIMIT - 2048) / STAGE;
+  static constexpr int STAGES = (SMEM_LIMIT - 2048) / STAGE > 8 ? 8 : (SMEM_LIMIT - 2048) / STAGE;
   static constexpr int SMEM = STAGES * STAGE + 1024;
 };
 constexpr long long WAIT_CYCLES = 4000000000LL;    // ~2 s at 2 GHz
@@ -112,9 +118,11 @@ __global__ void __launch_bounds__(THREADS, 1)
   const int split = (int)(blockIdx.x / g.tiles);
   const int64_t tm = tile / g.tiles_n, tn = tile - tm * g.tiles_n;
   const int64_t m0 = tm * MT, n0 = tn * NT;
-  const int kt_all = (int)((g.K + KT - 1) / KT);
-  const int kt0 = split * g.ksplit;
-  const int ktiles = min(kt_all, kt0 + g.ksplit) - kt0;    // K tiles of this CTA's range
+  // stages of KS K values; the split ranges are whole accumulation rounds (KT)
+  const int kt_all = (int)((g.K + KS - 1) / KS);
+  const int kt0 = split * g.ksplit * (KT / KS);
+  const int ktiles = min(kt_all, kt0 + g.ksplit * (KT / KS)) - kt0;   // stages of this CTA's range
+  const int nacc = (ktiles + 1) / 2;                                   // accumulation rounds
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -159,7 +167,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
         uint8_t* st = smem + s * STAGE_BYTES;
         tc::mbar_arrive_expect_tx(&full_bar[s], STAGE_BYTES);
-        const int kx = (kt0 + kt) * KT;
+        const int kx = (kt0 + kt) * KS;
         for (int p = 0; p < 2 * L; ++p)
           tc::tma_load_3d(st + p * A_PLANE_BYTES, &tmA, &full_bar[s], kx, (int)m0, p);
         for (int b = 0; b < 3 * L; ++b)
@@ -188,8 +196,11 @@ __global__ void __launch_bounds__(THREADS, 1)
       bool aborted = false, any_mma = false;
       for (int kt = 0; kt < ktiles; ++kt) {
         const int s = kt % STAGES;
-        const int b = kt & 1, ub = kt >> 1;
-        if (ub > 0 && !tc::mbar_wait_abortable(&tempty_bar[b], (ub - 1) & 1, WAIT_CYCLES, vstatus)) {
+        const int a = kt >> 1;                  // accumulation round: stages 2a, 2a + 1
+        const int b = a & 1, ub = a >> 1;
+        const bool round_start = (kt & 1) == 0;
+        if (round_start && ub > 0 &&
+            !tc::mbar_wait_abortable(&tempty_bar[b], (ub - 1) & 1, WAIT_CYCLES, vstatus)) {
           atomicExch(g.status, PTN_ERR_TIMEOUT);
           aborted = true;
           break;
@@ -204,30 +215,26 @@ __global__ void __launch_bounds__(THREADS, 1)
         const uint32_t sa = tc::smem_u32(smem + s * STAGE_BYTES);
         const uint32_t sb = sa + A_STAGE_BYTES;
         const uint32_t acc = tmem + (uint32_t)b * ACC_COLS;
-        bool first = true;
+        bool first = round_start;
         // smallest split products first, the leading (0, 0) product last
 #pragma unroll
         for (int lvl = L - 1; lvl >= 0; --lvl) {
 #pragma unroll
           for (int i = 0; i <= lvl; ++i) {
             const int j = lvl - i;
-#pragma unroll
-            for (int kk = 0; kk < KT / 16; ++kk) {
-              const uint32_t ko = kk * 32;
-              // A planes: 2i = Re level i, 2i+1 = Im level i.
-              // B level j at sb + 3j*B_BLOCK: window [Br; Bi] at +1 block, [-Bi; Br] at +0.
-              const uint64_t ar = tc::sdesc_sw64(sa + (2 * i) * A_PLANE_BYTES + ko);
-              const uint64_t ai = tc::sdesc_sw64(sa + (2 * i + 1) * A_PLANE_BYTES + ko);
-              const uint64_t bt = tc::sdesc_sw64(sb + (3 * j + 1) * B_BLOCK_BYTES + ko);
-              const uint64_t bb = tc::sdesc_sw64(sb + (3 * j) * B_BLOCK_BYTES + ko);
-              tc::mma_bf16(acc, ar, bt, idesc, first ? 0u : 1u);
-              tc::mma_bf16(acc, ai, bb, idesc, 1u);
-              first = false;
-            }
+            // A planes: 2i = Re level i, 2i+1 = Im level i.
+            // B level j at sb + 3j*B_BLOCK: window [Br; Bi] at +1 block, [-Bi; Br] at +0.
+            const uint64_t ar = tc::sdesc_sw32(sa + (2 * i) * A_PLANE_BYTES);
+            const uint64_t ai = tc::sdesc_sw32(sa + (2 * i + 1) * A_PLANE_BYTES);
+            const uint64_t bt = tc::sdesc_sw32(sb + (3 * j + 1) * B_BLOCK_BYTES);
+            const uint64_t bb = tc::sdesc_sw32(sb + (3 * j) * B_BLOCK_BYTES);
+            tc::mma_bf16(acc, ar, bt, idesc, first ? 0u : 1u);
+            tc::mma_bf16(acc, ai, bb, idesc, 1u);
+            first = false;
           }
         }
         tc::mma_commit(&empty_bar[s]);
-        tc::mma_commit(&tfull_bar[b]);
+        if (!round_start || kt == ktiles - 1) tc::mma_commit(&tfull_bar[b]);
       }
       if (aborted && any_mma) {
         // every MMA this thread issued completes before TMEM is freed
@@ -248,21 +255,24 @@ __global__ void __launch_bounds__(THREADS, 1)
       acc_im[i] = 0.f;
     }
     bool ok = true;
-    for (int kt = 0; kt < ktiles && ok; ++kt) {
-      const int b = kt & 1;
-      ok = tc::mbar_wait_abortable(&tfull_bar[b], (kt >> 1) & 1, WAIT_CYCLES, vstatus);
+    for (int a = 0; a < nacc && ok; ++a) {
+      const int b = a & 1;
+      ok = tc::mbar_wait_abortable(&tfull_bar[b], (a >> 1) & 1, WAIT_CYCLES, vstatus);
       if (!ok) break;
       tc::fence_after();
       const uint32_t tb = tmem + lane_off + (uint32_t)b * ACC_COLS;
+      // two loads in flight per wait (re and im of 16 columns)
 #pragma unroll
       for (int j0 = 0; j0 < NT; j0 += 16) {
-        float v[16];
-        tc::tmem_ld16(tb + (uint32_t)j0, v);
+        uint32_t vr[16], vi[16];
+        tc::tmem_ld16_nowait(tb + (uint32_t)j0, vr);
+        tc::tmem_ld16_nowait(tb + (uint32_t)(NT + j0), vi);
+        tc::tmem_wait_ld();
 #pragma unroll
-        for (int i = 0; i < 16; ++i) acc_re[j0 + i] += v[i];
-        tc::tmem_ld16(tb + (uint32_t)(NT + j0), v);
-#pragma unroll
-        for (int i = 0; i < 16; ++i) acc_im[j0 + i] += v[i];
+        for (int i = 0; i < 16; ++i) {
+          acc_re[j0 + i] += __uint_as_float(vr[i]);
+          acc_im[j0 + i] += __uint_as_float(vi[i]);
+        }
       }
       tc::fence_before();
       __syncwarp();
@@ -339,7 +349,7 @@ int make_map_3d(CUtensorMap* map, const void* base, uint64_t d0, uint64_t d1, ui
   if (!enc) return PTN_ERR_LAUNCH;
   CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims,
                                       strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                      CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                      CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? PTN_OK : PTN_ERR_ARG;
 }
@@ -611,10 +621,10 @@ extern "C" int ptn_cgemm_bf16x3(const ptn_cgemm_desc* d, void* stream) {
   CUtensorMap ta, tb;
   const int L = d->levels;
   if (make_map_3d(&ta, d->A, (uint64_t)d->K, (uint64_t)d->M, 2 * L, (uint64_t)d->lda * 2,
-                  (uint64_t)d->a_plane * 2, KT, MT))
+                  (uint64_t)d->a_plane * 2, KS, MT))
     return PTN_ERR_ARG;
   if (make_map_3d(&tb, d->Bx, (uint64_t)d->K, (uint64_t)d->N, 3 * L, (uint64_t)d->ldb * 2,
-                  (uint64_t)d->N * (uint64_t)d->ldb * 2, KT, NT))
+                  (uint64_t)d->N * (uint64_t)d->ldb * 2, KS, NT))
     return PTN_ERR_ARG;
   const int64_t tm = (d->M + MT - 1) / MT, tn = (d->N + NT - 1) / NT;
   g.tiles_n = tn;

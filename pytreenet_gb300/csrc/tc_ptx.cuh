@@ -154,6 +154,36 @@ __device__ __forceinline__ uint64_t sdesc_sw64(uint32_t saddr) {
   return d;
 }
 
+// Shared-memory matrix descriptor: K-major, SWIZZLE_32B (rows of 16 bf16,
+// 8-row atoms of 256 B).
+__device__ __forceinline__ uint64_t sdesc_sw32(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1u << 16;
+  d |= (uint64_t)(256u >> 4) << 32;
+  d |= (uint64_t)1u << 46;
+  d |= (uint64_t)6u << 61;                        // layout: SWIZZLE_32B
+  return d;
+}
+
+// Byte offset of element (row, k) in a K-major SW32 tile of 16-wide rows:
+// the 16-byte half of the row is flipped by bit 2 of the row index.
+__host__ __device__ __forceinline__ uint32_t sw32_offset(uint32_t row, uint32_t k) {
+  return row * 32u + ((((k >> 3) ^ ((row >> 2) & 1u)) & 1u) << 4) + ((k & 7u) << 1);
+}
+
+// Issue a 32x32b.x16 TMEM load without waiting; tmem_wait_ld completes all
+// loads issued so far.
+__device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
 // Byte offset of element (row, k) in a K-major SW64 tile of 32-wide rows.
 __host__ __device__ __forceinline__ uint32_t sw64_offset(uint32_t row, uint32_t k) {
   return row * 64u + ((((k >> 3) ^ ((row >> 1) & 3u)) & 3u) << 4) + ((k & 7u) << 1);

@@ -24,10 +24,12 @@ __global__ void __launch_bounds__(128) tc_selftest_kernel(const uint16_t* __rest
   __shared__ uint64_t bar;
   __shared__ uint32_t tmem_base;
   const int tid = threadIdx.x;
-  // K = 64: one SW128 tile, or two SW64 tiles of 32 (second at +8 KB)
+  // K = 64: one SW128 tile (sw64 = 0), two SW64 tiles of 32 (sw64 = 1,
+  // second at +8 KB), or four SW32 tiles of 16 (sw64 = 2, at +4 KB each)
   for (int e = tid; e < 128 * 64; e += 128) {
     const int r = e >> 6, k = e & 63;
-    const uint32_t off = sw64 ? (uint32_t)(k >> 5) * 8192u + tc::sw64_offset(r, k & 31) : tc::sw128_offset(r, k);
+    const uint32_t off = sw64 == 2 ? (uint32_t)(k >> 4) * 4096u + tc::sw32_offset(r, k & 15)
+                         : sw64 ? (uint32_t)(k >> 5) * 8192u + tc::sw64_offset(r, k & 31) : tc::sw128_offset(r, k);
     *reinterpret_cast<uint16_t*>(sA + off) = A[e];
     *reinterpret_cast<uint16_t*>(sB + off) = B[e];
   }
@@ -48,9 +50,12 @@ __global__ void __launch_bounds__(128) tc_selftest_kernel(const uint16_t* __rest
     const uint32_t idesc = tc::idesc_bf16(128, 128);
 #pragma unroll
     for (int kk = 0; kk < 4; ++kk) {
-      const uint32_t o = sw64 ? (uint32_t)(kk >> 1) * 8192u + (kk & 1) * 32u : kk * 32u;
-      const uint64_t ad = sw64 ? tc::sdesc_sw64(tc::smem_u32(sA) + o) : tc::sdesc_sw128(tc::smem_u32(sA) + o);
-      const uint64_t bd = sw64 ? tc::sdesc_sw64(tc::smem_u32(sB) + o) : tc::sdesc_sw128(tc::smem_u32(sB) + o);
+      const uint32_t o = sw64 == 2 ? (uint32_t)kk * 4096u
+                         : sw64 ? (uint32_t)(kk >> 1) * 8192u + (kk & 1) * 32u : kk * 32u;
+      const uint64_t ad = sw64 == 2 ? tc::sdesc_sw32(tc::smem_u32(sA) + o)
+                          : sw64 ? tc::sdesc_sw64(tc::smem_u32(sA) + o) : tc::sdesc_sw128(tc::smem_u32(sA) + o);
+      const uint64_t bd = sw64 == 2 ? tc::sdesc_sw32(tc::smem_u32(sB) + o)
+                          : sw64 ? tc::sdesc_sw64(tc::smem_u32(sB) + o) : tc::sdesc_sw128(tc::smem_u32(sB) + o);
       tc::mma_bf16(tmem, ad, bd, idesc, kk > 0 ? 1u : 0u);
     }
     tc::mma_commit(&bar);

@@ -43,7 +43,7 @@ def selftest_lib(lib):
     return t
 
 
-@pytest.mark.parametrize("sw64", [0, 1])
+@pytest.mark.parametrize("sw64", [0, 1, 2])
 def test_tcgen05_descriptor_selftest(selftest_lib, sw64):
     from pytreenet_gb300.engine import _stream_ptr
     A = _bf16_round(RNG.normal(size=(128, 64)))

@@ -282,6 +282,23 @@ def coupling_matrix(Tv, beta_v, Tw, beta_w, z):
     return beta_v * beta_w * (S.conj() * s.conj()[None, :]) @ K @ (P * p[None, :]).T
 
 
+# Deepest Krylov basis of a solve whose operator is a reduced-precision product
+# (a guard: the Lanczos stop triggers at the FP64 path's depths, 7-12 here).
+MIXED_MAX_KRYLOV_DIM = 96
+
+
+def _krylov_mode(maxdim):
+    """With tensor-core contractions the Krylov exponential projects on the
+    Lanczos tridiagonal (alpha_j, beta_j), as the engine's mixed path does: the
+    full symmetrised Arnoldi projection turns the operator's rounding far from
+    the diagonal into a coupling that keeps its adaptive stop from ever
+    triggering. Returns (tridiagonal, max Krylov dimension)."""
+    if not _LEVELS["levels"]:
+        return False, maxdim
+    cap = MIXED_MAX_KRYLOV_DIM if maxdim is None else min(int(maxdim), MIXED_MAX_KRYLOV_DIM)
+    return True, cap
+
+
 class _KrylovExp(torch.autograd.Function):
     @staticmethod
     def forward(ctx, x, op, dt, c, tol, maxdim, *params):
@@ -290,8 +307,9 @@ class _KrylovExp(torch.autograd.Function):
         x = x.contiguous()
         y = torch.empty_like(x)
         bx = {}
+        tri, maxdim = _krylov_mode(maxdim)
         _solver(x.device).expm(x.detach(), _tensor_apply(op, [p.detach() for p in params], x.shape),
-                               dt, c, tol, maxdim, out=y, basis=bx)
+                               dt, c, tol, maxdim, out=y, basis=bx, tridiagonal=tri)
         # the basis of x is kept for the backward pass (under checkpointing it
         # lives only while its step is being differentiated)
         ctx.save_for_backward(x, bx["Q"] if bx["m"] else x.new_zeros(0), *params)
@@ -309,7 +327,8 @@ class _KrylovExp(torch.autograd.Function):
         bx = {"Q": Qx, "T": Tx, "beta0": beta_x, "m": mx}
         bw = {}
         gx = torch.empty_like(x)
-        solver.expm(gy, ap, dt, -c, tol, maxdim, out=gx, basis=bw)
+        tri, maxdim = _krylov_mode(maxdim)
+        solver.expm(gy, ap, dt, -c, tol, maxdim, out=gx, basis=bw, tridiagonal=tri)
         grads = [None] * len(params)
         need = list(ctx.needs_input_grad[6:])
         if any(need) and bx["m"] > 0 and bw["m"] > 0:

@@ -12,7 +12,7 @@ is 537 MB in complex128), so no L2 flush is needed between steps.
   python bench.py --breakdown            # time per engine operation of one sweep
   python bench.py --fidelity-sweeps 20   # mixed vs plain complex128 over 20 sweeps
   python bench.py --impl reference --full-sweep   # one complete CPU oracle sweep
-  python bench.py --workload ternary|disorder|gradient   # the other configurations
+  python bench.py --workload c1|ternary|disorder|gradient   # the other configurations
   python bench.py --workload matvec --arm 2   # root H_eff matvec + Gram-Schmidt step (ncu target)
 
 Multi-GPU: replicas only (a sweep is sequential); each rank advances its own
@@ -70,8 +70,9 @@ def parse():
                     help="reference arm: time one complete oracle sweep and compare the per-operation model")
     ap.add_argument("--entries", type=int, default=1 << 24, help="gram_schmidt: vector length")
     ap.add_argument("--workload", default="ttree",
-                    choices=["ttree", "ternary", "disorder", "gradient", "matvec", "gram_schmidt"],
-                    help="ttree: one-site TDVP on the T-tree (headline); ternary: second-order "
+                    choices=["ttree", "c1", "ternary", "disorder", "gradient", "matvec", "gram_schmidt"],
+                    help="ttree: one-site TDVP on the T-tree (headline); c1: one-site TDVP on the "
+                         "15-node binary tree with <Z_i> at every site each step; ternary: second-order "
                          "two-site TDVP on the depth-3 ternary tree (40 sites, XXZ) with truncation; "
                          "disorder: many independent random-field realisations (binary tree, 31 sites); "
                          "gradient: d<Z_root>/d(g_i, J) after 30 one-site TDVP steps by the adjoint "
@@ -729,6 +730,105 @@ def run_gram_schmidt(args):
             "peak_source": src_h, "kernels": "gs_pass_kernel (3 passes) + partial-sum finish in the last CTA"}
 
 
+def run_c1(args):
+    """First-order one-site TDVP (Krylov) on the 15-node binary tree, TFIM J=1,
+    g=0.5, seeded random product state padded to chi=8, dt=0.01, with <Z_i> at
+    all 15 sites after every step. One step = run_one_time_step plus the 15
+    values read back to the host (``evaluate_operator_values``: one pass over
+    the tree). Also timed: the 15 values one operator at a time (the
+    reference's pattern), a whole 50-step ``run`` through the public API from
+    host tensors, and the NumPy oracle doing the same steps on the host."""
+    import torch
+    import pytreenet_gb300 as P
+    from pytreenet_gb300 import _lib
+    from pytreenet_gb300.engine import ttno_site_tensors
+    from pytreenet_gb300.workloads import binary_tfim_product_state
+    lib = _lib.load()
+    Z = np.diag([1.0, -1.0]).astype(complex)
+    dt, total = 0.01, 50
+
+    def make(seed=0):
+        st, H, spec, tensors = binary_tfim_product_state(n=15, chi=8, seed=seed)
+        ids = [nid for nid, _ in spec]
+        ops = {f"Z_{nid}": P.TensorProduct({nid: Z}) for nid in ids}
+        algo = P.FirstOrderOneSiteTDVP(st, H, dt, dt * total, ops,
+                                       config=P.TDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV),
+                                       solver_options={"krylov_tol": args.tol})
+        return algo, st, H, spec, tensors, ids
+    algo, st, H, spec, tensors, ids = make()
+
+    def step():
+        algo.run_one_time_step()
+        return algo.evaluate_operator_values()
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    l0 = lib.ptn_launch_counter() + algo.net.graph_launches
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(torch.cuda.current_device()) as clk:
+        start.record()
+        for _ in range(args.steps):
+            step()
+        stop.record()
+        torch.cuda.synchronize()
+    ms = start.elapsed_time(stop) / args.steps
+    launches = int(lib.ptn_launch_counter() + algo.net.graph_launches - l0) // args.steps
+
+    def timed(fn, reps=20):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return 1000.0 * (time.perf_counter() - t0) / reps
+    obs_pass = timed(algo.evaluate_operator_values)
+    obs_each = timed(lambda: [algo.net.expect_local({nid: Z}) for nid in ids])
+    vals = np.array(algo.evaluate_operator_values())
+    each = np.array([algo.net.expect_local({nid: Z}) for nid in ids])
+    # the public API end to end: a fresh driver on host tensors, 50 steps with
+    # the measurements, results on the host
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    a2 = make()[0]
+    res = a2.run(pgbar=False)
+    torch.cuda.synchronize()
+    run_s = time.perf_counter() - t0
+    line = {"metric": "one-site TDVP steps/sec with <Z_i> at all 15 sites per step (15-node binary tree, TFIM, chi=8)",
+            "value": 1000.0 / ms, "unit": "steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c128 (fp64)", "data": "synthetic",
+            "config": {"workload": "binary tree 15 sites, TFIM J=1 g=0.5, random product state padded to chi=8, "
+                                   f"first-order 1TDVP, dt={dt}, krylov_tol={args.tol}, <Z_i> every step",
+                       "l2": "state fits in L2 (launch-bound workload); no flush"},
+            "gpu_launches": launches, "clocks": clk.summary(),
+            "observables": {"one_pass_ms": obs_pass, "per_operator_ms": obs_each,
+                            "max_abs_difference": float(np.max(np.abs(vals - each)))},
+            "e2e": {"value": total / run_s, "unit": "steps/s", "what": f"{total}-step run() from host tensors "
+                    "with <Z_i> recorded every step, driver construction included",
+                    "h2d_bytes_per_step": int(sum(t.size for t in tensors.values()) * 16 // total),
+                    "d2h_bytes_per_step": 16 * len(ids), "seconds": run_s, "z_final": res[-1].real.tolist()}}
+    if not args.no_cpu_baseline:
+        import oracle as O
+        tree = O.OTree()
+        for nid, p in spec:
+            tree.add_root(nid) if p is None else tree.add_child(nid, p)
+        _, st2, H2, _, tensors2, _ = make()
+        W = ttno_site_tensors(st2, H2)
+        ora = O.FirstOrderOneSiteTDVPOracle(O.OState(tree, {k: np.array(v) for k, v in tensors2.items()}), W, dt,
+                                            krylov_tol=args.tol)
+        n_cpu = 10
+        t0 = time.perf_counter()
+        for _ in range(n_cpu):
+            ora.run_one_time_step()
+            [O.expect_product(ora.state, {nid: Z}) for nid in ids]
+        cpu = (time.perf_counter() - t0) / n_cpu
+        line["cpu_baseline"] = {"value": 1.0 / cpu, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"NumPy oracle: {n_cpu} steps of the same run, each with the 15 "
+                                          "<Z_i> by a full contraction per operator"}
+    return line
+
+
 def run_two_site(args):
     """Second-order two-site TDVP on the depth-3 ternary tree (40 sites), XXZ with
     per-edge couplings U[0.5, 1.5], truncation max_bond_dim=chi_max with
@@ -905,7 +1005,7 @@ def main():
     if args.impl == "reference" and args.full_sweep:
         print(json.dumps(run_reference_full_sweep(args)), flush=True)
         return
-    single = {"gradient": run_gradient, "disorder": run_disorder, "ternary": run_two_site, "matvec": run_matvec,
+    single = {"c1": run_c1, "gradient": run_gradient, "disorder": run_disorder, "ternary": run_two_site, "matvec": run_matvec,
               "gram_schmidt": run_gram_schmidt}
     if args.impl == "gb300" and (args.workload in single or args.breakdown or args.fidelity_sweeps):
         import torch

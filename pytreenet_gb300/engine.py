@@ -719,6 +719,9 @@ class DeviceNetwork:
         self.householder_count = 0     # splits done by Householder QR
         self.qr_rows_skipped = 0       # zero trailing rows the Householder QRs skipped
         self.graph_launches = 0
+        self._obs_sig = None           # tensors the cached observable plans were built on
+        self._obs_plans: dict = {}
+        self._ttno_nets: dict = {}     # id(TTNO) -> (TTNO, tensor signature, network)
         lib = _lib.load()
         kmax, wmax = 1, 1
         for nid in state._order:
@@ -1657,9 +1660,20 @@ class DeviceNetwork:
         ``contractions/state_operator_contraction.py:26-74``): a second network
         over the same device tensors (no copies) holds O and its own
         environments; all of them point to the root, whose H_eff applied to the
-        root tensor is contracted with its conjugate."""
-        other = DeviceNetwork(self.state, ttno, device=self.device,
-                              precision="plain")
+        root tensor is contracted with its conjugate. That network (its plans and
+        environment buffers) is kept per operator while the site tensors keep
+        their shapes and storage; each call copies the operator's tensors in and
+        recomputes the environments."""
+        sig = tuple((nid, tuple(t.shape), t.data_ptr()) for nid, t in self.t.items())
+        ent = self._ttno_nets.get(id(ttno))
+        if ent is not None and ent[0] is ttno and ent[1] == sig:
+            other = ent[2]
+            other.refresh_hamiltonian(ttno)
+        else:
+            if len(self._ttno_nets) >= 8:
+                self._ttno_nets.pop(next(iter(self._ttno_nets)))
+            other = DeviceNetwork(self.state, ttno, device=self.device, precision="plain")
+            self._ttno_nets[id(ttno)] = (ttno, sig, other)
         root = self.state.root_id
         other.init_cache_but_one(root)
         x = self.t[root]
@@ -1675,43 +1689,188 @@ class DeviceNetwork:
 
     def expect_local(self, ops: dict) -> complex:
         """<psi| prod_i O_i |psi> for single-site operators
-        (``TTNS.tensor_product_expectation_value``, ``ttns/ttns.py:240-264``)."""
-        st = self.state
-        cache = {}
+        (``TTNS.tensor_product_expectation_value``, ``ttns/ttns.py:240-264``);
+        ``{}`` gives <psi|psi>. One entry of ``expect_many``."""
+        return complex(self.expect_many([ops])[0])
 
-        def rec(nid, toward):
+    def expect_many(self, ops_list) -> np.ndarray:
+        """<psi| prod_i O_i |psi> for a list of products of one-site operators
+        (each a dict node -> d x d matrix acting on the physical leg; ``{}`` is
+        <psi|psi>), in one pass over the tree: one launch sequence, one copy of
+        the operator matrices to the device and one copy of the values back.
+
+        The reference evaluates each product separately as a deep copy, an
+        operator application and a contraction of the whole network
+        (``ttns/ttns.py:240-264``, ``contractions/state_state_contraction.py:29-66``,
+        called per operator by ``time_evolution/ttn_time_evolution.py:181-197``).
+        Here the pass computes norm environments N(u -> v) (the part of the
+        tree on u's side of the edge contracted with its conjugate; legs
+        (ket, bra)) toward the root for every edge and away from it on the
+        paths to the operators' nodes. A one-site product then needs only the
+        reduced density matrix of its node, rho[s, t] = psi[.., s] conj(psi[.., t])
+        with every neighbour's environment, and Tr(O rho); rho is computed once
+        per node however many operators act there. A product on several nodes
+        contracts only the subtrees that hold its factors and takes the
+        environments for the rest. The values are the reference's up to the
+        order of the floating-point sums.
+
+        The plan is cached per operator layout (the nodes of each product) and
+        kept while no site tensor changes shape or storage, so repeated
+        measurements (the ``run`` loop) reuse it and only copy the matrices."""
+        ops_list = [dict(op) for op in ops_list]
+        if not ops_list:
+            return np.zeros((0,), dtype=np.complex128)
+        mats = []
+        for op in ops_list:
+            for nid, m in op.items():
+                if nid not in self.t:
+                    raise KeyError(f"no node {nid!r} in the state")
+                m = np.asarray(m.detach().cpu().numpy() if isinstance(m, torch.Tensor) else m,
+                               dtype=np.complex128)
+                d = self.t[nid].shape[-1]
+                if m.shape != (d, d):
+                    raise ValueError(f"operator on {nid} has shape {m.shape}, the node's physical "
+                                     f"dimension is {d}")
+                mats.append(m.reshape(-1))
+        key = tuple(tuple(op) for op in ops_list)
+        sig = tuple((nid, tuple(t.shape), t.data_ptr()) for nid, t in self.t.items())
+        if self._obs_sig != sig:
+            self._obs_sig = sig
+            self._obs_plans = {}
+        rec = self._obs_plans.get(key)
+        if rec is None:
+            rec = self._obs_plans[key] = self._observable_plan(key)
+        plan, opbuf, vals = rec
+        if mats:
+            opbuf.copy_(torch.from_numpy(np.concatenate(mats)))
+        plan.run()
+        return vals.cpu().numpy().copy()      # the values buffer is the plan's
+
+    def _observable_plan(self, layout):
+        """(plan, operator buffer, values) for ``expect_many`` on products
+        acting on the nodes ``layout[i]``."""
+        st = self.state
+        root = st.root_id
+        cb = ChainBuilder(self.ws)
+        hold = []
+        nenv = {}
+        dev = self.device
+
+        def buf(shape):
+            t = torch.zeros(shape, dtype=CDT, device=dev)
+            hold.append(t)
+            return t
+
+        def parent(nid):
+            return st.nodes[nid].parent
+
+        def node_step(nid, toward, envs, op=None, rdm=None, out=None):
+            """psi[nid] (times ``op`` on the physical leg) with the environments
+            ``envs`` (neighbour index -> (chi, chi) tensor, legs (ket, bra)) and
+            conj(psi[nid]); the open leg is the bond to ``toward``, or the
+            physical pair into ``rdm``, or none (a scalar into ``out``)."""
             shape = self.shape(nid)
             n = len(shape) - 1
             nb = self.nbrs(nid)
-            cb = ChainBuilder(self.ws)
-            base = Operand.contiguous(("fixed", self.t[nid]), [f"a{k}" for k in range(n)] + ["s"], shape)
-            T = base
-            if nid in ops:
-                O = torch.as_tensor(np.asarray(ops[nid], dtype=np.complex128)).to(self.device)
-                cache[("op", nid)] = O
-                T = cb.contract(T, Operand.contiguous(("fixed", O), ["t", "s"], list(O.shape)), ["s"])
-                T = Operand(T.ref, [l if l != "t" else "s" for l in T.labels], T.dims, T.strides)
-            subs = []
-            for k, x in enumerate(nb):
-                if x == toward:
-                    continue
-                sub = rec(x, nid)
-                subs.append(sub)
-                T = cb.contract(T, Operand.contiguous(("fixed", sub), [f"a{k}", f"c{k}"], list(sub.shape)),
+            T = Operand.contiguous(("fixed", self.t[nid]), [f"a{k}" for k in range(n)] + ["s"], shape)
+            if op is not None:
+                T = cb.contract(T, Operand.contiguous(("fixed", op), ["t", "s"], list(op.shape)), ["s"])
+                T = Operand(T.ref, ["s" if l == "t" else l for l in T.labels], T.dims, T.strides)
+            for k in sorted(envs):
+                E = envs[k]
+                T = cb.contract(T, Operand.contiguous(("fixed", E), [f"a{k}", f"c{k}"], list(E.shape)),
                                 [f"a{k}"])
+            phys = "t" if rdm is not None else "s"
             B = Operand.contiguous(("fixed", self.t[nid]),
-                                   [f"c{k}" if nb[k] != toward else "z" for k in range(n)] + ["s"], shape)
-            if toward is None:
-                res = torch.zeros((1,), dtype=CDT, device=self.device)
-                outop = Operand(("fixed", res), [], [], [])
-                cb.contract(T, B, [f"c{k}" for k in range(n)] + ["s"], out=outop, conj_b=True)
+                                   [f"c{k}" if nb[k] != toward else "z" for k in range(n)] + [phys], shape)
+            closed = [f"c{k}" for k in range(n) if nb[k] != toward]
+            if rdm is not None:
+                d = shape[-1]
+                cb.contract(T, B, closed, out=Operand.contiguous(("fixed", rdm), ["s", "t"], [d, d]),
+                            conj_b=True)
+            elif toward is None:
+                cb.contract(T, B, closed + ["s"], out=Operand(("fixed", out), [], [], []), conj_b=True)
             else:
                 k0 = nb.index(toward)
                 chi = shape[k0]
-                res = torch.zeros((chi, chi), dtype=CDT, device=self.device)
-                outop = Operand.contiguous(("fixed", res), [f"a{k0}", "z"], [chi, chi])
-                cb.contract(T, B, [f"c{k}" for k in range(n) if k != k0] + ["s"], out=outop, conj_b=True)
-            cb.plan().run()
-            return res
-        r = rec(st.root_id, None)
-        return complex(r.cpu().numpy()[0])
+                cb.contract(T, B, closed + ["s"], out=Operand.contiguous(("fixed", out), [f"a{k0}", "z"],
+                                                                          [chi, chi]), conj_b=True)
+
+        def env(u, v):
+            """N(u -> v), built on first use (toward the root from the
+            children's, away from it from the parent's and the siblings')."""
+            if (u, v) in nenv:
+                return nenv[(u, v)]
+            nb = self.nbrs(u)
+            envs = {k: env(x, u) for k, x in enumerate(nb) if x != v}
+            E = buf((self.shape(u)[nb.index(v)],) * 2)
+            node_step(u, v, envs, out=E)
+            nenv[(u, v)] = E
+            return E
+
+        # every environment toward the root, leaves first
+        post = []
+
+        def walk(nid):
+            for c in st.nodes[nid].phys_children:
+                walk(c)
+            post.append(nid)
+        walk(root)
+        for nid in post:
+            if nid != root:
+                env(nid, parent(nid))
+
+        below = {}             # node -> the nodes of its subtree
+        for nid in post:
+            s = {nid}
+            for c in st.nodes[nid].phys_children:
+                s |= below[c]
+            below[nid] = s
+
+        total = sum(self.t[nid].shape[-1] ** 2 for op in layout for nid in op)
+        opbuf = buf((max(total, 1),))
+        vals = buf((len(layout),))
+        rdms = {}
+        off = 0
+        for i, nodes in enumerate(layout):
+            mats = {}
+            for nid in nodes:
+                d = self.t[nid].shape[-1]
+                mats[nid] = opbuf[off:off + d * d].view(d, d)
+                off += d * d
+            out = vals[i:i + 1]
+            hold.append(out)
+            if len(nodes) == 0:
+                nb = self.nbrs(root)
+                node_step(root, None, {k: env(x, root) for k, x in enumerate(nb)}, out=out)
+            elif len(nodes) == 1:
+                nid = nodes[0]
+                if nid not in rdms:
+                    d = self.t[nid].shape[-1]
+                    rdms[nid] = buf((d, d))
+                    nb = self.nbrs(nid)
+                    node_step(nid, None, {k: env(x, nid) for k, x in enumerate(nb)}, rdm=rdms[nid])
+                d = self.t[nid].shape[-1]
+                cb.contract(Operand.contiguous(("fixed", rdms[nid]), ["s", "t"], [d, d]),
+                            Operand.contiguous(("fixed", mats[nid]), ["t", "s"], [d, d]), ["s", "t"],
+                            out=Operand(("fixed", out), [], [], []))
+            else:
+                sites = set(nodes)
+
+                def rec(nid, toward, dst):
+                    nb = self.nbrs(nid)
+                    envs = {}
+                    for k, x in enumerate(nb):
+                        if x == toward:
+                            continue
+                        if below[x] & sites:
+                            sub = buf((self.shape(x)[self.nbrs(x).index(nid)],) * 2)
+                            rec(x, nid, sub)
+                            envs[k] = sub
+                        else:
+                            envs[k] = env(x, nid)
+                    node_step(nid, toward, envs, op=mats.get(nid), out=dst)
+                rec(root, None, out)
+        plan = cb.plan()
+        plan._hold = hold
+        return plan, opbuf, vals

@@ -181,9 +181,27 @@ class RunLoop:
         num = 1 if evaluation_time == "inf" else self.num_time_steps // evaluation_time
         self.results.initialize(self.result_init_dictionary(), num)
 
+    def evaluate_operator_values(self) -> list:
+        """The current value of every operator, in the order of their names.
+        A driver on a device network measures all products of one-site
+        operators in one pass over the tree (``DeviceNetwork.expect_many``) and
+        each TTNO on its own; the reference evaluates them one at a time
+        (``time_evolution/ttn_time_evolution.py:181-197``)."""
+        ops = list(self.operators.values())
+        net = getattr(self, "net", None)
+        if net is None or not hasattr(net, "expect_many"):
+            return [self.evaluate_operator(op) for op in ops]
+        from .ttn import TreeTensorNetworkOperator
+        vals = [None] * len(ops)
+        local = [i for i, op in enumerate(ops) if not isinstance(op, TreeTensorNetworkOperator)]
+        if local:
+            for i, v in zip(local, net.expect_many([ops[i] for i in local])):
+                vals[i] = complex(v)
+        return [v if v is not None else self.evaluate_operator(op) for v, op in zip(vals, ops)]
+
     def evaluate_operators_at(self, index: int):
-        for key, op in self.operators.items():
-            self.results.set_element(key, index, self.evaluate_operator(op))
+        for key, value in zip(self.operators, self.evaluate_operator_values()):
+            self.results.set_element(key, index, value)
         if self._flag("record_bond_dim"):
             for key, value in self.state.bond_dims().items():
                 self.results.set_element(key, index, value)
@@ -201,7 +219,7 @@ class RunLoop:
 
     def evaluate_operators(self):
         """The current expectation values in the order of the operator names."""
-        return np.array([self.evaluate_operator(op) for op in self.operators.values()])
+        return np.array(self.evaluate_operator_values())
 
     def run(self, evaluation_time=1, pgbar: bool = True):
         """``TimeEvolution.run`` (``time_evolution.py:346-368``): step, measure

@@ -723,7 +723,9 @@ class TreeTensorNetworkState(TreeTensorNetwork):
         else:
             raise TypeError("Invalid input type of operators!")
         net = self._device()
-        return {n: [net.expect_local(dict(op)) for op in ops] for n, ops in prepared.items()}
+        flat = [op for ops in prepared.values() for op in ops]
+        vals = iter(net.expect_many(flat))
+        return {n: [complex(next(vals)) for _ in ops] for n, ops in prepared.items()}
 
     def ttno_expectation_value(self, operator) -> complex:
         return self._device().expect_ttno(operator)

@@ -5,6 +5,7 @@ same C ABI), so these tests check everything the Python layer decides; the GPU
 tests check the kernels through the real library.
 """
 import numpy as np
+import torch
 import pytest
 
 import fake_ptn
@@ -1452,3 +1453,85 @@ def test_ttn_parentage_and_to_complex():
     assert t.tensors["r"].dtype == np.complex64
     with pytest.raises(ValueError):
         t.to_complex(32)
+
+
+def test_expect_many_one_pass(monkeypatch):
+    """DeviceNetwork.expect_many: one-site operators (several on one node, on
+    the root and on leaves), products on several nodes (in one subtree and
+    across the root) and the norm, against the oracle's full contraction per
+    product; the plan is built once per operator layout and rebuilt when a
+    site tensor changes shape."""
+    import pytreenet_gb300 as P
+    import oracle as O
+    from pytreenet_gb300.engine import DeviceNetwork
+    fake_ptn.install(monkeypatch)
+    c = load_case("ttree3_heis_chi6_o1")
+    st = build_ttn(P.TTNS, c["spec"], c["init"])
+    ost = oracle_state(c)
+    net = DeviceNetwork(st)
+    rng = np.random.default_rng(3)
+    ids = [nid for nid, _ in c["spec"]]
+
+    def herm(d):
+        m = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+        return m + m.conj().T
+    root = ids[0]
+    ops = [{root: herm(2)}, {ids[1]: Zm}, {ids[1]: herm(2)}, {ids[-1]: herm(2)}, {},
+           {ids[1]: Zm, ids[2]: herm(2)}, {ids[-1]: Zm, ids[1]: herm(2), root: herm(2)},
+           {ids[-2]: rng.normal(size=(2, 2)) + 1j * rng.normal(size=(2, 2))}]
+    got = net.expect_many(ops)
+    want = np.array([O.expect_product(ost, op) for op in ops])
+    assert np.max(np.abs(got - want)) < 1e-12 * max(1.0, np.max(np.abs(want)))
+    assert abs(net.expect_local({ids[1]: Zm}) - want[1]) < 1e-12
+    # the same layout with other matrices reuses the plan
+    n_plans = len(net._obs_plans)
+    ops2 = [{k: 2 * v for k, v in op.items()} for op in ops]
+    got2 = net.expect_many(ops2)
+    want2 = np.array([O.expect_product(ost, op) for op in ops2])
+    assert len(net._obs_plans) == n_plans
+    assert np.max(np.abs(got2 - want2)) < 1e-12 * max(1.0, np.max(np.abs(want2)))
+    with pytest.raises(ValueError):
+        net.expect_many([{ids[1]: np.eye(3)}])
+    with pytest.raises(KeyError):
+        net.expect_many([{"no-such-node": Zm}])
+    # a tensor replaced by one of another shape drops the plans
+    leaf = ids[-1]
+    t = net.t[leaf]
+    bigger = torch.zeros((t.shape[0] + 1,) + tuple(t.shape[1:]), dtype=t.dtype)
+    bigger[:t.shape[0]] = t
+    par = st.nodes[leaf].parent
+    tp = net.t[par]
+    ax = st.phys_axis(par, leaf)
+    shp = list(tp.shape)
+    shp[ax] += 1
+    tp2 = torch.zeros(shp, dtype=tp.dtype)
+    tp2.narrow(ax, 0, tp.shape[ax]).copy_(tp)
+    net._set_node_tensor(leaf, bigger)
+    net._set_node_tensor(par, tp2)
+    got3 = net.expect_many(ops)
+    assert np.max(np.abs(got3 - got)) < 1e-12 * max(1.0, np.max(np.abs(want)))
+
+
+def test_run_loop_measures_in_one_pass(monkeypatch):
+    """The run loop hands all one-site products to one expect_many call per
+    measurement and a TTNO to expect_ttno; the values are the per-operator ones."""
+    import pytreenet_gb300 as P
+    fake_ptn.install(monkeypatch)
+    c = load_case("ttree3_heis_chi6_o1")
+    st = build_ttn(P.TTNS, c["spec"], c["init"])
+    H = build_ttn(P.TTNO, c["spec"], c["ttno"])
+    ids = [nid for nid, _ in c["spec"]]
+    ops = {f"z{n}": P.TensorProduct({n: Zm}) for n in ids}
+    ops["energy"] = H
+    algo = P.FirstOrderOneSiteTDVP(st, H, c["dt"], 2 * c["dt"], ops,
+                                   config=P.TDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV),
+                                   solver_options={"krylov_tol": c["krylov_tol"]})
+    calls = []
+    orig = algo.net.expect_many
+    monkeypatch.setattr(algo.net, "expect_many", lambda lst: calls.append(len(lst)) or orig(lst))
+    algo.run(pgbar=False)
+    assert calls == [len(ids)] * 3
+    res = algo.results
+    for n in ids:
+        assert abs(res.operator_result(f"z{n}")[-1] - algo.net.expect_local({n: Zm})) < 1e-13
+    assert abs(res.operator_result("energy")[-1] - algo.net.expect_ttno(H)) < 1e-12

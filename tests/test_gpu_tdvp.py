@@ -96,3 +96,31 @@ def test_gpu_default_mode(name):
     one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), st)
     assert zerr < 1e-11
     assert one_minus_f < 1e-12
+
+
+def test_gpu_observables_one_pass():
+    """The run loop measures every <Z_i> in one pass over the tree
+    (``expect_many``) after each step: the values are the reference's saved
+    ones, and products across the root, several operators on one node and the
+    norm match the oracle's full contraction of the device state."""
+    import pytreenet_gb300 as P
+    name = "ttree3_heis_chi6_o1"
+    c = load_case(name)
+    st = build_ttn(P.TTNS, c["spec"], c["init"])
+    H = build_ttn(P.TTNO, c["spec"], c["ttno"])
+    ids = [nid for nid, _ in c["spec"]]
+    ops = {nid: P.TensorProduct({nid: Zm}) for nid in ids}
+    algo = P.FirstOrderOneSiteTDVP(st, H, c["dt"], c["dt"] * c["steps"], ops,
+                                   config=P.TDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV),
+                                   solver_options={"krylov_tol": c["krylov_tol"]})
+    res = algo.run(pgbar=False)
+    assert np.max(np.abs(res[1:] - c["z"])) < 1e-10
+    rng = np.random.default_rng(11)
+    X = np.array([[0, 1], [1, 0]], dtype=complex)
+    M = rng.normal(size=(2, 2)) + 1j * rng.normal(size=(2, 2))
+    prods = [{ids[1]: X}, {ids[1]: M}, {ids[0]: Zm, ids[-1]: X}, {ids[1]: X, ids[2]: X}, {},
+             {ids[-1]: M, ids[-2]: Zm, ids[0]: X}]
+    got = algo.net.expect_many(prods)
+    ost = O.OState(oracle_state(c).tree, {nid: algo.state.get_phys_numpy(nid) for nid in ids})
+    want = np.array([O.expect_product(ost, p) for p in prods])
+    assert np.max(np.abs(got - want)) < 1e-12

@@ -69,8 +69,10 @@ def parse():
     ap.add_argument("--full-sweep", action="store_true",
                     help="reference arm: time one complete oracle sweep and compare the per-operation model")
     ap.add_argument("--entries", type=int, default=1 << 24, help="gram_schmidt: vector length")
+    ap.add_argument("--qr-m", type=int, default=512, help="qr: rows")
+    ap.add_argument("--qr-k", type=int, default=256, help="qr: columns")
     ap.add_argument("--workload", default="ttree",
-                    choices=["ttree", "c1", "ternary", "disorder", "gradient", "matvec", "gram_schmidt"],
+                    choices=["ttree", "c1", "qr", "ternary", "disorder", "gradient", "matvec", "gram_schmidt"],
                     help="ttree: one-site TDVP on the T-tree (headline); c1: one-site TDVP on the "
                          "15-node binary tree with <Z_i> at every site each step; ternary: second-order "
                          "two-site TDVP on the depth-3 ternary tree (40 sites, XXZ) with truncation; "
@@ -331,10 +333,11 @@ def _measured_peak(kind: str):
         return 6800.0, "fallback 6.8 TB/s (MEASURED_PEAKS.json absent), of fallback"
 
 
-# DRAM bytes per launch of the root-matvec tensor-core steps, from the ncu
-# capture summarised in profiles/cgemm_bf16x6_root_matvec_chi256.md (filled in
-# once that capture exists; None until then).
-ROOT_MATVEC_DRAM_BYTES = None
+# DRAM bytes per root matvec at chi=256 of its three tensor-core steps (E0, E1,
+# E2: dram__bytes_read.sum + dram__bytes_write.sum from one ncu capture,
+# profiles/cgemm_bf16x6_root_matvec_chi256.md); the W step and the operand
+# conversions are not included.
+ROOT_MATVEC_DRAM_BYTES = 22.49e9
 
 
 def run_gb300(args, rank, world):
@@ -435,7 +438,9 @@ def run_gb300(args, rank, world):
                 "frac": (achieved / peak) if achieved else None,
                 "peak_source": peak_src + "; achieved counts algorithmic complex flops (8 per complex MAC); "
                                "the BF16x6 split issues 6x as many tensor flops",
-                "traffic": ROOT_MATVEC_DRAM_BYTES}
+                "traffic": ROOT_MATVEC_DRAM_BYTES if args.chi == 256 else None,
+                "traffic_scope": "DRAM bytes of the three tensor-core steps of one root matvec at chi=256 "
+                                 "(ncu, one capture); achieved is per matvec as well"}
     else:
         roof = {"bound": "tensor", "kernel": "H_eff matvec chain: zcontract_kernel (FP64)",
                 "achieved": achieved, "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
@@ -730,6 +735,51 @@ def run_gram_schmidt(args):
             "peak_source": src_h, "kernels": "gs_pass_kernel (3 passes) + partial-sum finish in the last CTA"}
 
 
+def run_qr(args):
+    """One Householder QR (LAPACK conventions, Q kept in place) of a seeded
+    random --qr-m x --qr-k complex128 matrix, the shape of the T-tree arm split
+    by default (512 x 256): the one-launch kernel (ptn_zqr_keep) and the launch
+    sequence (ptn_zqr_keep_steps), each timed with CUDA events around the call
+    only (the input is restored before each call), and the FP64 work
+    8 (m k^2 - k^3 / 3) flops of the factorisation plus as much for forming Q."""
+    import torch
+    from pytreenet_gb300 import _lib
+    from pytreenet_gb300.engine import _stream_ptr
+    lib = _lib.load()
+    m, k = args.qr_m, args.qr_k
+    g = torch.Generator().manual_seed(0)
+    A0 = torch.complex(torch.randn(m * k, generator=g, dtype=torch.float64),
+                       torch.randn(m * k, generator=g, dtype=torch.float64)).cuda()
+    A = torch.empty_like(A0)
+    rowoff = torch.arange(m, dtype=torch.int64, device="cuda")
+    R = torch.zeros(k * k, dtype=torch.complex128, device="cuda")
+    work = torch.zeros((int(lib.ptn_zqr_work_bytes(m, k)) + 15) // 16, dtype=torch.complex128, device="cuda")
+    out, res = {}, {}
+    for name, fn in (("one_launch", lib.ptn_zqr_keep), ("launch_sequence", lib.ptn_zqr_keep_steps)):
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(max(args.steps, 1))]
+        for i in range(max(args.warmup, 1) + len(ev)):
+            A.copy_(A0)
+            if i >= max(args.warmup, 1):
+                ev[i - max(args.warmup, 1)][0].record()
+            st = fn(A.data_ptr(), rowoff.data_ptr(), m, k, m, R.data_ptr(), work.data_ptr(), _stream_ptr())
+            if st != 0:
+                raise RuntimeError(f"QR status {st}")
+            if i >= max(args.warmup, 1):
+                ev[i - max(args.warmup, 1)][1].record()
+        torch.cuda.synchronize()
+        ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+        out[name] = {"ms": ms}
+        res[name] = (A.clone(), R.clone())
+    flops = 2 * 8 * (m * k * k - k ** 3 / 3)
+    return {"metric": f"Householder QR ms ({m} x {k} complex128, Q kept)", "results": out,
+            "fp64_gflop": flops / 1e9,
+            "fp64_tflops_one_launch": flops / (out["one_launch"]["ms"] / 1000.0) / 1e12,
+            "fp64_nominal_tflops": FP64_NOMINAL_TFLOPS,
+            "path": "one launch" if int(lib.ptn_zqr_path(m, k)) == 1 else "launch sequence",
+            "same_bits": all(torch.equal(x, y) for x, y in zip(res["one_launch"], res["launch_sequence"]))}
+
+
 def run_c1(args):
     """First-order one-site TDVP (Krylov) on the 15-node binary tree, TFIM J=1,
     g=0.5, seeded random product state padded to chi=8, dt=0.01, with <Z_i> at
@@ -1005,7 +1055,7 @@ def main():
     if args.impl == "reference" and args.full_sweep:
         print(json.dumps(run_reference_full_sweep(args)), flush=True)
         return
-    single = {"c1": run_c1, "gradient": run_gradient, "disorder": run_disorder, "ternary": run_two_site, "matvec": run_matvec,
+    single = {"qr": run_qr, "c1": run_c1, "gradient": run_gradient, "disorder": run_disorder, "ternary": run_two_site, "matvec": run_matvec,
               "gram_schmidt": run_gram_schmidt}
     if args.impl == "gb300" and (args.workload in single or args.breakdown or args.fidelity_sweeps):
         import torch

@@ -5,7 +5,9 @@ g_i and a coupling J), d<O>(T)/d theta_k is formed from 2 K (central) or
 K + 1 (forward) complete time evolutions on the engine. Each evolution is an
 ordinary driver run, so every one of them runs on the GPU path; the runs are
 independent and can also be spread over ``run_realisations`` workers.
-There is no adjoint (backward-in-time) TDVP here.
+This is the checker for the adjoint in ``adjoint.py`` (one forward and one
+backward sweep per gradient, whatever the number of parameters) and the
+fallback for parameters the adjoint does not cover.
 """
 from __future__ import annotations
 

@@ -8,9 +8,10 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 # bounds of the mixed-precision adjoint against the FP64 one on the 31-site,
-# chi=16, 10-step workload
+# chi=16, 10-step workload; measured on a GB300: |value difference| 1.6e-7,
+# gradient difference 1.9e-6 of the gradient's norm
 MIXED_VALUE_TOL = 1e-6
-MIXED_GRAD_TOL = 1e-4
+MIXED_GRAD_TOL = 1e-5
 
 
 def test_gpu_tdvp_gradient_matches_oracle_and_fd():

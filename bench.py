@@ -1003,7 +1003,8 @@ def run_gradient(args):
 
     def ham(th):
         return tfim_ttno(st, J=float(th[-1]), g={nid: float(th[i]) for i, (nid, _) in enumerate(spec)})
-    adj = OneSiteTDVPAdjoint(st, ham(theta), dt, nsteps, krylov_tol=tol, normalise=True)
+    adj = OneSiteTDVPAdjoint(st, ham(theta), dt, nsteps, krylov_tol=tol, normalise=True,
+                             precision=args.precision)
     for _ in range(args.warmup):
         coupling_gradient(adj, ham, theta, ops)
     torch.cuda.synchronize()
@@ -1035,17 +1036,30 @@ def run_gradient(args):
     h = 1e-5
     fd = {j: (run(theta + h * np.eye(theta.size)[j]) - run(theta - h * np.eye(theta.size)[j])) / (2 * h) for j in idx}
     err = max((abs(grad[j] - fd[j]) for j in idx), default=None)
+    plain = None
+    if args.precision == "mixed" and not args.no_plain:
+        # the complex128 adjoint on the same workload, timed the same way
+        adj64 = OneSiteTDVPAdjoint(st, ham(theta), dt, nsteps, krylov_tol=tol, normalise=True)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        v64, g64 = coupling_gradient(adj64, ham, theta, ops)
+        torch.cuda.synchronize()
+        plain = {"seconds": time.perf_counter() - t2, "value_difference": abs(val - v64),
+                 "gradient_difference_relative": float(np.linalg.norm(grad - g64) / np.linalg.norm(g64))}
     return {"metric": "gradient evaluations/sec (d<Z_root>/d(g_1..g_31, J), 30 one-site TDVP steps, "
                       f"31-site binary tree, chi={chi})",
             "value": 1.0 / sec, "unit": "gradients/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000 * sec, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "c128 (fp64)", "data": "synthetic",
+            "dtype": ("bf16x6 split contractions / f64 Krylov+QR+phi-integral" if args.precision == "mixed"
+                      else "c128 (fp64)"), "data": "synthetic",
             "config": {"workload": f"binary tree 31 sites, TFIM g_i~U[0.3,0.7], J=1, chi={chi} (bonds capped at the "
                                    f"subtree dimensions), first-order 1TDVP, dt={dt}, {nsteps} steps, "
-                                   f"krylov_tol={tol}", "timing": "wall clock per gradient, forward + backward"},
+                                   f"krylov_tol={tol}", "timing": "wall clock per gradient, forward + backward",
+                       "precision": args.precision},
             "gpu_launches": launches, "clocks": clk.summary(), "value_Z_root": val,
             "forward_seconds": fwd, "central_difference_seconds_estimate": 2 * theta.size * fwd,
             "forward_matches_driver": abs(v0 - val),
+            "plain_fp64_adjoint": plain,
             "fd_check": {"params": idx, "adjoint": [float(grad[j]) for j in idx], "central": [fd[j] for j in idx],
                          "max_abs_err": err, "grad_norm": float(np.linalg.norm(grad))}}
 

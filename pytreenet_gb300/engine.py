@@ -719,6 +719,13 @@ class DeviceNetwork:
         self.householder_count = 0     # splits done by Householder QR
         self.qr_rows_skipped = 0       # zero trailing rows the Householder QRs skipped
         self.graph_launches = 0
+        # modification stamps: _mod[node] = clock at the last write of its tensor,
+        # _env_at[(u, v)] = clock when E(u -> v) was computed, _w_at = clock of
+        # the last TTNO refresh (init_cache_but_one(reuse=True) reads them)
+        self._clock = 0
+        self._mod: dict = {}
+        self._env_at: dict = {}
+        self._w_at = 0
         self._obs_sig = None           # tensors the cached observable plans were built on
         self._obs_plans: dict = {}
         self._ttno_nets: dict = {}     # id(TTNO) -> (TTNO, tensor signature, network)
@@ -743,6 +750,8 @@ class DeviceNetwork:
         for nid, Wn in new.items():
             self.W[nid].copy_(torch.from_numpy(Wn))
         self.ham = hamiltonian
+        self._clock += 1
+        self._w_at = self._clock
 
     def _finish(self, cb: "ChainBuilder", own_fixed: bool = False):
         """The chain as a tensor-core plan on the reduced-precision paths, else FP64.
@@ -752,6 +761,12 @@ class DeviceNetwork:
         ``own_fixed``: the plan keeps its fixed operands converted (see
         ``MixedPlan``), for the operators of a Krylov solve."""
         return cb.mixed_plan(self.levels, own_fixed) if self.levels else cb.plan()
+
+    def _touch(self, *nids):
+        """Record a write of these nodes' tensors (environment reuse)."""
+        self._clock += 1
+        for nid in nids:
+            self._mod[nid] = self._clock
 
     # -- shapes ------------------------------------------------------------------
     def nbrs(self, nid):
@@ -858,16 +873,30 @@ class DeviceNetwork:
         p = self.env_plan(nid, nxt)
         p.run()
         self.flops += p.flops
+        self._env_at[(nid, nxt)] = self._clock
 
-    def init_cache_but_one(self, left_out):
+    def init_cache_but_one(self, left_out, reuse: bool = False):
         """All environments pointing toward ``left_out``
-        (``SandwichCache.init_cache_but_one``, ``contractions/sandwich_caching.py:97-126``)."""
+        (``SandwichCache.init_cache_but_one``, ``contractions/sandwich_caching.py:97-126``).
+        ``reuse``: keep an environment computed after the last write of every
+        tensor on its side of the edge (and of the TTNO) -- its inputs are
+        unchanged, so recomputing it would give the same bits. Only for callers
+        whose tensor writes all went through this network."""
+        self.env_reused = getattr(self, "env_reused", 0)
+
         def rec(nid, toward):
+            newest = self._mod.get(nid, 0)
             for nb in self.nbrs(nid):
                 if nb != toward:
-                    rec(nb, nid)
+                    newest = max(newest, rec(nb, nid))
             if toward is not None:
-                self.update_env(nid, toward)
+                at = self._env_at.get((nid, toward))
+                if (reuse and at is not None and (nid, toward) in self.env and at >= newest
+                        and at >= self._w_at):
+                    self.env_reused += 1
+                else:
+                    self.update_env(nid, toward)
+            return newest
         rec(left_out, None)
 
     # -- local evolutions ------------------------------------------------------------
@@ -892,6 +921,7 @@ class DeviceNetwork:
             self.flops += p.flops
         x = self.t[nid]
         self._held(p, lambda: self.local_exp(x, apply, dt, exp_factor, tol, maxdim, hermitian, out=x))
+        self._touch(nid)
         self.check_device_status()
 
     def local_exp(self, x, apply, dt, exp_factor, tol, maxdim, hermitian=True, out=None):
@@ -1013,6 +1043,11 @@ class DeviceNetwork:
         return Rd
 
     def qr_split(self, nid, nbr) -> torch.Tensor:
+        R = self._qr_split(nid, nbr)
+        self._touch(nid)
+        return R
+
+    def _qr_split(self, nid, nbr) -> torch.Tensor:
         """tensor[nid] <- Q (KEEP), returns R (k x k; legs: new bond, nbr-side bond).
         Rows in the reference's logical order (``util/tensor_splitting.py:60-107``)."""
         st = self.state
@@ -1159,6 +1194,7 @@ class DeviceNetwork:
                   "dznrm2")
             check(lib.ptn_zscal_ratio(t.data_ptr(), scal[0:].data_ptr(), scal[1:].data_ptr(), t.data_ptr(),
                                       t.numel(), _stream_ptr()), "zscal_ratio")
+        self._touch(dst)
         node = st.nodes[src]
         if node.parent == dst:
             dn = st.nodes[dst]
@@ -1306,6 +1342,7 @@ class DeviceNetwork:
         self.cholqr_fails = {k for k in self.cholqr_fails if k[0] != nid}
 
     def _set_node_tensor(self, nid, t: torch.Tensor):
+        self._touch(nid)
         self.t[nid] = t
         self.state._phys[nid] = t
         self.state.nodes[nid].shape = tuple(t.shape)
@@ -1501,6 +1538,7 @@ class DeviceNetwork:
             self.env.pop((v, u), None)
             self._set_node_tensor(u, tu)
             self._set_node_tensor(v, tv)
+        self._touch(u, v)
         # logical order: the node that gains the new child lists it first (core/ttn.py:1400-1448)
         if st.nodes[v].parent == u:
             nu_ = st.nodes[u]
@@ -1548,6 +1586,7 @@ class DeviceNetwork:
         p.run()
         self.flops += p.flops
         self.t[nid].view(-1).copy_(self.ws.bufs["gate_out"][:self.t[nid].numel()])
+        self._touch(nid)
 
     def apply_two_site_gate(self, u, v, op: torch.Tensor, svd) -> np.ndarray:
         """A two-site gate (legs out_u, out_v, in_u, in_v) on neighbours u, v:
@@ -1580,6 +1619,7 @@ class DeviceNetwork:
         scal = self.ws.get("kry_scal", 8, torch.float64)
         check(lib.ptn_dznrm2(t.data_ptr(), t.numel(), scal.data_ptr(), part.data_ptr(), _stream_ptr()), "dznrm2")
         check(lib.ptn_zscal_inv(t.data_ptr(), scal.data_ptr(), t.data_ptr(), t.numel(), _stream_ptr()), "zscal")
+        self._touch(c)
         return float(scal[0].item())
 
     def canonical_form(self, center):

@@ -547,7 +547,9 @@ class FirstOrderOneSiteTDVP(OneSiteTDVP):
                     self._move_orth_and_update_cache_for_path(op[-1])
                 self._update_site(nid)
                 self.net.move_orth_center(path[0])
-                self.net.init_cache_but_one(path[0])
+                # environments whose side of the tree the sweep's last moves
+                # did not touch are still exact: keep them
+                self.net.init_cache_but_one(path[0], reuse=True)
             elif i == 0:
                 assert self.state.orthogonality_center_id == nid
                 self._update_site(nid)

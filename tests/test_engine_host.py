@@ -1535,3 +1535,35 @@ def test_run_loop_measures_in_one_pass(monkeypatch):
     for n in ids:
         assert abs(res.operator_result(f"z{n}")[-1] - algo.net.expect_local({n: Zm})) < 1e-13
     assert abs(res.operator_result("energy")[-1] - algo.net.expect_ttno(H)) < 1e-12
+
+
+def test_first_order_reset_reuses_unchanged_environments(monkeypatch):
+    """The first-order step's closing reset keeps the environments whose side
+    of the tree was not written after they were computed: some are kept on the
+    T-tree, and the evolved tensors are bitwise those of a run that recomputes
+    every environment."""
+    import pytreenet_gb300 as P
+    from pytreenet_gb300.engine import DeviceNetwork
+    fake_ptn.install(monkeypatch)
+    c = load_case("ttree3_heis_chi6_o1")
+
+    def run(reuse):
+        st = build_ttn(P.TTNS, c["spec"], c["init"])
+        H = build_ttn(P.TTNO, c["spec"], c["ttno"])
+        algo = P.FirstOrderOneSiteTDVP(st, H, c["dt"], c["dt"] * c["steps"], {},
+                                       config=P.TDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV),
+                                       solver_options={"krylov_tol": c["krylov_tol"]})
+        if not reuse:
+            orig = algo.net.init_cache_but_one
+            algo.net.init_cache_but_one = lambda left_out, reuse=False: orig(left_out, reuse=False)
+        for _ in range(c["steps"]):
+            algo.run_one_time_step()
+        return algo, {nid: algo.state.get_phys_numpy(nid) for nid, _ in c["spec"]}
+    a, ta = run(True)
+    b, tb = run(False)
+    assert getattr(a.net, "env_reused", 0) > 0
+    assert getattr(b.net, "env_reused", 0) == 0
+    for nid in ta:
+        assert np.array_equal(ta[nid], tb[nid]), nid
+    for key, E in a.net.env.items():
+        assert np.array_equal(E.numpy(), b.net.env[key].numpy()), key

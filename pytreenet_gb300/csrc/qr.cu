@@ -389,25 +389,17 @@ inline unsigned grid1(int64_t n) {
 
 // ---- small m, one cooperative launch ---------------------------------------------------
 // The same Householder steps as hh_fact_small / extract_r_small / hh_form_small,
-// with the same arithmetic per column (thread-to-row map, reduction tree, scalar
-// formulas), so the results are the same bits; but all of them run in one launch.
-//
-// Factorisation: CTA b keeps the contiguous columns [b * cpc, b * cpc + cpc) in
-// shared memory. Reflector j is computed by the owner of column j as soon as
-// column j has received reflectors 0 .. j-1, published through V, tau and a flag,
-// and applied by every CTA to all of its later columns in one pass (one
-// reduction for the dot products of all of them). Consecutive columns share an
-// owner, so only one hand-over in cpc crosses CTAs (a bounded wait on a flag and
-// one L2 round trip); the owner applies its own reflectors from shared memory.
-// Each block reduction takes one barrier: warp sums go to one of two alternating
-// buffers and every thread adds them in warp order (block_sum's arithmetic).
-//
-// Formation: column c of Q is H_0 ... H_c e_c. CTA b forms the columns of the
-// snake order (b, 2G-1-b, 2G+b, ...), which balances the c + 1 steps they need,
-// once its own factorisation work is done and reflector c has been published.
+// with the same arithmetic per column (thread-to-row map, reduction tree,
+// scalar formulas), so the results are the same bits; but all of them run in
+// one launch. CTA b owns a few columns (snake order, so the Q formation work
+// -- column c needs c + 1 reflectors -- is balanced) and keeps them in shared
+// memory. Reflector j is computed once, by the owner of column j, as soon as
+// column j has received reflectors 0 .. j-1, and published through V, tau and
+// a flag; every CTA waits for the flag (bounded), then applies the reflector
+// to its own columns. The owner of column j + 1 updates that column first and
+// publishes reflector j + 1 right away, so the chain of dependent steps costs
+// one flag hand-over each instead of one kernel launch.
 constexpr long long HP_WAIT_CYCLES = 4000000000LL;   // ~2 s at 2 GHz
-constexpr int HP_MAXC = 8;                           // columns per CTA in the factorisation
-constexpr int HP_NW = ST / 32;
 
 struct HPArgs {
   double2* A;
@@ -420,138 +412,44 @@ struct HPArgs {
   int* ready;     // [p], zero on entry; ready[j] = 1 once reflector j is published
   int* status;    // nonzero: a wait ran out (every CTA stops)
   int G;          // CTAs
-  int cpc;        // factorisation columns per CTA (contiguous)
+  int cpc;        // columns per CTA (upper bound)
 };
 
-// i-th column of CTA b in the formation (snake order, increasing in i)
+// i-th column of CTA b (increasing in i)
 __device__ __forceinline__ int64_t hp_col(int b, int i, int G) {
   return (int64_t)i * G + ((i & 1) ? (G - 1 - b) : b);
 }
-
-// Block sums of nv complex partials (block_sum's arithmetic for each part), one barrier.
-__device__ __forceinline__ void hp_reduce(double2 (&w)[HP_MAXC], int nv, double2 (*red)[HP_MAXC][HP_NW],
-                                          int& rb) {
-  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-#pragma unroll
-  for (int i = 0; i < HP_MAXC; ++i)
-    if (i < nv) {
-      w[i].x = warp_sum(w[i].x);
-      w[i].y = warp_sum(w[i].y);
-      if (lane == 0) red[rb][i][wp] = w[i];
-    }
-  __syncthreads();
-#pragma unroll
-  for (int i = 0; i < HP_MAXC; ++i)
-    if (i < nv) {
-      double sx = 0.0, sy = 0.0;
-      for (int q = 0; q < HP_NW; ++q) {
-        sx += red[rb][i][q].x;
-        sy += red[rb][i][q].y;
-      }
-      w[i] = make_double2(sx, sy);
-    }
-  rb ^= 1;
-}
-
-__device__ __forceinline__ double hp_reduce1(double v, double (*red)[HP_NW], int& rb) {
-  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-  v = warp_sum(v);
-  if (lane == 0) red[rb][wp] = v;
-  __syncthreads();
-  double s = 0.0;
-  for (int q = 0; q < HP_NW; ++q) s += red[rb][q];
-  rb ^= 1;
-  return s;
+__device__ __forceinline__ int hp_owner(int64_t c, int G) {
+  const int64_t i = c / G, r = c - i * G;
+  return (int)((i & 1) ? (G - 1 - r) : r);
 }
 
 __global__ void __launch_bounds__(ST) hh_persistent_kernel(HPArgs a) {
   extern __shared__ double2 hsm[];           // [cpc][m] own columns, then [m] reflector
-  __shared__ double2 red[2][HP_MAXC][HP_NW];
-  __shared__ double redn[2][HP_NW];
-  __shared__ double2 sbeta[HP_MAXC];
+  __shared__ double red[ST / 32 + 1];
+  __shared__ double2 red2[ST / 32 + 1];
+  __shared__ double2 sc[2];
   __shared__ int abort_s;
   const int b = blockIdx.x, tid = threadIdx.x, G = a.G;
   const int64_t m = a.m, k = a.k, p = a.p, cs = a.cs;
   double2* vs = hsm + (int64_t)a.cpc * m;
-  int rb = 0, rn = 0;
-  const int64_t c0 = (int64_t)b * a.cpc;
-  const int nown = (int)(k - c0 < a.cpc ? k - c0 : a.cpc);
-  for (int i = 0; i < nown; ++i)
-    for (int64_t t = tid; t < m; t += ST) hsm[i * m + t] = a.A[a.rowoff[t] + (c0 + i) * cs];
+  int nown = 0;
+  while (nown < a.cpc && hp_col(b, nown, G) < k) ++nown;
+  for (int i = 0; i < nown; ++i) {
+    const int64_t c = hp_col(b, i, G);
+    for (int64_t t = tid; t < m; t += ST) hsm[i * m + t] = a.A[a.rowoff[t] + c * cs];
+  }
   if (tid == 0) abort_s = 0;
   __syncthreads();
 
-  // bounded wait for reflector j (thread 0 spins; the barrier hands the result on)
-  auto wait_flag = [&](int64_t j) -> bool {
+  // zlarfg on column j (own slot col) and publication of v_j, tau_j, beta_j
+  auto publish = [&](int64_t j, const double2* col) {
+    const int64_t len = m - j;
+    double acc = 0.0;
+    for (int64_t t = tid; t < len; t += ST)
+      if (t > 0) acc += cabs2(col[j + t]);
+    const double xn2 = block_sum<ST>(acc, red);
     if (tid == 0) {
-      const volatile int* flag = a.ready + j;
-      const volatile int* st = a.status;
-      const long long t0 = clock64();
-      for (unsigned it = 0;; ++it) {
-        if (*flag != 0) break;
-        if ((it & 255u) == 0u && *st != 0) { abort_s = 1; break; }
-        if (clock64() - t0 > HP_WAIT_CYCLES) {
-          atomicExch(a.status, PTN_ERR_TIMEOUT);
-          abort_s = 1;
-          break;
-        }
-      }
-      __threadfence();
-    }
-    __syncthreads();
-    return abort_s == 0;
-  };
-
-  // reflector j (staged in vs, rows j + t with t = tid + q * ST; f = conj(tau_j))
-  // applied to the own columns after j
-  auto apply = [&](int64_t j, double2 f) {
-    const int64_t len = m - j;
-    const int i0 = (int)(j + 1 - c0 > 0 ? j + 1 - c0 : 0);
-    const int nv = nown - i0;
-    if (nv <= 0) return;
-    double2 w[HP_MAXC];
-#pragma unroll
-    for (int i = 0; i < HP_MAXC; ++i) w[i] = make_double2(0.0, 0.0);
-    for (int64_t t = tid; t < len; t += ST) {
-      const double2 v = vs[t];
-#pragma unroll
-      for (int i = 0; i < HP_MAXC; ++i)
-        if (i < nv) w[i] = cfmac(v, hsm[(i0 + i) * m + j + t], w[i]);
-    }
-    hp_reduce(w, nv, red, rb);
-#pragma unroll
-    for (int i = 0; i < HP_MAXC; ++i)
-      if (i < nv) w[i] = cmul(f, w[i]);
-    for (int64_t t = tid; t < len; t += ST) {
-      const double2 v = vs[t];
-#pragma unroll
-      for (int i = 0; i < HP_MAXC; ++i)
-        if (i < nv) {
-          double2* q = hsm + (i0 + i) * m + j + t;
-          *q = csub(*q, cmul(v, w[i]));
-        }
-    }
-  };
-
-  bool ok = true;
-  const int64_t jend = (c0 + nown < p) ? c0 + nown : p;
-  for (int64_t j = 0; j < jend; ++j) {
-    const int64_t len = m - j;
-    double2 f;
-    if (j < c0) {
-      if (!wait_flag(j)) { ok = false; break; }
-      for (int64_t t = tid; t < len; t += ST) vs[t] = __ldcg(a.V + j * m + j + t);
-      f = __ldcg(a.tau + j);
-      f.y = -f.y;  // conj(tau): the factorisation applies H^H
-    } else {
-      // zlarfg on own column j; every thread forms the same scalars
-      __syncthreads();
-      const int i = (int)(j - c0);
-      const double2* col = hsm + i * m;
-      double acc = 0.0;
-      for (int64_t t = tid; t < len; t += ST)
-        if (t > 0) acc += cabs2(col[j + t]);
-      const double xn2 = hp_reduce1(acc, redn, rn);
       const double2 alpha = col[j];
       const double xnorm = sqrt(xn2);
       double2 t_, s_, b_;
@@ -568,104 +466,134 @@ __global__ void __launch_bounds__(ST) hh_persistent_kernel(HPArgs a) {
         s_ = make_double2(d.x / den, -d.y / den);
         b_ = make_double2(beta, 0.0);
       }
-      for (int64_t t = tid; t < len; t += ST) {
-        const double2 v = (t == 0) ? make_double2(1.0, 0.0) : cmul(col[j + t], s_);
-        vs[t] = v;
-        a.V[j * m + j + t] = v;
-      }
-      if (tid == 0) {
-        a.tau[j] = t_;
-        a.betas[j] = b_;
-        sbeta[i] = b_;
-      }
-      __threadfence();
-      __syncthreads();
-      if (tid == 0) atomicExch(a.ready + j, 1);
-      f = make_double2(t_.x, -t_.y);
-    }
-    apply(j, f);
-  }
-  __syncthreads();
-  if (ok) {
-    // R rows < p of the own columns (beta on the diagonal, the upper part above
-    // it); columns past p are KEEP padding of Q
-    for (int i = 0; i < nown; ++i) {
-      const int64_t c = c0 + i;
-      const double2* col = hsm + i * m;
-      for (int64_t r = tid; r < k; r += ST) {
-        double2 v = make_double2(0.0, 0.0);
-        if (r < p) {
-          if (c == r) v = sbeta[i];
-          else if (c > r) v = col[r];
-        }
-        a.R[r * k + c] = v;
-      }
-      if (c >= p)
-        for (int64_t t = tid; t < m; t += ST) a.A[a.rowoff[t] + c * cs] = make_double2(0.0, 0.0);
+      sc[1] = s_;
+      a.tau[j] = t_;
+      a.betas[j] = b_;
     }
     __syncthreads();
-    // Q columns (zung2r: column c = H_0 ... H_c e_c)
-    double2* col = hsm;
-    constexpr int PF = QR_SMALL_M / ST;                // rows per thread
-    for (int fi = 0;; ++fi) {
-      const int64_t c = hp_col(b, fi, G);
-      if (c >= p) break;
-      if (!wait_flag(c)) { ok = false; break; }      // flags are set in order: 0 .. c are out
-      const double2 tc = __ldcg(a.tau + c);
-      const double2* vc = a.V + c * m;
-      for (int64_t t = tid; t < m; t += ST) {
-        if (t < c) {
-          col[t] = make_double2(0.0, 0.0);
-        } else if (t == c) {
-          col[t] = make_double2(1.0 - tc.x, -tc.y);
-        } else {
-          const double2 vt = __ldcg(vc + t);
-          col[t] = make_double2(-(tc.x * vt.x - tc.y * vt.y), -(tc.x * vt.y + tc.y * vt.x));
+    const double2 s_ = sc[1];
+    for (int64_t t = tid; t < len; t += ST)
+      a.V[j * m + j + t] = (t == 0) ? make_double2(1.0, 0.0) : cmul(col[j + t], s_);
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) atomicExch(a.ready + j, 1);
+  };
+
+  if (p > 0 && hp_owner(0, G) == b) publish(0, hsm);      // column 0 is this CTA's slot 0
+  for (int64_t j = 0; j < p; ++j) {
+    if (tid == 0) {
+      const volatile int* flag = a.ready + j;
+      const volatile int* st = a.status;
+      const long long t0 = clock64();
+      for (unsigned it = 0;; ++it) {
+        if (*flag != 0) break;
+        if ((it & 255u) == 0u && *st != 0) { abort_s = 1; break; }
+        if (clock64() - t0 > HP_WAIT_CYCLES) {
+          atomicExch(a.status, PTN_ERR_TIMEOUT);
+          abort_s = 1;
+          break;
         }
       }
+      __threadfence();
+    }
+    __syncthreads();
+    if (abort_s) break;
+    const int64_t len = m - j;
+    // v_j and tau_j in one round trip to L2
+    if (tid == 0) sc[0] = __ldcg(a.tau + j);
+    for (int64_t t = tid; t < len; t += ST) vs[t] = __ldcg(a.V + j * m + j + t);
+    __syncthreads();
+    double2 f = sc[0];
+    f.y = -f.y;  // conj(tau): the factorisation applies H^H
+    for (int i = 0; i < nown; ++i) {
+      const int64_t c = hp_col(b, i, G);
+      if (c <= j) continue;
+      double2* col = hsm + i * m;
+      double2 w = make_double2(0.0, 0.0);
+      for (int64_t t = tid; t < len; t += ST) w = cfmac(vs[t], col[j + t], w);
+      w = block_sum2_fused<ST>(w, red2);
+      const double2 fw = cmul(f, w);
+      for (int64_t t = tid; t < len; t += ST) col[j + t] = csub(col[j + t], cmul(vs[t], fw));
       __syncthreads();
-      // H_{c-1}, ..., H_0 in turn; each step stages its reflector in shared
-      // memory, and the next one is fetched while this one is applied
-      double2 pre[PF];
-      double2 tpre = make_double2(0.0, 0.0);
-      if (c > 0) {
-        const double2* v = a.V + (c - 1) * m;
+      if (c == j + 1 && j + 1 < p) publish(j + 1, col);
+    }
+    __syncthreads();
+  }
+  if (abort_s) {
+    if (b == 0 && tid == 0) a.R[0] = make_double2(NAN, NAN);   // the result is not usable
+    return;
+  }
+  // R (rows < p: beta on the diagonal, the stored upper part above it), then Q
+  // (zung2r: column c = H_0 ... H_c e_c), KEEP padding past p
+  for (int i = 0; i < nown; ++i) {
+    const int64_t c = hp_col(b, i, G);
+    double2* col = hsm + i * m;
+    for (int64_t r = tid; r < k; r += ST) {
+      double2 v = make_double2(0.0, 0.0);
+      if (r < p) {
+        if (c == r) v = a.betas[r];
+        else if (c > r) v = col[r];
+      }
+      a.R[r * k + c] = v;
+    }
+    __syncthreads();
+    if (c >= p) {
+      for (int64_t t = tid; t < m; t += ST) a.A[a.rowoff[t] + c * cs] = make_double2(0.0, 0.0);
+      continue;
+    }
+    // reflectors come from other CTAs: read them through L2
+    const double2 tc = __ldcg(a.tau + c);
+    const double2* vc = a.V + c * m;
+    for (int64_t t = tid; t < m; t += ST) {
+      if (t < c) {
+        col[t] = make_double2(0.0, 0.0);
+      } else if (t == c) {
+        col[t] = make_double2(1.0 - tc.x, -tc.y);
+      } else {
+        const double2 vt = __ldcg(vc + t);
+        col[t] = make_double2(-(tc.x * vt.x - tc.y * vt.y), -(tc.x * vt.y + tc.y * vt.x));
+      }
+    }
+    __syncthreads();
+    // H_{c-1}, ..., H_0 in turn; each step stages its reflector in shared
+    // memory, and the next one is fetched while this one is applied
+    constexpr int PF = QR_SMALL_M / ST;                // rows per thread
+    double2 pre[PF];
+    double2 tpre = make_double2(0.0, 0.0);
+    if (c > 0) {
+      const double2* v = a.V + (c - 1) * m;
+#pragma unroll
+      for (int q = 0; q < PF; ++q) {
+        const int64_t t = (c - 1) + tid + (int64_t)q * ST;
+        pre[q] = t < m ? __ldcg(v + t) : make_double2(0.0, 0.0);
+      }
+      tpre = __ldcg(a.tau + (c - 1));
+    }
+    for (int64_t j = c - 1; j >= 0; --j) {
+#pragma unroll
+      for (int q = 0; q < PF; ++q) {
+        const int64_t t = j + tid + (int64_t)q * ST;
+        if (t < m) vs[t] = pre[q];
+      }
+      const double2 t_ = tpre;
+      if (j > 0) {
+        const double2* vn = a.V + (j - 1) * m;
 #pragma unroll
         for (int q = 0; q < PF; ++q) {
-          const int64_t t = (c - 1) + tid + (int64_t)q * ST;
-          pre[q] = t < m ? __ldcg(v + t) : make_double2(0.0, 0.0);
+          const int64_t t = (j - 1) + tid + (int64_t)q * ST;
+          pre[q] = t < m ? __ldcg(vn + t) : make_double2(0.0, 0.0);
         }
-        tpre = __ldcg(a.tau + (c - 1));
+        tpre = __ldcg(a.tau + (j - 1));
       }
-      for (int64_t j = c - 1; j >= 0; --j) {
-#pragma unroll
-        for (int q = 0; q < PF; ++q) {
-          const int64_t t = j + tid + (int64_t)q * ST;
-          if (t < m) vs[t] = pre[q];
-        }
-        const double2 t_ = tpre;
-        if (j > 0) {
-          const double2* vn = a.V + (j - 1) * m;
-#pragma unroll
-          for (int q = 0; q < PF; ++q) {
-            const int64_t t = (j - 1) + tid + (int64_t)q * ST;
-            pre[q] = t < m ? __ldcg(vn + t) : make_double2(0.0, 0.0);
-          }
-          tpre = __ldcg(a.tau + (j - 1));
-        }
-        double2 w[HP_MAXC];
-        w[0] = make_double2(0.0, 0.0);
-        for (int64_t t = j + tid; t < m; t += ST) w[0] = cfmac(vs[t], col[t], w[0]);
-        hp_reduce(w, 1, red, rb);
-        const double2 fw = cmul(t_, w[0]);
-        for (int64_t t = j + tid; t < m; t += ST) col[t] = csub(col[t], cmul(vs[t], fw));
-        __syncthreads();
-      }
-      for (int64_t t = tid; t < m; t += ST) a.A[a.rowoff[t] + c * cs] = col[t];
+      double2 w = make_double2(0.0, 0.0);
+      for (int64_t t = j + tid; t < m; t += ST) w = cfmac(vs[t], col[t], w);
+      w = block_sum2_fused<ST>(w, red2);
+      const double2 fw = cmul(t_, w);
+      for (int64_t t = j + tid; t < m; t += ST) col[t] = csub(col[t], cmul(vs[t], fw));
       __syncthreads();
     }
+    for (int64_t t = tid; t < m; t += ST) a.A[a.rowoff[t] + c * cs] = col[t];
   }
-  if (!ok && tid == 0) a.R[0] = make_double2(NAN, NAN);   // the result is not usable
 }
 
 }  // namespace
@@ -695,7 +623,7 @@ static bool hp_shape(int64_t m, int64_t k, int& G, int& cpc, size_t& smem) {
     if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&pr, dev) != cudaSuccess ||
         !pr.cooperativeLaunch)
       return d;
-    const size_t dyn = pr.sharedMemPerBlockOptin - 4096;    // room for the static shared memory
+    const size_t dyn = pr.sharedMemPerBlockOptin - 1024;    // room for the static shared memory
     if (cudaFuncSetAttribute(hh_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn) !=
         cudaSuccess)
       return d;
@@ -704,11 +632,9 @@ static bool hp_shape(int64_t m, int64_t k, int& G, int& cpc, size_t& smem) {
     return d;
   }();
   if (dv.n_sm <= 0 || m < 1 || k < 1 || m > QR_SMALL_M) return false;
-  // two columns per CTA, more when k exceeds twice the SMs (at most HP_MAXC)
-  int64_t c = 2;
-  if ((k + c - 1) / c > dv.n_sm) c = (k + dv.n_sm - 1) / dv.n_sm;
-  if (c > HP_MAXC) return false;
-  const int64_t g = (k + c - 1) / c;
+  int64_t g = (k + 1) / 2;                           // two columns per CTA
+  if (g > dv.n_sm) g = dv.n_sm;
+  const int64_t c = (k + g - 1) / g;
   const size_t bytes = (size_t)(c + 1) * (size_t)m * sizeof(double2);
   if (bytes > dv.dyn_max) return false;
   int max_per_sm = 0;

@@ -182,12 +182,15 @@ __global__ void __launch_bounds__(SVD_THREADS) zsvd_jacobi_kernel(SvdArgs a) {
 }
 
 // ---- small matrices: one CTA, everything in shared memory --------------------------------
-// For n <= SVD_SMALL_N columns and m <= SVD_SMALL_M rows the same sweeps run in
-// one CTA with CTA barriers between rounds (no cooperative launch, no global
-// traffic). Same pair schedule, rotation formula, thresholds and ordering as
-// the kernel above, one warp per pair, so the results are the same bit for bit.
-constexpr int64_t SVD_SMALL_N = 32, SVD_SMALL_M = 256;
-constexpr int SVD_SMALL_THREADS = 256;
+// For n <= SVD_SMALL_N columns whose working copy and rotations fit in shared
+// memory (SVD_SMALL_BYTES) the same sweeps run in one CTA with CTA barriers
+// between rounds (no cooperative launch, no global traffic). Same pair
+// schedule, rotation formula, thresholds and ordering as the kernel above, one
+// warp per pair (the pairs of a round are disjoint, so how they are spread over
+// the warps does not matter), so the results are the same bit for bit.
+constexpr int64_t SVD_SMALL_N = 64;
+constexpr int64_t SVD_SMALL_BYTES = 200 * 1024;
+constexpr int SVD_SMALL_THREADS = 1024;
 
 __device__ bool rotate_pair_smem(double2* A, double2* V, int64_t m, int64_t n, int64_t i, int64_t j, double tol,
                                  double zero2, int lane) {
@@ -382,12 +385,11 @@ extern "C" int ptn_zsvd_jacobi(const ptn_svd_desc* d, void* stream) {
   a.tol = 8.0 * sqrt((double)d->m) * 1.1102230246251565e-16;
   a.status = d->status;
   cudaStream_t s = ptn_stream(stream);
-  if (d->n <= SVD_SMALL_N && d->m <= SVD_SMALL_M) {
+  const size_t smem = (size_t)(d->m * d->n + d->n * d->n) * sizeof(double2);
+  if (d->n <= SVD_SMALL_N && smem <= (size_t)SVD_SMALL_BYTES) {
     static const cudaError_t attr = cudaFuncSetAttribute(
-        zsvd_jacobi_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-        (int)((SVD_SMALL_M * SVD_SMALL_N + SVD_SMALL_N * SVD_SMALL_N) * sizeof(double2)));
+        zsvd_jacobi_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SVD_SMALL_BYTES);
     if (attr != cudaSuccess) return PTN_ERR_LAUNCH;
-    const size_t smem = (size_t)(d->m * d->n + d->n * d->n) * sizeof(double2);
     PTN_COUNT(1);
     zsvd_jacobi_small_kernel<<<1, SVD_SMALL_THREADS, smem, s>>>(a);
     return ptn_launch_status();

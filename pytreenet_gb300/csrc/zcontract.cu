@@ -158,6 +158,58 @@ __global__ void __launch_bounds__(256) zcontract_kernel(const ContractArgs a) {
   }
 }
 
+// Few outputs over a long K (a reduced density matrix: 2 x 2 outputs summed
+// over every bond index; the last step of a small environment update): the
+// tiled kernel would walk K on one CTA in steps of BK. Here each output is
+// summed by a group of G = SMALL_THREADS / P threads (P = the next power of two
+// of M * N), lane g of the group taking k = g, g + G, ...; the group's partial
+// sums are then added by a fixed tree, so the result does not vary between runs.
+constexpr int SMALL_THREADS = 1024;
+constexpr int64_t SMALL_MAX_OUT = 256;   // M * N up to this (G >= 4)
+constexpr int64_t SMALL_MIN_K = 64;
+
+__global__ void __launch_bounds__(SMALL_THREADS) zcontract_small_kernel(const ContractArgs a) {
+  __shared__ double2 part[SMALL_THREADS];
+  const int tid = threadIdx.x;
+  const int64_t outs = a.M * a.N;
+  int P = 1;
+  while (P < outs) P <<= 1;
+  const int G = SMALL_THREADS / P;
+  const int o = tid / G, g = tid - o * G;
+  double2 acc = make_double2(0.0, 0.0);
+  int64_t ocm = 0, ocn = 0;
+  if (o < outs) {
+    const int64_t mi = o / a.N, ni = o - mi * a.N;
+    int64_t oa, ob;
+    decode(a.m, mi, oa, ocm);
+    decode(a.n, ni, ob, ocn);
+    for (int64_t k = g; k < a.K; k += G) {
+      int64_t ka, kb;
+      decode(a.k, k, ka, kb);
+      double2 x = a.A[oa + ka];
+      double2 y = a.B[kb + ob];
+      if (a.conj_a) x.y = -x.y;
+      if (a.conj_b) y.y = -y.y;
+      acc = cfma(x, y, acc);
+    }
+  }
+  part[tid] = acc;
+  __syncthreads();
+  for (int h = G / 2; h > 0; h >>= 1) {
+    if (g < h) {
+      const double2 u = part[tid + h];
+      part[tid] = make_double2(part[tid].x + u.x, part[tid].y + u.y);
+    }
+    __syncthreads();
+  }
+  if (g == 0 && o < outs) {
+    double2* p = a.C + ocm + ocn;
+    double2 v = cmul(a.alpha, part[tid]);
+    if (!a.beta_zero) v = cfma(a.beta, *p, v);
+    *p = v;
+  }
+}
+
 // C <- beta * C (zero when beta == 0) over the M x N output positions.
 __global__ void __launch_bounds__(256) zcontract_scale_c(const ContractArgs a) {
   const int64_t total = a.M * a.N;
@@ -224,13 +276,21 @@ extern "C" int ptn_zcontract(const ptn_contract_desc* d, void* stream) {
   a.N = N;
   a.K = K;
   if (M == 0 || N == 0) return PTN_OK;
+  cudaStream_t s = ptn_stream(stream);
+  if (M * N <= SMALL_MAX_OUT && K >= SMALL_MIN_K) {
+    a.tiles_n = 1;
+    a.k_chunk = K;
+    a.split = 0;
+    PTN_COUNT(1);
+    zcontract_small_kernel<<<1, SMALL_THREADS, 0, s>>>(a);
+    return ptn_launch_status();
+  }
   int64_t tm = (M + BM - 1) / BM, tn = (N + BN - 1) / BN;
   a.tiles_n = tn;
   int64_t tiles = tm * tn;
   if (tiles > 0x7fffffffLL) return PTN_ERR_UNSUPPORTED;
   int64_t splits = ptn_zcontract_splits(tiles, K, &a.k_chunk);
   a.split = splits > 1;
-  cudaStream_t s = ptn_stream(stream);
   if (a.split) {
     int64_t total = M * N;
     int64_t blocks = (total + 255) / 256;

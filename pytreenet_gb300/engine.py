@@ -1349,8 +1349,12 @@ class DeviceNetwork:
 
     # Jacobi runs on the q x q core when q is at most this, or when the kept
     # rank could exceed half of q; otherwise a subspace iteration reduces T to
-    # max_bond_dim + SUBSPACE_OVERSAMPLE columns first.
-    SVD_DIRECT_MAX = 384
+    # max_bond_dim + SUBSPACE_OVERSAMPLE columns first. Up to 64 columns the
+    # Jacobi sweeps run in one CTA (shared memory, CTA barriers); above, every
+    # round of a sweep is a grid-wide barrier (~4 ms for a 128 x 128 core), so a
+    # small kept rank goes through the subspace iteration, whose cores fit the
+    # one-CTA kernel.
+    SVD_DIRECT_MAX = 64
     SUBSPACE_OVERSAMPLE = 16
     SUBSPACE_MAX_ITERS = 8
 

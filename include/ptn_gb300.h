@@ -185,8 +185,10 @@ int ptn_ztri_inv_newton(const void* X, const void* R0, void* R, void* work, int6
  * C[m, n] = sum_k A[m, k] * B[n, k] over complex numbers; A and B are given as
  * `levels` BF16 pieces (2: ~16-bit mantissa, products i+j<2 = "BF16x3";
  * 3: ~24-bit, products i+j<3 = "BF16x6"). A: 2*levels planes (Re_0, Im_0,
- * Re_1, Im_1, ...), plane p at A + p * a_plane, row m at m * lda (lda, a_plane
- * multiples of 8, 16-byte aligned base). Bx: bf16 [levels][3 blocks
+ * Re_1, Im_1, ...), plane p at A + p * a_plane, row m at m * lda (a_plane a
+ * multiple of 8, 16-byte aligned base; lda a multiple of 8 unless K <= 32 and
+ * N <= 128, which run on a CUDA-core kernel that reads A without TMA, where
+ * any lda >= K is taken). Bx: bf16 [levels][3 blocks
  * (-Im, Re, Im)][N][ldb] as written by ptn_expand_b. The result is written
  * through m_out / n_out (dims + stride_c): out_kind 0 = complex128 at C,
  * 1 = BF16 level planes at C with plane stride c_plane. status: device int32,

@@ -418,13 +418,16 @@ constexpr int64_t SMALLK_MAX_K = 32;
 constexpr int64_t SMALLK_MAX_N = 128;
 constexpr int SMALLK_T = 128;
 
+// KK: the K of the instance (EXACT) or an upper bound with K read at run time;
+// an exact K leaves no predicated-off steps in the unrolled K loops.
+template <int KK, bool EXACT>
 __global__ void __launch_bounds__(SMALLK_T)
     cgemm_smallk_kernel(const __nv_bfloat16* __restrict__ A, int64_t lda, int64_t a_plane,
                         const __nv_bfloat16* __restrict__ Bx, int64_t ldb, GemmArgs g, int L) {
-  __shared__ float2 sB[SMALLK_MAX_N * SMALLK_MAX_K];
+  __shared__ float2 sB[SMALLK_MAX_N * KK];
   __shared__ int64_t noff[SMALLK_MAX_N];
   if (*(volatile int32_t*)g.status != 0) return;
-  const int N = (int)g.N, K = (int)g.K;
+  const int N = (int)g.N, K = EXACT ? KK : (int)g.K;
   const int64_t blk = (int64_t)N * ldb;
   for (int e = threadIdx.x; e < N * K; e += SMALLK_T) {
     const int n = e / K, kk = e - n * K;
@@ -433,16 +436,16 @@ __global__ void __launch_bounds__(SMALLK_T)
       re += __bfloat162float(Bx[(3 * lv + 1) * blk + (int64_t)n * ldb + kk]);
       im += __bfloat162float(Bx[(3 * lv + 2) * blk + (int64_t)n * ldb + kk]);
     }
-    sB[n * SMALLK_MAX_K + kk] = make_float2(re, im);
+    sB[n * KK + kk] = make_float2(re, im);
   }
   for (int n = threadIdx.x; n < N; n += SMALLK_T) noff[n] = decode_off(g.no, n);
   __syncthreads();
   for (int64_t m = blockIdx.x * (int64_t)SMALLK_T + threadIdx.x; m < g.M; m += (int64_t)gridDim.x * SMALLK_T) {
-    float2 a[SMALLK_MAX_K];
+    float2 a[KK];
 #pragma unroll
-    for (int kk = 0; kk < SMALLK_MAX_K; ++kk) {
+    for (int kk = 0; kk < KK; ++kk) {
       float re = 0.f, im = 0.f;
-      if (kk < K) {
+      if (EXACT || kk < K) {
         for (int lv = 0; lv < L; ++lv) {
           re += __bfloat162float(A[(2 * lv) * a_plane + m * lda + kk]);
           im += __bfloat162float(A[(2 * lv + 1) * a_plane + m * lda + kk]);
@@ -454,9 +457,9 @@ __global__ void __launch_bounds__(SMALLK_T)
     for (int n = 0; n < N; ++n) {
       float cr = 0.f, ci = 0.f;
 #pragma unroll
-      for (int kk = 0; kk < SMALLK_MAX_K; ++kk) {
-        if (kk < K) {
-          const float2 b = sB[n * SMALLK_MAX_K + kk];
+      for (int kk = 0; kk < KK; ++kk) {
+        if (EXACT || kk < K) {
+          const float2 b = sB[n * KK + kk];
           cr = fmaf(a[kk].x, b.x, cr);
           cr = fmaf(-a[kk].y, b.y, cr);
           ci = fmaf(a[kk].x, b.y, ci);
@@ -613,9 +616,30 @@ extern "C" int ptn_cgemm_bf16x3(const ptn_cgemm_desc* d, void* stream) {
     int64_t blocks = (d->M + SMALLK_T - 1) / SMALLK_T;
     if (blocks > 152 * 16) blocks = 152 * 16;
     PTN_COUNT(1);
-    cgemm_smallk_kernel<<<(unsigned)blocks, SMALLK_T, 0, ptn_stream(stream)>>>(
-        static_cast<const __nv_bfloat16*>(d->A), d->lda, d->a_plane, static_cast<const __nv_bfloat16*>(d->Bx),
-        d->ldb, g, d->levels);
+    const __nv_bfloat16* A = static_cast<const __nv_bfloat16*>(d->A);
+    const __nv_bfloat16* B = static_cast<const __nv_bfloat16*>(d->Bx);
+    cudaStream_t st = ptn_stream(stream);
+    switch (d->K) {
+#define PTN_SMALLK_CASE(k)                                                                              \
+  case k:                                                                                               \
+    cgemm_smallk_kernel<k, true><<<(unsigned)blocks, SMALLK_T, 0, st>>>(A, d->lda, d->a_plane, B, d->ldb, g, \
+                                                                        d->levels);                     \
+    break;
+      PTN_SMALLK_CASE(2)
+      PTN_SMALLK_CASE(3)
+      PTN_SMALLK_CASE(4)
+      PTN_SMALLK_CASE(5)
+      PTN_SMALLK_CASE(6)
+      PTN_SMALLK_CASE(8)
+      PTN_SMALLK_CASE(10)
+      PTN_SMALLK_CASE(12)
+      PTN_SMALLK_CASE(16)
+      PTN_SMALLK_CASE(20)
+#undef PTN_SMALLK_CASE
+      default:
+        cgemm_smallk_kernel<(int)SMALLK_MAX_K, false><<<(unsigned)blocks, SMALLK_T, 0, st>>>(
+            A, d->lda, d->a_plane, B, d->ldb, g, d->levels);
+    }
     return ptn_launch_status();
   }
   CUtensorMap ta, tb;

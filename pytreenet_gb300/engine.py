@@ -273,6 +273,12 @@ def _round8(x):
     return (x + 7) // 8 * 8
 
 
+# products that libptn_gb300 runs on its CUDA-core kernel instead of the
+# tensor-core pipeline (ptn_cgemm_bf16x3: K <= 32 and N <= 128)
+SMALLK_MAX_K = 32
+SMALLK_MAX_N = 128
+
+
 class MixedPlan:
     """The same contraction chain on the tensor cores (BF16 splits, FP32 accumulation).
 
@@ -328,7 +334,12 @@ class MixedPlan:
             else:
                 cols = list(kl)
             K = int(np.prod([dims[l] for l in cols] or [1]))
-            lda = _round8(K)
+            Nn = int(np.prod([dims[l] for l in nlab] or [1]))
+            # a product the CUDA-core kernel takes (K <= 32, N <= 128) reads its A
+            # rows without TMA, so they are not padded to 8 entries: a padded row
+            # would make the producing epilogue write partial sectors (read-modify-
+            # write in L2) and the consumer read the padding
+            lda = K if (K <= SMALLK_MAX_K and Nn <= SMALLK_MAX_N) else _round8(K)
             stride = {}
             s_ = 1
             for l in reversed(cols):
@@ -349,7 +360,7 @@ class MixedPlan:
             K = int(np.prod([dims[l] for l in cols] or [1]))
             self.flops += 8 * M * N * K
             aslot = f"mp{i % 2}"
-            plane = M * lda
+            plane = _round8(M * lda)
             if i == 0:
                 d = ConvertDesc()
                 _set_modes(d.rows, [dims[l] for l in rows], [A.strides[A.labels.index(l)] for l in rows], "stride_a")
@@ -394,8 +405,8 @@ class MixedPlan:
                 nM = int(np.prod([info[i + 1][3][l] for l in nrows] or [1]))
                 cslot = f"mp{(i + 1) % 2}"
                 g.out_kind = 1
-                g.c_plane = nM * nlda
-                self._need(cslot, 2 * L * nM * nlda)
+                g.c_plane = _round8(nM * nlda)
+                self._need(cslot, 2 * L * g.c_plane)
                 _set_modes(g.m_out, [dims[l] for l in rows], [ost[l] for l in rows], "stride_c")
                 _set_modes(g.n_out, [dims[l] for l in nlab], [ost[l] for l in nlab], "stride_c")
                 self.ops.append(("gemm", g, (aref, bref, ("ws", cslot))))
@@ -1351,10 +1362,13 @@ class DeviceNetwork:
     # rank could exceed half of q; otherwise a subspace iteration reduces T to
     # max_bond_dim + SUBSPACE_OVERSAMPLE columns first. Up to 64 columns the
     # Jacobi sweeps run in one CTA (shared memory, CTA barriers); above, every
-    # round of a sweep is a grid-wide barrier (~4 ms for a 128 x 128 core), so a
-    # small kept rank goes through the subspace iteration, whose cores fit the
-    # one-CTA kernel.
-    SVD_DIRECT_MAX = 64
+    # round of a sweep is a grid-wide barrier (~4 ms for a 128 x 128 core). The
+    # subspace iteration costs two QRs and a host round trip per iteration, so
+    # below SVD_DIRECT_MAX it is taken only for kept ranks up to
+    # SUBSPACE_SMALL_L columns and cores at least four times wider (measured on
+    # the 31-site binary tree: max_bond_dim 8 gains 40 % per step, 32 loses).
+    SVD_DIRECT_MAX = 384
+    SUBSPACE_SMALL_L = 24
     SUBSPACE_OVERSAMPLE = 16
     SUBSPACE_MAX_ITERS = 8
 
@@ -1496,7 +1510,7 @@ class DeviceNetwork:
         p, q = (m, n) if vfirst else (n, m)
         mbd = svd.max_bond_dim
         l = q if mbd == float("inf") else min(q, int(mbd) + self.SUBSPACE_OVERSAMPLE)
-        if q > self.SVD_DIRECT_MAX and 2 * l <= q:
+        if (q > self.SVD_DIRECT_MAX and 2 * l <= q) or (q > 64 and l <= self.SUBSPACE_SMALL_L and 4 * l <= q):
             Y, Z, Uj, Vj, s = self._subspace_factor(x2, p, q, l)
             left = (Y, p, Vj, l, l)        # Ut = Q1 Vj
             right = (Z, q, Uj, l, l)       # Vt = Qz Uj

@@ -334,6 +334,11 @@ int ptn_krylov_gs_step(const void* Q, int64_t ldq, int32_t nq, void* w, int64_t 
 
 unsigned long long ptn_launch_counter(void);
 
+/* Wait until all work issued on `stream` has finished (cudaStreamSynchronize);
+ * PTN_ERR_LAUNCH if an earlier asynchronous launch failed. The drivers call it
+ * once per Krylov batch and per QR split to read a few scalars back. */
+int ptn_stream_synchronize(void* stream);
+
 /* Scan a complex128 buffer for NaN/Inf; flag (device int32) is set to 1 if found. */
 int ptn_check_finite(const void* x, int64_t n, int32_t* flag, void* stream);
 

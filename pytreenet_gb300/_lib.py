@@ -109,6 +109,7 @@ SIGNATURES = {
     "ptn_zqr_keep_steps": (ctypes.c_int, [_P, _P, _I64, _I64, _I64, _P, _P, _P]),
     "ptn_check_finite": (ctypes.c_int, [_P, _I64, _P, _P]),
     "ptn_launch_counter": (ctypes.c_ulonglong, []),
+    "ptn_stream_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
     "ptn_zqr_noalloc_max_bytes": (_I64, []),
     "ptn_zqr_keep_noalloc": (ctypes.c_int, [_P, _P, _I64, _I64, _I64, _P, _P]),
     "ptn_zqr_keep_rows": (ctypes.c_int, [_P, _P, _I64, _I64, _I64, _I64, _P, _P, _P]),

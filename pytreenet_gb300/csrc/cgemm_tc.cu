@@ -599,7 +599,9 @@ extern "C" int ptn_cgemm_bf16x3(const ptn_cgemm_desc* d, void* stream) {
   if (!d || !d->A || !d->Bx || !d->C || !d->status) return PTN_ERR_ARG;
   if (d->M < 1 || d->N < 1 || d->K < 1) return PTN_ERR_ARG;
   if (d->levels != 2 && d->levels != 3) return PTN_ERR_ARG;
-  if (d->lda % 8 || d->ldb % 8 || d->lda < d->K || d->ldb < d->K) return PTN_ERR_ARG;
+  // the CUDA-core path (K <= 32, N <= 128) reads A without TMA: any lda >= K
+  const bool smallk = d->K <= SMALLK_MAX_K && d->N <= SMALLK_MAX_N;
+  if ((!smallk && d->lda % 8) || d->ldb % 8 || d->lda < d->K || d->ldb < d->K) return PTN_ERR_ARG;
   if (d->a_plane % 8 || (reinterpret_cast<uintptr_t>(d->A) & 15) || (reinterpret_cast<uintptr_t>(d->Bx) & 15))
     return PTN_ERR_ARG;
   if (d->M > 0x7fffffffLL || d->N > 0x7fffffffLL) return PTN_ERR_UNSUPPORTED;
@@ -612,7 +614,7 @@ extern "C" int ptn_cgemm_bf16x3(const ptn_cgemm_desc* d, void* stream) {
   g.c_plane = d->c_plane;
   g.status = d->status;
   if (fill_out(d->m_out, g.mo) || fill_out(d->n_out, g.no)) return PTN_ERR_ARG;
-  if (d->K <= SMALLK_MAX_K && d->N <= SMALLK_MAX_N) {
+  if (smallk) {
     int64_t blocks = (d->M + SMALLK_T - 1) / SMALLK_T;
     if (blocks > 152 * 16) blocks = 152 * 16;
     PTN_COUNT(1);

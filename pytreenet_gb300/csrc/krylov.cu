@@ -141,6 +141,10 @@ std::atomic<unsigned long long> g_ptn_launches{0};
 
 extern "C" unsigned long long ptn_launch_counter(void) { return g_ptn_launches.load(); }
 
+extern "C" int ptn_stream_synchronize(void* stream) {
+  return cudaStreamSynchronize(ptn_stream(stream)) == cudaSuccess ? PTN_OK : PTN_ERR_LAUNCH;
+}
+
 // ---- Gram-Schmidt step in three passes ----------------------------------------------------
 // One pass over w per kernel; each CTA writes fixed-order partial sums, and
 // the last CTA to finish (atomic ticket, no waiting) adds them up in CTA

@@ -31,7 +31,16 @@ CDT = torch.complex128
 DEFAULT_DEVICE = "cuda"
 
 
+_RAW_STREAM = getattr(torch._C, "_cuda_getCurrentRawStream", None)
+_CUR_DEVICE = getattr(torch._C, "_cuda_getDevice", None)
+
+
 def _stream_ptr():
+    """The current CUDA stream of the current device as a foreign-call
+    argument. Called once per launch sequence: the direct lookup costs ~1 us
+    where torch.cuda.current_stream() measured ~15 us per call."""
+    if _RAW_STREAM is not None and _CUR_DEVICE is not None:
+        return ctypes.c_void_p(_RAW_STREAM(_CUR_DEVICE()))
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
@@ -603,7 +612,7 @@ class KrylovSolver:
             if st is not None:
                 st_host.copy_(st[:1], non_blocking=True)
             if self.ws.device.type == "cuda":
-                torch.cuda.current_stream().synchronize()
+                check(lib.ptn_stream_synchronize(stream), "stream synchronize")
             if st is not None and int(st_host[0]) != 0:
                 code = int(st_host[0])
                 st.zero_()
@@ -1111,7 +1120,7 @@ class DeviceNetwork:
                                           work.data_ptr(), stream), "zchol_upper")
             host.copy_(words, non_blocking=True)
             if self.device.type == "cuda":
-                torch.cuda.current_stream().synchronize()
+                check(lib.ptn_stream_synchronize(stream), "stream synchronize")
             if scan:
                 m_used = max(1, int(host[0]))
             if use_chol:

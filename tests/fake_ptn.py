@@ -211,6 +211,11 @@ def _fake_expand_b(self, d_ref, stream):
 def _fake_cgemm(self, d_ref, stream):
     d = d_ref._obj
     M, K, N, L = d.M, d.K, d.N, d.levels
+    # the library's argument checks (ptn_cgemm_bf16x3): lda a multiple of 8
+    # except on the CUDA-core path (K <= 32, N <= 128), ldb always, planes too
+    smallk = K <= 32 and N <= 128
+    if (not smallk and d.lda % 8) or d.ldb % 8 or d.lda < K or d.ldb < K or d.a_plane % 8:
+        return 1
     a = _view(d.A, (2 * L - 1) * d.a_plane + M * d.lda, np.uint16)
 
     def plane(p):
@@ -243,6 +248,7 @@ FakeLib.ptn_to_planes = _fake_to_planes
 FakeLib.ptn_expand_b = _fake_expand_b
 FakeLib.ptn_cgemm_bf16x3 = _fake_cgemm
 FakeLib.ptn_launch_counter = lambda self: 0
+FakeLib.ptn_stream_synchronize = lambda self, stream: 0
 
 
 # ---- SVD and permute ------------------------------------------------------------

@@ -383,6 +383,48 @@ __global__ void to_planes_kernel(const double2* __restrict__ src, OutModes mm, O
   }
 }
 
+// The same conversion through a 32 x 32 shared-memory tile, for operands
+// whose rows are contiguous in the source while the K index is not (the first
+// step of a matvec contracting the parent leg reads x with a stride of the
+// whole rest of the tensor): the tile is read with the row index across the
+// threads and written with the K index across them, so both sides coalesce.
+// Each element is converted exactly as in to_planes_kernel.
+__global__ void __launch_bounds__(256) to_planes_tiled_kernel(const double2* __restrict__ src, OutModes mm,
+                                                              OutModes km, int64_t M, int64_t K, int64_t lda,
+                                                              int64_t plane, int conj, int L,
+                                                              __nv_bfloat16* __restrict__ dst) {
+  __shared__ double2 tile[32][33];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int64_t tiles_k = (K + 31) / 32;
+  const int64_t tiles = ((M + 31) / 32) * tiles_k;
+  for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x) {
+    const int64_t m0 = (t / tiles_k) * 32, k0 = (t - (t / tiles_k) * tiles_k) * 32;
+    for (int r = ty; r < 32; r += 8) {
+      const int64_t m = m0 + tx, k = k0 + r;
+      double2 v = make_double2(0.0, 0.0);
+      if (m < M && k < K) v = src[decode_off(mm, m) + decode_off(km, k)];
+      tile[r][tx] = v;
+    }
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8) {
+      const int64_t m = m0 + r, k = k0 + tx;
+      if (m < M && k < K) {
+        double2 v = tile[tx][r];
+        if (conj) v.y = -v.y;
+        __nv_bfloat16 re[3], im[3];
+        split_levels(v.x, L, re);
+        split_levels(v.y, L, im);
+        const int64_t o = m * lda + k;
+        for (int lv = 0; lv < L; ++lv) {
+          dst[(2 * lv) * plane + o] = re[lv];
+          dst[(2 * lv + 1) * plane + o] = im[lv];
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // Bx[level][block][n][k]: block 0 = -Bi, 1 = Br, 2 = Bi.
 __global__ void expand_b_kernel(const double2* __restrict__ src, OutModes nm, OutModes km, int64_t N, int64_t K,
                                 int64_t ldb, int conj, int L, __nv_bfloat16* __restrict__ dst) {
@@ -680,6 +722,16 @@ extern "C" int ptn_to_planes(const ptn_convert_desc* d, void* stream) {
   if (fill_src(d->rows, mm, M) || fill_src(d->cols, km, K)) return PTN_ERR_ARG;
   if (d->ld < K) return PTN_ERR_ARG;
   PTN_COUNT(1);
+  // innermost (fastest) source strides of the row and K indices
+  const int64_t sm = mm.n > 0 ? mm.stride[mm.n - 1] : 0, sk = km.n > 0 ? km.stride[km.n - 1] : 0;
+  const int64_t asm_ = sm < 0 ? -sm : sm, ask = sk < 0 ? -sk : sk;
+  if (M >= 32 && K >= 32 && asm_ <= 2 && ask > 2) {
+    const int64_t tiles = ((M + 31) / 32) * ((K + 31) / 32);
+    to_planes_tiled_kernel<<<(unsigned)(tiles < 152 * 16 ? tiles : 152 * 16), 256, 0, ptn_stream(stream)>>>(
+        static_cast<const double2*>(d->src), mm, km, M, K, d->ld, d->plane, d->conj, d->levels,
+        static_cast<__nv_bfloat16*>(d->dst));
+    return ptn_launch_status();
+  }
   to_planes_kernel<<<grid_for(M * K), 256, 0, ptn_stream(stream)>>>(
       static_cast<const double2*>(d->src), mm, km, M, K, d->ld, d->plane, d->conj, d->levels,
       static_cast<__nv_bfloat16*>(d->dst));

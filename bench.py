@@ -83,6 +83,7 @@ def parse():
                     help="gradient: parameters checked against central differences of the driver")
     ap.add_argument("--realisations", type=int, default=32, help="disorder: number of realisations")
     ap.add_argument("--workers", type=int, default=8, help="disorder: concurrent worker streams")
+    ap.add_argument("--processes", type=int, default=8, help="disorder: worker processes on the GPU")
     ap.add_argument("--chi-max", type=int, default=64, help="ternary: max_bond_dim of the SVD split")
     return ap.parse_args()
 
@@ -103,12 +104,15 @@ def config(args, precision):
 # work (Gram-Schmidt step) by vector length. Counted in a dry run of the oracle
 # driver at chi=8 (the schedule and the Krylov depths do not depend on chi in
 # any material way), timed at the bench's chi.
-def oracle_schedule_counts(arm, tol, dt):
+def oracle_schedule_counts(arm, tol, dt, chi=8, seconds=None, seed=0):
+    """Operation counts of one oracle sweep (a dry run at ``chi``). With a dict
+    ``seconds``, also the wall time spent in each operation class (the Krylov
+    class "gs" then holds the whole exponential minus its matvecs)."""
     import oracle as O
     import oracle.ptn_oracle as OP
     from pytreenet_gb300.workloads import t_tree_state, t_tree_heisenberg
-    st, spec, tensors = t_tree_state(arm_len=arm, chi=8, seed=0)
-    H, W = t_tree_heisenberg(st, seed=1)
+    st, spec, tensors = t_tree_state(arm_len=arm, chi=chi, seed=seed)
+    H, W = t_tree_heisenberg(st, seed=1 if seconds is None else 1000)
     tree = O.OTree()
     for nid, p in spec:
         tree.add_root(nid) if p is None else tree.add_child(nid, p)
@@ -120,8 +124,15 @@ def oracle_schedule_counts(arm, tol, dt):
 
     def wrap(fn, key):
         def w(*a, **k):
-            bump(key(*a))
-            return fn(*a, **k)
+            kk = key(*a)
+            bump(kk)
+            if seconds is None:
+                return fn(*a, **k)
+            t0 = time.perf_counter()
+            try:
+                return fn(*a, **k)
+            finally:
+                seconds[kk] = seconds.get(kk, 0.0) + time.perf_counter() - t0
         return w
     saved = (OP.heff_apply, OP.env_update, OP.qr_keep_split, OP.bond_apply, OP.absorb_r, OP.krylov_exp_action)
     OP.heff_apply = wrap(OP.heff_apply, lambda x, tree, nid, *r: ("heff", deg[nid]))
@@ -136,7 +147,13 @@ def oracle_schedule_counts(arm, tol, dt):
         n = psi.size
         cls = 0 if psi.ndim == 2 and psi.shape[0] == psi.shape[1] and psi.shape[0] > 2 else psi.ndim - 1
         local = []
+        if seconds is not None:
+            inner = sum(seconds.values())
+            t0 = time.perf_counter()
         out = orig_kry(psi, action, *a, stats=local, **k)
+        if seconds is not None:
+            own = time.perf_counter() - t0 - (sum(seconds.values()) - inner)
+            seconds[("gs", cls)] = seconds.get(("gs", cls), 0.0) + own
         for m in local:
             counts[("gs", cls)] = counts.get(("gs", cls), 0) + int(m)
         if stats is not None:
@@ -148,7 +165,13 @@ def oracle_schedule_counts(arm, tol, dt):
         c0 = algo.state.orth_center
         algo.state.tensors[c0] = algo.state.tensors[c0] / np.linalg.norm(algo.state.tensors[c0])
         counts.clear()
+        if seconds is not None:
+            seconds.clear()
+            t0 = time.perf_counter()
         algo.run_one_time_step()
+        if seconds is not None:
+            seconds["sweep"] = time.perf_counter() - t0
+            seconds["krylov_depth_mean"] = float(np.mean(algo.krylov_dims)) if algo.krylov_dims else None
     finally:
         (OP.heff_apply, OP.env_update, OP.qr_keep_split, OP.bond_apply, OP.absorb_r,
          OP.krylov_exp_action) = saved
@@ -593,31 +616,26 @@ def run_reference(args, rank, world):
 
 def run_reference_full_sweep(args):
     """One complete sweep of the NumPy oracle at the bench's config (canonical
-    form and initial environments untimed), beside the per-operation model's
-    prediction for the same sweep."""
-    import oracle as O
-    from pytreenet_gb300.workloads import t_tree_state, t_tree_heisenberg
-    st, spec, tensors = t_tree_state(arm_len=args.arm, chi=args.chi, seed=0)
-    H, W = t_tree_heisenberg(st, seed=1000)
-    tree = O.OTree()
-    for nid, p in spec:
-        tree.add_root(nid) if p is None else tree.add_child(nid, p)
-    t0 = time.perf_counter()
-    algo = O.FirstOrderOneSiteTDVPOracle(O.OState(tree, tensors), W, args.dt, krylov_tol=args.tol)
-    c0 = algo.state.orth_center
-    algo.state.tensors[c0] = algo.state.tensors[c0] / np.linalg.norm(algo.state.tensors[c0])
-    setup = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    algo.run_one_time_step()
-    sweep = time.perf_counter() - t0
+    form and initial environments untimed), with the time of every operation
+    class, beside the per-operation model's prediction for the same sweep
+    (counts from the chi=8 dry run times the isolated timings)."""
+    seconds = {}
+    full_counts = oracle_schedule_counts(args.arm, args.tol, args.dt, chi=args.chi, seconds=seconds)
+    sweep = seconds.pop("sweep")
+    depth = seconds.pop("krylov_depth_mean")
     counts = oracle_schedule_counts(args.arm, args.tol, args.dt)
     times = oracle_op_times(args.chi)
     model = model_sweep_seconds(counts, times)
+    per_class = {}
+    for key in sorted(set(full_counts) | set(counts), key=str):
+        per_class[f"{key[0]}/{key[1]}"] = {
+            "measured_s": seconds.get(key, 0.0), "count": full_counts.get(key, 0),
+            "model_s": counts.get(key, 0) * times.get(key, 0.0), "model_count": counts.get(key, 0)}
     return {"metric": metric_name(args) + " -- one complete oracle sweep", "value": 1.0 / sweep,
-            "unit": "sweeps/s", "seconds": sweep, "setup_seconds": setup, "model_seconds": model,
+            "unit": "sweeps/s", "seconds": sweep, "model_seconds": model,
             "model_error_relative": (model - sweep) / sweep, "cores": os.cpu_count(),
-            "krylov_depth_mean": float(np.mean(algo.krylov_dims)) if algo.krylov_dims else None,
-            "impl": "reference", "config": config(args, "plain complex128 (CPU)")}
+            "seconds_in_classes": sum(v for v in seconds.values()), "per_class": per_class,
+            "krylov_depth_mean": depth, "impl": "reference", "config": config(args, "plain complex128 (CPU)")}
 
 
 def run_fidelity(args):
@@ -946,21 +964,19 @@ def run_two_site(args):
 def run_disorder(args):
     """Independent realisations of second-order two-site TDVP on the 31-site
     binary tree (Heisenberg + random fields h_i ~ U[-2, 2], Neel start),
-    max_bond_dim cycling through 8, 16, 32, 64 over the realisations,
+    max_bond_dim cycling through 8, 16, 32, 64, 128 over the realisations,
     cutoff 1e-9, dt = 0.05; ``--steps`` time steps each (one step = a forward
-    and a backward sweep). Runs them one worker at a time, then with
-    ``--workers`` concurrent streams, and reports realisation-steps/s."""
+    and a backward sweep), each realisation's driver built inside the timed
+    region. Timed three ways: one worker thread, ``--workers`` threads on their
+    own streams, and ``--processes`` spawned worker processes on the same GPU
+    (pool started and warmed before the timed region). value = the fastest."""
+    import functools
     import torch
     import pytreenet_gb300 as P
-    from pytreenet_gb300.workloads import binary_neel_random_field
-    caps = [8, 16, 32, 64]
-
-    def make(i):
-        st, H, _, _, _ = binary_neel_random_field(n=31, seed=i)
-        cfg = P.TwoSiteTDVPConfig(time_evo_mode=P.TimeEvoMode.KRYLOV, max_bond_dim=caps[i % len(caps)],
-                                  rel_tol=1e-9, total_tol=1e-9)
-        return P.SecondOrderTwoSiteTDVP(st, H, 0.05, 100.0, {}, config=cfg, solver_options={"krylov_tol": 1e-10},
-                                        precision=args.precision)
+    from pytreenet_gb300.batch import realisation_pool
+    from pytreenet_gb300.workloads import disorder_realisation, realisation_bond_dims
+    caps = (8, 16, 32, 64, 128)
+    make = functools.partial(disorder_realisation, caps=caps, precision=args.precision)
     out = {}
     for w in (1, args.workers):
         P.run_realisations(make, min(w, args.realisations), 1, workers=w)      # warm-up
@@ -968,17 +984,30 @@ def run_disorder(args):
         t0 = time.perf_counter()
         P.run_realisations(make, args.realisations, args.steps, workers=w)
         torch.cuda.synchronize()
-        out[w] = args.realisations * args.steps / (time.perf_counter() - t0)
-    return {"metric": "two-site TDVP realisation-steps/sec (31-site binary tree, random fields, chi_max 8..64)",
-            "value": out[args.workers], "unit": "realisation-steps/s", "n_gpus": 1, "steps": args.steps,
+        out[f"threads_{w}"] = args.realisations * args.steps / (time.perf_counter() - t0)
+    if args.processes > 1:
+        pool = realisation_pool(args.processes)
+        try:
+            P.run_realisations(make, args.processes, 1, workers=1, on_done=realisation_bond_dims, pool=pool)
+            t0 = time.perf_counter()
+            P.run_realisations(make, args.realisations, args.steps, workers=1, on_done=realisation_bond_dims,
+                               pool=pool)
+            out[f"processes_{args.processes}"] = args.realisations * args.steps / (time.perf_counter() - t0)
+        finally:
+            pool.close()
+            pool.join()
+    best = max(out, key=out.get)
+    return {"metric": "two-site TDVP realisation-steps/sec (31-site binary tree, random fields, chi_max 8..128)",
+            "value": out[best], "unit": "realisation-steps/s", "n_gpus": 1, "steps": args.steps,
             "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "bf16x6 split contractions / f64 Krylov+QR+SVD" if args.precision == "mixed" else "c128 (fp64)",
             "data": "synthetic",
             "config": {"workload": f"{args.realisations} realisations x 31-site binary tree, Heisenberg + "
                                    "h_i~U[-2,2], Neel start, second-order 2TDVP, dt=0.05, cutoff 1e-9, "
-                                   "max_bond_dim 8/16/32/64", "workers": args.workers,
+                                   "max_bond_dim 8/16/32/64/128", "workers": args.workers,
+                       "processes": args.processes, "best": best,
                        "timing": "wall clock over all realisations, includes building each driver"},
-            "one_worker": out[1], "speedup_over_one_worker": out[args.workers] / out[1]}
+            "rates": out, "speedup_over_one_thread": out[best] / out["threads_1"]}
 
 
 def run_gradient(args):

@@ -391,8 +391,7 @@ inline unsigned grid1(int64_t n) {
 // The same Householder steps as hh_fact_small / extract_r_small / hh_form_small,
 // with the same arithmetic per column (thread-to-row map, reduction tree,
 // scalar formulas), so the results are the same bits; but all of them run in
-// one launch, with one barrier per block reduction (hp_sum1 / hp_sum2) and
-// the reflector scalars formed by every thread. CTA b owns a few columns (snake order, so the Q formation work
+// one launch. CTA b owns a few columns (snake order, so the Q formation work
 // -- column c needs c + 1 reflectors -- is balanced) and keeps them in shared
 // memory. Reflector j is computed once, by the owner of column j, as soon as
 // column j has received reflectors 0 .. j-1, and published through V, tau and
@@ -401,38 +400,6 @@ inline unsigned grid1(int64_t n) {
 // publishes reflector j + 1 right away, so the chain of dependent steps costs
 // one flag hand-over each instead of one kernel launch.
 constexpr long long HP_WAIT_CYCLES = 4000000000LL;   // ~2 s at 2 GHz
-constexpr int HP_NW = ST / 32;
-
-// block_sum's arithmetic (warp tree, warp sums added in warp order from 0.0)
-// with one barrier: lane 0 of each warp stores its sum in one of two
-// alternating buffers and every thread adds them itself. Two reductions apart,
-// a buffer is reused only after a barrier every thread has passed after
-// reading it.
-__device__ __forceinline__ double hp_sum1(double v, double (*red)[HP_NW], int& rb) {
-  v = warp_sum(v);
-  if ((threadIdx.x & 31) == 0) red[rb][threadIdx.x >> 5] = v;
-  __syncthreads();
-  double s = 0.0;
-#pragma unroll
-  for (int q = 0; q < HP_NW; ++q) s += red[rb][q];
-  rb ^= 1;
-  return s;
-}
-
-__device__ __forceinline__ double2 hp_sum2(double2 v, double2 (*red)[HP_NW], int& rb) {
-  v.x = warp_sum(v.x);
-  v.y = warp_sum(v.y);
-  if ((threadIdx.x & 31) == 0) red[rb][threadIdx.x >> 5] = v;
-  __syncthreads();
-  double sx = 0.0, sy = 0.0;
-#pragma unroll
-  for (int q = 0; q < HP_NW; ++q) {
-    sx += red[rb][q].x;
-    sy += red[rb][q].y;
-  }
-  rb ^= 1;
-  return make_double2(sx, sy);
-}
 
 struct HPArgs {
   double2* A;
@@ -459,10 +426,10 @@ __device__ __forceinline__ int hp_owner(int64_t c, int G) {
 
 __global__ void __launch_bounds__(ST) hh_persistent_kernel(HPArgs a) {
   extern __shared__ double2 hsm[];           // [cpc][m] own columns, then [m] reflector
-  __shared__ double redn[2][HP_NW];
-  __shared__ double2 red2[2][HP_NW];
+  __shared__ double red[ST / 32 + 1];
+  __shared__ double2 red2[ST / 32 + 1];
+  __shared__ double2 sc[2];
   __shared__ int abort_s;
-  int rn = 0, r2 = 0;
   const int b = blockIdx.x, tid = threadIdx.x, G = a.G;
   const int64_t m = a.m, k = a.k, p = a.p, cs = a.cs;
   double2* vs = hsm + (int64_t)a.cpc * m;
@@ -475,34 +442,36 @@ __global__ void __launch_bounds__(ST) hh_persistent_kernel(HPArgs a) {
   if (tid == 0) abort_s = 0;
   __syncthreads();
 
-  // zlarfg on column j (own slot col) and publication of v_j, tau_j, beta_j;
-  // every thread forms the same scalars (no broadcast)
+  // zlarfg on column j (own slot col) and publication of v_j, tau_j, beta_j
   auto publish = [&](int64_t j, const double2* col) {
     const int64_t len = m - j;
     double acc = 0.0;
     for (int64_t t = tid; t < len; t += ST)
       if (t > 0) acc += cabs2(col[j + t]);
-    const double xn2 = hp_sum1(acc, redn, rn);
-    const double2 alpha = col[j];
-    const double xnorm = sqrt(xn2);
-    double2 t_, s_, b_;
-    if (xnorm == 0.0 && alpha.y == 0.0) {
-      t_ = make_double2(0.0, 0.0);
-      s_ = make_double2(0.0, 0.0);
-      b_ = alpha;
-    } else {
-      const double nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xnorm * xnorm);
-      const double beta = (alpha.x >= 0.0) ? -nrm : nrm;
-      t_ = make_double2((beta - alpha.x) / beta, -alpha.y / beta);
-      const double2 d = make_double2(alpha.x - beta, alpha.y);
-      const double den = d.x * d.x + d.y * d.y;
-      s_ = make_double2(d.x / den, -d.y / den);
-      b_ = make_double2(beta, 0.0);
-    }
+    const double xn2 = block_sum<ST>(acc, red);
     if (tid == 0) {
+      const double2 alpha = col[j];
+      const double xnorm = sqrt(xn2);
+      double2 t_, s_, b_;
+      if (xnorm == 0.0 && alpha.y == 0.0) {
+        t_ = make_double2(0.0, 0.0);
+        s_ = make_double2(0.0, 0.0);
+        b_ = alpha;
+      } else {
+        const double nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xnorm * xnorm);
+        const double beta = (alpha.x >= 0.0) ? -nrm : nrm;
+        t_ = make_double2((beta - alpha.x) / beta, -alpha.y / beta);
+        const double2 d = make_double2(alpha.x - beta, alpha.y);
+        const double den = d.x * d.x + d.y * d.y;
+        s_ = make_double2(d.x / den, -d.y / den);
+        b_ = make_double2(beta, 0.0);
+      }
+      sc[1] = s_;
       a.tau[j] = t_;
       a.betas[j] = b_;
     }
+    __syncthreads();
+    const double2 s_ = sc[1];
     for (int64_t t = tid; t < len; t += ST)
       a.V[j * m + j + t] = (t == 0) ? make_double2(1.0, 0.0) : cmul(col[j + t], s_);
     __threadfence();
@@ -530,10 +499,11 @@ __global__ void __launch_bounds__(ST) hh_persistent_kernel(HPArgs a) {
     __syncthreads();
     if (abort_s) break;
     const int64_t len = m - j;
-    // v_j and tau_j in one round trip to L2; each thread reads back only the
-    // rows it stored, so no barrier is needed before they are used
-    double2 f = __ldcg(a.tau + j);
+    // v_j and tau_j in one round trip to L2
+    if (tid == 0) sc[0] = __ldcg(a.tau + j);
     for (int64_t t = tid; t < len; t += ST) vs[t] = __ldcg(a.V + j * m + j + t);
+    __syncthreads();
+    double2 f = sc[0];
     f.y = -f.y;  // conj(tau): the factorisation applies H^H
     for (int i = 0; i < nown; ++i) {
       const int64_t c = hp_col(b, i, G);
@@ -541,16 +511,14 @@ __global__ void __launch_bounds__(ST) hh_persistent_kernel(HPArgs a) {
       double2* col = hsm + i * m;
       double2 w = make_double2(0.0, 0.0);
       for (int64_t t = tid; t < len; t += ST) w = cfmac(vs[t], col[j + t], w);
-      w = hp_sum2(w, red2, r2);
+      w = block_sum2_fused<ST>(w, red2);
       const double2 fw = cmul(f, w);
       for (int64_t t = tid; t < len; t += ST) col[j + t] = csub(col[j + t], cmul(vs[t], fw));
-      if (c == j + 1 && j + 1 < p) {
-        __syncthreads();             // publish reads the column with the next step's row map
-        publish(j + 1, col);
-      }
+      __syncthreads();
+      if (c == j + 1 && j + 1 < p) publish(j + 1, col);
     }
+    __syncthreads();
   }
-  __syncthreads();                   // the last step's updates, before R and Q read the columns
   if (abort_s) {
     if (b == 0 && tid == 0) a.R[0] = make_double2(NAN, NAN);   // the result is not usable
     return;
@@ -619,7 +587,7 @@ __global__ void __launch_bounds__(ST) hh_persistent_kernel(HPArgs a) {
       }
       double2 w = make_double2(0.0, 0.0);
       for (int64_t t = j + tid; t < m; t += ST) w = cfmac(vs[t], col[t], w);
-      w = hp_sum2(w, red2, r2);
+      w = block_sum2_fused<ST>(w, red2);
       const double2 fw = cmul(t_, w);
       for (int64_t t = j + tid; t < m; t += ST) col[t] = csub(col[t], cmul(vs[t], fw));
       __syncthreads();

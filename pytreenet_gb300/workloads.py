@@ -233,3 +233,22 @@ def binary_neel_random_field(n: int = 31, seed: int = 0, h: float = 2.0):
     fields = {nid: rng.uniform(-h, h) for nid, _ in spec}
     H = heisenberg_ttno(st, fields)
     return st, H, spec, tensors, {nid: H.phys(nid) for nid in st._order}
+
+
+def disorder_realisation(i: int, caps=(8, 16, 32, 64), precision: str = "mixed", n: int = 31, h: float = 2.0,
+                         dt: float = 0.05, cutoff: float = 1e-9):
+    """Realisation i of the disorder average: ``binary_neel_random_field``
+    (seed i) under second-order two-site TDVP with max_bond_dim
+    caps[i mod len(caps)] and rel_tol = total_tol = cutoff. Module-level, so
+    worker processes can build it (``run_realisations(..., processes=P)``)."""
+    from .tdvp import SecondOrderTwoSiteTDVP, TimeEvoMode, TwoSiteTDVPConfig
+    st, H, _, _, _ = binary_neel_random_field(n=n, seed=i, h=h)
+    cfg = TwoSiteTDVPConfig(time_evo_mode=TimeEvoMode.KRYLOV, max_bond_dim=caps[i % len(caps)],
+                            rel_tol=cutoff, total_tol=cutoff)
+    return SecondOrderTwoSiteTDVP(st, H, dt, 1000 * dt, {}, config=cfg, solver_options={"krylov_tol": 1e-10},
+                                  precision=precision)
+
+
+def realisation_bond_dims(i: int, algo) -> dict:
+    """The bond dimensions of a finished realisation (a picklable result)."""
+    return dict(algo.state.bond_dims())

@@ -317,6 +317,42 @@ def test_engine_host_realisations_concurrent_equals_sequential(monkeypatch):
     assert seq[0][0] != seq[1][0] or any(not np.array_equal(seq[0][1][k], seq[1][1][k]) for k in seq[0][1])
 
 
+_CHILD_STANDIN = None
+
+
+def _standin_disorder_make(i):
+    """Realisation builder for a spawned worker process: the process starts
+    without the CPU stand-in for the library, so it installs it first."""
+    global _CHILD_STANDIN
+    if _CHILD_STANDIN is None:
+        _CHILD_STANDIN = pytest.MonkeyPatch()
+        fake_ptn.install(_CHILD_STANDIN)
+    from pytreenet_gb300.workloads import disorder_realisation
+    return disorder_realisation(i, caps=(2, 4), precision="plain", n=7)
+
+
+def _realisation_result(i, algo):
+    return (list(algo.bond_dims_history), {nid: algo.state.get_phys_numpy(nid).copy() for nid in algo.state._order})
+
+
+def test_realisations_in_worker_processes_equal_sequential(monkeypatch):
+    """run_realisations over two spawned worker processes returns, in
+    realisation order, exactly the results of running the realisations one
+    after the other in this process; without on_done it refuses."""
+    fake_ptn.install(monkeypatch)
+    import pytreenet_gb300 as P
+    from pytreenet_gb300.workloads import disorder_realisation
+    seq = P.run_realisations(lambda i: disorder_realisation(i, caps=(2, 4), precision="plain", n=7), 4, 2,
+                             workers=1, on_done=_realisation_result)
+    par = P.run_realisations(_standin_disorder_make, 4, 2, workers=1, on_done=_realisation_result, processes=2)
+    for (h1, s1), (h2, s2) in zip(seq, par):
+        assert h1 == h2
+        for nid in s1:
+            np.testing.assert_array_equal(s1[nid], s2[nid])
+    with pytest.raises(ValueError):
+        P.run_realisations(_standin_disorder_make, 2, 1, processes=2)
+
+
 def test_contraction_helpers_match_oracle(monkeypatch):
     """SandwichCache / contract_ket_ham_with_envs / contract_any /
     effective_single_site_evolution in the reference's conventions, against the

@@ -549,11 +549,13 @@ def run_breakdown(args):
         saved[name] = orig
 
         def timed(self, *a, **kw):
+            k = f"{name}:{key(*a)}"
             torch.cuda.synchronize()
+            torch.cuda.nvtx.range_push(k)      # ncu --nvtx-include "<name>:<class>/" selects one class
             t = time.perf_counter()
             r = orig(self, *a, **kw)
             torch.cuda.synchronize()
-            k = f"{name}:{key(*a)}"
+            torch.cuda.nvtx.range_pop()
             acc[k] += time.perf_counter() - t
             cnt[k] += 1
             return r

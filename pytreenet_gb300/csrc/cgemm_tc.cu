@@ -356,11 +356,20 @@ int make_map_3d(CUtensorMap* map, const void* base, uint64_t d0, uint64_t d1, ui
 
 // ---- conversions ---------------------------------------------------------------------
 // planes[p][m * lda + k] <- split(src[off_m(m) + off_k(k)]) for the complex128 source.
+// x ~ out[0] + ... + out[L-1] in BF16 pieces. Only the first remainder needs
+// double precision: x - bf16(x) is exact in FP64 (Sterbenz) and is rounded
+// once to FP32 (error <= 2^-32 |x|, below the 2^-25 |x| the three pieces
+// leave); the later pieces are split in FP32. GB300 issues FP64 at 1/64 of the
+// FP32 rate, and a split done wholly in FP64 made the conversion of the χ=256
+// root vector FP64-bound (0.93 ms for 33.5 M entries).
 __device__ __forceinline__ void split_levels(double x, int L, __nv_bfloat16* out) {
-  for (int lv = 0; lv < L; ++lv) {
-    const __nv_bfloat16 b = __double2bfloat16(x);
+  const __nv_bfloat16 b0 = __double2bfloat16(x);
+  out[0] = b0;
+  float r = (float)(x - (double)__bfloat162float(b0));
+  for (int lv = 1; lv < L; ++lv) {
+    const __nv_bfloat16 b = __float2bfloat16_rn(r);
     out[lv] = b;
-    x -= (double)__bfloat162float(b);
+    r -= __bfloat162float(b);
   }
 }
 

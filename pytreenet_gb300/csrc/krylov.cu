@@ -205,9 +205,24 @@ __global__ void __launch_bounds__(RT) gs_pass_kernel(const double2* __restrict__
   __syncthreads();
   if (!last) return;
   __threadfence();
-  if (threadIdx.x < nq || threadIdx.x == NQ) {
-    double2 t = make_double2(0.0, 0.0);
-    for (unsigned b = 0; b < gridDim.x; ++b) t = cadd(t, __ldcg(partial + (int64_t)b * (NQ + 1) + threadIdx.x));
+  // The CTAs' partial sums, added in CTA order by one thread per value (the
+  // order fixes the bits); they are staged through shared memory in chunks of
+  // GS_STAGE CTAs, loaded by every thread at once, so the adds wait on shared
+  // memory instead of one L2 round trip each.
+  constexpr int GS_STAGE = 64;
+  __shared__ double2 stage[GS_STAGE * (NQ + 1)];
+  double2 t = make_double2(0.0, 0.0);
+  const bool mine_v = threadIdx.x < nq || threadIdx.x == NQ;
+  for (unsigned b0 = 0; b0 < gridDim.x; b0 += GS_STAGE) {
+    const unsigned cnt = gridDim.x - b0 < GS_STAGE ? gridDim.x - b0 : GS_STAGE;
+    for (unsigned e = threadIdx.x; e < cnt * (NQ + 1); e += RT)
+      stage[e] = __ldcg(partial + (int64_t)b0 * (NQ + 1) + e);
+    __syncthreads();
+    if (mine_v)
+      for (unsigned b = 0; b < cnt; ++b) t = cadd(t, stage[b * (NQ + 1) + threadIdx.x]);
+    __syncthreads();
+  }
+  if (mine_v) {
     if (threadIdx.x == NQ) {
       if (mode != 1) nout[0] = sqrt(t.x);
     } else if (mode != 2) {

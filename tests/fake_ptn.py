@@ -149,11 +149,15 @@ def _bf16_val(bits):
 
 
 def _split_levels(v, L):
-    out = []
-    for _ in range(L):
-        b = _bf16_bits(v)
+    # the library's split: the first piece from the double, its remainder
+    # (exact in double) rounded once to FP32, the later pieces split in FP32
+    b = _bf16_bits(v)
+    out = [b]
+    r = (v - _bf16_val(b)).astype(np.float32)
+    for _ in range(1, L):
+        b = _bf16_bits(r)
         out.append(b)
-        v = v - _bf16_val(b)
+        r = (r - _bf16_val(b).astype(np.float32)).astype(np.float32)
     return out
 
 

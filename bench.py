@@ -360,7 +360,7 @@ def _measured_peak(kind: str):
 # E2: dram__bytes_read.sum + dram__bytes_write.sum from one ncu capture,
 # profiles/cgemm_bf16x6_root_matvec_chi256.md); the W step and the operand
 # conversions are not included.
-ROOT_MATVEC_DRAM_BYTES = 22.49e9
+ROOT_MATVEC_DRAM_BYTES = 17.60e9
 
 
 def run_gb300(args, rank, world):

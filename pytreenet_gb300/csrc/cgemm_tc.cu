@@ -557,13 +557,12 @@ __global__ void splitk_reduce_kernel(const float2* __restrict__ partial, int spl
       static_cast<double2*>(C)[o] = make_double2(re, im);
     } else {
       __nv_bfloat16* Cb = static_cast<__nv_bfloat16*>(C);
+      __nv_bfloat16 rb[3], ib[3];
+      split_levels(re, L, rb);
+      split_levels(im, L, ib);
       for (int lv = 0; lv < L; ++lv) {
-        const __nv_bfloat16 rb = __double2bfloat16(re);
-        const __nv_bfloat16 ib = __double2bfloat16(im);
-        Cb[(2 * lv) * c_plane + o] = rb;
-        Cb[(2 * lv + 1) * c_plane + o] = ib;
-        re -= (double)__bfloat162float(rb);
-        im -= (double)__bfloat162float(ib);
+        Cb[(2 * lv) * c_plane + o] = rb[lv];
+        Cb[(2 * lv + 1) * c_plane + o] = ib[lv];
       }
     }
   }

@@ -535,6 +535,92 @@ __global__ void __launch_bounds__(SMALLK_T)
   }
 }
 
+// The same product for BF16-plane outputs whose rows come in adjacent pairs:
+// thread t computes rows 2t and 2t + 1 and stores each plane entry of the pair
+// as one 4-byte bf16x2 (the host checks that the innermost row mode has
+// output stride 1 and an even extent and that every other stride is even, so
+// the pair is adjacent and 4-byte aligned). Half the store instructions, and a
+// warp writes 128 contiguous bytes per plane. Same arithmetic per output.
+template <int KK>
+__global__ void __launch_bounds__(SMALLK_T)
+    cgemm_smallk_pair_kernel(const __nv_bfloat16* __restrict__ A, int64_t lda, int64_t a_plane,
+                             const __nv_bfloat16* __restrict__ Bx, int64_t ldb, GemmArgs g, int L) {
+  __shared__ float2 sB[SMALLK_MAX_N * KK];
+  __shared__ int64_t noff[SMALLK_MAX_N];
+  if (*(volatile int32_t*)g.status != 0) return;
+  const int N = (int)g.N;
+  const int64_t blk = (int64_t)N * ldb;
+  for (int e = threadIdx.x; e < N * KK; e += SMALLK_T) {
+    const int n = e / KK, kk = e - n * KK;
+    float re = 0.f, im = 0.f;
+    for (int lv = 0; lv < L; ++lv) {
+      re += __bfloat162float(Bx[(3 * lv + 1) * blk + (int64_t)n * ldb + kk]);
+      im += __bfloat162float(Bx[(3 * lv + 2) * blk + (int64_t)n * ldb + kk]);
+    }
+    sB[n * KK + kk] = make_float2(re, im);
+  }
+  for (int n = threadIdx.x; n < N; n += SMALLK_T) noff[n] = decode_off(g.no, n);
+  __syncthreads();
+  const int64_t pairs = g.M / 2;
+  for (int64_t pr = blockIdx.x * (int64_t)SMALLK_T + threadIdx.x; pr < pairs;
+       pr += (int64_t)gridDim.x * SMALLK_T) {
+    const int64_t m = 2 * pr;
+    float2 a0[KK], a1[KK];
+#pragma unroll
+    for (int kk = 0; kk < KK; ++kk) {
+      float r0 = 0.f, i0 = 0.f, r1 = 0.f, i1 = 0.f;
+      for (int lv = 0; lv < L; ++lv) {
+        r0 += __bfloat162float(A[(2 * lv) * a_plane + m * lda + kk]);
+        i0 += __bfloat162float(A[(2 * lv + 1) * a_plane + m * lda + kk]);
+        r1 += __bfloat162float(A[(2 * lv) * a_plane + (m + 1) * lda + kk]);
+        i1 += __bfloat162float(A[(2 * lv + 1) * a_plane + (m + 1) * lda + kk]);
+      }
+      a0[kk] = make_float2(r0, i0);
+      a1[kk] = make_float2(r1, i1);
+    }
+    const int64_t moff = decode_off(g.mo, m);
+    __nv_bfloat16* C = static_cast<__nv_bfloat16*>(g.C);
+    for (int n = 0; n < N; ++n) {
+      float cr0 = 0.f, ci0 = 0.f, cr1 = 0.f, ci1 = 0.f;
+#pragma unroll
+      for (int kk = 0; kk < KK; ++kk) {
+        const float2 b = sB[n * KK + kk];
+        cr0 = fmaf(a0[kk].x, b.x, cr0);
+        cr0 = fmaf(-a0[kk].y, b.y, cr0);
+        ci0 = fmaf(a0[kk].x, b.y, ci0);
+        ci0 = fmaf(a0[kk].y, b.x, ci0);
+        cr1 = fmaf(a1[kk].x, b.x, cr1);
+        cr1 = fmaf(-a1[kk].y, b.y, cr1);
+        ci1 = fmaf(a1[kk].x, b.y, ci1);
+        ci1 = fmaf(a1[kk].y, b.x, ci1);
+      }
+      const int64_t o = moff + noff[n];
+      for (int lv = 0; lv < L; ++lv) {
+        const __nv_bfloat16 rb0 = __float2bfloat16_rn(cr0), ib0 = __float2bfloat16_rn(ci0);
+        const __nv_bfloat16 rb1 = __float2bfloat16_rn(cr1), ib1 = __float2bfloat16_rn(ci1);
+        *reinterpret_cast<__nv_bfloat162*>(C + (2 * lv) * g.c_plane + o) = __halves2bfloat162(rb0, rb1);
+        *reinterpret_cast<__nv_bfloat162*>(C + (2 * lv + 1) * g.c_plane + o) = __halves2bfloat162(ib0, ib1);
+        cr0 -= __bfloat162float(rb0);
+        ci0 -= __bfloat162float(ib0);
+        cr1 -= __bfloat162float(rb1);
+        ci1 -= __bfloat162float(ib1);
+      }
+    }
+  }
+}
+
+// Whether the rows of a BF16-plane output come in adjacent, 4-byte aligned
+// pairs (cgemm_smallk_pair_kernel).
+static bool smallk_pairs_ok(const GemmArgs& g, int64_t M) {
+  if (g.out_kind != 1 || M < 2 || M % 2 || g.mo.n < 1 || (g.c_plane & 1)) return false;
+  if (g.mo.stride[g.mo.n - 1] != 1 || g.mo.dim[g.mo.n - 1] % 2) return false;
+  for (int i = 0; i + 1 < g.mo.n; ++i)
+    if (g.mo.stride[i] & 1) return false;
+  for (int i = 0; i < g.no.n; ++i)
+    if (g.no.stride[i] & 1) return false;
+  return true;
+}
+
 // Sum of the split-K partial sums (FP64, ranges in order: deterministic),
 // written like the GEMM epilogue: complex128 through the output modes, or as
 // BF16 level planes.
@@ -671,6 +757,23 @@ extern "C" int ptn_cgemm_bf16x3(const ptn_cgemm_desc* d, void* stream) {
     const __nv_bfloat16* A = static_cast<const __nv_bfloat16*>(d->A);
     const __nv_bfloat16* B = static_cast<const __nv_bfloat16*>(d->Bx);
     cudaStream_t st = ptn_stream(stream);
+    if (smallk_pairs_ok(g, d->M)) {
+      int64_t pb = (d->M / 2 + SMALLK_T - 1) / SMALLK_T;
+      if (pb > 152 * 16) pb = 152 * 16;
+      switch (d->K) {
+#define PTN_SMALLK_PAIR(k)                                                                                     \
+  case k:                                                                                                       \
+    cgemm_smallk_pair_kernel<k><<<(unsigned)pb, SMALLK_T, 0, st>>>(A, d->lda, d->a_plane, B, d->ldb, g, d->levels); \
+    return ptn_launch_status();
+        PTN_SMALLK_PAIR(2)
+        PTN_SMALLK_PAIR(4)
+        PTN_SMALLK_PAIR(6)
+        PTN_SMALLK_PAIR(10)
+#undef PTN_SMALLK_PAIR
+        default:
+          break;
+      }
+    }
     switch (d->K) {
 #define PTN_SMALLK_CASE(k)                                                                              \
   case k:                                                                                               \

@@ -255,3 +255,35 @@ def test_cgemm_split_k_into_planes(lib):
     ref = (A @ B.T) @ D
     err = np.max(np.abs(C.cpu().numpy() - ref)) / (np.sqrt(K) * np.sqrt(N))
     assert err < 2e-6, err
+
+
+@pytest.mark.parametrize("K", [2, 4, 6, 10, 7, 20])
+def test_cgemm_small_k_chain_matches_fp64(lib, K):
+    """Products with K <= 32 run on the CUDA-core kernel compiled for their K
+    (7 takes the generic instance); when the next step contracts the inner
+    row leg of this step's output, the rows come in adjacent pairs and the
+    paired kernel writes bf16x2 (K = 2, 4, 6, 10). Chain
+    T[m1, m2, n] = sum_k A[m1, m2, k] B[n, k], then sum_m2 T[m1, m2, n] D[m2, p],
+    on the tensor-core path against the FP64 plan."""
+    from pytreenet_gb300.engine import Operand, ChainBuilder, Workspace
+    m1, m2, N, P = 96, 38, 50, 24
+    A, B, D = crandn(m1, m2, K), crandn(N, K), crandn(m2, P)
+    Ad, Bd, Dd = (torch.from_numpy(x).cuda() for x in (A, B, D))
+    outs = []
+    for mixed in (True, False):
+        C = torch.zeros((m1, N, P), dtype=torch.complex128, device="cuda")
+        ws = Workspace("cuda")
+        cb = ChainBuilder(ws)
+        T = cb.contract(Operand.contiguous(("fixed", Ad), ["a", "b", "k"], [m1, m2, K]),
+                        Operand.contiguous(("fixed", Bd), ["n", "k"], [N, K]), ["k"])
+        cb.contract(T, Operand.contiguous(("fixed", Dd), ["b", "p"], [m2, P]), ["b"],
+                    out=Operand.contiguous(("fixed", C), ["a", "n", "p"], [m1, N, P]))
+        p = cb.mixed_plan(3) if mixed else cb.plan()
+        p.run()
+        torch.cuda.synchronize()
+        if mixed:
+            assert int(ws.bufs["tc_status"].item()) == 0
+        outs.append(C.cpu().numpy())
+    ref = np.einsum("abk,nk,bp->anp", A, B, D)
+    assert np.max(np.abs(outs[1] - ref)) < 1e-10 * np.max(np.abs(ref))
+    assert np.max(np.abs(outs[0] - outs[1])) < 2e-6 * np.max(np.abs(ref))

@@ -621,7 +621,7 @@ static bool smallk_pairs_ok(const GemmArgs& g, int64_t M) {
   return true;
 }
 
-// Sum of the split-K partial sums (FP64, ranges in order: deterministic),
+// Sum of the split-K partial sums (compensated FP32, ranges in order: deterministic),
 // written like the GEMM epilogue: complex128 through the output modes, or as
 // BF16 level planes.
 __global__ void splitk_reduce_kernel(const float2* __restrict__ partial, int splits, int64_t M, int64_t N,
@@ -632,12 +632,20 @@ __global__ void splitk_reduce_kernel(const float2* __restrict__ partial, int spl
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
        e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t m = e / N, n = e - (e / N) * N;
-    double re = 0.0, im = 0.0;
+    // compensated (Kahan) sums in FP32, ranges in order: the FP32 pipe runs at
+    // 64x the FP64 rate on GB300, and the compensation keeps the error at the
+    // level of the partials' own rounding
+    float sr = 0.f, si = 0.f, cr = 0.f, ci = 0.f;
     for (int s = 0; s < splits; ++s) {
       const float2 p = partial[((int64_t)s * M + m) * N + n];
-      re += (double)p.x;
-      im += (double)p.y;
+      const float yr = p.x - cr, yi = p.y - ci;
+      const float tr = sr + yr, ti = si + yi;
+      cr = (tr - sr) - yr;
+      ci = (ti - si) - yi;
+      sr = tr;
+      si = ti;
     }
+    const double re = (double)sr - (double)cr, im = (double)si - (double)ci;
     const int64_t o = decode_off(mo, m) + decode_off(no, n);
     if (out_kind == 0) {
       static_cast<double2*>(C)[o] = make_double2(re, im);

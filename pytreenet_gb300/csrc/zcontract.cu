@@ -170,6 +170,7 @@ constexpr int64_t SMALL_MIN_K = 64;
 
 __global__ void __launch_bounds__(SMALL_THREADS) zcontract_small_kernel(const ContractArgs a) {
   __shared__ double2 part[SMALL_THREADS];
+  __shared__ int64_t offAk[SMALL_THREADS], offBk[SMALL_THREADS];
   const int tid = threadIdx.x;
   const int64_t outs = a.M * a.N;
   int P = 1;
@@ -177,21 +178,35 @@ __global__ void __launch_bounds__(SMALL_THREADS) zcontract_small_kernel(const Co
   const int G = SMALL_THREADS / P;
   const int o = tid / G, g = tid - o * G;
   double2 acc = make_double2(0.0, 0.0);
-  int64_t ocm = 0, ocn = 0;
+  int64_t oa = 0, ob = 0, ocm = 0, ocn = 0;
   if (o < outs) {
     const int64_t mi = o / a.N, ni = o - mi * a.N;
-    int64_t oa, ob;
     decode(a.m, mi, oa, ocm);
     decode(a.n, ni, ob, ocn);
-    for (int64_t k = g; k < a.K; k += G) {
-      int64_t ka, kb;
-      decode(a.k, k, ka, kb);
-      double2 x = a.A[oa + ka];
-      double2 y = a.B[kb + ob];
-      if (a.conj_a) x.y = -x.y;
-      if (a.conj_b) y.y = -y.y;
-      acc = cfma(x, y, acc);
+  }
+  // the K offsets of a chunk of SMALL_THREADS indices are decoded once, one
+  // per thread; each lane still takes k = g, g + G, ... in increasing order
+  // (G divides the chunk)
+  for (int64_t k0 = 0; k0 < a.K; k0 += SMALL_THREADS) {
+    {
+      const int64_t k = k0 + tid;
+      int64_t x = 0, y = 0;
+      if (k < a.K) decode(a.k, k, x, y);
+      offAk[tid] = x;
+      offBk[tid] = y;
     }
+    __syncthreads();
+    if (o < outs) {
+      const int cnt = (int)(a.K - k0 < SMALL_THREADS ? a.K - k0 : SMALL_THREADS);
+      for (int kk = g; kk < cnt; kk += G) {
+        double2 x = a.A[oa + offAk[kk]];
+        double2 y = a.B[offBk[kk] + ob];
+        if (a.conj_a) x.y = -x.y;
+        if (a.conj_b) y.y = -y.y;
+        acc = cfma(x, y, acc);
+      }
+    }
+    __syncthreads();
   }
   part[tid] = acc;
   __syncthreads();
@@ -210,7 +225,55 @@ __global__ void __launch_bounds__(SMALL_THREADS) zcontract_small_kernel(const Co
   }
 }
 
-// C <- beta * C (zero when beta == 0) over the M x N output positions.
+// Products with fewer output tiles than SMs (and no K split): the tiled
+// kernel would put a whole 64 x 64 tile -- most of it padding when M or N is
+// small -- on each of a few SMs, at ~2 FP64 FMAs per clock per SM. Here one
+// thread owns one output and adds A[m, k] B[k, n] over k in increasing order
+// with the same complex FMA as the tiled kernel, so the result has the same
+// bits; the K offsets are decoded once per CTA into shared memory.
+constexpr int ELEM_THREADS = 64;
+
+__global__ void __launch_bounds__(ELEM_THREADS) zcontract_elem_kernel(const ContractArgs a) {
+  __shared__ int64_t offAk[ELEM_THREADS], offBk[ELEM_THREADS];
+  const int64_t o = blockIdx.x * (int64_t)ELEM_THREADS + threadIdx.x;
+  const bool valid = o < a.M * a.N;
+  int64_t oa = 0, ocm = 0, ob = 0, ocn = 0;
+  if (valid) {
+    const int64_t mi = o / a.N, ni = o - mi * a.N;
+    decode(a.m, mi, oa, ocm);
+    decode(a.n, ni, ob, ocn);
+  }
+  double2 acc = make_double2(0.0, 0.0);
+  for (int64_t k0 = 0; k0 < a.K; k0 += ELEM_THREADS) {
+    __syncthreads();
+    {
+      const int64_t k = k0 + threadIdx.x;
+      int64_t x = -1, y = -1;
+      if (k < a.K) decode(a.k, k, x, y);
+      offAk[threadIdx.x] = x;
+      offBk[threadIdx.x] = y;
+    }
+    __syncthreads();
+    const int cnt = (int)(a.K - k0 < ELEM_THREADS ? a.K - k0 : ELEM_THREADS);
+    if (valid) {
+      for (int kk = 0; kk < cnt; ++kk) {
+        double2 av = a.A[oa + offAk[kk]];
+        double2 bv = a.B[offBk[kk] + ob];
+        if (a.conj_a) av.y = -av.y;
+        if (a.conj_b) bv.y = -bv.y;
+        acc = cfma(av, bv, acc);
+      }
+    }
+  }
+  if (valid) {
+    double2* p = a.C + ocm + ocn;
+    double2 v = cmul(a.alpha, acc);
+    if (!a.beta_zero) v = cfma(a.beta, *p, v);
+    *p = v;
+  }
+}
+
+// C <- beta * C (zero when beta == 0) over the M x N output positions.// C <- beta * C (zero when beta == 0) over the M x N output positions.
 __global__ void __launch_bounds__(256) zcontract_scale_c(const ContractArgs a) {
   const int64_t total = a.M * a.N;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
@@ -291,6 +354,14 @@ extern "C" int ptn_zcontract(const ptn_contract_desc* d, void* stream) {
   if (tiles > 0x7fffffffLL) return PTN_ERR_UNSUPPORTED;
   int64_t splits = ptn_zcontract_splits(tiles, K, &a.k_chunk);
   a.split = splits > 1;
+  if (!a.split && tiles < 152) {
+    const int64_t blocks = (M * N + ELEM_THREADS - 1) / ELEM_THREADS;
+    if (blocks <= 0x7fffffffLL) {
+      PTN_COUNT(1);
+      zcontract_elem_kernel<<<(unsigned)blocks, ELEM_THREADS, 0, s>>>(a);
+      return ptn_launch_status();
+    }
+  }
   if (a.split) {
     int64_t total = M * N;
     int64_t blocks = (total + 255) / 256;

@@ -1760,6 +1760,8 @@ class DeviceNetwork:
         ``{}`` gives <psi|psi>. One entry of ``expect_many``."""
         return complex(self.expect_many([ops])[0])
 
+    OBS_PLANS_KEPT = 16           # observable plans cached per network (operator layouts)
+
     def expect_many(self, ops_list) -> np.ndarray:
         """<psi| prod_i O_i |psi> for a list of products of one-site operators
         (each a dict node -> d x d matrix acting on the physical leg; ``{}`` is
@@ -1806,6 +1808,9 @@ class DeviceNetwork:
             self._obs_plans = {}
         rec = self._obs_plans.get(key)
         if rec is None:
+            if len(self._obs_plans) >= self.OBS_PLANS_KEPT:
+                # each plan holds its own norm environments (chi^2 per edge)
+                self._obs_plans.pop(next(iter(self._obs_plans)))
             rec = self._obs_plans[key] = self._observable_plan(key)
         plan, opbuf, vals = rec
         if mats:

@@ -198,7 +198,25 @@ __global__ void __launch_bounds__(SMALL_THREADS) zcontract_small_kernel(const Co
     __syncthreads();
     if (o < outs) {
       const int cnt = (int)(a.K - k0 < SMALL_THREADS ? a.K - k0 : SMALL_THREADS);
-      for (int kk = g; kk < cnt; kk += G) {
+      // eight operand pairs loaded ahead of their (in-order) accumulation, so
+      // the loads overlap; the order of the additions is unchanged
+      constexpr int AHEAD = 8;
+      int kk = g;
+      for (; kk + (AHEAD - 1) * G < cnt; kk += AHEAD * G) {
+        double2 x[AHEAD], y[AHEAD];
+#pragma unroll
+        for (int u = 0; u < AHEAD; ++u) {
+          x[u] = a.A[oa + offAk[kk + u * G]];
+          y[u] = a.B[offBk[kk + u * G] + ob];
+        }
+#pragma unroll
+        for (int u = 0; u < AHEAD; ++u) {
+          if (a.conj_a) x[u].y = -x[u].y;
+          if (a.conj_b) y[u].y = -y[u].y;
+          acc = cfma(x[u], y[u], acc);
+        }
+      }
+      for (; kk < cnt; kk += G) {
         double2 x = a.A[oa + offAk[kk]];
         double2 y = a.B[offBk[kk] + ob];
         if (a.conj_a) x.y = -x.y;
@@ -256,7 +274,23 @@ __global__ void __launch_bounds__(ELEM_THREADS) zcontract_elem_kernel(const Cont
     __syncthreads();
     const int cnt = (int)(a.K - k0 < ELEM_THREADS ? a.K - k0 : ELEM_THREADS);
     if (valid) {
-      for (int kk = 0; kk < cnt; ++kk) {
+      // operand pairs loaded four ahead of their in-order accumulation
+      int kk = 0;
+      for (; kk + 3 < cnt; kk += 4) {
+        double2 av[4], bv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          av[u] = a.A[oa + offAk[kk + u]];
+          bv[u] = a.B[offBk[kk + u] + ob];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          if (a.conj_a) av[u].y = -av[u].y;
+          if (a.conj_b) bv[u].y = -bv[u].y;
+          acc = cfma(av[u], bv[u], acc);
+        }
+      }
+      for (; kk < cnt; ++kk) {
         double2 av = a.A[oa + offAk[kk]];
         double2 bv = a.B[offBk[kk] + ob];
         if (a.conj_a) av.y = -av.y;

@@ -14,21 +14,8 @@ constexpr int RT = 256;        // threads per CTA
 constexpr int MAXQ = 16;       // vectors per multi-dot launch
 constexpr int64_t CHUNK = 1024;   // elements per CTA: enough CTAs to keep HBM busy on 131k-entry vectors
 
-// CTAs for an n-entry vector pass. The passes are bound by the FP64 pipe of
-// each SM (about 2 FMAs per clock), so a vector of 32 k entries or more gets
-// at least one CTA per SM (at most 256 entries per CTA): 65 k-entry bond
-// vectors ran on 64 of the 152 SMs, 131 k-entry arm vectors on 128. Below
-// 32 k entries the partition -- and with it the order of every partial sum --
-// is that of CHUNK alone.
-constexpr int64_t MIN_CTAS_FROM = 32768;
-constexpr int64_t MIN_CTAS = 152;
-
 inline int64_t nblocks_for(int64_t n) {
   int64_t b = (n + CHUNK - 1) / CHUNK;
-  if (n >= MIN_CTAS_FROM) {
-    const int64_t fill = (n + 255) / 256 < MIN_CTAS ? (n + 255) / 256 : MIN_CTAS;
-    if (b < fill) b = fill;
-  }
   if (b < 1) b = 1;
   if (b > 1184) b = 1184;  // 8 CTAs per SM on 148+ SMs
   return b;

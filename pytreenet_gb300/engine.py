@@ -47,12 +47,34 @@ def _stream_ptr():
 # ----------------------------------------------------------------------------
 # workspace
 # ----------------------------------------------------------------------------
+class _BufferTable(dict):
+    """The workspace's buffers; every replacement bumps the workspace's
+    generation, so plans re-read their pointers only when one moved."""
+
+    def __init__(self, ws):
+        super().__init__()
+        self._ws = ws
+
+    def __setitem__(self, key, value):
+        super().__setitem__(key, value)
+        self._ws.gen += 1
+
+    def __delitem__(self, key):
+        super().__delitem__(key)
+        self._ws.gen += 1
+
+    def pop(self, *a):
+        self._ws.gen += 1
+        return super().pop(*a)
+
+
 class Workspace:
     """Named device scratch buffers that only grow."""
 
     def __init__(self, device):
         self.device = device
-        self.bufs: dict[str, torch.Tensor] = {}
+        self.gen = 0                    # bumped whenever a buffer is replaced
+        self.bufs: dict[str, torch.Tensor] = _BufferTable(self)
 
     def get(self, name: str, numel: int, dtype=CDT) -> torch.Tensor:
         b = self.bufs.get(name)
@@ -196,13 +218,25 @@ class _NativeOps:
             self.ops[i].desc = ctypes.addressof(d)
         self.n = len(items)
         self.ptrs = (ctypes.c_void_p * len(self.refs))()
+        self._gen = -1
+        # fixed operands that are not tensors (pointer holders whose address
+        # changes between runs) are re-read on every run
+        self._moving = [i for i in range(2, len(self.refs))
+                        if self.refs[i][0] == "fixed" and not isinstance(self.refs[i][1], torch.Tensor)]
 
     def run(self, ws, x_ptr, y_ptr):
         p = self.ptrs
         p[0], p[1] = x_ptr or None, y_ptr or None
-        for i in range(2, len(self.refs)):
-            ref = self.refs[i]
-            p[i] = ref[1].data_ptr() if ref[0] == "fixed" else ws.ptr(ref[1])
+        # fixed tensors never move, workspace slots only when the workspace's
+        # generation changed since the table was last filled
+        if self._gen != ws.gen:
+            for i in range(2, len(self.refs)):
+                ref = self.refs[i]
+                p[i] = ref[1].data_ptr() if ref[0] == "fixed" else ws.ptr(ref[1])
+            self._gen = ws.gen
+        else:
+            for i in self._moving:
+                p[i] = self.refs[i][1].data_ptr()
         check(_lib.load().ptn_exec_ops(self.ops, self.n, p, len(self.refs), _stream_ptr()), "ptn_exec_ops")
 
 
@@ -216,11 +250,14 @@ class Plan:
         self.flops = sum(s.flops for s in steps)
 
     def run(self, x_ptr: int = 0, y_ptr: int = 0):
-        for name, n in self.ws_sizes.items():
-            self.ws.get(name, n)
+        ws = self.ws
+        if getattr(self, "_sized_at", None) != ws.gen:
+            for name, n in self.ws_sizes.items():
+                ws.get(name, n)
+            self._sized_at = ws.gen     # slots only grow: still large enough until one is replaced
         if not hasattr(self, "_exec"):
             self._exec = _NativeOps([(_lib.OP_ZCONTRACT, st.desc, st.refs) for st in self.steps])
-        self._exec.run(self.ws, x_ptr, y_ptr)
+        self._exec.run(ws, x_ptr, y_ptr)
 
 
 class ChainBuilder:
@@ -433,14 +470,16 @@ class MixedPlan:
         self.byte_sizes[name] = max(self.byte_sizes.get(name, 0), int(nbytes))
 
     def _build_exec(self):
-        for name, n in self.sizes.items():
-            self.ws.get(name, n + 64, torch.bfloat16)
-        for name, nb in self.byte_sizes.items():
-            self.ws.get(name, (nb + 15) // 16, CDT)
-        status = self.ws.bufs.get("tc_status")
-        if status is None:
-            status = torch.zeros(1, dtype=torch.int32, device=self.ws.device)
-            self.ws.bufs["tc_status"] = status
+        ws = self.ws
+        if getattr(self, "_sized_at", None) != ws.gen:
+            for name, n in self.sizes.items():
+                ws.get(name, n + 64, torch.bfloat16)
+            for name, nb in self.byte_sizes.items():
+                ws.get(name, (nb + 15) // 16, CDT)
+            if ws.bufs.get("tc_status") is None:
+                ws.bufs["tc_status"] = torch.zeros(1, dtype=torch.int32, device=ws.device)
+            self._sized_at = ws.gen     # slots only grow: still large enough until one is replaced
+        status = ws.bufs["tc_status"]
         if not hasattr(self, "_exec"):
             items = []
             for kind, d, refs in self.ops:

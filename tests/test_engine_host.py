@@ -1603,3 +1603,36 @@ def test_first_order_reset_reuses_unchanged_environments(monkeypatch):
         assert np.array_equal(ta[nid], tb[nid]), nid
     for key, E in a.net.env.items():
         assert np.array_equal(E.numpy(), b.net.env[key].numpy()), key
+
+
+def test_plan_rereads_moved_workspace_slots(monkeypatch):
+    """A plan keeps its operand addresses between runs only while the
+    workspace's buffers are unchanged: after a slot it uses is replaced by a
+    larger one (another plan grew it), the next run reads the new address and
+    still gives the right result."""
+    fake_ptn.install(monkeypatch)
+    from pytreenet_gb300.engine import ChainBuilder, Operand, Workspace
+    rng = np.random.default_rng(0)
+    ws = Workspace("cpu")
+    A = torch.from_numpy(rng.normal(size=(6, 5)) + 1j * rng.normal(size=(6, 5)))
+    B = torch.from_numpy(rng.normal(size=(5, 4)) + 1j * rng.normal(size=(5, 4)))
+    D = torch.from_numpy(rng.normal(size=(4, 3)) + 1j * rng.normal(size=(4, 3)))
+    out = torch.zeros((6, 3), dtype=torch.complex128)
+    cb = ChainBuilder(ws)
+    T = cb.contract(Operand.contiguous(("fixed", A), ["i", "k"], [6, 5]),
+                    Operand.contiguous(("fixed", B), ["k", "j"], [5, 4]), ["k"])     # T lives in a ws slot
+    cb.contract(T, Operand.contiguous(("fixed", D), ["j", "l"], [4, 3]), ["j"],
+                out=Operand.contiguous(("fixed", out), ["i", "l"], [6, 3]))
+    p = cb.plan()
+    ref = (A @ B @ D).numpy()
+    p.run()
+    assert np.allclose(out.numpy(), ref)
+    gen = ws.gen
+    name = T.ref[1]
+    old = ws.bufs[name]
+    ws.get(name, old.numel() * 4)              # the slot moves
+    assert ws.gen != gen and ws.bufs[name].data_ptr() != old.data_ptr()
+    old.fill_(float("nan"))                    # the old buffer must not be read again
+    out.zero_()
+    p.run()
+    assert np.allclose(out.numpy(), ref)

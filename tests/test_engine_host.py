@@ -1491,17 +1491,18 @@ def test_ttn_parentage_and_to_complex():
         t.to_complex(32)
 
 
-def test_expect_many_one_pass(monkeypatch):
+@pytest.mark.parametrize("name", ["ttree3_heis_chi6_o1", "binary7_tfim_chi4_o2", "ternary2_xxz_chi4_o1"])
+def test_expect_many_one_pass(monkeypatch, name):
     """DeviceNetwork.expect_many: one-site operators (several on one node, on
     the root and on leaves), products on several nodes (in one subtree and
     across the root) and the norm, against the oracle's full contraction per
-    product; the plan is built once per operator layout and rebuilt when a
-    site tensor changes shape."""
+    product, on a T-tree, a binary and a ternary tree; the plan is built once
+    per operator layout and rebuilt when a site tensor changes shape."""
     import pytreenet_gb300 as P
     import oracle as O
     from pytreenet_gb300.engine import DeviceNetwork
     fake_ptn.install(monkeypatch)
-    c = load_case("ttree3_heis_chi6_o1")
+    c = load_case(name)
     st = build_ttn(P.TTNS, c["spec"], c["init"])
     ost = oracle_state(c)
     net = DeviceNetwork(st)

@@ -31,7 +31,7 @@ def _worker(rank, world, port, out):
 
 def test_two_rank_aggregation_takes_the_slowest_rank():
     port = _free_port()
-    out = mp.Manager().dict()
+    out = mp.get_context("spawn").Manager().dict()
     mp.spawn(_worker, args=(2, port, out), nprocs=2, join=True)
     for rank in (0, 1):
         value, t_max = out[rank]

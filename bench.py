@@ -181,6 +181,13 @@ def oracle_schedule_counts(arm, tol, dt, chi=8, seconds=None, seed=0):
 # classes timed in one sample: node degree 1, 2, 3, and the bond (0)
 OP_CLASSES = (1, 2, 3, 0)
 
+# The per-operation model checked against one complete oracle sweep at the
+# headline size (chi=256, arms of 20) on a Grace host with 16 Arm cores
+# (``bench.py --impl reference --full-sweep``): recorded figures.
+MODEL_CHECK = {"command": "python bench.py --impl reference --full-sweep",
+               "full_sweep_seconds": 153.80, "model_seconds": 148.39, "model_error_relative": -0.0352,
+               "cores": 16, "host": "Grace (aarch64)"}
+
 
 def oracle_op_times(chi, classes=OP_CLASSES, depth=4):
     """Seconds per oracle operation at this chi for the given classes (one
@@ -598,10 +605,13 @@ def run_reference(args, rank, world):
     counts = oracle_schedule_counts(args.arm, args.tol, args.dt)
     times = {}
     samples = []
+    timed_wall = 0.0
     for i in range(args.warmup + args.steps):
         classes = OP_CLASSES if i == 0 else (OP_CLASSES[i % len(OP_CLASSES)],)
+        t0 = time.perf_counter()
         times.update(oracle_op_times(args.chi, classes))
         if i >= args.warmup:
+            timed_wall += time.perf_counter() - t0
             samples.append(model_sweep_seconds(counts, times))
     v = 1.0 / float(np.mean(samples))
     cb = {"value": v, "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
@@ -613,7 +623,10 @@ def run_reference(args, rank, world):
             "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c128 (fp64)", "data": "synthetic",
             "config": config(args, "plain complex128 (CPU)"), "impl": "reference", "cpu_baseline": cb,
-            "e2e": {"value": v, "unit": "sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": v, "unit": "sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "timing": {"ms_per_step": "modelled time of one complete sweep (not wall time of this run)",
+                       "sampled_wall_seconds": timed_wall,
+                       "model_check": MODEL_CHECK if args.chi == 256 and args.arm == 20 else None}}
 
 
 def run_reference_full_sweep(args):

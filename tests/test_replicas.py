@@ -50,3 +50,19 @@ def test_reference_arm_only_rank0_reports():
     import bench
     args = argparse.Namespace(warmup=0, steps=1, chi=8, arm=2, dt=0.01, tol=1e-10)
     assert bench.run_reference(args, rank=1, world=2) is None
+
+
+def test_reference_arm_line_states_its_timing():
+    """Rank 0's line: value and ms_per_step describe the same modelled sweep,
+    the wall time actually sampled is reported beside it, and the recorded
+    full-sweep check is attached only at the size it was measured at."""
+    import argparse
+    import bench
+    args = argparse.Namespace(warmup=1, steps=2, chi=8, arm=2, dt=0.01, tol=1e-10, precision="mixed")
+    line = bench.run_reference(args, rank=0, world=1)
+    assert line["impl"] == "reference"
+    assert line["ms_per_step"] == pytest.approx(1000.0 / line["value"])
+    assert line["e2e"]["value"] == line["value"] and line["cpu_baseline"]["value"] == line["value"]
+    assert line["timing"]["sampled_wall_seconds"] > 0.0
+    assert line["timing"]["model_check"] is None
+    assert bench.MODEL_CHECK["full_sweep_seconds"] > 0.0

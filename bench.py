@@ -188,6 +188,14 @@ MODEL_CHECK = {"command": "python bench.py --impl reference --full-sweep",
                "full_sweep_seconds": 153.80, "model_seconds": 148.39, "model_error_relative": -0.0352,
                "cores": 16, "host": "Grace (aarch64)"}
 
+# The mixed path against the plain complex128 path over the 20 sweeps of the
+# headline workload (``bench.py --fidelity-sweeps 20``, one GB300): recorded
+# figures. The default run compares one sweep; 20 plain sweeps take ~11 min.
+FIDELITY_20_SWEEPS = {"command": "python bench.py --fidelity-sweeps 20", "sweeps_compared": 20, "t": 0.2,
+                      "fidelity_error": 2.318e-09, "fidelity_error_per_unit_time": 1.159e-08,
+                      "fidelity_error_at_sweeps_1_10_17_20": [6.99e-12, 6.15e-10, 1.69e-09, 2.318e-09],
+                      "energy_error": 5.70e-06, "energy_error_relative": 1.96e-05}
+
 
 def oracle_op_times(chi, classes=OP_CLASSES, depth=4):
     """Seconds per oracle operation at this chi for the given classes (one
@@ -488,6 +496,7 @@ def run_gb300(args, rank, world):
     if args.precision == "mixed" and not args.no_plain and rank == 0:
         plain = compare_with_plain(args, 1)
         plain["speedup_mixed_over_plain"] = value / plain["sweeps_per_s"]
+        plain["recorded_20_sweeps"] = FIDELITY_20_SWEEPS if (args.chi == 256 and args.arm == 20) else None
     line = {"metric": metric_name(args), "value": value, "unit": "sweeps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,

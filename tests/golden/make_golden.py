@@ -952,6 +952,57 @@ def time_dep_cases(ptn):
     run_case_time_dep(ptn, "binary7_tfim_driven_o2", spec, random_state_tensors(spec, rng, 3), 0.05, 5, 2, 1e-12)
 
 
+def tfim_fields(ptn, spec, J, gs):
+    """H = -J sum Z_i Z_j - sum g_i X_i with one field per site."""
+    conv = {"mJZ": -J * Z, "Z": Z, "I2": np.eye(2, dtype=complex)}
+    terms = [ptn.TensorProduct({nid: "mJZ", p: "Z"}) for nid, p in spec if p is not None]
+    for i, (nid, _) in enumerate(spec):
+        conv[f"mgX{nid}"] = -gs[i] * X
+        terms.append(ptn.TensorProduct({nid: f"mgX{nid}"}))
+    return ptn.Hamiltonian(terms, conv)
+
+
+def config_shape_cases(ptn):
+    """The reference on the exact trees and Hamiltonian families of the five
+    benchmark configurations, at bond dimensions it runs in seconds (its
+    two-site contraction order needs chi^6 w^6 d^2 entries on the ternary tree,
+    so chi_max stays at 3 there):
+
+    * c2shape_ternary3_xxz_neel_chi3: ternary depth 3 (40 sites), XXZ with
+      per-edge Jxy, Jz ~ U[0.5, 1.5], Neel, second-order two-site TDVP,
+      max_bond_dim 3, cutoff 1e-10, dt 0.02, 4 steps;
+    * c3shape_ttree20_heis_chi8_o1: T-tree root + 3 x 20 (61 sites),
+      Heisenberg + fields h ~ U[-1, 1], capped random state (chi 8),
+      canonicalised, first-order one-site TDVP, dt 0.01, 2 sweeps;
+    * c4shape_binary31_heis_h2_neel_chi8: 31-site binary tree, Heisenberg +
+      fields h ~ U[-2, 2], Neel, second-order two-site TDVP, max_bond_dim 8,
+      cutoff 1e-9, dt 0.05, 2 steps;
+    * c5shape_binary31_tfim_gi_chi8_o1: 31-site binary TFIM, J = 1,
+      g_i ~ U[0.3, 0.7], capped random state (chi 8), canonicalised,
+      first-order one-site TDVP, dt 0.02, 5 steps.
+    """
+    rng = np.random.default_rng(2718)
+    spec = ternary_tree(3)
+    ne = len(spec) - 1
+    jxy = rng.uniform(0.5, 1.5, size=ne)
+    jz = rng.uniform(0.5, 1.5, size=ne)
+    run_case_two_site(ptn, "c2shape_ternary3_xxz_neel_chi3", spec, neel_state_tensors(spec),
+                      lambda psi: heisenberg_fields(ptn, spec, np.zeros(len(spec)), jxy, jz),
+                      0.02, 4, 1e-12, (3, 1e-10, 1e-10, False))
+    spec = t_tree(20)
+    h = rng.uniform(-1, 1, size=len(spec))
+    run_case(ptn, "c3shape_ttree20_heis_chi8_o1", spec, capped_state_tensors(spec, rng, 8),
+             lambda psi: heisenberg_fields(ptn, spec, h), 0.01, 2, 1, 1e-12, canonical_random=True)
+    spec = binary_tree(31)
+    h = rng.uniform(-2, 2, size=len(spec))
+    run_case_two_site(ptn, "c4shape_binary31_heis_h2_neel_chi8", spec, neel_state_tensors(spec),
+                      lambda psi: heisenberg_fields(ptn, spec, h), 0.05, 2, 1e-12, (8, 1e-9, 1e-9, False))
+    spec = binary_tree(31)
+    gs = rng.uniform(0.3, 0.7, size=len(spec))
+    run_case(ptn, "c5shape_binary31_tfim_gi_chi8_o1", spec, capped_state_tensors(spec, rng, 8),
+             lambda psi: tfim_fields(ptn, spec, 1.0, gs), 0.02, 5, 1, 1e-12, canonical_random=True)
+
+
 def main(ref_root):
     ptn = _import_reference(ref_root)
     rng = np.random.default_rng(1234)
@@ -1017,4 +1068,12 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    # python make_golden.py REF_ROOT [group ...]: all fixtures, or only the
+    # named generator groups (e.g. config_shape_cases)
+    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) > 2:
+        mod = _import_reference(ref)
+        for group in sys.argv[2:]:
+            globals()[group](mod)
+    else:
+        main(ref)

@@ -46,6 +46,10 @@ CASES = ["c1_binary15_tfim_chi8", "binary7_tfim_chi4_o2", "ttree3_heis_chi6_o1",
 TWO_SITE_CASES = ["ternary2_xxz_neel_2tdvp", "binary7_heis_2tdvp_trunc", "binary7_heis_2tdvp_l2l",
                   "binary7_heis_2tdvp_rk45", "binary7_heis_2tdvp_fastest"]
 ODE_MODES = ("RK45", "RK23", "DOP853")
+# the reference on the trees and Hamiltonian families of the five benchmark
+# configurations, at small bond dimensions (make_golden.py config_shape_cases)
+CONFIG_SHAPE_CASES = ["c3shape_ttree20_heis_chi8_o1", "c5shape_binary31_tfim_gi_chi8_o1"]
+CONFIG_SHAPE_TWO_SITE_CASES = ["c2shape_ternary3_xxz_neel_chi3", "c4shape_binary31_heis_h2_neel_chi8"]
 
 
 def case_solver(c, P):

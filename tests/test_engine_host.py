@@ -142,6 +142,38 @@ def test_engine_host_two_site_matches_reference(monkeypatch, name):
         assert algo.state.nodes[nid].children == algo.net.state.nodes[nid].children
 
 
+from golden_util import CONFIG_SHAPE_CASES, CONFIG_SHAPE_TWO_SITE_CASES  # noqa: E402
+
+
+@pytest.mark.parametrize("name", CONFIG_SHAPE_CASES)
+def test_engine_host_config_shape_one_site(monkeypatch, name):
+    """The engine's planning and Krylov control on the 61-site T-tree and the
+    31-site binary TFIM with per-site fields, against the reference's runs."""
+    fake_ptn.install(monkeypatch)
+    import oracle as O
+    c, out, zerr = _run_case(name)
+    got = O.OState(oracle_state(c).tree, out)
+    one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), got)
+    assert zerr < 1e-10
+    assert one_minus_f < 1e-12
+
+
+@pytest.mark.parametrize("name", CONFIG_SHAPE_TWO_SITE_CASES)
+def test_engine_host_config_shape_two_site(monkeypatch, name):
+    """Two-site TDVP with bond growth on the 40-site ternary tree and the
+    31-site binary tree with random fields, against the reference's runs:
+    same final bond dimensions, <Z_i> to 1e-10, 1-F < 1e-12."""
+    fake_ptn.install(monkeypatch)
+    import oracle as O
+    c, algo, out, zs = _run_two_site(name)
+    fin = oracle_state(c, "final")
+    for nid in fin.tensors:
+        assert fin.tensors[nid].shape == out[nid].shape, nid
+    one_minus_f, _ = fidelity_and_dist(fin, O.OState(oracle_state(c).tree, out))
+    assert np.max(np.abs(zs - c["z"])) < 1e-10
+    assert one_minus_f < 1e-12
+
+
 def test_engine_host_first_order_two_site_matches_oracle(monkeypatch):
     fake_ptn.install(monkeypatch)
     import oracle as O

@@ -277,3 +277,43 @@ def test_oracle_zipup_matches_reference(tag):
         assert out.tensors[i].shape == ref.tensors[i].shape, i
     a, b = O.state_vector(out, ids), O.state_vector(ref, ids)
     assert np.max(np.abs(a - b)) < 1e-12 * np.max(np.abs(b))
+
+
+from golden_util import CONFIG_SHAPE_CASES, CONFIG_SHAPE_TWO_SITE_CASES  # noqa: E402
+
+
+@pytest.mark.parametrize("name", CONFIG_SHAPE_CASES)
+def test_oracle_config_shape_one_site(name):
+    """The reference's one-site runs on the 61-site T-tree (Heisenberg +
+    fields) and the 31-site binary TFIM with one field per site: same update
+    path, <Z_i> after every step to 1e-10, final state 1-F < 1e-12, energy."""
+    c = load_case(name)
+    algo, zerr = _run(c)
+    one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), algo.state)
+    assert zerr < 1e-10
+    assert one_minus_f < 1e-12
+    e = O.ttno_expectation(algo.state, c["ttno"])
+    assert abs(e - c["energy_final"]) < 1e-10 * max(1.0, abs(c["energy_final"]))
+
+
+@pytest.mark.parametrize("name", CONFIG_SHAPE_TWO_SITE_CASES)
+def test_oracle_config_shape_two_site(name):
+    """The reference's second-order two-site runs on the 40-site ternary tree
+    (XXZ, Neel, bonds growing to 3) and the 31-site binary tree (random fields
+    up to 2, Neel, bonds growing to 8 at cutoff 1e-9): same final bond
+    dimensions, <Z_i> after every step to 1e-10, 1-F < 1e-12."""
+    c = load_case(name)
+    algo = O.SecondOrderTwoSiteTDVPOracle(oracle_state(c), c["ttno"], c["dt"], O.SVDParams(**c["svd"]),
+                                          krylov_tol=c["krylov_tol"])
+    assert algo.update_path == c["update_path"]
+    zerr = 0.0
+    for k in range(c["steps"]):
+        algo.run_one_time_step()
+        z = np.array([O.expect_product(algo.state, {nid: Zm}) for nid, _ in c["spec"]])
+        zerr = max(zerr, float(np.max(np.abs(z - c["z"][k]))))
+    fin = oracle_state(c, "final")
+    for nid in fin.tensors:
+        assert fin.tensors[nid].shape == algo.state.tensors[nid].shape, nid
+    one_minus_f, _ = fidelity_and_dist(fin, algo.state)
+    assert zerr < 1e-10
+    assert one_minus_f < 1e-12

@@ -56,7 +56,8 @@ def test_engine_host_c1_padded(monkeypatch):
 
 
 @pytest.mark.parametrize("name,precision", [("ttree3_heis_chi6_o1", "bf16x6"), ("ternary2_xxz_chi4_o1", "bf16x3"),
-                                            ("binary7_tfim_chi4_o2", "bf16x6")])
+                                            ("binary7_tfim_chi4_o2", "bf16x6"),
+                                            ("c3shape_ttree20_heis_chi8_o1", "bf16x6")])
 def test_engine_host_mixed_layouts(monkeypatch, name, precision):
     """The tensor-core plans (operand layouts chosen per step, epilogue strides)
     give the reference's result up to BF16x3 rounding."""
@@ -172,6 +173,22 @@ def test_engine_host_config_shape_two_site(monkeypatch, name):
     one_minus_f, _ = fidelity_and_dist(fin, O.OState(oracle_state(c).tree, out))
     assert np.max(np.abs(zs - c["z"])) < 1e-10
     assert one_minus_f < 1e-12
+
+
+@pytest.mark.parametrize("name", CONFIG_SHAPE_TWO_SITE_CASES)
+def test_engine_host_config_shape_two_site_mixed(monkeypatch, name):
+    """The BF16x6 plans of the two-site path (emulated by the stand-in
+    library) on the same trees: measured |dZ| 2e-7 to 4e-7 and 1-F below
+    3e-13 against the reference, with the same final bond dimensions."""
+    fake_ptn.install(monkeypatch)
+    import oracle as O
+    c, algo, out, zs = _run_two_site(name, precision="mixed")
+    fin = oracle_state(c, "final")
+    for nid in fin.tensors:
+        assert fin.tensors[nid].shape == out[nid].shape, nid
+    one_minus_f, _ = fidelity_and_dist(fin, O.OState(oracle_state(c).tree, out))
+    assert np.max(np.abs(zs - c["z"])) < 2e-6
+    assert one_minus_f < 1e-10
 
 
 def test_engine_host_first_order_two_site_matches_oracle(monkeypatch):

@@ -29,5 +29,7 @@ def test_gpu_config_shape_one_site(name):
         zerr = max(zerr, float(np.max(np.abs(np.array(z) - c["z"][k]))))
     got = O.OState(oracle_state(c).tree, {nid: algo.state.get_phys_numpy(nid) for nid, _ in c["spec"]})
     one_minus_f, _ = fidelity_and_dist(oracle_state(c, "final"), got)
-    assert zerr < 1e-10
+    # ~120 Krylov solves per run: a stop test that falls within rounding of
+    # its threshold may add or drop one basis vector (<= krylov_tol each)
+    assert zerr < 1e-9
     assert one_minus_f < 1e-12
